@@ -1,0 +1,70 @@
+"""In-tree build of libcorrfunc_gb300.so (C host layer + sm_103a CUDA engine).
+
+    python -m corrfunc_gb300.build          # or corrfunc_gb300.build.build()
+
+The host C files are compiled with gcc (-ffp-contract=off keeps the double-precision
+finalisation free of contractions), the CUDA engine with nvcc for sm_103a only, and both are
+linked into corrfunc_gb300/libcorrfunc_gb300.so.  Translation units compile in parallel.
+"""
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+INCLUDE = os.path.join(ROOT, "include")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libcorrfunc_gb300.so")
+
+NVCC_ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _nvcc():
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(cand):
+        raise RuntimeError("nvcc not found; the CUDA toolkit is required to build corrfunc_gb300")
+    return cand
+
+
+def _cuda_root(nvcc):
+    return os.path.dirname(os.path.dirname(os.path.realpath(nvcc)))
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build step failed:\n%s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    return r
+
+
+def build(verbose=False, extra_nvcc=()):
+    os.makedirs(BUILD, exist_ok=True)
+    nvcc = _nvcc()
+    cuda = _cuda_root(nvcc)
+    inc = ["-I" + INCLUDE, "-I" + CSRC, "-I" + os.path.join(cuda, "include")]
+    jobs = []
+    for c in ("cf_api.c", "cf_common.c"):
+        obj = os.path.join(BUILD, c[:-2] + ".o")
+        jobs.append(["gcc", "-std=gnu11", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
+                    + inc + ["-c", os.path.join(CSRC, c), "-o", obj])
+    cu_obj = os.path.join(BUILD, "cf_engine.o")
+    jobs.append([nvcc] + NVCC_ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
+                                      "-Xcompiler", "-ffp-contract=off"] + list(extra_nvcc) + inc
+                + ["-c", os.path.join(CSRC, "cf_engine.cu"), "-o", cu_obj])
+    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        for r in ex.map(_run, jobs):
+            if verbose and (r.stdout or r.stderr):
+                print(r.stdout, r.stderr)
+    objs = [os.path.join(BUILD, "cf_api.o"), os.path.join(BUILD, "cf_common.o"), cu_obj]
+    tmp = LIB + ".tmp"
+    _run([nvcc] + NVCC_ARCH + ["-shared", "-o", tmp] + objs
+         + ["-L" + os.path.join(cuda, "lib64"), "-lcudart_static", "-lpthread", "-ldl", "-lrt", "-lm"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

@@ -1,0 +1,963 @@
+/*
+ * cf_api.c -- the six public pair-counting entry points (C ABI of libcorrfunc_gb300.so).
+ *
+ * Each function keeps the reference's prototype, validation, side effects on the options
+ * struct and result packing; the pair counting itself is handed to the CUDA engine
+ * (cf_engine_run).  Finalisation (auto-correlation doubling, self pairs, averages, xi / wp
+ * from the analytic random counts) follows the reference drivers cited per function.
+ * All arithmetic after counting is double precision, also for float inputs.
+ */
+#define _GNU_SOURCE
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <sys/time.h>
+#include <time.h>
+
+#include "corrfunc_gb300.h"
+#include "cf_internal.h"
+#include "cf_host.h"
+
+static double wall_now(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_REALTIME, &ts);
+    return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+#define CF_ERR(...)                         \
+    do {                                    \
+        fprintf(stderr, "Error: " __VA_ARGS__); \
+        fprintf(stderr, "\n");              \
+    } while (0)
+
+/* float_type and API version checks (theory/DD/countpairs.c:46-55) */
+static int check_options(const struct config_options *options, const char *fn)
+{
+    if (options == NULL) {
+        CF_ERR("In %s> options can not be NULL", fn);
+        return EXIT_FAILURE;
+    }
+    if (!(options->float_type == sizeof(float) || options->float_type == sizeof(double))) {
+        CF_ERR("In %s> Can only handle doubles or floats. Got an array of size = %zu", fn, options->float_type);
+        return EXIT_FAILURE;
+    }
+    if (strncmp(options->version, CF_API_VERSION, sizeof(options->version) - 1) != 0) {
+        CF_ERR("Do not know this API version = `%s'. Expected version = `%s'", options->version, CF_API_VERSION);
+        return EXIT_FAILURE;
+    }
+    return EXIT_SUCCESS;
+}
+
+/* max_cells / refine-factor sanitation done at the top of every theory driver
+ * (theory/DD/countpairs_impl.c.src:175-189) */
+static void sanitize_lattice_options(struct config_options *options)
+{
+    if (options->max_cells_per_dim == 0) {
+        fprintf(stderr, "Warning: Max. cells per dimension is set to 0 - resetting to `NLATMAX' = %d\n", NLATMAX);
+        options->max_cells_per_dim = NLATMAX;
+    }
+    for (int i = 0; i < 3; i++) {
+        if (options->bin_refine_factors[i] < 1) {
+            fprintf(stderr, "Warning: bin refine factor along axis = %d *must* be >=1. Instead found bin refine factor =%d\n",
+                    i, options->bin_refine_factors[i]);
+            reset_bin_refine_factors(options);
+            break;
+        }
+    }
+}
+
+static double wval(const void *w, int64_t j, size_t es)
+{
+    return es == sizeof(float) ? (double)((const float *)w)[j] : ((const double *)w)[j];
+}
+
+static double self_weight_sum(const void *w, int64_t n, size_t es)
+{
+    double s = 0.0;
+    for (int64_t j = 0; j < n; j++) {
+        const double v = wval(w, j, es);
+        s += v * v;
+    }
+    return s;
+}
+
+static void fill_rule_extent(cf_refrule *R, const struct config_options *options, double sx, double sy, double sz,
+                             int dfl_kind, int boost_kind, int64_t np1)
+{
+    memset(R, 0, sizeof(*R));
+    R->kind = CF_REF_EXTENT;
+    R->periodic = options->periodic;
+    R->boxsize[0] = options->boxsize_x;
+    R->boxsize[1] = options->boxsize_y == BOXSIZE_NOTGIVEN ? options->boxsize_x : options->boxsize_y;
+    R->boxsize[2] = options->boxsize_z == BOXSIZE_NOTGIVEN ? options->boxsize_x : options->boxsize_z;
+    R->max_size[0] = sx;
+    R->max_size[1] = sy;
+    R->max_size[2] = sz;
+    for (int a = 0; a < 3; a++) R->refine[a] = options->bin_refine_factors[a];
+    R->custom_refine = (options->binning_flags & BINNING_REF_MASK) == BINNING_CUST;
+    R->max_cells = options->max_cells_per_dim;
+    R->dfl_kind = dfl_kind;
+    R->boost_kind = boost_kind;
+    R->np1 = np1;
+}
+
+static void fill_rule_box(cf_refrule *R, const struct config_options *options, double boxsize, double sx, double sz,
+                          int dfl_kind, int64_t np1)
+{
+    memset(R, 0, sizeof(*R));
+    R->kind = CF_REF_BOX;
+    R->periodic = 1;
+    R->boxsize[0] = R->boxsize[1] = R->boxsize[2] = boxsize;
+    R->max_size[0] = sx;
+    R->max_size[1] = sx;
+    R->max_size[2] = sz;
+    for (int a = 0; a < 3; a++) R->refine[a] = options->bin_refine_factors[a];
+    R->custom_refine = (options->binning_flags & BINNING_REF_MASK) == BINNING_CUST;
+    R->max_cells = options->max_cells_per_dim;
+    R->dfl_kind = dfl_kind;
+    R->boost_kind = CF_BOOST_XY;
+    R->np1 = np1;
+}
+
+static int alloc_hist(cf_hist *H, int nbins)
+{
+    H->nbins = nbins;
+    H->npairs = calloc((size_t)nbins, sizeof(uint64_t));
+    H->avg = calloc((size_t)nbins, sizeof(double));
+    H->wsum = calloc((size_t)nbins, sizeof(double));
+    if (!H->npairs || !H->avg || !H->wsum) {
+        free(H->npairs);
+        free(H->avg);
+        free(H->wsum);
+        CF_ERR("could not allocate %d histogram bins", nbins);
+        return EXIT_FAILURE;
+    }
+    return EXIT_SUCCESS;
+}
+
+static void free_hist(cf_hist *H)
+{
+    free(H->npairs);
+    free(H->avg);
+    free(H->wsum);
+    H->npairs = NULL;
+    H->avg = NULL;
+    H->wsum = NULL;
+}
+
+/* Finalisation common to all drivers: x2 for auto-correlations, self pairs when the first
+ * bin starts at zero (count into self_idx, weights into flat bin 1 exactly as the reference
+ * does, e.g. theory/DDrppi/countpairs_rp_pi_impl.c.src:603-642), then averages. */
+static void finalize_hist(cf_hist *H, int autocorr, int first_edge_is_zero, int self_idx, int64_t n1, double self_w,
+                          int need_avg, int need_w, int div_start)
+{
+    if (autocorr) {
+        for (int i = 0; i < H->nbins; i++) {
+            H->npairs[i] *= 2;
+            H->avg[i] *= 2.0;
+            H->wsum[i] *= 2.0;
+        }
+        if (first_edge_is_zero) {
+            H->npairs[self_idx] += (uint64_t)n1;
+            if (need_w) H->wsum[1] += self_w;
+        }
+    }
+    for (int i = div_start; i < H->nbins; i++) {
+        if (H->npairs[i] > 0) {
+            if (need_avg) H->avg[i] /= (double)H->npairs[i];
+            if (need_w) H->wsum[i] /= (double)H->npairs[i];
+        }
+    }
+}
+
+static void init_job(cf_job *J, const struct config_options *options, int mode, int autocorr)
+{
+    memset(J, 0, sizeof(*J));
+    J->mode = mode;
+    J->autocorr = autocorr;
+    J->precision = cf_engine_get_precision();
+    cf_formula_for_isa(options->instruction_set, &J->fma_formula, &J->chord_formula);
+    J->elem_size = (int)options->float_type;
+    J->need_avg = options->need_avg_sep ? 1 : 0;
+}
+
+static int read_bins(const char *binfile, double **rupp, int *nbin, double *rmin, double *rmax)
+{
+    if (cf_setup_bins(binfile, rmin, rmax, nbin, rupp) != EXIT_SUCCESS) return EXIT_FAILURE;
+    if (!(*rmin >= 0.0 && *rmax > 0.0 && *rmin < *rmax && *nbin > 0)) {
+        CF_ERR("Could not setup with R bins correctly. (rmin = %lf, rmax = %lf, with nbins = %d). "
+               "Expected non-zero rmin/rmax with rmax > rmin and nbins >=1 ",
+               *rmin, *rmax, *nbin);
+        free(*rupp);
+        *rupp = NULL;
+        return EXIT_FAILURE;
+    }
+    if (*nbin > CF_MAX_EDGES) {
+        CF_ERR("at most %d bins are supported (got %d)", CF_MAX_EDGES - 1, *nbin - 1);
+        free(*rupp);
+        *rupp = NULL;
+        return EXIT_FAILURE;
+    }
+    return EXIT_SUCCESS;
+}
+
+static int check_weights(const struct extra_options *extra, int autocorr)
+{
+    if (extra->weight_method == NONE) return EXIT_SUCCESS;
+    if (extra->weight_method != PAIR_PRODUCT) {
+        CF_ERR("unknown weight method %d", (int)extra->weight_method);
+        return EXIT_FAILURE;
+    }
+    if (extra->weights0.weights[0] == NULL || (!autocorr && extra->weights1.weights[0] == NULL)) {
+        CF_ERR("pair_product weighting needs one weight array per particle set");
+        return EXIT_FAILURE;
+    }
+    return EXIT_SUCCESS;
+}
+
+/* ========================= countpairs (DD) ========================= */
+/* theory/DD/countpairs.c:34-77 + theory/DD/countpairs_impl.c.src:136-707 */
+int countpairs(const int64_t ND1, void *X1, void *Y1, void *Z1, const int64_t ND2, void *X2, void *Y2, void *Z2,
+               const int numthreads, const int autocorr, const char *binfile, results_countpairs *results,
+               struct config_options *options, struct extra_options *extra)
+{
+    (void)numthreads;
+    const double t0 = wall_now();
+    if (check_options(options, __func__) != EXIT_SUCCESS || results == NULL) return EXIT_FAILURE;
+    struct extra_options dummy;
+    if (extra == NULL) {
+        dummy = get_extra_options(NONE);
+        extra = &dummy;
+    }
+    if (autocorr != 0 && autocorr != 1) {
+        CF_ERR("Strange value of autocorr = %d. Expected to receive either 1 (auto-correlations) or 0 (cross-correlations)", autocorr);
+        return EXIT_FAILURE;
+    }
+    if (check_weights(extra, autocorr) != EXIT_SUCCESS) return EXIT_FAILURE;
+    const int need_w = extra->weight_method != NONE;
+    sanitize_lattice_options(options);
+    options->sort_on_z = 1;
+    double *rupp = NULL, rmin, rmax;
+    int nbin;
+    if (read_bins(binfile, &rupp, &nbin, &rmin, &rmax) != EXIT_SUCCESS) return EXIT_FAILURE;
+    if (options->periodic && options->boxsize == BOXSIZE_NOTGIVEN) {
+        fprintf(stderr, "boxsize = %g must be specified with periodic wrap. Please specify a non-zero boxsize, or zero to "
+                        "detect the particle extent, or -1 to make a dimension non-periodic.\n", options->boxsize);
+        free(rupp);
+        return EXIT_FAILURE;
+    }
+    cf_job J;
+    init_job(&J, options, CF_MODE_R3, autocorr);
+    J.n1 = ND1;
+    J.n2 = autocorr ? ND1 : ND2;
+    J.x1 = X1; J.y1 = Y1; J.z1 = Z1;
+    J.x2 = autocorr ? X1 : X2; J.y2 = autocorr ? Y1 : Y2; J.z2 = autocorr ? Z1 : Z2;
+    J.need_weight = need_w;
+    J.w1 = need_w ? extra->weights0.weights[0] : NULL;
+    J.w2 = need_w ? (autocorr ? extra->weights0.weights[0] : extra->weights1.weights[0]) : NULL;
+    fill_rule_extent(&J.rule, options, rmax, rmax, rmax, CF_DFL_PER_AXIS, CF_BOOST_XY, ND1);
+    J.rmax_xy = J.rmax_z = J.rmax_3d = rmax;
+    J.nedges = nbin;
+    for (int i = 0; i < nbin; i++) J.edges[i] = rupp[i] * rupp[i];
+    cf_hist H;
+    if (alloc_hist(&H, nbin) != EXIT_SUCCESS) {
+        free(rupp);
+        return EXIT_FAILURE;
+    }
+    if (cf_engine_run(&J, &H) != EXIT_SUCCESS) {
+        free_hist(&H);
+        free(rupp);
+        return EXIT_FAILURE;
+    }
+    const double self_w = (autocorr && need_w && rupp[0] <= 0.0) ? self_weight_sum(J.w1, ND1, options->float_type) : 0.0;
+    finalize_hist(&H, autocorr, rupp[0] <= 0.0, 1, ND1, self_w, options->need_avg_sep, need_w, 0);
+    results->nbin = nbin;
+    results->npairs = malloc(sizeof(uint64_t) * nbin);
+    results->rupp = malloc(sizeof(double) * nbin);
+    results->rpavg = calloc(nbin, sizeof(double));
+    results->weightavg = calloc(nbin, sizeof(double));
+    if (!results->npairs || !results->rupp || !results->rpavg || !results->weightavg) {
+        free_results(results);
+        free_hist(&H);
+        free(rupp);
+        return EXIT_FAILURE;
+    }
+    for (int i = 0; i < nbin; i++) {
+        results->npairs[i] = H.npairs[i];
+        results->rupp[i] = rupp[i];
+        results->rpavg[i] = options->need_avg_sep ? H.avg[i] : 0.0;
+        results->weightavg[i] = need_w ? H.wsum[i] : 0.0;
+    }
+    free_hist(&H);
+    free(rupp);
+    reset_bin_refine_factors(options);
+    if (options->c_api_timer) options->c_api_time = wall_now() - t0;
+    return EXIT_SUCCESS;
+}
+
+void free_results(results_countpairs *results)
+{
+    if (results == NULL) return;
+    free(results->npairs);
+    free(results->rupp);
+    free(results->rpavg);
+    free(results->weightavg);
+    results->npairs = NULL;
+    results->rupp = NULL;
+    results->rpavg = NULL;
+    results->weightavg = NULL;
+}
+
+/* ========================= countpairs_rp_pi (DDrppi) ========================= */
+/* theory/DDrppi/countpairs_rp_pi_impl.c.src:135-709 */
+int countpairs_rp_pi(const int64_t ND1, void *X1, void *Y1, void *Z1, const int64_t ND2, void *X2, void *Y2, void *Z2,
+                     const int numthreads, const int autocorr, const char *binfile, const double pimax,
+                     results_countpairs_rp_pi *results, struct config_options *options, struct extra_options *extra)
+{
+    (void)numthreads;
+    const double t0 = wall_now();
+    if (check_options(options, __func__) != EXIT_SUCCESS || results == NULL) return EXIT_FAILURE;
+    struct extra_options dummy;
+    if (extra == NULL) {
+        dummy = get_extra_options(NONE);
+        extra = &dummy;
+    }
+    if (autocorr != 0 && autocorr != 1) {
+        CF_ERR("Strange value of autocorr = %d", autocorr);
+        return EXIT_FAILURE;
+    }
+    if (check_weights(extra, autocorr) != EXIT_SUCCESS) return EXIT_FAILURE;
+    const int need_w = extra->weight_method != NONE;
+    sanitize_lattice_options(options);
+    options->sort_on_z = 1;
+    const int npibin = (int)pimax;
+    if (npibin < 1) {
+        CF_ERR("pimax = %g gives %d pi bins; pimax must be at least 1", pimax, npibin);
+        return EXIT_FAILURE;
+    }
+    double *rupp = NULL, rpmin, rpmax;
+    int nrpbin;
+    if (read_bins(binfile, &rupp, &nrpbin, &rpmin, &rpmax) != EXIT_SUCCESS) return EXIT_FAILURE;
+    if (options->periodic && options->boxsize == BOXSIZE_NOTGIVEN) {
+        fprintf(stderr, "boxsize = %g must be specified with periodic wrap.\n", options->boxsize);
+        free(rupp);
+        return EXIT_FAILURE;
+    }
+    const int64_t totnbins = (int64_t)(npibin + 1) * (nrpbin + 1);
+    cf_job J;
+    init_job(&J, options, CF_MODE_RPPI, autocorr);
+    J.n1 = ND1;
+    J.n2 = autocorr ? ND1 : ND2;
+    J.x1 = X1; J.y1 = Y1; J.z1 = Z1;
+    J.x2 = autocorr ? X1 : X2; J.y2 = autocorr ? Y1 : Y2; J.z2 = autocorr ? Z1 : Z2;
+    J.need_weight = need_w;
+    J.w1 = need_w ? extra->weights0.weights[0] : NULL;
+    J.w2 = need_w ? (autocorr ? extra->weights0.weights[0] : extra->weights1.weights[0]) : NULL;
+    fill_rule_extent(&J.rule, options, rpmax, rpmax, pimax, CF_DFL_PER_AXIS, CF_BOOST_XY, ND1);
+    J.rmax_xy = rpmax;
+    J.rmax_z = pimax;
+    J.rmax_3d = 0.0;
+    J.pimax = pimax;
+    J.npibin = npibin;
+    J.nedges = nrpbin;
+    for (int i = 0; i < nrpbin; i++) J.edges[i] = rupp[i] * rupp[i];
+    cf_hist H;
+    if (alloc_hist(&H, nrpbin * (npibin + 1)) != EXIT_SUCCESS) {
+        free(rupp);
+        return EXIT_FAILURE;
+    }
+    if (cf_engine_run(&J, &H) != EXIT_SUCCESS) {
+        free_hist(&H);
+        free(rupp);
+        return EXIT_FAILURE;
+    }
+    const double self_w = (autocorr && need_w && rupp[0] <= 0.0) ? self_weight_sum(J.w1, ND1, options->float_type) : 0.0;
+    finalize_hist(&H, autocorr, rupp[0] <= 0.0, npibin + 1, ND1, self_w, options->need_avg_sep, need_w, 0);
+    results->nbin = nrpbin;
+    results->npibin = npibin;
+    results->pimax = pimax;
+    results->npairs = calloc((size_t)totnbins, sizeof(uint64_t));
+    results->rupp = malloc(sizeof(double) * nrpbin);
+    results->rpavg = calloc((size_t)totnbins, sizeof(double));
+    results->weightavg = calloc((size_t)totnbins, sizeof(double));
+    if (!results->npairs || !results->rupp || !results->rpavg || !results->weightavg) {
+        free_results_rp_pi(results);
+        free_hist(&H);
+        free(rupp);
+        return EXIT_FAILURE;
+    }
+    for (int i = 0; i < nrpbin; i++) {
+        results->rupp[i] = rupp[i];
+        for (int j = 0; j < npibin; j++) {
+            const int64_t idx = (int64_t)i * (npibin + 1) + j;
+            results->npairs[idx] = H.npairs[idx];
+            results->rpavg[idx] = options->need_avg_sep ? H.avg[idx] : 0.0;
+            results->weightavg[idx] = need_w ? H.wsum[idx] : 0.0;
+        }
+    }
+    free_hist(&H);
+    free(rupp);
+    reset_bin_refine_factors(options);
+    if (options->c_api_timer) options->c_api_time = wall_now() - t0;
+    return EXIT_SUCCESS;
+}
+
+void free_results_rp_pi(results_countpairs_rp_pi *results)
+{
+    if (results == NULL) return;
+    free(results->npairs);
+    free(results->rupp);
+    free(results->rpavg);
+    free(results->weightavg);
+    results->npairs = NULL;
+    results->rupp = NULL;
+    results->rpavg = NULL;
+    results->weightavg = NULL;
+}
+
+/* ========================= countpairs_s_mu (DDsmu) ========================= */
+/* theory/DDsmu/countpairs_s_mu_impl.c.src:136-717 */
+int countpairs_s_mu(const int64_t ND1, void *X1, void *Y1, void *Z1, const int64_t ND2, void *X2, void *Y2, void *Z2,
+                    const int numthreads, const int autocorr, const char *sbinfile, const double mu_max,
+                    const int nmu_bins, results_countpairs_s_mu *results, struct config_options *options,
+                    struct extra_options *extra)
+{
+    (void)numthreads;
+    const double t0 = wall_now();
+    if (check_options(options, __func__) != EXIT_SUCCESS || results == NULL) return EXIT_FAILURE;
+    struct extra_options dummy;
+    if (extra == NULL) {
+        dummy = get_extra_options(NONE);
+        extra = &dummy;
+    }
+    if (autocorr != 0 && autocorr != 1) {
+        CF_ERR("Strange value of autocorr = %d", autocorr);
+        return EXIT_FAILURE;
+    }
+    if (check_weights(extra, autocorr) != EXIT_SUCCESS) return EXIT_FAILURE;
+    const int need_w = extra->weight_method != NONE;
+    sanitize_lattice_options(options);
+    options->sort_on_z = 1;
+    double *supp = NULL, smin, smax;
+    int nsbin;
+    if (read_bins(sbinfile, &supp, &nsbin, &smin, &smax) != EXIT_SUCCESS) return EXIT_FAILURE;
+    if (mu_max <= 0.0 || mu_max > 1.0) {
+        CF_ERR("max_mu (max. value for the cosine of the angle with line of sight) must be greater than 0 and at most 1). "
+               "The passed value is max_mu = %lf. Please change it to be > 0 and <= 1.0", mu_max);
+        free(supp);
+        return EXIT_FAILURE;
+    }
+    if (nmu_bins < 1) {
+        CF_ERR("Number of mu bins = %d must be at least 1", nmu_bins);
+        free(supp);
+        return EXIT_FAILURE;
+    }
+    if (options->periodic && options->boxsize == BOXSIZE_NOTGIVEN) {
+        fprintf(stderr, "boxsize = %g must be specified with periodic wrap.\n", options->boxsize);
+        free(supp);
+        return EXIT_FAILURE;
+    }
+    const double pimax = smax * mu_max;
+    const int64_t totnbins = (int64_t)(nmu_bins + 1) * (nsbin + 1);
+    cf_job J;
+    init_job(&J, options, CF_MODE_SMU, autocorr);
+    J.n1 = ND1;
+    J.n2 = autocorr ? ND1 : ND2;
+    J.x1 = X1; J.y1 = Y1; J.z1 = Z1;
+    J.x2 = autocorr ? X1 : X2; J.y2 = autocorr ? Y1 : Y2; J.z2 = autocorr ? Z1 : Z2;
+    J.need_weight = need_w;
+    J.w1 = need_w ? extra->weights0.weights[0] : NULL;
+    J.w2 = need_w ? (autocorr ? extra->weights0.weights[0] : extra->weights1.weights[0]) : NULL;
+    fill_rule_extent(&J.rule, options, smax, smax, pimax, CF_DFL_NONE, CF_BOOST_NONE, ND1);
+    J.rmax_xy = smax;
+    J.rmax_z = pimax;
+    J.rmax_3d = smax;
+    J.mu_max = mu_max;
+    J.npibin = nmu_bins;
+    J.nedges = nsbin;
+    for (int i = 0; i < nsbin; i++) J.edges[i] = supp[i] * supp[i];
+    cf_hist H;
+    if (alloc_hist(&H, nsbin * (nmu_bins + 1)) != EXIT_SUCCESS) {
+        free(supp);
+        return EXIT_FAILURE;
+    }
+    if (cf_engine_run(&J, &H) != EXIT_SUCCESS) {
+        free_hist(&H);
+        free(supp);
+        return EXIT_FAILURE;
+    }
+    const double self_w = (autocorr && need_w && supp[0] <= 0.0) ? self_weight_sum(J.w1, ND1, options->float_type) : 0.0;
+    finalize_hist(&H, autocorr, supp[0] <= 0.0, nmu_bins + 1, ND1, self_w, options->need_avg_sep, need_w, 0);
+    results->nsbin = nsbin;
+    results->nmu_bins = nmu_bins;
+    results->mu_max = mu_max;
+    results->mu_min = 0.0;
+    results->npairs = calloc((size_t)totnbins, sizeof(uint64_t));
+    results->supp = malloc(sizeof(double) * nsbin);
+    results->savg = calloc((size_t)totnbins, sizeof(double));
+    results->weightavg = calloc((size_t)totnbins, sizeof(double));
+    if (!results->npairs || !results->supp || !results->savg || !results->weightavg) {
+        free_results_s_mu(results);
+        free_hist(&H);
+        free(supp);
+        return EXIT_FAILURE;
+    }
+    for (int i = 0; i < nsbin; i++) {
+        results->supp[i] = supp[i];
+        for (int j = 0; j < nmu_bins; j++) {
+            const int64_t idx = (int64_t)i * (nmu_bins + 1) + j;
+            results->npairs[idx] = H.npairs[idx];
+            results->savg[idx] = options->need_avg_sep ? H.avg[idx] : 0.0;
+            results->weightavg[idx] = need_w ? H.wsum[idx] : 0.0;
+        }
+    }
+    free_hist(&H);
+    free(supp);
+    reset_bin_refine_factors(options);
+    if (options->c_api_timer) options->c_api_time = wall_now() - t0;
+    return EXIT_SUCCESS;
+}
+
+void free_results_s_mu(results_countpairs_s_mu *results)
+{
+    if (results == NULL) return;
+    free(results->npairs);
+    free(results->supp);
+    free(results->savg);
+    free(results->weightavg);
+    results->npairs = NULL;
+    results->supp = NULL;
+    results->savg = NULL;
+    results->weightavg = NULL;
+}
+
+/* weighted sums for the analytic RR of xi / wp (theory/xi/countpairs_xi_impl.c.src:581-596) */
+static void weight_sums(const struct extra_options *extra, int need_w, int64_t nd, size_t es, double *ws, double *wss)
+{
+    *ws = (double)nd;
+    *wss = (double)nd;
+    if (need_w && extra->weight_method == PAIR_PRODUCT) {
+        const void *w = extra->weights0.weights[0];
+        double a = 0.0, b = 0.0;
+        for (int64_t j = 0; j < nd; j++) {
+            const double v = wval(w, j, es);
+            a += v;
+            b += v * v;
+        }
+        *ws = a;
+        *wss = (double)nd + b;
+    }
+}
+
+/* ========================= countpairs_wp ========================= */
+/* theory/wp/countpairs_wp_impl.c.src:148-676 */
+int countpairs_wp(const int64_t ND, void *X, void *Y, void *Z, const double boxsize, const int numthreads,
+                  const char *binfile, const double pimax, results_countpairs_wp *results,
+                  struct config_options *options, struct extra_options *extra)
+{
+    (void)numthreads;
+    const double t0 = wall_now();
+    if (check_options(options, __func__) != EXIT_SUCCESS || results == NULL) return EXIT_FAILURE;
+    struct extra_options dummy;
+    if (extra == NULL) {
+        dummy = get_extra_options(NONE);
+        extra = &dummy;
+    }
+    options->periodic = 1;
+    options->autocorr = 1;
+    if (check_weights(extra, 1) != EXIT_SUCCESS) return EXIT_FAILURE;
+    const int need_w = extra->weight_method != NONE;
+    sanitize_lattice_options(options);
+    options->sort_on_z = 1;
+    double *rupp = NULL, rpmin, rpmax;
+    int nrpbins;
+    if (read_bins(binfile, &rupp, &nrpbins, &rpmin, &rpmax) != EXIT_SUCCESS) return EXIT_FAILURE;
+    cf_job J;
+    init_job(&J, options, CF_MODE_WP, 1);
+    J.n1 = J.n2 = ND;
+    J.x1 = J.x2 = X;
+    J.y1 = J.y2 = Y;
+    J.z1 = J.z2 = Z;
+    J.need_weight = need_w;
+    J.w1 = J.w2 = need_w ? extra->weights0.weights[0] : NULL;
+    fill_rule_box(&J.rule, options, boxsize, rpmax, pimax, CF_DFL_WP, ND);
+    J.rmax_xy = rpmax;
+    J.rmax_z = pimax;
+    J.rmax_3d = 0.0;
+    J.pimax = pimax;
+    J.npibin = 1;
+    J.nedges = nrpbins;
+    for (int i = 0; i < nrpbins; i++) J.edges[i] = rupp[i] * rupp[i];
+    cf_hist H;
+    if (alloc_hist(&H, nrpbins) != EXIT_SUCCESS) {
+        free(rupp);
+        return EXIT_FAILURE;
+    }
+    if (cf_engine_run(&J, &H) != EXIT_SUCCESS) {
+        free_hist(&H);
+        free(rupp);
+        return EXIT_FAILURE;
+    }
+    const double self_w = (need_w && rupp[0] <= 0.0) ? self_weight_sum(J.w1, ND, options->float_type) : 0.0;
+    finalize_hist(&H, 1, rupp[0] <= 0.0, 1, ND, self_w, options->need_avg_sep, need_w, 0);
+    results->nbin = nrpbins;
+    results->pimax = pimax;
+    results->npairs = malloc(sizeof(uint64_t) * nrpbins);
+    results->wp = malloc(sizeof(double) * nrpbins);
+    results->rupp = malloc(sizeof(double) * nrpbins);
+    results->rpavg = malloc(sizeof(double) * nrpbins);
+    results->weightavg = calloc(nrpbins, sizeof(double));
+    if (!results->npairs || !results->wp || !results->rupp || !results->rpavg || !results->weightavg) {
+        free_results_wp(results);
+        free_hist(&H);
+        free(rupp);
+        return EXIT_FAILURE;
+    }
+    double weightsum, weight_sqr_sum;
+    weight_sums(extra, need_w, ND, options->float_type, &weightsum, &weight_sqr_sum);
+    /* analytic RR and w_p (theory/wp/countpairs_wp_impl.c.src:622-660) */
+    const double prefac_density_DD = weightsum * (weightsum - weightsum / ND) / (boxsize * boxsize * boxsize);
+    double rlow = 0.0;
+    const double twice_pimax = 2.0 * pimax;
+    for (int i = 0; i < nrpbins; i++) {
+        results->npairs[i] = H.npairs[i];
+        results->rupp[i] = rupp[i];
+        results->rpavg[i] = options->need_avg_sep ? H.avg[i] : 0.0;
+        results->weightavg[i] = need_w ? H.wsum[i] : 0.0;
+        double weight0 = (double)results->npairs[i];
+        if (need_w && extra->weight_method == PAIR_PRODUCT) weight0 *= results->weightavg[i];
+        const double vol = M_PI * (results->rupp[i] * results->rupp[i] - rlow * rlow) * twice_pimax;
+        if (vol > 0.0) {
+            double weightrandom = prefac_density_DD * vol;
+            if (rlow <= 0.) weightrandom += weight_sqr_sum;
+            results->wp[i] = (weight0 / weightrandom - 1) * twice_pimax;
+        } else {
+            results->wp[i] = -2.0 * twice_pimax;
+        }
+        rlow = results->rupp[i];
+    }
+    free_hist(&H);
+    free(rupp);
+    reset_bin_refine_factors(options);
+    options->totncells_timings = 0; /* per cell-pair CPU timings do not exist on the GPU path */
+    if (options->c_api_timer) options->c_api_time = (wall_now() - t0) * 1e9; /* nanoseconds, as the reference's wp */
+    return EXIT_SUCCESS;
+}
+
+void free_results_wp(results_countpairs_wp *results)
+{
+    if (results == NULL) return;
+    free(results->npairs);
+    free(results->wp);
+    free(results->rupp);
+    free(results->rpavg);
+    free(results->weightavg);
+    results->npairs = NULL;
+    results->wp = NULL;
+    results->rupp = NULL;
+    results->rpavg = NULL;
+    results->weightavg = NULL;
+}
+
+/* ========================= countpairs_xi ========================= */
+/* theory/xi/countpairs_xi_impl.c.src:135-643 */
+int countpairs_xi(const int64_t ND, void *X, void *Y, void *Z, const double boxsize, const int numthreads,
+                  const char *binfile, results_countpairs_xi *results, struct config_options *options,
+                  struct extra_options *extra)
+{
+    (void)numthreads;
+    const double t0 = wall_now();
+    if (check_options(options, __func__) != EXIT_SUCCESS || results == NULL) return EXIT_FAILURE;
+    struct extra_options dummy;
+    if (extra == NULL) {
+        dummy = get_extra_options(NONE);
+        extra = &dummy;
+    }
+    options->periodic = 1;
+    options->autocorr = 1;
+    if (check_weights(extra, 1) != EXIT_SUCCESS) return EXIT_FAILURE;
+    const int need_w = extra->weight_method != NONE;
+    sanitize_lattice_options(options);
+    options->sort_on_z = 1;
+    double *rupp = NULL, rmin, rmax;
+    int nbins;
+    if (read_bins(binfile, &rupp, &nbins, &rmin, &rmax) != EXIT_SUCCESS) return EXIT_FAILURE;
+    cf_job J;
+    init_job(&J, options, CF_MODE_R3, 1);
+    J.n1 = J.n2 = ND;
+    J.x1 = J.x2 = X;
+    J.y1 = J.y2 = Y;
+    J.z1 = J.z2 = Z;
+    J.need_weight = need_w;
+    J.w1 = J.w2 = need_w ? extra->weights0.weights[0] : NULL;
+    fill_rule_box(&J.rule, options, boxsize, rmax, rmax, CF_DFL_XI, ND);
+    J.rmax_xy = J.rmax_z = J.rmax_3d = rmax;
+    J.nedges = nbins;
+    for (int i = 0; i < nbins; i++) J.edges[i] = rupp[i] * rupp[i];
+    cf_hist H;
+    if (alloc_hist(&H, nbins) != EXIT_SUCCESS) {
+        free(rupp);
+        return EXIT_FAILURE;
+    }
+    if (cf_engine_run(&J, &H) != EXIT_SUCCESS) {
+        free_hist(&H);
+        free(rupp);
+        return EXIT_FAILURE;
+    }
+    const double self_w = (need_w && rupp[0] <= 0.0) ? self_weight_sum(J.w1, ND, options->float_type) : 0.0;
+    finalize_hist(&H, 1, rupp[0] <= 0.0, 1, ND, self_w, options->need_avg_sep, need_w, 0);
+    results->nbin = nbins;
+    results->npairs = malloc(sizeof(uint64_t) * nbins);
+    results->xi = malloc(sizeof(double) * nbins);
+    results->rupp = malloc(sizeof(double) * nbins);
+    results->ravg = malloc(sizeof(double) * nbins);
+    results->weightavg = calloc(nbins, sizeof(double));
+    if (!results->npairs || !results->xi || !results->rupp || !results->ravg || !results->weightavg) {
+        free_results_xi(results);
+        free_hist(&H);
+        free(rupp);
+        return EXIT_FAILURE;
+    }
+    double weightsum, weight_sqr_sum;
+    weight_sums(extra, need_w, ND, options->float_type, &weightsum, &weight_sqr_sum);
+    /* analytic RR and xi (theory/xi/countpairs_xi_impl.c.src:597-626) */
+    const double prefac_density = weightsum * (weightsum - weightsum / ND) / (boxsize * boxsize * boxsize);
+    double rlow = 0.0;
+    for (int i = 0; i < nbins; i++) {
+        results->npairs[i] = H.npairs[i];
+        results->rupp[i] = rupp[i];
+        results->ravg[i] = options->need_avg_sep ? H.avg[i] : 0.0;
+        results->weightavg[i] = need_w ? H.wsum[i] : 0.0;
+        double weight0 = (double)results->npairs[i];
+        if (need_w && extra->weight_method == PAIR_PRODUCT) weight0 *= results->weightavg[i];
+        const double vol = 4.0 / 3.0 * M_PI * (rupp[i] * rupp[i] * rupp[i] - rlow * rlow * rlow);
+        if (vol > 0.0) {
+            double weightrandom = prefac_density * vol;
+            if (rlow <= 0.) weightrandom += weight_sqr_sum;
+            results->xi[i] = (weight0 / weightrandom - 1.0);
+        } else {
+            results->xi[i] = -2.0;
+        }
+        rlow = results->rupp[i];
+    }
+    free_hist(&H);
+    free(rupp);
+    reset_bin_refine_factors(options);
+    if (options->c_api_timer) options->c_api_time = wall_now() - t0;
+    return EXIT_SUCCESS;
+}
+
+void free_results_xi(results_countpairs_xi *results)
+{
+    if (results == NULL) return;
+    free(results->npairs);
+    free(results->xi);
+    free(results->rupp);
+    free(results->ravg);
+    free(results->weightavg);
+    results->npairs = NULL;
+    results->xi = NULL;
+    results->rupp = NULL;
+    results->ravg = NULL;
+    results->weightavg = NULL;
+}
+
+/* ========================= countpairs_theta_mocks (DDtheta) ========================= */
+/* RA / DEC sanity fix-ups (mocks/DDtheta_mocks/countpairs_theta_mocks_impl.c.src:42-83):
+ * the reference shifts RA by +180 and DEC by -90 in place when they look like the other
+ * convention. */
+static int check_ra_dec(int64_t n, void *ra, void *dec, size_t es)
+{
+    if (n == 0) return EXIT_SUCCESS;
+    if (ra == NULL || dec == NULL) {
+        CF_ERR("Input arrays can not be NULL. Have RA = %p DEC = %p", ra, dec);
+        return EXIT_FAILURE;
+    }
+    int fix_ra = 0, fix_dec = 0;
+    for (int64_t i = 0; i < n; i++) {
+        const double r = wval(ra, i, es), d = wval(dec, i, es);
+        if (r < 0.0) fix_ra = 1;
+        if (!(d <= 180.0)) {
+            CF_ERR("Declination should not be more than 180. Did you swap ra and dec?");
+            return EXIT_FAILURE;
+        }
+        if (d > 90.0) fix_dec = 1;
+    }
+    if (fix_ra || fix_dec) {
+        if (fix_ra) fprintf(stderr, "DDtheta> Out of range values found for ra. Expected ra to be in the range [0.0,360.0]. Found ra values in [-180,180] -- fixing that\n");
+        if (fix_dec) fprintf(stderr, "DDtheta> Out of range values found for dec. Expected dec to be in the range [-90.0,90.0]. Found dec values in [0,180] -- fixing that\n");
+        for (int64_t i = 0; i < n; i++) {
+            if (es == sizeof(float)) {
+                if (fix_ra) ((float *)ra)[i] += 180.0f;
+                if (fix_dec) ((float *)dec)[i] -= 90.0f;
+            } else {
+                if (fix_ra) ((double *)ra)[i] += 180.0;
+                if (fix_dec) ((double *)dec)[i] -= 90.0;
+            }
+        }
+    }
+    return EXIT_SUCCESS;
+}
+
+#define CF_PI_OVER_180 0.017453292519943295769236907684886127134428718885417254560971
+
+/* unit vectors on the host with libm, as the reference does
+ * (mocks/DDtheta_mocks/countpairs_theta_mocks_impl.c.src:586-608) */
+static int unit_vectors(int64_t n, const void *ra, const void *dec, const void *w, size_t es, double **X, double **Y,
+                        double **Z, double **W)
+{
+    *X = malloc(sizeof(double) * (n > 0 ? n : 1));
+    *Y = malloc(sizeof(double) * (n > 0 ? n : 1));
+    *Z = malloc(sizeof(double) * (n > 0 ? n : 1));
+    *W = w ? malloc(sizeof(double) * (n > 0 ? n : 1)) : NULL;
+    if (!*X || !*Y || !*Z || (w && !*W)) return EXIT_FAILURE;
+    for (int64_t i = 0; i < n; i++) {
+        const double r = wval(ra, i, es), d = wval(dec, i, es);
+        const double cd = cos(d * CF_PI_OVER_180);
+        (*X)[i] = cd * cos(r * CF_PI_OVER_180);
+        (*Y)[i] = cd * sin(r * CF_PI_OVER_180);
+        (*Z)[i] = sin(d * CF_PI_OVER_180);
+        if (w) (*W)[i] = wval(w, i, es);
+    }
+    return EXIT_SUCCESS;
+}
+
+int countpairs_theta_mocks(const int64_t ND1, void *phi1, void *theta1, const int64_t ND2, void *phi2, void *theta2,
+                           const int numthreads, const int autocorr, const char *binfile,
+                           results_countpairs_theta *results, struct config_options *options,
+                           struct extra_options *extra)
+{
+    (void)numthreads;
+    const double t0 = wall_now();
+    if (check_options(options, __func__) != EXIT_SUCCESS || results == NULL) return EXIT_FAILURE;
+    struct extra_options dummy;
+    if (extra == NULL) {
+        dummy = get_extra_options(NONE);
+        extra = &dummy;
+    }
+    if (autocorr != 0 && autocorr != 1) {
+        CF_ERR("Strange value of autocorr = %d", autocorr);
+        return EXIT_FAILURE;
+    }
+    if (ND1 == 0 || ND2 == 0) {
+        /* mocks/DDtheta_mocks/countpairs_theta_mocks_impl.c.src:464-477 */
+        fprintf(stderr, "Warning: Received 0 particles in at least one of the arrays. len(array1) = %lld len(array2) = %lld\n",
+                (long long)ND1, (long long)ND2);
+        results->npairs = NULL;
+        results->theta_avg = NULL;
+        results->weightavg = NULL;
+        results->theta_upp = NULL;
+        results->nbin = 0;
+        return EXIT_SUCCESS;
+    }
+    if (check_weights(extra, autocorr) != EXIT_SUCCESS) return EXIT_FAILURE;
+    const int need_w = extra->weight_method != NONE;
+    const size_t es = options->float_type;
+    if (check_ra_dec(ND1, phi1, theta1, es) != EXIT_SUCCESS) return EXIT_FAILURE;
+    if (!autocorr && check_ra_dec(ND2, phi2, theta2, es) != EXIT_SUCCESS) return EXIT_FAILURE;
+    if (options->max_cells_per_dim == 0) options->max_cells_per_dim = NLATMAX;
+    double *theta_upp = NULL, thetamin, thetamax;
+    int nthetabin;
+    if (cf_setup_bins(binfile, &thetamin, &thetamax, &nthetabin, &theta_upp) != EXIT_SUCCESS) return EXIT_FAILURE;
+    if (!(thetamin >= 0.0 && thetamax > 0.0 && thetamin < thetamax && thetamax <= 180.0 && nthetabin >= 1)) {
+        CF_ERR("Could not setup with theta bins correctly. (thetamin = %lf, thetamax = %lf, with nbins = %d). "
+               "Expected non-zero rmin/rmax with thetamax > thetamin and nbins >=1 ",
+               thetamin, thetamax, nthetabin);
+        free(theta_upp);
+        return EXIT_FAILURE;
+    }
+    if (nthetabin > CF_MAX_EDGES) {
+        CF_ERR("at most %d bins are supported", CF_MAX_EDGES - 1);
+        free(theta_upp);
+        return EXIT_FAILURE;
+    }
+    double *X1 = NULL, *Y1 = NULL, *Z1 = NULL, *W1 = NULL, *X2 = NULL, *Y2 = NULL, *Z2 = NULL, *W2 = NULL;
+    int rc = unit_vectors(ND1, phi1, theta1, need_w ? extra->weights0.weights[0] : NULL, es, &X1, &Y1, &Z1, &W1);
+    if (rc == EXIT_SUCCESS && !autocorr)
+        rc = unit_vectors(ND2, phi2, theta2, need_w ? extra->weights1.weights[0] : NULL, es, &X2, &Y2, &Z2, &W2);
+    cf_hist H;
+    memset(&H, 0, sizeof(H));
+    if (rc == EXIT_SUCCESS) rc = alloc_hist(&H, nthetabin);
+    if (rc == EXIT_SUCCESS) {
+        cf_job J;
+        init_job(&J, options, CF_MODE_THETA, autocorr);
+        J.elem_size = 8;
+        J.n1 = ND1;
+        J.n2 = autocorr ? ND1 : ND2;
+        J.x1 = X1; J.y1 = Y1; J.z1 = Z1; J.w1 = W1;
+        J.x2 = autocorr ? X1 : X2; J.y2 = autocorr ? Y1 : Y2; J.z2 = autocorr ? Z1 : Z2; J.w2 = autocorr ? W1 : W2;
+        J.need_weight = need_w;
+        J.rule.kind = CF_REF_NONE;
+        J.nedges = nthetabin;
+        for (int i = 0; i < nthetabin; i++) J.edges[i] = cos(theta_upp[i] * CF_PI_OVER_180);
+        const double cmax = J.edges[nthetabin - 1];
+        const double chord = sqrt(2.0 * (1.0 - cmax) + 1e-14) * (1.0 + 1e-9);
+        J.rmax_xy = J.rmax_z = J.rmax_3d = chord;
+        rc = cf_engine_run(&J, &H);
+    }
+    if (rc == EXIT_SUCCESS) {
+        const double self_w = (autocorr && need_w && theta_upp[0] <= 0.0) ? self_weight_sum(W1, ND1, 8) : 0.0;
+        finalize_hist(&H, autocorr, theta_upp[0] <= 0.0, 1, ND1, self_w, options->need_avg_sep, need_w, 1);
+        results->nbin = nthetabin;
+        results->npairs = malloc(sizeof(uint64_t) * nthetabin);
+        results->theta_upp = malloc(sizeof(double) * nthetabin);
+        results->theta_avg = malloc(sizeof(double) * nthetabin);
+        results->weightavg = calloc(nthetabin, sizeof(double));
+        if (!results->npairs || !results->theta_upp || !results->theta_avg || !results->weightavg) {
+            free_results_countpairs_theta(results);
+            rc = EXIT_FAILURE;
+        } else {
+            for (int i = 0; i < nthetabin; i++) {
+                results->npairs[i] = H.npairs[i];
+                results->theta_upp[i] = theta_upp[i];
+                results->theta_avg[i] = options->need_avg_sep ? H.avg[i] : 0.0;
+                results->weightavg[i] = need_w ? H.wsum[i] : 0.0;
+            }
+        }
+    }
+    free_hist(&H);
+    free(X1); free(Y1); free(Z1); free(W1);
+    free(X2); free(Y2); free(Z2); free(W2);
+    free(theta_upp);
+    if (rc != EXIT_SUCCESS) return EXIT_FAILURE;
+    reset_bin_refine_factors(options);
+    if (options->c_api_timer) options->c_api_time = wall_now() - t0;
+    return EXIT_SUCCESS;
+}
+
+void free_results_countpairs_theta(results_countpairs_theta *results)
+{
+    if (results == NULL) return;
+    free(results->npairs);
+    free(results->theta_upp);
+    free(results->theta_avg);
+    free(results->weightavg);
+    results->npairs = NULL;
+    results->theta_upp = NULL;
+    results->theta_avg = NULL;
+    results->weightavg = NULL;
+}
+
+/* ========================= GB300 extensions ========================= */
+int cf_gpu_set_precision(int mode) { return cf_engine_set_precision(mode); }
+
+int cf_gpu_get_precision(void) { return cf_engine_get_precision(); }
+
+int cf_gpu_last_stats(cf_gpu_stats *out)
+{
+    if (out == NULL) return EXIT_FAILURE;
+    cf_engine_stats s;
+    if (cf_engine_last_stats(&s) != EXIT_SUCCESS) return EXIT_FAILURE;
+    out->pair_kernel_ms = s.pair_kernel_ms;
+    out->gridlink_ms = s.gridlink_ms;
+    out->total_gpu_ms = s.total_gpu_ms;
+    out->pairs_evaluated = s.pairs_evaluated;
+    out->pairs_refined = s.pairs_refined;
+    out->tasks = s.tasks;
+    out->kernel_launches = s.kernel_launches;
+    out->num_cells = s.num_cells;
+    return EXIT_SUCCESS;
+}

@@ -1,0 +1,185 @@
+// cf_device.cuh -- device-side data structures and per-pair arithmetic shared by the
+// GB300 pair-counting kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cf {
+
+// One unit of pair work: up to 32 consecutive points of one lattice column ("i-chunk")
+// against one contiguous range of points of a neighbouring column ("j-range") with a fixed
+// periodic image.  meta packs: bits 0-5 i_count-1, bits 8/10/12 (2 bits each) image+1 per
+// axis, bit 16 'own' (auto-correlation, same column, same image: count only j > i).
+struct Task {
+    uint32_t i_begin;
+    uint32_t j_begin;
+    uint32_t j_end;
+    uint32_t meta;
+};
+
+__host__ __device__ inline uint32_t task_meta(int icount, int mx, int my, int mz, int own)
+{
+    return (uint32_t)(icount - 1) | ((uint32_t)(mx + 1) << 8) | ((uint32_t)(my + 1) << 10) |
+           ((uint32_t)(mz + 1) << 12) | ((uint32_t)own << 16);
+}
+
+// Sorted point record kept per lattice (SoA of these arrays).
+struct Lattice {
+    float4 *hi;       // x_hi, y_hi, z_hi on the per-axis grid q (exact differences), w as float
+    float4 *lo;       // x - x_hi, y - y_hi, z - z_hi (float), unused
+    double4_32a *dbl;     // original coordinates (x, y, z, w) in double
+    int *refcell;     // cell index of the point in the reference lattice (first-point rule)
+    int *orig;        // index of the point in the caller's arrays
+    uint32_t *cellid; // GPU lattice cell of each sorted point
+    uint32_t *cell_start; // ncells + 1 offsets
+};
+
+enum { MODE_R3 = 0, MODE_RPPI = 1, MODE_WP = 2, MODE_SMU = 3, MODE_THETA = 4 };
+
+struct PairArgs {
+    // lattices (set 1 = i points, set 2 = j points; identical for auto-correlations)
+    const float4 *hi1, *lo1;
+    const double4_32a *d1;
+    const int *rc1, *or1;
+    const float4 *hi2, *lo2;
+    const double4_32a *d2;
+    const int *rc2, *or2;
+
+    const Task *tasks;
+    uint32_t ntasks;
+    uint32_t *task_counter;
+
+    unsigned long long *g_cnt;  // nbins
+    double *g_avg;              // nbins
+    double *g_w;                // nbins
+    unsigned long long *g_stats; // [0] evaluated pairs, [1] refined pairs
+    const double *g_edges;      // nedges (double, reference values)
+    const float *g_guard;       // 2*nedges: lo guards then hi guards
+
+    int nedges;
+    int nbins;
+    int npibin;                 // rp-pi: pi bins, s-mu: mu bins
+    int autocorr;
+    int fma_formula;
+    int chord_formula;
+
+    // image offsets per axis for image index m+1 (m = -1, 0, +1)
+    float ohi[3][3];
+    float olo[3][3];
+    double odbl[3][3];
+
+    // rp-pi / wp / s-mu constants (reference values and FP32 classification bands)
+    double pimax;
+    double inv_dpi;
+    double sqr_mu_max;
+    double inv_dmu;
+    float pimax_lo_f, pimax_hi_f;  // guard band around pimax for |dz|
+    float inv_dpi_f;
+    float pibin_band;              // half-width (in pi-bin units) of the ambiguity band
+    float mu_band_abs;             // absolute mu error bound numerator (divided by s)
+    float mu_max_f;
+    float inv_dmu_f;
+    float dz_err;                  // bound on |dz_f32 - dz_ref|
+    float dxy_err;                 // bound on |(dx,dy)_f32 - (dx,dy)_ref|
+
+    // fixed-point scales for the per-warp accumulators
+    float avg_scale_f;
+    double avg_unscale;
+    float w_scale_f;
+    double w_unscale;
+};
+
+// ---------------------------------------------------------------------------------------
+// Reference (double-precision) evaluation of one pair, with the first point of the pair
+// shifted by the periodic offset, exactly as the reference kernels do.  Every operation uses
+// an explicitly rounded intrinsic so that no fused multiply-add is introduced unless the
+// formula being reproduced has one.
+// Returns the flat histogram bin, or -1 when the pair is not counted.
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ int bin_upper(const double *e, int n, double v)
+{
+    // number of edges <= v (edges sorted ascending)
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (e[mid] <= v) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ int bin_theta(const double *c, int n, double v)
+{
+    // reference rule: largest k in [1, n-1] with v <= c[k-1]; c is descending.
+    // number of leading edges with c[k] >= v
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (c[mid] >= v) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+template <int MODE>
+__device__ __forceinline__ int ref_eval(const PairArgs &A, const double *se,
+                                        double xa, double ya, double za,
+                                        double xb, double yb, double zb,
+                                        double ox, double oy, double oz, double *avg_term)
+{
+    const int nb = A.nedges;
+    if (MODE == MODE_THETA) {
+        double c;
+        if (A.chord_formula) {
+            const double dx = __dsub_rn(xb, xa), dy = __dsub_rn(yb, ya), dz = __dsub_rn(zb, za);
+            double ch2;
+            if (A.fma_formula) ch2 = __fma_rn(dz, dz, __fma_rn(dy, dy, __dmul_rn(dx, dx)));
+            else ch2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+            c = __dsub_rn(1.0, __dmul_rn(0.5, ch2));
+        } else {
+            c = __dadd_rn(__dadd_rn(__dmul_rn(xb, xa), __dmul_rn(yb, ya)), __dmul_rn(zb, za));
+        }
+        if (c > se[0] || c <= se[nb - 1]) return -1;
+        const int k = bin_theta(se, nb, c);  // >= 1 since c <= se[0]
+        *avg_term = 57.29577951308232087679815481410517033240547246656432154916024 * acos(c);
+        return k;
+    }
+    const double xpos = __dadd_rn(xa, ox), ypos = __dadd_rn(ya, oy), zpos = __dadd_rn(za, oz);
+    const double dx = __dsub_rn(xb, xpos), dy = __dsub_rn(yb, ypos), dz = __dsub_rn(zb, zpos);
+    if (MODE == MODE_R3) {
+        double r2;
+        if (A.fma_formula) r2 = __fma_rn(dz, dz, __fma_rn(dy, dy, __dmul_rn(dx, dx)));
+        else r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+        if (r2 >= se[nb - 1] || r2 < se[0]) return -1;
+        *avg_term = __dsqrt_rn(r2);
+        return bin_upper(se, nb, r2);
+    }
+    if (MODE == MODE_RPPI || MODE == MODE_WP) {
+        if (dz <= -A.pimax || dz >= A.pimax) return -1;
+        double r2;
+        if (A.fma_formula) r2 = __fma_rn(dy, dy, __dmul_rn(dx, dx));
+        else r2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+        if (r2 >= se[nb - 1] || r2 < se[0]) return -1;
+        const int kbin = bin_upper(se, nb, r2);
+        *avg_term = __dsqrt_rn(r2);
+        if (MODE == MODE_WP) return kbin;
+        int pibin = (int)__dmul_rn(fabs(dz), A.inv_dpi);
+        pibin = pibin > A.npibin ? A.npibin : pibin;
+        return kbin * (A.npibin + 1) + pibin;
+    }
+    // MODE_SMU
+    {
+        const double sqr_dz = __dmul_rn(dz, dz);
+        double s2;
+        if (A.fma_formula) s2 = __fma_rn(dx, dx, __fma_rn(dy, dy, sqr_dz));
+        else s2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), sqr_dz);
+        if (s2 >= se[nb - 1] || s2 < se[0]) return -1;
+        if (sqr_dz >= __dmul_rn(s2, A.sqr_mu_max)) return -1;
+        const double mu = __dsqrt_rn(__ddiv_rn(sqr_dz, s2));
+        int mubin = (int)__dmul_rn(mu, A.inv_dmu);
+        mubin = mubin > A.npibin ? A.npibin : mubin;
+        const int kbin = bin_upper(se, nb, s2);
+        *avg_term = __dsqrt_rn(s2);
+        return kbin * (A.npibin + 1) + mubin;
+    }
+}
+
+}  // namespace cf

@@ -1,0 +1,121 @@
+/*
+ * cf_internal.h -- interface between the C host layer (cf_api.c, cf_common.c) and the
+ * CUDA engine (cf_engine.cu).  Plain C types only.
+ */
+#pragma once
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Pair-separation kinds.  Each one is a family of reference kernels. */
+enum {
+    CF_MODE_R3 = 0,    /* 3-D r^2 bins: countpairs (DD) and countpairs_xi */
+    CF_MODE_RPPI = 1,  /* rp^2 bins x linear |pi| bins: countpairs_rp_pi */
+    CF_MODE_WP = 2,    /* rp^2 bins with |pi| < pimax: countpairs_wp */
+    CF_MODE_SMU = 3,   /* s^2 bins x linear mu bins: countpairs_s_mu */
+    CF_MODE_THETA = 4  /* angular bins on unit vectors: countpairs_theta_mocks */
+};
+
+#define CF_MAX_EDGES 512
+
+#ifndef CF_PRECISION_FP32_REFINE
+#define CF_PRECISION_FP32_REFINE 0
+#define CF_PRECISION_FP64 1
+#endif
+
+/* How the reference builds its lattice for one call; resolved against the data extent by
+ * cf_resolve_geometry() once the engine has measured it.  The resolved lattice fixes which
+ * point of a wrapped auto-correlation pair the reference shifts, and (for xi / wp, whose
+ * lattice is the fixed box) which points it rejects as out of bounds. */
+enum { CF_REF_NONE = 0, CF_REF_EXTENT = 1, CF_REF_BOX = 2 };
+enum { CF_DFL_PER_AXIS = 0, CF_DFL_XI = 1, CF_DFL_WP = 2, CF_DFL_NONE = 3 };
+enum { CF_BOOST_XY = 0, CF_BOOST_NONE = 1 };
+
+typedef struct {
+    int kind;            /* CF_REF_* */
+    int periodic;        /* options->periodic */
+    double boxsize[3];   /* options->boxsize_x/_y/_z with y/z defaulted to x (or the box for xi/wp) */
+    double max_size[3];  /* cell size limit per axis handed to gridlink (rmax, rmax, pimax ...) */
+    int refine[3];       /* options->bin_refine_factors at call time */
+    int custom_refine;   /* binning scheme is BINNING_CUST */
+    int max_cells;       /* options->max_cells_per_dim */
+    int dfl_kind;        /* CF_DFL_* */
+    int boost_kind;      /* CF_BOOST_* */
+    int64_t np1;         /* ND1, for the boost heuristic */
+} cf_refrule;
+
+typedef struct {
+    int periodic[3];
+    double wrap[3];
+    double ref_min[3];
+    double ref_inv[3];
+    int ref_nmesh[3];
+    int refine_used[3];
+} cf_geometry;
+
+/* Restates the wrap / refine / gridlink-size logic of the reference drivers
+ * (theory/DD/countpairs_impl.c.src:231-332, theory/xi/countpairs_xi_impl.c.src:211-262,
+ * theory/wp/countpairs_wp_impl.c.src:236-290, utils/gridlink_utils.c.src:31-49).
+ * lo/hi: data extent (both sets).  Returns EXIT_FAILURE (message on stderr) where the
+ * reference would fail. */
+int cf_resolve_geometry(const cf_refrule *rule, const double lo[3], const double hi[3], cf_geometry *out);
+
+typedef struct {
+    int mode;
+    int autocorr;
+    int precision;       /* CF_PRECISION_FP32_REFINE or CF_PRECISION_FP64 */
+    int fma_formula;     /* evaluate the double-precision formula of the reference's AVX512F kernels */
+    int chord_formula;   /* theta: cos = 1 - chord^2/2 (SIMD kernels) instead of the dot product */
+    int elem_size;       /* 4 or 8: element type of the host position / weight arrays */
+
+    int64_t n1, n2;
+    const void *x1, *y1, *z1, *w1;  /* host arrays (w1 may be NULL) */
+    const void *x2, *y2, *z2, *w2;  /* ignored when autocorr */
+
+    cf_refrule rule;     /* resolved by the engine once the extent is known */
+    cf_geometry geom;    /* output: the resolved geometry (filled by cf_engine_run) */
+
+    /* separation limits that bound the neighbour search */
+    double rmax_xy;      /* max separation in the (x,y) plane (3-D: rmax; rp-pi: rpmax; theta: chord) */
+    double rmax_z;       /* max |dz| (3-D: rmax; rp-pi: pimax; s-mu: min(smax, smax*mu_max)) */
+    double rmax_3d;      /* spherical limit, or 0 when the mode has none (rp-pi / wp) */
+
+    int nedges;          /* number of bin edges incl. the junk-bin lower edge */
+    double edges[CF_MAX_EDGES]; /* squared separations (R3/RPPI/WP/SMU) or cos(theta) (THETA) */
+    double pimax;        /* RPPI / WP */
+    int npibin;          /* RPPI: pi bins; SMU: mu bins */
+    double mu_max;       /* SMU */
+
+    int need_avg;
+    int need_weight;
+} cf_job;
+
+typedef struct {
+    int nbins;           /* total flat bins: nedges, or nedges*(npibin+1) for 2-D modes */
+    uint64_t *npairs;    /* caller-allocated, nbins entries each */
+    double *avg;         /* sum of separations (r, rp, s, or theta in degrees) */
+    double *wsum;        /* sum of w1*w2 */
+} cf_hist;
+
+int cf_engine_run(cf_job *job, cf_hist *out);
+int cf_engine_set_precision(int mode);
+int cf_engine_get_precision(void);
+
+typedef struct {
+    double pair_kernel_ms;
+    double gridlink_ms;
+    double total_gpu_ms;
+    uint64_t pairs_evaluated;
+    uint64_t pairs_refined;
+    uint64_t tasks;
+    int kernel_launches;
+    int num_cells;
+} cf_engine_stats;
+int cf_engine_last_stats(cf_engine_stats *out);
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,94 @@
+"""Python front end for the angular pair counter, mirroring Corrfunc.mocks.DDtheta_mocks
+(Corrfunc/mocks/DDtheta_mocks.py:19-357)."""
+import ctypes
+
+import numpy as np
+
+from . import _capi as C
+
+DDTHETA_DTYPE = np.dtype([("thetamin", np.float64), ("thetamax", np.float64), ("thetaavg", np.float64),
+                          ("npairs", np.uint64), ("weightavg", np.float64)])
+
+
+def _fix_ra_dec(ra, dec):
+    """In-place wrap as Corrfunc/utils.py:421-461 does: RA += 180 when any RA < 0, DEC -= 90 when
+    any DEC > 90 (the caller's arrays are modified, as with the reference)."""
+    if not hasattr(ra, "dtype") or not hasattr(dec, "dtype"):
+        raise TypeError("Input RA array must be a numpy array")
+    if min(ra) < 0.0:
+        print("Warning: found negative RA values, wrapping into [0.0, 360.0]  range")
+        ra += 180.0
+    if max(dec) > 90.0:
+        print("Warning: found DEC values more than 90.0; wrapping into [-90.0, 90.0] range")
+        dec -= 90.0
+    return ra, dec
+
+
+def run_DDtheta_mocks(lib, autocorr, nthreads, binfile, RA1, DEC1, weights1=None, RA2=None, DEC2=None,
+                      weights2=None, link_in_dec=True, link_in_ra=True, verbose=False, output_thetaavg=False,
+                      fast_acos=False, ra_refine_factor=2, dec_refine_factor=2, max_cells_per_dim=100,
+                      copy_particles=True, enable_min_sep_opt=True, c_api_timer=False, isa="fastest",
+                      weight_type=None):
+    if not autocorr and (RA2 is None or DEC2 is None):
+        raise ValueError("Must pass valid arrays for RA2/DEC2 for computing cross-correlation")
+    RA1, DEC1 = _fix_ra_dec(RA1, DEC1)
+    RA1 = C.as_positions(RA1)
+    dt = RA1.dtype
+    DEC1 = C.as_positions(DEC1, dt)
+    if not autocorr:
+        RA2, DEC2 = _fix_ra_dec(RA2, DEC2)
+        RA2 = C.as_positions(RA2, dt)
+        DEC2 = C.as_positions(DEC2, dt)
+    else:
+        RA2 = DEC2 = None
+    w1, w2 = C.process_weights(weights1, weights2, RA1, RA2, weight_type, autocorr)
+    if link_in_ra:
+        link_in_dec = True
+    o = C.get_config_options()
+    o.verbose = 1 if verbose else 0
+    o.instruction_set = C.translate_isa(isa) if isinstance(isa, str) else int(isa)
+    o.link_in_dec = 1 if link_in_dec else 0
+    o.link_in_ra = 1 if link_in_ra else 0
+    o.need_avg_sep = 1 if output_thetaavg else 0
+    o.fast_acos = 1 if fast_acos else 0
+    o.max_cells_per_dim = int(max_cells_per_dim)
+    o.copy_particles = 1 if copy_particles else 0
+    o.enable_min_sep_opt = 1 if enable_min_sep_opt else 0
+    o.c_api_timer = 1 if c_api_timer else 0
+    o.autocorr = 1 if autocorr else 0
+    o.periodic = 0
+    o.float_type = dt.itemsize
+    C.set_refine(o, (ra_refine_factor, dec_refine_factor, o.bin_refine_factors[2]))
+    extra = C.get_extra_options(C.weight_method_by_name(weight_type))
+    keep = []
+    C.fill_weights(extra, w1, w2, keep)
+    res = C.ResultsTheta()
+    if autocorr:
+        # the CPython binding hands the first set over twice (mocks/python_bindings/_countpairs_mocks.c:1885)
+        RA2p, DEC2p, n2 = RA1, DEC1, len(RA1)
+    else:
+        RA2p, DEC2p, n2 = RA2, DEC2, len(RA2)
+    with C.BinFile(binfile) as bf:
+        rc = lib.countpairs_theta_mocks(len(RA1), C.ptr(RA1), C.ptr(DEC1), n2, C.ptr(RA2p), C.ptr(DEC2p),
+                                        int(nthreads), int(autocorr), bf.encode(), ctypes.byref(res),
+                                        ctypes.byref(o), ctypes.byref(extra))
+    if rc != 0:
+        raise RuntimeError("RuntimeError occurred")
+    nb = res.nbin if bool(res.npairs) else 0
+    npairs = C.carray(res.npairs, nb, np.uint64)
+    tupp = C.carray(res.theta_upp, nb, np.float64)
+    tavg = C.carray(res.theta_avg, nb, np.float64)
+    wavg = C.carray(res.weightavg, nb, np.float64)
+    lib.free_results_countpairs_theta(ctypes.byref(res))
+    out = np.zeros(max(nb - 1, 0), dtype=DDTHETA_DTYPE)
+    out["thetamin"] = tupp[:-1]
+    out["thetamax"] = tupp[1:]
+    out["thetaavg"] = tavg[1:]
+    out["npairs"] = npairs[1:]
+    out["weightavg"] = wavg[1:]
+    return (out, o.c_api_time) if c_api_timer else out
+
+
+def DDtheta_mocks(*args, **kwargs):
+    """Angular pair counts DD(theta); see Corrfunc.mocks.DDtheta_mocks."""
+    return run_DDtheta_mocks(C.library(), *args, **kwargs)

@@ -1,0 +1,288 @@
+"""Python front end for the theory pair counters, mirroring Corrfunc.theory.
+
+``DD``, ``DDrppi``, ``DDsmu``, ``wp`` and ``xi`` take the same arguments and return the same
+numpy structured arrays as Corrfunc 2.5.3 (Corrfunc/theory/DD.py:16-284 and siblings).  They
+call the C ABI of libcorrfunc_gb300.so, whose counting runs on the GPU.  The ``run_*``
+functions take the library handle explicitly; any library exporting the reference's C API
+(theory/DD/countpairs.h and siblings) can be driven by them.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _capi as C
+
+DD_DTYPE = np.dtype([("rmin", np.float64), ("rmax", np.float64), ("ravg", np.float64),
+                     ("npairs", np.uint64), ("weightavg", np.float64)])
+DDRPPI_DTYPE = np.dtype([("rmin", np.float64), ("rmax", np.float64), ("rpavg", np.float64),
+                         ("pimax", np.float64), ("npairs", np.uint64), ("weightavg", np.float64)])
+DDSMU_DTYPE = np.dtype([("smin", np.float64), ("smax", np.float64), ("savg", np.float64),
+                        ("mu_max", np.float64), ("npairs", np.uint64), ("weightavg", np.float64)])
+WP_DTYPE = np.dtype([("rmin", np.float64), ("rmax", np.float64), ("rpavg", np.float64),
+                     ("wp", np.float64), ("npairs", np.uint64), ("weightavg", np.float64)])
+XI_DTYPE = np.dtype([("rmin", np.float64), ("rmax", np.float64), ("ravg", np.float64),
+                     ("xi", np.float64), ("npairs", np.uint64), ("weightavg", np.float64)])
+
+
+def _boxsize3(boxsize):
+    b = np.atleast_1d(boxsize)
+    if len(b) == 1:
+        return (float(b[0]),) * 3
+    return tuple(float(v) for v in b)
+
+
+def _common_options(nthreads, periodic, boxsize, verbose, need_avg, refine, max_cells, copy_particles,
+                    enable_min_sep_opt, c_api_timer, isa, dtype):
+    o = C.get_config_options()
+    o.verbose = 1 if verbose else 0
+    o.periodic = 1 if periodic else 0
+    o.need_avg_sep = 1 if need_avg else 0
+    o.c_api_timer = 1 if c_api_timer else 0
+    o.copy_particles = 1 if copy_particles else 0
+    o.enable_min_sep_opt = 1 if enable_min_sep_opt else 0
+    o.max_cells_per_dim = int(max_cells)
+    o.instruction_set = C.translate_isa(isa) if isinstance(isa, str) else int(isa)
+    o.float_type = np.dtype(dtype).itemsize
+    if boxsize is not None:
+        bx, by, bz = _boxsize3(boxsize)
+        o.boxsize_x, o.boxsize_y, o.boxsize_z = bx, by, bz
+    C.set_refine(o, refine)
+    return o
+
+
+def _pair_inputs(autocorr, X1, Y1, Z1, X2, Y2, Z2, weights1, weights2, weight_type):
+    if not autocorr and (X2 is None or Y2 is None or Z2 is None):
+        raise ValueError("Must pass valid arrays for X2/Y2/Z2 for computing cross-correlation")
+    X1 = C.as_positions(X1)
+    dt = X1.dtype
+    Y1 = C.as_positions(Y1, dt)
+    Z1 = C.as_positions(Z1, dt)
+    if not autocorr:
+        X2, Y2, Z2 = (C.as_positions(a, dt) for a in (X2, Y2, Z2))
+    else:
+        X2 = Y2 = Z2 = None
+    w1, w2 = C.process_weights(weights1, weights2, X1, X2, weight_type, autocorr)
+    return X1, Y1, Z1, X2, Y2, Z2, w1, w2
+
+
+def run_DD(lib, autocorr, nthreads, binfile, X1, Y1, Z1, weights1=None, periodic=True, boxsize=None, X2=None,
+           Y2=None, Z2=None, weights2=None, verbose=False, output_ravg=False, xbin_refine_factor=2,
+           ybin_refine_factor=2, zbin_refine_factor=1, max_cells_per_dim=100, copy_particles=True,
+           enable_min_sep_opt=True, c_api_timer=False, isa="fastest", weight_type=None):
+    if periodic and boxsize is None:
+        raise ValueError("Must specify a boxsize if periodic=True")
+    X1, Y1, Z1, X2, Y2, Z2, w1, w2 = _pair_inputs(autocorr, X1, Y1, Z1, X2, Y2, Z2, weights1, weights2, weight_type)
+    o = _common_options(nthreads, periodic, boxsize, verbose, output_ravg,
+                        (xbin_refine_factor, ybin_refine_factor, zbin_refine_factor), max_cells_per_dim,
+                        copy_particles, enable_min_sep_opt, c_api_timer, isa, X1.dtype)
+    extra = C.get_extra_options(C.weight_method_by_name(weight_type))
+    keep = []
+    C.fill_weights(extra, w1, w2, keep)
+    res = C.ResultsDD()
+    n2 = 0 if autocorr else len(X2)
+    with C.BinFile(binfile) as bf:
+        rc = lib.countpairs(len(X1), C.ptr(X1), C.ptr(Y1), C.ptr(Z1), n2, C.ptr(X2), C.ptr(Y2), C.ptr(Z2),
+                            int(nthreads), int(autocorr), bf.encode(), ctypes.byref(res), ctypes.byref(o),
+                            ctypes.byref(extra))
+    if rc != 0:
+        raise RuntimeError("RuntimeError occurred")
+    nb = res.nbin
+    npairs = C.carray(res.npairs, nb, np.uint64)
+    rupp = C.carray(res.rupp, nb, np.float64)
+    ravg = C.carray(res.rpavg, nb, np.float64)
+    wavg = C.carray(res.weightavg, nb, np.float64)
+    lib.free_results(ctypes.byref(res))
+    out = np.zeros(max(nb - 1, 0), dtype=DD_DTYPE)
+    out["rmin"] = rupp[:-1]
+    out["rmax"] = rupp[1:]
+    out["ravg"] = ravg[1:]
+    out["npairs"] = npairs[1:]
+    out["weightavg"] = wavg[1:]
+    return (out, o.c_api_time) if c_api_timer else out
+
+
+def run_DDrppi(lib, autocorr, nthreads, pimax, binfile, X1, Y1, Z1, weights1=None, periodic=True, boxsize=None,
+               X2=None, Y2=None, Z2=None, weights2=None, verbose=False, output_rpavg=False, xbin_refine_factor=2,
+               ybin_refine_factor=2, zbin_refine_factor=1, max_cells_per_dim=100, copy_particles=True,
+               enable_min_sep_opt=True, c_api_timer=False, isa="fastest", weight_type=None):
+    if periodic and boxsize is None:
+        raise ValueError("Must specify a boxsize if periodic=True")
+    X1, Y1, Z1, X2, Y2, Z2, w1, w2 = _pair_inputs(autocorr, X1, Y1, Z1, X2, Y2, Z2, weights1, weights2, weight_type)
+    o = _common_options(nthreads, periodic, boxsize, verbose, output_rpavg,
+                        (xbin_refine_factor, ybin_refine_factor, zbin_refine_factor), max_cells_per_dim,
+                        copy_particles, enable_min_sep_opt, c_api_timer, isa, X1.dtype)
+    extra = C.get_extra_options(C.weight_method_by_name(weight_type))
+    keep = []
+    C.fill_weights(extra, w1, w2, keep)
+    res = C.ResultsRpPi()
+    n2 = 0 if autocorr else len(X2)
+    with C.BinFile(binfile) as bf:
+        rc = lib.countpairs_rp_pi(len(X1), C.ptr(X1), C.ptr(Y1), C.ptr(Z1), n2, C.ptr(X2), C.ptr(Y2), C.ptr(Z2),
+                                  int(nthreads), int(autocorr), bf.encode(), float(pimax), ctypes.byref(res),
+                                  ctypes.byref(o), ctypes.byref(extra))
+    if rc != 0:
+        raise RuntimeError("RuntimeError occurred")
+    nb, npi = res.nbin, res.npibin
+    tot = (nb + 1) * (npi + 1)
+    npairs = C.carray(res.npairs, tot, np.uint64)
+    rupp = C.carray(res.rupp, nb, np.float64)
+    rpavg = C.carray(res.rpavg, tot, np.float64)
+    wavg = C.carray(res.weightavg, tot, np.float64)
+    lib.free_results_rp_pi(ctypes.byref(res))
+    dpi = float(pimax) / npi
+    rows = []
+    for i in range(1, nb):
+        for j in range(npi):
+            idx = i * (npi + 1) + j
+            rows.append((rupp[i - 1], rupp[i], rpavg[idx], (j + 1) * dpi, npairs[idx], wavg[idx]))
+    out = np.array(rows, dtype=DDRPPI_DTYPE)
+    return (out, o.c_api_time) if c_api_timer else out
+
+
+def run_DDsmu(lib, autocorr, nthreads, binfile, mu_max, nmu_bins, X1, Y1, Z1, weights1=None, periodic=True,
+              boxsize=None, X2=None, Y2=None, Z2=None, weights2=None, verbose=False, output_savg=False,
+              fast_divide_and_NR_steps=0, xbin_refine_factor=2, ybin_refine_factor=2, zbin_refine_factor=1,
+              max_cells_per_dim=100, copy_particles=True, enable_min_sep_opt=True, c_api_timer=False,
+              isa="fastest", weight_type=None):
+    if periodic and boxsize is None:
+        raise ValueError("Must specify a boxsize if periodic=True")
+    X1, Y1, Z1, X2, Y2, Z2, w1, w2 = _pair_inputs(autocorr, X1, Y1, Z1, X2, Y2, Z2, weights1, weights2, weight_type)
+    o = _common_options(nthreads, periodic, boxsize, verbose, output_savg,
+                        (xbin_refine_factor, ybin_refine_factor, zbin_refine_factor), max_cells_per_dim,
+                        copy_particles, enable_min_sep_opt, c_api_timer, isa, X1.dtype)
+    o.fast_divide_and_NR_steps = int(fast_divide_and_NR_steps)
+    extra = C.get_extra_options(C.weight_method_by_name(weight_type))
+    keep = []
+    C.fill_weights(extra, w1, w2, keep)
+    res = C.ResultsSMu()
+    n2 = 0 if autocorr else len(X2)
+    with C.BinFile(binfile) as bf:
+        rc = lib.countpairs_s_mu(len(X1), C.ptr(X1), C.ptr(Y1), C.ptr(Z1), n2, C.ptr(X2), C.ptr(Y2), C.ptr(Z2),
+                                 int(nthreads), int(autocorr), bf.encode(), float(mu_max), int(nmu_bins),
+                                 ctypes.byref(res), ctypes.byref(o), ctypes.byref(extra))
+    if rc != 0:
+        raise RuntimeError("RuntimeError occurred")
+    nb, nmu = res.nsbin, res.nmu_bins
+    tot = (nb + 1) * (nmu + 1)
+    npairs = C.carray(res.npairs, tot, np.uint64)
+    supp = C.carray(res.supp, nb, np.float64)
+    savg = C.carray(res.savg, tot, np.float64)
+    wavg = C.carray(res.weightavg, tot, np.float64)
+    lib.free_results_s_mu(ctypes.byref(res))
+    dmu = float(mu_max) / nmu
+    rows = []
+    for i in range(1, nb):
+        for j in range(nmu):
+            idx = i * (nmu + 1) + j
+            rows.append((supp[i - 1], supp[i], savg[idx], (j + 1) * dmu, npairs[idx], wavg[idx]))
+    out = np.array(rows, dtype=DDSMU_DTYPE)
+    return (out, o.c_api_time) if c_api_timer else out
+
+
+def run_wp(lib, boxsize, pimax, nthreads, binfile, X, Y, Z, weights=None, weight_type=None, verbose=False,
+           output_rpavg=False, xbin_refine_factor=2, ybin_refine_factor=2, zbin_refine_factor=1,
+           max_cells_per_dim=100, copy_particles=True, enable_min_sep_opt=True, c_api_timer=False,
+           c_cell_timer=False, isa="fastest"):
+    X = C.as_positions(X)
+    Y = C.as_positions(Y, X.dtype)
+    Z = C.as_positions(Z, X.dtype)
+    w1, _ = C.process_weights(weights, None, X, None, weight_type, True)
+    o = _common_options(nthreads, True, boxsize, verbose, output_rpavg,
+                        (xbin_refine_factor, ybin_refine_factor, zbin_refine_factor), max_cells_per_dim,
+                        copy_particles, enable_min_sep_opt, c_api_timer, isa, X.dtype)
+    o.c_cell_timer = 1 if c_cell_timer else 0
+    extra = C.get_extra_options(C.weight_method_by_name(weight_type))
+    keep = []
+    C.fill_weights(extra, w1, None, keep)
+    res = C.ResultsWp()
+    with C.BinFile(binfile) as bf:
+        rc = lib.countpairs_wp(len(X), C.ptr(X), C.ptr(Y), C.ptr(Z), float(_boxsize3(boxsize)[0]), int(nthreads),
+                               bf.encode(), float(pimax), ctypes.byref(res), ctypes.byref(o), ctypes.byref(extra))
+    if rc != 0:
+        raise RuntimeError("RuntimeError occurred")
+    nb = res.nbin
+    npairs = C.carray(res.npairs, nb, np.uint64)
+    rupp = C.carray(res.rupp, nb, np.float64)
+    rpavg = C.carray(res.rpavg, nb, np.float64)
+    wp_ = C.carray(res.wp, nb, np.float64)
+    wavg = C.carray(res.weightavg, nb, np.float64)
+    lib.free_results_wp(ctypes.byref(res))
+    out = np.zeros(max(nb - 1, 0), dtype=WP_DTYPE)
+    out["rmin"] = rupp[:-1]
+    out["rmax"] = rupp[1:]
+    out["rpavg"] = rpavg[1:]
+    out["wp"] = wp_[1:]
+    out["npairs"] = npairs[1:]
+    out["weightavg"] = wavg[1:]
+    if c_api_timer or c_cell_timer:
+        ret = [out]
+        if c_api_timer:
+            ret.append(o.c_api_time)
+        if c_cell_timer:
+            ret.append(np.zeros(0, dtype=[("N1", np.int64), ("N2", np.int64), ("time_in_ns", np.int64),
+                                          ("first_cellindex", np.int32), ("second_cellindex", np.int32),
+                                          ("tid", np.int32)]))
+        return tuple(ret)
+    return out
+
+
+def run_xi(lib, boxsize, nthreads, binfile, X, Y, Z, weights=None, weight_type=None, verbose=False,
+           output_ravg=False, xbin_refine_factor=2, ybin_refine_factor=2, zbin_refine_factor=1,
+           max_cells_per_dim=100, copy_particles=True, enable_min_sep_opt=True, c_api_timer=False,
+           isa="fastest"):
+    X = C.as_positions(X)
+    Y = C.as_positions(Y, X.dtype)
+    Z = C.as_positions(Z, X.dtype)
+    w1, _ = C.process_weights(weights, None, X, None, weight_type, True)
+    o = _common_options(nthreads, True, boxsize, verbose, output_ravg,
+                        (xbin_refine_factor, ybin_refine_factor, zbin_refine_factor), max_cells_per_dim,
+                        copy_particles, enable_min_sep_opt, c_api_timer, isa, X.dtype)
+    extra = C.get_extra_options(C.weight_method_by_name(weight_type))
+    keep = []
+    C.fill_weights(extra, w1, None, keep)
+    res = C.ResultsXi()
+    with C.BinFile(binfile) as bf:
+        rc = lib.countpairs_xi(len(X), C.ptr(X), C.ptr(Y), C.ptr(Z), float(_boxsize3(boxsize)[0]), int(nthreads),
+                               bf.encode(), ctypes.byref(res), ctypes.byref(o), ctypes.byref(extra))
+    if rc != 0:
+        raise RuntimeError("RuntimeError occurred")
+    nb = res.nbin
+    npairs = C.carray(res.npairs, nb, np.uint64)
+    rupp = C.carray(res.rupp, nb, np.float64)
+    ravg = C.carray(res.ravg, nb, np.float64)
+    xi_ = C.carray(res.xi, nb, np.float64)
+    wavg = C.carray(res.weightavg, nb, np.float64)
+    lib.free_results_xi(ctypes.byref(res))
+    out = np.zeros(max(nb - 1, 0), dtype=XI_DTYPE)
+    out["rmin"] = rupp[:-1]
+    out["rmax"] = rupp[1:]
+    out["ravg"] = ravg[1:]
+    out["xi"] = xi_[1:]
+    out["npairs"] = npairs[1:]
+    out["weightavg"] = wavg[1:]
+    return (out, o.c_api_time) if c_api_timer else out
+
+
+def DD(*args, **kwargs):
+    """3-D pair counts DD(r); see Corrfunc.theory.DD (Corrfunc/theory/DD.py:16)."""
+    return run_DD(C.library(), *args, **kwargs)
+
+
+def DDrppi(*args, **kwargs):
+    """Pair counts in (rp, pi); see Corrfunc.theory.DDrppi."""
+    return run_DDrppi(C.library(), *args, **kwargs)
+
+
+def DDsmu(*args, **kwargs):
+    """Pair counts in (s, mu); see Corrfunc.theory.DDsmu."""
+    return run_DDsmu(C.library(), *args, **kwargs)
+
+
+def wp(*args, **kwargs):
+    """Projected correlation function w_p(rp) in a periodic box; see Corrfunc.theory.wp."""
+    return run_wp(C.library(), *args, **kwargs)
+
+
+def xi(*args, **kwargs):
+    """3-D correlation function xi(r) in a periodic box; see Corrfunc.theory.xi."""
+    return run_xi(C.library(), *args, **kwargs)

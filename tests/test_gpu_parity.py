@@ -1,0 +1,248 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle, the committed golden
+vectors and, where built, the reference libraries.  npairs must be bit-exact; averages within
+1e-6 relative (double inputs) / 1e-4 (float inputs)."""
+import json
+import os
+import sys
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+import cases  # noqa: E402
+from test_oracle import GOLDEN, _oracle_call, brute_numpy  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+RTOL_AVG = 1e-6
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    import corrfunc_gb300
+    lib = corrfunc_gb300.library()
+    yield corrfunc_gb300
+    lib.cf_gpu_set_precision(0)
+
+
+@pytest.fixture(params=["fp32_refine", "fp64"])
+def precision(request, gpu):
+    gpu.set_precision(request.param)
+    yield request.param
+    gpu.set_precision("fp32_refine")
+
+
+def _gpu_call(case):
+    from corrfunc_gb300 import _capi as C
+    args, kw = cases.make_inputs(case)
+    return cases.runner(case["func"])(C.library(), *args, **kw)
+
+
+def _check(func, got, want, rtol):
+    assert np.array_equal(np.asarray(got["npairs"], dtype=np.uint64), np.asarray(want["npairs"], dtype=np.uint64)), \
+        "npairs differ:\n%s\n%s" % (list(got["npairs"]), list(want["npairs"]))
+    f = cases.AVG_FIELD[func]
+    np.testing.assert_allclose(np.asarray(got[f], float), np.asarray(want[f] if f in want.dtype.names else want["avg"],
+                                                                     float), rtol=rtol, atol=1e-12)
+    np.testing.assert_allclose(np.asarray(got["weightavg"], float), np.asarray(want["weightavg"], float), rtol=rtol,
+                               atol=1e-12)
+
+
+@pytest.mark.parametrize("case", cases.CASES, ids=[c["name"] for c in cases.CASES])
+def test_gpu_matches_golden(gpu, precision, case):
+    got = _gpu_call(case)
+    gold = GOLDEN["cases"][case["name"]]
+    assert [int(v) for v in got["npairs"]] == gold["npairs"]
+    rtol = 1e-4 if case["dtype"] == "f4" else RTOL_AVG
+    f = cases.AVG_FIELD[case["func"]]
+    np.testing.assert_allclose(got[f], gold["avg"], rtol=rtol, atol=1e-12)
+    np.testing.assert_allclose(got["weightavg"], gold["weightavg"], rtol=rtol, atol=1e-12)
+    if case["func"] == "wp":
+        np.testing.assert_allclose(got["wp"], gold["wp"], rtol=1e-9, atol=1e-9)
+    if case["func"] == "xi":
+        np.testing.assert_allclose(got["xi"], gold["xi"], rtol=1e-9, atol=1e-9)
+
+
+@pytest.mark.parametrize("case", cases.CASES, ids=[c["name"] for c in cases.CASES])
+def test_gpu_matches_oracle(gpu, orc, case):
+    got = _gpu_call(case)
+    want = _oracle_call(orc, case)
+    rtol = 1e-4 if case["dtype"] == "f4" else RTOL_AVG
+    _check(case["func"], got, want, rtol)
+
+
+def test_gpu_dd_doctest(gpu, precision):
+    from corrfunc_gb300 import theory
+    d = GOLDEN["dd_doctest"]
+    np.random.seed(d["seed"])
+    X = np.random.uniform(0, d["boxsize"], d["N"])
+    Y = np.random.uniform(0, d["boxsize"], d["N"])
+    Z = np.random.uniform(0, d["boxsize"], d["N"])
+    res = theory.DD(1, 4, d["edges"], X, Y, Z, weights1=np.ones_like(X), weight_type="pair_product",
+                    output_ravg=True, boxsize=d["boxsize"], periodic=True)
+    table = np.array(d["doctest_table"])
+    assert list(res["npairs"]) == [int(v) for v in table[:, 3]]
+    np.testing.assert_allclose(res["ravg"], table[:, 2], atol=5e-7)
+    np.testing.assert_allclose(res["ravg"], d["reference"]["avg"], rtol=RTOL_AVG)
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+@pytest.mark.parametrize("boxsize", [123.0, (51.0, 75.0, 123.0)], ids=["iso", "aniso"])
+@pytest.mark.parametrize("func", ["DD", "DDrppi", "DDsmu"])
+@pytest.mark.parametrize("autocorr", [0, 1])
+def test_gpu_brute_clouds(gpu, func, boxsize, periodic, autocorr):
+    """Port of Corrfunc/tests/test_theory.py:205-288 (two clouds, rmax up to 0.49 L)."""
+    from corrfunc_gb300 import theory
+    np.random.seed(1234)
+    npts, eps = 100, 0.2
+    box = np.array(boxsize)
+    bins = np.linspace(0.01, 0.49 * box.min(), 20) if periodic else np.linspace(0.01, 2 * box.max(), 20)
+    pimax = np.floor(0.49 * box.min())
+    pos = np.random.uniform(low=-eps, high=eps, size=(npts, 3)) * box
+    pos[npts // 2:] += box / 2.0
+    pos %= box
+    brute = brute_numpy(func, pos, box, periodic, bins, pimax=pimax, mu_max=0.5, nmu=10)
+    p = pos.T
+    kw = dict(periodic=periodic, boxsize=boxsize, X2=p[0], Y2=p[1], Z2=p[2])
+    if func == "DD":
+        got = theory.DD(autocorr, 1, bins, p[0], p[1], p[2], **kw)["npairs"]
+    elif func == "DDrppi":
+        got = theory.DDrppi(autocorr, 1, pimax, bins, p[0], p[1], p[2], **kw)["npairs"]
+    else:
+        got = theory.DDsmu(autocorr, 1, bins, 0.5, 10, p[0], p[1], p[2], **kw)["npairs"]
+    assert np.array_equal(np.asarray(got, dtype=np.int64), brute.astype(np.int64))
+
+
+@pytest.mark.parametrize("N", [1, 2])
+def test_gpu_narrow_extent(gpu, N):
+    from corrfunc_gb300 import theory
+    pos = np.array([[0.0, 0.0], [0.0, 0.0], [0.0, 0.5]]) if N == 2 else np.array([[0.1], [0.2], [0.3]])
+    res = theory.DD(1, 1, [0.2, 0.6, 1.0], pos[0], pos[1], pos[2], boxsize=(3.0, 3.0, 3.0), periodic=True)
+    assert list(res["npairs"]) == ([2, 0] if N == 2 else [0, 0])
+
+
+@pytest.mark.parametrize("autocorr", [0, 1])
+def test_gpu_duplicate_cellpairs(gpu, autocorr):
+    from corrfunc_gb300 import theory
+    L = 432.0
+    pos = np.array([[0.02, 0.98], [0.0, 0.0], [0.0, 0.0]]) * L
+    r = theory.DD(autocorr, 1, np.array([0.01, 0.4]) * L, pos[0], pos[1], pos[2], X2=pos[0], Y2=pos[1], Z2=pos[2],
+                  boxsize=L, periodic=True)
+    assert list(r["npairs"]) == [2]
+    pos = np.array([[0.0, 0.0], [0.0, 0.0], [0.0, 0.48]]) * L
+    r = theory.DD(autocorr, 1, np.array([0.2, 0.3, 0.49]) * L, pos[0], pos[1], pos[2], X2=pos[0], Y2=pos[1],
+                  Z2=pos[2], boxsize=L, periodic=True)
+    assert list(r["npairs"]) == [0, 2]
+
+
+def test_gpu_empty_inputs(gpu):
+    from corrfunc_gb300 import theory
+    e = np.zeros(0)
+    r = theory.DD(1, 1, [1.0, 2.0, 3.0], e, e, e, boxsize=10.0, periodic=True)
+    assert list(r["npairs"]) == [0, 0]
+    x = np.array([1.0, 2.0])
+    r = theory.DD(0, 1, [0.5, 2.0, 3.0], x, x, x, X2=e, Y2=e, Z2=e, boxsize=10.0, periodic=True)
+    assert list(r["npairs"]) == [0, 0]
+
+
+def test_gpu_pairs_on_bin_edges(gpu, orc, precision):
+    """Pairs placed at separations equal to (or one ulp either side of) the bin edges: every such
+    pair is inside the FP32 ambiguity band and must be decided by the FP64 re-evaluation."""
+    from corrfunc_gb300 import theory
+    edges = np.array([0.5, 1.0, 2.0, 3.0, 5.0])
+    xs, ys, zs = [], [], []
+    base = 10.0
+    k = 0
+    for e in edges:
+        for d in (np.nextafter(e, 0), e, np.nextafter(e, 100)):
+            x0 = base + 7.0 * k
+            xs += [x0, x0 + d]
+            ys += [5.0, 5.0]
+            zs += [5.0, 5.0]
+            k += 1
+    # a 3-4-5 triangle lands exactly on r^2 = 25 in exact arithmetic
+    xs += [200.0, 203.0]
+    ys += [5.0, 9.0]
+    zs += [5.0, 5.0]
+    x, y, z = (np.array(a) for a in (xs, ys, zs))
+    got = theory.DD(1, 1, edges, x, y, z, periodic=False, output_ravg=True)
+    want = orc.DD(1, edges, x, y, z, periodic=False, output_ravg=True)
+    assert np.array_equal(got["npairs"], want["npairs"])
+    s = gpu.last_stats()
+    assert s["pairs_refined"] > 0 or precision == "fp64"
+
+
+@pytest.mark.parametrize("func", ["DD", "DDrppi", "DDsmu", "DDtheta"])
+def test_gpu_fp32_refine_equals_fp64(gpu, func):
+    """The FP32+FP64-refinement form and the plain FP64 form give identical counts."""
+    from corrfunc_gb300 import catalogs as cat
+    from corrfunc_gb300 import mocks, theory
+    outs = []
+    for prec in ("fp32_refine", "fp64"):
+        gpu.set_precision(prec)
+        if func == "DDtheta":
+            ra, dec = cat.sky_cap(20000, 5)
+            r = mocks.DDtheta_mocks(1, 1, cat.log_bins(0.01, 5.0, 12), ra, dec, output_thetaavg=True)
+            outs.append((r["npairs"].copy(), r["thetaavg"].copy()))
+        else:
+            x, y, z = cat.clustered_box(30000, 250.0, 9, sigma=2.0, mean_occupancy=60)
+            bins = cat.log_bins(0.1, 20.0, 14)
+            if func == "DD":
+                r = theory.DD(1, 1, bins, x, y, z, boxsize=250.0, output_ravg=True)
+                f = "ravg"
+            elif func == "DDrppi":
+                r = theory.DDrppi(1, 1, 20.0, bins, x, y, z, boxsize=250.0, output_rpavg=True)
+                f = "rpavg"
+            else:
+                r = theory.DDsmu(1, 1, bins, 1.0, 10, x, y, z, boxsize=250.0, output_savg=True)
+                f = "savg"
+            outs.append((r["npairs"].copy(), r[f].copy()))
+    gpu.set_precision("fp32_refine")
+    assert np.array_equal(outs[0][0], outs[1][0])
+    np.testing.assert_allclose(outs[0][1], outs[1][1], rtol=RTOL_AVG, atol=1e-12)
+
+
+@pytest.mark.parametrize("func", ["DD", "DDrppi", "DDsmu", "wp", "xi", "DDtheta"])
+def test_gpu_matches_reference_library_larger(gpu, reflibs, func):
+    """Sizes the brute-force oracle would take long on, against the reference library itself."""
+    from corrfunc_gb300 import _capi as C
+    from corrfunc_gb300 import catalogs as cat
+    from corrfunc_gb300 import mocks, theory
+    lib = C.library()
+    n, L = 200000, 300.0
+    x, y, z = cat.clustered_box(n, L, 3, sigma=2.0, mean_occupancy=80)
+    w = cat.weights(n, 4)
+    bins = cat.log_bins(0.1, 25.0, 16)
+    kw = dict(weights1=w, weight_type="pair_product", boxsize=L, isa="fallback")
+    if func == "DD":
+        a = theory.run_DD(lib, 1, 4, bins, x, y, z, output_ravg=True, **kw)
+        b = theory.run_DD(reflibs["DD"], 1, 16, bins, x, y, z, output_ravg=True, **kw)
+        f = "ravg"
+    elif func == "DDrppi":
+        a = theory.run_DDrppi(lib, 1, 4, 30.0, bins, x, y, z, output_rpavg=True, **kw)
+        b = theory.run_DDrppi(reflibs["DDrppi"], 1, 16, 30.0, bins, x, y, z, output_rpavg=True, **kw)
+        f = "rpavg"
+    elif func == "DDsmu":
+        a = theory.run_DDsmu(lib, 1, 4, bins, 1.0, 10, x, y, z, output_savg=True, **kw)
+        b = theory.run_DDsmu(reflibs["DDsmu"], 1, 16, bins, 1.0, 10, x, y, z, output_savg=True, **kw)
+        f = "savg"
+    elif func == "wp":
+        a = theory.run_wp(lib, L, 30.0, 4, bins, x, y, z, weights=w, weight_type="pair_product",
+                          output_rpavg=True, isa="fallback")
+        b = theory.run_wp(reflibs["wp"], L, 30.0, 16, bins, x, y, z, weights=w, weight_type="pair_product",
+                          output_rpavg=True, isa="fallback")
+        f = "rpavg"
+    elif func == "xi":
+        a = theory.run_xi(lib, L, 4, bins, x, y, z, output_ravg=True, isa="fallback")
+        b = theory.run_xi(reflibs["xi"], L, 16, bins, x, y, z, output_ravg=True, isa="fallback")
+        f = "ravg"
+    else:
+        ra, dec = cat.sky_cap(100000, 8)
+        tb = cat.log_bins(0.01, 5.0, 12)
+        a = mocks.run_DDtheta_mocks(lib, 1, 4, tb, ra.copy(), dec.copy(), output_thetaavg=True, isa="fallback")
+        b = mocks.run_DDtheta_mocks(reflibs["DDtheta"], 1, 16, tb, ra.copy(), dec.copy(), output_thetaavg=True,
+                                    isa="fallback")
+        f = "thetaavg"
+    assert np.array_equal(a["npairs"], b["npairs"])
+    np.testing.assert_allclose(a[f], b[f], rtol=RTOL_AVG, atol=1e-12)
