@@ -1,0 +1,412 @@
+#!/usr/bin/env python3
+"""Benchmark: pair evaluations/s of the GB300 pair counter on the reference's headline workload.
+
+Workload (one step = one full countpairs() call: device gridlink, device worklist, pair kernel,
+histogram read-back): DD(r) cross-correlation with pair_product weights, N1 = N2 = 2,000,000
+clustered points (80% in Gaussian blobs of sigma 2, Poisson occupancy 80; 20% uniform) in a
+periodic L = 1000 box, 25 log bins 0.1-50, float64 positions, FP32 classification + FP64 edge
+re-evaluation.  Seeded synthetic inputs stand in for a survey catalogue.
+
+Units: pair evaluations = candidate pairs of the *reference's* lattice (computed by
+cf_reference_candidate_pairs, a restatement of the reference's gridlink + cell-pair list), so
+the number does not depend on how the GPU tiles the work.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  With --gpus N > 1 (launched by torchrun) every rank runs an independent
+replica of the workload on its own GPU ("replicas only": the path needs no collective).
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "pair evaluations/sec (reference-lattice candidate pairs), DD cross-correlation"
+UNIT = "pairs/s"
+WORKLOAD = dict(workload="theory DD cross-correlation with pair_product weights, N1=N2=2,000,000 clustered "
+                         "points, periodic L=1000, 25 log bins 0.1-50, float64",
+                n1=2_000_000, n2=2_000_000, boxsize=1000.0, nbins=25, rmin=0.1, rmax=50.0, seeds=[1, 2],
+                weights="U[0.5,1.5]", precision="fp32_refine")
+FLOP_PER_PAIR = 8  # 3 FADD + 1 FMUL + 2 FFMA per 3-D separation
+# dram__bytes_read.sum + dram__bytes_write.sum of one pair-kernel launch on this workload,
+# from the ncu capture summarised in profiles/ (None until captured)
+PAIR_KERNEL_TRAFFIC_BYTES = None
+
+
+def _rank_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def make_workload(dtype=np.float64):
+    from corrfunc_gb300 import catalogs as cat
+    L = WORKLOAD["boxsize"]
+    x1, y1, z1 = cat.clustered_box(WORKLOAD["n1"], L, WORKLOAD["seeds"][0], dtype=dtype)
+    x2, y2, z2 = cat.clustered_box(WORKLOAD["n2"], L, WORKLOAD["seeds"][1], dtype=dtype)
+    w1 = cat.weights(WORKLOAD["n1"], 101, dtype=dtype)
+    w2 = cat.weights(WORKLOAD["n2"], 102, dtype=dtype)
+    bins = cat.log_bins(WORKLOAD["rmin"], WORKLOAD["rmax"], WORKLOAD["nbins"])
+    return (x1, y1, z1, w1), (x2, y2, z2, w2), bins
+
+
+def options_for(C, L, dtype):
+    o = C.get_config_options()
+    o.verbose = 0
+    o.periodic = 1
+    o.boxsize_x = o.boxsize_y = o.boxsize_z = L
+    o.float_type = np.dtype(dtype).itemsize
+    o.instruction_set = 0
+    return o
+
+
+def extra_for(C, w1, w2):
+    e = C.get_extra_options(C.WEIGHT_PAIR_PRODUCT)
+    e.weights0.weights[0] = w1
+    e.weights1.weights[0] = w2
+    e.weights0.num_weights = e.weights1.num_weights = 1
+    return e
+
+
+def reference_work(lib, C, set1, set2, binfile, dtype):
+    lib.cf_reference_candidate_pairs.argtypes = ([ctypes.c_int64] + [ctypes.c_void_p] * 3 + [ctypes.c_int64]
+                                                 + [ctypes.c_void_p] * 3
+                                                 + [ctypes.c_int, ctypes.c_char_p, ctypes.POINTER(C.ConfigOptions),
+                                                    ctypes.POINTER(ctypes.c_uint64)])
+    lib.cf_reference_candidate_pairs.restype = ctypes.c_int
+    o = options_for(C, WORKLOAD["boxsize"], dtype)
+    out = ctypes.c_uint64()
+    rc = lib.cf_reference_candidate_pairs(len(set1[0]), *(C.ptr(a) for a in set1[:3]), len(set2[0]),
+                                          *(C.ptr(a) for a in set2[:3]), 0, binfile.encode(), ctypes.byref(o),
+                                          ctypes.byref(out))
+    if rc != 0:
+        raise RuntimeError("cf_reference_candidate_pairs failed")
+    return int(out.value)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ["clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.hw_slowdown",
+              "clocks_event_reasons.hw_thermal_slowdown", "clocks_event_reasons.sw_thermal_slowdown",
+              "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + ",".join(self.FIELDS),
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def flush_l2(torch, dev):
+    # write a buffer larger than the 129 MB L2 between timed steps
+    if not hasattr(flush_l2, "buf"):
+        flush_l2.buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    flush_l2.buf.fill_(1.0)
+    torch.cuda.synchronize(dev)
+
+
+def cpu_reference_run(set1, set2, bins, nthreads, dtype, frac=1.0):
+    """The reference's own countpairs() (oracle/_ref, all host threads) on a subsample keeping a
+    fraction `frac` of each catalogue; returns (seconds, reference-lattice candidates)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from corrfunc_gb300 import _capi as C
+    from corrfunc_gb300 import theory
+    so = os.path.join(ROOT, "oracle", "_ref", "libcf_ref_DD.so")
+    if not os.path.exists(so):
+        return None
+    ref = C.bind(so)
+    n1 = int(len(set1[0]) * frac)
+    n2 = int(len(set2[0]) * frac)
+    s1 = tuple(np.ascontiguousarray(a[:n1]) for a in set1)
+    s2 = tuple(np.ascontiguousarray(a[:n2]) for a in set2)
+    t0 = time.perf_counter()
+    theory.run_DD(ref, 0, nthreads, bins, s1[0], s1[1], s1[2], weights1=s1[3], X2=s2[0], Y2=s2[1], Z2=s2[2],
+                  weights2=s2[3], weight_type="pair_product", periodic=True, boxsize=WORKLOAD["boxsize"],
+                  isa="fastest")
+    dt = time.perf_counter() - t0
+    gpu_lib = C.bind(C.LIB_PATH, gpu=True)
+    with C.BinFile(bins) as bf:
+        work = reference_work(gpu_lib, C, s1, s2, bf, dtype)
+    return dt, work, n1, n2
+
+
+def run_reference_arm(args):
+    rank, world, _ = _rank_env()
+    if rank != 0:
+        return
+    set1, set2, bins = make_workload()
+    nthreads = os.cpu_count() or 1
+    # size the sample so that one step stays within ~20 s of CPU time
+    frac = 1.0
+    probe = cpu_reference_run(set1, set2, bins, nthreads, np.float64, frac=0.1)
+    if probe is None:
+        print(json.dumps({"impl": "reference", "unavailable": "reference pair counters were not built in oracle/_ref"}))
+        return
+    est_full = probe[0] * 100.0
+    if est_full > 20.0:
+        frac = max(0.05, (20.0 / est_full) ** 0.5)
+    times, works = [], []
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        cpu_reference_run(set1, set2, bins, nthreads, np.float64, frac=frac)
+    for _ in range(args.steps):
+        dt, work, n1, n2 = cpu_reference_run(set1, set2, bins, nthreads, np.float64, frac=frac)
+        times.append(dt)
+        works.append(work)
+    value = sum(works) / sum(times)
+    sample = "first %d and %d points of the two catalogues (fraction %.3f of each)" % (n1, n2, frac)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded clustered catalogues)",
+            "config": dict(WORKLOAD, sample=sample), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "reference",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp32_refine", choices=["fp32_refine", "fp64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--extras", action="store_true", help="also time the FP64 form and the north-star workload")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference_arm(args)
+
+    rank, world, local = _rank_env()
+    import torch
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+
+    import corrfunc_gb300
+    from corrfunc_gb300 import _capi as C
+    lib = corrfunc_gb300.library()
+    lib.cf_gpu_countpairs_device.argtypes = lib.countpairs.argtypes
+    lib.cf_gpu_countpairs_device.restype = ctypes.c_int
+    lib.cf_gpu_fp32_peak_tflops.argtypes = [ctypes.POINTER(ctypes.c_double)]
+    corrfunc_gb300.set_precision(args.precision)
+
+    set1, set2, bins = make_workload()
+    binf = C.BinFile(bins)
+    binfile = binf.__enter__()
+    work = reference_work(lib, C, set1, set2, binfile, np.float64)
+
+    # inputs resident in HBM
+    d1 = [torch.from_numpy(a).to(dev) for a in set1]
+    d2 = [torch.from_numpy(a).to(dev) for a in set2]
+    torch.cuda.synchronize(dev)
+    o = options_for(C, WORKLOAD["boxsize"], np.float64)
+
+    def step_device():
+        e = extra_for(C, d1[3].data_ptr(), d2[3].data_ptr())
+        res = C.ResultsDD()
+        rc = lib.cf_gpu_countpairs_device(len(set1[0]), *(ctypes.c_void_p(t.data_ptr()) for t in d1[:3]),
+                                          len(set2[0]), *(ctypes.c_void_p(t.data_ptr()) for t in d2[:3]), 1, 0,
+                                          binfile.encode(), ctypes.byref(res), ctypes.byref(o), ctypes.byref(e))
+        if rc != 0:
+            raise RuntimeError("countpairs on device inputs failed")
+        npairs = np.ctypeslib.as_array(res.npairs, shape=(res.nbin,)).copy()
+        lib.free_results(ctypes.byref(res))
+        return npairs, corrfunc_gb300.last_stats()
+
+    # host arrays in pinned memory for the end-to-end leg
+    h1 = [torch.from_numpy(a).pin_memory() for a in set1]
+    h2 = [torch.from_numpy(a).pin_memory() for a in set2]
+    hn1 = [t.numpy() for t in h1]
+    hn2 = [t.numpy() for t in h2]
+
+    def step_host():
+        e = extra_for(C, hn1[3].ctypes.data, hn2[3].ctypes.data)
+        res = C.ResultsDD()
+        rc = lib.countpairs(len(hn1[0]), *(C.ptr(a) for a in hn1[:3]), len(hn2[0]), *(C.ptr(a) for a in hn2[:3]),
+                            1, 0, binfile.encode(), ctypes.byref(res), ctypes.byref(o), ctypes.byref(e))
+        if rc != 0:
+            raise RuntimeError("countpairs failed")
+        npairs = np.ctypeslib.as_array(res.npairs, shape=(res.nbin,)).copy()
+        lib.free_results(ctypes.byref(res))
+        return npairs, corrfunc_gb300.last_stats()
+
+    for _ in range(max(args.warmup, 3)):
+        ref_np, _ = step_device()
+        flush_l2(torch, dev)
+
+    gpu_ms, pair_ms, grid_ms, launches, evaluated, refined, wall = [], [], [], 0, 0, 0, []
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            npairs, st = step_device()
+            wall.append(time.perf_counter() - t0)
+            if not np.array_equal(npairs, ref_np):
+                raise RuntimeError("non-deterministic pair counts between steps")
+            gpu_ms.append(st["total_gpu_ms"])
+            pair_ms.append(st["pair_kernel_ms"])
+            grid_ms.append(st["gridlink_ms"])
+            launches += st["kernel_launches"]
+            evaluated += st["pairs_evaluated"]
+            refined += st["pairs_refined"]
+            flush_l2(torch, dev)
+    torch.cuda.synchronize(dev)
+    total_s = sum(gpu_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([total_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.barrier()
+        total_s = float(t.item())
+    value = world * work * args.steps / total_s
+
+    # end-to-end through the public C API with host (pinned) buffers
+    for _ in range(2):
+        step_host()
+    e2e_t = []
+    for _ in range(args.steps):
+        flush_l2(torch, dev)
+        t0 = time.perf_counter()
+        npairs_h, _st = step_host()
+        e2e_t.append(time.perf_counter() - t0)
+        if not np.array_equal(npairs_h, ref_np):
+            raise RuntimeError("host-buffer path disagrees with the device-buffer path")
+    e2e_value = world * work * args.steps / sum(e2e_t)
+    h2d = sum(a.nbytes for a in hn1) + sum(a.nbytes for a in hn2)
+    d2h = (WORKLOAD["nbins"] + 1) * (8 + 8 + 8 + 8)
+
+    peak = ctypes.c_double()
+    lib.cf_gpu_fp32_peak_tflops(ctypes.byref(peak))
+    pair_s = sum(pair_ms) / 1e3 / args.steps
+    achieved = work * FLOP_PER_PAIR / pair_s / 1e12
+    traffic = PAIR_KERNEL_TRAFFIC_BYTES
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": sum(gpu_ms) / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64-refine" if args.precision == "fp32_refine" else "f64",
+            "data": "synthetic (seeded clustered catalogues, numpy PCG64)",
+            "config": dict(WORKLOAD, precision=args.precision, l2="flushed between steps (256 MB write)",
+                           reference_lattice_candidates=work),
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
+                         "frac": achieved / peak.value if peak.value else None, "traffic": traffic,
+                         "kernel": "k_pairs_f32<MODE_R3,false,true>" if args.precision == "fp32_refine"
+                         else "k_pairs_f64<MODE_R3,false,true>",
+                         "peak_source": "measured: FP32 FMA calibration kernel (cf_gpu_fp32_peak_tflops) in this run",
+                         "flop_per_pair": FLOP_PER_PAIR},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": 1e3 * sum(e2e_t) / args.steps},
+            "gpu_launches": launches,
+            "kernel_ms": {"pair_kernel": sum(pair_ms) / args.steps, "gridlink_and_worklist": sum(grid_ms) / args.steps,
+                          "step_total": sum(gpu_ms) / args.steps, "host_wall": 1e3 * sum(wall) / args.steps},
+            "pairs": {"reference_lattice_candidates": work, "gpu_evaluated": evaluated // args.steps,
+                      "fp64_refined": refined // args.steps, "counted": int(np.sum(ref_np))},
+            "clocks": clocks.summary()}
+
+    if args.extras and rank == 0:
+        line["extras"] = extras(lib, C, corrfunc_gb300, torch, dev, args)
+        corrfunc_gb300.set_precision(args.precision)
+
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        r = cpu_reference_run(set1, set2, bins, os.cpu_count() or 1, np.float64,
+                              frac=float(os.environ.get("CF_BENCH_CPU_FRAC", "0.25")))
+        if r is None:
+            line["cpu_baseline"] = None
+        else:
+            dt, cw, n1, n2 = r
+            line["cpu_baseline"] = {"value": cw / dt, "unit": UNIT, "cores": os.cpu_count(), "kind": "reference",
+                                    "sample": "first %d and %d points of the two catalogues, one run" % (n1, n2),
+                                    "seconds": dt}
+    binf.__exit__(None, None, None)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def extras(lib, C, cf, torch, dev, args):
+    """FP64 form on the same workload, and the 1M-point periodic DD auto-correlation target."""
+    out = {}
+    from corrfunc_gb300 import catalogs as cat
+    from corrfunc_gb300 import theory
+    set1, set2, bins = make_workload()
+    for prec in ("fp64", "fp32_refine"):
+        cf.set_precision(prec)
+        theory.DD(0, 1, bins, *set1[:3], weights1=set1[3], X2=set2[0], Y2=set2[1], Z2=set2[2], weights2=set2[3],
+                  weight_type="pair_product", boxsize=WORKLOAD["boxsize"], isa="fallback")
+        st = cf.last_stats()
+        out["cfg2_" + prec + "_pair_kernel_ms"] = st["pair_kernel_ms"]
+    for L in (420.0, 1000.0):
+        x, y, z = cat.uniform_box(1_000_000, L, 0)
+        b = cat.log_bins(0.1, 25.0, 20)
+        with C.BinFile(b) as bf:
+            work = reference_work(lib, C, (x, y, z), (x, y, z), bf, np.float64) if False else None
+        for prec in ("fp64", "fp32_refine"):
+            cf.set_precision(prec)
+            ms = []
+            for _ in range(3):
+                r = theory.DD(1, 1, b, x, y, z, boxsize=L, isa="fallback")
+                ms.append(cf.last_stats())
+            out["northstar_L%d_%s" % (int(L), prec)] = {"pair_kernel_ms": min(s["pair_kernel_ms"] for s in ms),
+                                                        "total_gpu_ms": min(s["total_gpu_ms"] for s in ms),
+                                                        "npairs_sum": int(np.sum(r["npairs"]))}
+    return out
+
+
+if __name__ == "__main__":
+    main()

@@ -200,15 +200,29 @@ def get_extra_options(weight_method=WEIGHT_NONE):
     return e
 
 
+def host_highest_isa():
+    """The highest instruction set of this host, as the reference's CPython binding resolves
+    isa = -1 before calling the C library (theory/python_bindings/_countpairs.c:1239-1241)."""
+    try:
+        flags = open("/proc/cpuinfo").read()
+    except OSError:
+        return ISA_ENUMS["FALLBACK"]
+    for name, flag in (("AVX512F", " avx512f"), ("AVX2", " avx2"), ("AVX", " avx "), ("SSE42", " sse4_2")):
+        if flag in flags:
+            return ISA_ENUMS[name]
+    return ISA_ENUMS["FALLBACK"]
+
+
 def translate_isa(isa):
-    """isa string -> enum (Corrfunc/utils.py:464-518)."""
+    """isa string -> enum (Corrfunc/utils.py:464-518); "fastest" resolves to the host's highest."""
     if not isinstance(isa, str):
         raise TypeError("isa must be a string")
     up = isa.upper()
     if up not in VALID_ISA:
         raise ValueError("Desired instruction set = {0} is not in the list of valid instruction sets = {1}"
                          .format(isa, VALID_ISA))
-    return ISA_ENUMS[up]
+    v = ISA_ENUMS[up]
+    return host_highest_isa() if v == -1 else v
 
 
 def set_refine(o, refine):

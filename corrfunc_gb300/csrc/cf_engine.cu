@@ -718,6 +718,24 @@ __global__ void __launch_bounds__(256) k_pairs_f64(PairArgs A, SmemLayout SL)
 }
 
 // ------------------------------------------------------------------------------------
+// FP32 FMA-pipe calibration: 8 independent dependency chains per thread keep every FMA
+// lane busy; 2 FLOP per fmaf.  Used only as the measured denominator of the pair kernels'
+// FP32 roofline fraction.
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_fma_peak(float *out, int iters, float a, float b)
+{
+    float v[8];
+    for (int k = 0; k < 8; k++) v[k] = threadIdx.x * 1e-3f + k;
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) v[k] = fmaf(v[k], a, b);
+    }
+    float s = 0.f;
+    for (int k = 0; k < 8; k++) s += v[k];
+    if (s == 12345.678f) out[blockIdx.x] = s;  // keeps the chains live
+}
+
+// ------------------------------------------------------------------------------------
 // host side: buffers, launch helpers
 // ------------------------------------------------------------------------------------
 struct DevBuf {
@@ -739,7 +757,8 @@ static int ensure(DevBuf &b, size_t bytes)
 }
 
 struct SetBufs {
-    DevBuf raw[4];  // x, y, z, w as given (float or double)
+    DevBuf raw[4];  // device copies of x, y, z, w as given (float or double)
+    const void *in[4];  // arrays the lattice is built from: raw[] or caller-owned device arrays
     DevBuf cellid_u, count, fill, cell_start;
     DevBuf hi, lo, dbl, refcell, orig, cellid;
 };
@@ -754,6 +773,7 @@ struct Engine {
     DevBuf mm, oob, scan_tmp[4], chunk_cnt, chunk_off, chunk_begin, chunk_count, ntask, task_off, tasks;
     DevBuf hist_cnt, hist_avg, hist_w, stats, counter, edges, guards;
     int precision = CF_PRECISION_FP32_REFINE;
+    int launches = 0;  // kernels launched by the current call
     cf_engine_stats last;
 };
 
@@ -799,15 +819,19 @@ static int scan_u32(const uint32_t *in, uint32_t *out, uint32_t n, int level)
     uint32_t *bs = (uint32_t *)g_eng.scan_tmp[level].p;
     uint32_t *bs_scan = bs + nblk;  // nblk+1 entries
     k_scan_tile<<<nblk, 1024, 0, st>>>(in, out, n, bs);
+    g_eng.launches++;
     CF_CUDA(cudaGetLastError());
     if (nblk == 1) {
         k_write_total_single<<<1, 1, 0, st>>>(out, n, bs);
+        g_eng.launches++;
         CF_CUDA(cudaGetLastError());
         return EXIT_SUCCESS;
     }
     if (scan_u32(bs, bs_scan, nblk, level + 1) != EXIT_SUCCESS) return EXIT_FAILURE;
     k_scan_add<<<nblk, 1024, 0, st>>>(out, n, bs_scan);
+    g_eng.launches++;
     k_set_total<<<1, 1, 0, st>>>(out, n, bs_scan, nblk);
+    g_eng.launches++;
     CF_CUDA(cudaGetLastError());
     return EXIT_SUCCESS;
 }
@@ -843,20 +867,26 @@ static float f_up(double v)
 
 template <typename T>
 static int upload_and_minmax(int s, int64_t n, const void *x, const void *y, const void *z, const void *w,
-                             unsigned long long *mm_dev)
+                             bool on_device, unsigned long long *mm_dev)
 {
     SetBufs &B = g_eng.set[s];
     const size_t bytes = sizeof(T) * (size_t)n;
     const void *src[4] = {x, y, z, w};
     for (int k = 0; k < 4; k++) {
+        B.in[k] = nullptr;
         if (k == 3 && !w) continue;
+        if (on_device) {
+            B.in[k] = src[k];
+            continue;
+        }
         if (ensure(B.raw[k], bytes) != EXIT_SUCCESS) return EXIT_FAILURE;
         CF_CUDA(cudaMemcpyAsync(B.raw[k].p, src[k], bytes, cudaMemcpyHostToDevice, g_eng.stream));
+        B.in[k] = B.raw[k].p;
     }
-    k_minmax<T><<<grid_for(n, 256), 256, 0, g_eng.stream>>>((const T *)B.raw[0].p, (const T *)B.raw[1].p,
-                                                            (const T *)B.raw[2].p, w ? (const T *)B.raw[3].p : nullptr,
-                                                            n, mm_dev);
+    k_minmax<T><<<grid_for(n, 256), 256, 0, g_eng.stream>>>((const T *)B.in[0], (const T *)B.in[1],
+                                                            (const T *)B.in[2], (const T *)B.in[3], n, mm_dev);
     CF_CUDA(cudaGetLastError());
+    g_eng.launches++;
     return EXIT_SUCCESS;
 }
 
@@ -872,10 +902,11 @@ static int build_lattice(int s, int64_t n, bool has_w, const Geom &g, uint32_t n
         return EXIT_FAILURE;
     CF_CUDA(cudaMemsetAsync(B.count.p, 0, sizeof(uint32_t) * ncells, st));
     CF_CUDA(cudaMemsetAsync(B.fill.p, 0, sizeof(uint32_t) * ncells, st));
-    const T *x = (const T *)B.raw[0].p, *y = (const T *)B.raw[1].p, *z = (const T *)B.raw[2].p;
-    const T *w = has_w ? (const T *)B.raw[3].p : nullptr;
+    const T *x = (const T *)B.in[0], *y = (const T *)B.in[1], *z = (const T *)B.in[2];
+    const T *w = has_w ? (const T *)B.in[3] : nullptr;
     const int grid = grid_for(n, 256);
     k_assign<T><<<grid, 256, 0, st>>>(x, y, z, n, g, (uint32_t *)B.cellid_u.p, (uint32_t *)B.count.p, oob);
+    g_eng.launches++;
     CF_CUDA(cudaGetLastError());
     if (scan_u32((const uint32_t *)B.count.p, (uint32_t *)B.cell_start.p, ncells, 0) != EXIT_SUCCESS) return EXIT_FAILURE;
     Lattice L;
@@ -888,6 +919,7 @@ static int build_lattice(int s, int64_t n, bool has_w, const Geom &g, uint32_t n
     L.cell_start = (uint32_t *)B.cell_start.p;
     k_scatter<T><<<grid, 256, 0, st>>>(x, y, z, w, n, g, (const uint32_t *)B.cellid_u.p,
                                        (const uint32_t *)B.cell_start.p, (uint32_t *)B.fill.p, L);
+    g_eng.launches++;
     CF_CUDA(cudaGetLastError());
     return EXIT_SUCCESS;
 }
@@ -911,12 +943,14 @@ static int launch_pairs_t(const PairArgs &A, bool f64, int *launched)
         CF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, SL.total));
         if (per_sm < 1) per_sm = 1;
         kern<<<g_eng.num_sms * per_sm, threads, SL.total, g_eng.stream>>>(A, SL);
+        g_eng.launches++;
     } else {
         auto kern = k_pairs_f32<MODE, AVG, W>;
         CF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SL.total));
         CF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, SL.total));
         if (per_sm < 1) per_sm = 1;
         kern<<<g_eng.num_sms * per_sm, threads, SL.total, g_eng.stream>>>(A, SL);
+        g_eng.launches++;
     }
     CF_CUDA(cudaGetLastError());
     (*launched)++;
@@ -957,6 +991,7 @@ static int run_locked(cf_job *J, cf_hist *H)
     if (engine_init() != EXIT_SUCCESS) return EXIT_FAILURE;
     cudaStream_t st = g_eng.stream;
     memset(&g_eng.last, 0, sizeof(g_eng.last));
+    g_eng.launches = 0;
     const int mode = J->mode;
     const bool two_d = (mode == MODE_RPPI || mode == MODE_SMU);
     const int nbins = two_d ? J->nedges * (J->npibin + 1) : J->nedges;
@@ -985,8 +1020,8 @@ static int run_locked(cf_job *J, cf_hist *H)
         const void *x = s ? J->x2 : J->x1, *y = s ? J->y2 : J->y1, *z = s ? J->z2 : J->z1;
         const void *w = need_w ? (s ? J->w2 : J->w1) : nullptr;
         if (!x || !y || !z || (need_w && !w)) CF_FAIL("NULL input array");
-        int rc = isf ? upload_and_minmax<float>(s, n, x, y, z, w, mm + 8 * s)
-                     : upload_and_minmax<double>(s, n, x, y, z, w, mm + 8 * s);
+        int rc = isf ? upload_and_minmax<float>(s, n, x, y, z, w, J->inputs_on_device != 0, mm + 8 * s)
+                     : upload_and_minmax<double>(s, n, x, y, z, w, J->inputs_on_device != 0, mm + 8 * s);
         if (rc != EXIT_SUCCESS) return EXIT_FAILURE;
     }
     const bool dev_float = isf;
@@ -1086,6 +1121,7 @@ static int run_locked(cf_job *J, cf_hist *H)
         return EXIT_FAILURE;
     k_col_chunks<<<(ncols + 255) / 256, 256, 0, st>>>((const uint32_t *)S1.cell_start.p, (int)ncols, g.n[2],
                                                       (uint32_t *)g_eng.chunk_cnt.p);
+    g_eng.launches++;
     CF_CUDA(cudaGetLastError());
     if (scan_u32((const uint32_t *)g_eng.chunk_cnt.p, (uint32_t *)g_eng.chunk_off.p, ncols, 0) != EXIT_SUCCESS)
         return EXIT_FAILURE;
@@ -1095,6 +1131,7 @@ static int run_locked(cf_job *J, cf_hist *H)
     k_chunk_emit<<<(ncols + 255) / 256, 256, 0, st>>>((const uint32_t *)S1.cell_start.p, (int)ncols, g.n[2],
                                                       (const uint32_t *)g_eng.chunk_off.p,
                                                       (uint32_t *)g_eng.chunk_begin.p, (uint32_t *)g_eng.chunk_count.p);
+    g_eng.launches++;
     CF_CUDA(cudaGetLastError());
     uint32_t nchunks = 0;
     unsigned long long oob_h = 0;
@@ -1139,6 +1176,7 @@ static int run_locked(cf_job *J, cf_hist *H)
                                                             (const uint32_t *)g_eng.chunk_count.p,
                                                             (const uint32_t *)S1.cellid.p,
                                                             (const uint32_t *)S2.cell_start.p, (uint32_t *)g_eng.ntask.p);
+        g_eng.launches++;
         CF_CUDA(cudaGetLastError());
     }
     if (scan_u32((const uint32_t *)g_eng.ntask.p, (uint32_t *)g_eng.task_off.p, nchunks, 0) != EXIT_SUCCESS)
@@ -1154,6 +1192,7 @@ static int run_locked(cf_job *J, cf_hist *H)
                                                            (const uint32_t *)g_eng.chunk_count.p,
                                                            (const uint32_t *)S1.cellid.p, (const uint32_t *)S2.cell_start.p,
                                                            (const uint32_t *)g_eng.task_off.p, (Task *)g_eng.tasks.p);
+        g_eng.launches++;
         CF_CUDA(cudaGetLastError());
     }
     g_eng.last.tasks = ntasks;
@@ -1289,7 +1328,8 @@ static int run_locked(cf_job *J, cf_hist *H)
     g_eng.last.total_gpu_ms = ms_total;
     g_eng.last.pairs_evaluated = stats_h[0];
     g_eng.last.pairs_refined = stats_h[1];
-    g_eng.last.kernel_launches = launched;
+    g_eng.last.kernel_launches = g_eng.launches;
+    (void)launched;
     return EXIT_SUCCESS;
 }
 
@@ -1313,6 +1353,38 @@ extern "C" int cf_engine_set_precision(int mode)
 }
 
 extern "C" int cf_engine_get_precision(void) { return g_eng.precision; }
+
+extern "C" int cf_engine_copy_to_host(void *dst, const void *src, size_t bytes)
+{
+    CF_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+    return EXIT_SUCCESS;
+}
+
+extern "C" int cf_engine_fp32_peak(double *tflops)
+{
+    pthread_mutex_lock(&g_lock);
+    int rc = engine_init();
+    if (rc == EXIT_SUCCESS) {
+        rc = [&]() -> int {
+            DevBuf tmp;
+            if (ensure(tmp, 4096 * sizeof(float)) != EXIT_SUCCESS) return EXIT_FAILURE;
+            const int blocks = g_eng.num_sms * 8, threads = 256, iters = 1 << 16;
+            const float a = 0.999999f, b = 1e-7f;
+            k_fma_peak<<<blocks, threads, 0, g_eng.stream>>>((float *)tmp.p, 256, a, b);  // warm-up
+            CF_CUDA(cudaEventRecord(g_eng.ev[0], g_eng.stream));
+            k_fma_peak<<<blocks, threads, 0, g_eng.stream>>>((float *)tmp.p, iters, a, b);
+            CF_CUDA(cudaEventRecord(g_eng.ev[1], g_eng.stream));
+            CF_CUDA(cudaEventSynchronize(g_eng.ev[1]));
+            float ms = 0.f;
+            CF_CUDA(cudaEventElapsedTime(&ms, g_eng.ev[0], g_eng.ev[1]));
+            cudaFree(tmp.p);
+            *tflops = (double)blocks * threads * iters * 8.0 * 2.0 / (ms * 1e-3) / 1e12;
+            return EXIT_SUCCESS;
+        }();
+    }
+    pthread_mutex_unlock(&g_lock);
+    return rc;
+}
 
 extern "C" int cf_engine_last_stats(cf_engine_stats *out)
 {

@@ -69,7 +69,8 @@ typedef struct {
     int precision;       /* CF_PRECISION_FP32_REFINE or CF_PRECISION_FP64 */
     int fma_formula;     /* evaluate the double-precision formula of the reference's AVX512F kernels */
     int chord_formula;   /* theta: cos = 1 - chord^2/2 (SIMD kernels) instead of the dot product */
-    int elem_size;       /* 4 or 8: element type of the host position / weight arrays */
+    int elem_size;       /* 4 or 8: element type of the position / weight arrays */
+    int inputs_on_device; /* x/y/z/w are device pointers on the current device (no host copy) */
 
     int64_t n1, n2;
     const void *x1, *y1, *z1, *w1;  /* host arrays (w1 may be NULL) */
@@ -115,6 +116,8 @@ typedef struct {
     int num_cells;
 } cf_engine_stats;
 int cf_engine_last_stats(cf_engine_stats *out);
+int cf_engine_fp32_peak(double *tflops);
+int cf_engine_copy_to_host(void *dst, const void *src, size_t bytes);
 
 #ifdef __cplusplus
 }

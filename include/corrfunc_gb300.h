@@ -285,6 +285,27 @@ typedef struct {
 } cf_gpu_stats;
 int cf_gpu_last_stats(cf_gpu_stats *out);
 
+/* countpairs() with X1..Z2 and the weight arrays of `extra` already resident on the current CUDA
+ * device (device pointers); nothing is copied host to device.  No reference counterpart: it lets
+ * a caller that keeps catalogues in GPU memory skip the upload. */
+int cf_gpu_countpairs_device(const int64_t ND1, void *X1, void *Y1, void *Z1,
+                             const int64_t ND2, void *X2, void *Y2, void *Z2,
+                             const int numthreads, const int autocorr, const char *binfile,
+                             results_countpairs *results, struct config_options *options,
+                             struct extra_options *extra);
+
+/* Measured FP32 fused-multiply-add throughput of the current device in TFLOP/s (a calibration
+ * kernel; denominator of the pair kernels' FP32 roofline fraction).  No reference counterpart. */
+int cf_gpu_fp32_peak_tflops(double *tflops);
+
+/* The algorithmic work unit of countpairs(): the number of candidate pairs the reference's own
+ * lattice and cell-pair list (utils/gridlink_impl.c.src:65-625) would evaluate for these
+ * arguments.  Host arrays; runs on the CPU.  No reference counterpart. */
+int cf_reference_candidate_pairs(const int64_t ND1, void *X1, void *Y1, void *Z1,
+                                 const int64_t ND2, void *X2, void *Y2, void *Z2,
+                                 const int autocorr, const char *binfile,
+                                 struct config_options *options, uint64_t *candidates);
+
 /* ---------------- header-only helpers (utils/defs.h:158-346, 369-419) ----------------
  * Callers compile these themselves, exactly as with the reference header. */
 
