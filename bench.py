@@ -33,10 +33,17 @@ sys.path.insert(0, ROOT)
 
 METRIC = "pair evaluations/sec (reference-lattice candidate pairs), DD cross-correlation"
 UNIT = "pairs/s"
-WORKLOAD = dict(workload="theory DD cross-correlation with pair_product weights, N1=N2=2,000,000 clustered "
-                         "points, periodic L=1000, 25 log bins 0.1-50, float64",
-                n1=2_000_000, n2=2_000_000, boxsize=1000.0, nbins=25, rmin=0.1, rmax=50.0, seeds=[1, 2],
-                weights="U[0.5,1.5]", precision="fp32_refine")
+WORKLOADS = {
+    "cfg2": dict(workload="theory DD cross-correlation with pair_product weights, N1=N2=2,000,000 clustered "
+                          "points, periodic L=1000, 25 log bins 0.1-50, float64",
+                 n1=2_000_000, n2=2_000_000, boxsize=1000.0, nbins=25, rmin=0.1, rmax=50.0, seeds=[1, 2],
+                 weights="U[0.5,1.5]", kind="clustered", autocorr=0),
+    "northstar": dict(workload="theory DD auto-correlation, N=1,000,000 uniform points, periodic L=420, "
+                               "20 log bins 0.1-25, float64",
+                      n1=1_000_000, n2=0, boxsize=420.0, nbins=20, rmin=0.1, rmax=25.0, seeds=[0],
+                      weights=None, kind="uniform", autocorr=1),
+}
+WORKLOAD = dict(WORKLOADS["cfg2"])
 FLOP_PER_PAIR = 8  # 3 FADD + 1 FMUL + 2 FFMA per 3-D separation
 # dram__bytes_read.sum + dram__bytes_write.sum of one pair-kernel launch on this workload,
 # from the ncu capture summarised in profiles/ (None until captured)
@@ -50,12 +57,16 @@ def _rank_env():
 def make_workload(dtype=np.float64):
     from corrfunc_gb300 import catalogs as cat
     L = WORKLOAD["boxsize"]
-    x1, y1, z1 = cat.clustered_box(WORKLOAD["n1"], L, WORKLOAD["seeds"][0], dtype=dtype)
-    x2, y2, z2 = cat.clustered_box(WORKLOAD["n2"], L, WORKLOAD["seeds"][1], dtype=dtype)
+    gen = cat.clustered_box if WORKLOAD["kind"] == "clustered" else cat.uniform_box
+    x1, y1, z1 = gen(WORKLOAD["n1"], L, WORKLOAD["seeds"][0], dtype=dtype)
     w1 = cat.weights(WORKLOAD["n1"], 101, dtype=dtype)
-    w2 = cat.weights(WORKLOAD["n2"], 102, dtype=dtype)
+    if WORKLOAD["autocorr"]:
+        set2 = (x1, y1, z1, w1)
+    else:
+        x2, y2, z2 = gen(WORKLOAD["n2"], L, WORKLOAD["seeds"][1], dtype=dtype)
+        set2 = (x2, y2, z2, cat.weights(WORKLOAD["n2"], 102, dtype=dtype))
     bins = cat.log_bins(WORKLOAD["rmin"], WORKLOAD["rmax"], WORKLOAD["nbins"])
-    return (x1, y1, z1, w1), (x2, y2, z2, w2), bins
+    return (x1, y1, z1, w1), set2, bins
 
 
 def options_for(C, L, dtype):
@@ -69,6 +80,8 @@ def options_for(C, L, dtype):
 
 
 def extra_for(C, w1, w2):
+    if WORKLOAD["weights"] is None:
+        return C.get_extra_options()
     e = C.get_extra_options(C.WEIGHT_PAIR_PRODUCT)
     e.weights0.weights[0] = w1
     e.weights1.weights[0] = w2
@@ -84,8 +97,9 @@ def reference_work(lib, C, set1, set2, binfile, dtype):
     lib.cf_reference_candidate_pairs.restype = ctypes.c_int
     o = options_for(C, WORKLOAD["boxsize"], dtype)
     out = ctypes.c_uint64()
+    auto = 1 if set2[0] is set1[0] else 0
     rc = lib.cf_reference_candidate_pairs(len(set1[0]), *(C.ptr(a) for a in set1[:3]), len(set2[0]),
-                                          *(C.ptr(a) for a in set2[:3]), 0, binfile.encode(), ctypes.byref(o),
+                                          *(C.ptr(a) for a in set2[:3]), auto, binfile.encode(), ctypes.byref(o),
                                           ctypes.byref(out))
     if rc != 0:
         raise RuntimeError("cf_reference_candidate_pairs failed")
@@ -171,10 +185,16 @@ def cpu_reference_run(set1, set2, bins, nthreads, dtype, frac=1.0):
     n2 = int(len(set2[0]) * frac)
     s1 = tuple(np.ascontiguousarray(a[:n1]) for a in set1)
     s2 = tuple(np.ascontiguousarray(a[:n2]) for a in set2)
+    wkw = dict(weights1=s1[3], weights2=s2[3], weight_type="pair_product") if WORKLOAD["weights"] else {}
     t0 = time.perf_counter()
-    theory.run_DD(ref, 0, nthreads, bins, s1[0], s1[1], s1[2], weights1=s1[3], X2=s2[0], Y2=s2[1], Z2=s2[2],
-                  weights2=s2[3], weight_type="pair_product", periodic=True, boxsize=WORKLOAD["boxsize"],
-                  isa="fastest")
+    if WORKLOAD["autocorr"]:
+        wkw.pop("weights2", None)
+        theory.run_DD(ref, 1, nthreads, bins, s1[0], s1[1], s1[2], periodic=True, boxsize=WORKLOAD["boxsize"],
+                      isa="fastest", **wkw)
+        s2 = s1
+    else:
+        theory.run_DD(ref, 0, nthreads, bins, s1[0], s1[1], s1[2], X2=s2[0], Y2=s2[1], Z2=s2[2], periodic=True,
+                      boxsize=WORKLOAD["boxsize"], isa="fastest", **wkw)
     dt = time.perf_counter() - t0
     gpu_lib = C.bind(C.LIB_PATH, gpu=True)
     with C.BinFile(bins) as bf:
@@ -225,7 +245,10 @@ def main():
     ap.add_argument("--precision", default="fp32_refine", choices=["fp32_refine", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--extras", action="store_true", help="also time the FP64 form and the north-star workload")
+    ap.add_argument("--workload", default="cfg2", choices=sorted(WORKLOADS))
     args = ap.parse_args()
+    WORKLOAD.clear()
+    WORKLOAD.update(WORKLOADS[args.workload])
     if args.impl == "reference":
         return run_reference_arm(args)
 
@@ -260,7 +283,8 @@ def main():
         e = extra_for(C, d1[3].data_ptr(), d2[3].data_ptr())
         res = C.ResultsDD()
         rc = lib.cf_gpu_countpairs_device(len(set1[0]), *(ctypes.c_void_p(t.data_ptr()) for t in d1[:3]),
-                                          len(set2[0]), *(ctypes.c_void_p(t.data_ptr()) for t in d2[:3]), 1, 0,
+                                          len(set2[0]), *(ctypes.c_void_p(t.data_ptr()) for t in d2[:3]), 1,
+                                          WORKLOAD["autocorr"],
                                           binfile.encode(), ctypes.byref(res), ctypes.byref(o), ctypes.byref(e))
         if rc != 0:
             raise RuntimeError("countpairs on device inputs failed")
@@ -278,7 +302,8 @@ def main():
         e = extra_for(C, hn1[3].ctypes.data, hn2[3].ctypes.data)
         res = C.ResultsDD()
         rc = lib.countpairs(len(hn1[0]), *(C.ptr(a) for a in hn1[:3]), len(hn2[0]), *(C.ptr(a) for a in hn2[:3]),
-                            1, 0, binfile.encode(), ctypes.byref(res), ctypes.byref(o), ctypes.byref(e))
+                            1, WORKLOAD["autocorr"], binfile.encode(), ctypes.byref(res), ctypes.byref(o),
+                            ctypes.byref(e))
         if rc != 0:
             raise RuntimeError("countpairs failed")
         npairs = np.ctypeslib.as_array(res.npairs, shape=(res.nbin,)).copy()
@@ -328,7 +353,8 @@ def main():
         if not np.array_equal(npairs_h, ref_np):
             raise RuntimeError("host-buffer path disagrees with the device-buffer path")
     e2e_value = world * work * args.steps / sum(e2e_t)
-    h2d = sum(a.nbytes for a in hn1) + sum(a.nbytes for a in hn2)
+    nper = 4 if WORKLOAD["weights"] else 3
+    h2d = sum(a.nbytes for a in hn1[:nper]) + (0 if WORKLOAD["autocorr"] else sum(a.nbytes for a in hn2[:nper]))
     d2h = (WORKLOAD["nbins"] + 1) * (8 + 8 + 8 + 8)
 
     peak = ctypes.c_double()
@@ -345,13 +371,16 @@ def main():
                            reference_lattice_candidates=work),
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                          "frac": achieved / peak.value if peak.value else None, "traffic": traffic,
-                         "kernel": "k_pairs_f32<MODE_R3,false,true>" if args.precision == "fp32_refine"
-                         else "k_pairs_f64<MODE_R3,false,true>",
+                         "kernel": "%s<MODE_R3,false,%s>" % ("k_pairs_f32" if args.precision == "fp32_refine"
+                                                             else "k_pairs_f64",
+                                                             "true" if WORKLOAD["weights"] else "false"),
                          "peak_source": "measured: FP32 FMA calibration kernel (cf_gpu_fp32_peak_tflops) in this run",
                          "flop_per_pair": FLOP_PER_PAIR},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": 1e3 * sum(e2e_t) / args.steps},
             "gpu_launches": launches,
+            "launch": {"blocks_per_sm": st["blocks_per_sm"], "warps_per_block": st["warps_per_block"],
+                       "lane_stride": st["lane_stride"]},
             "kernel_ms": {"pair_kernel": sum(pair_ms) / args.steps, "gridlink_and_worklist": sum(grid_ms) / args.steps,
                           "step_total": sum(gpu_ms) / args.steps, "host_wall": 1e3 * sum(wall) / args.steps},
             "pairs": {"reference_lattice_candidates": work, "gpu_evaluated": evaluated // args.steps,

@@ -991,6 +991,10 @@ int cf_gpu_last_stats(cf_gpu_stats *out)
     out->tasks = s.tasks;
     out->kernel_launches = s.kernel_launches;
     out->num_cells = s.num_cells;
+    out->blocks_per_sm = s.blocks_per_sm;
+    out->warps_per_block = s.warps_per_block;
+    out->lane_stride = s.lane_stride;
+    out->reserved = 0;
     return EXIT_SUCCESS;
 }
 

@@ -55,8 +55,20 @@ struct PairArgs {
     unsigned long long *g_stats; // [0] evaluated pairs, [1] refined pairs
     const double *g_edges;      // nedges (double, reference values)
     const float *g_guard;       // 2*nedges: lo guards then hi guards
+    const uint32_t *g_lut;      // bin lookup on the float bits of the classified quantity (row byte offsets)
+    uint32_t trash_off;         // byte offset of the trash row (rejected / deferred pairs)
+    uint32_t row_bytes;         // bytes between consecutive histogram rows (4 * lane stride)
+    int lane_stride_hint;       // layout the LUT offsets were built for
+    int lut_n_hint;
+    int lut_shift;              // bucket = (float_bits >> lut_shift) - lut_base
+    int lut_base;
+    int lut_n;                  // buckets; entry lut_n is the reject entry
+    uint32_t lut_mul;           // 2^(32 - lut_shift): bucket = mad.hi(bits, lut_mul, -lut_base)
+    float q_floor;              // added to q in the fast path so that q = 0 stays in the table
+    uint32_t lut_negbase;
 
     int nedges;
+    int guard_search_top;       // largest power of two <= nedges - 1 (0 when nedges < 2)
     int nbins;
     int npibin;                 // rp-pi: pi bins, s-mu: mu bins
     int autocorr;
@@ -76,6 +88,8 @@ struct PairArgs {
     float pimax_lo_f, pimax_hi_f;  // guard band around pimax for |dz|
     float inv_dpi_f;
     float pibin_band;              // half-width (in pi-bin units) of the ambiguity band
+    float inv_dpi256_f;            // 256 / dpi (fast pi-bin rounding)
+    int pi_band_q;                 // ambiguity half-width in 1/256 pi-bin units (fast path)
     float mu_band_abs;             // absolute mu error bound numerator (divided by s)
     float mu_max_f;
     float inv_dmu_f;

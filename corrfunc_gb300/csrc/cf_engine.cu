@@ -49,6 +49,19 @@ constexpr int kChunk = 32;          // points per i-chunk (one per lane)
 constexpr uint32_t kJMax = 2048;    // max j points per task
 constexpr int kRxy = 2;             // lattice columns per rmax_xy
 constexpr int kZFine = 8;           // z slabs per rmax_z
+// the FP32 pair kernel's largest block and the resident blocks of that size per SM it is compiled
+// for: 2 x 512 threads caps it at 64 registers (32 resident warps per SM)
+#ifndef CF_PAIR_MAX_THREADS
+#define CF_PAIR_MAX_THREADS 512
+#endif
+#ifndef CF_PAIR_MIN_BLOCKS
+#define CF_PAIR_MIN_BLOCKS 2
+#endif
+// pairs whose table offsets are computed before their shared reductions are issued
+#ifndef CF_PAIR_GROUP
+#define CF_PAIR_GROUP 8
+#endif
+
 constexpr uint64_t kFlushPairs = 1ull << 22;  // per-warp accumulator flush interval
 constexpr int kScanTile = 4096;
 
@@ -380,86 +393,142 @@ __global__ void k_task_emit(TaskGeom G, uint32_t nchunks, const uint32_t *chunk_
 // pair kernels
 // ------------------------------------------------------------------------------------
 struct SmemLayout {
-    int nedges, nbins, warps;
-    size_t edges_off, guard_off, stage_off, hist_off, per_warp_hist, per_warp_stage, total;
+    int nedges, nbins, warps, lut_n, lane_stride;
+    int nrows;  // histogram rows incl. the trash rows that absorb rejected / deferred pairs
+    bool need_avg, need_w, fixed64;
+    size_t edges_off, guard_off, lut_off, stage_off, hist_off, per_warp_hist, per_warp_stage, total;
 };
 
 __host__ __device__ inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-__host__ __device__ inline SmemLayout smem_layout(int nedges, int nbins, int warps, bool f64)
+constexpr int kRefineQueue = 64;  // per-warp queue of pairs awaiting the FP64 re-evaluation
+constexpr int kSlowQueue = 64;    // per-warp queue of pairs in flagged table buckets
+
+struct RefineEntry {
+    uint32_t i, j, meta;  // meta: image code bits 8-13 as in Task
+};
+
+// Histogram accumulators live in shared memory, one set per warp.  With lane_stride == 32 every
+// lane owns a private column (bank = lane, no conflicts, no contention); for large 2-D
+// histograms lane_stride == 1 and the lanes of a warp share one row through shared atomics.
+// Weight and separation sums are 64-bit fixed point (one term below 2^40, flushed into the FP64
+// global histogram at most every kFlushPairs pairs, so a column never exceeds 2^62).
+__host__ __device__ inline SmemLayout smem_layout(int nedges, int nbins, int warps, bool f64, int lut_n, int lane_stride,
+                                                  bool need_avg, bool need_w, bool store_dz)
 {
     SmemLayout L;
+    L.need_avg = need_avg;
+    L.need_w = need_w;
+    L.fixed64 = true;
+    (void)f64;
     L.nedges = nedges;
     L.nbins = nbins;
     L.warps = warps;
+    L.lut_n = lut_n;
+    L.lane_stride = lane_stride;
+    // trash rows: one for 1-D modes, one row of 2-D cells (npibin + 1 = nbins / nedges) otherwise
+    L.nrows = nbins + (store_dz && nbins > nedges ? nbins / nedges : 1);
     size_t o = 0;
     L.edges_off = o;
     o = align_up(o + sizeof(double) * nedges, 16);
     L.guard_off = o;
     o = align_up(o + sizeof(float) * 2 * nedges, 16);
+    L.lut_off = o;
+    o = align_up(o + sizeof(uint32_t) * (lut_n + 1), 16);
     L.stage_off = o;
-    // f32: float4 hi[32] + float4 lo[32]; f64: double4_32a[32] + int rc[32] + int orig[32]
-    L.per_warp_stage = f64 ? (32 * sizeof(double4_32a) + 64 * sizeof(int)) : (64 * sizeof(float4));
+    // f32: float4 hi[32] + float4 lo[32] + refine queue; f64: double4_32a[32] + int rc[32] + int orig[32]
+    L.per_warp_stage = f64 ? (32 * sizeof(double4_32a) + 64 * sizeof(int))
+                           : (64 * sizeof(float4) + (kRefineQueue + kSlowQueue) * sizeof(RefineEntry) + 16);
     o = align_up(o + L.per_warp_stage * warps, 16);
     L.hist_off = o;
-    L.per_warp_hist = align_up((size_t)nbins * (8 + 8 + 4), 16);
+    const size_t vb = 8;
+    L.per_warp_hist = align_up((size_t)L.nrows * lane_stride * (4 + (need_avg ? vb : 0) + (need_w ? vb : 0)) + 32, 16);
     o += L.per_warp_hist * warps;
     L.total = o;
     return L;
 }
 
 struct WarpHist {
-    unsigned long long *avg;
-    unsigned long long *w;
+    void *avg;
+    void *w;
     uint32_t *cnt;
+    int ls;  // lane stride
 };
 
 __device__ __forceinline__ WarpHist warp_hist(unsigned char *smem, const SmemLayout &L, int warp)
 {
     unsigned char *p = smem + L.hist_off + L.per_warp_hist * warp;
+    const size_t n = (size_t)L.nrows * L.lane_stride;
+    const size_t vb = 8;
     WarpHist h;
-    h.avg = (unsigned long long *)p;
-    h.w = (unsigned long long *)(p + 8 * (size_t)L.nbins);
-    h.cnt = (uint32_t *)(p + 16 * (size_t)L.nbins);
+    size_t o = 0;
+    h.avg = (void *)(p + o);
+    if (L.need_avg) o += vb * n;
+    h.w = (void *)(p + o);
+    if (L.need_w) o += vb * n;
+    h.cnt = (uint32_t *)(p + o);
+    h.ls = L.lane_stride;
     return h;
 }
 
-template <bool NEED_AVG, bool NEED_W>
+__device__ __forceinline__ void zero_hist(WarpHist h, const SmemLayout &L, int lane)
+{
+    const int n = L.nrows * h.ls;
+    for (int b = lane; b < n; b += 32) {
+        h.cnt[b] = 0;
+        if (L.fixed64) {
+            if (L.need_avg) ((unsigned long long *)h.avg)[b] = 0;
+            if (L.need_w) ((unsigned long long *)h.w)[b] = 0;
+        } else {
+            if (L.need_avg) ((float *)h.avg)[b] = 0.f;
+            if (L.need_w) ((float *)h.w)[b] = 0.f;
+        }
+    }
+}
+
+template <bool NEED_AVG, bool NEED_W, bool FIXED64>
 __device__ __forceinline__ void flush_hist(const PairArgs &A, WarpHist h, int lane)
 {
+    __syncwarp();
     for (int b = lane; b < A.nbins; b += 32) {
-        const uint32_t c = h.cnt[b];
-        if (c) {
-            atomicAdd(&A.g_cnt[b], (unsigned long long)c);
-            h.cnt[b] = 0;
-        }
-        if (NEED_AVG) {
-            const long long v = (long long)h.avg[b];
-            if (v) {
-                atomicAdd(&A.g_avg[b], (double)v * A.avg_unscale);
-                h.avg[b] = 0;
+        unsigned long long c = 0;
+        long long va = 0, vw = 0;
+        double fa = 0.0, fw = 0.0;
+        for (int t = 0; t < h.ls; t++) {
+            const int l = (t + lane) & (h.ls - 1);  // skewed so that the lanes hit distinct banks
+            const int idx = b * h.ls + l;
+            c += h.cnt[idx];
+            h.cnt[idx] = 0;
+            if (FIXED64) {
+                if (NEED_AVG) {
+                    va += ((long long *)h.avg)[idx];
+                    ((long long *)h.avg)[idx] = 0;
+                }
+                if (NEED_W) {
+                    vw += ((long long *)h.w)[idx];
+                    ((long long *)h.w)[idx] = 0;
+                }
+            } else {
+                if (NEED_AVG) {
+                    fa += (double)((float *)h.avg)[idx];
+                    ((float *)h.avg)[idx] = 0.f;
+                }
+                if (NEED_W) {
+                    fw += (double)((float *)h.w)[idx];
+                    ((float *)h.w)[idx] = 0.f;
+                }
             }
         }
-        if (NEED_W) {
-            const long long v = (long long)h.w[b];
-            if (v) {
-                atomicAdd(&A.g_w[b], (double)v * A.w_unscale);
-                h.w[b] = 0;
-            }
+        if (c) atomicAdd(&A.g_cnt[b], c);
+        if (FIXED64) {
+            if (NEED_AVG && va) atomicAdd(&A.g_avg[b], (double)va * A.avg_unscale);
+            if (NEED_W && vw) atomicAdd(&A.g_w[b], (double)vw * A.w_unscale);
+        } else {
+            if (NEED_AVG && fa != 0.0) atomicAdd(&A.g_avg[b], fa);
+            if (NEED_W && fw != 0.0) atomicAdd(&A.g_w[b], fw);
         }
     }
     __syncwarp();
-}
-
-__device__ __forceinline__ int guard_upper(const float *glo, int n, float v)
-{
-    // number of lower guards <= v
-    int lo = 0, hi = n;
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (glo[mid] <= v) lo = mid + 1; else hi = mid;
-    }
-    return lo;
 }
 
 // first-point rule of the reference for wrapped auto-correlation pairs
@@ -472,8 +541,8 @@ __device__ __forceinline__ bool j_is_first(const PairArgs &A, uint32_t i, uint32
 }
 
 template <int MODE>
-__device__ __forceinline__ int refine_pair(const PairArgs &A, const double *se, uint32_t i, uint32_t j,
-                                           int mx, int my, int mz, double *avg_term, double *wprod)
+__device__ __noinline__ int refine_pair(const PairArgs &A, const double *se, uint32_t i, uint32_t j,
+                                        int mx, int my, int mz, double *avg_term, double *wprod)
 {
     const double4_32a pi = A.d1[i], pj = A.d2[j];
     *wprod = pi.w * pj.w;
@@ -488,31 +557,320 @@ __device__ __forceinline__ int refine_pair(const PairArgs &A, const double *se, 
     return ref_eval<MODE>(A, se, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, -ox, -oy, -oz, avg_term);
 }
 
+// LUT bucket of the classified FP32 quantity q (r^2, rp^2, s^2 or chord^2): one mad.hi on the
+// float bits (bucket = (bits >> shift) - base), clamped to the reject entry lut_n.
+__device__ __forceinline__ uint32_t lut_bucket(const PairArgs &A, float q)
+{
+    uint32_t r;
+    asm("mad.hi.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(__float_as_uint(q)), "r"(A.lut_mul), "r"(A.lut_negbase));
+    return min(r, (uint32_t)A.lut_n);
+}
+
+// Exact FP32 classification of q against the guard bands: the bin m (1..nedges-1) with
+// *amb = false when q is provably on one side of every edge, *amb = true when q lies inside an
+// edge's band, or 0 when q is provably outside [rmin, rmax).
+__device__ __forceinline__ int classify_q(const PairArgs &A, const float *glo, const float *ghi, float q, bool *amb)
+{
+    const int n = A.nedges;
+    *amb = false;
+    if (q < glo[0] || q >= ghi[n - 1]) return 0;
+    // m = 1 + #{k in [1, n) : glo[k] <= q}; the guards are non-decreasing (binary lifting)
+    int pos = 0;
+    for (int step = A.guard_search_top; step > 0; step >>= 1)
+        if (pos + step <= n - 1 && glo[pos + step] <= q) pos += step;
+    const int m = pos + 1;
+    *amb = q < ghi[m - 1];
+    return m;
+}
+
+// Exact FP32 classification of one candidate whose LUT bucket is flagged: guard scan and the
+// 2-D bin checks.  Returns the flat bin (with its FP32 accumulator terms), -1 when the pair is
+// provably not counted, or -2 when it lies inside an error band and needs the reference's FP64
+// formula.
 template <int MODE, bool NEED_AVG, bool NEED_W>
-__global__ void __launch_bounds__(256) k_pairs_f32(PairArgs A, SmemLayout SL)
+__device__ __noinline__ int slow_candidate(const PairArgs &A, const float *glo, const float *ghi, float4 pj, float4 pjl,
+                                           float xi, float yi, float zi, float xil, float yil, float zil, float wi,
+                                           float *favg, float *fw)
+{
+    const float dx = pj.x - xi, dy = pj.y - yi, dz = pj.z - zi;
+    float q;  // the fast path's expression, so that the pair lands in the same flagged bucket
+    if (MODE == MODE_RPPI || MODE == MODE_WP) q = fmaf(dy, dy, fmaf(dx, dx, A.q_floor));
+    else q = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, A.q_floor)));
+    bool amb;
+    const int m = classify_q(A, glo, ghi, q, &amb);
+    if (m == 0) return -1;
+    int bin = m;
+    if (MODE == MODE_RPPI || MODE == MODE_WP) {
+        const float adz = fabsf(dz);
+        if (adz >= A.pimax_hi_f) return -1;
+        if (adz > A.pimax_lo_f) amb = true;
+        if (MODE == MODE_RPPI) {
+            const float tpi = adz * A.inv_dpi_f;
+            int pb = (int)tpi;
+            const float fr = tpi - (float)pb;
+            if ((pb >= 1 && fr < A.pibin_band) || (1.f - fr) < A.pibin_band) amb = true;
+            pb = pb > A.npibin ? A.npibin : pb;
+            bin = m * (A.npibin + 1) + pb;
+        }
+    }
+    if (MODE == MODE_SMU) {
+        if (!(q > 0.f)) amb = true;
+        const float sqq = sqrtf(q);
+        const float mu = fabsf(dz) / sqq;
+        const float emu = A.mu_band_abs / sqq + 6e-7f * mu + 1e-7f;
+        if (mu >= A.mu_max_f + emu) return -1;  // definitely mu >= mu_max
+        if (mu > A.mu_max_f - emu) amb = true;
+        const float tmu = mu * A.inv_dmu_f;
+        int pb = (int)tmu;
+        const float bt = emu * A.inv_dmu_f + 3e-7f * tmu;
+        const float fr = tmu - (float)pb;
+        if ((pb >= 1 && fr < bt) || (1.f - fr) < bt) amb = true;
+        pb = pb > A.npibin ? A.npibin : pb;
+        bin = m * (A.npibin + 1) + pb;
+    }
+    if (amb) return -2;
+    if (NEED_AVG) {
+        const float dxp = dx + (pjl.x - xil), dyp = dy + (pjl.y - yil), dzp = dz + (pjl.z - zil);
+        if (MODE == MODE_RPPI || MODE == MODE_WP) {
+            *favg = sqrtf(fmaf(dyp, dyp, dxp * dxp));
+        } else if (MODE == MODE_THETA) {
+            const float ch = sqrtf(fmaf(dzp, dzp, fmaf(dyp, dyp, dxp * dxp)));
+            *favg = 2.f * asinf(0.5f * ch) * 57.29577951308232f;
+        } else {
+            *favg = sqrtf(fmaf(dzp, dzp, fmaf(dyp, dyp, dxp * dxp)));
+        }
+    }
+    if (NEED_W) *fw = wi * pj.w;
+    return bin;
+}
+
+template <bool NEED_AVG, bool NEED_W>
+__device__ __forceinline__ void accumulate(const PairArgs &A, WarpHist h, int hidx, double davg, double dw)
+{
+    atomicAdd(&h.cnt[hidx], 1u);
+    if (NEED_AVG) atomicAdd(&((unsigned long long *)h.avg)[hidx], (unsigned long long)__double2ll_rn(davg * (double)A.avg_scale_f));
+    if (NEED_W) atomicAdd(&((unsigned long long *)h.w)[hidx], (unsigned long long)__double2ll_rn(dw * (double)A.w_scale_f));
+}
+
+__device__ __forceinline__ void red_shared_u32(uint32_t saddr, uint32_t v)
+{
+    asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(saddr), "r"(v));
+}
+
+__device__ __forceinline__ void red_shared_u64(uint32_t saddr, unsigned long long v)
+{
+    asm volatile("red.shared.add.u64 [%0], %1;" ::"r"(saddr), "l"(v));
+}
+
+// Fast classification of one pair.  k is the tile position (compile-time in full tiles).  The
+// LUT entry is the byte offset of the histogram row the pair belongs to (a trash row when the
+// pair is rejected or deferred) with bit 31 set when the pair must go through the exact slow
+// path; the caller issues one unconditional conflict-free shared reduction per pair.
+template <int MODE, bool NEED_AVG, bool NEED_W, bool OWN>
+__device__ __forceinline__ uint32_t pair_offset(const PairArgs &A, const float4 *__restrict__ sjhi,
+                                                const float4 *__restrict__ sjlo, const uint32_t *__restrict__ lut,
+                                                int k, uint32_t jb, uint32_t i, float xi, float yi, float zi,
+                                                float xil, float yil, float zil, float wis, uint32_t &slow,
+                                                long long &vw, long long &vavg)
+{
+    const float4 pj = sjhi[k];
+    const float dx = pj.x - xi, dy = pj.y - yi, dz = pj.z - zi;
+    // q_floor (1e-30 when rmin <= 0, else 0) keeps exact-zero separations inside the table
+    float q;
+    if (MODE == MODE_RPPI || MODE == MODE_WP) q = fmaf(dy, dy, fmaf(dx, dx, A.q_floor));
+    else q = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, A.q_floor)));
+    const uint32_t e = lut[lut_bucket(A, q)];
+    uint32_t off = e & 0x7fffffffu;
+    slow = e >> 31;
+    if (OWN) {
+        const bool keep = jb + (uint32_t)k > i;
+        off = keep ? off : A.trash_off;
+        slow = keep ? slow : 0u;
+    }
+    if (MODE == MODE_RPPI || MODE == MODE_WP || MODE == MODE_SMU) {
+        const float adz = fabsf(dz);
+        const bool real = off != A.trash_off;  // a definite rp / s bin
+        bool rej, amb;
+        uint32_t add = 0;
+        if (MODE == MODE_SMU) {
+            const float inv_s = rsqrtf(q);
+            const float mu = adz * inv_s;
+            const float emu = A.mu_band_abs * inv_s + 1e-6f * mu + 1e-7f;
+            rej = !(mu < A.mu_max_f + emu);
+            const float tmu = mu * A.inv_dmu_f;
+            const float rt = rintf(tmu);
+            amb = (mu > A.mu_max_f - emu) || (fabsf(tmu - rt) < emu * A.inv_dmu_f + 4e-7f * tmu && rt >= 0.5f);
+            add = (uint32_t)min((int)tmu, A.npibin) * A.row_bytes;
+        } else {
+            rej = !(adz < A.pimax_hi_f);
+            amb = adz > A.pimax_lo_f;
+            if (MODE == MODE_RPPI) {
+                // round(|dz| / dpi * 256) with the 1.5*2^23 constant: pi bin and its 8-bit fraction
+                const int v = __float_as_int(fmaf(adz, A.inv_dpi256_f, 12582912.0f)) - 0x4B400000;
+                amb = amb || (((v + A.pi_band_q) & 255) < 2 * A.pi_band_q);
+                add = (uint32_t)min(v >> 8, A.npibin) * A.row_bytes;
+            }
+        }
+        slow = (!rej && (slow || (real && amb))) ? 1u : 0u;
+        off = (real && !rej && !amb) ? off + add : A.trash_off;
+    }
+    if (NEED_W) vw = __float2ll_rn(wis * pj.w);
+    if (NEED_AVG) {
+        const float4 pjl = sjlo[k];
+        const float dxp = dx + (pjl.x - xil), dyp = dy + (pjl.y - yil), dzp = dz + (pjl.z - zil);
+        float favg;
+        if (MODE == MODE_RPPI || MODE == MODE_WP) {
+            favg = sqrtf(fmaf(dyp, dyp, dxp * dxp));
+        } else if (MODE == MODE_THETA) {
+            const float ch = sqrtf(fmaf(dzp, dzp, fmaf(dyp, dyp, dxp * dxp)));
+            favg = 2.f * asinf(0.5f * ch) * 57.29577951308232f;
+        } else {
+            favg = sqrtf(fmaf(dzp, dzp, fmaf(dyp, dyp, dxp * dxp)));
+        }
+        vavg = __float2ll_rn(favg * A.avg_scale_f);
+    }
+    return off;
+}
+
+template <int MODE, bool NEED_AVG, bool NEED_W, bool OWN, int U>
+__device__ __forceinline__ void pairs_group(const PairArgs &A, const float4 *__restrict__ sjhi,
+                                            const float4 *__restrict__ sjlo, const uint32_t *__restrict__ lut, int k0,
+                                            uint32_t jb, uint32_t i, float xi, float yi, float zi, float xil, float yil,
+                                            float zil, float wis, uint32_t cnt_s, uint32_t avg_s, uint32_t w_s,
+                                            uint32_t &slowbits)
+{
+    uint32_t off[U];
+    long long vw[U], va[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+        uint32_t sl;
+        vw[u] = 0;
+        va[u] = 0;
+        off[u] = pair_offset<MODE, NEED_AVG, NEED_W, OWN>(A, sjhi, sjlo, lut, k0 + u, jb, i, xi, yi, zi, xil, yil, zil,
+                                                          wis, sl, vw[u], va[u]);
+        slowbits += sl << (k0 + u);
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+        red_shared_u32(cnt_s + off[u], 1u);
+        if (NEED_W) red_shared_u64(w_s + 2 * off[u], (unsigned long long)vw[u]);
+        if (NEED_AVG) red_shared_u64(avg_s + 2 * off[u], (unsigned long long)va[u]);
+    }
+}
+
+template <int MODE, bool NEED_AVG, bool NEED_W, bool OWN>
+__device__ __forceinline__ uint32_t tile_fast(const PairArgs &A, const float4 *__restrict__ sjhi,
+                                              const float4 *__restrict__ sjlo, const uint32_t *__restrict__ lut, int nj,
+                                              uint32_t jb, uint32_t i, float xi, float yi, float zi, float xil, float yil,
+                                              float zil, float wis, uint32_t cnt_s, uint32_t avg_s, uint32_t w_s)
+{
+    uint32_t slowbits = 0;
+    if (nj == 32) {
+#pragma unroll
+        for (int k0 = 0; k0 < 32; k0 += CF_PAIR_GROUP)
+            pairs_group<MODE, NEED_AVG, NEED_W, OWN, CF_PAIR_GROUP>(A, sjhi, sjlo, lut, k0, jb, i, xi, yi, zi, xil, yil, zil, wis,
+                                                        cnt_s, avg_s, w_s, slowbits);
+    } else {
+        for (int k = 0; k < nj; k++)
+            pairs_group<MODE, NEED_AVG, NEED_W, OWN, 1>(A, sjhi, sjlo, lut, k, jb, i, xi, yi, zi, xil, yil, zil, wis,
+                                                        cnt_s, avg_s, w_s, slowbits);
+    }
+    return slowbits;
+}
+
+// Dense FP64 re-evaluation of up to 32 queued pairs (one per lane).
+template <int MODE, bool NEED_AVG, bool NEED_W>
+__device__ __noinline__ void refine_batch(const PairArgs &A, const double *se, const RefineEntry *q, int count,
+                                          WarpHist h, int hl, int lane)
+{
+    if (lane < count) {
+        const RefineEntry r = q[lane];
+        const int mx = (int)((r.meta >> 8) & 3u) - 1, my = (int)((r.meta >> 10) & 3u) - 1,
+                  mz = (int)((r.meta >> 12) & 3u) - 1;
+        double davg = 0.0, dw = 0.0;
+        const int bin = refine_pair<MODE>(A, se, r.i, r.j, mx, my, mz, &davg, &dw);
+        if (bin >= 0) accumulate<NEED_AVG, NEED_W>(A, h, bin * h.ls + hl, davg, dw);
+    }
+    __syncwarp();
+}
+
+// Exact FP32 classification of up to 32 queued pairs in flagged buckets (one per lane; the pairs
+// come from any lane and tile of the warp, so a warp spends one pass per 32 such pairs instead of
+// one pass per flagged pair of its busiest lane).  Both points are re-read from the lattice
+// arrays, which the warp touched a moment ago.  Pairs inside an error band move on to the FP64
+// queue.
+template <int MODE, bool NEED_AVG, bool NEED_W>
+__device__ __noinline__ void slow_batch(const PairArgs &A, const double *se, const float *glo, const float *ghi,
+                                        const RefineEntry *sq, int count, RefineEntry *rq, int *rq_count, WarpHist h,
+                                        int hl, int lane, unsigned long long *refined)
+{
+    if (lane < count) {
+        const RefineEntry e = sq[lane];
+        const int mx = (int)((e.meta >> 8) & 3u) - 1, my = (int)((e.meta >> 10) & 3u) - 1,
+                  mz = (int)((e.meta >> 12) & 3u) - 1;
+        const float4 pi = A.hi1[e.i];
+        const float4 pj = A.hi2[e.j];
+        const float xi = pi.x - A.ohi[0][mx + 1], yi = pi.y - A.ohi[1][my + 1], zi = pi.z - A.ohi[2][mz + 1];
+        float xil = 0.f, yil = 0.f, zil = 0.f;
+        float4 pjl = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (NEED_AVG) {
+            const float4 pl = A.lo1[e.i];
+            xil = pl.x - A.olo[0][mx + 1];
+            yil = pl.y - A.olo[1][my + 1];
+            zil = pl.z - A.olo[2][mz + 1];
+            pjl = A.lo2[e.j];
+        }
+        float favg = 0.f, fw = 0.f;
+        const int bin = slow_candidate<MODE, NEED_AVG, NEED_W>(A, glo, ghi, pj, pjl, xi, yi, zi, xil, yil, zil, pi.w,
+                                                               &favg, &fw);
+        if (bin >= 0) {
+            accumulate<NEED_AVG, NEED_W>(A, h, bin * h.ls + hl, (double)favg, (double)fw);
+        } else if (bin == -2) {
+            const int pos = atomicAdd(rq_count, 1);
+            rq[pos] = e;
+            (*refined)++;
+        }
+    }
+    __syncwarp();
+    const int cnt = *rq_count;
+    if (cnt >= 32) {
+        refine_batch<MODE, NEED_AVG, NEED_W>(A, se, rq + (cnt - 32), 32, h, hl, lane);
+        if (lane == 0) *rq_count = cnt - 32;
+        __syncwarp();
+    }
+}
+
+template <int MODE, bool NEED_AVG, bool NEED_W>
+__global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pairs_f32(PairArgs A, SmemLayout SL)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     double *se = (double *)(smem + SL.edges_off);
     float *glo = (float *)(smem + SL.guard_off);
     float *ghi = glo + A.nedges;
+    uint32_t *lut = (uint32_t *)(smem + SL.lut_off);
     for (int k = threadIdx.x; k < A.nedges; k += blockDim.x) {
         se[k] = A.g_edges[k];
         glo[k] = A.g_guard[k];
         ghi[k] = A.g_guard[A.nedges + k];
     }
+    for (int k = threadIdx.x; k <= SL.lut_n; k += blockDim.x) lut[k] = A.g_lut[k];
     float4 *sjhi = (float4 *)(smem + SL.stage_off + SL.per_warp_stage * warp);
     float4 *sjlo = sjhi + 32;
+    RefineEntry *rq = (RefineEntry *)(sjlo + 32);
+    RefineEntry *sq = rq + kRefineQueue;
+    int *rq_count = (int *)(sq + kSlowQueue);
+    int sq_n = 0;  // warp-uniform fill of the slow queue (always < 32 between tiles)
     WarpHist h = warp_hist(smem, SL, warp);
-    for (int b = lane; b < A.nbins; b += 32) {
-        h.cnt[b] = 0;
-        h.avg[b] = 0;
-        h.w[b] = 0;
-    }
+    zero_hist(h, SL, lane);
+    if (lane == 0) *rq_count = 0;
+    const int hl = lane & (SL.lane_stride - 1);
+    // shared-window addresses of this lane's column: count rows are 4 bytes apart per lane stride,
+    // the 64-bit sum rows twice that (offset doubled at the reduction)
+    const uint32_t cnt_s = (uint32_t)__cvta_generic_to_shared(h.cnt) + 4u * hl;
+    const uint32_t avg_s = (uint32_t)__cvta_generic_to_shared(h.avg) + 8u * hl;
+    const uint32_t w_s = (uint32_t)__cvta_generic_to_shared(h.w) + 8u * hl;
     __syncthreads();
-    const float g_lo0 = glo[0];
-    const float g_hiN = ghi[A.nedges - 1];
-    const int nedges = A.nedges;
     uint64_t since_flush = 0, evaluated = 0;
     unsigned long long refined = 0;
 
@@ -528,7 +886,7 @@ __global__ void __launch_bounds__(256) k_pairs_f32(PairArgs A, SmemLayout SL)
         const bool own = (T.meta >> 16) & 1u;
         const uint32_t i = T.i_begin + lane;
         const bool ivalid = lane < icount;
-        float4 pi = ivalid ? A.hi1[i] : make_float4(1e30f, 1e30f, 1e30f, 0.f);
+        const float4 pi = ivalid ? A.hi1[i] : make_float4(1e30f, 1e30f, 1e30f, 0.f);
         // j is shifted by the image offset o; equivalently shift i by -o (exact on the grid)
         const float xi = pi.x - A.ohi[0][mx + 1], yi = pi.y - A.ohi[1][my + 1], zi = pi.z - A.ohi[2][mz + 1];
         float xil = 0.f, yil = 0.f, zil = 0.f;
@@ -539,86 +897,37 @@ __global__ void __launch_bounds__(256) k_pairs_f32(PairArgs A, SmemLayout SL)
             zil = pl.z - A.olo[2][mz + 1];
         }
         for (uint32_t jb = T.j_begin; jb < T.j_end; jb += 32) {
-            const uint32_t nj = min(32u, T.j_end - jb);
-            if ((uint32_t)lane < nj) {
+            const int nj = (int)min(32u, T.j_end - jb);
+            if (lane < nj) {
                 sjhi[lane] = A.hi2[jb + lane];
                 if (NEED_AVG) sjlo[lane] = A.lo2[jb + lane];
             }
             __syncwarp();
-            for (uint32_t k = 0; k < nj; k++) {
-                const float4 pj = sjhi[k];
-                const float dx = pj.x - xi, dy = pj.y - yi, dz = pj.z - zi;
-                float r2;
-                if (MODE == MODE_RPPI || MODE == MODE_WP) {
-                    r2 = fmaf(dy, dy, dx * dx);
-                    if (fabsf(dz) >= A.pimax_hi_f) continue;
-                } else {
-                    r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            const float wi_s = pi.w * A.w_scale_f;
+            uint32_t slowbits = own ? tile_fast<MODE, NEED_AVG, NEED_W, true>(A, sjhi, sjlo, lut, nj, jb, i, xi, yi, zi,
+                                                                           xil, yil, zil, wi_s, cnt_s, avg_s, w_s)
+                                    : tile_fast<MODE, NEED_AVG, NEED_W, false>(A, sjhi, sjlo, lut, nj, jb, i, xi, yi,
+                                                                            zi, xil, yil, zil, wi_s, cnt_s, avg_s, w_s);
+            // candidates in flagged buckets go to the warp's slow queue, one bit per lane per round
+            // (a round appends at most 32 entries, so the queue never holds more than 63)
+            while (true) {
+                const uint32_t want = __ballot_sync(0xffffffffu, slowbits != 0);
+                if (!want) break;
+                if (slowbits) {
+                    const int b = (int)(__float_as_uint(__uint2float_rz(slowbits)) >> 23) - 127;
+                    slowbits ^= 1u << b;
+                    RefineEntry r;
+                    r.i = i;
+                    r.j = jb + (uint32_t)b;
+                    r.meta = T.meta;
+                    sq[sq_n + __popc(want & ((1u << lane) - 1u))] = r;
                 }
-                if (!(r2 >= g_lo0 && r2 < g_hiN)) continue;
-                const uint32_t j = jb + k;
-                if (own && j <= i) continue;
-                // ---- candidate inside the outer guards: classify ----
-                const int m = guard_upper(glo, nedges, r2);
-                bool amb = r2 < ghi[m - 1];
-                int bin = m;
-                if (MODE == MODE_RPPI || MODE == MODE_WP) {
-                    const float adz = fabsf(dz);
-                    if (adz > A.pimax_lo_f) amb = true;
-                    if (MODE == MODE_RPPI) {
-                        const float tpi = adz * A.inv_dpi_f;
-                        int pb = (int)tpi;
-                        const float fr = tpi - (float)pb;
-                        if ((pb >= 1 && fr < A.pibin_band) || (1.f - fr) < A.pibin_band) amb = true;
-                        pb = pb > A.npibin ? A.npibin : pb;
-                        bin = m * (A.npibin + 1) + pb;
-                    }
-                }
-                float favg = 0.f;
-                if (MODE == MODE_SMU) {
-                    if (!(r2 > 0.f)) amb = true;
-                    const float s = sqrtf(r2);
-                    const float mu = fabsf(dz) / s;
-                    const float emu = A.mu_band_abs / s + 6e-7f * mu + 1e-7f;
-                    if (mu >= A.mu_max_f + emu) continue;  // definitely mu >= mu_max
-                    if (mu > A.mu_max_f - emu) amb = true;
-                    const float tmu = mu * A.inv_dmu_f;
-                    int pb = (int)tmu;
-                    const float bt = emu * A.inv_dmu_f + 3e-7f * tmu;
-                    const float fr = tmu - (float)pb;
-                    if ((pb >= 1 && fr < bt) || (1.f - fr) < bt) amb = true;
-                    pb = pb > A.npibin ? A.npibin : pb;
-                    bin = m * (A.npibin + 1) + pb;
-                }
-                double davg = 0.0, dw = 0.0;
-                bool use_double = false;
-                if (amb) {
-                    refined++;
-                    bin = refine_pair<MODE>(A, se, i, j, mx, my, mz, &davg, &dw);
-                    if (bin < 0) continue;
-                    use_double = true;
-                } else if (NEED_AVG) {
-                    const float4 pjl = sjlo[k];
-                    const float dxp = dx + (pjl.x - xil), dyp = dy + (pjl.y - yil), dzp = dz + (pjl.z - zil);
-                    if (MODE == MODE_RPPI || MODE == MODE_WP) {
-                        favg = sqrtf(fmaf(dyp, dyp, dxp * dxp));
-                    } else if (MODE == MODE_THETA) {
-                        const float ch = sqrtf(fmaf(dzp, dzp, fmaf(dyp, dyp, dxp * dxp)));
-                        favg = 2.f * asinf(0.5f * ch) * 57.29577951308232f;
-                    } else {
-                        favg = sqrtf(fmaf(dzp, dzp, fmaf(dyp, dyp, dxp * dxp)));
-                    }
-                }
-                atomicAdd(&h.cnt[bin], 1u);
-                if (NEED_AVG) {
-                    const long long v = use_double ? __double2ll_rn(davg * (double)A.avg_scale_f)
-                                                   : __float2ll_rn(favg * A.avg_scale_f);
-                    atomicAdd(&h.avg[bin], (unsigned long long)v);
-                }
-                if (NEED_W) {
-                    const long long v = use_double ? __double2ll_rn(dw * (double)A.w_scale_f)
-                                                   : __float2ll_rn((pi.w * pj.w) * A.w_scale_f);
-                    atomicAdd(&h.w[bin], (unsigned long long)v);
+                sq_n += __popc(want);
+                __syncwarp();
+                if (sq_n >= 32) {
+                    slow_batch<MODE, NEED_AVG, NEED_W>(A, se, glo, ghi, sq + (sq_n - 32), 32, rq, rq_count, h, hl,
+                                                       lane, &refined);
+                    sq_n -= 32;
                 }
             }
             __syncwarp();
@@ -627,11 +936,15 @@ __global__ void __launch_bounds__(256) k_pairs_f32(PairArgs A, SmemLayout SL)
         since_flush += np;
         evaluated += np;
         if (since_flush > kFlushPairs) {
-            flush_hist<NEED_AVG, NEED_W>(A, h, lane);
+            flush_hist<NEED_AVG, NEED_W, true>(A, h, lane);
             since_flush = 0;
         }
     }
-    flush_hist<NEED_AVG, NEED_W>(A, h, lane);
+    __syncwarp();
+    if (sq_n > 0) slow_batch<MODE, NEED_AVG, NEED_W>(A, se, glo, ghi, sq, sq_n, rq, rq_count, h, hl, lane, &refined);
+    const int rest = *rq_count;
+    if (rest > 0) refine_batch<MODE, NEED_AVG, NEED_W>(A, se, rq, rest, h, hl, lane);
+    flush_hist<NEED_AVG, NEED_W, true>(A, h, lane);
     for (int off = 16; off; off >>= 1) refined += __shfl_down_sync(0xffffffffu, refined, off);
     if (lane == 0) {
         atomicAdd(&A.g_stats[0], (unsigned long long)evaluated);
@@ -650,11 +963,8 @@ __global__ void __launch_bounds__(256) k_pairs_f64(PairArgs A, SmemLayout SL)
     int *srcell = (int *)(sj + 32);
     int *sorig = srcell + 32;
     WarpHist h = warp_hist(smem, SL, warp);
-    for (int b = lane; b < A.nbins; b += 32) {
-        h.cnt[b] = 0;
-        h.avg[b] = 0;
-        h.w[b] = 0;
-    }
+    zero_hist(h, SL, lane);
+    const int hl = lane & (SL.lane_stride - 1);
     __syncthreads();
     uint64_t since_flush = 0, evaluated = 0;
     const double avg_scale = (double)A.avg_scale_f, w_scale = (double)A.w_scale_f;
@@ -698,9 +1008,12 @@ __global__ void __launch_bounds__(256) k_pairs_f64(PairArgs A, SmemLayout SL)
                         bin = ref_eval<MODE>(A, se, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, -ox, -oy, -oz, &avg_term);
                     }
                     if (bin < 0) continue;
-                    atomicAdd(&h.cnt[bin], 1u);
-                    if (NEED_AVG) atomicAdd(&h.avg[bin], (unsigned long long)__double2ll_rn(avg_term * avg_scale));
-                    if (NEED_W) atomicAdd(&h.w[bin], (unsigned long long)__double2ll_rn(pi.w * pj.w * w_scale));
+                    const int hidx = bin * h.ls + hl;
+                    atomicAdd(&h.cnt[hidx], 1u);
+                    if (NEED_AVG)
+                        atomicAdd(&((unsigned long long *)h.avg)[hidx], (unsigned long long)__double2ll_rn(avg_term * avg_scale));
+                    if (NEED_W)
+                        atomicAdd(&((unsigned long long *)h.w)[hidx], (unsigned long long)__double2ll_rn(pi.w * pj.w * w_scale));
                 }
             }
             __syncwarp();
@@ -709,11 +1022,11 @@ __global__ void __launch_bounds__(256) k_pairs_f64(PairArgs A, SmemLayout SL)
         since_flush += np;
         evaluated += np;
         if (since_flush > kFlushPairs) {
-            flush_hist<NEED_AVG, NEED_W>(A, h, lane);
+            flush_hist<NEED_AVG, NEED_W, true>(A, h, lane);
             since_flush = 0;
         }
     }
-    flush_hist<NEED_AVG, NEED_W>(A, h, lane);
+    flush_hist<NEED_AVG, NEED_W, true>(A, h, lane);
     if (lane == 0) atomicAdd(&A.g_stats[0], (unsigned long long)evaluated);
 }
 
@@ -771,9 +1084,11 @@ struct Engine {
     cudaEvent_t ev[6];
     SetBufs set[2];
     DevBuf mm, oob, scan_tmp[4], chunk_cnt, chunk_off, chunk_begin, chunk_count, ntask, task_off, tasks;
-    DevBuf hist_cnt, hist_avg, hist_w, stats, counter, edges, guards;
+    DevBuf hist_cnt, hist_avg, hist_w, stats, counter, edges, guards, lut;
     int precision = CF_PRECISION_FP32_REFINE;
     int launches = 0;  // kernels launched by the current call
+    size_t smem_per_sm = 228 * 1024;
+    int last_blocks_per_sm = 0, last_warps_per_block = 0, last_lane_stride = 0;
     cf_engine_stats last;
 };
 
@@ -799,6 +1114,7 @@ static int engine_init(void)
     }
     g_eng.device = dev;
     g_eng.num_sms = prop.multiProcessorCount;
+    g_eng.smem_per_sm = prop.sharedMemPerMultiprocessor;
     CF_CUDA(cudaStreamCreateWithFlags(&g_eng.stream, cudaStreamNonBlocking));
     for (int k = 0; k < 6; k++) CF_CUDA(cudaEventCreate(&g_eng.ev[k]));
     g_eng.init = true;
@@ -924,18 +1240,82 @@ static int build_lattice(int s, int64_t n, bool has_w, const Geom &g, uint32_t n
     return EXIT_SUCCESS;
 }
 
+// Histogram layout / block size that keeps the most warps resident: private per-lane columns
+// (conflict-free) or one shared row per warp (shared atomics), 8/4/2 warps per block.
+template <int MODE, bool AVG, bool W>
+static int pair_kernel_regs_t(bool f64)
+{
+    cudaFuncAttributes fa;
+    const cudaError_t rc = f64 ? cudaFuncGetAttributes(&fa, k_pairs_f64<MODE, AVG, W>)
+                               : cudaFuncGetAttributes(&fa, k_pairs_f32<MODE, AVG, W>);
+    return rc == cudaSuccess && fa.numRegs > 0 ? fa.numRegs : 64;
+}
+
+template <int MODE>
+static int pair_kernel_regs_m(bool f64, bool avg, bool w)
+{
+    if (avg && w) return pair_kernel_regs_t<MODE, true, true>(f64);
+    if (avg) return pair_kernel_regs_t<MODE, true, false>(f64);
+    if (w) return pair_kernel_regs_t<MODE, false, true>(f64);
+    return pair_kernel_regs_t<MODE, false, false>(f64);
+}
+
+static int pair_kernel_regs(int mode, bool f64, bool avg, bool w)
+{
+    switch (mode) {
+    case MODE_R3: return pair_kernel_regs_m<MODE_R3>(f64, avg, w);
+    case MODE_RPPI: return pair_kernel_regs_m<MODE_RPPI>(f64, avg, w);
+    case MODE_WP: return pair_kernel_regs_m<MODE_WP>(f64, avg, w);
+    case MODE_SMU: return pair_kernel_regs_m<MODE_SMU>(f64, avg, w);
+    default: return pair_kernel_regs_m<MODE_THETA>(f64, avg, w);
+    }
+}
+
+// Histogram layout and block size.  Lanes l and l + lane_stride share a column; the score is the
+// resident warps per SM (shared memory and registers) discounted by the expected contention of
+// shared columns (1 = private, 2 = 2-way, ... 32 = the whole warp on one row).
+static SmemLayout choose_layout(int mode, bool f64, bool avg, bool w, int nedges, int nbins, int lut_n)
+{
+    const bool dz = (mode == MODE_RPPI || mode == MODE_WP || mode == MODE_SMU);
+    const int regs = pair_kernel_regs(mode, f64, avg, w);
+    const int warps_by_regs = 65536 / (32 * ((regs + 7) / 8 * 8));
+    SmemLayout SL = smem_layout(nedges, nbins, 8, f64, lut_n, 1, avg, w, dz);
+    double best = -1.0;
+    const int lstrides[5] = {32, 16, 8, 4, 1};
+    // measured: 2-way sharing costs a few per cent, 4-way about a third (64-bit weight sums)
+    const double lfactor[5] = {1.0, 0.92, 0.6, 0.45, 0.2};
+    const int max_warps = f64 ? 8 : CF_PAIR_MAX_THREADS / 32;
+    const int wopts[3] = {max_warps, max_warps / 2, max_warps / 4};
+    for (int li = 0; li < 5; li++) {
+        for (int wi = 0; wi < 3; wi++) {
+            const SmemLayout c = smem_layout(nedges, nbins, wopts[wi], f64, lut_n, lstrides[li], avg, w, dz);
+            if (c.total > 220 * 1024) continue;
+            int blocks = (int)(g_eng.smem_per_sm / (c.total + 1024));
+            const int max_blocks_threads = 2048 / (32 * wopts[wi]);
+            if (blocks > max_blocks_threads) blocks = max_blocks_threads;
+            const int max_blocks_regs = warps_by_regs / wopts[wi];
+            if (blocks > max_blocks_regs) blocks = max_blocks_regs;
+            int resident = blocks * wopts[wi];
+            if (resident > 48) resident = 48;
+            const double score = resident * lfactor[li] + 1e-3 * wopts[wi];
+            if (score > best) {
+                best = score;
+                SL = c;
+            }
+        }
+    }
+    return SL;
+}
+
 template <int MODE, bool AVG, bool W>
 static int launch_pairs_t(const PairArgs &A, bool f64, int *launched)
 {
     const int nedges = A.nedges;
-    int warps = 8;
-    SmemLayout SL = smem_layout(nedges, A.nbins, warps, f64);
-    while (SL.total > 200 * 1024 && warps > 1) {
-        warps >>= 1;
-        SL = smem_layout(nedges, A.nbins, warps, f64);
-    }
+    constexpr bool DZ = (MODE == MODE_RPPI || MODE == MODE_WP || MODE == MODE_SMU);
+    SmemLayout SL = choose_layout(MODE, f64, AVG, W, nedges, A.nbins, A.lut_n);
+    if (!f64 && SL.lane_stride != A.lane_stride_hint) CF_FAIL("internal: histogram layout changed after the table was built");
     if (SL.total > 220 * 1024) CF_FAIL("histogram too large for on-chip accumulation (%d bins)", A.nbins);
-    const int threads = warps * 32;
+    const int threads = SL.warps * 32;
     int per_sm = 1;
     if (f64) {
         auto kern = k_pairs_f64<MODE, AVG, W>;
@@ -943,17 +1323,22 @@ static int launch_pairs_t(const PairArgs &A, bool f64, int *launched)
         CF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, SL.total));
         if (per_sm < 1) per_sm = 1;
         kern<<<g_eng.num_sms * per_sm, threads, SL.total, g_eng.stream>>>(A, SL);
-        g_eng.launches++;
     } else {
         auto kern = k_pairs_f32<MODE, AVG, W>;
         CF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SL.total));
         CF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, SL.total));
         if (per_sm < 1) per_sm = 1;
         kern<<<g_eng.num_sms * per_sm, threads, SL.total, g_eng.stream>>>(A, SL);
-        g_eng.launches++;
     }
     CF_CUDA(cudaGetLastError());
+    g_eng.launches++;
     (*launched)++;
+    g_eng.last_blocks_per_sm = per_sm;
+    g_eng.last_warps_per_block = SL.warps;
+    g_eng.last_lane_stride = SL.lane_stride;
+    g_eng.last.blocks_per_sm = per_sm;
+    g_eng.last.warps_per_block = SL.warps;
+    g_eng.last.lane_stride = SL.lane_stride;
     return EXIT_SUCCESS;
 }
 
@@ -1214,6 +1599,9 @@ static int run_locked(cf_job *J, cf_hist *H)
     A.tasks = (const Task *)g_eng.tasks.p;
     A.ntasks = ntasks;
     A.nedges = J->nedges;
+    A.guard_search_top = 0;
+    while (2 * A.guard_search_top + (A.guard_search_top == 0) <= J->nedges - 1)
+        A.guard_search_top = A.guard_search_top ? 2 * A.guard_search_top : 1;
     A.nbins = nbins;
     A.npibin = J->npibin;
     A.autocorr = autocorr;
@@ -1251,6 +1639,55 @@ static int run_locked(cf_job *J, cf_hist *H)
     // keep both guard arrays non-decreasing (widening a band is always safe)
     for (int k = J->nedges - 2; k >= 0; k--) guards_h[k] = fminf(guards_h[k], guards_h[k + 1]);
     for (int k = 1; k < J->nedges; k++) guards_h[J->nedges + k] = fmaxf(guards_h[J->nedges + k], guards_h[J->nedges + k - 1]);
+    // bin lookup table on the float bits of the classified quantity: entry = number of lower
+    // guards <= the bucket's low end, flagged when a guard boundary (or a band) falls in the bucket
+    {
+        const float qlo = fmaxf(guards_h[0], 1e-30f);
+        A.q_floor = guards_h[0] <= 1e-30f ? 1e-30f : 0.f;
+        const float qhi = fmaxf(guards_h[2 * J->nedges - 1], qlo);
+        uint32_t blo, bhi;
+        memcpy(&blo, &qlo, 4);
+        memcpy(&bhi, &qhi, 4);
+        int shift = 1;
+        while (((bhi >> shift) - (blo >> shift)) + 1 > 4096u) shift++;
+        const int base = (int)(blo >> shift);
+        const int n = (int)((bhi >> shift) - (blo >> shift)) + 1;
+        if (ensure(g_eng.lut, sizeof(uint32_t) * (n + 1)) != EXIT_SUCCESS) return EXIT_FAILURE;
+        uint32_t *lut_h = (uint32_t *)malloc(sizeof(uint32_t) * (n + 1));
+        if (!lut_h) CF_FAIL("out of host memory");
+        // row byte offsets: the layout (private columns or shared row) is fixed before the launch
+        const int ls = choose_layout(mode, false, J->need_avg != 0, need_w, J->nedges, nbins, n).lane_stride;
+        const uint32_t ostride = (mode == MODE_RPPI || mode == MODE_SMU) ? (uint32_t)(J->npibin + 1) : 1u;
+        const uint32_t row_bytes = (uint32_t)(4 * ls);
+        const uint32_t trash = (uint32_t)nbins * row_bytes;
+        const float *glo_h = guards_h, *ghi_h = guards_h + J->nedges;
+        for (int t = 0; t < n; t++) {
+            const uint32_t ulo = (uint32_t)(base + t) << shift;
+            const uint32_t uhi = (((uint32_t)(base + t + 1)) << shift) - 1u;
+            float vlo, vhi;
+            memcpy(&vlo, &ulo, 4);
+            memcpy(&vhi, &uhi, 4);
+            int mlo = 0, mhi = 0;
+            while (mlo < J->nedges && glo_h[mlo] <= vlo) mlo++;
+            while (mhi < J->nedges && glo_h[mhi] <= vhi) mhi++;
+            const bool definite = (mlo == mhi) && mlo >= 1 && mlo < J->nedges && vlo >= ghi_h[mlo - 1] &&
+                                  vhi < ghi_h[J->nedges - 1];
+            lut_h[t] = definite ? (uint32_t)mlo * ostride * row_bytes : (trash | 0x80000000u);
+        }
+        lut_h[n] = trash;  // reject: below the first bucket (q < rmin^2) or above the last (q >= rmax^2)
+        CF_CUDA(cudaMemcpyAsync(g_eng.lut.p, lut_h, sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice, st));
+        CF_CUDA(cudaStreamSynchronize(st));
+        free(lut_h);
+        A.g_lut = (const uint32_t *)g_eng.lut.p;
+        A.trash_off = trash;
+        A.row_bytes = row_bytes;
+        A.lane_stride_hint = ls;
+        A.lut_shift = shift;
+        A.lut_base = base;
+        A.lut_mul = 1u << (32 - shift);
+        A.lut_negbase = (uint32_t)(-base);
+        A.lut_n = n;
+    }
     CF_CUDA(cudaMemcpyAsync(g_eng.edges.p, J->edges, sizeof(double) * J->nedges, cudaMemcpyHostToDevice, st));
     CF_CUDA(cudaMemcpyAsync(g_eng.guards.p, guards_h, sizeof(float) * 2 * J->nedges, cudaMemcpyHostToDevice, st));
     A.g_edges = (const double *)g_eng.edges.p;
@@ -1268,6 +1705,10 @@ static int run_locked(cf_job *J, cf_hist *H)
         // |t_f32 - t_ref| <= |dz err| * inv_dpi + FP32 rounding of the product (relative 2^-23 of t <= npibin)
         A.pibin_band = (float)(2.0 * (bz * A.inv_dpi + 3.0 * 5.96e-8 * (double)J->npibin + 1e-12));
         if (mode == MODE_WP) A.pibin_band = 0.f;
+        // fast path: round(|dz| * 256 / dpi) must stay below 2^22 for the magic-constant rounding
+        A.inv_dpi256_f = (float)(A.inv_dpi * 256.0);
+        A.pi_band_q = (int)ceil(A.pibin_band * 256.0) + 2;
+        if ((double)J->npibin * 256.0 > 4.0e6 || A.pi_band_q > 100) A.pi_band_q = 128;  // everything slow
     }
     if (mode == MODE_SMU) {
         A.sqr_mu_max = J->mu_max * J->mu_max;

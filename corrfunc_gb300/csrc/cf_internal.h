@@ -114,6 +114,10 @@ typedef struct {
     uint64_t tasks;
     int kernel_launches;
     int num_cells;
+    int blocks_per_sm;
+    int warps_per_block;
+    int lane_stride;
+    int reserved;
 } cf_engine_stats;
 int cf_engine_last_stats(cf_engine_stats *out);
 int cf_engine_fp32_peak(double *tflops);

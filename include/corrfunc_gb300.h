@@ -282,6 +282,10 @@ typedef struct {
     uint64_t tasks;
     int kernel_launches;
     int num_cells;
+    int blocks_per_sm;   /* launch shape of the last pair kernel */
+    int warps_per_block;
+    int lane_stride;     /* lanes l and l + lane_stride share one histogram column (32 = private) */
+    int reserved;
 } cf_gpu_stats;
 int cf_gpu_last_stats(cf_gpu_stats *out);
 

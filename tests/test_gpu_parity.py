@@ -247,3 +247,25 @@ def test_gpu_matches_reference_library_larger(gpu, reflibs, func):
         f = "thetaavg"
     assert np.array_equal(a["npairs"], b["npairs"])
     np.testing.assert_allclose(a[f], b[f], rtol=RTOL_AVG, atol=1e-12)
+
+
+@pytest.mark.parametrize("func", ["DD", "DDrppi", "DDsmu"])
+def test_gpu_zero_separation_pairs_with_rmin_zero(gpu, orc, func):
+    """Duplicated points (separation exactly 0) count in the first bin when rmin = 0."""
+    from corrfunc_gb300 import theory
+    rng = np.random.default_rng(17)
+    x, y, z = (rng.random(300) * 20.0 for _ in range(3))
+    x2, y2, z2 = np.concatenate([x, x[:50]]), np.concatenate([y, y[:50]]), np.concatenate([z, z[:50]])
+    bins = [0.0, 0.5, 1.0, 2.0]
+    kw = dict(X2=x2, Y2=y2, Z2=z2, periodic=False)
+    if func == "DD":
+        got = theory.DD(0, 1, bins, x, y, z, **kw)
+        want = orc.DD(0, bins, x, y, z, **kw)
+    elif func == "DDrppi":
+        got = theory.DDrppi(0, 1, 3.0, bins, x, y, z, **kw)
+        want = orc.DDrppi(0, 3.0, bins, x, y, z, **kw)
+    else:
+        got = theory.DDsmu(0, 1, bins, 1.0, 4, x, y, z, **kw)
+        want = orc.DDsmu(0, bins, 1.0, 4, x, y, z, **kw)
+    assert np.array_equal(got["npairs"], want["npairs"])
+    assert int(got["npairs"].sum()) > 0
