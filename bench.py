@@ -45,9 +45,10 @@ WORKLOADS = {
 }
 WORKLOAD = dict(WORKLOADS["cfg2"])
 FLOP_PER_PAIR = 8  # 3 FADD + 1 FMUL + 2 FFMA per 3-D separation
-# dram__bytes_read.sum + dram__bytes_write.sum of one pair-kernel launch on this workload,
-# from the ncu capture summarised in profiles/ (None until captured)
-PAIR_KERNEL_TRAFFIC_BYTES = None
+# dram__bytes_read.sum + dram__bytes_write.sum of one FP32 pair-kernel launch per workload, from
+# the ncu captures summarised in profiles/k_pairs_f32_cfg2_dram_traffic.md and
+# profiles/k_pairs_f32_northstar_full.md
+PAIR_KERNEL_TRAFFIC_BYTES = {"cfg2": 220_670_976 + 3_506_688, "northstar": 54_269_440 + 1_935_104}
 
 
 def _rank_env():
@@ -361,7 +362,7 @@ def main():
     lib.cf_gpu_fp32_peak_tflops(ctypes.byref(peak))
     pair_s = sum(pair_ms) / 1e3 / args.steps
     achieved = work * FLOP_PER_PAIR / pair_s / 1e12
-    traffic = PAIR_KERNEL_TRAFFIC_BYTES
+    traffic = PAIR_KERNEL_TRAFFIC_BYTES.get(args.workload) if args.precision == "fp32_refine" else None
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": sum(gpu_ms) / args.steps, "higher_is_better": True,
