@@ -1311,7 +1311,6 @@ template <int MODE, bool AVG, bool W>
 static int launch_pairs_t(const PairArgs &A, bool f64, int *launched)
 {
     const int nedges = A.nedges;
-    constexpr bool DZ = (MODE == MODE_RPPI || MODE == MODE_WP || MODE == MODE_SMU);
     SmemLayout SL = choose_layout(MODE, f64, AVG, W, nedges, A.nbins, A.lut_n);
     if (!f64 && SL.lane_stride != A.lane_stride_hint) CF_FAIL("internal: histogram layout changed after the table was built");
     if (SL.total > 220 * 1024) CF_FAIL("histogram too large for on-chip accumulation (%d bins)", A.nbins);
