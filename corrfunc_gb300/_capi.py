@@ -133,6 +133,10 @@ class GpuStats(Structure):
 
 
 _GPU_PROTOS["cf_gpu_last_stats"] = ([POINTER(GpuStats)], c_int)
+_GPU_PROTOS["cf_gpu_countpairs_cross_noalloc"] = (
+    [c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
+     POINTER(c_double), c_int, c_double, c_double, c_double, c_int, POINTER(c_uint64), POINTER(c_double),
+     POINTER(c_double), c_void_p], c_int)
 
 PACKAGE_DIR = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PACKAGE_DIR, "libcorrfunc_gb300.so")

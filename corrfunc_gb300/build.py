@@ -50,15 +50,18 @@ def build(verbose=False, extra_nvcc=()):
         obj = os.path.join(BUILD, c[:-2] + ".o")
         jobs.append(["gcc", "-std=gnu11", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
                     + inc + ["-c", os.path.join(CSRC, c), "-o", obj])
-    cu_obj = os.path.join(BUILD, "cf_engine.o")
-    jobs.append([nvcc] + NVCC_ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
-                                      "-Xcompiler", "-ffp-contract=off"] + list(extra_nvcc) + inc
-                + ["-c", os.path.join(CSRC, "cf_engine.cu"), "-o", cu_obj])
+    cu_objs = []
+    for cu in ("cf_engine.cu", "cf_noalloc.cu"):
+        obj = os.path.join(BUILD, cu[:-3] + ".o")
+        cu_objs.append(obj)
+        jobs.append([nvcc] + NVCC_ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
+                                          "-Xcompiler", "-ffp-contract=off"] + list(extra_nvcc) + inc
+                    + ["-c", os.path.join(CSRC, cu), "-o", obj])
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         for r in ex.map(_run, jobs):
             if verbose and (r.stdout or r.stderr):
                 print(r.stdout, r.stderr)
-    objs = [os.path.join(BUILD, "cf_api.o"), os.path.join(BUILD, "cf_common.o"), cu_obj]
+    objs = [os.path.join(BUILD, "cf_api.o"), os.path.join(BUILD, "cf_common.o")] + cu_objs
     tmp = LIB + ".tmp"
     _run([nvcc] + NVCC_ARCH + ["-shared", "-o", tmp] + objs
          + ["-L" + os.path.join(cuda, "lib64"), "-lcudart_static", "-lpthread", "-ldl", "-lrt", "-lm"])

@@ -310,6 +310,38 @@ int cf_reference_candidate_pairs(const int64_t ND1, void *X1, void *Y1, void *Z1
                                  const int autocorr, const char *binfile,
                                  struct config_options *options, uint64_t *candidates);
 
+/* DD(r) cross-correlation (autocorr = 0) of two catalogues resident on the current CUDA device,
+ * by direct summation over all ND1 * ND2 pairs in double precision, for callers that must not
+ * allocate memory inside the call (device memory reserved up front, no cudaMalloc/cudaFree and
+ * the synchronisation they may bring, no host heap).  No counterpart in the reference.
+ *
+ *   X1..W2     device pointers to double arrays; W1 and W2 both NULL (no weights) or both set
+ *              (pair_product weights).
+ *   edges      host array of the nedges bin edges as a bin file lists them (rmin, then each
+ *              upper edge); 2 <= nedges <= 128, larger values are rejected with an error.
+ *   periodic   minimum-image wrapping with the given box sizes (boxsize_y/_z <= 0 take
+ *              boxsize_x); needs rmax < 0.49 * box size along every axis.
+ *   instruction_set  the reference isa whose double-precision formula the counts follow
+ *              (AVX512F chains fused multiply-adds, the others do not; < 0 picks this host's).
+ *   npairs, ravg, weightavg  caller-provided host arrays of nedges entries (ravg / weightavg
+ *              may be NULL); entry k counts edges[k-1] <= r < edges[k], entry 0 stays 0, and
+ *              averages are normalised as countpairs() does.
+ *   stream     the cudaStream_t to run on (NULL: the default stream); the call returns after
+ *              the stream has drained.
+ *
+ * Scratch is a fixed 4 KB device array inside the library.  The first call on each device looks
+ * up its address (set-up); make that first call before any stream capture begins.  Each call
+ * writes the squared edges and zeros over the accumulators itself, so nothing has to be cleared
+ * beforehand.  All calls on one device share that array: calls that overlap in time (two host
+ * threads, or two streams) race and corrupt each other's counts, so serialise them.  Cost grows
+ * as ND1 * ND2, so this is meant for small catalogues. */
+int cf_gpu_countpairs_cross_noalloc(const int64_t ND1, const double *X1, const double *Y1, const double *Z1,
+                                    const double *W1, const int64_t ND2, const double *X2, const double *Y2,
+                                    const double *Z2, const double *W2, const int nedges, const double *edges,
+                                    const int periodic, const double boxsize_x, const double boxsize_y,
+                                    const double boxsize_z, const int instruction_set, uint64_t *npairs,
+                                    double *ravg, double *weightavg, void *stream);
+
 /* ---------------- header-only helpers (utils/defs.h:158-346, 369-419) ----------------
  * Callers compile these themselves, exactly as with the reference header. */
 
