@@ -119,13 +119,24 @@ __global__ void k_minmax(const T *x, const T *y, const T *z, const T *w, int64_t
             v[k] = (k & 1) || k == 6 ? fmax(v[k], o) : fmin(v[k], o);
         }
     }
-    if (bad) atomicMax(&mm[7], 1ull);
-    if ((threadIdx.x & 31) == 0) {
-        for (int k = 0; k < 7; k++) {
-            const unsigned long long e = ord_enc(v[k]);
-            if ((k & 1) || k == 6) atomicMax(&mm[k], e); else atomicMin(&mm[k], e);
-        }
+    // one set of atomics per block (blockDim.x <= 256)
+    __shared__ double part[8][7];
+    __shared__ int any_bad;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    if (threadIdx.x == 0) any_bad = 0;
+    __syncthreads();
+    if (bad) any_bad = 1;
+    if (lane == 0)
+        for (int k = 0; k < 7; k++) part[warp][k] = v[k];
+    __syncthreads();
+    if (threadIdx.x < 7) {
+        const int k = threadIdx.x;
+        double r = part[0][k];
+        for (int q = 1; q < nwarps; q++) r = (k & 1) || k == 6 ? fmax(r, part[q][k]) : fmin(r, part[q][k]);
+        const unsigned long long e = ord_enc(r);
+        if ((k & 1) || k == 6) atomicMax(&mm[k], e); else atomicMin(&mm[k], e);
     }
+    if (threadIdx.x == 0 && any_bad) atomicMax(&mm[7], 1ull);
 }
 
 __device__ __forceinline__ int axis_cell(double c, const Geom &g, int a)
@@ -681,7 +692,7 @@ __device__ __forceinline__ uint32_t pair_offset(const PairArgs &A, const float4 
     else q = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, A.q_floor)));
     const uint32_t e = lut[lut_bucket(A, q)];
     uint32_t off = e & 0x7fffffffu;
-    slow = e >> 31;
+    slow = e;  // bit 31: flagged bucket
     if (OWN) {
         const bool keep = jb + (uint32_t)k > i;
         off = keep ? off : A.trash_off;
@@ -711,7 +722,7 @@ __device__ __forceinline__ uint32_t pair_offset(const PairArgs &A, const float4 
                 add = (uint32_t)min(v >> 8, A.npibin) * A.row_bytes;
             }
         }
-        slow = (!rej && (slow || (real && amb))) ? 1u : 0u;
+        slow = (!rej && ((slow >> 31) || (real && amb))) ? 0x80000000u : 0u;
         off = (real && !rej && !amb) ? off + add : A.trash_off;
     }
     if (NEED_W) vw = __float2ll_rn(wis * pj.w);
@@ -748,7 +759,7 @@ __device__ __forceinline__ void pairs_group(const PairArgs &A, const float4 *__r
         va[u] = 0;
         off[u] = pair_offset<MODE, NEED_AVG, NEED_W, OWN>(A, sjhi, sjlo, lut, k0 + u, jb, i, xi, yi, zi, xil, yil, zil,
                                                           wis, sl, vw[u], va[u]);
-        slowbits += sl << (k0 + u);
+        slowbits = __funnelshift_l(sl, slowbits, 1);  // pair k of n ends at bit n - 1 - k
     }
 #pragma unroll
     for (int u = 0; u < U; u++) {
@@ -918,7 +929,7 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
                     slowbits ^= 1u << b;
                     RefineEntry r;
                     r.i = i;
-                    r.j = jb + (uint32_t)b;
+                    r.j = jb + (uint32_t)(nj - 1 - b);  // bit n - 1 - k holds pair k
                     r.meta = T.meta;
                     sq[sq_n + __popc(want & ((1u << lane) - 1u))] = r;
                 }
@@ -1069,6 +1080,26 @@ static int ensure(DevBuf &b, size_t bytes)
     return EXIT_SUCCESS;
 }
 
+// pinned host staging (small uploads and the histogram read-back go through it, so none of
+// those copies waits on the host); only grown between calls, after the stream has drained
+struct HostBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+};
+
+static int ensure_host(HostBuf &b, size_t bytes)
+{
+    if (bytes == 0) bytes = 16;
+    if (b.cap >= bytes) return EXIT_SUCCESS;
+    if (b.p) cudaFreeHost(b.p);
+    b.p = nullptr;
+    b.cap = 0;
+    size_t want = bytes + bytes / 4;
+    CF_CUDA(cudaHostAlloc(&b.p, want, cudaHostAllocDefault));
+    b.cap = want;
+    return EXIT_SUCCESS;
+}
+
 struct SetBufs {
     DevBuf raw[4];  // device copies of x, y, z, w as given (float or double)
     const void *in[4];  // arrays the lattice is built from: raw[] or caller-owned device arrays
@@ -1085,6 +1116,8 @@ struct Engine {
     SetBufs set[2];
     DevBuf mm, oob, scan_tmp[4], chunk_cnt, chunk_off, chunk_begin, chunk_count, ntask, task_off, tasks;
     DevBuf hist_cnt, hist_avg, hist_w, stats, counter, edges, guards, lut;
+    HostBuf h_small, h_tab, h_hist;
+    int regs_cache[5][4][2] = {};  // registers per thread of each pair kernel (0 = not queried)
     int precision = CF_PRECISION_FP32_REFINE;
     int launches = 0;  // kernels launched by the current call
     size_t smem_per_sm = 228 * 1024;
@@ -1199,7 +1232,9 @@ static int upload_and_minmax(int s, int64_t n, const void *x, const void *y, con
         CF_CUDA(cudaMemcpyAsync(B.raw[k].p, src[k], bytes, cudaMemcpyHostToDevice, g_eng.stream));
         B.in[k] = B.raw[k].p;
     }
-    k_minmax<T><<<grid_for(n, 256), 256, 0, g_eng.stream>>>((const T *)B.in[0], (const T *)B.in[1],
+    int mgrid = grid_for(n, 256);
+    if (mgrid > 4 * g_eng.num_sms) mgrid = 4 * g_eng.num_sms;
+    k_minmax<T><<<mgrid, 256, 0, g_eng.stream>>>((const T *)B.in[0], (const T *)B.in[1],
                                                             (const T *)B.in[2], (const T *)B.in[3], n, mm_dev);
     CF_CUDA(cudaGetLastError());
     g_eng.launches++;
@@ -1262,13 +1297,16 @@ static int pair_kernel_regs_m(bool f64, bool avg, bool w)
 
 static int pair_kernel_regs(int mode, bool f64, bool avg, bool w)
 {
+    int &c = g_eng.regs_cache[mode < 0 || mode > 4 ? 4 : mode][(avg ? 2 : 0) + (w ? 1 : 0)][f64 ? 1 : 0];
+    if (c > 0) return c;
     switch (mode) {
-    case MODE_R3: return pair_kernel_regs_m<MODE_R3>(f64, avg, w);
-    case MODE_RPPI: return pair_kernel_regs_m<MODE_RPPI>(f64, avg, w);
-    case MODE_WP: return pair_kernel_regs_m<MODE_WP>(f64, avg, w);
-    case MODE_SMU: return pair_kernel_regs_m<MODE_SMU>(f64, avg, w);
-    default: return pair_kernel_regs_m<MODE_THETA>(f64, avg, w);
+    case MODE_R3: c = pair_kernel_regs_m<MODE_R3>(f64, avg, w); break;
+    case MODE_RPPI: c = pair_kernel_regs_m<MODE_RPPI>(f64, avg, w); break;
+    case MODE_WP: c = pair_kernel_regs_m<MODE_WP>(f64, avg, w); break;
+    case MODE_SMU: c = pair_kernel_regs_m<MODE_SMU>(f64, avg, w); break;
+    default: c = pair_kernel_regs_m<MODE_THETA>(f64, avg, w); break;
     }
+    return c;
 }
 
 // Histogram layout and block size.  Lanes l and l + lane_stride share a column; the score is the
@@ -1370,6 +1408,94 @@ static double edge_band(double e, double delta)
     return 2.0 * (3.1 * u * fabs(e) + 2.0 * re * delta + delta * delta + 1e-14 * (fabs(e) + 1.0));
 }
 
+// Error bands, guards and the bucket table of one call, built on the host into pinned memory
+// and uploaded stream-ordered (no host wait); done while the lattice kernels run.
+struct Tables {
+    int lut_n, shift, base, ls;
+    uint32_t row_bytes, trash;
+    float q_floor;
+    double dxy, d3;
+};
+
+static int build_tables(const cf_job *J, int mode, int nbins, bool need_w, const double delta[3], Tables *T)
+{
+    cudaStream_t st = g_eng.stream;
+    // coordinate error bounds
+    const double dxy = sqrt(delta[0] * delta[0] + delta[1] * delta[1]);
+    const double d3 = sqrt(dxy * dxy + delta[2] * delta[2]);
+    T->dxy = dxy;
+    T->d3 = d3;
+    const double dlim = (mode == MODE_RPPI || mode == MODE_WP) ? dxy : d3;
+    // guards: for theta the classified quantity is the squared chord 2*(1 - cos)
+    if (ensure(g_eng.edges, sizeof(double) * J->nedges) || ensure(g_eng.guards, sizeof(float) * 2 * J->nedges))
+        return EXIT_FAILURE;
+    const size_t tab_bytes = sizeof(double) * CF_MAX_EDGES + sizeof(float) * 2 * CF_MAX_EDGES + sizeof(uint32_t) * 4100;
+    if (ensure_host(g_eng.h_tab, tab_bytes) != EXIT_SUCCESS) return EXIT_FAILURE;
+    double *edges_h = (double *)g_eng.h_tab.p;
+    float *guards_h = (float *)(edges_h + CF_MAX_EDGES);
+    uint32_t *lut_h = (uint32_t *)(guards_h + 2 * CF_MAX_EDGES);
+    memcpy(edges_h, J->edges, sizeof(double) * J->nedges);
+    for (int k = 0; k < J->nedges; k++) {
+        double e = J->edges[k];
+        double band;
+        if (mode == MODE_THETA) {
+            e = 2.0 * (1.0 - J->edges[k]);
+            band = edge_band(e, dlim) + 8e-15;
+        } else {
+            band = edge_band(e, dlim);
+        }
+        guards_h[k] = f_down(e - band);
+        guards_h[J->nedges + k] = f_up(e + band);
+    }
+    // keep both guard arrays non-decreasing (widening a band is always safe)
+    for (int k = J->nedges - 2; k >= 0; k--) guards_h[k] = fminf(guards_h[k], guards_h[k + 1]);
+    for (int k = 1; k < J->nedges; k++) guards_h[J->nedges + k] = fmaxf(guards_h[J->nedges + k], guards_h[J->nedges + k - 1]);
+    // bin lookup table on the float bits of the classified quantity: entry = byte offset of the
+    // histogram row of the bucket's bin, or the trash row flagged (bit 31) when a guard boundary
+    // (or a band) falls in the bucket
+    const float qlo = fmaxf(guards_h[0], 1e-30f);
+    T->q_floor = guards_h[0] <= 1e-30f ? 1e-30f : 0.f;
+    const float qhi = fmaxf(guards_h[2 * J->nedges - 1], qlo);
+    uint32_t blo, bhi;
+    memcpy(&blo, &qlo, 4);
+    memcpy(&bhi, &qhi, 4);
+    int shift = 1;
+    while (((bhi >> shift) - (blo >> shift)) + 1 > 4096u) shift++;
+    const int base = (int)(blo >> shift);
+    const int n = (int)((bhi >> shift) - (blo >> shift)) + 1;
+    if (ensure(g_eng.lut, sizeof(uint32_t) * (n + 1)) != EXIT_SUCCESS) return EXIT_FAILURE;
+    // row byte offsets: the layout (private columns or shared row) is fixed before the launch
+    const int ls = choose_layout(mode, false, J->need_avg != 0, need_w, J->nedges, nbins, n).lane_stride;
+    const uint32_t ostride = (mode == MODE_RPPI || mode == MODE_SMU) ? (uint32_t)(J->npibin + 1) : 1u;
+    const uint32_t row_bytes = (uint32_t)(4 * ls);
+    const uint32_t trash = (uint32_t)nbins * row_bytes;
+    const float *glo_h = guards_h, *ghi_h = guards_h + J->nedges;
+    int mlo = 0, mhi = 0;  // both non-decreasing in the bucket index
+    for (int t = 0; t < n; t++) {
+        const uint32_t ulo = (uint32_t)(base + t) << shift;
+        const uint32_t uhi = (((uint32_t)(base + t + 1)) << shift) - 1u;
+        float vlo, vhi;
+        memcpy(&vlo, &ulo, 4);
+        memcpy(&vhi, &uhi, 4);
+        while (mlo < J->nedges && glo_h[mlo] <= vlo) mlo++;
+        while (mhi < J->nedges && glo_h[mhi] <= vhi) mhi++;
+        const bool definite = (mlo == mhi) && mlo >= 1 && mlo < J->nedges && vlo >= ghi_h[mlo - 1] &&
+                              vhi < ghi_h[J->nedges - 1];
+        lut_h[t] = definite ? (uint32_t)mlo * ostride * row_bytes : (trash | 0x80000000u);
+    }
+    lut_h[n] = trash;  // reject: below the first bucket (q < rmin^2) or above the last (q >= rmax^2)
+    CF_CUDA(cudaMemcpyAsync(g_eng.lut.p, lut_h, sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice, st));
+    CF_CUDA(cudaMemcpyAsync(g_eng.edges.p, edges_h, sizeof(double) * J->nedges, cudaMemcpyHostToDevice, st));
+    CF_CUDA(cudaMemcpyAsync(g_eng.guards.p, guards_h, sizeof(float) * 2 * J->nedges, cudaMemcpyHostToDevice, st));
+    T->lut_n = n;
+    T->shift = shift;
+    T->base = base;
+    T->ls = ls;
+    T->row_bytes = row_bytes;
+    T->trash = trash;
+    return EXIT_SUCCESS;
+}
+
 static int run_locked(cf_job *J, cf_hist *H)
 {
     if (engine_init() != EXIT_SUCCESS) return EXIT_FAILURE;
@@ -1391,13 +1517,16 @@ static int run_locked(cf_job *J, cf_hist *H)
     const bool isf = J->elem_size == 4;
     const bool need_w = J->need_weight != 0;
 
+    CF_CUDA(cudaStreamSynchronize(st));  // pinned staging is reused: nothing of a failed call may be pending
     CF_CUDA(cudaEventRecord(g_eng.ev[0], st));
     // ---- upload + extent ----
     if (ensure(g_eng.mm, sizeof(unsigned long long) * 16) != EXIT_SUCCESS) return EXIT_FAILURE;
     unsigned long long *mm = (unsigned long long *)g_eng.mm.p;
-    unsigned long long mm_init[16];
+    if (ensure_host(g_eng.h_small, sizeof(unsigned long long) * 32) != EXIT_SUCCESS) return EXIT_FAILURE;
+    unsigned long long *mm_init = (unsigned long long *)g_eng.h_small.p;
+    unsigned long long *mmh = mm_init + 16;
     for (int k = 0; k < 16; k++) mm_init[k] = (k % 8 == 6 || k % 8 == 7 || (k % 8) % 2 == 1) ? 0ull : ~0ull;
-    CF_CUDA(cudaMemcpyAsync(mm, mm_init, sizeof(mm_init), cudaMemcpyHostToDevice, st));
+    CF_CUDA(cudaMemcpyAsync(mm, mm_init, sizeof(unsigned long long) * 16, cudaMemcpyHostToDevice, st));
     const int nsets = autocorr ? 1 : 2;
     for (int s = 0; s < nsets; s++) {
         const int64_t n = s ? n2 : n1;
@@ -1409,8 +1538,7 @@ static int run_locked(cf_job *J, cf_hist *H)
         if (rc != EXIT_SUCCESS) return EXIT_FAILURE;
     }
     const bool dev_float = isf;
-    unsigned long long mmh[16];
-    CF_CUDA(cudaMemcpyAsync(mmh, mm, sizeof(mmh), cudaMemcpyDeviceToHost, st));
+    CF_CUDA(cudaMemcpyAsync(mmh, mm, sizeof(unsigned long long) * 16, cudaMemcpyDeviceToHost, st));
     CF_CUDA(cudaStreamSynchronize(st));
     double lo[3], hi[3], wmax[2] = {0, 0};
     for (int a = 0; a < 3; a++) {
@@ -1499,6 +1627,8 @@ static int run_locked(cf_job *J, cf_hist *H)
     }
     SetBufs &S1 = g_eng.set[0];
     SetBufs &S2 = g_eng.set[nsets - 1];
+    Tables T;
+    if (build_tables(J, mode, nbins, need_w, delta, &T) != EXIT_SUCCESS) return EXIT_FAILURE;
 
     // ---- chunks ----
     if (ensure(g_eng.chunk_cnt, sizeof(uint32_t) * ncols) || ensure(g_eng.chunk_off, sizeof(uint32_t) * ((size_t)ncols + 1)))
@@ -1615,80 +1745,17 @@ static int run_locked(cf_job *J, cf_hist *H)
             A.olo[a][m + 1] = (float)(o - oh);
         }
     }
-    // coordinate error bounds
-    const double dxy = sqrt(delta[0] * delta[0] + delta[1] * delta[1]);
-    const double d3 = sqrt(dxy * dxy + delta[2] * delta[2]);
-    const double dlim = (mode == MODE_RPPI || mode == MODE_WP) ? dxy : d3;
-    // guards: for theta the classified quantity is the squared chord 2*(1 - cos)
-    if (ensure(g_eng.edges, sizeof(double) * J->nedges) || ensure(g_eng.guards, sizeof(float) * 2 * J->nedges))
-        return EXIT_FAILURE;
-    float guards_h[2 * CF_MAX_EDGES];
-    for (int k = 0; k < J->nedges; k++) {
-        double e = J->edges[k];
-        double band;
-        if (mode == MODE_THETA) {
-            e = 2.0 * (1.0 - J->edges[k]);
-            band = edge_band(e, dlim) + 8e-15;
-        } else {
-            band = edge_band(e, dlim);
-        }
-        guards_h[k] = f_down(e - band);
-        guards_h[J->nedges + k] = f_up(e + band);
-    }
-    // keep both guard arrays non-decreasing (widening a band is always safe)
-    for (int k = J->nedges - 2; k >= 0; k--) guards_h[k] = fminf(guards_h[k], guards_h[k + 1]);
-    for (int k = 1; k < J->nedges; k++) guards_h[J->nedges + k] = fmaxf(guards_h[J->nedges + k], guards_h[J->nedges + k - 1]);
-    // bin lookup table on the float bits of the classified quantity: entry = number of lower
-    // guards <= the bucket's low end, flagged when a guard boundary (or a band) falls in the bucket
-    {
-        const float qlo = fmaxf(guards_h[0], 1e-30f);
-        A.q_floor = guards_h[0] <= 1e-30f ? 1e-30f : 0.f;
-        const float qhi = fmaxf(guards_h[2 * J->nedges - 1], qlo);
-        uint32_t blo, bhi;
-        memcpy(&blo, &qlo, 4);
-        memcpy(&bhi, &qhi, 4);
-        int shift = 1;
-        while (((bhi >> shift) - (blo >> shift)) + 1 > 4096u) shift++;
-        const int base = (int)(blo >> shift);
-        const int n = (int)((bhi >> shift) - (blo >> shift)) + 1;
-        if (ensure(g_eng.lut, sizeof(uint32_t) * (n + 1)) != EXIT_SUCCESS) return EXIT_FAILURE;
-        uint32_t *lut_h = (uint32_t *)malloc(sizeof(uint32_t) * (n + 1));
-        if (!lut_h) CF_FAIL("out of host memory");
-        // row byte offsets: the layout (private columns or shared row) is fixed before the launch
-        const int ls = choose_layout(mode, false, J->need_avg != 0, need_w, J->nedges, nbins, n).lane_stride;
-        const uint32_t ostride = (mode == MODE_RPPI || mode == MODE_SMU) ? (uint32_t)(J->npibin + 1) : 1u;
-        const uint32_t row_bytes = (uint32_t)(4 * ls);
-        const uint32_t trash = (uint32_t)nbins * row_bytes;
-        const float *glo_h = guards_h, *ghi_h = guards_h + J->nedges;
-        for (int t = 0; t < n; t++) {
-            const uint32_t ulo = (uint32_t)(base + t) << shift;
-            const uint32_t uhi = (((uint32_t)(base + t + 1)) << shift) - 1u;
-            float vlo, vhi;
-            memcpy(&vlo, &ulo, 4);
-            memcpy(&vhi, &uhi, 4);
-            int mlo = 0, mhi = 0;
-            while (mlo < J->nedges && glo_h[mlo] <= vlo) mlo++;
-            while (mhi < J->nedges && glo_h[mhi] <= vhi) mhi++;
-            const bool definite = (mlo == mhi) && mlo >= 1 && mlo < J->nedges && vlo >= ghi_h[mlo - 1] &&
-                                  vhi < ghi_h[J->nedges - 1];
-            lut_h[t] = definite ? (uint32_t)mlo * ostride * row_bytes : (trash | 0x80000000u);
-        }
-        lut_h[n] = trash;  // reject: below the first bucket (q < rmin^2) or above the last (q >= rmax^2)
-        CF_CUDA(cudaMemcpyAsync(g_eng.lut.p, lut_h, sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice, st));
-        CF_CUDA(cudaStreamSynchronize(st));
-        free(lut_h);
-        A.g_lut = (const uint32_t *)g_eng.lut.p;
-        A.trash_off = trash;
-        A.row_bytes = row_bytes;
-        A.lane_stride_hint = ls;
-        A.lut_shift = shift;
-        A.lut_base = base;
-        A.lut_mul = 1u << (32 - shift);
-        A.lut_negbase = (uint32_t)(-base);
-        A.lut_n = n;
-    }
-    CF_CUDA(cudaMemcpyAsync(g_eng.edges.p, J->edges, sizeof(double) * J->nedges, cudaMemcpyHostToDevice, st));
-    CF_CUDA(cudaMemcpyAsync(g_eng.guards.p, guards_h, sizeof(float) * 2 * J->nedges, cudaMemcpyHostToDevice, st));
+    const double dxy = T.dxy, d3 = T.d3;
+    A.g_lut = (const uint32_t *)g_eng.lut.p;
+    A.trash_off = T.trash;
+    A.row_bytes = T.row_bytes;
+    A.lane_stride_hint = T.ls;
+    A.lut_shift = T.shift;
+    A.lut_base = T.base;
+    A.lut_mul = 1u << (32 - T.shift);
+    A.lut_negbase = (uint32_t)(-T.base);
+    A.lut_n = T.lut_n;
+    A.q_floor = T.q_floor;
     A.g_edges = (const double *)g_eng.edges.p;
     A.g_guard = (const float *)g_eng.guards.p;
     A.dz_err = (float)(2.0 * delta[2]);
@@ -1752,13 +1819,19 @@ static int run_locked(cf_job *J, cf_hist *H)
         if (launch_pairs(mode, A, f64, J->need_avg != 0, need_w, &launched) != EXIT_SUCCESS) return EXIT_FAILURE;
     }
     CF_CUDA(cudaEventRecord(g_eng.ev[3], st));
-    unsigned long long stats_h[4];
-    CF_CUDA(cudaMemcpyAsync(H->npairs, g_eng.hist_cnt.p, sizeof(uint64_t) * nbins, cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaMemcpyAsync(H->avg, g_eng.hist_avg.p, sizeof(double) * nbins, cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaMemcpyAsync(H->wsum, g_eng.hist_w.p, sizeof(double) * nbins, cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaMemcpyAsync(stats_h, g_eng.stats.p, sizeof(stats_h), cudaMemcpyDeviceToHost, st));
+    if (ensure_host(g_eng.h_hist, sizeof(uint64_t) * (3 * (size_t)nbins + 4)) != EXIT_SUCCESS) return EXIT_FAILURE;
+    uint64_t *cnt_h = (uint64_t *)g_eng.h_hist.p;
+    double *avg_h = (double *)(cnt_h + nbins), *w_h = avg_h + nbins;
+    unsigned long long *stats_h = (unsigned long long *)(w_h + nbins);
+    CF_CUDA(cudaMemcpyAsync(cnt_h, g_eng.hist_cnt.p, sizeof(uint64_t) * nbins, cudaMemcpyDeviceToHost, st));
+    CF_CUDA(cudaMemcpyAsync(avg_h, g_eng.hist_avg.p, sizeof(double) * nbins, cudaMemcpyDeviceToHost, st));
+    CF_CUDA(cudaMemcpyAsync(w_h, g_eng.hist_w.p, sizeof(double) * nbins, cudaMemcpyDeviceToHost, st));
+    CF_CUDA(cudaMemcpyAsync(stats_h, g_eng.stats.p, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost, st));
     CF_CUDA(cudaEventRecord(g_eng.ev[4], st));
     CF_CUDA(cudaStreamSynchronize(st));
+    memcpy(H->npairs, cnt_h, sizeof(uint64_t) * nbins);
+    memcpy(H->avg, avg_h, sizeof(double) * nbins);
+    memcpy(H->wsum, w_h, sizeof(double) * nbins);
     float ms_pairs = 0.f, ms_grid = 0.f, ms_total = 0.f;
     CF_CUDA(cudaEventElapsedTime(&ms_pairs, g_eng.ev[2], g_eng.ev[3]));
     CF_CUDA(cudaEventElapsedTime(&ms_grid, g_eng.ev[0], g_eng.ev[1]));
