@@ -43,6 +43,12 @@ WORKLOADS = {
                       n1=1_000_000, n2=0, boxsize=420.0, nbins=20, rmin=0.1, rmax=25.0, seeds=[0],
                       weights=None, kind="uniform", autocorr=1),
 }
+WORKLOADS["cfg5"] = dict(workload="batched DD cross-correlations: 64 clustered catalogues of 50,000-500,000 points "
+                                   "(log-uniform sizes) against one 5,000,000-point uniform catalogue, periodic "
+                                   "L=1000, 20 log bins 0.1-25, float32 positions, pair_product weights U[0.5,1.5]",
+                          nbatch=64, nmin=50_000, nmax=500_000, n2=5_000_000, boxsize=1000.0, nbins=20, rmin=0.1,
+                          rmax=25.0, size_seed=100, seeds="0-63", random_seed=1000, weights="U[0.5,1.5]",
+                          kind="batched", autocorr=0)
 WORKLOAD = dict(WORKLOADS["cfg2"])
 FLOP_PER_PAIR = 8  # 3 FADD + 1 FMUL + 2 FFMA per 3-D separation
 # dram__bytes_read.sum + dram__bytes_write.sum of one FP32 pair-kernel launch per workload, from
@@ -203,9 +209,219 @@ def cpu_reference_run(set1, set2, bins, nthreads, dtype, frac=1.0):
     return dt, work, n1, n2
 
 
+def make_batch_workload():
+    from corrfunc_gb300 import catalogs as cat
+    W = WORKLOAD
+    rng = np.random.default_rng(W["size_seed"])
+    sizes = np.round(np.exp(rng.uniform(np.log(W["nmin"]), np.log(W["nmax"]), W["nbatch"]))).astype(np.int64)
+    L = W["boxsize"]
+    cats = []
+    for k, n in enumerate(sizes):
+        x, y, z = cat.clustered_box(int(n), L, k, dtype=np.float32)
+        cats.append((x, y, z, cat.weights(int(n), 200 + k, dtype=np.float32)))
+    x, y, z = cat.uniform_box(W["n2"], L, W["random_seed"], dtype=np.float32)
+    rand = (x, y, z, cat.weights(W["n2"], 2000, dtype=np.float32))
+    bins = cat.log_bins(W["rmin"], W["rmax"], W["nbins"])
+    return cats, rand, bins
+
+
+def run_batch_workload(args):
+    """Configuration 5: all catalogues in one replayed CUDA graph (one pair-kernel launch) against
+    the same catalogues counted by 64 sequential countpairs() calls."""
+    rank, world, local = _rank_env()
+    import torch
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import corrfunc_gb300
+    from corrfunc_gb300 import _capi as C
+    from corrfunc_gb300 import theory
+    lib = corrfunc_gb300.library()
+    lib.cf_gpu_countpairs_device.argtypes = lib.countpairs.argtypes
+    lib.cf_gpu_countpairs_device.restype = ctypes.c_int
+    lib.cf_gpu_fp32_peak_tflops.argtypes = [ctypes.POINTER(ctypes.c_double)]
+    corrfunc_gb300.set_precision(args.precision)
+    cats, rand, bins = make_batch_workload()
+    L = WORKLOAD["boxsize"]
+    binf = C.BinFile(bins)
+    binfile = binf.__enter__()
+    work = sum(reference_work(lib, C, c, rand, binfile, np.float32) for c in cats)
+
+    dcats = [[torch.from_numpy(a).to(dev) for a in c] for c in cats]
+    drand = [torch.from_numpy(a).to(dev) for a in rand]
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    batch = theory.DDCrossBatch(bins, dcats, drand, periodic=True, boxsize=L, weight_type="pair_product",
+                                autotune=True)
+    plan_s = time.perf_counter() - t0
+    o = options_for(C, L, np.float32)
+
+    def one_plain(k):
+        c = dcats[k]
+        e = extra_for(C, c[3].data_ptr(), drand[3].data_ptr())
+        res = C.ResultsDD()
+        rc = lib.cf_gpu_countpairs_device(len(cats[k][0]), *(ctypes.c_void_p(t.data_ptr()) for t in c[:3]),
+                                          WORKLOAD["n2"], *(ctypes.c_void_p(t.data_ptr()) for t in drand[:3]), 1, 0,
+                                          binfile.encode(), ctypes.byref(res), ctypes.byref(o), ctypes.byref(e))
+        if rc != 0:
+            raise RuntimeError("countpairs on device inputs failed")
+        npairs = np.ctypeslib.as_array(res.npairs, shape=(res.nbin,)).copy()
+        lib.free_results(ctypes.byref(res))
+        return npairs, corrfunc_gb300.last_stats()
+
+    # parity of the batch against the plain path on every catalogue (outside the timed region)
+    first = batch.run()
+    for k in range(len(cats)):
+        npairs, _ = one_plain(k)
+        if not np.array_equal(first[k]["npairs"], npairs[1:]):
+            raise RuntimeError("batched counts differ from countpairs() for catalogue %d" % k)
+
+    for _ in range(max(args.warmup, 3)):
+        batch.run()
+        flush_l2(torch, dev)
+    gpu_ms, pair_ms, launches, evaluated, refined = [], [], 0, 0, 0
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            out = batch.run()
+            st = corrfunc_gb300.last_stats()
+            if not all(np.array_equal(a["npairs"], b["npairs"]) for a, b in zip(out, first)):
+                raise RuntimeError("non-deterministic batched counts")
+            gpu_ms.append(st["total_gpu_ms"])
+            pair_ms.append(st["pair_kernel_ms"])
+            launches += st["kernel_launches"]
+            evaluated += st["pairs_evaluated"]
+            refined += st["pairs_refined"]
+            flush_l2(torch, dev)
+    torch.cuda.synchronize(dev)
+    total_s = sum(gpu_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([total_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = world * work * args.steps / total_s
+
+    # the same 64 counts as 64 sequential plain calls (device inputs), GPU time per call summed
+    seq_ms = []
+    for _ in range(2):
+        tot = 0.0
+        for k in range(len(cats)):
+            _, st = one_plain(k)
+            tot += st["total_gpu_ms"]
+        seq_ms.append(tot)
+        flush_l2(torch, dev)
+
+    # end to end: copy every catalogue from pinned host memory, replay, read the histograms back
+    hcats = [[torch.from_numpy(a).pin_memory() for a in c] for c in cats]
+    hrand = [torch.from_numpy(a).pin_memory() for a in rand]
+    h2d = sum(t.numel() * t.element_size() for c in hcats for t in c) + sum(t.numel() * t.element_size()
+                                                                          for t in hrand)
+    d2h = len(cats) * (WORKLOAD["nbins"] + 1) * 3 * 8
+    e2e_t = []
+    for _ in range(args.steps):
+        flush_l2(torch, dev)
+        t0 = time.perf_counter()
+        for dc, hc in zip(dcats, hcats):
+            for d, h in zip(dc, hc):
+                d.copy_(h, non_blocking=True)
+        for d, h in zip(drand, hrand):
+            d.copy_(h, non_blocking=True)
+        torch.cuda.synchronize(dev)
+        out = batch.run()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_value = world * work * args.steps / sum(e2e_t)
+
+    peak = ctypes.c_double()
+    lib.cf_gpu_fp32_peak_tflops(ctypes.byref(peak))
+    pair_s = sum(pair_ms) / 1e3 / args.steps
+    achieved = work * FLOP_PER_PAIR / pair_s / 1e12
+    st = corrfunc_gb300.last_stats()
+    line = {"metric": "pair evaluations/sec (reference-lattice candidate pairs), batched DD cross-correlations",
+            "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
+            "ms_per_step": sum(gpu_ms) / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64-refine" if args.precision == "fp32_refine" else "f64",
+            "data": "synthetic (seeded clustered and uniform catalogues, numpy PCG64)",
+            "config": dict(WORKLOAD, precision=args.precision, l2="flushed between steps (256 MB write)",
+                           reference_lattice_candidates=work, catalogue_points=int(sum(len(c[0]) for c in cats))),
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
+                         "frac": achieved / peak.value if peak.value else None, "traffic": None,
+                         "kernel": "k_pairs_f32<MODE_R3,false,true> (one launch for all catalogues)",
+                         "peak_source": "measured: FP32 FMA calibration kernel (cf_gpu_fp32_peak_tflops) in this run",
+                         "flop_per_pair": FLOP_PER_PAIR},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": 1e3 * sum(e2e_t) / args.steps},
+            "gpu_launches": launches,
+            "batch": {"graph_ms": sum(gpu_ms) / args.steps, "pair_kernel_ms": sum(pair_ms) / args.steps,
+                      "sequential_64_calls_ms": min(seq_ms), "speedup_vs_sequential": min(seq_ms) / (sum(gpu_ms) / args.steps),
+                      "plan_s": plan_s, "kernels_per_graph": st["kernel_launches"],
+                      "tuned_layout": {"lane_stride": st["lane_stride"], "warps_per_block": st["warps_per_block"]}},
+            "pairs": {"reference_lattice_candidates": work, "gpu_evaluated": evaluated // args.steps,
+                      "fp64_refined": refined // args.steps,
+                      "counted": int(sum(int(a["npairs"].sum()) for a in first))},
+            "clocks": clocks.summary()}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        r = cpu_batch_reference(cats, rand, bins, os.cpu_count() or 1)
+        line["cpu_baseline"] = None if r is None else {
+            "value": r[1] / r[0], "unit": UNIT, "cores": os.cpu_count(), "kind": "reference",
+            "sample": "the first %d catalogues against the full random catalogue, one run" % r[2], "seconds": r[0]}
+    batch.close()
+    binf.__exit__(None, None, None)
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def cpu_batch_reference(cats, rand, bins, nthreads, ncat=4):
+    """The reference's countpairs() (oracle/_ref) on the first ncat catalogues against the random
+    catalogue; returns (seconds, reference-lattice candidates, ncat)."""
+    from corrfunc_gb300 import _capi as C
+    from corrfunc_gb300 import theory
+    so = os.path.join(ROOT, "oracle", "_ref", "libcf_ref_DD.so")
+    if not os.path.exists(so):
+        return None
+    ref = C.bind(so)
+    gpu_lib = C.bind(C.LIB_PATH, gpu=True)
+    dt, work = 0.0, 0
+    with C.BinFile(bins) as bf:
+        for c in cats[:ncat]:
+            t0 = time.perf_counter()
+            theory.run_DD(ref, 0, nthreads, bins, c[0], c[1], c[2], X2=rand[0], Y2=rand[1], Z2=rand[2],
+                          weights1=c[3], weights2=rand[3], weight_type="pair_product", periodic=True,
+                          boxsize=WORKLOAD["boxsize"], isa="fastest")
+            dt += time.perf_counter() - t0
+            work += reference_work(gpu_lib, C, c, rand, bf, np.float32)
+    return dt, work, ncat
+
+
 def run_reference_arm(args):
     rank, world, _ = _rank_env()
     if rank != 0:
+        return
+    if WORKLOAD.get("kind") == "batched":
+        cats, rand, bins = make_batch_workload()
+        times, works = [], []
+        for _ in range(args.steps):
+            r = cpu_batch_reference(cats, rand, bins, os.cpu_count() or 1, ncat=8)
+            if r is None:
+                print(json.dumps({"impl": "reference",
+                                  "unavailable": "reference pair counters were not built in oracle/_ref"}))
+                return
+            times.append(r[0])
+            works.append(r[1])
+        value = sum(works) / sum(times)
+        sample = "the first 8 of the 64 catalogues against the full random catalogue"
+        print(json.dumps({"metric": "pair evaluations/sec (reference-lattice candidate pairs), batched DD "
+                                    "cross-correlations", "value": value, "unit": UNIT, "n_gpus": args.gpus,
+                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                          "data": "synthetic (seeded clustered and uniform catalogues)",
+                          "config": dict(WORKLOAD, sample=sample), "impl": "reference",
+                          "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "reference",
+                                           "sample": sample},
+                          "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
         return
     set1, set2, bins = make_workload()
     nthreads = os.cpu_count() or 1
@@ -252,6 +468,8 @@ def main():
     WORKLOAD.update(WORKLOADS[args.workload])
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.workload == "cfg5":
+        return run_batch_workload(args)
 
     rank, world, local = _rank_env()
     import torch

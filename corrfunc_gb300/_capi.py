@@ -133,6 +133,12 @@ class GpuStats(Structure):
 
 
 _GPU_PROTOS["cf_gpu_last_stats"] = ([POINTER(GpuStats)], c_int)
+_GPU_PROTOS["cf_gpu_batch_plan"] = (
+    [c_int, POINTER(c_int64), POINTER(c_void_p), POINTER(c_void_p), POINTER(c_void_p), POINTER(c_void_p), c_int64,
+     c_void_p, c_void_p, c_void_p, c_void_p, ctypes.c_char_p, POINTER(ConfigOptions), c_int, c_int,
+     POINTER(c_void_p)], c_int)
+_GPU_PROTOS["cf_gpu_batch_run"] = ([c_void_p, POINTER(ResultsDD)], c_int)
+_GPU_PROTOS["cf_gpu_batch_free"] = ([c_void_p], None)
 _GPU_PROTOS["cf_gpu_countpairs_cross_noalloc"] = (
     [c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
      POINTER(c_double), c_int, c_double, c_double, c_double, c_int, POINTER(c_uint64), POINTER(c_double),

@@ -330,6 +330,134 @@ int cf_gpu_countpairs_device(const int64_t ND1, void *X1, void *Y1, void *Z1, co
     return countpairs_impl(ND1, X1, Y1, Z1, ND2, X2, Y2, Z2, numthreads, autocorr, binfile, results, options, extra, 1);
 }
 
+/* ========================= batched DD cross-correlations ========================= */
+/* No reference counterpart: many countpairs(autocorr = 0) calls against one set-2 catalogue,
+ * planned once and replayed as one CUDA graph. */
+struct cf_gpu_batch {
+    cf_batch *eng;
+    int nbatch;
+    int nbin;
+    double *rupp;
+    int need_avg;
+    int need_w;
+};
+
+int cf_gpu_batch_plan(const int nbatch, const int64_t *ND1, void *const *X1, void *const *Y1, void *const *Z1,
+                      void *const *W1, const int64_t ND2, void *X2, void *Y2, void *Z2, void *W2, const char *binfile,
+                      struct config_options *options, const int weight_method, const int autotune,
+                      cf_gpu_batch **plan)
+{
+    if (plan == NULL) return EXIT_FAILURE;
+    *plan = NULL;
+    if (check_options(options, __func__) != EXIT_SUCCESS) return EXIT_FAILURE;
+    if (nbatch < 1 || ND1 == NULL || X1 == NULL || Y1 == NULL || Z1 == NULL) {
+        CF_ERR("a batch needs at least one set-1 catalogue");
+        return EXIT_FAILURE;
+    }
+    if (weight_method != NONE && weight_method != PAIR_PRODUCT) {
+        CF_ERR("unknown weight method %d", weight_method);
+        return EXIT_FAILURE;
+    }
+    const int need_w = weight_method == PAIR_PRODUCT;
+    if (need_w && (W1 == NULL || W2 == NULL)) {
+        CF_ERR("pair_product weighting needs one weight array per particle set");
+        return EXIT_FAILURE;
+    }
+    sanitize_lattice_options(options);
+    options->sort_on_z = 1;
+    double *rupp = NULL, rmin, rmax;
+    int nbin;
+    if (read_bins(binfile, &rupp, &nbin, &rmin, &rmax) != EXIT_SUCCESS) return EXIT_FAILURE;
+    if (options->periodic && options->boxsize == BOXSIZE_NOTGIVEN) {
+        fprintf(stderr, "boxsize = %g must be specified with periodic wrap. Please specify a non-zero boxsize, or zero to "
+                        "detect the particle extent, or -1 to make a dimension non-periodic.\n", options->boxsize);
+        free(rupp);
+        return EXIT_FAILURE;
+    }
+    cf_job J;
+    init_job(&J, options, CF_MODE_R3, 0);
+    J.inputs_on_device = 1;
+    J.n1 = ND1[0];
+    J.n2 = ND2;
+    J.x2 = X2; J.y2 = Y2; J.z2 = Z2;
+    J.need_weight = need_w;
+    J.w2 = need_w ? W2 : NULL;
+    fill_rule_extent(&J.rule, options, rmax, rmax, rmax, CF_DFL_PER_AXIS, CF_BOOST_XY, ND1[0]);
+    J.rmax_xy = J.rmax_z = J.rmax_3d = rmax;
+    J.nedges = nbin;
+    for (int i = 0; i < nbin; i++) J.edges[i] = rupp[i] * rupp[i];
+    cf_gpu_batch *P = calloc(1, sizeof(cf_gpu_batch));
+    if (P == NULL) {
+        free(rupp);
+        return EXIT_FAILURE;
+    }
+    if (cf_engine_batch_plan(&J, nbatch, ND1, (const void *const *)X1, (const void *const *)Y1,
+                             (const void *const *)Z1, need_w ? (const void *const *)W1 : NULL, autotune,
+                             &P->eng) != EXIT_SUCCESS) {
+        free(P);
+        free(rupp);
+        return EXIT_FAILURE;
+    }
+    P->nbatch = nbatch;
+    P->nbin = nbin;
+    P->rupp = rupp;
+    P->need_avg = options->need_avg_sep ? 1 : 0;
+    P->need_w = need_w;
+    reset_bin_refine_factors(options);
+    *plan = P;
+    return EXIT_SUCCESS;
+}
+
+int cf_gpu_batch_run(cf_gpu_batch *plan, results_countpairs *results)
+{
+    if (plan == NULL || results == NULL) return EXIT_FAILURE;
+    const int nb = plan->nbatch, nbin = plan->nbin;
+    cf_hist *H = calloc((size_t)nb, sizeof(cf_hist));
+    if (H == NULL) return EXIT_FAILURE;
+    int rc = EXIT_SUCCESS;
+    for (int b = 0; b < nb && rc == EXIT_SUCCESS; b++) rc = alloc_hist(&H[b], nbin);
+    if (rc == EXIT_SUCCESS) rc = cf_engine_batch_run(plan->eng, H);
+    for (int b = 0; b < nb; b++) {
+        results[b].npairs = NULL;
+        results[b].rupp = NULL;
+        results[b].rpavg = NULL;
+        results[b].weightavg = NULL;
+        results[b].nbin = 0;
+    }
+    for (int b = 0; b < nb && rc == EXIT_SUCCESS; b++) {
+        finalize_hist(&H[b], 0, plan->rupp[0] <= 0.0, 1, 0, 0.0, plan->need_avg, plan->need_w, 0);
+        results_countpairs *r = &results[b];
+        r->nbin = nbin;
+        r->npairs = malloc(sizeof(uint64_t) * nbin);
+        r->rupp = malloc(sizeof(double) * nbin);
+        r->rpavg = calloc(nbin, sizeof(double));
+        r->weightavg = calloc(nbin, sizeof(double));
+        if (!r->npairs || !r->rupp || !r->rpavg || !r->weightavg) {
+            rc = EXIT_FAILURE;
+            break;
+        }
+        for (int i = 0; i < nbin; i++) {
+            r->npairs[i] = H[b].npairs[i];
+            r->rupp[i] = plan->rupp[i];
+            r->rpavg[i] = plan->need_avg ? H[b].avg[i] : 0.0;
+            r->weightavg[i] = plan->need_w ? H[b].wsum[i] : 0.0;
+        }
+    }
+    if (rc != EXIT_SUCCESS)
+        for (int b = 0; b < nb; b++) free_results(&results[b]);
+    for (int b = 0; b < nb; b++) free_hist(&H[b]);
+    free(H);
+    return rc;
+}
+
+void cf_gpu_batch_free(cf_gpu_batch *plan)
+{
+    if (plan == NULL) return;
+    cf_engine_batch_free(plan->eng);
+    free(plan->rupp);
+    free(plan);
+}
+
 void free_results(results_countpairs *results)
 {
     if (results == NULL) return;

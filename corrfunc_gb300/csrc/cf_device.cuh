@@ -46,7 +46,8 @@ struct PairArgs {
     const int *rc2, *or2;
 
     const Task *tasks;
-    uint32_t ntasks;
+    uint32_t ntasks;            // task count, or the work-list capacity when ntask_dev is set
+    const uint32_t *ntask_dev;  // device-resident task count (batched work lists), or null
     uint32_t *task_counter;
 
     unsigned long long *g_cnt;  // nbins

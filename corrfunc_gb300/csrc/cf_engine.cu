@@ -46,6 +46,7 @@ using namespace cf;
 namespace {
 
 constexpr int kChunk = 32;          // points per i-chunk (one per lane)
+constexpr int kCatShift = 17;       // Task::meta bits 17-31: catalogue of a batched count
 constexpr uint32_t kJMax = 2048;    // max j points per task
 constexpr int kRxy = 2;             // lattice columns per rmax_xy
 constexpr int kZFine = 8;           // z slabs per rmax_z
@@ -79,6 +80,12 @@ struct Geom {
     double ref_inv[3];
     int ref_n[3];
     int check_ref_bounds;
+    // replays of a planned batch: points must stay inside the planned box and weights within the
+    // planned maximum (the lattice and the error bounds were sized for them); violations are
+    // counted in *extent_err (null: no check)
+    unsigned long long *extent_err;
+    double chk_lo[3], chk_hi[3];
+    double chk_wmax;
 };
 
 __device__ __forceinline__ unsigned long long ord_enc(double v)
@@ -155,6 +162,9 @@ __global__ void k_assign(const T *x, const T *y, const T *z, int64_t n, Geom g,
         const double a = ld(x, i), b = ld(y, i), c = ld(z, i);
         const int ix = axis_cell(a, g, 0), iy = axis_cell(b, g, 1), iz = axis_cell(c, g, 2);
         const uint32_t cell = ((uint32_t)ix * g.n[1] + iy) * (uint32_t)g.n[2] + iz;
+        if (g.extent_err && !(a >= g.chk_lo[0] && a <= g.chk_hi[0] && b >= g.chk_lo[1] && b <= g.chk_hi[1] &&
+                              c >= g.chk_lo[2] && c <= g.chk_hi[2]))
+            atomicAdd(g.extent_err, 1ull);
         cellid[i] = cell;
         atomicAdd(&count[cell], 1u);
         if (g.check_ref_bounds) {
@@ -188,6 +198,7 @@ __global__ void k_scatter(const T *x, const T *y, const T *z, const T *w, int64_
         const uint32_t pos = cell_start[c] + atomicAdd(&fill[c], 1u);
         const double a = ld(x, i), b = ld(y, i), cz = ld(z, i);
         const double wv = w ? ld(w, i) : 1.0;
+        if (g.extent_err && w && !(fabs(wv) <= g.chk_wmax)) atomicAdd(g.extent_err, 1ull);
         float hx, hy, hz, lx, ly, lz;
         split_hi_lo(a - g.origin[0], g.q[0], g.inv_q[0], &hx, &lx);
         split_hi_lo(b - g.origin[1], g.q[1], g.inv_q[1], &hy, &ly);
@@ -282,16 +293,20 @@ __global__ void k_col_chunks(const uint32_t *cell_start, int ncols, int nz, uint
     chunks_per_col[c] = (b - a + kChunk - 1) / kChunk;
 }
 
+// chunk_begin holds absolute point indices (point_base + index within the catalogue's lattice);
+// chunk_cat, when given, receives the catalogue number of every chunk (batched counts)
 __global__ void k_chunk_emit(const uint32_t *cell_start, int ncols, int nz, const uint32_t *chunk_off,
-                             uint32_t *chunk_begin, uint32_t *chunk_count)
+                             uint32_t *chunk_begin, uint32_t *chunk_count, uint32_t point_base, uint16_t *chunk_cat,
+                             uint16_t cat)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncols) return;
     const uint32_t a = cell_start[(uint32_t)c * nz], b = cell_start[(uint32_t)(c + 1) * nz];
     uint32_t o = chunk_off[c];
     for (uint32_t p = a; p < b; p += kChunk, o++) {
-        chunk_begin[o] = p;
+        chunk_begin[o] = point_base + p;
         chunk_count[o] = min((uint32_t)kChunk, b - p);
+        if (chunk_cat) chunk_cat[o] = cat;
     }
 }
 
@@ -318,8 +333,9 @@ __device__ __forceinline__ int floordiv(int a, int b)
 // Enumerates the tasks of one chunk.  With emit == false it only counts them.
 template <bool EMIT>
 __device__ uint32_t chunk_tasks(const TaskGeom &G, uint32_t ib, uint32_t icount, const uint32_t *cellid1,
-                                const uint32_t *cs2, Task *out)
+                                const uint32_t *cs2, Task *out, uint32_t cat, uint32_t room)
 {
+    if (icount == 0) return 0;  // unused chunk slot of a batched work list
     const uint32_t c0 = cellid1[ib], c1 = cellid1[ib + icount - 1];
     const int nz = G.nz;
     const int col = (int)(c0 / nz);
@@ -368,12 +384,12 @@ __device__ uint32_t chunk_tasks(const TaskGeom &G, uint32_t ib, uint32_t icount,
                 if (own_img) jb = ib;  // forward half of the own column
                 if (je <= jb) continue;
                 for (uint32_t p = jb; p < je; p += kJMax) {
-                    if (EMIT) {
+                    if (EMIT && ntask < room) {
                         Task t;
                         t.i_begin = ib;
                         t.j_begin = p;
                         t.j_end = min(je, p + kJMax);
-                        t.meta = task_meta((int)icount, mx, my, mz, own_img && p == jb ? 1 : 0);
+                        t.meta = task_meta((int)icount, mx, my, mz, own_img && p == jb ? 1 : 0) | (cat << kCatShift);
                         out[ntask] = t;
                     }
                     ntask++;
@@ -389,15 +405,22 @@ __global__ void k_task_count(TaskGeom G, uint32_t nchunks, const uint32_t *chunk
 {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nchunks) return;
-    ntasks[k] = chunk_tasks<false>(G, chunk_begin[k], chunk_count[k], cellid1, cs2, nullptr);
+    ntasks[k] = chunk_tasks<false>(G, chunk_begin[k], chunk_count[k], cellid1, cs2, nullptr, 0, 0);
 }
 
+// Writes the tasks of every chunk at its offset; with a capacity smaller than the total the tail
+// is dropped and *overflow set (a batched work list replayed on catalogues that grew).
 __global__ void k_task_emit(TaskGeom G, uint32_t nchunks, const uint32_t *chunk_begin, const uint32_t *chunk_count,
-                            const uint32_t *cellid1, const uint32_t *cs2, const uint32_t *task_off, Task *tasks)
+                            const uint32_t *cellid1, const uint32_t *cs2, const uint32_t *task_off, Task *tasks,
+                            const uint16_t *chunk_cat, uint32_t capacity, uint32_t *overflow)
 {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nchunks) return;
-    chunk_tasks<true>(G, chunk_begin[k], chunk_count[k], cellid1, cs2, tasks + task_off[k]);
+    const uint32_t off = task_off[k];
+    const uint32_t room = off < capacity ? capacity - off : 0u;
+    const uint32_t n = chunk_tasks<true>(G, chunk_begin[k], chunk_count[k], cellid1, cs2, tasks + off,
+                                         chunk_cat ? (uint32_t)chunk_cat[k] : 0u, room);
+    if (n > room && overflow) atomicOr(overflow, 1u);
 }
 
 // ------------------------------------------------------------------------------------
@@ -498,9 +521,12 @@ __device__ __forceinline__ void zero_hist(WarpHist h, const SmemLayout &L, int l
 }
 
 template <bool NEED_AVG, bool NEED_W, bool FIXED64>
-__device__ __forceinline__ void flush_hist(const PairArgs &A, WarpHist h, int lane)
+__device__ __forceinline__ void flush_hist(const PairArgs &A, WarpHist h, int lane, uint32_t cat = 0)
 {
     __syncwarp();
+    unsigned long long *g_cnt = A.g_cnt + (size_t)cat * A.nbins;
+    double *g_avg = A.g_avg + (size_t)cat * A.nbins;
+    double *g_w = A.g_w + (size_t)cat * A.nbins;
     for (int b = lane; b < A.nbins; b += 32) {
         unsigned long long c = 0;
         long long va = 0, vw = 0;
@@ -530,13 +556,13 @@ __device__ __forceinline__ void flush_hist(const PairArgs &A, WarpHist h, int la
                 }
             }
         }
-        if (c) atomicAdd(&A.g_cnt[b], c);
+        if (c) atomicAdd(&g_cnt[b], c);
         if (FIXED64) {
-            if (NEED_AVG && va) atomicAdd(&A.g_avg[b], (double)va * A.avg_unscale);
-            if (NEED_W && vw) atomicAdd(&A.g_w[b], (double)vw * A.w_unscale);
+            if (NEED_AVG && va) atomicAdd(&g_avg[b], (double)va * A.avg_unscale);
+            if (NEED_W && vw) atomicAdd(&g_w[b], (double)vw * A.w_unscale);
         } else {
-            if (NEED_AVG && fa != 0.0) atomicAdd(&A.g_avg[b], fa);
-            if (NEED_W && fw != 0.0) atomicAdd(&A.g_w[b], fw);
+            if (NEED_AVG && fa != 0.0) atomicAdd(&g_avg[b], fa);
+            if (NEED_W && fw != 0.0) atomicAdd(&g_w[b], fw);
         }
     }
     __syncwarp();
@@ -884,13 +910,33 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
     __syncthreads();
     uint64_t since_flush = 0, evaluated = 0;
     unsigned long long refined = 0;
+    const uint32_t ntasks = A.ntask_dev ? min(*A.ntask_dev, A.ntasks) : A.ntasks;
+    uint32_t cur_cat = 0;  // catalogue whose counts the warp's histogram holds (batched counts)
 
     while (true) {
         uint32_t t = 0;
         if (lane == 0) t = atomicAdd(A.task_counter, 1u);
         t = __shfl_sync(0xffffffffu, t, 0);
-        if (t >= A.ntasks) break;
+        if (t >= ntasks) break;
         const Task T = A.tasks[t];
+        const uint32_t cat = T.meta >> kCatShift;
+        if (cat != cur_cat) {
+            // queued pairs belong to the previous catalogue: settle them, then hand over
+            __syncwarp();
+            if (sq_n > 0) {
+                slow_batch<MODE, NEED_AVG, NEED_W>(A, se, glo, ghi, sq, sq_n, rq, rq_count, h, hl, lane, &refined);
+                sq_n = 0;
+            }
+            const int rest = *rq_count;
+            if (rest > 0) {
+                refine_batch<MODE, NEED_AVG, NEED_W>(A, se, rq, rest, h, hl, lane);
+                if (lane == 0) *rq_count = 0;
+                __syncwarp();
+            }
+            flush_hist<NEED_AVG, NEED_W, true>(A, h, lane, cur_cat);
+            cur_cat = cat;
+            since_flush = 0;
+        }
         const int icount = (int)(T.meta & 63u) + 1;
         const int mx = (int)((T.meta >> 8) & 3u) - 1, my = (int)((T.meta >> 10) & 3u) - 1,
                   mz = (int)((T.meta >> 12) & 3u) - 1;
@@ -947,7 +993,7 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
         since_flush += np;
         evaluated += np;
         if (since_flush > kFlushPairs) {
-            flush_hist<NEED_AVG, NEED_W, true>(A, h, lane);
+            flush_hist<NEED_AVG, NEED_W, true>(A, h, lane, cur_cat);
             since_flush = 0;
         }
     }
@@ -955,7 +1001,7 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
     if (sq_n > 0) slow_batch<MODE, NEED_AVG, NEED_W>(A, se, glo, ghi, sq, sq_n, rq, rq_count, h, hl, lane, &refined);
     const int rest = *rq_count;
     if (rest > 0) refine_batch<MODE, NEED_AVG, NEED_W>(A, se, rq, rest, h, hl, lane);
-    flush_hist<NEED_AVG, NEED_W, true>(A, h, lane);
+    flush_hist<NEED_AVG, NEED_W, true>(A, h, lane, cur_cat);
     for (int off = 16; off; off >>= 1) refined += __shfl_down_sync(0xffffffffu, refined, off);
     if (lane == 0) {
         atomicAdd(&A.g_stats[0], (unsigned long long)evaluated);
@@ -979,13 +1025,21 @@ __global__ void __launch_bounds__(256) k_pairs_f64(PairArgs A, SmemLayout SL)
     __syncthreads();
     uint64_t since_flush = 0, evaluated = 0;
     const double avg_scale = (double)A.avg_scale_f, w_scale = (double)A.w_scale_f;
+    const uint32_t ntasks = A.ntask_dev ? min(*A.ntask_dev, A.ntasks) : A.ntasks;
+    uint32_t cur_cat = 0;
 
     while (true) {
         uint32_t t = 0;
         if (lane == 0) t = atomicAdd(A.task_counter, 1u);
         t = __shfl_sync(0xffffffffu, t, 0);
-        if (t >= A.ntasks) break;
+        if (t >= ntasks) break;
         const Task T = A.tasks[t];
+        const uint32_t cat = T.meta >> kCatShift;
+        if (cat != cur_cat) {
+            flush_hist<NEED_AVG, NEED_W, true>(A, h, lane, cur_cat);
+            cur_cat = cat;
+            since_flush = 0;
+        }
         const int icount = (int)(T.meta & 63u) + 1;
         const int mx = (int)((T.meta >> 8) & 3u) - 1, my = (int)((T.meta >> 10) & 3u) - 1,
                   mz = (int)((T.meta >> 12) & 3u) - 1;
@@ -1033,11 +1087,11 @@ __global__ void __launch_bounds__(256) k_pairs_f64(PairArgs A, SmemLayout SL)
         since_flush += np;
         evaluated += np;
         if (since_flush > kFlushPairs) {
-            flush_hist<NEED_AVG, NEED_W, true>(A, h, lane);
+            flush_hist<NEED_AVG, NEED_W, true>(A, h, lane, cur_cat);
             since_flush = 0;
         }
     }
-    flush_hist<NEED_AVG, NEED_W, true>(A, h, lane);
+    flush_hist<NEED_AVG, NEED_W, true>(A, h, lane, cur_cat);
     if (lane == 0) atomicAdd(&A.g_stats[0], (unsigned long long)evaluated);
 }
 
@@ -1107,17 +1161,52 @@ struct SetBufs {
     DevBuf hi, lo, dbl, refcell, orig, cellid;
 };
 
+// Every device and pinned buffer one count uses.  Single calls share the engine's workspace;
+// a batch plan owns one, so that its captured graph never sees a buffer move.
+struct Workspace {
+    SetBufs set[2];
+    DevBuf mm, oob, scan_tmp[4], chunk_cnt, chunk_off, chunk_begin, chunk_count, chunk_cat, ntask, task_off, tasks;
+    DevBuf hist_cnt, hist_avg, hist_w, stats, counter, edges, guards, lut;
+    HostBuf h_small, h_tab, h_hist;
+};
+
+static void release(DevBuf &b)
+{
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.cap = 0;
+}
+
+static void release_workspace(Workspace &W)
+{
+    for (int s = 0; s < 2; s++) {
+        SetBufs &B = W.set[s];
+        for (int k = 0; k < 4; k++) release(B.raw[k]);
+        DevBuf *v[] = {&B.cellid_u, &B.count, &B.fill, &B.cell_start, &B.hi, &B.lo, &B.dbl, &B.refcell, &B.orig, &B.cellid};
+        for (DevBuf *d : v) release(*d);
+    }
+    for (int k = 0; k < 4; k++) release(W.scan_tmp[k]);
+    DevBuf *v[] = {&W.mm, &W.oob, &W.chunk_cnt, &W.chunk_off, &W.chunk_begin, &W.chunk_count, &W.chunk_cat, &W.ntask,
+                   &W.task_off, &W.tasks, &W.hist_cnt, &W.hist_avg, &W.hist_w, &W.stats, &W.counter, &W.edges,
+                   &W.guards, &W.lut};
+    for (DevBuf *d : v) release(*d);
+    HostBuf *h[] = {&W.h_small, &W.h_tab, &W.h_hist};
+    for (HostBuf *b : h) {
+        if (b->p) cudaFreeHost(b->p);
+        b->p = nullptr;
+        b->cap = 0;
+    }
+}
+
 struct Engine {
     bool init = false;
     int device = -1;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[6];
-    SetBufs set[2];
-    DevBuf mm, oob, scan_tmp[4], chunk_cnt, chunk_off, chunk_begin, chunk_count, ntask, task_off, tasks;
-    DevBuf hist_cnt, hist_avg, hist_w, stats, counter, edges, guards, lut;
-    HostBuf h_small, h_tab, h_hist;
+    Workspace ws;
     int regs_cache[5][4][2] = {};  // registers per thread of each pair kernel (0 = not queried)
+    int force_ls = 0, force_warps = 0;  // FP32 pair-kernel layout chosen by the batch tuner (0 = scored)
     int precision = CF_PRECISION_FP32_REFINE;
     int launches = 0;  // kernels launched by the current call
     size_t smem_per_sm = 228 * 1024;
@@ -1155,7 +1244,7 @@ static int engine_init(void)
 }
 
 // exclusive scan; out must have n+1 entries
-static int scan_u32(const uint32_t *in, uint32_t *out, uint32_t n, int level)
+static int scan_u32(Workspace &W, const uint32_t *in, uint32_t *out, uint32_t n, int level)
 {
     cudaStream_t st = g_eng.stream;
     if (n == 0) {
@@ -1164,8 +1253,8 @@ static int scan_u32(const uint32_t *in, uint32_t *out, uint32_t n, int level)
     }
     if (level >= 4) CF_FAIL("scan too deep");
     const uint32_t nblk = (n + kScanTile - 1) / kScanTile;
-    if (ensure(g_eng.scan_tmp[level], sizeof(uint32_t) * (2 * (size_t)nblk + 2)) != EXIT_SUCCESS) return EXIT_FAILURE;
-    uint32_t *bs = (uint32_t *)g_eng.scan_tmp[level].p;
+    if (ensure(W.scan_tmp[level], sizeof(uint32_t) * (2 * (size_t)nblk + 2)) != EXIT_SUCCESS) return EXIT_FAILURE;
+    uint32_t *bs = (uint32_t *)W.scan_tmp[level].p;
     uint32_t *bs_scan = bs + nblk;  // nblk+1 entries
     k_scan_tile<<<nblk, 1024, 0, st>>>(in, out, n, bs);
     g_eng.launches++;
@@ -1176,7 +1265,7 @@ static int scan_u32(const uint32_t *in, uint32_t *out, uint32_t n, int level)
         CF_CUDA(cudaGetLastError());
         return EXIT_SUCCESS;
     }
-    if (scan_u32(bs, bs_scan, nblk, level + 1) != EXIT_SUCCESS) return EXIT_FAILURE;
+    if (scan_u32(W, bs, bs_scan, nblk, level + 1) != EXIT_SUCCESS) return EXIT_FAILURE;
     k_scan_add<<<nblk, 1024, 0, st>>>(out, n, bs_scan);
     g_eng.launches++;
     k_set_total<<<1, 1, 0, st>>>(out, n, bs_scan, nblk);
@@ -1215,10 +1304,10 @@ static float f_up(double v)
 }
 
 template <typename T>
-static int upload_and_minmax(int s, int64_t n, const void *x, const void *y, const void *z, const void *w,
+static int upload_and_minmax(Workspace &W, int s, int64_t n, const void *x, const void *y, const void *z, const void *w,
                              bool on_device, unsigned long long *mm_dev)
 {
-    SetBufs &B = g_eng.set[s];
+    SetBufs &B = W.set[s];
     const size_t bytes = sizeof(T) * (size_t)n;
     const void *src[4] = {x, y, z, w};
     for (int k = 0; k < 4; k++) {
@@ -1241,38 +1330,60 @@ static int upload_and_minmax(int s, int64_t n, const void *x, const void *y, con
     return EXIT_SUCCESS;
 }
 
+// Counting sort of one catalogue into lattice records at point offset `base` of B (whose
+// per-point buffers already hold base + n points); B's per-cell arrays are reused.
 template <typename T>
-static int build_lattice(int s, int64_t n, bool has_w, const Geom &g, uint32_t ncells, unsigned long long *oob)
+static int build_lattice_at(Workspace &W, SetBufs &B, int64_t n, int64_t base, const T *x, const T *y, const T *z,
+                            const T *w, const Geom &g, uint32_t ncells, unsigned long long *oob)
 {
-    SetBufs &B = g_eng.set[s];
     cudaStream_t st = g_eng.stream;
-    if (ensure(B.cellid_u, sizeof(uint32_t) * n) || ensure(B.count, sizeof(uint32_t) * ncells) ||
-        ensure(B.fill, sizeof(uint32_t) * ncells) || ensure(B.cell_start, sizeof(uint32_t) * ((size_t)ncells + 1)) ||
-        ensure(B.hi, sizeof(float4) * n) || ensure(B.lo, sizeof(float4) * n) || ensure(B.dbl, sizeof(double4_32a) * n) ||
-        ensure(B.refcell, sizeof(int) * n) || ensure(B.orig, sizeof(int) * n) || ensure(B.cellid, sizeof(uint32_t) * n))
+    if (ensure(B.count, sizeof(uint32_t) * ncells) || ensure(B.fill, sizeof(uint32_t) * ncells) ||
+        ensure(B.cell_start, sizeof(uint32_t) * ((size_t)ncells + 1)))
         return EXIT_FAILURE;
     CF_CUDA(cudaMemsetAsync(B.count.p, 0, sizeof(uint32_t) * ncells, st));
     CF_CUDA(cudaMemsetAsync(B.fill.p, 0, sizeof(uint32_t) * ncells, st));
-    const T *x = (const T *)B.in[0], *y = (const T *)B.in[1], *z = (const T *)B.in[2];
-    const T *w = has_w ? (const T *)B.in[3] : nullptr;
+    if (n <= 0) {
+        CF_CUDA(cudaMemsetAsync(B.cell_start.p, 0, sizeof(uint32_t) * ((size_t)ncells + 1), st));
+        return EXIT_SUCCESS;
+    }
+    uint32_t *cellid_u = (uint32_t *)B.cellid_u.p + base;
     const int grid = grid_for(n, 256);
-    k_assign<T><<<grid, 256, 0, st>>>(x, y, z, n, g, (uint32_t *)B.cellid_u.p, (uint32_t *)B.count.p, oob);
+    k_assign<T><<<grid, 256, 0, st>>>(x, y, z, n, g, cellid_u, (uint32_t *)B.count.p, oob);
     g_eng.launches++;
     CF_CUDA(cudaGetLastError());
-    if (scan_u32((const uint32_t *)B.count.p, (uint32_t *)B.cell_start.p, ncells, 0) != EXIT_SUCCESS) return EXIT_FAILURE;
+    if (scan_u32(W, (const uint32_t *)B.count.p, (uint32_t *)B.cell_start.p, ncells, 0) != EXIT_SUCCESS) return EXIT_FAILURE;
     Lattice L;
-    L.hi = (float4 *)B.hi.p;
-    L.lo = (float4 *)B.lo.p;
-    L.dbl = (double4_32a *)B.dbl.p;
-    L.refcell = (int *)B.refcell.p;
-    L.orig = (int *)B.orig.p;
-    L.cellid = (uint32_t *)B.cellid.p;
+    L.hi = (float4 *)B.hi.p + base;
+    L.lo = (float4 *)B.lo.p + base;
+    L.dbl = (double4_32a *)B.dbl.p + base;
+    L.refcell = (int *)B.refcell.p + base;
+    L.orig = (int *)B.orig.p + base;
+    L.cellid = (uint32_t *)B.cellid.p + base;
     L.cell_start = (uint32_t *)B.cell_start.p;
-    k_scatter<T><<<grid, 256, 0, st>>>(x, y, z, w, n, g, (const uint32_t *)B.cellid_u.p,
-                                       (const uint32_t *)B.cell_start.p, (uint32_t *)B.fill.p, L);
+    k_scatter<T><<<grid, 256, 0, st>>>(x, y, z, w, n, g, cellid_u, (const uint32_t *)B.cell_start.p,
+                                       (uint32_t *)B.fill.p, L);
     g_eng.launches++;
     CF_CUDA(cudaGetLastError());
     return EXIT_SUCCESS;
+}
+
+static int ensure_points(SetBufs &B, int64_t n)
+{
+    if (ensure(B.cellid_u, sizeof(uint32_t) * n) || ensure(B.hi, sizeof(float4) * n) || ensure(B.lo, sizeof(float4) * n) ||
+        ensure(B.dbl, sizeof(double4_32a) * n) || ensure(B.refcell, sizeof(int) * n) || ensure(B.orig, sizeof(int) * n) ||
+        ensure(B.cellid, sizeof(uint32_t) * n))
+        return EXIT_FAILURE;
+    return EXIT_SUCCESS;
+}
+
+template <typename T>
+static int build_lattice(Workspace &W, int s, int64_t n, bool has_w, const Geom &g, uint32_t ncells, unsigned long long *oob)
+{
+    SetBufs &B = W.set[s];
+    if (ensure_points(B, n) != EXIT_SUCCESS) return EXIT_FAILURE;
+    const T *x = (const T *)B.in[0], *y = (const T *)B.in[1], *z = (const T *)B.in[2];
+    const T *w = has_w ? (const T *)B.in[3] : nullptr;
+    return build_lattice_at<T>(W, B, n, 0, x, y, z, w, g, ncells, oob);
 }
 
 // Histogram layout / block size that keeps the most warps resident: private per-lane columns
@@ -1315,6 +1426,10 @@ static int pair_kernel_regs(int mode, bool f64, bool avg, bool w)
 static SmemLayout choose_layout(int mode, bool f64, bool avg, bool w, int nedges, int nbins, int lut_n)
 {
     const bool dz = (mode == MODE_RPPI || mode == MODE_WP || mode == MODE_SMU);
+    if (!f64 && g_eng.force_ls > 0 && g_eng.force_warps > 0) {
+        const SmemLayout c = smem_layout(nedges, nbins, g_eng.force_warps, f64, lut_n, g_eng.force_ls, avg, w, dz);
+        if (c.total <= 220 * 1024) return c;
+    }
     const int regs = pair_kernel_regs(mode, f64, avg, w);
     const int warps_by_regs = 65536 / (32 * ((regs + 7) / 8 * 8));
     SmemLayout SL = smem_layout(nedges, nbins, 8, f64, lut_n, 1, avg, w, dz);
@@ -1417,7 +1532,7 @@ struct Tables {
     double dxy, d3;
 };
 
-static int build_tables(const cf_job *J, int mode, int nbins, bool need_w, const double delta[3], Tables *T)
+static int build_tables(Workspace &W, const cf_job *J, int mode, int nbins, bool need_w, const double delta[3], Tables *T)
 {
     cudaStream_t st = g_eng.stream;
     // coordinate error bounds
@@ -1427,11 +1542,11 @@ static int build_tables(const cf_job *J, int mode, int nbins, bool need_w, const
     T->d3 = d3;
     const double dlim = (mode == MODE_RPPI || mode == MODE_WP) ? dxy : d3;
     // guards: for theta the classified quantity is the squared chord 2*(1 - cos)
-    if (ensure(g_eng.edges, sizeof(double) * J->nedges) || ensure(g_eng.guards, sizeof(float) * 2 * J->nedges))
+    if (ensure(W.edges, sizeof(double) * J->nedges) || ensure(W.guards, sizeof(float) * 2 * J->nedges))
         return EXIT_FAILURE;
     const size_t tab_bytes = sizeof(double) * CF_MAX_EDGES + sizeof(float) * 2 * CF_MAX_EDGES + sizeof(uint32_t) * 4100;
-    if (ensure_host(g_eng.h_tab, tab_bytes) != EXIT_SUCCESS) return EXIT_FAILURE;
-    double *edges_h = (double *)g_eng.h_tab.p;
+    if (ensure_host(W.h_tab, tab_bytes) != EXIT_SUCCESS) return EXIT_FAILURE;
+    double *edges_h = (double *)W.h_tab.p;
     float *guards_h = (float *)(edges_h + CF_MAX_EDGES);
     uint32_t *lut_h = (uint32_t *)(guards_h + 2 * CF_MAX_EDGES);
     memcpy(edges_h, J->edges, sizeof(double) * J->nedges);
@@ -1463,7 +1578,7 @@ static int build_tables(const cf_job *J, int mode, int nbins, bool need_w, const
     while (((bhi >> shift) - (blo >> shift)) + 1 > 4096u) shift++;
     const int base = (int)(blo >> shift);
     const int n = (int)((bhi >> shift) - (blo >> shift)) + 1;
-    if (ensure(g_eng.lut, sizeof(uint32_t) * (n + 1)) != EXIT_SUCCESS) return EXIT_FAILURE;
+    if (ensure(W.lut, sizeof(uint32_t) * (n + 1)) != EXIT_SUCCESS) return EXIT_FAILURE;
     // row byte offsets: the layout (private columns or shared row) is fixed before the launch
     const int ls = choose_layout(mode, false, J->need_avg != 0, need_w, J->nedges, nbins, n).lane_stride;
     const uint32_t ostride = (mode == MODE_RPPI || mode == MODE_SMU) ? (uint32_t)(J->npibin + 1) : 1u;
@@ -1484,9 +1599,9 @@ static int build_tables(const cf_job *J, int mode, int nbins, bool need_w, const
         lut_h[t] = definite ? (uint32_t)mlo * ostride * row_bytes : (trash | 0x80000000u);
     }
     lut_h[n] = trash;  // reject: below the first bucket (q < rmin^2) or above the last (q >= rmax^2)
-    CF_CUDA(cudaMemcpyAsync(g_eng.lut.p, lut_h, sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice, st));
-    CF_CUDA(cudaMemcpyAsync(g_eng.edges.p, edges_h, sizeof(double) * J->nedges, cudaMemcpyHostToDevice, st));
-    CF_CUDA(cudaMemcpyAsync(g_eng.guards.p, guards_h, sizeof(float) * 2 * J->nedges, cudaMemcpyHostToDevice, st));
+    CF_CUDA(cudaMemcpyAsync(W.lut.p, lut_h, sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice, st));
+    CF_CUDA(cudaMemcpyAsync(W.edges.p, edges_h, sizeof(double) * J->nedges, cudaMemcpyHostToDevice, st));
+    CF_CUDA(cudaMemcpyAsync(W.guards.p, guards_h, sizeof(float) * 2 * J->nedges, cudaMemcpyHostToDevice, st));
     T->lut_n = n;
     T->shift = shift;
     T->base = base;
@@ -1496,75 +1611,16 @@ static int build_tables(const cf_job *J, int mode, int nbins, bool need_w, const
     return EXIT_SUCCESS;
 }
 
-static int run_locked(cf_job *J, cf_hist *H)
+// GPU lattice over the data extent [lo, hi] (or the periodic length): columns of about rlim/2 in
+// x and y, slabs of rlim_z/8 in z, a power-of-two FP32 grid q per axis and the coordinate error
+// bound delta of the hi/lo split.
+static int gpu_geometry(const cf_job *J, const cf_geometry &geo, const double lo[3], const double hi[3], Geom &g,
+                        double delta[3])
 {
-    if (engine_init() != EXIT_SUCCESS) return EXIT_FAILURE;
-    cudaStream_t st = g_eng.stream;
-    memset(&g_eng.last, 0, sizeof(g_eng.last));
-    g_eng.launches = 0;
-    const int mode = J->mode;
-    const bool two_d = (mode == MODE_RPPI || mode == MODE_SMU);
-    const int nbins = two_d ? J->nedges * (J->npibin + 1) : J->nedges;
-    if (H->nbins != nbins) CF_FAIL("internal: histogram size mismatch (%d vs %d)", H->nbins, nbins);
-    memset(H->npairs, 0, sizeof(uint64_t) * nbins);
-    memset(H->avg, 0, sizeof(double) * nbins);
-    memset(H->wsum, 0, sizeof(double) * nbins);
-    const bool autocorr = J->autocorr != 0;
-    const int64_t n1 = J->n1, n2 = autocorr ? J->n1 : J->n2;
-    if (n1 <= 0 || n2 <= 0) return EXIT_SUCCESS;
-    if (n1 >= (1ll << 31) || n2 >= (1ll << 31)) CF_FAIL("at most 2^31-1 points per set are supported");
-    if (J->elem_size != 4 && J->elem_size != 8) CF_FAIL("element size must be 4 or 8");
-    const bool isf = J->elem_size == 4;
-    const bool need_w = J->need_weight != 0;
-
-    CF_CUDA(cudaStreamSynchronize(st));  // pinned staging is reused: nothing of a failed call may be pending
-    CF_CUDA(cudaEventRecord(g_eng.ev[0], st));
-    // ---- upload + extent ----
-    if (ensure(g_eng.mm, sizeof(unsigned long long) * 16) != EXIT_SUCCESS) return EXIT_FAILURE;
-    unsigned long long *mm = (unsigned long long *)g_eng.mm.p;
-    if (ensure_host(g_eng.h_small, sizeof(unsigned long long) * 32) != EXIT_SUCCESS) return EXIT_FAILURE;
-    unsigned long long *mm_init = (unsigned long long *)g_eng.h_small.p;
-    unsigned long long *mmh = mm_init + 16;
-    for (int k = 0; k < 16; k++) mm_init[k] = (k % 8 == 6 || k % 8 == 7 || (k % 8) % 2 == 1) ? 0ull : ~0ull;
-    CF_CUDA(cudaMemcpyAsync(mm, mm_init, sizeof(unsigned long long) * 16, cudaMemcpyHostToDevice, st));
-    const int nsets = autocorr ? 1 : 2;
-    for (int s = 0; s < nsets; s++) {
-        const int64_t n = s ? n2 : n1;
-        const void *x = s ? J->x2 : J->x1, *y = s ? J->y2 : J->y1, *z = s ? J->z2 : J->z1;
-        const void *w = need_w ? (s ? J->w2 : J->w1) : nullptr;
-        if (!x || !y || !z || (need_w && !w)) CF_FAIL("NULL input array");
-        int rc = isf ? upload_and_minmax<float>(s, n, x, y, z, w, J->inputs_on_device != 0, mm + 8 * s)
-                     : upload_and_minmax<double>(s, n, x, y, z, w, J->inputs_on_device != 0, mm + 8 * s);
-        if (rc != EXIT_SUCCESS) return EXIT_FAILURE;
-    }
-    const bool dev_float = isf;
-    CF_CUDA(cudaMemcpyAsync(mmh, mm, sizeof(unsigned long long) * 16, cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaStreamSynchronize(st));
-    double lo[3], hi[3], wmax[2] = {0, 0};
-    for (int a = 0; a < 3; a++) {
-        lo[a] = ord_dec(mmh[2 * a]);
-        hi[a] = ord_dec(mmh[2 * a + 1]);
-        if (nsets == 2) {
-            lo[a] = fmin(lo[a], ord_dec(mmh[8 + 2 * a]));
-            hi[a] = fmax(hi[a], ord_dec(mmh[8 + 2 * a + 1]));
-        }
-    }
-    wmax[0] = ord_dec(mmh[6]);
-    wmax[1] = nsets == 2 ? ord_dec(mmh[14]) : wmax[0];
-    if (mmh[7] != 0 || (nsets == 2 && mmh[15] != 0)) CF_FAIL("non-finite input coordinates");
-    for (int a = 0; a < 3; a++) {
-        if (!isfinite(lo[a]) || !isfinite(hi[a])) CF_FAIL("non-finite input coordinates");
-    }
-    cf_geometry geo;
-    if (cf_resolve_geometry(&J->rule, lo, hi, &geo) != EXIT_SUCCESS) return EXIT_FAILURE;
-    J->geom = geo;
-
-    // ---- GPU lattice geometry ----
-    Geom g;
     memset(&g, 0, sizeof(g));
+    double span[3];
     const double rlim[3] = {J->rmax_xy, J->rmax_xy, J->rmax_z};
     const int refine[3] = {kRxy, kRxy, kZFine};
-    double span[3], delta[3];
     for (int a = 0; a < 3; a++) {
         const bool per = geo.periodic[a] && geo.wrap[a] > 0.0;
         double ext = hi[a] - lo[a];
@@ -1611,60 +1667,20 @@ static int run_locked(cf_job *J, cf_hist *H)
         }
     }
     g.check_ref_bounds = (J->rule.kind == CF_REF_BOX) ? 1 : 0;
-    const uint32_t ncols = (uint32_t)g.n[0] * g.n[1];
-    const uint32_t ncells = ncols * (uint32_t)g.n[2];
-    g_eng.last.num_cells = (int)ncells;
+    return EXIT_SUCCESS;
+}
 
-    // ---- lattices ----
-    if (ensure(g_eng.oob, sizeof(unsigned long long)) != EXIT_SUCCESS) return EXIT_FAILURE;
-    unsigned long long *oob = (unsigned long long *)g_eng.oob.p;
-    CF_CUDA(cudaMemsetAsync(oob, 0, sizeof(unsigned long long), st));
-    for (int s = 0; s < nsets; s++) {
-        const int64_t n = s ? n2 : n1;
-        int rc = dev_float ? build_lattice<float>(s, n, need_w, g, ncells, oob)
-                           : build_lattice<double>(s, n, need_w, g, ncells, oob);
-        if (rc != EXIT_SUCCESS) return EXIT_FAILURE;
-    }
-    SetBufs &S1 = g_eng.set[0];
-    SetBufs &S2 = g_eng.set[nsets - 1];
-    Tables T;
-    if (build_tables(J, mode, nbins, need_w, delta, &T) != EXIT_SUCCESS) return EXIT_FAILURE;
-
-    // ---- chunks ----
-    if (ensure(g_eng.chunk_cnt, sizeof(uint32_t) * ncols) || ensure(g_eng.chunk_off, sizeof(uint32_t) * ((size_t)ncols + 1)))
-        return EXIT_FAILURE;
-    k_col_chunks<<<(ncols + 255) / 256, 256, 0, st>>>((const uint32_t *)S1.cell_start.p, (int)ncols, g.n[2],
-                                                      (uint32_t *)g_eng.chunk_cnt.p);
-    g_eng.launches++;
-    CF_CUDA(cudaGetLastError());
-    if (scan_u32((const uint32_t *)g_eng.chunk_cnt.p, (uint32_t *)g_eng.chunk_off.p, ncols, 0) != EXIT_SUCCESS)
-        return EXIT_FAILURE;
-    const uint32_t max_chunks = (uint32_t)((n1 + kChunk - 1) / kChunk + ncols);
-    if (ensure(g_eng.chunk_begin, sizeof(uint32_t) * max_chunks) || ensure(g_eng.chunk_count, sizeof(uint32_t) * max_chunks))
-        return EXIT_FAILURE;
-    k_chunk_emit<<<(ncols + 255) / 256, 256, 0, st>>>((const uint32_t *)S1.cell_start.p, (int)ncols, g.n[2],
-                                                      (const uint32_t *)g_eng.chunk_off.p,
-                                                      (uint32_t *)g_eng.chunk_begin.p, (uint32_t *)g_eng.chunk_count.p);
-    g_eng.launches++;
-    CF_CUDA(cudaGetLastError());
-    uint32_t nchunks = 0;
-    unsigned long long oob_h = 0;
-    CF_CUDA(cudaMemcpyAsync(&nchunks, (uint32_t *)g_eng.chunk_off.p + ncols, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaMemcpyAsync(&oob_h, oob, sizeof(oob_h), cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaStreamSynchronize(st));
-    if (oob_h > 0) CF_FAIL("%llu particles are out of bounds. Check periodic wrapping?", oob_h);
-    if (nchunks > max_chunks) CF_FAIL("internal: chunk count overflow");
-
-    // ---- tasks ----
-    if (ensure(g_eng.counter, sizeof(uint32_t) * 4) != EXIT_SUCCESS) return EXIT_FAILURE;
-    CF_CUDA(cudaMemsetAsync(g_eng.counter.p, 0, sizeof(uint32_t) * 4, st));
+// Neighbour-search parameters of the work list: reach in columns and the z / 3-D limits, with
+// margins that cover the FP64 rounding of the cell assignment.
+static int task_geometry(const cf_job *J, const cf_geometry &geo, const Geom &g, const double lo[3], const double hi[3],
+                         bool autocorr, int mode, TaskGeom &G)
+{
     // prune margins cover FP64 rounding of the cell assignment only (the FP32 error bounds
     // matter for classification, not for which neighbours are visited)
     double maxabs_all = 0.0;
     for (int a = 0; a < 3; a++) maxabs_all = fmax(maxabs_all, fmax(fabs(lo[a]), fabs(hi[a])) + (geo.periodic[a] ? geo.wrap[a] : 0.0));
     const double margin_xy = 1e-9 * fmax(g.s[0], g.s[1]) + 1e-13 * maxabs_all;
     const double margin_z = 1e-9 * g.s[2] + 1e-13 * maxabs_all;
-    TaskGeom G;
     memset(&G, 0, sizeof(G));
     G.nx = g.n[0];
     G.ny = g.n[1];
@@ -1681,52 +1697,14 @@ static int run_locked(cf_job *J, cf_hist *H)
     G.reach_x = (int)ceil(G.rmax_xy / g.s[0]);
     G.reach_y = (int)ceil(G.rmax_xy / g.s[1]);
     if (G.reach_x > 64 || G.reach_y > 64) CF_FAIL("internal: neighbour reach too large");
-    G.error = (uint32_t *)g_eng.counter.p + 2;
-    if (ensure(g_eng.ntask, sizeof(uint32_t) * ((size_t)nchunks + 1)) ||
-        ensure(g_eng.task_off, sizeof(uint32_t) * ((size_t)nchunks + 2)))
-        return EXIT_FAILURE;
-    if (nchunks > 0) {
-        k_task_count<<<(nchunks + 127) / 128, 128, 0, st>>>(G, nchunks, (const uint32_t *)g_eng.chunk_begin.p,
-                                                            (const uint32_t *)g_eng.chunk_count.p,
-                                                            (const uint32_t *)S1.cellid.p,
-                                                            (const uint32_t *)S2.cell_start.p, (uint32_t *)g_eng.ntask.p);
-        g_eng.launches++;
-        CF_CUDA(cudaGetLastError());
-    }
-    if (scan_u32((const uint32_t *)g_eng.ntask.p, (uint32_t *)g_eng.task_off.p, nchunks, 0) != EXIT_SUCCESS)
-        return EXIT_FAILURE;
-    uint32_t ntasks = 0, task_err = 0;
-    CF_CUDA(cudaMemcpyAsync(&ntasks, (uint32_t *)g_eng.task_off.p + nchunks, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaMemcpyAsync(&task_err, G.error, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaStreamSynchronize(st));
-    if (task_err) CF_FAIL("internal: neighbour search needed a periodic image beyond +-1");
-    if (ensure(g_eng.tasks, sizeof(Task) * ((size_t)ntasks + 1)) != EXIT_SUCCESS) return EXIT_FAILURE;
-    if (nchunks > 0) {
-        k_task_emit<<<(nchunks + 127) / 128, 128, 0, st>>>(G, nchunks, (const uint32_t *)g_eng.chunk_begin.p,
-                                                           (const uint32_t *)g_eng.chunk_count.p,
-                                                           (const uint32_t *)S1.cellid.p, (const uint32_t *)S2.cell_start.p,
-                                                           (const uint32_t *)g_eng.task_off.p, (Task *)g_eng.tasks.p);
-        g_eng.launches++;
-        CF_CUDA(cudaGetLastError());
-    }
-    g_eng.last.tasks = ntasks;
-    CF_CUDA(cudaEventRecord(g_eng.ev[1], st));
+    return EXIT_SUCCESS;
+}
 
-    // ---- pair-kernel arguments ----
-    PairArgs A;
-    memset(&A, 0, sizeof(A));
-    A.hi1 = (const float4 *)S1.hi.p;
-    A.lo1 = (const float4 *)S1.lo.p;
-    A.d1 = (const double4_32a *)S1.dbl.p;
-    A.rc1 = (const int *)S1.refcell.p;
-    A.or1 = (const int *)S1.orig.p;
-    A.hi2 = (const float4 *)S2.hi.p;
-    A.lo2 = (const float4 *)S2.lo.p;
-    A.d2 = (const double4_32a *)S2.dbl.p;
-    A.rc2 = (const int *)S2.refcell.p;
-    A.or2 = (const int *)S2.orig.p;
-    A.tasks = (const Task *)g_eng.tasks.p;
-    A.ntasks = ntasks;
+// Bin, band and accumulator constants of the pair kernels (everything but the buffers).
+static void pair_constants(PairArgs &A, const cf_job *J, int mode, int nbins, bool autocorr, const TaskGeom &G,
+                           const cf_geometry &geo, const Geom &g, const double delta[3], const Tables &T,
+                           const double wmax[2], Workspace &W)
+{
     A.nedges = J->nedges;
     A.guard_search_top = 0;
     while (2 * A.guard_search_top + (A.guard_search_top == 0) <= J->nedges - 1)
@@ -1746,7 +1724,7 @@ static int run_locked(cf_job *J, cf_hist *H)
         }
     }
     const double dxy = T.dxy, d3 = T.d3;
-    A.g_lut = (const uint32_t *)g_eng.lut.p;
+    A.g_lut = (const uint32_t *)W.lut.p;
     A.trash_off = T.trash;
     A.row_bytes = T.row_bytes;
     A.lane_stride_hint = T.ls;
@@ -1756,8 +1734,8 @@ static int run_locked(cf_job *J, cf_hist *H)
     A.lut_negbase = (uint32_t)(-T.base);
     A.lut_n = T.lut_n;
     A.q_floor = T.q_floor;
-    A.g_edges = (const double *)g_eng.edges.p;
-    A.g_guard = (const float *)g_eng.guards.p;
+    A.g_edges = (const double *)W.edges.p;
+    A.g_guard = (const float *)W.guards.p;
     A.dz_err = (float)(2.0 * delta[2]);
     A.dxy_err = (float)(2.0 * dxy);
     if (mode == MODE_RPPI || mode == MODE_WP) {
@@ -1797,20 +1775,189 @@ static int run_locked(cf_job *J, cf_hist *H)
     A.w_scale_f = (float)ldexp(1.0, sw);
     A.w_unscale = ldexp(1.0, -sw);
 
-    if (ensure(g_eng.hist_cnt, sizeof(unsigned long long) * nbins) || ensure(g_eng.hist_avg, sizeof(double) * nbins) ||
-        ensure(g_eng.hist_w, sizeof(double) * nbins) || ensure(g_eng.stats, sizeof(unsigned long long) * 4) ||
-        ensure(g_eng.counter, sizeof(uint32_t) * 4))
+}
+
+static int run_locked(cf_job *J, cf_hist *H)
+{
+    Workspace &W = g_eng.ws;
+    if (engine_init() != EXIT_SUCCESS) return EXIT_FAILURE;
+    cudaStream_t st = g_eng.stream;
+    memset(&g_eng.last, 0, sizeof(g_eng.last));
+    g_eng.launches = 0;
+    const int mode = J->mode;
+    const bool two_d = (mode == MODE_RPPI || mode == MODE_SMU);
+    const int nbins = two_d ? J->nedges * (J->npibin + 1) : J->nedges;
+    if (H->nbins != nbins) CF_FAIL("internal: histogram size mismatch (%d vs %d)", H->nbins, nbins);
+    memset(H->npairs, 0, sizeof(uint64_t) * nbins);
+    memset(H->avg, 0, sizeof(double) * nbins);
+    memset(H->wsum, 0, sizeof(double) * nbins);
+    const bool autocorr = J->autocorr != 0;
+    const int64_t n1 = J->n1, n2 = autocorr ? J->n1 : J->n2;
+    if (n1 <= 0 || n2 <= 0) return EXIT_SUCCESS;
+    if (n1 >= (1ll << 31) || n2 >= (1ll << 31)) CF_FAIL("at most 2^31-1 points per set are supported");
+    if (J->elem_size != 4 && J->elem_size != 8) CF_FAIL("element size must be 4 or 8");
+    const bool isf = J->elem_size == 4;
+    const bool need_w = J->need_weight != 0;
+
+    CF_CUDA(cudaStreamSynchronize(st));  // pinned staging is reused: nothing of a failed call may be pending
+    CF_CUDA(cudaEventRecord(g_eng.ev[0], st));
+    // ---- upload + extent ----
+    if (ensure(W.mm, sizeof(unsigned long long) * 16) != EXIT_SUCCESS) return EXIT_FAILURE;
+    unsigned long long *mm = (unsigned long long *)W.mm.p;
+    if (ensure_host(W.h_small, sizeof(unsigned long long) * 32) != EXIT_SUCCESS) return EXIT_FAILURE;
+    unsigned long long *mm_init = (unsigned long long *)W.h_small.p;
+    unsigned long long *mmh = mm_init + 16;
+    for (int k = 0; k < 16; k++) mm_init[k] = (k % 8 == 6 || k % 8 == 7 || (k % 8) % 2 == 1) ? 0ull : ~0ull;
+    CF_CUDA(cudaMemcpyAsync(mm, mm_init, sizeof(unsigned long long) * 16, cudaMemcpyHostToDevice, st));
+    const int nsets = autocorr ? 1 : 2;
+    for (int s = 0; s < nsets; s++) {
+        const int64_t n = s ? n2 : n1;
+        const void *x = s ? J->x2 : J->x1, *y = s ? J->y2 : J->y1, *z = s ? J->z2 : J->z1;
+        const void *w = need_w ? (s ? J->w2 : J->w1) : nullptr;
+        if (!x || !y || !z || (need_w && !w)) CF_FAIL("NULL input array");
+        int rc = isf ? upload_and_minmax<float>(W, s, n, x, y, z, w, J->inputs_on_device != 0, mm + 8 * s)
+                     : upload_and_minmax<double>(W, s, n, x, y, z, w, J->inputs_on_device != 0, mm + 8 * s);
+        if (rc != EXIT_SUCCESS) return EXIT_FAILURE;
+    }
+    const bool dev_float = isf;
+    CF_CUDA(cudaMemcpyAsync(mmh, mm, sizeof(unsigned long long) * 16, cudaMemcpyDeviceToHost, st));
+    CF_CUDA(cudaStreamSynchronize(st));
+    double lo[3], hi[3], wmax[2] = {0, 0};
+    for (int a = 0; a < 3; a++) {
+        lo[a] = ord_dec(mmh[2 * a]);
+        hi[a] = ord_dec(mmh[2 * a + 1]);
+        if (nsets == 2) {
+            lo[a] = fmin(lo[a], ord_dec(mmh[8 + 2 * a]));
+            hi[a] = fmax(hi[a], ord_dec(mmh[8 + 2 * a + 1]));
+        }
+    }
+    wmax[0] = ord_dec(mmh[6]);
+    wmax[1] = nsets == 2 ? ord_dec(mmh[14]) : wmax[0];
+    if (mmh[7] != 0 || (nsets == 2 && mmh[15] != 0)) CF_FAIL("non-finite input coordinates");
+    for (int a = 0; a < 3; a++) {
+        if (!isfinite(lo[a]) || !isfinite(hi[a])) CF_FAIL("non-finite input coordinates");
+    }
+    cf_geometry geo;
+    if (cf_resolve_geometry(&J->rule, lo, hi, &geo) != EXIT_SUCCESS) return EXIT_FAILURE;
+    J->geom = geo;
+
+    // ---- GPU lattice geometry ----
+    Geom g;
+    double delta[3];
+    if (gpu_geometry(J, geo, lo, hi, g, delta) != EXIT_SUCCESS) return EXIT_FAILURE;
+    const uint32_t ncols = (uint32_t)g.n[0] * g.n[1];
+    const uint32_t ncells = ncols * (uint32_t)g.n[2];
+    g_eng.last.num_cells = (int)ncells;
+
+    // ---- lattices ----
+    if (ensure(W.oob, sizeof(unsigned long long)) != EXIT_SUCCESS) return EXIT_FAILURE;
+    unsigned long long *oob = (unsigned long long *)W.oob.p;
+    CF_CUDA(cudaMemsetAsync(oob, 0, sizeof(unsigned long long), st));
+    for (int s = 0; s < nsets; s++) {
+        const int64_t n = s ? n2 : n1;
+        int rc = dev_float ? build_lattice<float>(W, s, n, need_w, g, ncells, oob)
+                           : build_lattice<double>(W, s, n, need_w, g, ncells, oob);
+        if (rc != EXIT_SUCCESS) return EXIT_FAILURE;
+    }
+    SetBufs &S1 = W.set[0];
+    SetBufs &S2 = W.set[nsets - 1];
+    Tables T;
+    if (build_tables(W, J, mode, nbins, need_w, delta, &T) != EXIT_SUCCESS) return EXIT_FAILURE;
+
+    // ---- chunks ----
+    if (ensure(W.chunk_cnt, sizeof(uint32_t) * ncols) || ensure(W.chunk_off, sizeof(uint32_t) * ((size_t)ncols + 1)))
         return EXIT_FAILURE;
-    CF_CUDA(cudaMemsetAsync(g_eng.hist_cnt.p, 0, sizeof(unsigned long long) * nbins, st));
-    CF_CUDA(cudaMemsetAsync(g_eng.hist_avg.p, 0, sizeof(double) * nbins, st));
-    CF_CUDA(cudaMemsetAsync(g_eng.hist_w.p, 0, sizeof(double) * nbins, st));
-    CF_CUDA(cudaMemsetAsync(g_eng.stats.p, 0, sizeof(unsigned long long) * 4, st));
-    CF_CUDA(cudaMemsetAsync(g_eng.counter.p, 0, sizeof(uint32_t) * 4, st));
-    A.g_cnt = (unsigned long long *)g_eng.hist_cnt.p;
-    A.g_avg = (double *)g_eng.hist_avg.p;
-    A.g_w = (double *)g_eng.hist_w.p;
-    A.g_stats = (unsigned long long *)g_eng.stats.p;
-    A.task_counter = (uint32_t *)g_eng.counter.p;
+    k_col_chunks<<<(ncols + 255) / 256, 256, 0, st>>>((const uint32_t *)S1.cell_start.p, (int)ncols, g.n[2],
+                                                      (uint32_t *)W.chunk_cnt.p);
+    g_eng.launches++;
+    CF_CUDA(cudaGetLastError());
+    if (scan_u32(W, (const uint32_t *)W.chunk_cnt.p, (uint32_t *)W.chunk_off.p, ncols, 0) != EXIT_SUCCESS)
+        return EXIT_FAILURE;
+    const uint32_t max_chunks = (uint32_t)((n1 + kChunk - 1) / kChunk + ncols);
+    if (ensure(W.chunk_begin, sizeof(uint32_t) * max_chunks) || ensure(W.chunk_count, sizeof(uint32_t) * max_chunks))
+        return EXIT_FAILURE;
+    k_chunk_emit<<<(ncols + 255) / 256, 256, 0, st>>>((const uint32_t *)S1.cell_start.p, (int)ncols, g.n[2],
+                                                      (const uint32_t *)W.chunk_off.p,
+                                                      (uint32_t *)W.chunk_begin.p, (uint32_t *)W.chunk_count.p,
+                                                      0u, nullptr, 0);
+    g_eng.launches++;
+    CF_CUDA(cudaGetLastError());
+    uint32_t nchunks = 0;
+    unsigned long long oob_h = 0;
+    CF_CUDA(cudaMemcpyAsync(&nchunks, (uint32_t *)W.chunk_off.p + ncols, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CF_CUDA(cudaMemcpyAsync(&oob_h, oob, sizeof(oob_h), cudaMemcpyDeviceToHost, st));
+    CF_CUDA(cudaStreamSynchronize(st));
+    if (oob_h > 0) CF_FAIL("%llu particles are out of bounds. Check periodic wrapping?", oob_h);
+    if (nchunks > max_chunks) CF_FAIL("internal: chunk count overflow");
+
+    // ---- tasks ----
+    if (ensure(W.counter, sizeof(uint32_t) * 4) != EXIT_SUCCESS) return EXIT_FAILURE;
+    CF_CUDA(cudaMemsetAsync(W.counter.p, 0, sizeof(uint32_t) * 4, st));
+    TaskGeom G;
+    if (task_geometry(J, geo, g, lo, hi, autocorr, mode, G) != EXIT_SUCCESS) return EXIT_FAILURE;
+    G.error = (uint32_t *)W.counter.p + 2;
+    if (ensure(W.ntask, sizeof(uint32_t) * ((size_t)nchunks + 1)) ||
+        ensure(W.task_off, sizeof(uint32_t) * ((size_t)nchunks + 2)))
+        return EXIT_FAILURE;
+    if (nchunks > 0) {
+        k_task_count<<<(nchunks + 127) / 128, 128, 0, st>>>(G, nchunks, (const uint32_t *)W.chunk_begin.p,
+                                                            (const uint32_t *)W.chunk_count.p,
+                                                            (const uint32_t *)S1.cellid.p,
+                                                            (const uint32_t *)S2.cell_start.p, (uint32_t *)W.ntask.p);
+        g_eng.launches++;
+        CF_CUDA(cudaGetLastError());
+    }
+    if (scan_u32(W, (const uint32_t *)W.ntask.p, (uint32_t *)W.task_off.p, nchunks, 0) != EXIT_SUCCESS)
+        return EXIT_FAILURE;
+    uint32_t ntasks = 0, task_err = 0;
+    CF_CUDA(cudaMemcpyAsync(&ntasks, (uint32_t *)W.task_off.p + nchunks, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CF_CUDA(cudaMemcpyAsync(&task_err, G.error, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CF_CUDA(cudaStreamSynchronize(st));
+    if (task_err) CF_FAIL("internal: neighbour search needed a periodic image beyond +-1");
+    if (ensure(W.tasks, sizeof(Task) * ((size_t)ntasks + 1)) != EXIT_SUCCESS) return EXIT_FAILURE;
+    if (nchunks > 0) {
+        k_task_emit<<<(nchunks + 127) / 128, 128, 0, st>>>(G, nchunks, (const uint32_t *)W.chunk_begin.p,
+                                                           (const uint32_t *)W.chunk_count.p,
+                                                           (const uint32_t *)S1.cellid.p, (const uint32_t *)S2.cell_start.p,
+                                                           (const uint32_t *)W.task_off.p, (Task *)W.tasks.p,
+                                                           nullptr, ntasks, nullptr);
+        g_eng.launches++;
+        CF_CUDA(cudaGetLastError());
+    }
+    g_eng.last.tasks = ntasks;
+    CF_CUDA(cudaEventRecord(g_eng.ev[1], st));
+
+    // ---- pair-kernel arguments ----
+    PairArgs A;
+    memset(&A, 0, sizeof(A));
+    A.hi1 = (const float4 *)S1.hi.p;
+    A.lo1 = (const float4 *)S1.lo.p;
+    A.d1 = (const double4_32a *)S1.dbl.p;
+    A.rc1 = (const int *)S1.refcell.p;
+    A.or1 = (const int *)S1.orig.p;
+    A.hi2 = (const float4 *)S2.hi.p;
+    A.lo2 = (const float4 *)S2.lo.p;
+    A.d2 = (const double4_32a *)S2.dbl.p;
+    A.rc2 = (const int *)S2.refcell.p;
+    A.or2 = (const int *)S2.orig.p;
+    A.tasks = (const Task *)W.tasks.p;
+    A.ntasks = ntasks;
+    pair_constants(A, J, mode, nbins, autocorr, G, geo, g, delta, T, wmax, W);
+
+    if (ensure(W.hist_cnt, sizeof(unsigned long long) * nbins) || ensure(W.hist_avg, sizeof(double) * nbins) ||
+        ensure(W.hist_w, sizeof(double) * nbins) || ensure(W.stats, sizeof(unsigned long long) * 4) ||
+        ensure(W.counter, sizeof(uint32_t) * 4))
+        return EXIT_FAILURE;
+    CF_CUDA(cudaMemsetAsync(W.hist_cnt.p, 0, sizeof(unsigned long long) * nbins, st));
+    CF_CUDA(cudaMemsetAsync(W.hist_avg.p, 0, sizeof(double) * nbins, st));
+    CF_CUDA(cudaMemsetAsync(W.hist_w.p, 0, sizeof(double) * nbins, st));
+    CF_CUDA(cudaMemsetAsync(W.stats.p, 0, sizeof(unsigned long long) * 4, st));
+    CF_CUDA(cudaMemsetAsync(W.counter.p, 0, sizeof(uint32_t) * 4, st));
+    A.g_cnt = (unsigned long long *)W.hist_cnt.p;
+    A.g_avg = (double *)W.hist_avg.p;
+    A.g_w = (double *)W.hist_w.p;
+    A.g_stats = (unsigned long long *)W.stats.p;
+    A.task_counter = (uint32_t *)W.counter.p;
 
     int launched = 0;
     CF_CUDA(cudaEventRecord(g_eng.ev[2], st));
@@ -1819,14 +1966,14 @@ static int run_locked(cf_job *J, cf_hist *H)
         if (launch_pairs(mode, A, f64, J->need_avg != 0, need_w, &launched) != EXIT_SUCCESS) return EXIT_FAILURE;
     }
     CF_CUDA(cudaEventRecord(g_eng.ev[3], st));
-    if (ensure_host(g_eng.h_hist, sizeof(uint64_t) * (3 * (size_t)nbins + 4)) != EXIT_SUCCESS) return EXIT_FAILURE;
-    uint64_t *cnt_h = (uint64_t *)g_eng.h_hist.p;
+    if (ensure_host(W.h_hist, sizeof(uint64_t) * (3 * (size_t)nbins + 4)) != EXIT_SUCCESS) return EXIT_FAILURE;
+    uint64_t *cnt_h = (uint64_t *)W.h_hist.p;
     double *avg_h = (double *)(cnt_h + nbins), *w_h = avg_h + nbins;
     unsigned long long *stats_h = (unsigned long long *)(w_h + nbins);
-    CF_CUDA(cudaMemcpyAsync(cnt_h, g_eng.hist_cnt.p, sizeof(uint64_t) * nbins, cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaMemcpyAsync(avg_h, g_eng.hist_avg.p, sizeof(double) * nbins, cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaMemcpyAsync(w_h, g_eng.hist_w.p, sizeof(double) * nbins, cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaMemcpyAsync(stats_h, g_eng.stats.p, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost, st));
+    CF_CUDA(cudaMemcpyAsync(cnt_h, W.hist_cnt.p, sizeof(uint64_t) * nbins, cudaMemcpyDeviceToHost, st));
+    CF_CUDA(cudaMemcpyAsync(avg_h, W.hist_avg.p, sizeof(double) * nbins, cudaMemcpyDeviceToHost, st));
+    CF_CUDA(cudaMemcpyAsync(w_h, W.hist_w.p, sizeof(double) * nbins, cudaMemcpyDeviceToHost, st));
+    CF_CUDA(cudaMemcpyAsync(stats_h, W.stats.p, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost, st));
     CF_CUDA(cudaEventRecord(g_eng.ev[4], st));
     CF_CUDA(cudaStreamSynchronize(st));
     memcpy(H->npairs, cnt_h, sizeof(uint64_t) * nbins);
@@ -1843,6 +1990,500 @@ static int run_locked(cf_job *J, cf_hist *H)
     g_eng.last.pairs_refined = stats_h[1];
     g_eng.last.kernel_launches = g_eng.launches;
     (void)launched;
+    return EXIT_SUCCESS;
+}
+
+
+// ------------------------------------------------------------------------------------
+// batched cross-correlations: many set-1 catalogues against one set-2 catalogue
+// ------------------------------------------------------------------------------------
+// One plan owns its workspace.  The set-1 catalogues are sorted one after another into one
+// lattice (catalogue b at point offset pbase[b]); each catalogue gets a fixed range of chunk
+// slots (unused slots hold empty chunks), so the whole work list is built without host waits;
+// tasks carry their catalogue in Task::meta and the pair kernel flushes its per-warp histogram
+// into that catalogue's slice of the global histogram.  The sequence is run once eagerly (to
+// size the work list and, optionally, to time candidate histogram layouts) and then captured
+// as a CUDA graph that every run replays.
+struct BatchPlan {
+    Workspace W;
+    cf_job J;
+    int nbatch = 0, mode = MODE_R3, nbins = 0;
+    bool isf = false, need_w = false;
+    int64_t *n1 = nullptr, *pbase = nullptr, total1 = 0;
+    const void **x1 = nullptr, **y1 = nullptr, **z1 = nullptr, **w1 = nullptr;
+    uint32_t *cbase = nullptr, total_slots = 0, ncols = 0, ncells = 0;
+    uint32_t task_cap = 0, ntasks = 0;
+    Geom g;
+    TaskGeom G;
+    Tables T;
+    PairArgs A;
+    cf_geometry geo;
+    double delta[3], wmax[2];
+    int ls = 0, warps = 0;  // chosen FP32 layout (0: scored)
+    int kernels = 0;        // kernels in one run
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t ev[4];
+    bool events = false;
+};
+
+template <typename T>
+static int batch_lattices(BatchPlan &P)
+{
+    Workspace &W = P.W;
+    cudaStream_t st = g_eng.stream;
+    unsigned long long *oob = (unsigned long long *)W.oob.p;
+    Geom g1 = P.g, g2 = P.g;
+    g1.extent_err = g2.extent_err = oob + 1;
+    g1.chk_wmax = P.wmax[0];
+    g2.chk_wmax = P.wmax[1];
+    const T *w2 = P.need_w ? (const T *)P.J.w2 : nullptr;
+    if (build_lattice_at<T>(W, W.set[1], P.J.n2, 0, (const T *)P.J.x2, (const T *)P.J.y2, (const T *)P.J.z2, w2, g2,
+                            P.ncells, oob) != EXIT_SUCCESS)
+        return EXIT_FAILURE;
+    const int nz = P.g.n[2];
+    for (int b = 0; b < P.nbatch; b++) {
+        const T *w = P.need_w ? (const T *)P.w1[b] : nullptr;
+        if (build_lattice_at<T>(W, W.set[0], P.n1[b], P.pbase[b], (const T *)P.x1[b], (const T *)P.y1[b],
+                                (const T *)P.z1[b], w, g1, P.ncells, oob) != EXIT_SUCCESS)
+            return EXIT_FAILURE;
+        if (P.n1[b] == 0) continue;
+        k_col_chunks<<<(P.ncols + 255) / 256, 256, 0, st>>>((const uint32_t *)W.set[0].cell_start.p, (int)P.ncols, nz,
+                                                            (uint32_t *)W.chunk_cnt.p);
+        g_eng.launches++;
+        CF_CUDA(cudaGetLastError());
+        if (scan_u32(W, (const uint32_t *)W.chunk_cnt.p, (uint32_t *)W.chunk_off.p, P.ncols, 0) != EXIT_SUCCESS)
+            return EXIT_FAILURE;
+        k_chunk_emit<<<(P.ncols + 255) / 256, 256, 0, st>>>(
+            (const uint32_t *)W.set[0].cell_start.p, (int)P.ncols, nz, (const uint32_t *)W.chunk_off.p,
+            (uint32_t *)W.chunk_begin.p + P.cbase[b], (uint32_t *)W.chunk_count.p + P.cbase[b], (uint32_t)P.pbase[b],
+            (uint16_t *)W.chunk_cat.p + P.cbase[b], (uint16_t)b);
+        g_eng.launches++;
+        CF_CUDA(cudaGetLastError());
+    }
+    return EXIT_SUCCESS;
+}
+
+// Records ev on the engine stream; inside a stream capture as an external event node, so that
+// replays of the graph record it too.
+static int record_event(cudaEvent_t ev)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CF_CUDA(cudaStreamIsCapturing(g_eng.stream, &cs));
+    if (cs == cudaStreamCaptureStatusActive) CF_CUDA(cudaEventRecordWithFlags(ev, g_eng.stream, cudaEventRecordExternal));
+    else CF_CUDA(cudaEventRecord(ev, g_eng.stream));
+    return EXIT_SUCCESS;
+}
+
+// Enqueues lattices and task counts (phase 0), or task emission, pair kernel and read-back
+// (phase 1), on the engine stream.  No host waits inside either phase.
+static int batch_enqueue(BatchPlan &P, int phase, bool timing)
+{
+    Workspace &W = P.W;
+    cudaStream_t st = g_eng.stream;
+    if (phase == 0) {
+        CF_CUDA(cudaMemsetAsync(W.counter.p, 0, sizeof(uint32_t) * 4, st));
+        CF_CUDA(cudaMemsetAsync(W.oob.p, 0, sizeof(unsigned long long) * 2, st));
+        CF_CUDA(cudaMemsetAsync(W.chunk_count.p, 0, sizeof(uint32_t) * P.total_slots, st));
+        const int rc = P.isf ? batch_lattices<float>(P) : batch_lattices<double>(P);
+        if (rc != EXIT_SUCCESS) return EXIT_FAILURE;
+        k_task_count<<<(P.total_slots + 127) / 128, 128, 0, st>>>(
+            P.G, P.total_slots, (const uint32_t *)W.chunk_begin.p, (const uint32_t *)W.chunk_count.p,
+            (const uint32_t *)W.set[0].cellid.p, (const uint32_t *)W.set[1].cell_start.p, (uint32_t *)W.ntask.p);
+        g_eng.launches++;
+        CF_CUDA(cudaGetLastError());
+        return scan_u32(W, (const uint32_t *)W.ntask.p, (uint32_t *)W.task_off.p, P.total_slots, 0);
+    }
+    k_task_emit<<<(P.total_slots + 127) / 128, 128, 0, st>>>(
+        P.G, P.total_slots, (const uint32_t *)W.chunk_begin.p, (const uint32_t *)W.chunk_count.p,
+        (const uint32_t *)W.set[0].cellid.p, (const uint32_t *)W.set[1].cell_start.p, (const uint32_t *)W.task_off.p,
+        (Task *)W.tasks.p, (const uint16_t *)W.chunk_cat.p, P.task_cap, (uint32_t *)W.counter.p + 3);
+    g_eng.launches++;
+    CF_CUDA(cudaGetLastError());
+    const size_t hb = sizeof(uint64_t) * (size_t)P.nbatch * P.nbins;
+    CF_CUDA(cudaMemsetAsync(W.hist_cnt.p, 0, hb, st));
+    CF_CUDA(cudaMemsetAsync(W.hist_avg.p, 0, hb, st));
+    CF_CUDA(cudaMemsetAsync(W.hist_w.p, 0, hb, st));
+    CF_CUDA(cudaMemsetAsync(W.stats.p, 0, sizeof(unsigned long long) * 4, st));
+    CF_CUDA(cudaMemsetAsync(W.counter.p, 0, sizeof(uint32_t), st));  // task counter only
+    if (timing && record_event(P.ev[1]) != EXIT_SUCCESS) return EXIT_FAILURE;
+    int launched = 0;
+    const bool f64 = g_eng.precision == CF_PRECISION_FP64;
+    const int fls = g_eng.force_ls, fw = g_eng.force_warps;
+    g_eng.force_ls = P.ls;
+    g_eng.force_warps = P.warps;
+    const int rc = launch_pairs(P.mode, P.A, f64, P.J.need_avg != 0, P.need_w, &launched);
+    g_eng.force_ls = fls;
+    g_eng.force_warps = fw;
+    if (rc != EXIT_SUCCESS) return EXIT_FAILURE;
+    if (timing && record_event(P.ev[2]) != EXIT_SUCCESS) return EXIT_FAILURE;
+    uint64_t *cnt_h = (uint64_t *)W.h_hist.p;
+    double *avg_h = (double *)(cnt_h + (size_t)P.nbatch * P.nbins), *w_h = avg_h + (size_t)P.nbatch * P.nbins;
+    unsigned long long *stats_h = (unsigned long long *)(w_h + (size_t)P.nbatch * P.nbins);
+    CF_CUDA(cudaMemcpyAsync(cnt_h, W.hist_cnt.p, hb, cudaMemcpyDeviceToHost, st));
+    CF_CUDA(cudaMemcpyAsync(avg_h, W.hist_avg.p, hb, cudaMemcpyDeviceToHost, st));
+    CF_CUDA(cudaMemcpyAsync(w_h, W.hist_w.p, hb, cudaMemcpyDeviceToHost, st));
+    CF_CUDA(cudaMemcpyAsync(stats_h, W.stats.p, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost, st));
+    CF_CUDA(cudaMemcpyAsync(stats_h + 4, W.counter.p, sizeof(uint32_t) * 4, cudaMemcpyDeviceToHost, st));
+    CF_CUDA(cudaMemcpyAsync(stats_h + 6, W.oob.p, sizeof(unsigned long long) * 2, cudaMemcpyDeviceToHost, st));
+    return EXIT_SUCCESS;
+}
+
+// Checks the flags of a finished run and copies catalogue b's raw sums into H[b].
+static int batch_collect(BatchPlan &P, cf_hist *H)
+{
+    Workspace &W = P.W;
+    const size_t nb = (size_t)P.nbatch * P.nbins;
+    const uint64_t *cnt_h = (const uint64_t *)W.h_hist.p;
+    const double *avg_h = (const double *)(cnt_h + nb), *w_h = avg_h + nb;
+    const unsigned long long *stats_h = (const unsigned long long *)(w_h + nb);
+    const uint32_t *flags = (const uint32_t *)(stats_h + 4);
+    if (stats_h[6] > 0) CF_FAIL("%llu particles are out of bounds. Check periodic wrapping?", stats_h[6]);
+    if (stats_h[7] > 0)
+        CF_FAIL("%llu points or weights left the box / weight range the batch was planned for; plan again", stats_h[7]);
+    if (flags[2]) CF_FAIL("internal: neighbour search needed a periodic image beyond +-1");
+    if (flags[3]) CF_FAIL("the batch work list outgrew its plan (catalogues changed since planning); plan again");
+    for (int b = 0; b < P.nbatch; b++) {
+        if (H[b].nbins != P.nbins) CF_FAIL("internal: histogram size mismatch");
+        memcpy(H[b].npairs, cnt_h + (size_t)b * P.nbins, sizeof(uint64_t) * P.nbins);
+        memcpy(H[b].avg, avg_h + (size_t)b * P.nbins, sizeof(double) * P.nbins);
+        memcpy(H[b].wsum, w_h + (size_t)b * P.nbins, sizeof(double) * P.nbins);
+    }
+    g_eng.last.pairs_evaluated = stats_h[0];
+    g_eng.last.pairs_refined = stats_h[1];
+    return EXIT_SUCCESS;
+}
+
+static void batch_destroy(BatchPlan *P)
+{
+    if (!P) return;
+    if (P->exec) cudaGraphExecDestroy(P->exec);
+    if (P->graph) cudaGraphDestroy(P->graph);
+    if (P->events)
+        for (int k = 0; k < 4; k++) cudaEventDestroy(P->ev[k]);
+    if (g_eng.stream) cudaStreamSynchronize(g_eng.stream);
+    release_workspace(P->W);
+    free(P->n1);
+    free(P->pbase);
+    free(P->cbase);
+    free((void *)P->x1);
+    delete P;
+}
+
+static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, const void *const *x1,
+                             const void *const *y1, const void *const *z1, const void *const *w1, int tune,
+                             BatchPlan **out)
+{
+    *out = nullptr;
+    if (engine_init() != EXIT_SUCCESS) return EXIT_FAILURE;
+    if (nbatch < 1 || nbatch > (1 << 15) - 1) CF_FAIL("batch size %d outside [1, 32767]", nbatch);
+    if (tmpl->mode != MODE_R3 || tmpl->autocorr) CF_FAIL("internal: batched counts are DD cross-correlations");
+    if (tmpl->elem_size != 4 && tmpl->elem_size != 8) CF_FAIL("element size must be 4 or 8");
+    if (tmpl->n2 <= 0 || tmpl->n2 >= (1ll << 31)) CF_FAIL("set 2 must hold between 1 and 2^31-1 points");
+    cudaStream_t st = g_eng.stream;
+    CF_CUDA(cudaStreamSynchronize(st));
+    BatchPlan *P = new BatchPlan();
+    P->J = *tmpl;
+    P->nbatch = nbatch;
+    P->isf = tmpl->elem_size == 4;
+    P->need_w = tmpl->need_weight != 0;
+    P->nbins = tmpl->nedges;
+    P->n1 = (int64_t *)calloc(nbatch, sizeof(int64_t));
+    P->pbase = (int64_t *)calloc(nbatch + 1, sizeof(int64_t));
+    P->cbase = (uint32_t *)calloc(nbatch + 1, sizeof(uint32_t));
+    P->x1 = (const void **)calloc(4 * (size_t)nbatch, sizeof(void *));
+    if (!P->n1 || !P->pbase || !P->cbase || !P->x1) {
+        batch_destroy(P);
+        CF_FAIL("out of host memory");
+    }
+    P->y1 = P->x1 + nbatch;
+    P->z1 = P->y1 + nbatch;
+    P->w1 = P->z1 + nbatch;
+    for (int b = 0; b < nbatch; b++) {
+        if (n1[b] < 0 || (n1[b] > 0 && (!x1[b] || !y1[b] || !z1[b] || (P->need_w && !w1[b])))) {
+            batch_destroy(P);
+            CF_FAIL("catalogue %d: negative size or NULL array", b);
+        }
+        P->n1[b] = n1[b];
+        P->x1[b] = x1[b];
+        P->y1[b] = y1[b];
+        P->z1[b] = z1[b];
+        P->w1[b] = P->need_w ? w1[b] : nullptr;
+        P->pbase[b + 1] = P->pbase[b] + n1[b];
+    }
+    P->total1 = P->pbase[nbatch];
+    if (P->total1 >= (1ll << 31)) {
+        batch_destroy(P);
+        CF_FAIL("the batch holds %lld set-1 points; at most 2^31-1 are supported", (long long)P->total1);
+    }
+    Workspace &W = P->W;
+    int rc = EXIT_SUCCESS;
+    do {
+        // ---- extent of everything (set 1 in slots 0-7, set 2 in 8-15) ----
+        if ((rc = ensure(W.mm, sizeof(unsigned long long) * 16)) != EXIT_SUCCESS) break;
+        if ((rc = ensure_host(W.h_small, sizeof(unsigned long long) * 32)) != EXIT_SUCCESS) break;
+        unsigned long long *mm = (unsigned long long *)W.mm.p;
+        unsigned long long *mm_init = (unsigned long long *)W.h_small.p, *mmh = mm_init + 16;
+        for (int k = 0; k < 16; k++) mm_init[k] = (k % 8 == 6 || k % 8 == 7 || (k % 8) % 2 == 1) ? 0ull : ~0ull;
+        if (cudaMemcpyAsync(mm, mm_init, sizeof(unsigned long long) * 16, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+            rc = EXIT_FAILURE;
+            break;
+        }
+        for (int s = 0; s <= nbatch; s++) {
+            const bool r = s == nbatch;
+            const int64_t n = r ? P->J.n2 : P->n1[s];
+            if (n == 0) continue;
+            const void *x = r ? P->J.x2 : P->x1[s], *y = r ? P->J.y2 : P->y1[s], *z = r ? P->J.z2 : P->z1[s];
+            const void *w = P->need_w ? (r ? P->J.w2 : P->w1[s]) : nullptr;
+            int grid = grid_for(n, 256);
+            if (grid > 4 * g_eng.num_sms) grid = 4 * g_eng.num_sms;
+            unsigned long long *slot = mm + (r ? 8 : 0);
+            if (P->isf) k_minmax<float><<<grid, 256, 0, st>>>((const float *)x, (const float *)y, (const float *)z,
+                                                               (const float *)w, n, slot);
+            else k_minmax<double><<<grid, 256, 0, st>>>((const double *)x, (const double *)y, (const double *)z,
+                                                         (const double *)w, n, slot);
+        }
+        if (cudaMemcpyAsync(mmh, mm, sizeof(unsigned long long) * 16, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess) {
+            fprintf(stderr, "corrfunc_gb300: CUDA error '%s' while measuring the batch extent\n",
+                    cudaGetErrorString(cudaGetLastError()));
+            rc = EXIT_FAILURE;
+            break;
+        }
+        double lo[3], hi[3];
+        for (int a = 0; a < 3; a++) {
+            lo[a] = fmin(ord_dec(mmh[2 * a]), ord_dec(mmh[8 + 2 * a]));
+            hi[a] = fmax(ord_dec(mmh[2 * a + 1]), ord_dec(mmh[8 + 2 * a + 1]));
+        }
+        P->wmax[0] = ord_dec(mmh[6]);
+        P->wmax[1] = ord_dec(mmh[14]);
+        if (mmh[7] != 0 || mmh[15] != 0) {
+            fprintf(stderr, "corrfunc_gb300: non-finite input coordinates\n");
+            rc = EXIT_FAILURE;
+            break;
+        }
+        bool finite = true;
+        for (int a = 0; a < 3; a++) finite = finite && isfinite(lo[a]) && isfinite(hi[a]);
+        if (!finite) {
+            fprintf(stderr, "corrfunc_gb300: non-finite input coordinates\n");
+            rc = EXIT_FAILURE;
+            break;
+        }
+        if ((rc = cf_resolve_geometry(&P->J.rule, lo, hi, &P->geo)) != EXIT_SUCCESS) break;
+        P->J.geom = P->geo;
+        // the GPU lattice of a periodic axis spans the whole box when the data lie in [0, L], so
+        // that replays may move points anywhere inside it
+        double glo[3], ghi[3];
+        for (int a = 0; a < 3; a++) {
+            const bool per = P->geo.periodic[a] && P->geo.wrap[a] > 0.0;
+            const bool inbox = per && lo[a] >= 0.0 && hi[a] <= P->geo.wrap[a];
+            glo[a] = inbox ? 0.0 : lo[a];
+            ghi[a] = inbox ? P->geo.wrap[a] : hi[a];
+        }
+        if ((rc = gpu_geometry(&P->J, P->geo, glo, ghi, P->g, P->delta)) != EXIT_SUCCESS) break;
+        for (int a = 0; a < 3; a++) {
+            const bool per = P->geo.periodic[a] && P->geo.wrap[a] > 0.0;
+            P->g.chk_lo[a] = glo[a];
+            P->g.chk_hi[a] = per ? glo[a] + P->geo.wrap[a] : ghi[a];
+        }
+        P->ncols = (uint32_t)P->g.n[0] * P->g.n[1];
+        P->ncells = P->ncols * (uint32_t)P->g.n[2];
+        g_eng.last.num_cells = (int)P->ncells;
+
+        // ---- buffers ----
+        for (int b = 0; b < nbatch; b++)
+            P->cbase[b + 1] = P->cbase[b] + (uint32_t)((P->n1[b] + kChunk - 1) / kChunk + (P->n1[b] > 0 ? P->ncols : 0));
+        P->total_slots = P->cbase[nbatch];
+        const size_t nb = (size_t)nbatch * P->nbins;
+        if ((rc = ensure_points(W.set[0], P->total1 > 0 ? P->total1 : 1)) != EXIT_SUCCESS ||
+            (rc = ensure_points(W.set[1], P->J.n2)) != EXIT_SUCCESS ||
+            (rc = ensure(W.oob, sizeof(unsigned long long) * 2)) != EXIT_SUCCESS ||
+            (rc = ensure(W.counter, sizeof(uint32_t) * 4)) != EXIT_SUCCESS ||
+            (rc = ensure(W.chunk_cnt, sizeof(uint32_t) * P->ncols)) != EXIT_SUCCESS ||
+            (rc = ensure(W.chunk_off, sizeof(uint32_t) * ((size_t)P->ncols + 1))) != EXIT_SUCCESS ||
+            (rc = ensure(W.chunk_begin, sizeof(uint32_t) * ((size_t)P->total_slots + 1))) != EXIT_SUCCESS ||
+            (rc = ensure(W.chunk_count, sizeof(uint32_t) * ((size_t)P->total_slots + 1))) != EXIT_SUCCESS ||
+            (rc = ensure(W.chunk_cat, sizeof(uint16_t) * ((size_t)P->total_slots + 1))) != EXIT_SUCCESS ||
+            (rc = ensure(W.ntask, sizeof(uint32_t) * ((size_t)P->total_slots + 1))) != EXIT_SUCCESS ||
+            (rc = ensure(W.task_off, sizeof(uint32_t) * ((size_t)P->total_slots + 2))) != EXIT_SUCCESS ||
+            (rc = ensure(W.hist_cnt, sizeof(uint64_t) * nb)) != EXIT_SUCCESS ||
+            (rc = ensure(W.hist_avg, sizeof(double) * nb)) != EXIT_SUCCESS ||
+            (rc = ensure(W.hist_w, sizeof(double) * nb)) != EXIT_SUCCESS ||
+            (rc = ensure(W.stats, sizeof(unsigned long long) * 4)) != EXIT_SUCCESS ||
+            (rc = ensure_host(W.h_hist, sizeof(uint64_t) * (3 * nb + 10))) != EXIT_SUCCESS)
+            break;
+        if ((rc = task_geometry(&P->J, P->geo, P->g, glo, ghi, false, MODE_R3, P->G)) != EXIT_SUCCESS) break;
+        P->G.error = (uint32_t *)W.counter.p + 2;
+        if ((rc = build_tables(W, &P->J, MODE_R3, P->nbins, P->need_w, P->delta, &P->T)) != EXIT_SUCCESS) break;
+
+        // ---- eager run: size the work list ----
+        if ((rc = batch_enqueue(*P, 0, false)) != EXIT_SUCCESS) break;
+        uint32_t *cnt_h = (uint32_t *)(mmh + 8);
+        if (cudaMemcpyAsync(cnt_h, (uint32_t *)W.task_off.p + P->total_slots, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                            st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess) {
+            fprintf(stderr, "corrfunc_gb300: CUDA error '%s' while building the batch work list\n",
+                    cudaGetErrorString(cudaGetLastError()));
+            rc = EXIT_FAILURE;
+            break;
+        }
+        P->ntasks = *cnt_h;
+        // room for replays on catalogues of the same sizes whose points moved: twice the planned
+        // work list plus eight tasks per chunk of set 1 (a replay that still outgrows it fails)
+        P->task_cap = 2 * P->ntasks + 8 * (uint32_t)((P->total1 + kChunk - 1) / kChunk) + 1024;
+        if ((rc = ensure(W.tasks, sizeof(Task) * (size_t)P->task_cap)) != EXIT_SUCCESS) break;
+
+        PairArgs &A = P->A;
+        memset(&A, 0, sizeof(A));
+        A.hi1 = (const float4 *)W.set[0].hi.p;
+        A.lo1 = (const float4 *)W.set[0].lo.p;
+        A.d1 = (const double4_32a *)W.set[0].dbl.p;
+        A.rc1 = (const int *)W.set[0].refcell.p;
+        A.or1 = (const int *)W.set[0].orig.p;
+        A.hi2 = (const float4 *)W.set[1].hi.p;
+        A.lo2 = (const float4 *)W.set[1].lo.p;
+        A.d2 = (const double4_32a *)W.set[1].dbl.p;
+        A.rc2 = (const int *)W.set[1].refcell.p;
+        A.or2 = (const int *)W.set[1].orig.p;
+        A.tasks = (const Task *)W.tasks.p;
+        A.ntasks = P->task_cap;
+        A.ntask_dev = (const uint32_t *)W.task_off.p + P->total_slots;
+        pair_constants(A, &P->J, MODE_R3, P->nbins, false, P->G, P->geo, P->g, P->delta, P->T, P->wmax, W);
+        A.g_cnt = (unsigned long long *)W.hist_cnt.p;
+        A.g_avg = (double *)W.hist_avg.p;
+        A.g_w = (double *)W.hist_w.p;
+        A.g_stats = (unsigned long long *)W.stats.p;
+        A.task_counter = (uint32_t *)W.counter.p;
+        for (int k = 0; k < 4; k++)
+            if (cudaEventCreate(&P->ev[k]) != cudaSuccess) rc = EXIT_FAILURE;
+        if (rc != EXIT_SUCCESS) break;
+        P->events = true;
+        if ((rc = batch_enqueue(*P, 1, false)) != EXIT_SUCCESS) break;
+        if (cudaStreamSynchronize(st) != cudaSuccess) {
+            fprintf(stderr, "corrfunc_gb300: CUDA error '%s' in the batch pair kernel\n",
+                    cudaGetErrorString(cudaGetLastError()));
+            rc = EXIT_FAILURE;
+            break;
+        }
+        {
+            const unsigned long long *stats_h = (const unsigned long long *)((const uint64_t *)W.h_hist.p + 3 * nb);
+            const uint32_t *flags = (const uint32_t *)(stats_h + 4);
+            if (stats_h[6] > 0 || stats_h[7] > 0 || flags[2] || flags[3]) {
+                fprintf(stderr, "corrfunc_gb300: batch planning failed (out-of-bounds points or work-list error)\n");
+                rc = EXIT_FAILURE;
+                break;
+            }
+        }
+
+        // ---- tuner: time the FP32 layouts that fit, keep the fastest ----
+        if (tune && g_eng.precision == CF_PRECISION_FP32_REFINE) {
+            const int cand_ls[3] = {32, 16, 8};
+            const int cand_w[3] = {16, 8, 4};
+            float best = 1e30f;
+            int best_ls = 0, best_w = 0;
+            for (int li = 0; li < 3 && rc == EXIT_SUCCESS; li++) {
+                for (int wi = 0; wi < 3 && rc == EXIT_SUCCESS; wi++) {
+                    const SmemLayout c = smem_layout(P->J.nedges, P->nbins, cand_w[wi], false, P->T.lut_n, cand_ls[li],
+                                                     P->J.need_avg != 0, P->need_w, false);
+                    if (c.total > 220 * 1024) continue;
+                    g_eng.force_ls = cand_ls[li];
+                    g_eng.force_warps = cand_w[wi];
+                    Tables T2;
+                    if ((rc = build_tables(W, &P->J, MODE_R3, P->nbins, P->need_w, P->delta, &T2)) != EXIT_SUCCESS) break;
+                    P->T = T2;
+                    pair_constants(A, &P->J, MODE_R3, P->nbins, false, P->G, P->geo, P->g, P->delta, P->T, P->wmax, W);
+                    P->ls = cand_ls[li];
+                    P->warps = cand_w[wi];
+                    float ms = 0.f;
+                    for (int rep = 0; rep < 2 && rc == EXIT_SUCCESS; rep++) {
+                        if ((rc = batch_enqueue(*P, 1, true)) != EXIT_SUCCESS) break;
+                        if (cudaStreamSynchronize(st) != cudaSuccess ||
+                            cudaEventElapsedTime(&ms, P->ev[1], P->ev[2]) != cudaSuccess) {
+                            fprintf(stderr, "corrfunc_gb300: CUDA error while tuning the batch layout\n");
+                            rc = EXIT_FAILURE;
+                        }
+                    }
+                    if (rc == EXIT_SUCCESS && ms < best) {
+                        best = ms;
+                        best_ls = cand_ls[li];
+                        best_w = cand_w[wi];
+                    }
+                }
+            }
+            g_eng.force_ls = 0;
+            g_eng.force_warps = 0;
+            if (rc != EXIT_SUCCESS) break;
+            P->ls = best_ls;
+            P->warps = best_w;
+            g_eng.force_ls = best_ls;
+            g_eng.force_warps = best_w;
+            Tables T2;
+            rc = build_tables(W, &P->J, MODE_R3, P->nbins, P->need_w, P->delta, &T2);
+            g_eng.force_ls = 0;
+            g_eng.force_warps = 0;
+            if (rc != EXIT_SUCCESS) break;
+            P->T = T2;
+            pair_constants(A, &P->J, MODE_R3, P->nbins, false, P->G, P->geo, P->g, P->delta, P->T, P->wmax, W);
+            if (cudaStreamSynchronize(st) != cudaSuccess) {
+                rc = EXIT_FAILURE;
+                break;
+            }
+        }
+
+        // ---- capture the whole sequence as one graph ----
+        const int launches0 = g_eng.launches;
+        if (cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+            fprintf(stderr, "corrfunc_gb300: cannot capture the batch graph\n");
+            rc = EXIT_FAILURE;
+            break;
+        }
+        int rc0 = record_event(P->ev[0]);
+        if (rc0 == EXIT_SUCCESS) rc0 = batch_enqueue(*P, 0, false);
+        if (rc0 == EXIT_SUCCESS) rc0 = batch_enqueue(*P, 1, true);
+        if (rc0 == EXIT_SUCCESS) rc0 = record_event(P->ev[3]);
+        const cudaError_t ec = cudaStreamEndCapture(st, &P->graph);
+        if (rc0 != EXIT_SUCCESS || ec != cudaSuccess) {
+            fprintf(stderr, "corrfunc_gb300: capturing the batch graph failed (%s)\n", cudaGetErrorString(ec));
+            rc = EXIT_FAILURE;
+            break;
+        }
+        P->kernels = g_eng.launches - launches0;
+        if (cudaGraphInstantiate(&P->exec, P->graph, 0) != cudaSuccess) {
+            fprintf(stderr, "corrfunc_gb300: instantiating the batch graph failed\n");
+            rc = EXIT_FAILURE;
+            break;
+        }
+    } while (0);
+    if (rc != EXIT_SUCCESS) {
+        g_eng.force_ls = 0;
+        g_eng.force_warps = 0;
+        batch_destroy(P);
+        return EXIT_FAILURE;
+    }
+    *out = P;
+    return EXIT_SUCCESS;
+}
+
+static int batch_run_locked(BatchPlan *P, cf_hist *H)
+{
+    if (engine_init() != EXIT_SUCCESS) return EXIT_FAILURE;
+    cudaStream_t st = g_eng.stream;
+    CF_CUDA(cudaStreamSynchronize(st));
+    memset(&g_eng.last, 0, sizeof(g_eng.last));
+    CF_CUDA(cudaGraphLaunch(P->exec, st));
+    CF_CUDA(cudaStreamSynchronize(st));
+    if (batch_collect(*P, H) != EXIT_SUCCESS) return EXIT_FAILURE;
+    float ms_total = 0.f, ms_pairs = 0.f;
+    CF_CUDA(cudaEventElapsedTime(&ms_total, P->ev[0], P->ev[3]));
+    CF_CUDA(cudaEventElapsedTime(&ms_pairs, P->ev[1], P->ev[2]));
+    g_eng.last.total_gpu_ms = ms_total;
+    g_eng.last.pair_kernel_ms = ms_pairs;
+    g_eng.last.gridlink_ms = ms_total - ms_pairs;
+    g_eng.last.tasks = P->ntasks;
+    g_eng.last.kernel_launches = P->kernels;
+    g_eng.last.num_cells = (int)P->ncells;
+    g_eng.last.lane_stride = P->ls;
+    g_eng.last.warps_per_block = P->warps;
     return EXIT_SUCCESS;
 }
 
@@ -1906,4 +2547,33 @@ extern "C" int cf_engine_last_stats(cf_engine_stats *out)
     *out = g_eng.last;
     pthread_mutex_unlock(&g_lock);
     return EXIT_SUCCESS;
+}
+
+extern "C" int cf_engine_batch_plan(const cf_job *tmpl, int nbatch, const int64_t *n1, const void *const *x1,
+                                    const void *const *y1, const void *const *z1, const void *const *w1, int tune,
+                                    cf_batch **out)
+{
+    pthread_mutex_lock(&g_lock);
+    BatchPlan *P = nullptr;
+    const int rc = batch_plan_locked(tmpl, nbatch, n1, x1, y1, z1, w1, tune, &P);
+    pthread_mutex_unlock(&g_lock);
+    *out = (cf_batch *)P;
+    return rc;
+}
+
+extern "C" int cf_engine_batch_run(cf_batch *plan, cf_hist *out)
+{
+    if (!plan || !out) return EXIT_FAILURE;
+    pthread_mutex_lock(&g_lock);
+    const int rc = batch_run_locked((BatchPlan *)plan, out);
+    pthread_mutex_unlock(&g_lock);
+    return rc;
+}
+
+extern "C" void cf_engine_batch_free(cf_batch *plan)
+{
+    if (!plan) return;
+    pthread_mutex_lock(&g_lock);
+    batch_destroy((BatchPlan *)plan);
+    pthread_mutex_unlock(&g_lock);
 }

@@ -102,6 +102,16 @@ typedef struct {
 } cf_hist;
 
 int cf_engine_run(cf_job *job, cf_hist *out);
+
+/* Batched DD cross-correlations: nbatch set-1 catalogues (device arrays) against the set-2
+ * catalogue of tmpl, planned once (extent, lattices, work list, optional layout tuning, CUDA
+ * graph capture) and replayed by cf_engine_batch_run into out[0..nbatch-1] (raw sums). */
+typedef struct cf_batch cf_batch;
+int cf_engine_batch_plan(const cf_job *tmpl, int nbatch, const int64_t *n1, const void *const *x1,
+                         const void *const *y1, const void *const *z1, const void *const *w1, int tune,
+                         cf_batch **out);
+int cf_engine_batch_run(cf_batch *plan, cf_hist *out);
+void cf_engine_batch_free(cf_batch *plan);
 int cf_engine_set_precision(int mode);
 int cf_engine_get_precision(void);
 

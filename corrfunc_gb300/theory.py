@@ -263,6 +263,89 @@ def run_xi(lib, boxsize, nthreads, binfile, X, Y, Z, weights=None, weight_type=N
     return (out, o.c_api_time) if c_api_timer else out
 
 
+def _device_array(a):
+    """(device pointer, numpy dtype, length) of a CUDA array (``__cuda_array_interface__``, e.g. a
+    torch tensor on the GPU)."""
+    iface = getattr(a, "__cuda_array_interface__", None)
+    if iface is None:
+        raise TypeError("batched counts take device arrays (objects with __cuda_array_interface__)")
+    if iface.get("strides") not in (None, (np.dtype(iface["typestr"]).itemsize,)):
+        raise ValueError("device arrays must be contiguous")
+    return int(iface["data"][0]), np.dtype(iface["typestr"]), int(iface["shape"][0])
+
+
+class DDCrossBatch:
+    """DD(r) cross-correlations of many catalogues against one catalogue, planned once and replayed
+    as one CUDA graph (``cf_gpu_batch_plan`` / ``cf_gpu_batch_run``).  ``catalogues`` is a list of
+    (X, Y, Z[, weights]) device arrays; ``second`` is (X2, Y2, Z2[, weights2]).  ``run()`` returns
+    one record array per catalogue, each equal to
+    ``DD(0, nthreads, binfile, X, Y, Z, X2=X2, Y2=Y2, Z2=Z2, ...)`` on the same arrays."""
+
+    def __init__(self, binfile, catalogues, second, periodic=True, boxsize=None, output_ravg=False,
+                 weight_type=None, autotune=True, isa="fastest", xbin_refine_factor=2, ybin_refine_factor=2,
+                 zbin_refine_factor=1, max_cells_per_dim=100, lib=None):
+        if periodic and boxsize is None:
+            raise ValueError("Must specify a boxsize if periodic=True")
+        self._lib = lib or C.library()
+        need_w = weight_type is not None
+        cols = [[_device_array(a) for a in cat[:4 if need_w else 3]] for cat in catalogues]
+        sec = [_device_array(a) for a in second[:4 if need_w else 3]]
+        dt = sec[0][1]
+        if dt not in (np.dtype(np.float32), np.dtype(np.float64)):
+            raise TypeError("positions must be float32 or float64")
+        for cat in cols + [sec]:
+            if any(c[1] != dt for c in cat) or any(c[2] != cat[0][2] for c in cat):
+                raise ValueError("every array must have the dtype and length of the first")
+        o = _common_options(1, periodic, boxsize, False, output_ravg,
+                            (xbin_refine_factor, ybin_refine_factor, zbin_refine_factor), max_cells_per_dim,
+                            True, True, False, isa, dt)
+        nb = len(cols)
+        P = ctypes.c_void_p * nb
+        self._n1 = (ctypes.c_int64 * nb)(*[c[0][2] for c in cols])
+        self._ptr = [P(*[c[k][0] for c in cols]) for k in range(3)]
+        self._w = P(*[c[3][0] for c in cols]) if need_w else None
+        method = C.weight_method_by_name(weight_type)
+        plan = ctypes.c_void_p()
+        with C.BinFile(binfile) as bf:
+            rc = self._lib.cf_gpu_batch_plan(nb, self._n1, self._ptr[0], self._ptr[1], self._ptr[2], self._w,
+                                             sec[0][2], sec[0][0], sec[1][0], sec[2][0],
+                                             sec[3][0] if need_w else None, bf.encode(), ctypes.byref(o),
+                                             int(method), 1 if autotune else 0, ctypes.byref(plan))
+        if rc != 0:
+            raise RuntimeError("RuntimeError occurred")
+        self._plan = plan
+        self.nbatch = nb
+
+    def run(self):
+        res = (C.ResultsDD * self.nbatch)()
+        if self._lib.cf_gpu_batch_run(self._plan, res) != 0:
+            raise RuntimeError("RuntimeError occurred")
+        outs = []
+        for r in res:
+            nb = r.nbin
+            out = np.zeros(max(nb - 1, 0), dtype=DD_DTYPE)
+            rupp = C.carray(r.rupp, nb, np.float64)
+            out["rmin"] = rupp[:-1]
+            out["rmax"] = rupp[1:]
+            out["ravg"] = C.carray(r.rpavg, nb, np.float64)[1:]
+            out["npairs"] = C.carray(r.npairs, nb, np.uint64)[1:]
+            out["weightavg"] = C.carray(r.weightavg, nb, np.float64)[1:]
+            self._lib.free_results(ctypes.byref(r))
+            outs.append(out)
+        return outs
+
+    def close(self):
+        if getattr(self, "_plan", None):
+            self._lib.cf_gpu_batch_free(self._plan)
+            self._plan = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def DD(*args, **kwargs):
     """3-D pair counts DD(r); see Corrfunc.theory.DD (Corrfunc/theory/DD.py:16)."""
     return run_DD(C.library(), *args, **kwargs)

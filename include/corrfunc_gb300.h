@@ -298,6 +298,29 @@ int cf_gpu_countpairs_device(const int64_t ND1, void *X1, void *Y1, void *Z1,
                              results_countpairs *results, struct config_options *options,
                              struct extra_options *extra);
 
+/* Batched DD(r) cross-correlations: nbatch set-1 catalogues, each against the same set-2
+ * catalogue, with the same bins and options.  No reference counterpart: it replaces nbatch
+ * countpairs(..., autocorr = 0, ...) calls (jackknife / bootstrap subsamples against one random
+ * catalogue) and gives results[b] exactly as that call would.
+ *
+ *   ND1[b], X1[b], Y1[b], Z1[b], W1[b]  catalogue b, device pointers (float or double as
+ *          options->float_type); W1 / W2 are read only with weight_method = PAIR_PRODUCT.
+ *   X2 .. W2  the set-2 catalogue, device pointers.
+ *   autotune  non-zero: time the pair kernel's histogram layouts while planning, keep the fastest.
+ *
+ * cf_gpu_batch_plan measures the data, builds every lattice and the merged work list once,
+ * checks it, and captures the whole count (lattices, work list, one pair-kernel launch for all
+ * catalogues, read-back) as a CUDA graph.  cf_gpu_batch_run replays that graph on the arrays the
+ * plan was made with -- their contents may change between runs, their sizes may not -- and fills
+ * results[0 .. nbatch-1] (release each with free_results).  cf_gpu_batch_free releases the plan. */
+typedef struct cf_gpu_batch cf_gpu_batch;
+int cf_gpu_batch_plan(const int nbatch, const int64_t *ND1, void *const *X1, void *const *Y1, void *const *Z1,
+                      void *const *W1, const int64_t ND2, void *X2, void *Y2, void *Z2, void *W2,
+                      const char *binfile, struct config_options *options, const int weight_method,
+                      const int autotune, cf_gpu_batch **plan);
+int cf_gpu_batch_run(cf_gpu_batch *plan, results_countpairs *results);
+void cf_gpu_batch_free(cf_gpu_batch *plan);
+
 /* Measured FP32 fused-multiply-add throughput of the current device in TFLOP/s (a calibration
  * kernel; denominator of the pair kernels' FP32 roofline fraction).  No reference counterpart. */
 int cf_gpu_fp32_peak_tflops(double *tflops);
