@@ -1614,13 +1614,55 @@ static int build_tables(Workspace &W, const cf_job *J, int mode, int nbins, bool
 // GPU lattice over the data extent [lo, hi] (or the periodic length): columns of about rlim/2 in
 // x and y, slabs of rlim_z/8 in z, a power-of-two FP32 grid q per axis and the coordinate error
 // bound delta of the hi/lo split.
+// Columns per rmax in x and y.  A task pairs a chunk of 32 set-1 points of one column with the
+// z-window of each neighbour column; the candidates per chunk are the set-2 points in
+//   sum over neighbour columns of  A * (e + 2 W),
+// A the column area, e the z-extent of the chunk (32 points at the set-1 density, at most the
+// box) and W the z reach of that column.  Dense set-1 catalogues favour narrow columns (small A),
+// sparse ones wide columns (fewer neighbours, shorter chunks).
+static int choose_rxy(const cf_job *J, const double ext[3])
+{
+    const double r = J->rmax_xy;
+    double vol = 1.0;
+    for (int a = 0; a < 3; a++) vol *= fmax(ext[a], 1e-300);
+    const double rho1 = (double)J->n1 / vol;
+    if (!(r > 0.0) || !(rho1 > 0.0) || !(ext[2] > 0.0)) return kRxy;
+    double cost_of[4] = {INFINITY, INFINITY, INFINITY, INFINITY};
+    for (int R = 1; R <= 3; R++) {
+        const double s = r / R * (1.0 + 1e-6), A = s * s;
+        const double e = fmin(kChunk / (rho1 * A), ext[2]);
+        double cost = 0.0;
+        for (int dx = -R; dx <= R; dx++) {
+            for (int dy = -R; dy <= R; dy++) {
+                const double rx = fmax(0.0, (double)(abs(dx) - 1)) * s, ry = fmax(0.0, (double)(abs(dy) - 1)) * s;
+                const double d2 = rx * rx + ry * ry;
+                if (d2 >= r * r) continue;
+                double W = J->rmax_z;
+                if (J->rmax_3d > 0.0) W = fmin(W, sqrt(fmax(0.0, J->rmax_3d * J->rmax_3d - d2)));
+                cost += A * (e + 2.0 * W);
+            }
+        }
+        cost_of[R] = cost;
+    }
+    int best = kRxy;  // the default unless another width is clearly cheaper
+    for (int R = 1; R <= 3; R++)
+        if (cost_of[R] < 0.97 * cost_of[best]) best = R;
+    return best;
+}
+
 static int gpu_geometry(const cf_job *J, const cf_geometry &geo, const double lo[3], const double hi[3], Geom &g,
                         double delta[3])
 {
     memset(&g, 0, sizeof(g));
     double span[3];
     const double rlim[3] = {J->rmax_xy, J->rmax_xy, J->rmax_z};
-    const int refine[3] = {kRxy, kRxy, kZFine};
+    double ext0[3];
+    for (int a = 0; a < 3; a++) {
+        const bool per = geo.periodic[a] && geo.wrap[a] > 0.0;
+        ext0[a] = per ? geo.wrap[a] : hi[a] - lo[a];
+    }
+    const int rxy = choose_rxy(J, ext0);
+    const int refine[3] = {rxy, rxy, kZFine};
     for (int a = 0; a < 3; a++) {
         const bool per = geo.periodic[a] && geo.wrap[a] > 0.0;
         double ext = hi[a] - lo[a];
@@ -2280,6 +2322,7 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
             glo[a] = inbox ? 0.0 : lo[a];
             ghi[a] = inbox ? P->geo.wrap[a] : hi[a];
         }
+        P->J.n1 = (P->total1 + nbatch - 1) / nbatch;  // column width follows the mean catalogue density
         if ((rc = gpu_geometry(&P->J, P->geo, glo, ghi, P->g, P->delta)) != EXIT_SUCCESS) break;
         for (int a = 0; a < 3; a++) {
             const bool per = P->geo.periodic[a] && P->geo.wrap[a] > 0.0;
