@@ -47,6 +47,10 @@ namespace {
 
 constexpr int kChunk = 32;          // points per i-chunk (one per lane)
 constexpr int kCatShift = 17;       // Task::meta bits 17-31: catalogue of a batched count
+#ifndef CF_PAD_MIN
+#define CF_PAD_MIN 8
+#endif
+constexpr int kPadMin = CF_PAD_MIN;  // partial j tiles above this size run padded to 32
 constexpr uint32_t kJMax = 2048;    // max j points per task
 constexpr int kRxy = 2;             // lattice columns per rmax_xy
 constexpr int kZFine = 8;           // z slabs per rmax_z
@@ -689,6 +693,20 @@ __device__ __forceinline__ void accumulate(const PairArgs &A, WarpHist h, int hi
     if (NEED_W) atomicAdd(&((unsigned long long *)h.w)[hidx], (unsigned long long)__double2ll_rn(dw * (double)A.w_scale_f));
 }
 
+// Round a float x (|x| < 2^40, already scaled to fixed point) to a 64-bit integer with 32-bit
+// conversions only: on this GPU a 64-bit float-to-integer conversion runs on the FP64 pipe.
+// x = h * 2^20 + r with h = trunc(x / 2^20) and r = x - h * 2^20 exact (|r| < 2^20), then
+// round(x) = h * 2^20 + round(r).  Non-finite or larger x (rejected pairs, trash row) saturate.
+__device__ __forceinline__ long long fix64(float x)
+{
+    const int h = __float2int_rz(x * 9.5367431640625e-07f);  // x / 2^20
+    const float r = fmaf((float)h, -1048576.0f, x);
+    const int l = __float2int_rn(r);
+    long long v;
+    asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(v) : "r"(h), "r"(1 << 20), "l"((long long)l));
+    return v;
+}
+
 __device__ __forceinline__ void red_shared_u32(uint32_t saddr, uint32_t v)
 {
     asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(saddr), "r"(v));
@@ -751,7 +769,7 @@ __device__ __forceinline__ uint32_t pair_offset(const PairArgs &A, const float4 
         slow = (!rej && ((slow >> 31) || (real && amb))) ? 0x80000000u : 0u;
         off = (real && !rej && !amb) ? off + add : A.trash_off;
     }
-    if (NEED_W) vw = __float2ll_rn(wis * pj.w);
+    if (NEED_W) vw = fix64(wis * pj.w);
     if (NEED_AVG) {
         const float4 pjl = sjlo[k];
         const float dxp = dx + (pjl.x - xil), dyp = dy + (pjl.y - yil), dzp = dz + (pjl.z - zil);
@@ -764,7 +782,7 @@ __device__ __forceinline__ uint32_t pair_offset(const PairArgs &A, const float4 
         } else {
             favg = sqrtf(fmaf(dzp, dzp, fmaf(dyp, dyp, dxp * dxp)));
         }
-        vavg = __float2ll_rn(favg * A.avg_scale_f);
+        vavg = fix64(favg * A.avg_scale_f);
     }
     return off;
 }
@@ -954,11 +972,18 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
             zil = pl.z - A.olo[2][mz + 1];
         }
         for (uint32_t jb = T.j_begin; jb < T.j_end; jb += 32) {
-            const int nj = (int)min(32u, T.j_end - jb);
+            int nj = (int)min(32u, T.j_end - jb);
             if (lane < nj) {
                 sjhi[lane] = A.hi2[jb + lane];
                 if (NEED_AVG) sjlo[lane] = A.lo2[jb + lane];
+            } else if (nj > kPadMin) {
+                // pad a partial tile with far-away points and run it fully unrolled: q overflows to
+                // +inf (the reject bucket, zero weight) against valid i points and against the
+                // +1e30 stand-in of lanes without an i point alike
+                sjhi[lane] = make_float4(-1e30f, -1e30f, -1e30f, 0.f);
+                if (NEED_AVG) sjlo[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
             }
+            if (nj > kPadMin) nj = 32;
             __syncwarp();
             const float wi_s = pi.w * A.w_scale_f;
             uint32_t slowbits = own ? tile_fast<MODE, NEED_AVG, NEED_W, true>(A, sjhi, sjlo, lut, nj, jb, i, xi, yi, zi,
@@ -1804,7 +1829,7 @@ static void pair_constants(PairArgs &A, const cf_job *J, int mode, int nbins, bo
         A.inv_dmu_f = (float)A.inv_dmu;
         A.mu_band_abs = (float)(2.0 * (delta[2] + d3) * 2.0 + 1e-12);
     }
-    // fixed-point accumulator scales: one term must stay below 2^40
+    // fixed-point accumulator scales: one term stays below 2^40
     double avg_max = 1.0;
     if (mode == MODE_THETA) avg_max = 180.0;
     else avg_max = sqrt(fabs(J->edges[J->nedges - 1])) * 1.01 + 1e-300;
