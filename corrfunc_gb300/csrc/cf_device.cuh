@@ -98,8 +98,8 @@ struct PairArgs {
     float dxy_err;                 // bound on |(dx,dy)_f32 - (dx,dy)_ref|
 
     // fixed-point scales for the per-warp accumulators
-    float avg_scale_f;
-    double avg_unscale;
+    const float *g_ascale;      // per separation bin: fixed-point scale of the separation sums
+    int rbin_div;               // flat bin / rbin_div = separation bin (npibin + 1 for 2-D histograms)
     float w_scale_f;
     double w_unscale;
 };

@@ -67,7 +67,6 @@ constexpr int kZFine = 8;           // z slabs per rmax_z
 #define CF_PAIR_GROUP 8
 #endif
 
-constexpr uint64_t kFlushPairs = 1ull << 22;  // per-warp accumulator flush interval
 constexpr int kScanTile = 4096;
 
 // ------------------------------------------------------------------------------------
@@ -433,8 +432,9 @@ __global__ void k_task_emit(TaskGeom G, uint32_t nchunks, const uint32_t *chunk_
 struct SmemLayout {
     int nedges, nbins, warps, lut_n, lane_stride;
     int nrows;  // histogram rows incl. the trash rows that absorb rejected / deferred pairs
-    bool need_avg, need_w, fixed64;
-    size_t edges_off, guard_off, lut_off, stage_off, hist_off, per_warp_hist, per_warp_stage, total;
+    bool need_avg, need_w;
+    int entry_words;  // 32-bit words per histogram entry: count [, avg hi, avg lo] [, w hi, w lo]
+    size_t edges_off, guard_off, ascale_off, lut_off, stage_off, hist_off, per_warp_hist, per_warp_stage, total;
 };
 
 __host__ __device__ inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -447,17 +447,22 @@ struct RefineEntry {
 };
 
 // Histogram accumulators live in shared memory, one set per warp.  With lane_stride == 32 every
-// lane owns a private column (bank = lane, no conflicts, no contention); for large 2-D
-// histograms lane_stride == 1 and the lanes of a warp share one row through shared atomics.
-// Weight and separation sums are 64-bit fixed point (one term below 2^40, flushed into the FP64
-// global histogram at most every kFlushPairs pairs, so a column never exceeds 2^62).
+// lane owns a private column (no contention); for large 2-D histograms lanes share columns
+// through shared atomics.  An entry is 1, 3 or 5 consecutive 32-bit words: the count, then the
+// separation and weight sums as 32-bit fixed-point terms split into a signed high half (bits
+// 16-31) and an unsigned low half (bits 0-15).  Only 32-bit shared reductions are used: 64-bit
+// and floating-point shared atomics run several times slower on this GPU.  Odd entry sizes keep
+// the private columns on distinct banks.  A column takes at most kColumnTerms terms between
+// flushes into the FP64 global histogram, so neither half can overflow.
+constexpr int kColumnTerms = 1 << 15;
+
 __host__ __device__ inline SmemLayout smem_layout(int nedges, int nbins, int warps, bool f64, int lut_n, int lane_stride,
                                                   bool need_avg, bool need_w, bool store_dz)
 {
     SmemLayout L;
     L.need_avg = need_avg;
     L.need_w = need_w;
-    L.fixed64 = true;
+    L.entry_words = 1 + (need_avg ? 2 : 0) + (need_w ? 2 : 0);
     (void)f64;
     L.nedges = nedges;
     L.nbins = nbins;
@@ -471,6 +476,8 @@ __host__ __device__ inline SmemLayout smem_layout(int nedges, int nbins, int war
     o = align_up(o + sizeof(double) * nedges, 16);
     L.guard_off = o;
     o = align_up(o + sizeof(float) * 2 * nedges, 16);
+    L.ascale_off = o;
+    o = align_up(o + sizeof(float) * nedges, 16);
     L.lut_off = o;
     o = align_up(o + sizeof(uint32_t) * (lut_n + 1), 16);
     L.stage_off = o;
@@ -479,52 +486,48 @@ __host__ __device__ inline SmemLayout smem_layout(int nedges, int nbins, int war
                            : (64 * sizeof(float4) + (kRefineQueue + kSlowQueue) * sizeof(RefineEntry) + 16);
     o = align_up(o + L.per_warp_stage * warps, 16);
     L.hist_off = o;
-    const size_t vb = 8;
-    L.per_warp_hist = align_up((size_t)L.nrows * lane_stride * (4 + (need_avg ? vb : 0) + (need_w ? vb : 0)) + 32, 16);
+    L.per_warp_hist = align_up((size_t)L.nrows * lane_stride * 4 * L.entry_words + 32, 16);
     o += L.per_warp_hist * warps;
     L.total = o;
     return L;
 }
 
 struct WarpHist {
-    void *avg;
-    void *w;
-    uint32_t *cnt;
-    int ls;  // lane stride
+    uint32_t *e;          // entries: (row * ls + column) * ew words
+    int ls;               // lane stride
+    int ew;               // words per entry
+    const float *ascale;  // fixed-point scale of the separation sums per separation bin (shared)
 };
 
 __device__ __forceinline__ WarpHist warp_hist(unsigned char *smem, const SmemLayout &L, int warp)
 {
-    unsigned char *p = smem + L.hist_off + L.per_warp_hist * warp;
-    const size_t n = (size_t)L.nrows * L.lane_stride;
-    const size_t vb = 8;
     WarpHist h;
-    size_t o = 0;
-    h.avg = (void *)(p + o);
-    if (L.need_avg) o += vb * n;
-    h.w = (void *)(p + o);
-    if (L.need_w) o += vb * n;
-    h.cnt = (uint32_t *)(p + o);
+    h.e = (uint32_t *)(smem + L.hist_off + L.per_warp_hist * warp);
     h.ls = L.lane_stride;
+    h.ew = L.entry_words;
+    h.ascale = (const float *)(smem + L.ascale_off);
     return h;
 }
 
 __device__ __forceinline__ void zero_hist(WarpHist h, const SmemLayout &L, int lane)
 {
-    const int n = L.nrows * h.ls;
-    for (int b = lane; b < n; b += 32) {
-        h.cnt[b] = 0;
-        if (L.fixed64) {
-            if (L.need_avg) ((unsigned long long *)h.avg)[b] = 0;
-            if (L.need_w) ((unsigned long long *)h.w)[b] = 0;
-        } else {
-            if (L.need_avg) ((float *)h.avg)[b] = 0.f;
-            if (L.need_w) ((float *)h.w)[b] = 0.f;
-        }
-    }
+    const int n = L.nrows * h.ls * h.ew;
+    for (int b = lane; b < n; b += 32) h.e[b] = 0;
 }
 
-template <bool NEED_AVG, bool NEED_W, bool FIXED64>
+// word offsets of the sums inside an entry
+template <bool NEED_AVG>
+__host__ __device__ constexpr int avg_word() { return 1; }
+template <bool NEED_AVG>
+__host__ __device__ constexpr int w_word() { return NEED_AVG ? 3 : 1; }
+
+__device__ __forceinline__ void add_term(uint32_t *hi_lo, int v)
+{
+    atomicAdd(hi_lo, (uint32_t)(v >> 16));
+    atomicAdd(hi_lo + 1, (uint32_t)v & 0xffffu);
+}
+
+template <bool NEED_AVG, bool NEED_W>
 __device__ __forceinline__ void flush_hist(const PairArgs &A, WarpHist h, int lane, uint32_t cat = 0)
 {
     __syncwarp();
@@ -532,41 +535,36 @@ __device__ __forceinline__ void flush_hist(const PairArgs &A, WarpHist h, int la
     double *g_avg = A.g_avg + (size_t)cat * A.nbins;
     double *g_w = A.g_w + (size_t)cat * A.nbins;
     for (int b = lane; b < A.nbins; b += 32) {
-        unsigned long long c = 0;
-        long long va = 0, vw = 0;
-        double fa = 0.0, fw = 0.0;
+        unsigned long long c = 0, al = 0, wl = 0;
+        long long ah = 0, wh = 0;
         for (int t = 0; t < h.ls; t++) {
             const int l = (t + lane) & (h.ls - 1);  // skewed so that the lanes hit distinct banks
-            const int idx = b * h.ls + l;
-            c += h.cnt[idx];
-            h.cnt[idx] = 0;
-            if (FIXED64) {
-                if (NEED_AVG) {
-                    va += ((long long *)h.avg)[idx];
-                    ((long long *)h.avg)[idx] = 0;
-                }
-                if (NEED_W) {
-                    vw += ((long long *)h.w)[idx];
-                    ((long long *)h.w)[idx] = 0;
-                }
-            } else {
-                if (NEED_AVG) {
-                    fa += (double)((float *)h.avg)[idx];
-                    ((float *)h.avg)[idx] = 0.f;
-                }
-                if (NEED_W) {
-                    fw += (double)((float *)h.w)[idx];
-                    ((float *)h.w)[idx] = 0.f;
-                }
+            uint32_t *e = h.e + (size_t)(b * h.ls + l) * h.ew;
+            c += e[0];
+            e[0] = 0;
+            if (NEED_AVG) {
+                uint32_t *s = e + avg_word<NEED_AVG>();
+                ah += (int)s[0];
+                al += s[1];
+                s[0] = 0;
+                s[1] = 0;
+            }
+            if (NEED_W) {
+                uint32_t *s = e + w_word<NEED_AVG>();
+                wh += (int)s[0];
+                wl += s[1];
+                s[0] = 0;
+                s[1] = 0;
             }
         }
         if (c) atomicAdd(&g_cnt[b], c);
-        if (FIXED64) {
-            if (NEED_AVG && va) atomicAdd(&g_avg[b], (double)va * A.avg_unscale);
-            if (NEED_W && vw) atomicAdd(&g_w[b], (double)vw * A.w_unscale);
-        } else {
-            if (NEED_AVG && fa != 0.0) atomicAdd(&g_avg[b], fa);
-            if (NEED_W && fw != 0.0) atomicAdd(&g_w[b], fw);
+        if (NEED_AVG) {
+            const long long va = ah * 65536ll + (long long)al;
+            if (va) atomicAdd(&g_avg[b], (double)va / (double)h.ascale[b / A.rbin_div]);
+        }
+        if (NEED_W) {
+            const long long vw = wh * 65536ll + (long long)wl;
+            if (vw) atomicAdd(&g_w[b], (double)vw * A.w_unscale);
         }
     }
     __syncwarp();
@@ -685,26 +683,14 @@ __device__ __noinline__ int slow_candidate(const PairArgs &A, const float *glo, 
     return bin;
 }
 
+// one pair of flat bin `bin` into column entry hidx (slow path, FP64 path)
 template <bool NEED_AVG, bool NEED_W>
-__device__ __forceinline__ void accumulate(const PairArgs &A, WarpHist h, int hidx, double davg, double dw)
+__device__ __forceinline__ void accumulate(const PairArgs &A, WarpHist h, int bin, int hidx, double davg, double dw)
 {
-    atomicAdd(&h.cnt[hidx], 1u);
-    if (NEED_AVG) atomicAdd(&((unsigned long long *)h.avg)[hidx], (unsigned long long)__double2ll_rn(davg * (double)A.avg_scale_f));
-    if (NEED_W) atomicAdd(&((unsigned long long *)h.w)[hidx], (unsigned long long)__double2ll_rn(dw * (double)A.w_scale_f));
-}
-
-// Round a float x (|x| < 2^40, already scaled to fixed point) to a 64-bit integer with 32-bit
-// conversions only: on this GPU a 64-bit float-to-integer conversion runs on the FP64 pipe.
-// x = h * 2^20 + r with h = trunc(x / 2^20) and r = x - h * 2^20 exact (|r| < 2^20), then
-// round(x) = h * 2^20 + round(r).  Non-finite or larger x (rejected pairs, trash row) saturate.
-__device__ __forceinline__ long long fix64(float x)
-{
-    const int h = __float2int_rz(x * 9.5367431640625e-07f);  // x / 2^20
-    const float r = fmaf((float)h, -1048576.0f, x);
-    const int l = __float2int_rn(r);
-    long long v;
-    asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(v) : "r"(h), "r"(1 << 20), "l"((long long)l));
-    return v;
+    uint32_t *e = h.e + (size_t)hidx * h.ew;
+    atomicAdd(e, 1u);
+    if (NEED_AVG) add_term(e + avg_word<NEED_AVG>(), __double2int_rn(davg * (double)h.ascale[bin / A.rbin_div]));
+    if (NEED_W) add_term(e + w_word<NEED_AVG>(), __double2int_rn(dw * (double)A.w_scale_f));
 }
 
 __device__ __forceinline__ void red_shared_u32(uint32_t saddr, uint32_t v)
@@ -712,9 +698,10 @@ __device__ __forceinline__ void red_shared_u32(uint32_t saddr, uint32_t v)
     asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(saddr), "r"(v));
 }
 
-__device__ __forceinline__ void red_shared_u64(uint32_t saddr, unsigned long long v)
+template <int IMM>
+__device__ __forceinline__ void red_shared_u32_at(uint32_t saddr, uint32_t v)
 {
-    asm volatile("red.shared.add.u64 [%0], %1;" ::"r"(saddr), "l"(v));
+    asm volatile("red.shared.add.u32 [%0+%2], %1;" ::"r"(saddr), "r"(v), "n"(IMM));
 }
 
 // Fast classification of one pair.  k is the tile position (compile-time in full tiles).  The
@@ -724,9 +711,9 @@ __device__ __forceinline__ void red_shared_u64(uint32_t saddr, unsigned long lon
 template <int MODE, bool NEED_AVG, bool NEED_W, bool OWN>
 __device__ __forceinline__ uint32_t pair_offset(const PairArgs &A, const float4 *__restrict__ sjhi,
                                                 const float4 *__restrict__ sjlo, const uint32_t *__restrict__ lut,
-                                                int k, uint32_t jb, uint32_t i, float xi, float yi, float zi,
+                                                const float *__restrict__ ascale, int k, uint32_t jb, uint32_t i, float xi, float yi, float zi,
                                                 float xil, float yil, float zil, float wis, uint32_t &slow,
-                                                long long &vw, long long &vavg)
+                                                int &vw, int &vavg)
 {
     const float4 pj = sjhi[k];
     const float dx = pj.x - xi, dy = pj.y - yi, dz = pj.z - zi;
@@ -735,8 +722,8 @@ __device__ __forceinline__ uint32_t pair_offset(const PairArgs &A, const float4 
     if (MODE == MODE_RPPI || MODE == MODE_WP) q = fmaf(dy, dy, fmaf(dx, dx, A.q_floor));
     else q = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, A.q_floor)));
     const uint32_t e = lut[lut_bucket(A, q)];
-    uint32_t off = e & 0x7fffffffu;
-    slow = e;  // bit 31: flagged bucket
+    uint32_t off = e & 0x003fffffu;  // bits 0-21: row byte offset, 22-30: separation bin, 31: flagged
+    slow = e;
     if (OWN) {
         const bool keep = jb + (uint32_t)k > i;
         off = keep ? off : A.trash_off;
@@ -769,7 +756,7 @@ __device__ __forceinline__ uint32_t pair_offset(const PairArgs &A, const float4 
         slow = (!rej && ((slow >> 31) || (real && amb))) ? 0x80000000u : 0u;
         off = (real && !rej && !amb) ? off + add : A.trash_off;
     }
-    if (NEED_W) vw = fix64(wis * pj.w);
+    if (NEED_W) vw = __float2int_rn(wis * pj.w);  // 32-bit term (rejected pairs saturate into the trash row)
     if (NEED_AVG) {
         const float4 pjl = sjlo[k];
         const float dxp = dx + (pjl.x - xil), dyp = dy + (pjl.y - yil), dzp = dz + (pjl.z - zil);
@@ -782,53 +769,61 @@ __device__ __forceinline__ uint32_t pair_offset(const PairArgs &A, const float4 
         } else {
             favg = sqrtf(fmaf(dzp, dzp, fmaf(dyp, dyp, dxp * dxp)));
         }
-        vavg = fix64(favg * A.avg_scale_f);
+        vavg = __float2int_rn(favg * ascale[(e >> 22) & 0x1ffu]);
     }
     return off;
 }
 
 template <int MODE, bool NEED_AVG, bool NEED_W, bool OWN, int U>
 __device__ __forceinline__ void pairs_group(const PairArgs &A, const float4 *__restrict__ sjhi,
-                                            const float4 *__restrict__ sjlo, const uint32_t *__restrict__ lut, int k0,
+                                            const float4 *__restrict__ sjlo, const uint32_t *__restrict__ lut,
+                                            const float *__restrict__ ascale, int k0,
                                             uint32_t jb, uint32_t i, float xi, float yi, float zi, float xil, float yil,
-                                            float zil, float wis, uint32_t cnt_s, uint32_t avg_s, uint32_t w_s,
-                                            uint32_t &slowbits)
+                                            float zil, float wis, uint32_t cnt_s, uint32_t &slowbits)
 {
     uint32_t off[U];
-    long long vw[U], va[U];
+    int vw[U], va[U];
 #pragma unroll
     for (int u = 0; u < U; u++) {
         uint32_t sl;
         vw[u] = 0;
         va[u] = 0;
-        off[u] = pair_offset<MODE, NEED_AVG, NEED_W, OWN>(A, sjhi, sjlo, lut, k0 + u, jb, i, xi, yi, zi, xil, yil, zil,
+        off[u] = pair_offset<MODE, NEED_AVG, NEED_W, OWN>(A, sjhi, sjlo, lut, ascale, k0 + u, jb, i, xi, yi, zi, xil, yil, zil,
                                                           wis, sl, vw[u], va[u]);
         slowbits = __funnelshift_l(sl, slowbits, 1);  // pair k of n ends at bit n - 1 - k
     }
 #pragma unroll
     for (int u = 0; u < U; u++) {
-        red_shared_u32(cnt_s + off[u], 1u);
-        if (NEED_W) red_shared_u64(w_s + 2 * off[u], (unsigned long long)vw[u]);
-        if (NEED_AVG) red_shared_u64(avg_s + 2 * off[u], (unsigned long long)va[u]);
+        const uint32_t e = cnt_s + off[u];  // this lane's entry in the pair's row
+        red_shared_u32_at<0>(e, 1u);
+        if (NEED_AVG) {
+            red_shared_u32_at<4 * avg_word<NEED_AVG>()>(e, (uint32_t)(va[u] >> 16));
+            red_shared_u32_at<4 * avg_word<NEED_AVG>() + 4>(e, (uint32_t)va[u] & 0xffffu);
+        }
+        if (NEED_W) {
+            red_shared_u32_at<4 * w_word<NEED_AVG>()>(e, (uint32_t)(vw[u] >> 16));
+            red_shared_u32_at<4 * w_word<NEED_AVG>() + 4>(e, (uint32_t)vw[u] & 0xffffu);
+        }
     }
 }
 
 template <int MODE, bool NEED_AVG, bool NEED_W, bool OWN>
 __device__ __forceinline__ uint32_t tile_fast(const PairArgs &A, const float4 *__restrict__ sjhi,
-                                              const float4 *__restrict__ sjlo, const uint32_t *__restrict__ lut, int nj,
+                                              const float4 *__restrict__ sjlo, const uint32_t *__restrict__ lut,
+                                              const float *__restrict__ ascale, int nj,
                                               uint32_t jb, uint32_t i, float xi, float yi, float zi, float xil, float yil,
-                                              float zil, float wis, uint32_t cnt_s, uint32_t avg_s, uint32_t w_s)
+                                              float zil, float wis, uint32_t cnt_s)
 {
     uint32_t slowbits = 0;
     if (nj == 32) {
 #pragma unroll
         for (int k0 = 0; k0 < 32; k0 += CF_PAIR_GROUP)
-            pairs_group<MODE, NEED_AVG, NEED_W, OWN, CF_PAIR_GROUP>(A, sjhi, sjlo, lut, k0, jb, i, xi, yi, zi, xil, yil, zil, wis,
-                                                        cnt_s, avg_s, w_s, slowbits);
+            pairs_group<MODE, NEED_AVG, NEED_W, OWN, CF_PAIR_GROUP>(A, sjhi, sjlo, lut, ascale, k0, jb, i, xi, yi, zi, xil,
+                                                                    yil, zil, wis, cnt_s, slowbits);
     } else {
         for (int k = 0; k < nj; k++)
-            pairs_group<MODE, NEED_AVG, NEED_W, OWN, 1>(A, sjhi, sjlo, lut, k, jb, i, xi, yi, zi, xil, yil, zil, wis,
-                                                        cnt_s, avg_s, w_s, slowbits);
+            pairs_group<MODE, NEED_AVG, NEED_W, OWN, 1>(A, sjhi, sjlo, lut, ascale, k, jb, i, xi, yi, zi, xil, yil, zil, wis,
+                                                        cnt_s, slowbits);
     }
     return slowbits;
 }
@@ -844,7 +839,7 @@ __device__ __noinline__ void refine_batch(const PairArgs &A, const double *se, c
                   mz = (int)((r.meta >> 12) & 3u) - 1;
         double davg = 0.0, dw = 0.0;
         const int bin = refine_pair<MODE>(A, se, r.i, r.j, mx, my, mz, &davg, &dw);
-        if (bin >= 0) accumulate<NEED_AVG, NEED_W>(A, h, bin * h.ls + hl, davg, dw);
+        if (bin >= 0) accumulate<NEED_AVG, NEED_W>(A, h, bin, bin * h.ls + hl, davg, dw);
     }
     __syncwarp();
 }
@@ -879,7 +874,7 @@ __device__ __noinline__ void slow_batch(const PairArgs &A, const double *se, con
         const int bin = slow_candidate<MODE, NEED_AVG, NEED_W>(A, glo, ghi, pj, pjl, xi, yi, zi, xil, yil, zil, pi.w,
                                                                &favg, &fw);
         if (bin >= 0) {
-            accumulate<NEED_AVG, NEED_W>(A, h, bin * h.ls + hl, (double)favg, (double)fw);
+            accumulate<NEED_AVG, NEED_W>(A, h, bin, bin * h.ls + hl, (double)favg, (double)fw);
         } else if (bin == -2) {
             const int pos = atomicAdd(rq_count, 1);
             rq[pos] = e;
@@ -904,10 +899,12 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
     float *glo = (float *)(smem + SL.guard_off);
     float *ghi = glo + A.nedges;
     uint32_t *lut = (uint32_t *)(smem + SL.lut_off);
+    float *asc = (float *)(smem + SL.ascale_off);
     for (int k = threadIdx.x; k < A.nedges; k += blockDim.x) {
         se[k] = A.g_edges[k];
         glo[k] = A.g_guard[k];
         ghi[k] = A.g_guard[A.nedges + k];
+        asc[k] = A.g_ascale[k];
     }
     for (int k = threadIdx.x; k <= SL.lut_n; k += blockDim.x) lut[k] = A.g_lut[k];
     float4 *sjhi = (float4 *)(smem + SL.stage_off + SL.per_warp_stage * warp);
@@ -920,16 +917,17 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
     zero_hist(h, SL, lane);
     if (lane == 0) *rq_count = 0;
     const int hl = lane & (SL.lane_stride - 1);
-    // shared-window addresses of this lane's column: count rows are 4 bytes apart per lane stride,
-    // the 64-bit sum rows twice that (offset doubled at the reduction)
-    const uint32_t cnt_s = (uint32_t)__cvta_generic_to_shared(h.cnt) + 4u * hl;
-    const uint32_t avg_s = (uint32_t)__cvta_generic_to_shared(h.avg) + 8u * hl;
-    const uint32_t w_s = (uint32_t)__cvta_generic_to_shared(h.w) + 8u * hl;
+    // shared-window address of this lane's entry in row 0; a pair's table entry is its row offset
+    const uint32_t cnt_s = (uint32_t)__cvta_generic_to_shared(h.e) + 4u * h.ew * hl;
     __syncthreads();
-    uint64_t since_flush = 0, evaluated = 0;
+    uint64_t evaluated = 0;
     unsigned long long refined = 0;
     const uint32_t ntasks = A.ntask_dev ? min(*A.ntask_dev, A.ntasks) : A.ntasks;
     uint32_t cur_cat = 0;  // catalogue whose counts the warp's histogram holds (batched counts)
+    // terms a column may have taken since the last flush: per tile 32 fast-path pairs per lane
+    // sharing the column, plus at most 32 slow-queue and 32 FP64 terms
+    uint32_t col_terms = 0;
+    const uint32_t tile_terms = 32u * (32u / (uint32_t)SL.lane_stride) + 64u;
 
     while (true) {
         uint32_t t = 0;
@@ -951,9 +949,9 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
                 if (lane == 0) *rq_count = 0;
                 __syncwarp();
             }
-            flush_hist<NEED_AVG, NEED_W, true>(A, h, lane, cur_cat);
+            flush_hist<NEED_AVG, NEED_W>(A, h, lane, cur_cat);
             cur_cat = cat;
-            since_flush = 0;
+            col_terms = 0;
         }
         const int icount = (int)(T.meta & 63u) + 1;
         const int mx = (int)((T.meta >> 8) & 3u) - 1, my = (int)((T.meta >> 10) & 3u) - 1,
@@ -986,10 +984,10 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
             if (nj > kPadMin) nj = 32;
             __syncwarp();
             const float wi_s = pi.w * A.w_scale_f;
-            uint32_t slowbits = own ? tile_fast<MODE, NEED_AVG, NEED_W, true>(A, sjhi, sjlo, lut, nj, jb, i, xi, yi, zi,
-                                                                           xil, yil, zil, wi_s, cnt_s, avg_s, w_s)
-                                    : tile_fast<MODE, NEED_AVG, NEED_W, false>(A, sjhi, sjlo, lut, nj, jb, i, xi, yi,
-                                                                            zi, xil, yil, zil, wi_s, cnt_s, avg_s, w_s);
+            uint32_t slowbits = own ? tile_fast<MODE, NEED_AVG, NEED_W, true>(A, sjhi, sjlo, lut, h.ascale, nj, jb, i, xi, yi, zi,
+                                                                           xil, yil, zil, wi_s, cnt_s)
+                                    : tile_fast<MODE, NEED_AVG, NEED_W, false>(A, sjhi, sjlo, lut, h.ascale, nj, jb, i, xi, yi,
+                                                                            zi, xil, yil, zil, wi_s, cnt_s);
             // candidates in flagged buckets go to the warp's slow queue, one bit per lane per round
             // (a round appends at most 32 entries, so the queue never holds more than 63)
             while (true) {
@@ -1013,20 +1011,19 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
                 }
             }
             __syncwarp();
+            col_terms += tile_terms;
+            if (col_terms + tile_terms > (uint32_t)kColumnTerms) {
+                flush_hist<NEED_AVG, NEED_W>(A, h, lane, cur_cat);
+                col_terms = 0;
+            }
         }
-        const uint64_t np = (uint64_t)icount * (T.j_end - T.j_begin);
-        since_flush += np;
-        evaluated += np;
-        if (since_flush > kFlushPairs) {
-            flush_hist<NEED_AVG, NEED_W, true>(A, h, lane, cur_cat);
-            since_flush = 0;
-        }
+        evaluated += (uint64_t)icount * (T.j_end - T.j_begin);
     }
     __syncwarp();
     if (sq_n > 0) slow_batch<MODE, NEED_AVG, NEED_W>(A, se, glo, ghi, sq, sq_n, rq, rq_count, h, hl, lane, &refined);
     const int rest = *rq_count;
     if (rest > 0) refine_batch<MODE, NEED_AVG, NEED_W>(A, se, rq, rest, h, hl, lane);
-    flush_hist<NEED_AVG, NEED_W, true>(A, h, lane, cur_cat);
+    flush_hist<NEED_AVG, NEED_W>(A, h, lane, cur_cat);
     for (int off = 16; off; off >>= 1) refined += __shfl_down_sync(0xffffffffu, refined, off);
     if (lane == 0) {
         atomicAdd(&A.g_stats[0], (unsigned long long)evaluated);
@@ -1040,7 +1037,11 @@ __global__ void __launch_bounds__(256) k_pairs_f64(PairArgs A, SmemLayout SL)
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     double *se = (double *)(smem + SL.edges_off);
-    for (int k = threadIdx.x; k < A.nedges; k += blockDim.x) se[k] = A.g_edges[k];
+    float *asc = (float *)(smem + SL.ascale_off);
+    for (int k = threadIdx.x; k < A.nedges; k += blockDim.x) {
+        se[k] = A.g_edges[k];
+        asc[k] = A.g_ascale[k];
+    }
     double4_32a *sj = (double4_32a *)(smem + SL.stage_off + SL.per_warp_stage * warp);
     int *srcell = (int *)(sj + 32);
     int *sorig = srcell + 32;
@@ -1048,10 +1049,11 @@ __global__ void __launch_bounds__(256) k_pairs_f64(PairArgs A, SmemLayout SL)
     zero_hist(h, SL, lane);
     const int hl = lane & (SL.lane_stride - 1);
     __syncthreads();
-    uint64_t since_flush = 0, evaluated = 0;
-    const double avg_scale = (double)A.avg_scale_f, w_scale = (double)A.w_scale_f;
+    uint64_t evaluated = 0;
     const uint32_t ntasks = A.ntask_dev ? min(*A.ntask_dev, A.ntasks) : A.ntasks;
     uint32_t cur_cat = 0;
+    uint32_t col_terms = 0;
+    const uint32_t tile_terms = 32u * (32u / (uint32_t)SL.lane_stride);
 
     while (true) {
         uint32_t t = 0;
@@ -1061,9 +1063,9 @@ __global__ void __launch_bounds__(256) k_pairs_f64(PairArgs A, SmemLayout SL)
         const Task T = A.tasks[t];
         const uint32_t cat = T.meta >> kCatShift;
         if (cat != cur_cat) {
-            flush_hist<NEED_AVG, NEED_W, true>(A, h, lane, cur_cat);
+            flush_hist<NEED_AVG, NEED_W>(A, h, lane, cur_cat);
             cur_cat = cat;
-            since_flush = 0;
+            col_terms = 0;
         }
         const int icount = (int)(T.meta & 63u) + 1;
         const int mx = (int)((T.meta >> 8) & 3u) - 1, my = (int)((T.meta >> 10) & 3u) - 1,
@@ -1098,25 +1100,19 @@ __global__ void __launch_bounds__(256) k_pairs_f64(PairArgs A, SmemLayout SL)
                         bin = ref_eval<MODE>(A, se, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, -ox, -oy, -oz, &avg_term);
                     }
                     if (bin < 0) continue;
-                    const int hidx = bin * h.ls + hl;
-                    atomicAdd(&h.cnt[hidx], 1u);
-                    if (NEED_AVG)
-                        atomicAdd(&((unsigned long long *)h.avg)[hidx], (unsigned long long)__double2ll_rn(avg_term * avg_scale));
-                    if (NEED_W)
-                        atomicAdd(&((unsigned long long *)h.w)[hidx], (unsigned long long)__double2ll_rn(pi.w * pj.w * w_scale));
+                    accumulate<NEED_AVG, NEED_W>(A, h, bin, bin * h.ls + hl, avg_term, pi.w * pj.w);
                 }
             }
             __syncwarp();
+            col_terms += tile_terms;
+            if (col_terms + tile_terms > (uint32_t)kColumnTerms) {
+                flush_hist<NEED_AVG, NEED_W>(A, h, lane, cur_cat);
+                col_terms = 0;
+            }
         }
-        const uint64_t np = (uint64_t)icount * (T.j_end - T.j_begin);
-        since_flush += np;
-        evaluated += np;
-        if (since_flush > kFlushPairs) {
-            flush_hist<NEED_AVG, NEED_W, true>(A, h, lane, cur_cat);
-            since_flush = 0;
-        }
+        evaluated += (uint64_t)icount * (T.j_end - T.j_begin);
     }
-    flush_hist<NEED_AVG, NEED_W, true>(A, h, lane, cur_cat);
+    flush_hist<NEED_AVG, NEED_W>(A, h, lane, cur_cat);
     if (lane == 0) atomicAdd(&A.g_stats[0], (unsigned long long)evaluated);
 }
 
@@ -1191,7 +1187,7 @@ struct SetBufs {
 struct Workspace {
     SetBufs set[2];
     DevBuf mm, oob, scan_tmp[4], chunk_cnt, chunk_off, chunk_begin, chunk_count, chunk_cat, ntask, task_off, tasks;
-    DevBuf hist_cnt, hist_avg, hist_w, stats, counter, edges, guards, lut;
+    DevBuf hist_cnt, hist_avg, hist_w, stats, counter, edges, guards, lut, ascale;
     HostBuf h_small, h_tab, h_hist;
 };
 
@@ -1213,7 +1209,7 @@ static void release_workspace(Workspace &W)
     for (int k = 0; k < 4; k++) release(W.scan_tmp[k]);
     DevBuf *v[] = {&W.mm, &W.oob, &W.chunk_cnt, &W.chunk_off, &W.chunk_begin, &W.chunk_count, &W.chunk_cat, &W.ntask,
                    &W.task_off, &W.tasks, &W.hist_cnt, &W.hist_avg, &W.hist_w, &W.stats, &W.counter, &W.edges,
-                   &W.guards, &W.lut};
+                   &W.guards, &W.lut, &W.ascale};
     for (DevBuf *d : v) release(*d);
     HostBuf *h[] = {&W.h_small, &W.h_tab, &W.h_hist};
     for (HostBuf *b : h) {
@@ -1567,14 +1563,27 @@ static int build_tables(Workspace &W, const cf_job *J, int mode, int nbins, bool
     T->d3 = d3;
     const double dlim = (mode == MODE_RPPI || mode == MODE_WP) ? dxy : d3;
     // guards: for theta the classified quantity is the squared chord 2*(1 - cos)
-    if (ensure(W.edges, sizeof(double) * J->nedges) || ensure(W.guards, sizeof(float) * 2 * J->nedges))
+    if (ensure(W.edges, sizeof(double) * J->nedges) || ensure(W.guards, sizeof(float) * 2 * J->nedges) ||
+        ensure(W.ascale, sizeof(float) * J->nedges))
         return EXIT_FAILURE;
-    const size_t tab_bytes = sizeof(double) * CF_MAX_EDGES + sizeof(float) * 2 * CF_MAX_EDGES + sizeof(uint32_t) * 4100;
+    const size_t tab_bytes = sizeof(double) * CF_MAX_EDGES + sizeof(float) * 3 * CF_MAX_EDGES + sizeof(uint32_t) * 4100;
     if (ensure_host(W.h_tab, tab_bytes) != EXIT_SUCCESS) return EXIT_FAILURE;
     double *edges_h = (double *)W.h_tab.p;
     float *guards_h = (float *)(edges_h + CF_MAX_EDGES);
-    uint32_t *lut_h = (uint32_t *)(guards_h + 2 * CF_MAX_EDGES);
+    float *ascale_h = guards_h + 2 * CF_MAX_EDGES;
+    uint32_t *lut_h = (uint32_t *)(ascale_h + CF_MAX_EDGES);
     memcpy(edges_h, J->edges, sizeof(double) * J->nedges);
+    // fixed-point scale of the separation sums per separation bin m (values in [edge m-1, edge m)):
+    // one term stays below 2^30, i.e. a relative resolution of 2^-30 of the bin's upper edge
+    for (int m = 0; m < J->nedges; m++) {
+        const int mm = m > 0 ? m : (J->nedges > 1 ? 1 : 0);
+        double top = mode == MODE_THETA ? acos(fmax(-1.0, fmin(1.0, J->edges[mm]))) * 57.29577951308232
+                                        : sqrt(fabs(J->edges[mm]));
+        top = fmax(top * 1.01, 1e-30);
+        int ex = 30 - (int)ceil(log2(top));
+        ex = ex > 100 ? 100 : (ex < -100 ? -100 : ex);
+        ascale_h[m] = (float)ldexp(1.0, ex);
+    }
     for (int k = 0; k < J->nedges; k++) {
         double e = J->edges[k];
         double band;
@@ -1607,8 +1616,10 @@ static int build_tables(Workspace &W, const cf_job *J, int mode, int nbins, bool
     // row byte offsets: the layout (private columns or shared row) is fixed before the launch
     const int ls = choose_layout(mode, false, J->need_avg != 0, need_w, J->nedges, nbins, n).lane_stride;
     const uint32_t ostride = (mode == MODE_RPPI || mode == MODE_SMU) ? (uint32_t)(J->npibin + 1) : 1u;
-    const uint32_t row_bytes = (uint32_t)(4 * ls);
+    const int ew = 1 + (J->need_avg ? 2 : 0) + (need_w ? 2 : 0);  // words per histogram entry
+    const uint32_t row_bytes = (uint32_t)(4 * ew * ls);
     const uint32_t trash = (uint32_t)nbins * row_bytes;
+    if ((size_t)(nbins + J->npibin + 2) * row_bytes >= (1u << 22)) CF_FAIL("internal: histogram rows beyond the table's offset field");
     const float *glo_h = guards_h, *ghi_h = guards_h + J->nedges;
     int mlo = 0, mhi = 0;  // both non-decreasing in the bucket index
     for (int t = 0; t < n; t++) {
@@ -1621,12 +1632,13 @@ static int build_tables(Workspace &W, const cf_job *J, int mode, int nbins, bool
         while (mhi < J->nedges && glo_h[mhi] <= vhi) mhi++;
         const bool definite = (mlo == mhi) && mlo >= 1 && mlo < J->nedges && vlo >= ghi_h[mlo - 1] &&
                               vhi < ghi_h[J->nedges - 1];
-        lut_h[t] = definite ? (uint32_t)mlo * ostride * row_bytes : (trash | 0x80000000u);
+        lut_h[t] = definite ? ((uint32_t)mlo * ostride * row_bytes | ((uint32_t)mlo << 22)) : (trash | 0x80000000u);
     }
     lut_h[n] = trash;  // reject: below the first bucket (q < rmin^2) or above the last (q >= rmax^2)
     CF_CUDA(cudaMemcpyAsync(W.lut.p, lut_h, sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice, st));
     CF_CUDA(cudaMemcpyAsync(W.edges.p, edges_h, sizeof(double) * J->nedges, cudaMemcpyHostToDevice, st));
     CF_CUDA(cudaMemcpyAsync(W.guards.p, guards_h, sizeof(float) * 2 * J->nedges, cudaMemcpyHostToDevice, st));
+    CF_CUDA(cudaMemcpyAsync(W.ascale.p, ascale_h, sizeof(float) * J->nedges, cudaMemcpyHostToDevice, st));
     T->lut_n = n;
     T->shift = shift;
     T->base = base;
@@ -1792,6 +1804,8 @@ static void pair_constants(PairArgs &A, const cf_job *J, int mode, int nbins, bo
     }
     const double dxy = T.dxy, d3 = T.d3;
     A.g_lut = (const uint32_t *)W.lut.p;
+    A.g_ascale = (const float *)W.ascale.p;
+    A.rbin_div = (mode == MODE_RPPI || mode == MODE_SMU) ? J->npibin + 1 : 1;
     A.trash_off = T.trash;
     A.row_bytes = T.row_bytes;
     A.lane_stride_hint = T.ls;
@@ -1829,15 +1843,9 @@ static void pair_constants(PairArgs &A, const cf_job *J, int mode, int nbins, bo
         A.inv_dmu_f = (float)A.inv_dmu;
         A.mu_band_abs = (float)(2.0 * (delta[2] + d3) * 2.0 + 1e-12);
     }
-    // fixed-point accumulator scales: one term stays below 2^40
-    double avg_max = 1.0;
-    if (mode == MODE_THETA) avg_max = 180.0;
-    else avg_max = sqrt(fabs(J->edges[J->nedges - 1])) * 1.01 + 1e-300;
-    const int sa = 40 - (int)ceil(log2(avg_max));
-    A.avg_scale_f = (float)ldexp(1.0, sa);
-    A.avg_unscale = ldexp(1.0, -sa);
+    // weight sums: one term wi * wj stays below 2^30 (relative resolution 2^-30 of the largest product)
     const double w2 = fmax(wmax[0] * wmax[1], 1e-30) * 1.01;
-    int sw = 40 - (int)ceil(log2(w2));
+    int sw = 30 - (int)ceil(log2(w2));
     if (sw > 100) sw = 100;
     A.w_scale_f = (float)ldexp(1.0, sw);
     A.w_unscale = ldexp(1.0, -sw);
