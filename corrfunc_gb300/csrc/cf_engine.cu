@@ -693,11 +693,6 @@ __device__ __forceinline__ void accumulate(const PairArgs &A, WarpHist h, int bi
     if (NEED_W) add_term(e + w_word<NEED_AVG>(), __double2int_rn(dw * (double)A.w_scale_f));
 }
 
-__device__ __forceinline__ void red_shared_u32(uint32_t saddr, uint32_t v)
-{
-    asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(saddr), "r"(v));
-}
-
 template <int IMM>
 __device__ __forceinline__ void red_shared_u32_at(uint32_t saddr, uint32_t v)
 {
@@ -1939,17 +1934,17 @@ static int run_locked(cf_job *J, cf_hist *H)
     Tables T;
     if (build_tables(W, J, mode, nbins, need_w, delta, &T) != EXIT_SUCCESS) return EXIT_FAILURE;
 
-    // ---- chunks ----
-    if (ensure(W.chunk_cnt, sizeof(uint32_t) * ncols) || ensure(W.chunk_off, sizeof(uint32_t) * ((size_t)ncols + 1)))
+    // ---- chunks: fixed slot range (empty slots hold 0 points), no host wait ----
+    const uint32_t max_chunks = (uint32_t)((n1 + kChunk - 1) / kChunk + ncols);
+    if (ensure(W.chunk_cnt, sizeof(uint32_t) * ncols) || ensure(W.chunk_off, sizeof(uint32_t) * ((size_t)ncols + 1)) ||
+        ensure(W.chunk_begin, sizeof(uint32_t) * max_chunks) || ensure(W.chunk_count, sizeof(uint32_t) * max_chunks))
         return EXIT_FAILURE;
+    CF_CUDA(cudaMemsetAsync(W.chunk_count.p, 0, sizeof(uint32_t) * max_chunks, st));
     k_col_chunks<<<(ncols + 255) / 256, 256, 0, st>>>((const uint32_t *)S1.cell_start.p, (int)ncols, g.n[2],
                                                       (uint32_t *)W.chunk_cnt.p);
     g_eng.launches++;
     CF_CUDA(cudaGetLastError());
     if (scan_u32(W, (const uint32_t *)W.chunk_cnt.p, (uint32_t *)W.chunk_off.p, ncols, 0) != EXIT_SUCCESS)
-        return EXIT_FAILURE;
-    const uint32_t max_chunks = (uint32_t)((n1 + kChunk - 1) / kChunk + ncols);
-    if (ensure(W.chunk_begin, sizeof(uint32_t) * max_chunks) || ensure(W.chunk_count, sizeof(uint32_t) * max_chunks))
         return EXIT_FAILURE;
     k_chunk_emit<<<(ncols + 255) / 256, 256, 0, st>>>((const uint32_t *)S1.cell_start.p, (int)ncols, g.n[2],
                                                       (const uint32_t *)W.chunk_off.p,
@@ -1957,50 +1952,31 @@ static int run_locked(cf_job *J, cf_hist *H)
                                                       0u, nullptr, 0);
     g_eng.launches++;
     CF_CUDA(cudaGetLastError());
-    uint32_t nchunks = 0;
-    unsigned long long oob_h = 0;
-    CF_CUDA(cudaMemcpyAsync(&nchunks, (uint32_t *)W.chunk_off.p + ncols, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaMemcpyAsync(&oob_h, oob, sizeof(oob_h), cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaStreamSynchronize(st));
-    if (oob_h > 0) CF_FAIL("%llu particles are out of bounds. Check periodic wrapping?", oob_h);
-    if (nchunks > max_chunks) CF_FAIL("internal: chunk count overflow");
 
-    // ---- tasks ----
+    // ---- tasks: counted and emitted on the device into a buffer sized from earlier calls ----
     if (ensure(W.counter, sizeof(uint32_t) * 4) != EXIT_SUCCESS) return EXIT_FAILURE;
     CF_CUDA(cudaMemsetAsync(W.counter.p, 0, sizeof(uint32_t) * 4, st));
     TaskGeom G;
     if (task_geometry(J, geo, g, lo, hi, autocorr, mode, G) != EXIT_SUCCESS) return EXIT_FAILURE;
     G.error = (uint32_t *)W.counter.p + 2;
-    if (ensure(W.ntask, sizeof(uint32_t) * ((size_t)nchunks + 1)) ||
-        ensure(W.task_off, sizeof(uint32_t) * ((size_t)nchunks + 2)))
+    if (ensure(W.ntask, sizeof(uint32_t) * ((size_t)max_chunks + 1)) ||
+        ensure(W.task_off, sizeof(uint32_t) * ((size_t)max_chunks + 2)))
         return EXIT_FAILURE;
-    if (nchunks > 0) {
-        k_task_count<<<(nchunks + 127) / 128, 128, 0, st>>>(G, nchunks, (const uint32_t *)W.chunk_begin.p,
-                                                            (const uint32_t *)W.chunk_count.p,
-                                                            (const uint32_t *)S1.cellid.p,
-                                                            (const uint32_t *)S2.cell_start.p, (uint32_t *)W.ntask.p);
-        g_eng.launches++;
-        CF_CUDA(cudaGetLastError());
-    }
-    if (scan_u32(W, (const uint32_t *)W.ntask.p, (uint32_t *)W.task_off.p, nchunks, 0) != EXIT_SUCCESS)
-        return EXIT_FAILURE;
-    uint32_t ntasks = 0, task_err = 0;
-    CF_CUDA(cudaMemcpyAsync(&ntasks, (uint32_t *)W.task_off.p + nchunks, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaMemcpyAsync(&task_err, G.error, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaStreamSynchronize(st));
-    if (task_err) CF_FAIL("internal: neighbour search needed a periodic image beyond +-1");
-    if (ensure(W.tasks, sizeof(Task) * ((size_t)ntasks + 1)) != EXIT_SUCCESS) return EXIT_FAILURE;
-    if (nchunks > 0) {
-        k_task_emit<<<(nchunks + 127) / 128, 128, 0, st>>>(G, nchunks, (const uint32_t *)W.chunk_begin.p,
+    k_task_count<<<(max_chunks + 127) / 128, 128, 0, st>>>(G, max_chunks, (const uint32_t *)W.chunk_begin.p,
                                                            (const uint32_t *)W.chunk_count.p,
-                                                           (const uint32_t *)S1.cellid.p, (const uint32_t *)S2.cell_start.p,
-                                                           (const uint32_t *)W.task_off.p, (Task *)W.tasks.p,
-                                                           nullptr, ntasks, nullptr);
-        g_eng.launches++;
-        CF_CUDA(cudaGetLastError());
-    }
-    g_eng.last.tasks = ntasks;
-    CF_CUDA(cudaEventRecord(g_eng.ev[1], st));
+                                                           (const uint32_t *)S1.cellid.p,
+                                                           (const uint32_t *)S2.cell_start.p, (uint32_t *)W.ntask.p);
+    g_eng.launches++;
+    CF_CUDA(cudaGetLastError());
+    if (scan_u32(W, (const uint32_t *)W.ntask.p, (uint32_t *)W.task_off.p, max_chunks, 0) != EXIT_SUCCESS)
+        return EXIT_FAILURE;
+    // capacity: what this lattice needed last time, else about one task per neighbour column
+    const size_t guess = (size_t)max_chunks * (2 * G.reach_x + 1) * (2 * G.reach_y + 1) * 5 / 4 + 1024;
+    size_t cap = W.tasks.cap / sizeof(Task);
+    if (cap < guess) cap = guess;
+    if (ensure(W.tasks, sizeof(Task) * cap) != EXIT_SUCCESS) return EXIT_FAILURE;
+    cap = W.tasks.cap / sizeof(Task);
+    if (cap > 0xffffffffu) cap = 0xffffffffu;
 
     // ---- pair-kernel arguments ----
     PairArgs A;
@@ -2015,42 +1991,67 @@ static int run_locked(cf_job *J, cf_hist *H)
     A.d2 = (const double4_32a *)S2.dbl.p;
     A.rc2 = (const int *)S2.refcell.p;
     A.or2 = (const int *)S2.orig.p;
-    A.tasks = (const Task *)W.tasks.p;
-    A.ntasks = ntasks;
+    A.ntask_dev = (const uint32_t *)W.task_off.p + max_chunks;
     pair_constants(A, J, mode, nbins, autocorr, G, geo, g, delta, T, wmax, W);
-
     if (ensure(W.hist_cnt, sizeof(unsigned long long) * nbins) || ensure(W.hist_avg, sizeof(double) * nbins) ||
-        ensure(W.hist_w, sizeof(double) * nbins) || ensure(W.stats, sizeof(unsigned long long) * 4) ||
-        ensure(W.counter, sizeof(uint32_t) * 4))
+        ensure(W.hist_w, sizeof(double) * nbins) || ensure(W.stats, sizeof(unsigned long long) * 4))
         return EXIT_FAILURE;
-    CF_CUDA(cudaMemsetAsync(W.hist_cnt.p, 0, sizeof(unsigned long long) * nbins, st));
-    CF_CUDA(cudaMemsetAsync(W.hist_avg.p, 0, sizeof(double) * nbins, st));
-    CF_CUDA(cudaMemsetAsync(W.hist_w.p, 0, sizeof(double) * nbins, st));
-    CF_CUDA(cudaMemsetAsync(W.stats.p, 0, sizeof(unsigned long long) * 4, st));
-    CF_CUDA(cudaMemsetAsync(W.counter.p, 0, sizeof(uint32_t) * 4, st));
     A.g_cnt = (unsigned long long *)W.hist_cnt.p;
     A.g_avg = (double *)W.hist_avg.p;
     A.g_w = (double *)W.hist_w.p;
     A.g_stats = (unsigned long long *)W.stats.p;
     A.task_counter = (uint32_t *)W.counter.p;
-
-    int launched = 0;
-    CF_CUDA(cudaEventRecord(g_eng.ev[2], st));
-    if (ntasks > 0) {
-        const bool f64 = g_eng.precision == CF_PRECISION_FP64;
-        if (launch_pairs(mode, A, f64, J->need_avg != 0, need_w, &launched) != EXIT_SUCCESS) return EXIT_FAILURE;
-    }
-    CF_CUDA(cudaEventRecord(g_eng.ev[3], st));
-    if (ensure_host(W.h_hist, sizeof(uint64_t) * (3 * (size_t)nbins + 4)) != EXIT_SUCCESS) return EXIT_FAILURE;
+    if (ensure_host(W.h_hist, sizeof(uint64_t) * (3 * (size_t)nbins + 8)) != EXIT_SUCCESS) return EXIT_FAILURE;
     uint64_t *cnt_h = (uint64_t *)W.h_hist.p;
     double *avg_h = (double *)(cnt_h + nbins), *w_h = avg_h + nbins;
     unsigned long long *stats_h = (unsigned long long *)(w_h + nbins);
-    CF_CUDA(cudaMemcpyAsync(cnt_h, W.hist_cnt.p, sizeof(uint64_t) * nbins, cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaMemcpyAsync(avg_h, W.hist_avg.p, sizeof(double) * nbins, cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaMemcpyAsync(w_h, W.hist_w.p, sizeof(double) * nbins, cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaMemcpyAsync(stats_h, W.stats.p, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaEventRecord(g_eng.ev[4], st));
-    CF_CUDA(cudaStreamSynchronize(st));
+    const uint32_t *flags_h = (const uint32_t *)(stats_h + 4);  // counter[0..3]: task counter, -, image, overflow
+    const unsigned long long *oob_h = stats_h + 6;
+    const uint32_t *ntasks_h = (const uint32_t *)(stats_h + 7);
+
+    for (int attempt = 0; attempt < 2; attempt++) {
+        A.tasks = (const Task *)W.tasks.p;
+        A.ntasks = (uint32_t)cap;
+        k_task_emit<<<(max_chunks + 127) / 128, 128, 0, st>>>(G, max_chunks, (const uint32_t *)W.chunk_begin.p,
+                                                              (const uint32_t *)W.chunk_count.p,
+                                                              (const uint32_t *)S1.cellid.p,
+                                                              (const uint32_t *)S2.cell_start.p,
+                                                              (const uint32_t *)W.task_off.p, (Task *)W.tasks.p, nullptr,
+                                                              (uint32_t)cap, (uint32_t *)W.counter.p + 3);
+        g_eng.launches++;
+        CF_CUDA(cudaGetLastError());
+        CF_CUDA(cudaEventRecord(g_eng.ev[1], st));
+        CF_CUDA(cudaMemsetAsync(W.hist_cnt.p, 0, sizeof(unsigned long long) * nbins, st));
+        CF_CUDA(cudaMemsetAsync(W.hist_avg.p, 0, sizeof(double) * nbins, st));
+        CF_CUDA(cudaMemsetAsync(W.hist_w.p, 0, sizeof(double) * nbins, st));
+        CF_CUDA(cudaMemsetAsync(W.stats.p, 0, sizeof(unsigned long long) * 4, st));
+        CF_CUDA(cudaMemsetAsync(W.counter.p, 0, sizeof(uint32_t), st));  // task counter
+        int launched = 0;
+        CF_CUDA(cudaEventRecord(g_eng.ev[2], st));
+        const bool f64 = g_eng.precision == CF_PRECISION_FP64;
+        if (launch_pairs(mode, A, f64, J->need_avg != 0, need_w, &launched) != EXIT_SUCCESS) return EXIT_FAILURE;
+        CF_CUDA(cudaEventRecord(g_eng.ev[3], st));
+        CF_CUDA(cudaMemcpyAsync(cnt_h, W.hist_cnt.p, sizeof(uint64_t) * nbins, cudaMemcpyDeviceToHost, st));
+        CF_CUDA(cudaMemcpyAsync(avg_h, W.hist_avg.p, sizeof(double) * nbins, cudaMemcpyDeviceToHost, st));
+        CF_CUDA(cudaMemcpyAsync(w_h, W.hist_w.p, sizeof(double) * nbins, cudaMemcpyDeviceToHost, st));
+        CF_CUDA(cudaMemcpyAsync(stats_h, W.stats.p, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost, st));
+        CF_CUDA(cudaMemcpyAsync((void *)flags_h, W.counter.p, sizeof(uint32_t) * 4, cudaMemcpyDeviceToHost, st));
+        CF_CUDA(cudaMemcpyAsync((void *)oob_h, oob, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        CF_CUDA(cudaMemcpyAsync((void *)ntasks_h, A.ntask_dev, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        CF_CUDA(cudaEventRecord(g_eng.ev[4], st));
+        CF_CUDA(cudaStreamSynchronize(st));
+        if (*oob_h > 0) CF_FAIL("%llu particles are out of bounds. Check periodic wrapping?", *oob_h);
+        if (flags_h[2]) CF_FAIL("internal: neighbour search needed a periodic image beyond +-1");
+        if (!flags_h[3]) break;
+        // the work list outgrew the buffer: size it exactly and run the pair kernel again
+        if (attempt == 1) CF_FAIL("internal: work list overflow after resizing");
+        cap = (size_t)*ntasks_h + 1024;
+        if (ensure(W.tasks, sizeof(Task) * cap) != EXIT_SUCCESS) return EXIT_FAILURE;
+        cap = W.tasks.cap / sizeof(Task);
+        if (cap > 0xffffffffu) cap = 0xffffffffu;
+        CF_CUDA(cudaMemsetAsync(W.counter.p, 0, sizeof(uint32_t) * 4, st));
+    }
+    g_eng.last.tasks = *ntasks_h;
     memcpy(H->npairs, cnt_h, sizeof(uint64_t) * nbins);
     memcpy(H->avg, avg_h, sizeof(double) * nbins);
     memcpy(H->wsum, w_h, sizeof(double) * nbins);
@@ -2064,7 +2065,6 @@ static int run_locked(cf_job *J, cf_hist *H)
     g_eng.last.pairs_evaluated = stats_h[0];
     g_eng.last.pairs_refined = stats_h[1];
     g_eng.last.kernel_launches = g_eng.launches;
-    (void)launched;
     return EXIT_SUCCESS;
 }
 
