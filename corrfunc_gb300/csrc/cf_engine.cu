@@ -108,45 +108,141 @@ __host__ inline double ord_dec(unsigned long long u)
 template <typename T>
 __device__ __forceinline__ double ld(const T *p, int64_t i) { return (double)p[i]; }
 
-// min/max of x,y,z (slots 0..5: xmin,xmax,ymin,ymax,zmin,zmax) and max |w| (slot 6)
-template <typename T>
-__global__ void k_minmax(const T *x, const T *y, const T *z, const T *w, int64_t n,
-                         unsigned long long *mm)
+// Data extent.  Values are compared as order-preserving unsigned keys (integer min/max on the
+// ALU pipe; double min/max would run on the slow FP64 pipe): per block into partials[block][0..7]
+// (xmin, xmax, ymin, ymax, zmin, zmax keys, max |w| bits, non-finite flag), then one block folds
+// the partials into mm (slots as above, ord_enc of the double values) with a few atomics.
+__device__ __forceinline__ uint32_t okey(float v)
 {
-    double v[7] = {INFINITY, -INFINITY, INFINITY, -INFINITY, INFINITY, -INFINITY, 0.0};
-    bool bad = false;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double a = ld(x, i), b = ld(y, i), c = ld(z, i);
-        if (!isfinite(a) || !isfinite(b) || !isfinite(c)) bad = true;
-        v[0] = fmin(v[0], a); v[1] = fmax(v[1], a);
-        v[2] = fmin(v[2], b); v[3] = fmax(v[3], b);
-        v[4] = fmin(v[4], c); v[5] = fmax(v[5], c);
-        if (w) v[6] = fmax(v[6], fabs(ld(w, i)));
+    const uint32_t u = __float_as_uint(v);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ unsigned long long okey(double v)
+{
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ bool nonfinite(float v) { return (__float_as_uint(v) & 0x7f800000u) == 0x7f800000u; }
+__device__ __forceinline__ bool nonfinite(double v)
+{
+    return (((unsigned long long)__double_as_longlong(v) >> 52) & 0x7ffu) == 0x7ffu;
+}
+__device__ __forceinline__ uint32_t abskey(float v) { return __float_as_uint(v) & 0x7fffffffu; }
+__device__ __forceinline__ unsigned long long abskey(double v)
+{
+    return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+}
+__device__ __forceinline__ double key_value(uint32_t k)
+{
+    return (double)__uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+__device__ __forceinline__ double key_value(unsigned long long k)
+{
+    return __longlong_as_double((long long)((k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k));
+}
+__device__ __forceinline__ uint32_t warp_min(uint32_t v) { return __reduce_min_sync(0xffffffffu, v); }
+__device__ __forceinline__ uint32_t warp_max(uint32_t v) { return __reduce_max_sync(0xffffffffu, v); }
+__device__ __forceinline__ unsigned long long warp_min(unsigned long long v)
+{
+    for (int o = 16; o; o >>= 1) {
+        const unsigned long long t = __shfl_xor_sync(0xffffffffu, v, o);
+        v = t < v ? t : v;
     }
-    for (int off = 16; off; off >>= 1) {
-        for (int k = 0; k < 7; k++) {
-            const double o = __shfl_down_sync(0xffffffffu, v[k], off);
-            v[k] = (k & 1) || k == 6 ? fmax(v[k], o) : fmin(v[k], o);
+    return v;
+}
+__device__ __forceinline__ unsigned long long warp_max(unsigned long long v)
+{
+    for (int o = 16; o; o >>= 1) {
+        const unsigned long long t = __shfl_xor_sync(0xffffffffu, v, o);
+        v = t > v ? t : v;
+    }
+    return v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_minmax(const T *x, const T *y, const T *z, const T *w, int64_t n,
+                                                unsigned long long *partials)
+{
+    using K = decltype(okey(T(0)));
+    K mn[3] = {(K)~(K)0, (K)~(K)0, (K)~(K)0}, mx[3] = {0, 0, 0}, wm = 0;
+    uint32_t bad = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const T c[3] = {x[i], y[i], z[i]};
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            bad |= nonfinite(c[a]) ? 1u : 0u;
+            const K k = okey(c[a]);
+            mn[a] = k < mn[a] ? k : mn[a];
+            mx[a] = k > mx[a] ? k : mx[a];
+        }
+        if (w) {
+            const K k = abskey(w[i]);
+            wm = k > wm ? k : wm;
         }
     }
-    // one set of atomics per block (blockDim.x <= 256)
-    __shared__ double part[8][7];
-    __shared__ int any_bad;
+    __shared__ unsigned long long part[8][8];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-    if (threadIdx.x == 0) any_bad = 0;
-    __syncthreads();
-    if (bad) any_bad = 1;
-    if (lane == 0)
-        for (int k = 0; k < 7; k++) part[warp][k] = v[k];
-    __syncthreads();
-    if (threadIdx.x < 7) {
-        const int k = threadIdx.x;
-        double r = part[0][k];
-        for (int q = 1; q < nwarps; q++) r = (k & 1) || k == 6 ? fmax(r, part[q][k]) : fmin(r, part[q][k]);
-        const unsigned long long e = ord_enc(r);
-        if ((k & 1) || k == 6) atomicMax(&mm[k], e); else atomicMin(&mm[k], e);
+    K r[7];
+    for (int a = 0; a < 3; a++) {
+        r[2 * a] = warp_min(mn[a]);
+        r[2 * a + 1] = warp_max(mx[a]);
     }
-    if (threadIdx.x == 0 && any_bad) atomicMax(&mm[7], 1ull);
+    r[6] = warp_max(wm);
+    bad = __any_sync(0xffffffffu, bad != 0) ? 1u : 0u;
+    if (lane == 0) {
+        for (int k = 0; k < 7; k++) part[warp][k] = (unsigned long long)r[k];
+        part[warp][7] = bad;
+    }
+    __syncthreads();
+    if (threadIdx.x < 8) {
+        const int k = threadIdx.x;
+        unsigned long long v = part[0][k];
+        for (int q = 1; q < nwarps; q++) {
+            const unsigned long long o = part[q][k];
+            const bool is_min = k < 6 && (k & 1) == 0;
+            v = is_min ? (o < v ? o : v) : (o > v ? o : v);
+        }
+        partials[(size_t)blockIdx.x * 8 + k] = v;
+    }
+}
+
+// folds nblk partials (keys of type K) into mm; one block of 256 threads
+template <typename T>
+__global__ void __launch_bounds__(256) k_minmax_fold(const unsigned long long *partials, int nblk,
+                                                     unsigned long long *mm)
+{
+    using K = decltype(okey(T(0)));
+    __shared__ unsigned long long red[8][8];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = 0; k < 8; k++) {
+        const bool is_min = k < 6 && (k & 1) == 0;
+        K v = is_min ? (K)~(K)0 : (K)0;
+        for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
+            const K o = (K)partials[(size_t)b * 8 + k];
+            v = is_min ? (o < v ? o : v) : (o > v ? o : v);
+        }
+        v = is_min ? warp_min(v) : warp_max(v);
+        if (lane == 0) red[warp][k] = (unsigned long long)v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 8) {
+        const int k = threadIdx.x;
+        const bool is_min = k < 6 && (k & 1) == 0;
+        K v = (K)red[0][k];
+        for (int q = 1; q < (int)(blockDim.x >> 5); q++) {
+            const K o = (K)red[q][k];
+            v = is_min ? (o < v ? o : v) : (o > v ? o : v);
+        }
+        if (k == 7) {
+            if (v) atomicMax(&mm[7], 1ull);
+        } else if (k == 6) {
+            const double wv = key_value((K)(v | ((K)1 << (sizeof(K) * 8 - 1))));  // non-negative value
+            atomicMax(&mm[6], ord_enc(wv));
+        } else {
+            const unsigned long long e = ord_enc(key_value(v));
+            if (is_min) atomicMin(&mm[k], e); else atomicMax(&mm[k], e);
+        }
+    }
 }
 
 __device__ __forceinline__ int axis_cell(double c, const Geom &g, int a)
@@ -333,96 +429,99 @@ __device__ __forceinline__ int floordiv(int a, int b)
     return q;
 }
 
-// Enumerates the tasks of one chunk.  With emit == false it only counts them.
+// Tasks of one chunk against one neighbour column (dx, dy): one per periodic z image whose window
+// is not empty, split into ranges of at most kJMax points.  With EMIT == false only counted.
 template <bool EMIT>
-__device__ uint32_t chunk_tasks(const TaskGeom &G, uint32_t ib, uint32_t icount, const uint32_t *cellid1,
-                                const uint32_t *cs2, Task *out, uint32_t cat, uint32_t room)
+__device__ uint32_t chunk_col_tasks(const TaskGeom &G, uint32_t ib, uint32_t icount, const uint32_t *cellid1,
+                                    const uint32_t *cs2, Task *out, uint32_t cat, uint32_t room, int dx, int dy)
 {
-    if (icount == 0) return 0;  // unused chunk slot of a batched work list
+    if (icount == 0) return 0;  // unused chunk slot
+    if (G.autocorr && (dx < 0 || (dx == 0 && dy < 0))) return 0;  // half stencil
     const uint32_t c0 = cellid1[ib], c1 = cellid1[ib + icount - 1];
     const int nz = G.nz;
     const int col = (int)(c0 / nz);
     const int a = (int)(c0 % nz), b = (int)(c1 % nz);
     const int ix = col / G.ny, iy = col % G.ny;
-    uint32_t ntask = 0;
     // periodic images are encoded in two bits; the lattice construction keeps |m| <= 1
     // (neighbour reach < half the period), anything else is reported and skipped.
-
-    for (int dx = -G.reach_x; dx <= G.reach_x; dx++) {
-        const int ux = ix + dx;
-        int mx = 0, cx = ux;
-        if (G.periodic[0]) { mx = floordiv(ux, G.nx); cx = ux - mx * G.nx; }
-        else if (ux < 0 || ux >= G.nx) continue;
-        for (int dy = -G.reach_y; dy <= G.reach_y; dy++) {
-            if (G.autocorr && (dx < 0 || (dx == 0 && dy < 0))) continue;  // half stencil
-            const int uy = iy + dy;
-            int my = 0, cy = uy;
-            if (G.periodic[1]) { my = floordiv(uy, G.ny); cy = uy - my * G.ny; }
-            else if (uy < 0 || uy >= G.ny) continue;
-            const double rx = fmax(0.0, (double)(abs(dx) - 1)) * G.s[0];
-            const double ry = fmax(0.0, (double)(abs(dy) - 1)) * G.s[1];
-            const double rho2 = rx * rx + ry * ry;
-            if (rho2 >= G.rmax_xy * G.rmax_xy) continue;
-            double W = G.rmax_z;
-            if (G.rmax_3d > 0.0) W = fmin(W, sqrt(fmax(0.0, G.rmax_3d * G.rmax_3d - rho2)));
-            const int wz = (int)ceil(W / G.s[2]);
-            const bool own = G.autocorr && dx == 0 && dy == 0;
-            const int klo = own ? a : a - wz;
-            const int khi = b + wz;
-            const int col2 = cx * G.ny + cy;
-            const int mlo = G.periodic[2] ? floordiv(klo, nz) : 0;
-            const int mhi = G.periodic[2] ? floordiv(khi, nz) : 0;
-            if (mx < -1 || mx > 1 || my < -1 || my > 1 || mlo < -1 || mhi > 1) {
-                if (G.error) atomicOr(G.error, 1u);
-                continue;
+    const int ux = ix + dx;
+    int mx = 0, cx = ux;
+    if (G.periodic[0]) { mx = floordiv(ux, G.nx); cx = ux - mx * G.nx; }
+    else if (ux < 0 || ux >= G.nx) return 0;
+    const int uy = iy + dy;
+    int my = 0, cy = uy;
+    if (G.periodic[1]) { my = floordiv(uy, G.ny); cy = uy - my * G.ny; }
+    else if (uy < 0 || uy >= G.ny) return 0;
+    const double rx = fmax(0.0, (double)(abs(dx) - 1)) * G.s[0];
+    const double ry = fmax(0.0, (double)(abs(dy) - 1)) * G.s[1];
+    const double rho2 = rx * rx + ry * ry;
+    if (rho2 >= G.rmax_xy * G.rmax_xy) return 0;
+    double W = G.rmax_z;
+    if (G.rmax_3d > 0.0) W = fmin(W, sqrt(fmax(0.0, G.rmax_3d * G.rmax_3d - rho2)));
+    const int wz = (int)ceil(W / G.s[2]);
+    const bool own = G.autocorr && dx == 0 && dy == 0;
+    const int klo = own ? a : a - wz;
+    const int khi = b + wz;
+    const int col2 = cx * G.ny + cy;
+    const int mlo = G.periodic[2] ? floordiv(klo, nz) : 0;
+    const int mhi = G.periodic[2] ? floordiv(khi, nz) : 0;
+    if (mx < -1 || mx > 1 || my < -1 || my > 1 || mlo < -1 || mhi > 1) {
+        if (G.error) atomicOr(G.error, 1u);
+        return 0;
+    }
+    uint32_t ntask = 0;
+    for (int mz = mlo; mz <= mhi; mz++) {
+        int s0 = klo - mz * nz, s1 = khi - mz * nz;
+        s0 = s0 < 0 ? 0 : s0;
+        s1 = s1 > nz - 1 ? nz - 1 : s1;
+        if (s0 > s1) continue;
+        uint32_t jb = cs2[(uint32_t)col2 * nz + s0];
+        const uint32_t je = cs2[(uint32_t)col2 * nz + s1 + 1];
+        const bool own_img = own && mz == 0 && mx == 0 && my == 0;
+        if (own_img) jb = ib;  // forward half of the own column
+        if (je <= jb) continue;
+        for (uint32_t p = jb; p < je; p += kJMax) {
+            if (EMIT && ntask < room) {
+                Task t;
+                t.i_begin = ib;
+                t.j_begin = p;
+                t.j_end = min(je, p + kJMax);
+                t.meta = task_meta((int)icount, mx, my, mz, own_img && p == jb ? 1 : 0) | (cat << kCatShift);
+                out[ntask] = t;
             }
-            for (int mz = mlo; mz <= mhi; mz++) {
-                int s0 = klo - mz * nz, s1 = khi - mz * nz;
-                s0 = s0 < 0 ? 0 : s0;
-                s1 = s1 > nz - 1 ? nz - 1 : s1;
-                if (s0 > s1) continue;
-                uint32_t jb = cs2[(uint32_t)col2 * nz + s0];
-                const uint32_t je = cs2[(uint32_t)col2 * nz + s1 + 1];
-                const bool own_img = own && mz == 0 && mx == 0 && my == 0;
-                if (own_img) jb = ib;  // forward half of the own column
-                if (je <= jb) continue;
-                for (uint32_t p = jb; p < je; p += kJMax) {
-                    if (EMIT && ntask < room) {
-                        Task t;
-                        t.i_begin = ib;
-                        t.j_begin = p;
-                        t.j_end = min(je, p + kJMax);
-                        t.meta = task_meta((int)icount, mx, my, mz, own_img && p == jb ? 1 : 0) | (cat << kCatShift);
-                        out[ntask] = t;
-                    }
-                    ntask++;
-                }
-            }
+            ntask++;
         }
     }
     return ntask;
 }
 
-__global__ void k_task_count(TaskGeom G, uint32_t nchunks, const uint32_t *chunk_begin, const uint32_t *chunk_count,
+// One thread per (chunk slot, neighbour column): k = slot * ncoff + column offset index.
+__global__ void k_task_count(TaskGeom G, uint32_t nslots, const uint32_t *chunk_begin, const uint32_t *chunk_count,
                              const uint32_t *cellid1, const uint32_t *cs2, uint32_t *ntasks)
 {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nchunks) return;
-    ntasks[k] = chunk_tasks<false>(G, chunk_begin[k], chunk_count[k], cellid1, cs2, nullptr, 0, 0);
+    const uint32_t ny = 2 * G.reach_y + 1, ncoff = (2 * G.reach_x + 1) * ny;
+    const uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (k >= (uint64_t)nslots * ncoff) return;
+    const uint32_t slot = (uint32_t)(k / ncoff), c = (uint32_t)(k % ncoff);
+    ntasks[k] = chunk_col_tasks<false>(G, chunk_begin[slot], chunk_count[slot], cellid1, cs2, nullptr, 0, 0,
+                                       (int)(c / ny) - G.reach_x, (int)(c % ny) - G.reach_y);
 }
 
-// Writes the tasks of every chunk at its offset; with a capacity smaller than the total the tail
-// is dropped and *overflow set (a batched work list replayed on catalogues that grew).
-__global__ void k_task_emit(TaskGeom G, uint32_t nchunks, const uint32_t *chunk_begin, const uint32_t *chunk_count,
+// Writes the tasks of every (chunk, column) at its offset; with a capacity smaller than the total
+// the tail is dropped and *overflow set (the caller resizes and runs again).
+__global__ void k_task_emit(TaskGeom G, uint32_t nslots, const uint32_t *chunk_begin, const uint32_t *chunk_count,
                             const uint32_t *cellid1, const uint32_t *cs2, const uint32_t *task_off, Task *tasks,
                             const uint16_t *chunk_cat, uint32_t capacity, uint32_t *overflow)
 {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nchunks) return;
+    const uint32_t ny = 2 * G.reach_y + 1, ncoff = (2 * G.reach_x + 1) * ny;
+    const uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (k >= (uint64_t)nslots * ncoff) return;
+    const uint32_t slot = (uint32_t)(k / ncoff), c = (uint32_t)(k % ncoff);
     const uint32_t off = task_off[k];
     const uint32_t room = off < capacity ? capacity - off : 0u;
-    const uint32_t n = chunk_tasks<true>(G, chunk_begin[k], chunk_count[k], cellid1, cs2, tasks + off,
-                                         chunk_cat ? (uint32_t)chunk_cat[k] : 0u, room);
+    const uint32_t n = chunk_col_tasks<true>(G, chunk_begin[slot], chunk_count[slot], cellid1, cs2, tasks + off,
+                                             chunk_cat ? (uint32_t)chunk_cat[slot] : 0u, room,
+                                             (int)(c / ny) - G.reach_x, (int)(c % ny) - G.reach_y);
     if (n > room && overflow) atomicOr(overflow, 1u);
 }
 
@@ -1181,7 +1280,7 @@ struct SetBufs {
 // a batch plan owns one, so that its captured graph never sees a buffer move.
 struct Workspace {
     SetBufs set[2];
-    DevBuf mm, oob, scan_tmp[4], chunk_cnt, chunk_off, chunk_begin, chunk_count, chunk_cat, ntask, task_off, tasks;
+    DevBuf mm, mm_part, oob, scan_tmp[4], chunk_cnt, chunk_off, chunk_begin, chunk_count, chunk_cat, ntask, task_off, tasks;
     DevBuf hist_cnt, hist_avg, hist_w, stats, counter, edges, guards, lut, ascale;
     HostBuf h_small, h_tab, h_hist;
 };
@@ -1202,7 +1301,7 @@ static void release_workspace(Workspace &W)
         for (DevBuf *d : v) release(*d);
     }
     for (int k = 0; k < 4; k++) release(W.scan_tmp[k]);
-    DevBuf *v[] = {&W.mm, &W.oob, &W.chunk_cnt, &W.chunk_off, &W.chunk_begin, &W.chunk_count, &W.chunk_cat, &W.ntask,
+    DevBuf *v[] = {&W.mm, &W.mm_part, &W.oob, &W.chunk_cnt, &W.chunk_off, &W.chunk_begin, &W.chunk_count, &W.chunk_cat, &W.ntask,
                    &W.task_off, &W.tasks, &W.hist_cnt, &W.hist_avg, &W.hist_w, &W.stats, &W.counter, &W.edges,
                    &W.guards, &W.lut, &W.ascale};
     for (DevBuf *d : v) release(*d);
@@ -1319,6 +1418,22 @@ static float f_up(double v)
     return f;
 }
 
+// extent of one catalogue folded into mm[0..7] (two passes, partials in W.mm_part)
+template <typename T>
+static int minmax_into(Workspace &W, const T *x, const T *y, const T *z, const T *w, int64_t n, unsigned long long *mm)
+{
+    if (n <= 0) return EXIT_SUCCESS;
+    int grid = grid_for(n, 256);
+    if (grid > 4 * g_eng.num_sms) grid = 4 * g_eng.num_sms;
+    if (ensure(W.mm_part, sizeof(unsigned long long) * 8 * (size_t)grid) != EXIT_SUCCESS) return EXIT_FAILURE;
+    k_minmax<T><<<grid, 256, 0, g_eng.stream>>>(x, y, z, w, n, (unsigned long long *)W.mm_part.p);
+    CF_CUDA(cudaGetLastError());
+    k_minmax_fold<T><<<1, 256, 0, g_eng.stream>>>((const unsigned long long *)W.mm_part.p, grid, mm);
+    CF_CUDA(cudaGetLastError());
+    g_eng.launches += 2;
+    return EXIT_SUCCESS;
+}
+
 template <typename T>
 static int upload_and_minmax(Workspace &W, int s, int64_t n, const void *x, const void *y, const void *z, const void *w,
                              bool on_device, unsigned long long *mm_dev)
@@ -1337,13 +1452,8 @@ static int upload_and_minmax(Workspace &W, int s, int64_t n, const void *x, cons
         CF_CUDA(cudaMemcpyAsync(B.raw[k].p, src[k], bytes, cudaMemcpyHostToDevice, g_eng.stream));
         B.in[k] = B.raw[k].p;
     }
-    int mgrid = grid_for(n, 256);
-    if (mgrid > 4 * g_eng.num_sms) mgrid = 4 * g_eng.num_sms;
-    k_minmax<T><<<mgrid, 256, 0, g_eng.stream>>>((const T *)B.in[0], (const T *)B.in[1],
-                                                            (const T *)B.in[2], (const T *)B.in[3], n, mm_dev);
-    CF_CUDA(cudaGetLastError());
-    g_eng.launches++;
-    return EXIT_SUCCESS;
+    return minmax_into<T>(W, (const T *)B.in[0], (const T *)B.in[1], (const T *)B.in[2], (const T *)B.in[3], n,
+                          mm_dev);
 }
 
 // Counting sort of one catalogue into lattice records at point offset `base` of B (whose
@@ -1959,16 +2069,17 @@ static int run_locked(cf_job *J, cf_hist *H)
     TaskGeom G;
     if (task_geometry(J, geo, g, lo, hi, autocorr, mode, G) != EXIT_SUCCESS) return EXIT_FAILURE;
     G.error = (uint32_t *)W.counter.p + 2;
-    if (ensure(W.ntask, sizeof(uint32_t) * ((size_t)max_chunks + 1)) ||
-        ensure(W.task_off, sizeof(uint32_t) * ((size_t)max_chunks + 2)))
+    const uint32_t nentries = max_chunks * (uint32_t)((2 * G.reach_x + 1) * (2 * G.reach_y + 1));
+    if (ensure(W.ntask, sizeof(uint32_t) * ((size_t)nentries + 1)) ||
+        ensure(W.task_off, sizeof(uint32_t) * ((size_t)nentries + 2)))
         return EXIT_FAILURE;
-    k_task_count<<<(max_chunks + 127) / 128, 128, 0, st>>>(G, max_chunks, (const uint32_t *)W.chunk_begin.p,
+    k_task_count<<<(nentries + 127) / 128, 128, 0, st>>>(G, max_chunks, (const uint32_t *)W.chunk_begin.p,
                                                            (const uint32_t *)W.chunk_count.p,
                                                            (const uint32_t *)S1.cellid.p,
                                                            (const uint32_t *)S2.cell_start.p, (uint32_t *)W.ntask.p);
     g_eng.launches++;
     CF_CUDA(cudaGetLastError());
-    if (scan_u32(W, (const uint32_t *)W.ntask.p, (uint32_t *)W.task_off.p, max_chunks, 0) != EXIT_SUCCESS)
+    if (scan_u32(W, (const uint32_t *)W.ntask.p, (uint32_t *)W.task_off.p, nentries, 0) != EXIT_SUCCESS)
         return EXIT_FAILURE;
     // capacity: what this lattice needed last time, else about one task per neighbour column
     const size_t guess = (size_t)max_chunks * (2 * G.reach_x + 1) * (2 * G.reach_y + 1) * 5 / 4 + 1024;
@@ -1991,7 +2102,7 @@ static int run_locked(cf_job *J, cf_hist *H)
     A.d2 = (const double4_32a *)S2.dbl.p;
     A.rc2 = (const int *)S2.refcell.p;
     A.or2 = (const int *)S2.orig.p;
-    A.ntask_dev = (const uint32_t *)W.task_off.p + max_chunks;
+    A.ntask_dev = (const uint32_t *)W.task_off.p + nentries;
     pair_constants(A, J, mode, nbins, autocorr, G, geo, g, delta, T, wmax, W);
     if (ensure(W.hist_cnt, sizeof(unsigned long long) * nbins) || ensure(W.hist_avg, sizeof(double) * nbins) ||
         ensure(W.hist_w, sizeof(double) * nbins) || ensure(W.stats, sizeof(unsigned long long) * 4))
@@ -2012,7 +2123,7 @@ static int run_locked(cf_job *J, cf_hist *H)
     for (int attempt = 0; attempt < 2; attempt++) {
         A.tasks = (const Task *)W.tasks.p;
         A.ntasks = (uint32_t)cap;
-        k_task_emit<<<(max_chunks + 127) / 128, 128, 0, st>>>(G, max_chunks, (const uint32_t *)W.chunk_begin.p,
+        k_task_emit<<<(nentries + 127) / 128, 128, 0, st>>>(G, max_chunks, (const uint32_t *)W.chunk_begin.p,
                                                               (const uint32_t *)W.chunk_count.p,
                                                               (const uint32_t *)S1.cellid.p,
                                                               (const uint32_t *)S2.cell_start.p,
@@ -2086,7 +2197,7 @@ struct BatchPlan {
     bool isf = false, need_w = false;
     int64_t *n1 = nullptr, *pbase = nullptr, total1 = 0;
     const void **x1 = nullptr, **y1 = nullptr, **z1 = nullptr, **w1 = nullptr;
-    uint32_t *cbase = nullptr, total_slots = 0, ncols = 0, ncells = 0;
+    uint32_t *cbase = nullptr, total_slots = 0, nentries = 0, ncols = 0, ncells = 0;
     uint32_t task_cap = 0, ntasks = 0;
     Geom g;
     TaskGeom G;
@@ -2162,14 +2273,14 @@ static int batch_enqueue(BatchPlan &P, int phase, bool timing)
         CF_CUDA(cudaMemsetAsync(W.chunk_count.p, 0, sizeof(uint32_t) * P.total_slots, st));
         const int rc = P.isf ? batch_lattices<float>(P) : batch_lattices<double>(P);
         if (rc != EXIT_SUCCESS) return EXIT_FAILURE;
-        k_task_count<<<(P.total_slots + 127) / 128, 128, 0, st>>>(
+        k_task_count<<<(P.nentries + 127) / 128, 128, 0, st>>>(
             P.G, P.total_slots, (const uint32_t *)W.chunk_begin.p, (const uint32_t *)W.chunk_count.p,
             (const uint32_t *)W.set[0].cellid.p, (const uint32_t *)W.set[1].cell_start.p, (uint32_t *)W.ntask.p);
         g_eng.launches++;
         CF_CUDA(cudaGetLastError());
-        return scan_u32(W, (const uint32_t *)W.ntask.p, (uint32_t *)W.task_off.p, P.total_slots, 0);
+        return scan_u32(W, (const uint32_t *)W.ntask.p, (uint32_t *)W.task_off.p, P.nentries, 0);
     }
-    k_task_emit<<<(P.total_slots + 127) / 128, 128, 0, st>>>(
+    k_task_emit<<<(P.nentries + 127) / 128, 128, 0, st>>>(
         P.G, P.total_slots, (const uint32_t *)W.chunk_begin.p, (const uint32_t *)W.chunk_count.p,
         (const uint32_t *)W.set[0].cellid.p, (const uint32_t *)W.set[1].cell_start.p, (const uint32_t *)W.task_off.p,
         (Task *)W.tasks.p, (const uint16_t *)W.chunk_cat.p, P.task_cap, (uint32_t *)W.counter.p + 3);
@@ -2310,14 +2421,14 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
             if (n == 0) continue;
             const void *x = r ? P->J.x2 : P->x1[s], *y = r ? P->J.y2 : P->y1[s], *z = r ? P->J.z2 : P->z1[s];
             const void *w = P->need_w ? (r ? P->J.w2 : P->w1[s]) : nullptr;
-            int grid = grid_for(n, 256);
-            if (grid > 4 * g_eng.num_sms) grid = 4 * g_eng.num_sms;
             unsigned long long *slot = mm + (r ? 8 : 0);
-            if (P->isf) k_minmax<float><<<grid, 256, 0, st>>>((const float *)x, (const float *)y, (const float *)z,
-                                                               (const float *)w, n, slot);
-            else k_minmax<double><<<grid, 256, 0, st>>>((const double *)x, (const double *)y, (const double *)z,
-                                                         (const double *)w, n, slot);
+            rc = P->isf ? minmax_into<float>(W, (const float *)x, (const float *)y, (const float *)z, (const float *)w,
+                                             n, slot)
+                        : minmax_into<double>(W, (const double *)x, (const double *)y, (const double *)z,
+                                              (const double *)w, n, slot);
+            if (rc != EXIT_SUCCESS) break;
         }
+        if (rc != EXIT_SUCCESS) break;
         if (cudaMemcpyAsync(mmh, mm, sizeof(unsigned long long) * 16, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
             cudaStreamSynchronize(st) != cudaSuccess) {
             fprintf(stderr, "corrfunc_gb300: CUDA error '%s' while measuring the batch extent\n",
@@ -2380,8 +2491,6 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
             (rc = ensure(W.chunk_begin, sizeof(uint32_t) * ((size_t)P->total_slots + 1))) != EXIT_SUCCESS ||
             (rc = ensure(W.chunk_count, sizeof(uint32_t) * ((size_t)P->total_slots + 1))) != EXIT_SUCCESS ||
             (rc = ensure(W.chunk_cat, sizeof(uint16_t) * ((size_t)P->total_slots + 1))) != EXIT_SUCCESS ||
-            (rc = ensure(W.ntask, sizeof(uint32_t) * ((size_t)P->total_slots + 1))) != EXIT_SUCCESS ||
-            (rc = ensure(W.task_off, sizeof(uint32_t) * ((size_t)P->total_slots + 2))) != EXIT_SUCCESS ||
             (rc = ensure(W.hist_cnt, sizeof(uint64_t) * nb)) != EXIT_SUCCESS ||
             (rc = ensure(W.hist_avg, sizeof(double) * nb)) != EXIT_SUCCESS ||
             (rc = ensure(W.hist_w, sizeof(double) * nb)) != EXIT_SUCCESS ||
@@ -2389,13 +2498,17 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
             (rc = ensure_host(W.h_hist, sizeof(uint64_t) * (3 * nb + 10))) != EXIT_SUCCESS)
             break;
         if ((rc = task_geometry(&P->J, P->geo, P->g, glo, ghi, false, MODE_R3, P->G)) != EXIT_SUCCESS) break;
+        P->nentries = P->total_slots * (uint32_t)((2 * P->G.reach_x + 1) * (2 * P->G.reach_y + 1));
+        if ((rc = ensure(W.ntask, sizeof(uint32_t) * ((size_t)P->nentries + 1))) != EXIT_SUCCESS ||
+            (rc = ensure(W.task_off, sizeof(uint32_t) * ((size_t)P->nentries + 2))) != EXIT_SUCCESS)
+            break;
         P->G.error = (uint32_t *)W.counter.p + 2;
         if ((rc = build_tables(W, &P->J, MODE_R3, P->nbins, P->need_w, P->delta, &P->T)) != EXIT_SUCCESS) break;
 
         // ---- eager run: size the work list ----
         if ((rc = batch_enqueue(*P, 0, false)) != EXIT_SUCCESS) break;
         uint32_t *cnt_h = (uint32_t *)(mmh + 8);
-        if (cudaMemcpyAsync(cnt_h, (uint32_t *)W.task_off.p + P->total_slots, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+        if (cudaMemcpyAsync(cnt_h, (uint32_t *)W.task_off.p + P->nentries, sizeof(uint32_t), cudaMemcpyDeviceToHost,
                             st) != cudaSuccess ||
             cudaStreamSynchronize(st) != cudaSuccess) {
             fprintf(stderr, "corrfunc_gb300: CUDA error '%s' while building the batch work list\n",
@@ -2423,7 +2536,7 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
         A.or2 = (const int *)W.set[1].orig.p;
         A.tasks = (const Task *)W.tasks.p;
         A.ntasks = P->task_cap;
-        A.ntask_dev = (const uint32_t *)W.task_off.p + P->total_slots;
+        A.ntask_dev = (const uint32_t *)W.task_off.p + P->nentries;
         pair_constants(A, &P->J, MODE_R3, P->nbins, false, P->G, P->geo, P->g, P->delta, P->T, P->wmax, W);
         A.g_cnt = (unsigned long long *)W.hist_cnt.p;
         A.g_avg = (double *)W.hist_avg.p;
