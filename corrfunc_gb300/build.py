@@ -66,7 +66,42 @@ def build(verbose=False, extra_nvcc=()):
     _run([nvcc] + NVCC_ARCH + ["-shared", "-o", tmp] + objs
          + ["-L" + os.path.join(cuda, "lib64"), "-lcudart_static", "-lpthread", "-ldl", "-lrt", "-lm"])
     os.replace(tmp, LIB)
+    build_python_modules(verbose)
     return LIB
+
+
+def python_module_paths():
+    import sysconfig
+    suffix = sysconfig.get_config_var("EXT_SUFFIX") or ".so"
+    return [os.path.join(HERE, name + suffix) for name in ("_countpairs", "_countpairs_mocks")]
+
+
+def build_python_modules(verbose=False):
+    """CPython extension modules _countpairs / _countpairs_mocks (csrc/cf_pymodule.c), linked
+    against libcorrfunc_gb300.so in this directory.  Skipped with a note when the Python or numpy
+    headers are missing."""
+    import sysconfig
+    pyinc = sysconfig.get_paths().get("include", "")
+    try:
+        import numpy
+        npinc = numpy.get_include()
+    except Exception:
+        npinc = ""
+    if not (os.path.exists(os.path.join(pyinc, "Python.h")) and
+            os.path.exists(os.path.join(npinc, "numpy", "arrayobject.h"))):
+        print("corrfunc_gb300: Python or numpy headers not found; _countpairs modules not built")
+        return []
+    src = os.path.join(CSRC, "cf_pymodule.c")
+    obj = os.path.join(BUILD, "cf_pymodule.o")
+    _run(["gcc", "-std=gnu11", "-O2", "-fPIC", "-Wall", "-Wno-unused-function", "-Wno-missing-field-initializers",
+          "-I" + INCLUDE, "-I" + pyinc, "-I" + npinc, "-c", src, "-o", obj])
+    out = []
+    for path in python_module_paths():
+        tmp = path + ".tmp"
+        _run(["gcc", "-shared", "-o", tmp, obj, "-L" + HERE, "-lcorrfunc_gb300", "-Wl,-rpath,$ORIGIN"])
+        os.replace(tmp, path)
+        out.append(path)
+    return out
 
 
 if __name__ == "__main__":
