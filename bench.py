@@ -61,6 +61,24 @@ def _rank_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def max_over_ranks(seconds, world, device):
+    """Replicas only: every rank times its own copy of the workload; the job's time is the
+    slowest rank's (all ranks take part in the reduction)."""
+    if world <= 1:
+        return seconds
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def replica_throughput(work_per_step, steps, seconds, world):
+    """Whole-job throughput of `world` replicas, each doing `work_per_step` per step."""
+    return world * work_per_step * steps / seconds
+
+
 def make_workload(dtype=np.float64):
     from corrfunc_gb300 import catalogs as cat
     L = WORKLOAD["boxsize"]
@@ -298,12 +316,8 @@ def run_batch_workload(args):
             refined += st["pairs_refined"]
             flush_l2(torch, dev)
     torch.cuda.synchronize(dev)
-    total_s = sum(gpu_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([total_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
-    value = world * work * args.steps / total_s
+    total_s = max_over_ranks(sum(gpu_ms) / 1e3, world, dev)
+    value = replica_throughput(work, args.steps, total_s, world)
 
     # the same 64 counts as 64 sequential plain calls (device inputs), GPU time per call summed
     seq_ms = []
@@ -552,13 +566,8 @@ def main():
             refined += st["pairs_refined"]
             flush_l2(torch, dev)
     torch.cuda.synchronize(dev)
-    total_s = sum(gpu_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([total_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.barrier()
-        total_s = float(t.item())
-    value = world * work * args.steps / total_s
+    total_s = max_over_ranks(sum(gpu_ms) / 1e3, world, dev)
+    value = replica_throughput(work, args.steps, total_s, world)
 
     # end-to-end through the public C API with host (pinned) buffers
     for _ in range(2):
