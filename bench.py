@@ -612,7 +612,8 @@ def main():
             "kernel_ms": {"pair_kernel": sum(pair_ms) / args.steps, "gridlink_and_worklist": sum(grid_ms) / args.steps,
                           "step_total": sum(gpu_ms) / args.steps, "host_wall": 1e3 * sum(wall) / args.steps},
             "pairs": {"reference_lattice_candidates": work, "gpu_evaluated": evaluated // args.steps,
-                      "fp64_refined": refined // args.steps, "counted": int(np.sum(ref_np))},
+                      "fp32_slow_path": st["pairs_slow"], "fp64_refined": refined // args.steps,
+                      "counted": int(np.sum(ref_np))},
             "clocks": clocks.summary()}
 
     if args.extras and rank == 0:

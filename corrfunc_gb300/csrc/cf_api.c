@@ -1123,6 +1123,7 @@ int cf_gpu_last_stats(cf_gpu_stats *out)
     out->warps_per_block = s.warps_per_block;
     out->lane_stride = s.lane_stride;
     out->reserved = 0;
+    out->pairs_slow = s.pairs_slow;
     return EXIT_SUCCESS;
 }
 

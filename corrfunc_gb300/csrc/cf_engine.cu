@@ -53,7 +53,10 @@ constexpr int kCatShift = 17;       // Task::meta bits 17-31: catalogue of a bat
 constexpr int kPadMin = CF_PAD_MIN;  // partial j tiles above this size run padded to 32
 constexpr uint32_t kJMax = 2048;    // max j points per task
 constexpr int kRxy = 2;             // lattice columns per rmax_xy
-constexpr int kZFine = 8;           // z slabs per rmax_z
+#ifndef CF_Z_SLABS
+#define CF_Z_SLABS 32
+#endif
+constexpr int kZFine = CF_Z_SLABS;  // z slabs per rmax_z
 // the FP32 pair kernel's largest block and the resident blocks of that size per SM it is compiled
 // for: 2 x 512 threads caps it at 64 registers (32 resident warps per SM)
 #ifndef CF_PAIR_MAX_THREADS
@@ -1015,7 +1018,7 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
     const uint32_t cnt_s = (uint32_t)__cvta_generic_to_shared(h.e) + 4u * h.ew * hl;
     __syncthreads();
     uint64_t evaluated = 0;
-    unsigned long long refined = 0;
+    unsigned long long refined = 0, queued = 0;
     const uint32_t ntasks = A.ntask_dev ? min(*A.ntask_dev, A.ntasks) : A.ntasks;
     uint32_t cur_cat = 0;  // catalogue whose counts the warp's histogram holds (batched counts)
     // terms a column may have taken since the last flush: per tile 32 fast-path pairs per lane
@@ -1097,6 +1100,7 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
                     sq[sq_n + __popc(want & ((1u << lane) - 1u))] = r;
                 }
                 sq_n += __popc(want);
+                queued += __popc(want);
                 __syncwarp();
                 if (sq_n >= 32) {
                     slow_batch<MODE, NEED_AVG, NEED_W>(A, se, glo, ghi, sq + (sq_n - 32), 32, rq, rq_count, h, hl,
@@ -1122,6 +1126,7 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
     if (lane == 0) {
         atomicAdd(&A.g_stats[0], (unsigned long long)evaluated);
         atomicAdd(&A.g_stats[1], refined);
+        atomicAdd(&A.g_stats[2], queued);
     }
 }
 
@@ -2175,6 +2180,7 @@ static int run_locked(cf_job *J, cf_hist *H)
     g_eng.last.total_gpu_ms = ms_total;
     g_eng.last.pairs_evaluated = stats_h[0];
     g_eng.last.pairs_refined = stats_h[1];
+    g_eng.last.pairs_slow = stats_h[2];
     g_eng.last.kernel_launches = g_eng.launches;
     return EXIT_SUCCESS;
 }
@@ -2337,6 +2343,7 @@ static int batch_collect(BatchPlan &P, cf_hist *H)
     }
     g_eng.last.pairs_evaluated = stats_h[0];
     g_eng.last.pairs_refined = stats_h[1];
+    g_eng.last.pairs_slow = stats_h[2];
     return EXIT_SUCCESS;
 }
 

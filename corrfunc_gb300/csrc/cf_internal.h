@@ -128,6 +128,7 @@ typedef struct {
     int warps_per_block;
     int lane_stride;
     int reserved;
+    uint64_t pairs_slow;
 } cf_engine_stats;
 int cf_engine_last_stats(cf_engine_stats *out);
 int cf_engine_fp32_peak(double *tflops);
