@@ -663,6 +663,45 @@ def extras(lib, C, cf, torch, dev, args):
             out["northstar_L%d_%s" % (int(L), prec)] = {"pair_kernel_ms": min(s["pair_kernel_ms"] for s in ms),
                                                         "total_gpu_ms": min(s["total_gpu_ms"] for s in ms),
                                                         "npairs_sum": int(np.sum(r["npairs"]))}
+    out.update(other_counters(cf, cat, theory))
+    cf.set_precision(args.precision)
+    return out
+
+
+def other_counters(cf, cat, theory):
+    """The other pair counters on the survey's configurations 3 and 4 (timing only; units are the
+    GPU's own evaluated pairs and the pairs counted, since the reference-lattice work unit is
+    defined for DD): DDrppi, wp and DDsmu on 1M clustered points in L=1000, DDtheta on 1M points
+    of a sky cap."""
+    from corrfunc_gb300 import mocks
+    out = {}
+    L = 1000.0
+    x, y, z = cat.clustered_box(1_000_000, L, 3)
+    rp = cat.log_bins(0.1, 25.0, 14)
+    sb = cat.log_bins(0.1, 50.0, 20)
+    ra, dec = cat.sky_cap(1_000_000, 4)
+    tb = cat.log_bins(0.01, 10.0, 20)
+    runs = {
+        "cfg3_DDrppi": lambda: theory.DDrppi(1, 1, 40.0, rp, x, y, z, boxsize=L, isa="fallback"),
+        "cfg3_wp": lambda: theory.wp(L, 40.0, 1, rp, x, y, z, isa="fallback"),
+        "cfg3_DDsmu": lambda: theory.DDsmu(1, 1, sb, 1.0, 10, x, y, z, boxsize=L, isa="fallback"),
+        "cfg4_DDtheta": lambda: mocks.DDtheta_mocks(1, 1, tb, ra.copy(), dec.copy(), output_thetaavg=True,
+                                                    isa="fallback"),
+    }
+    for name, fn in runs.items():
+        for prec in ("fp64", "fp32_refine"):
+            cf.set_precision(prec)
+            ms = []
+            for _ in range(3 if prec == "fp32_refine" else 1):
+                r = fn()
+                ms.append(cf.last_stats())
+            best = min(ms, key=lambda s: s["pair_kernel_ms"])
+            out["%s_%s" % (name, prec)] = {"pair_kernel_ms": best["pair_kernel_ms"],
+                                          "total_gpu_ms": best["total_gpu_ms"],
+                                          "gpu_evaluated_pairs": best["pairs_evaluated"],
+                                          "fp32_slow_path": best["pairs_slow"],
+                                          "fp64_refined": best["pairs_refined"],
+                                          "npairs_sum": int(np.sum(r["npairs"]))}
     return out
 
 
