@@ -269,3 +269,45 @@ def test_gpu_zero_separation_pairs_with_rmin_zero(gpu, orc, func):
         want = orc.DDsmu(0, bins, 1.0, 4, x, y, z, **kw)
     assert np.array_equal(got["npairs"], want["npairs"])
     assert int(got["npairs"].sum()) > 0
+
+
+@pytest.mark.parametrize("refine,max_cells", [((1, 1, 1), 100), ((3, 3, 2), 100), ((2, 2, 1), 5)],
+                         ids=["refine111", "refine332", "maxcells5"])
+def test_gpu_reference_lattice_variants(gpu, orc, refine, max_cells):
+    """Custom refine factors and a small max_cells_per_dim change the reference lattice, hence
+    which point of a wrapped pair is shifted: counts and averages still follow the oracle."""
+    from corrfunc_gb300 import theory
+    rng = np.random.default_rng(77)
+    L = 60.0
+    x, y, z = (rng.random(4000) * L for _ in range(3))
+    w = rng.uniform(0.5, 1.5, 4000)
+    bins = np.logspace(np.log10(0.2), np.log10(14.0), 12)
+    kw = dict(weights1=w, weight_type="pair_product", periodic=True, boxsize=L, output_ravg=True,
+              xbin_refine_factor=refine[0], ybin_refine_factor=refine[1], zbin_refine_factor=refine[2],
+              max_cells_per_dim=max_cells)
+    got = theory.DD(1, 1, bins, x, y, z, **kw)
+    want = orc.DD(1, bins, x, y, z, weights1=w, weight_type="pair_product", periodic=True, boxsize=L,
+                  output_ravg=True, refine=refine, custom_refine=refine != (2, 2, 1), max_cells_per_dim=max_cells)
+    assert np.array_equal(got["npairs"], want["npairs"])
+    np.testing.assert_allclose(got["ravg"], want["ravg"], rtol=RTOL_AVG, atol=1e-12)
+    np.testing.assert_allclose(got["weightavg"], want["weightavg"], rtol=RTOL_AVG, atol=1e-12)
+
+
+def test_gpu_many_bins_and_fine_2d_histograms(gpu, orc):
+    """300 radial bins (shared histogram columns) and 2-D histograms with 120 pi / 90 mu bins."""
+    from corrfunc_gb300 import theory
+    rng = np.random.default_rng(78)
+    L = 80.0
+    x, y, z = (rng.random(5000) * L for _ in range(3))
+    bins = np.linspace(0.05, 12.0, 301)
+    got = theory.DD(1, 1, bins, x, y, z, periodic=True, boxsize=L, output_ravg=True)
+    want = orc.DD(1, bins, x, y, z, periodic=True, boxsize=L, output_ravg=True)
+    assert np.array_equal(got["npairs"], want["npairs"])
+    np.testing.assert_allclose(got["ravg"], want["ravg"], rtol=RTOL_AVG, atol=1e-12)
+    rp = np.logspace(np.log10(0.1), np.log10(10.0), 16)
+    got = theory.DDrppi(1, 1, 24.0, rp, x, y, z, periodic=True, boxsize=L)
+    want = orc.DDrppi(1, 24.0, rp, x, y, z, periodic=True, boxsize=L)
+    assert np.array_equal(got["npairs"], want["npairs"])
+    got = theory.DDsmu(1, 1, rp, 1.0, 90, x, y, z, periodic=True, boxsize=L)
+    want = orc.DDsmu(1, rp, 1.0, 90, x, y, z, periodic=True, boxsize=L)
+    assert np.array_equal(got["npairs"], want["npairs"])
