@@ -117,6 +117,15 @@ _PROTOS = {
                                 ctypes.c_char_p, POINTER(ResultsTheta), POINTER(ConfigOptions),
                                 POINTER(ExtraOptions)], c_int),
     "free_results_countpairs_theta": ([POINTER(ResultsTheta)], None),
+    # the mocks result structs have the layouts of the theory rp-pi / s-mu ones
+    "countpairs_mocks": ([c_int64, c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_int,
+                          c_int, ctypes.c_char_p, c_double, c_int, POINTER(ResultsRpPi), POINTER(ConfigOptions),
+                          POINTER(ExtraOptions)], c_int),
+    "free_results_mocks": ([POINTER(ResultsRpPi)], None),
+    "countpairs_mocks_s_mu": ([c_int64, c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_int,
+                               c_int, ctypes.c_char_p, c_double, c_int, c_int, POINTER(ResultsSMu),
+                               POINTER(ConfigOptions), POINTER(ExtraOptions)], c_int),
+    "free_results_mocks_s_mu": ([POINTER(ResultsSMu)], None),
 }
 
 _GPU_PROTOS = {

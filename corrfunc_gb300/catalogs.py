@@ -51,6 +51,29 @@ def sky_cap(n, seed, ra_max=90.0, dec_max=60.0, dtype=np.float64):
     return ra.astype(dtype), dec.astype(dtype)
 
 
+def survey(n, seed, ra=(150.0, 180.0), dec=(0.0, 30.0), cz=(6000.0, 12000.0), frac_clustered=0.6, dtype=np.float64):
+    """(RA, DEC, cz) of a synthetic redshift survey: a fraction of the galaxies in compact groups
+    (0.2 deg, 200 km/s scatter), the rest uniform on the sky patch (sin DEC uniform) and in cz."""
+    rng = np.random.default_rng(seed)
+    sd = np.sin(np.radians(dec))
+    nc = int(n * frac_clustered)
+    nu = n - nc
+    r = rng.uniform(ra[0], ra[1], nu)
+    d = np.degrees(np.arcsin(rng.uniform(sd[0], sd[1], nu)))
+    c = rng.uniform(cz[0], cz[1], nu)
+    if nc:
+        ng = max(1, nc // 25)
+        g = rng.integers(0, ng, nc)
+        gr = rng.uniform(ra[0], ra[1], ng)
+        gd = np.degrees(np.arcsin(rng.uniform(sd[0], sd[1], ng)))
+        gc = rng.uniform(cz[0], cz[1], ng)
+        r = np.concatenate([r, np.clip(gr[g] + rng.normal(0.0, 0.2, nc), ra[0], ra[1])])
+        d = np.concatenate([d, np.clip(gd[g] + rng.normal(0.0, 0.2, nc), dec[0], dec[1])])
+        c = np.concatenate([c, np.clip(gc[g] + rng.normal(0.0, 200.0, nc), cz[0], cz[1])])
+    perm = rng.permutation(n)
+    return r[perm].astype(dtype), d[perm].astype(dtype), c[perm].astype(dtype)
+
+
 def weights(n, seed, lo=0.5, hi=1.5, dtype=np.float64):
     rng = np.random.default_rng(seed)
     return rng.uniform(lo, hi, n).astype(dtype)

@@ -1101,6 +1101,440 @@ void free_results_countpairs_theta(results_countpairs_theta *results)
     results->weightavg = NULL;
 }
 
+/* ==================== countpairs_mocks (DDrppi_mocks), countpairs_mocks_s_mu (DDsmu_mocks) ==================== */
+#define CF_SPEED_OF_LIGHT 299800.0 /* km/s, utils/set_cosmo_dist.h:19 */
+
+/* (RA, DEC, cz) sanity fix-ups, in place as the reference does
+ * (mocks/DDrppi_mocks/countpairs_rp_pi_mocks_impl.c.src:43-112; the DDsmu_mocks copy is
+ * mocks/DDsmu_mocks/countpairs_s_mu_mocks_impl.c.src:44-113): RA in [-180, 180] is shifted by
+ * +180, DEC in [0, 180] by -90, and redshifts (max < 10 unless the third column already is a
+ * comoving distance) are multiplied by the speed of light. */
+static int check_ra_dec_cz(int64_t n, void *ra, void *dec, void *cz, size_t es, int is_comoving)
+{
+    if (n == 0) return EXIT_SUCCESS;
+    if (ra == NULL || dec == NULL || cz == NULL) {
+        CF_ERR("Input arrays can not be NULL. Have RA = %p DEC = %p cz = %p", ra, dec, cz);
+        return EXIT_FAILURE;
+    }
+    int fix_cz = 0, fix_ra = 0, fix_dec = 0;
+    double max_cz = 0.0;
+    for (int64_t i = 0; i < n; i++) {
+        const double c = wval(cz, i, es), r = wval(ra, i, es), d = wval(dec, i, es);
+        if (c > max_cz) max_cz = c;
+        if (r < 0.0) fix_ra = 1;
+        if (d > 90.0) fix_dec = 1;
+        if (d > 180) {
+            CF_ERR("theta[%lld] = %g should be less than 180 deg", (long long)i, d);
+            return EXIT_FAILURE;
+        }
+    }
+    if (max_cz < 10.0 && !is_comoving) fix_cz = 1;
+    if (fix_ra) fprintf(stderr, "check_ra_dec_cz> Out of range values found for ra. Expected ra to be in the range [0.0,360.0]. Found ra values in [-180,180] -- fixing that\n");
+    if (fix_dec) fprintf(stderr, "check_ra_dec_cz> Out of range values found for dec. Expected dec to be in the range [-90.0,90.0]. Found dec values in [0,180] -- fixing that\n");
+    if (fix_cz) fprintf(stderr, "check_ra_dec_cz> Out of range values found for cz. Expected input to be `cz' but found `z' instead. max_cz (found in input) = %g threshold = %g\n", max_cz, 10.0);
+    if (!(fix_ra || fix_dec || fix_cz)) return EXIT_SUCCESS;
+    for (int64_t i = 0; i < n; i++) {
+        if (es == sizeof(float)) {
+            if (fix_ra) ((float *)ra)[i] += 180.0f;
+            if (fix_dec) ((float *)dec)[i] -= 90.0f;
+            if (fix_cz) ((float *)cz)[i] *= (float)CF_SPEED_OF_LIGHT;
+        } else {
+            if (fix_ra) ((double *)ra)[i] += 180.0;
+            if (fix_dec) ((double *)dec)[i] -= 90.0;
+            if (fix_cz) ((double *)cz)[i] *= CF_SPEED_OF_LIGHT;
+        }
+    }
+    return EXIT_SUCCESS;
+}
+
+/* Omega_matter of the two built-in cosmologies (utils/cosmology_params.c:28-55): 1 = LasDamas,
+ * 2 = Planck; both flat (Omega_Lambda = 1 - Omega_m). */
+static int cosmology_omega_m(int cosmology, double *omega_m)
+{
+    switch (cosmology) {
+    case 1: *omega_m = 0.25; return EXIT_SUCCESS;
+    case 2: *omega_m = 0.302; return EXIT_SUCCESS;
+    }
+    fprintf(stderr, "ERROR: In init_cosmology> Cosmology=%d not implemented\n", cosmology);
+    return EXIT_FAILURE;
+}
+
+/* Comoving distance table D_c(z) in Mpc/h (utils/set_cosmo_dist.c:26-67): Simpson's rule with
+ * step dz = 1e-2 / max_size on 1/E(z), one sample every 1/max_size in z up to zmax.  The
+ * operation order is the reference's (this file is compiled without contractions).  Returns
+ * the number of samples. */
+static int comoving_table(double zmax, int max_size, double omega_m, double *zc, double *dc)
+{
+    const double omega_l = 1.0 - omega_m;
+    const double omega_k = 1.0 - omega_m - omega_l;
+    const double Dh = CF_SPEED_OF_LIGHT * 0.01 / 1.0;
+    const double Deltaz = 1.0 / max_size;
+    const double dz = 1e-2 * Deltaz;
+    const double eps = 1e-10;
+    double Eint = 0.0, E2 = 1.0, z2 = Deltaz;
+    int i = 0;
+    for (double z = 2.0 * dz; z < zmax; z += 2.0 * dz) {
+        const double E0 = E2;
+        const double a1 = 1 + z - dz, a2 = 1 + z;
+        const double E1 = 1.0 / sqrt(omega_m * (a1 * a1 * a1) + omega_k * (1 + z - dz) + omega_l);
+        E2 = 1.0 / sqrt(omega_m * (a2 * a2 * a2) + omega_k * (1 + z) + omega_l);
+        Eint += dz * (E0 + 4. * E1 + E2) / 3.;
+        if (z > (z2 - eps) && z < (z2 + eps)) {
+            if (i >= max_size) break;
+            zc[i] = z;
+            dc[i] = Eint * Dh;
+            z2 += Deltaz;
+            i++;
+        }
+    }
+    return i;
+}
+
+/* Piecewise-linear interpolation of the table at x: the segment [x_k, x_k+1] with
+ * x_k <= x < x_k+1 (the last segment for x = x_n-1), y = y_k + (x - x_k) / (x_k+1 - x_k) * (y_k+1 - y_k).
+ * This is the evaluation order of the linear interpolant the reference takes from GSL
+ * (gsl_interp_linear, used at mocks/DDrppi_mocks/countpairs_rp_pi_mocks_impl.c.src:345-356).
+ * Points outside the table are an error (GSL raises a domain error there). */
+static int interp_linear(const double *xs, const double *ys, int n, double x, double *y)
+{
+    if (n < 2 || !(x >= xs[0] && x <= xs[n - 1])) return EXIT_FAILURE;
+    int lo = 0, hi = n - 1;
+    while (hi > lo + 1) {
+        const int mid = (lo + hi) / 2;
+        if (xs[mid] > x) hi = mid; else lo = mid;
+    }
+    const double dx = xs[lo + 1] - xs[lo];
+    if (!(dx > 0.0)) return EXIT_FAILURE;
+    *y = ys[lo] + (x - xs[lo]) / dx * (ys[lo + 1] - ys[lo]);
+    return EXIT_SUCCESS;
+}
+
+/* Comoving Cartesian positions of one catalogue, on the host with libm as the reference does
+ * (mocks/DDrppi_mocks/countpairs_rp_pi_mocks_impl.c.src:318-392):
+ *   X = D cos(DEC) cos(RA), Y = D cos(DEC) sin(RA), Z = D sin(DEC)
+ * with D the third column itself (is_comoving_dist) or D_c(cz / c) from the table. */
+static int mock_positions(int64_t n, const void *ra, const void *dec, const void *cz, const void *w, size_t es,
+                          const double *zc, const double *dcs, int nz, double **X, double **Y, double **Z, double **W)
+{
+    const size_t m = (size_t)(n > 0 ? n : 1);
+    *X = malloc(sizeof(double) * m);
+    *Y = malloc(sizeof(double) * m);
+    *Z = malloc(sizeof(double) * m);
+    *W = w ? malloc(sizeof(double) * m) : NULL;
+    if (!*X || !*Y || !*Z || (w && !*W)) return EXIT_FAILURE;
+    const double inv_c = 1.0 / CF_SPEED_OF_LIGHT;
+    for (int64_t i = 0; i < n; i++) {
+        double D = wval(cz, i, es);
+        if (zc != NULL && interp_linear(zc, dcs, nz, D * inv_c, &D) != EXIT_SUCCESS) {
+            CF_ERR("cz[%lld] = %g is outside the comoving-distance table (z in [%g, %g])", (long long)i,
+                   wval(cz, i, es), zc[0], zc[nz - 1]);
+            return EXIT_FAILURE;
+        }
+        const double r = wval(ra, i, es), d = wval(dec, i, es);
+        (*X)[i] = D * cos(d * CF_PI_OVER_180) * cos(r * CF_PI_OVER_180);
+        (*Y)[i] = D * cos(d * CF_PI_OVER_180) * sin(r * CF_PI_OVER_180);
+        (*Z)[i] = D * sin(d * CF_PI_OVER_180);
+        if (w) (*W)[i] = wval(w, i, es);
+    }
+    return EXIT_SUCCESS;
+}
+
+typedef struct {
+    double *X1, *Y1, *Z1, *W1, *X2, *Y2, *Z2, *W2;
+} mock_sets;
+
+static void free_mock_sets(mock_sets *M)
+{
+    free(M->X1); free(M->Y1); free(M->Z1); free(M->W1);
+    free(M->X2); free(M->Y2); free(M->Z2); free(M->W2);
+    memset(M, 0, sizeof(*M));
+}
+
+/* Both catalogues to comoving XYZ (double).  The distance table spans z up to
+ * max(cz) / c + 0.01 over both sets (countpairs_rp_pi_mocks_impl.c.src:330-343). */
+static int mock_inputs(int64_t ND1, void *ra1, void *dec1, void *cz1, int64_t ND2, void *ra2, void *dec2, void *cz2,
+                       int autocorr, int cosmology, const struct config_options *options,
+                       const struct extra_options *extra, mock_sets *M)
+{
+    memset(M, 0, sizeof(*M));
+    const size_t es = options->float_type;
+    const int need_w = extra->weight_method != NONE;
+    double *zc = NULL, *dcs = NULL;
+    int nz = 0, rc = EXIT_SUCCESS;
+    if (!options->is_comoving_dist) {
+        double omega_m;
+        if (cosmology_omega_m(cosmology, &omega_m) != EXIT_SUCCESS) return EXIT_FAILURE;
+        double czmax = 0.0;
+        for (int64_t i = 0; i < ND1; i++) if (wval(cz1, i, es) > czmax) czmax = wval(cz1, i, es);
+        if (!autocorr)
+            for (int64_t i = 0; i < ND2; i++) if (wval(cz2, i, es) > czmax) czmax = wval(cz2, i, es);
+        const double zmax = czmax * (1.0 / CF_SPEED_OF_LIGHT) + 0.01;
+        const int max_size = 10000;
+        zc = calloc(max_size, sizeof(double));
+        dcs = calloc(max_size, sizeof(double));
+        if (!zc || !dcs) rc = EXIT_FAILURE;
+        if (rc == EXIT_SUCCESS) nz = comoving_table(zmax, max_size, omega_m, zc, dcs);
+        if (rc == EXIT_SUCCESS && nz < 2) {
+            CF_ERR("comoving-distance table has %d samples (zmax = %g)", nz, zmax);
+            rc = EXIT_FAILURE;
+        }
+    }
+    if (rc == EXIT_SUCCESS)
+        rc = mock_positions(ND1, ra1, dec1, cz1, need_w ? extra->weights0.weights[0] : NULL, es, zc, dcs, nz, &M->X1,
+                            &M->Y1, &M->Z1, &M->W1);
+    if (rc == EXIT_SUCCESS && !autocorr)
+        rc = mock_positions(ND2, ra2, dec2, cz2, need_w ? extra->weights1.weights[0] : NULL, es, zc, dcs, nz, &M->X2,
+                            &M->Y2, &M->Z2, &M->W2);
+    free(zc);
+    free(dcs);
+    if (rc != EXIT_SUCCESS) free_mock_sets(M);
+    return rc;
+}
+
+static void mock_job(cf_job *J, const struct config_options *options, int mode, int autocorr, int64_t ND1,
+                     int64_t ND2, const mock_sets *M, int need_w, double max_sep)
+{
+    init_job(J, options, mode, autocorr);
+    J->elem_size = 8;
+    J->n1 = ND1;
+    J->n2 = autocorr ? ND1 : ND2;
+    J->x1 = M->X1; J->y1 = M->Y1; J->z1 = M->Z1; J->w1 = M->W1;
+    J->x2 = autocorr ? M->X1 : M->X2;
+    J->y2 = autocorr ? M->Y1 : M->Y2;
+    J->z2 = autocorr ? M->Z1 : M->Z2;
+    J->w2 = autocorr ? M->W1 : M->W2;
+    J->need_weight = need_w;
+    J->rule.kind = CF_REF_NONE;
+    J->rmax_xy = J->rmax_z = J->rmax_3d = max_sep;
+}
+
+/* mocks/DDrppi_mocks/countpairs_rp_pi_mocks.c + countpairs_rp_pi_mocks_impl.c.src:200-847 */
+int countpairs_mocks(const int64_t ND1, void *ra1, void *dec1, void *czD1, const int64_t ND2, void *ra2, void *dec2,
+                     void *czD2, const int numthreads, const int autocorr, const char *binfile, const double pimax,
+                     const int cosmology, results_countpairs_mocks *results, struct config_options *options,
+                     struct extra_options *extra)
+{
+    (void)numthreads;
+    const double t0 = wall_now();
+    if (check_options(options, __func__) != EXIT_SUCCESS || results == NULL) return EXIT_FAILURE;
+    struct extra_options dummy;
+    if (extra == NULL) {
+        dummy = get_extra_options(NONE);
+        extra = &dummy;
+    }
+    options->sort_on_z = 1;
+    memset(results, 0, sizeof(*results));
+    if (ND1 == 0 || (autocorr == 0 && ND2 == 0)) return EXIT_SUCCESS;
+    if (autocorr != 0 && autocorr != 1) {
+        CF_ERR("Strange value of autocorr = %d", autocorr);
+        return EXIT_FAILURE;
+    }
+    if (check_weights(extra, autocorr) != EXIT_SUCCESS) return EXIT_FAILURE;
+    const int need_w = extra->weight_method != NONE;
+    const size_t es = options->float_type;
+    if (check_ra_dec_cz(ND1, ra1, dec1, czD1, es, options->is_comoving_dist) != EXIT_SUCCESS) return EXIT_FAILURE;
+    if (!autocorr && check_ra_dec_cz(ND2, ra2, dec2, czD2, es, options->is_comoving_dist) != EXIT_SUCCESS)
+        return EXIT_FAILURE;
+    sanitize_lattice_options(options);
+    const int npibin = (int)pimax;
+    if (npibin < 1) {
+        CF_ERR("pimax = %g gives %d pi bins; pimax must be at least 1", pimax, npibin);
+        return EXIT_FAILURE;
+    }
+    double omega_m;
+    if (cosmology_omega_m(cosmology, &omega_m) != EXIT_SUCCESS) return EXIT_FAILURE;
+    double *rupp = NULL, rpmin, rpmax;
+    int nrpbin;
+    if (cf_setup_bins(binfile, &rpmin, &rpmax, &nrpbin, &rupp) != EXIT_SUCCESS) return EXIT_FAILURE;
+    if (!(rpmin > 0.0 && rpmax > 0.0 && rpmin < rpmax && nrpbin > 0) || nrpbin > CF_MAX_EDGES) {
+        CF_ERR("Could not setup with R bins correctly. (rmin = %lf, rmax = %lf, with nbins = %d). Expected non-zero "
+               "rmin/rmax with rmax > rmin and nbins >=1 ", rpmin, rpmax, nrpbin);
+        free(rupp);
+        return EXIT_FAILURE;
+    }
+    mock_sets M;
+    if (mock_inputs(ND1, ra1, dec1, czD1, ND2, ra2, dec2, czD2, autocorr, cosmology, options, extra, &M) !=
+        EXIT_SUCCESS) {
+        free(rupp);
+        return EXIT_FAILURE;
+    }
+    const int64_t totnbins = (int64_t)(npibin + 1) * (nrpbin + 1);
+    cf_job J;
+    mock_job(&J, options, CF_MODE_RPPI_MOCK, autocorr, ND1, ND2, &M, need_w, sqrt(rpmax * rpmax + pimax * pimax));
+    J.pimax = pimax;
+    J.npibin = npibin;
+    J.nedges = nrpbin;
+    for (int i = 0; i < nrpbin; i++) J.edges[i] = rupp[i] * rupp[i];
+    cf_hist H;
+    int rc = alloc_hist(&H, nrpbin * (npibin + 1));
+    if (rc == EXIT_SUCCESS) rc = cf_engine_run(&J, &H);
+    free_mock_sets(&M);
+    if (rc != EXIT_SUCCESS) {
+        free_hist(&H);
+        free(rupp);
+        return EXIT_FAILURE;
+    }
+    /* rpmin > 0: no self pairs (countpairs_rp_pi_mocks_impl.c.src:730-765) */
+    finalize_hist(&H, autocorr, 0, npibin + 1, ND1, 0.0, options->need_avg_sep, need_w, 0);
+    results->nbin = nrpbin;
+    results->npibin = npibin;
+    results->pimax = pimax;
+    results->npairs = calloc((size_t)totnbins, sizeof(uint64_t));
+    results->rupp = malloc(sizeof(double) * nrpbin);
+    results->rpavg = calloc((size_t)totnbins, sizeof(double));
+    results->weightavg = calloc((size_t)totnbins, sizeof(double));
+    if (!results->npairs || !results->rupp || !results->rpavg || !results->weightavg) {
+        free_results_mocks(results);
+        free_hist(&H);
+        free(rupp);
+        return EXIT_FAILURE;
+    }
+    for (int i = 0; i < nrpbin; i++) {
+        results->rupp[i] = rupp[i];
+        for (int j = 0; j < npibin; j++) {
+            const int64_t idx = (int64_t)i * (npibin + 1) + j;
+            results->npairs[idx] = H.npairs[idx];
+            results->rpavg[idx] = options->need_avg_sep ? H.avg[idx] : 0.0;
+            results->weightavg[idx] = need_w ? H.wsum[idx] : 0.0;
+        }
+    }
+    free_hist(&H);
+    free(rupp);
+    reset_bin_refine_factors(options);
+    if (options->c_api_timer) options->c_api_time = wall_now() - t0;
+    return EXIT_SUCCESS;
+}
+
+void free_results_mocks(results_countpairs_mocks *results)
+{
+    if (results == NULL) return;
+    free(results->npairs);
+    free(results->rupp);
+    free(results->rpavg);
+    free(results->weightavg);
+    results->npairs = NULL;
+    results->rupp = NULL;
+    results->rpavg = NULL;
+    results->weightavg = NULL;
+}
+
+/* mocks/DDsmu_mocks/countpairs_s_mu_mocks.c + countpairs_s_mu_mocks_impl.c.src:203-846 */
+int countpairs_mocks_s_mu(const int64_t ND1, void *ra1, void *dec1, void *czD1, const int64_t ND2, void *ra2,
+                          void *dec2, void *czD2, const int numthreads, const int autocorr, const char *sbinfile,
+                          const double mu_max, const int nmu_bins, const int cosmology,
+                          results_countpairs_mocks_s_mu *results, struct config_options *options,
+                          struct extra_options *extra)
+{
+    (void)numthreads;
+    const double t0 = wall_now();
+    if (check_options(options, __func__) != EXIT_SUCCESS || results == NULL) return EXIT_FAILURE;
+    struct extra_options dummy;
+    if (extra == NULL) {
+        dummy = get_extra_options(NONE);
+        extra = &dummy;
+    }
+    options->sort_on_z = 1;
+    memset(results, 0, sizeof(*results));
+    if (ND1 == 0 || (autocorr == 0 && ND2 == 0)) return EXIT_SUCCESS;
+    if (autocorr != 0 && autocorr != 1) {
+        CF_ERR("Strange value of autocorr = %d", autocorr);
+        return EXIT_FAILURE;
+    }
+    if (check_weights(extra, autocorr) != EXIT_SUCCESS) return EXIT_FAILURE;
+    const int need_w = extra->weight_method != NONE;
+    const size_t es = options->float_type;
+    if (check_ra_dec_cz(ND1, ra1, dec1, czD1, es, options->is_comoving_dist) != EXIT_SUCCESS) return EXIT_FAILURE;
+    if (!autocorr && check_ra_dec_cz(ND2, ra2, dec2, czD2, es, options->is_comoving_dist) != EXIT_SUCCESS)
+        return EXIT_FAILURE;
+    sanitize_lattice_options(options);
+    double omega_m;
+    if (cosmology_omega_m(cosmology, &omega_m) != EXIT_SUCCESS) return EXIT_FAILURE;
+    double *supp = NULL, smin, smax;
+    int nsbin;
+    if (cf_setup_bins(sbinfile, &smin, &smax, &nsbin, &supp) != EXIT_SUCCESS) return EXIT_FAILURE;
+    if (!(smin > 0.0 && smax > 0.0 && smin < smax && nsbin > 0) || nsbin > CF_MAX_EDGES) {
+        CF_ERR("Could not setup with S bins correctly. (smin = %lf, smax = %lf, with nbins = %d). Expected non-zero "
+               "smin/smax with smax > smin and nbins >=1 ", smin, smax, nsbin);
+        free(supp);
+        return EXIT_FAILURE;
+    }
+    if (mu_max <= 0.0 || mu_max > 1.0) {
+        CF_ERR("max_mu (max. value for the cosine of the angle with line of sight) must be greater than 0 and at most "
+               "1).\nThe passed value is max_mu = %lf. Please change it to be > 0 and <= 1.0", mu_max);
+        free(supp);
+        return EXIT_FAILURE;
+    }
+    if (nmu_bins < 1) {
+        CF_ERR("Number of mu bins = %d must be at least 1", nmu_bins);
+        free(supp);
+        return EXIT_FAILURE;
+    }
+    mock_sets M;
+    if (mock_inputs(ND1, ra1, dec1, czD1, ND2, ra2, dec2, czD2, autocorr, cosmology, options, extra, &M) !=
+        EXIT_SUCCESS) {
+        free(supp);
+        return EXIT_FAILURE;
+    }
+    const int64_t totnbins = (int64_t)(nmu_bins + 1) * (nsbin + 1);
+    cf_job J;
+    mock_job(&J, options, CF_MODE_SMU_MOCK, autocorr, ND1, ND2, &M, need_w, smax);
+    J.mu_max = mu_max;
+    J.npibin = nmu_bins;
+    J.nedges = nsbin;
+    for (int i = 0; i < nsbin; i++) J.edges[i] = supp[i] * supp[i];
+    cf_hist H;
+    int rc = alloc_hist(&H, nsbin * (nmu_bins + 1));
+    if (rc == EXIT_SUCCESS) rc = cf_engine_run(&J, &H);
+    free_mock_sets(&M);
+    if (rc != EXIT_SUCCESS) {
+        free_hist(&H);
+        free(supp);
+        return EXIT_FAILURE;
+    }
+    finalize_hist(&H, autocorr, 0, nmu_bins + 1, ND1, 0.0, options->need_avg_sep, need_w, 0);
+    results->nsbin = nsbin;
+    results->nmu_bins = nmu_bins;
+    results->mu_max = mu_max;
+    results->mu_min = 0.0;
+    results->npairs = calloc((size_t)totnbins, sizeof(uint64_t));
+    results->supp = malloc(sizeof(double) * nsbin);
+    results->savg = calloc((size_t)totnbins, sizeof(double));
+    results->weightavg = calloc((size_t)totnbins, sizeof(double));
+    if (!results->npairs || !results->supp || !results->savg || !results->weightavg) {
+        free_results_mocks_s_mu(results);
+        free_hist(&H);
+        free(supp);
+        return EXIT_FAILURE;
+    }
+    for (int i = 0; i < nsbin; i++) {
+        results->supp[i] = supp[i];
+        for (int j = 0; j < nmu_bins; j++) {
+            const int64_t idx = (int64_t)i * (nmu_bins + 1) + j;
+            results->npairs[idx] = H.npairs[idx];
+            results->savg[idx] = options->need_avg_sep ? H.avg[idx] : 0.0;
+            results->weightavg[idx] = need_w ? H.wsum[idx] : 0.0;
+        }
+    }
+    free_hist(&H);
+    free(supp);
+    reset_bin_refine_factors(options);
+    if (options->c_api_timer) options->c_api_time = wall_now() - t0;
+    return EXIT_SUCCESS;
+}
+
+void free_results_mocks_s_mu(results_countpairs_mocks_s_mu *results)
+{
+    if (results == NULL) return;
+    free(results->npairs);
+    free(results->supp);
+    free(results->savg);
+    free(results->weightavg);
+    results->npairs = NULL;
+    results->supp = NULL;
+    results->savg = NULL;
+    results->weightavg = NULL;
+}
+
 /* ========================= GB300 extensions ========================= */
 int cf_gpu_set_precision(int mode) { return cf_engine_set_precision(mode); }
 

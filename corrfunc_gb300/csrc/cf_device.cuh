@@ -34,7 +34,17 @@ struct Lattice {
     uint32_t *cell_start; // ncells + 1 offsets
 };
 
-enum { MODE_R3 = 0, MODE_RPPI = 1, MODE_WP = 2, MODE_SMU = 3, MODE_THETA = 4 };
+// MODE_RPPI_MOCK / MODE_SMU_MOCK: rp-pi and s-mu about the pair's line of sight (comoving
+// positions of a survey, observer at the origin, no periodic images).
+enum { MODE_R3 = 0, MODE_RPPI = 1, MODE_WP = 2, MODE_SMU = 3, MODE_THETA = 4, MODE_RPPI_MOCK = 5, MODE_SMU_MOCK = 6 };
+constexpr int kNumModes = 7;
+
+__host__ __device__ constexpr bool mode_is_mock(int m) { return m == MODE_RPPI_MOCK || m == MODE_SMU_MOCK; }
+// flat 2-D histograms (separation bin * (npibin + 1) + pi or mu bin)
+__host__ __device__ constexpr bool mode_two_d(int m)
+{
+    return m == MODE_RPPI || m == MODE_SMU || m == MODE_RPPI_MOCK || m == MODE_SMU_MOCK;
+}
 
 struct PairArgs {
     // lattices (set 1 = i points, set 2 = j points; identical for auto-correlations)
@@ -156,6 +166,62 @@ __device__ __forceinline__ int ref_eval(const PairArgs &A, const double *se,
         const int k = bin_theta(se, nb, c);  // >= 1 since c <= se[0]
         *avg_term = 57.29577951308232087679815481410517033240547246656432154916024 * acos(c);
         return k;
+    }
+    if (MODE == MODE_RPPI_MOCK || MODE == MODE_SMU_MOCK) {
+        // s = x_second - x_first and the (unhalved) line of sight l = x_first + x_second.  Three
+        // formula families: fallback, left-to-right sums
+        // (mocks/DDrppi_mocks/countpairs_rp_pi_mocks_kernels.c.src:1232-1257,
+        // mocks/DDsmu_mocks/countpairs_s_mu_mocks_kernels.c.src:1173-1190); AVX / SSE, sums nested
+        // to the right (rp_pi :528-563, s_mu :505-546); AVX512F, fused chains (rp_pi :210-262,
+        // s_mu :202-245).  The SIMD kernels drop pi >= pimax (mu >= mu_max) and truncate the flat
+        // index from the double sum bin * (n + 1) + pi / dpi (rp_pi :312-319, s_mu :289-296); the
+        // fallback files those pairs in column n and truncates pi / dpi alone.
+        // Swapping the two points negates s and keeps l, so every quantity is symmetric.
+        const double px = __dadd_rn(xa, xb), py = __dadd_rn(ya, yb), pz = __dadd_rn(za, zb);
+        const double sx = __dsub_rn(xb, xa), sy = __dsub_rn(yb, ya), sz = __dsub_rn(zb, za);
+        double s2, sl, l2;
+        if (A.fma_formula) {
+            s2 = __fma_rn(sx, sx, __fma_rn(sy, sy, __dmul_rn(sz, sz)));
+            sl = __fma_rn(pz, sz, __dadd_rn(__dmul_rn(px, sx), __dmul_rn(py, sy)));
+            l2 = __fma_rn(px, px, __fma_rn(py, py, __dmul_rn(pz, pz)));
+        } else if (A.chord_formula) {
+            s2 = __dadd_rn(__dmul_rn(sx, sx), __dadd_rn(__dmul_rn(sy, sy), __dmul_rn(sz, sz)));
+            sl = __dadd_rn(__dmul_rn(pz, sz), __dadd_rn(__dmul_rn(py, sy), __dmul_rn(px, sx)));
+            l2 = __dadd_rn(__dmul_rn(px, px), __dadd_rn(__dmul_rn(py, py), __dmul_rn(pz, pz)));
+        } else {
+            s2 = __dadd_rn(__dadd_rn(__dmul_rn(sx, sx), __dmul_rn(sy, sy)), __dmul_rn(sz, sz));
+            sl = __dadd_rn(__dadd_rn(__dmul_rn(px, sx), __dmul_rn(py, sy)), __dmul_rn(pz, sz));
+            l2 = __dadd_rn(__dadd_rn(__dmul_rn(px, px), __dmul_rn(py, py)), __dmul_rn(pz, pz));
+        }
+        const bool simd = A.fma_formula || A.chord_formula;
+        const double sl2 = __dmul_rn(sl, sl);
+        const int nrow = A.npibin + 1;
+        double ratio, limit;  // pi^2 or mu^2 and its upper limit
+        int kbin;
+        if (MODE == MODE_RPPI_MOCK) {
+            const double sqr_pimax = __dmul_rn(A.pimax, A.pimax);
+            if (!(s2 < __dadd_rn(se[nb - 1], sqr_pimax))) return -1;
+            if (!(sl2 < __dmul_rn(l2, sqr_pimax))) return -1;
+            ratio = __ddiv_rn(sl2, l2);
+            limit = sqr_pimax;
+            const double dperp2 = __dsub_rn(s2, ratio);
+            if (dperp2 >= se[nb - 1] || dperp2 < se[0]) return -1;
+            kbin = bin_upper(se, nb, dperp2);
+            *avg_term = __dsqrt_rn(dperp2);
+        } else {
+            if (s2 >= se[nb - 1] || s2 < se[0]) return -1;
+            ratio = __ddiv_rn(sl2, __dmul_rn(l2, s2));
+            if (ratio != ratio) return -1;  // l = 0: points mirrored through the observer
+            limit = A.sqr_mu_max;
+            kbin = bin_upper(se, nb, s2);
+            *avg_term = __dsqrt_rn(s2);
+        }
+        const double t = __dmul_rn(__dsqrt_rn(ratio), MODE == MODE_RPPI_MOCK ? A.inv_dpi : A.inv_dmu);
+        if (simd) {
+            if (!(ratio < limit)) return -1;
+            return min(__double2int_rz(__dadd_rn((double)(kbin * nrow), t)), kbin * nrow + A.npibin);
+        }
+        return kbin * nrow + (ratio >= limit ? A.npibin : min(__double2int_rz(t), A.npibin));
     }
     const double xpos = __dadd_rn(xa, ox), ypos = __dadd_rn(ya, oy), zpos = __dadd_rn(za, oz);
     const double dx = __dsub_rn(xb, xpos), dy = __dsub_rn(yb, ypos), dz = __dsub_rn(zb, zpos);

@@ -72,6 +72,11 @@ constexpr int kZFine = CF_Z_SLABS;  // z slabs per rmax_z
 
 constexpr int kScanTile = 4096;
 
+// modes with an FP32 classification kernel (the others always run the FP64 kernel)
+constexpr bool has_f32_path(int mode) { return !mode_is_mock(mode); }
+template <int MODE>
+constexpr bool kHasF32 = has_f32_path(MODE);
+
 // ------------------------------------------------------------------------------------
 // geometry of the GPU lattice and of the reference lattice
 // ------------------------------------------------------------------------------------
@@ -1325,7 +1330,7 @@ struct Engine {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[6];
     Workspace ws;
-    int regs_cache[5][4][2] = {};  // registers per thread of each pair kernel (0 = not queried)
+    int regs_cache[kNumModes][4][2] = {};  // registers per thread of each pair kernel (0 = not queried)
     int force_ls = 0, force_warps = 0;  // FP32 pair-kernel layout chosen by the batch tuner (0 = scored)
     int precision = CF_PRECISION_FP32_REFINE;
     int launches = 0;  // kernels launched by the current call
@@ -1523,8 +1528,12 @@ template <int MODE, bool AVG, bool W>
 static int pair_kernel_regs_t(bool f64)
 {
     cudaFuncAttributes fa;
-    const cudaError_t rc = f64 ? cudaFuncGetAttributes(&fa, k_pairs_f64<MODE, AVG, W>)
-                               : cudaFuncGetAttributes(&fa, k_pairs_f32<MODE, AVG, W>);
+    cudaError_t rc;
+    if constexpr (kHasF32<MODE>) {
+        rc = f64 ? cudaFuncGetAttributes(&fa, k_pairs_f64<MODE, AVG, W>) : cudaFuncGetAttributes(&fa, k_pairs_f32<MODE, AVG, W>);
+    } else {
+        rc = cudaFuncGetAttributes(&fa, k_pairs_f64<MODE, AVG, W>);
+    }
     return rc == cudaSuccess && fa.numRegs > 0 ? fa.numRegs : 64;
 }
 
@@ -1539,13 +1548,15 @@ static int pair_kernel_regs_m(bool f64, bool avg, bool w)
 
 static int pair_kernel_regs(int mode, bool f64, bool avg, bool w)
 {
-    int &c = g_eng.regs_cache[mode < 0 || mode > 4 ? 4 : mode][(avg ? 2 : 0) + (w ? 1 : 0)][f64 ? 1 : 0];
+    int &c = g_eng.regs_cache[mode < 0 || mode >= kNumModes ? MODE_THETA : mode][(avg ? 2 : 0) + (w ? 1 : 0)][f64 ? 1 : 0];
     if (c > 0) return c;
     switch (mode) {
     case MODE_R3: c = pair_kernel_regs_m<MODE_R3>(f64, avg, w); break;
     case MODE_RPPI: c = pair_kernel_regs_m<MODE_RPPI>(f64, avg, w); break;
     case MODE_WP: c = pair_kernel_regs_m<MODE_WP>(f64, avg, w); break;
     case MODE_SMU: c = pair_kernel_regs_m<MODE_SMU>(f64, avg, w); break;
+    case MODE_RPPI_MOCK: c = pair_kernel_regs_m<MODE_RPPI_MOCK>(f64, avg, w); break;
+    case MODE_SMU_MOCK: c = pair_kernel_regs_m<MODE_SMU_MOCK>(f64, avg, w); break;
     default: c = pair_kernel_regs_m<MODE_THETA>(f64, avg, w); break;
     }
     return c;
@@ -1556,7 +1567,7 @@ static int pair_kernel_regs(int mode, bool f64, bool avg, bool w)
 // shared columns (1 = private, 2 = 2-way, ... 32 = the whole warp on one row).
 static SmemLayout choose_layout(int mode, bool f64, bool avg, bool w, int nedges, int nbins, int lut_n)
 {
-    const bool dz = (mode == MODE_RPPI || mode == MODE_WP || mode == MODE_SMU);
+    const bool dz = (mode == MODE_RPPI || mode == MODE_WP || mode == MODE_SMU || mode_is_mock(mode));
     if (!f64 && g_eng.force_ls > 0 && g_eng.force_warps > 0) {
         const SmemLayout c = smem_layout(nedges, nbins, g_eng.force_warps, f64, lut_n, g_eng.force_ls, avg, w, dz);
         if (c.total <= 220 * 1024) return c;
@@ -1606,12 +1617,14 @@ static int launch_pairs_t(const PairArgs &A, bool f64, int *launched)
         CF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, SL.total));
         if (per_sm < 1) per_sm = 1;
         kern<<<g_eng.num_sms * per_sm, threads, SL.total, g_eng.stream>>>(A, SL);
-    } else {
+    } else if constexpr (kHasF32<MODE>) {
         auto kern = k_pairs_f32<MODE, AVG, W>;
         CF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SL.total));
         CF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, SL.total));
         if (per_sm < 1) per_sm = 1;
         kern<<<g_eng.num_sms * per_sm, threads, SL.total, g_eng.stream>>>(A, SL);
+    } else {
+        CF_FAIL("internal: no FP32 pair kernel for mode %d", MODE);
     }
     CF_CUDA(cudaGetLastError());
     g_eng.launches++;
@@ -1642,6 +1655,8 @@ static int launch_pairs(int mode, const PairArgs &A, bool f64, bool avg, bool w,
     case MODE_WP: return launch_pairs_m<MODE_WP>(A, f64, avg, w, launched);
     case MODE_SMU: return launch_pairs_m<MODE_SMU>(A, f64, avg, w, launched);
     case MODE_THETA: return launch_pairs_m<MODE_THETA>(A, f64, avg, w, launched);
+    case MODE_RPPI_MOCK: return launch_pairs_m<MODE_RPPI_MOCK>(A, f64, avg, w, launched);
+    case MODE_SMU_MOCK: return launch_pairs_m<MODE_SMU_MOCK>(A, f64, avg, w, launched);
     }
     CF_FAIL("unknown mode %d", mode);
 }
@@ -1725,7 +1740,7 @@ static int build_tables(Workspace &W, const cf_job *J, int mode, int nbins, bool
     if (ensure(W.lut, sizeof(uint32_t) * (n + 1)) != EXIT_SUCCESS) return EXIT_FAILURE;
     // row byte offsets: the layout (private columns or shared row) is fixed before the launch
     const int ls = choose_layout(mode, false, J->need_avg != 0, need_w, J->nedges, nbins, n).lane_stride;
-    const uint32_t ostride = (mode == MODE_RPPI || mode == MODE_SMU) ? (uint32_t)(J->npibin + 1) : 1u;
+    const uint32_t ostride = mode_two_d(mode) ? (uint32_t)(J->npibin + 1) : 1u;
     const int ew = 1 + (J->need_avg ? 2 : 0) + (need_w ? 2 : 0);  // words per histogram entry
     const uint32_t row_bytes = (uint32_t)(4 * ew * ls);
     const uint32_t trash = (uint32_t)nbins * row_bytes;
@@ -1915,7 +1930,7 @@ static void pair_constants(PairArgs &A, const cf_job *J, int mode, int nbins, bo
     const double dxy = T.dxy, d3 = T.d3;
     A.g_lut = (const uint32_t *)W.lut.p;
     A.g_ascale = (const float *)W.ascale.p;
-    A.rbin_div = (mode == MODE_RPPI || mode == MODE_SMU) ? J->npibin + 1 : 1;
+    A.rbin_div = mode_two_d(mode) ? J->npibin + 1 : 1;
     A.trash_off = T.trash;
     A.row_bytes = T.row_bytes;
     A.lane_stride_hint = T.ls;
@@ -1929,6 +1944,14 @@ static void pair_constants(PairArgs &A, const cf_job *J, int mode, int nbins, bo
     A.g_guard = (const float *)W.guards.p;
     A.dz_err = (float)(2.0 * delta[2]);
     A.dxy_err = (float)(2.0 * dxy);
+    if (mode == MODE_RPPI_MOCK) {
+        A.pimax = J->pimax;
+        A.inv_dpi = 1.0 / (J->pimax / J->npibin);
+    }
+    if (mode == MODE_SMU_MOCK) {
+        A.sqr_mu_max = J->mu_max * J->mu_max;
+        A.inv_dmu = 1.0 / (J->mu_max / J->npibin);
+    }
     if (mode == MODE_RPPI || mode == MODE_WP) {
         A.pimax = J->pimax;
         const double dpi = J->pimax / J->npibin;
@@ -1970,8 +1993,7 @@ static int run_locked(cf_job *J, cf_hist *H)
     memset(&g_eng.last, 0, sizeof(g_eng.last));
     g_eng.launches = 0;
     const int mode = J->mode;
-    const bool two_d = (mode == MODE_RPPI || mode == MODE_SMU);
-    const int nbins = two_d ? J->nedges * (J->npibin + 1) : J->nedges;
+    const int nbins = mode_two_d(mode) ? J->nedges * (J->npibin + 1) : J->nedges;
     if (H->nbins != nbins) CF_FAIL("internal: histogram size mismatch (%d vs %d)", H->nbins, nbins);
     memset(H->npairs, 0, sizeof(uint64_t) * nbins);
     memset(H->avg, 0, sizeof(double) * nbins);
@@ -2144,7 +2166,7 @@ static int run_locked(cf_job *J, cf_hist *H)
         CF_CUDA(cudaMemsetAsync(W.counter.p, 0, sizeof(uint32_t), st));  // task counter
         int launched = 0;
         CF_CUDA(cudaEventRecord(g_eng.ev[2], st));
-        const bool f64 = g_eng.precision == CF_PRECISION_FP64;
+        const bool f64 = g_eng.precision == CF_PRECISION_FP64 || !has_f32_path(mode);
         if (launch_pairs(mode, A, f64, J->need_avg != 0, need_w, &launched) != EXIT_SUCCESS) return EXIT_FAILURE;
         CF_CUDA(cudaEventRecord(g_eng.ev[3], st));
         CF_CUDA(cudaMemcpyAsync(cnt_h, W.hist_cnt.p, sizeof(uint64_t) * nbins, cudaMemcpyDeviceToHost, st));

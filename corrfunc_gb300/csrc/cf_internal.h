@@ -16,7 +16,9 @@ enum {
     CF_MODE_RPPI = 1,  /* rp^2 bins x linear |pi| bins: countpairs_rp_pi */
     CF_MODE_WP = 2,    /* rp^2 bins with |pi| < pimax: countpairs_wp */
     CF_MODE_SMU = 3,   /* s^2 bins x linear mu bins: countpairs_s_mu */
-    CF_MODE_THETA = 4  /* angular bins on unit vectors: countpairs_theta_mocks */
+    CF_MODE_THETA = 4, /* angular bins on unit vectors: countpairs_theta_mocks */
+    CF_MODE_RPPI_MOCK = 5, /* rp^2 x pi bins about each pair's line of sight: countpairs_mocks */
+    CF_MODE_SMU_MOCK = 6   /* s^2 x mu bins about each pair's line of sight: countpairs_mocks_s_mu */
 };
 
 #define CF_MAX_EDGES 512

@@ -207,6 +207,29 @@ typedef struct {
     int nbin;
 } results_countpairs_theta;
 
+/* mocks/DDrppi_mocks/countpairs_rp_pi_mocks.h:19-27: 2-D layout npairs[i*(npibin+1) + j] */
+typedef struct {
+    uint64_t *npairs;
+    double *rupp;
+    double *rpavg;
+    double *weightavg;
+    double pimax;
+    int nbin;
+    int npibin;
+} results_countpairs_mocks;
+
+/* mocks/DDsmu_mocks/countpairs_s_mu_mocks.h:19-28: 2-D layout npairs[i*(nmu_bins+1) + j] */
+typedef struct {
+    uint64_t *npairs;
+    double *supp;
+    double *savg;
+    double mu_max;
+    double mu_min;
+    double *weightavg;
+    int nsbin;
+    int nmu_bins;
+} results_countpairs_mocks_s_mu;
+
 /* ---------------- entry points ---------------- */
 
 /* Replaces countpairs(), theory/DD/countpairs.h:28-35 (3-D DD(r) counts). */
@@ -260,6 +283,29 @@ int countpairs_theta_mocks(const int64_t ND1, void *phi1, void *theta1,
                            struct extra_options *extra);
 /* Replaces free_results_countpairs_theta(), mocks/DDtheta_mocks/countpairs_theta_mocks.h. */
 void free_results_countpairs_theta(results_countpairs_theta *results);
+
+/* Replaces countpairs_mocks(), mocks/DDrppi_mocks/countpairs_rp_pi_mocks.h:29-37: DD(rp, pi) of
+ * a survey catalogue (RA, DEC in degrees; cz in km/s, or the comoving distance in Mpc/h when
+ * options->is_comoving_dist is set), rp and pi about each pair's line of sight, cosmology 1
+ * (LasDamas) or 2 (Planck) for cz -> distance.  RA/DEC/cz are fixed up in place exactly where
+ * the reference fixes them (RA in [-180, 180], DEC in [0, 180], redshifts instead of cz). */
+int countpairs_mocks(const int64_t ND1, void *theta1, void *phi1, void *czD1,
+                     const int64_t ND2, void *theta2, void *phi2, void *czD2,
+                     const int numthreads, const int autocorr, const char *binfile, const double pimax,
+                     const int cosmology, results_countpairs_mocks *results, struct config_options *options,
+                     struct extra_options *extra);
+/* Replaces free_results_mocks(), mocks/DDrppi_mocks/countpairs_rp_pi_mocks.h:39. */
+void free_results_mocks(results_countpairs_mocks *results);
+
+/* Replaces countpairs_mocks_s_mu(), mocks/DDsmu_mocks/countpairs_s_mu_mocks.h:30-40: DD(s, mu) of
+ * a survey catalogue, mu the cosine of the angle between s and the pair's line of sight. */
+int countpairs_mocks_s_mu(const int64_t ND1, void *theta1, void *phi1, void *czD1,
+                          const int64_t ND2, void *theta2, void *phi2, void *czD2,
+                          const int numthreads, const int autocorr, const char *sbinfile, const double mu_max,
+                          const int nmu_bins, const int cosmology, results_countpairs_mocks_s_mu *results,
+                          struct config_options *options, struct extra_options *extra);
+/* Replaces free_results_mocks_s_mu(), mocks/DDsmu_mocks/countpairs_s_mu_mocks.h:42. */
+void free_results_mocks_s_mu(results_countpairs_mocks_s_mu *results);
 
 /* ---------------- GB300 extensions (no reference counterpart) ----------------
  * Counting precision of the GPU engine.  CF_PRECISION_FP32_REFINE (default) classifies

@@ -30,6 +30,14 @@
  *   - theta: cos = (x2*x1 + y2*y1) + z2*z1 on unit vectors, accept cosmax < cos <= cosmin,
  *           bin = max k with cos <= cos_upp[k-1]
  *           (mocks/DDtheta_mocks/countpairs_theta_mocks_kernels.c.src:138-192).
+ *   - rp-pi and s-mu of survey catalogues (comoving XYZ, observer at the origin, no wrap):
+ *           s = x2 - x1, l = x1 + x2, pi^2 = (s.l)^2 / |l|^2, rp^2 = s^2 - pi^2, mu^2 = (s.l)^2 / (|l|^2 s^2)
+ *           (mocks/DDrppi_mocks/countpairs_rp_pi_mocks_kernels.c.src:1232-1283,
+ *            mocks/DDsmu_mocks/countpairs_s_mu_mocks_kernels.c.src:1173-1206), in the three
+ *           formula families of those files (fallback, AVX/SSE, AVX512F).
+ *   - cz -> comoving distance (utils/set_cosmo_dist.c:26-67, Simpson table; linear
+ *           interpolation in z = cz / c as gsl_interp_linear evaluates it) and XYZ
+ *           (mocks/DDrppi_mocks/countpairs_rp_pi_mocks_impl.c.src:318-392): cfo_mock_xyz.
  *
  * Outputs are the *raw* per-bin sums (each unordered auto pair counted once); the
  * finalisation (x2 for auto, self pairs, averages, xi / wp) is restated in oracle.py.
@@ -42,7 +50,7 @@
 #include <omp.h>
 #endif
 
-enum { CFO_R3 = 0, CFO_RPPI = 1, CFO_WP = 2, CFO_SMU = 3, CFO_THETA = 4 };
+enum { CFO_R3 = 0, CFO_RPPI = 1, CFO_WP = 2, CFO_SMU = 3, CFO_THETA = 4, CFO_RPPI_MOCK = 5, CFO_SMU_MOCK = 6 };
 
 typedef struct {
     int32_t mode;
@@ -114,6 +122,65 @@ static inline int eval_pair(const cfo_params *p, double xa, double ya, double za
         }
         return -1;
     }
+    if (p->mode == CFO_RPPI_MOCK || p->mode == CFO_SMU_MOCK) {
+        const double parx = xa + xb, pary = ya + yb, parz = za + zb;
+        const double perpx = xb - xa, perpy = yb - ya, perpz = zb - za;
+        double s2, sdl, l2;
+        if (p->fma_formula) {
+            s2 = fma(perpx, perpx, fma(perpy, perpy, perpz * perpz));
+            volatile double t = parx * perpx + pary * perpy;
+            sdl = fma(parz, perpz, t);
+            l2 = fma(parx, parx, fma(pary, pary, parz * parz));
+        } else if (p->chord_formula) {
+            volatile double t1 = perpy * perpy + perpz * perpz, t2 = pary * perpy + parx * perpx,
+                            t3 = pary * pary + parz * parz;
+            s2 = perpx * perpx + t1;
+            sdl = parz * perpz + t2;
+            l2 = parx * parx + t3;
+        } else {
+            volatile double t1 = perpx * perpx + perpy * perpy, t2 = parx * perpx + pary * perpy,
+                            t3 = parx * parx + pary * pary;
+            s2 = t1 + perpz * perpz;
+            sdl = t2 + parz * perpz;
+            l2 = t3 + parz * parz;
+        }
+        const int simd = p->fma_formula || p->chord_formula;
+        const double sqr_sdl = sdl * sdl;
+        const int nrow = p->npibin + 1;
+        double ratio, limit, inv_d;
+        int kbin = -1;
+        if (p->mode == CFO_RPPI_MOCK) {
+            const double pimax = p->pimax, sqr_pimax = pimax * pimax;
+            if (s2 >= e[nb - 1] + sqr_pimax) return -1;
+            if (sqr_sdl >= l2 * sqr_pimax) return -1;
+            ratio = sqr_sdl / l2;
+            limit = sqr_pimax;
+            inv_d = 1.0 / (pimax / p->npibin);
+            const double dperp2 = s2 - ratio;
+            if (dperp2 >= e[nb - 1] || dperp2 < e[0]) return -1;
+            for (int k = nb - 1; k >= 1; k--) if (dperp2 >= e[k - 1]) { kbin = k; break; }
+            if (p->need_avg) *avg_term = sqrt(dperp2);
+        } else {
+            const double mu_max = p->pimax;
+            if (s2 >= e[nb - 1] || s2 < e[0]) return -1;
+            ratio = sqr_sdl / (l2 * s2);
+            if (ratio != ratio) return -1;
+            limit = mu_max * mu_max;
+            inv_d = 1.0 / (mu_max / (double)p->npibin);
+            for (int k = nb - 1; k >= 1; k--) if (s2 >= e[k - 1]) { kbin = k; break; }
+            if (p->need_avg) *avg_term = sqrt(s2);
+        }
+        if (kbin < 0) return -1;
+        const double t = sqrt(ratio) * inv_d;
+        if (simd) {
+            if (!(ratio < limit)) return -1;
+            int flat = (int)((double)(kbin * nrow) + t);
+            return flat > kbin * nrow + p->npibin ? kbin * nrow + p->npibin : flat;
+        }
+        int b = ratio >= limit ? p->npibin : (int)t;
+        b = b > p->npibin ? p->npibin : b;
+        return kbin * nrow + b;
+    }
     const double xpos = xa + ox, ypos = ya + oy, zpos = za + oz;
     const double dx = xb - xpos, dy = yb - ypos, dz = zb - zpos;
     if (p->mode == CFO_R3) {
@@ -184,7 +251,8 @@ static inline int eval_pair(const cfo_params *p, double xa, double ya, double za
 
 int cfo_num_bins(const cfo_params *p)
 {
-    if (p->mode == CFO_RPPI || p->mode == CFO_SMU) return p->nedges * (p->npibin + 1);
+    if (p->mode == CFO_RPPI || p->mode == CFO_SMU || p->mode == CFO_RPPI_MOCK || p->mode == CFO_SMU_MOCK)
+        return p->nedges * (p->npibin + 1);
     return p->nedges;
 }
 
@@ -207,6 +275,11 @@ int cfo_count(const cfo_params *p,
 #else
     (void)nthreads;
 #endif
+    /* mocks: pairs with |dz| beyond the largest separation are rejected by the per-pair test
+     * anyway; skipping them only saves time */
+    double zcut = INFINITY;
+    if (p->mode == CFO_RPPI_MOCK) zcut = sqrt(p->edges[p->nedges - 1] + p->pimax * p->pimax) * (1.0 + 1e-9) + 1e-300;
+    if (p->mode == CFO_SMU_MOCK) zcut = sqrt(p->edges[p->nedges - 1]) * (1.0 + 1e-9) + 1e-300;
 #pragma omp parallel
     {
         uint64_t *ln = calloc(nbins, sizeof(uint64_t));
@@ -217,9 +290,10 @@ int cfo_count(const cfo_params *p,
             const int64_t j0 = p->autocorr ? i + 1 : 0;
             const int cell_i = (p->autocorr && p->mode != CFO_THETA) ? ref_cell(p, x1[i], y1[i], z1[i]) : 0;
             for (int64_t j = j0; j < n2; j++) {
+                if (fabs(z2[j] - z1[i]) >= zcut) continue;
                 /* a = set-1 point, b = set-2 point; offsets that move a next to b */
                 double ox = 0.0, oy = 0.0, oz = 0.0;
-                if (p->mode != CFO_THETA) {
+                if (p->mode != CFO_THETA && p->mode != CFO_RPPI_MOCK && p->mode != CFO_SMU_MOCK) {
                     ox = image_offset(x1[i], x2[j], p->periodic[0], p->wrap[0]);
                     oy = image_offset(y1[i], y2[j], p->periodic[1], p->wrap[1]);
                     oz = image_offset(z1[i], z2[j], p->periodic[2], p->wrap[2]);
@@ -258,4 +332,72 @@ int cfo_count(const cfo_params *p,
         free(lw);
     }
     return 0;
+}
+
+/* ---- survey positions: cz -> comoving distance -> XYZ ---- */
+
+/* D_c(z) table (utils/set_cosmo_dist.c:26-67): Simpson's rule on 1/E(z), step 1e-2/max_size,
+ * a sample every 1/max_size; returns the number of samples. */
+static int cfo_cosmo_table(double zmax, int max_size, double omega_m, double *zc, double *dc)
+{
+    const double OL = 1.0 - omega_m;
+    const double Ok = 1.0 - omega_m - OL;
+    const double Dh = 299800.0 * 0.01 / 1.0;
+    const double Deltaz = 1.0 / max_size;
+    const double dz = 1e-2 * Deltaz;
+    double Eint = 0.0, E2 = 1.0, z2 = Deltaz;
+    int n = 0;
+    for (double z = 2.0 * dz; z < zmax; z += 2.0 * dz) {
+        const double E0 = E2;
+        const double u = 1 + z - dz, v = 1 + z;
+        const double E1 = 1.0 / sqrt(omega_m * (u * u * u) + Ok * (1 + z - dz) + OL);
+        E2 = 1.0 / sqrt(omega_m * (v * v * v) + Ok * (1 + z) + OL);
+        Eint += dz * (E0 + 4. * E1 + E2) / 3.;
+        if (z > (z2 - 1e-10) && z < (z2 + 1e-10)) {
+            if (n >= max_size) break;
+            zc[n] = z;
+            dc[n] = Eint * Dh;
+            z2 += Deltaz;
+            n++;
+        }
+    }
+    return n;
+}
+
+/* Positions of one catalogue.  is_comoving: cz already holds the distance.  Otherwise the
+ * table spans z up to zmax (max cz / c + 0.01 over the catalogues of the call).  Returns 0, or
+ * -1 when a redshift falls outside the table. */
+int cfo_mock_xyz(int64_t n, const double *ra, const double *dec, const double *cz, int is_comoving, double omega_m,
+                 double zmax, double *x, double *y, double *z)
+{
+    const double P = 0.017453292519943295769236907684886127134428718885417254560971;
+    const int max_size = 10000;
+    double *zc = NULL, *dc = NULL;
+    int nz = 0;
+    if (!is_comoving) {
+        zc = calloc(max_size, sizeof(double));
+        dc = calloc(max_size, sizeof(double));
+        nz = cfo_cosmo_table(zmax, max_size, omega_m, zc, dc);
+    }
+    const double inv_c = 1.0 / 299800.0;
+    int rc = 0;
+    for (int64_t i = 0; i < n; i++) {
+        double D = cz[i];
+        if (!is_comoving) {
+            const double zz = cz[i] * inv_c;
+            if (nz < 2 || !(zz >= zc[0] && zz <= zc[nz - 1])) { rc = -1; break; }
+            int lo = 0, hi = nz - 1;
+            while (hi > lo + 1) {
+                const int mid = (lo + hi) / 2;
+                if (zc[mid] > zz) hi = mid; else lo = mid;
+            }
+            D = dc[lo] + (zz - zc[lo]) / (zc[lo + 1] - zc[lo]) * (dc[lo + 1] - dc[lo]);
+        }
+        x[i] = D * cos(dec[i] * P) * cos(ra[i] * P);
+        y[i] = D * cos(dec[i] * P) * sin(ra[i] * P);
+        z[i] = D * sin(dec[i] * P);
+    }
+    free(zc);
+    free(dc);
+    return rc;
 }

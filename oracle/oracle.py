@@ -15,7 +15,10 @@ surrounding driver logic:
     theory/DDrppi/countpairs_rp_pi_impl.c.src:618-642), averages, xi and wp from the analytic
     random counts (theory/xi/countpairs_xi_impl.c.src:581-626, theory/wp/countpairs_wp_impl.c.src:615-660);
   * angular inputs: unit vectors from RA/DEC with libm
-    (mocks/DDtheta_mocks/countpairs_theta_mocks_impl.c.src:569-608).
+    (mocks/DDtheta_mocks/countpairs_theta_mocks_impl.c.src:569-608);
+  * survey inputs of DDrppi_mocks / DDsmu_mocks: the in-place RA/DEC/cz fix-ups
+    (mocks/DDrppi_mocks/countpairs_rp_pi_mocks_impl.c.src:43-112), cosmology 1 / 2
+    (utils/cosmology_params.c:28-55) and the comoving positions (cfo_mock_xyz in cf_oracle.c).
 
 Results are returned in the same structured-array layout as corrfunc_gb300.theory / .mocks.
 """
@@ -29,7 +32,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 SO = os.path.join(HERE, "liboracle.so")
 
-R3, RPPI, WP, SMU, THETA = 0, 1, 2, 3, 4
+R3, RPPI, WP, SMU, THETA, RPPI_MOCK, SMU_MOCK = 0, 1, 2, 3, 4, 5, 6
+SPEED_OF_LIGHT = 299800.0
+OMEGA_M = {1: 0.25, 2: 0.302}
 PI_OVER_180 = 0.017453292519943295769236907684886127134428718885417254560971
 
 
@@ -160,7 +165,7 @@ def _count(mode, autocorr, pos1, w1, pos2, w2, edges, lattice, fma, chord, npibi
     p.pimax = float(pimax)
     p.need_avg = int(bool(need_avg))
     p.need_weight = int(bool(need_w))
-    nb = len(e) * (npibin + 1) if mode in (RPPI, SMU) else len(e)
+    nb = len(e) * (npibin + 1) if mode in (RPPI, SMU, RPPI_MOCK, SMU_MOCK) else len(e)
     npairs = np.zeros(nb, dtype=np.uint64)
     avg = np.zeros(nb)
     ws = np.zeros(nb)
@@ -433,3 +438,91 @@ def DDtheta_mocks(autocorr, binfile, RA1, DEC1, weights1=None, RA2=None, DEC2=No
     out["thetamin"], out["thetamax"] = tupp[:-1], tupp[1:]
     out["thetaavg"], out["npairs"], out["weightavg"] = a[1:], c[1:], w[1:]
     return out
+
+
+def fix_ra_dec_cz(ra, dec, cz, is_comoving_dist):
+    """In-place fix-ups of mocks/DDrppi_mocks/countpairs_rp_pi_mocks_impl.c.src:43-112."""
+    if np.any(dec > 180):
+        raise RuntimeError("DEC above 180 degrees")
+    if np.any(ra < 0.0):
+        ra += 180.0
+    if np.any(dec > 90.0):
+        dec -= 90.0
+    if max(0.0, float(np.max(cz))) < 10.0 and not is_comoving_dist:
+        cz *= SPEED_OF_LIGHT
+
+
+def mock_xyz(ra, dec, cz, is_comoving_dist, cosmology, zmax):
+    lib = _lib()
+    ra, dec, cz = (np.ascontiguousarray(a, dtype=np.float64) for a in (ra, dec, cz))
+    n = len(ra)
+    x, y, z = np.zeros(n), np.zeros(n), np.zeros(n)
+
+    def P(a):
+        return a.ctypes.data_as(ctypes.c_void_p)
+
+    lib.cfo_mock_xyz.restype = ctypes.c_int
+    rc = lib.cfo_mock_xyz(ctypes.c_int64(n), P(ra), P(dec), P(cz), ctypes.c_int(int(bool(is_comoving_dist))),
+                          ctypes.c_double(OMEGA_M.get(cosmology, 0.25)), ctypes.c_double(zmax), P(x), P(y), P(z))
+    if rc != 0:
+        raise RuntimeError("redshift outside the comoving-distance table")
+    return x, y, z
+
+
+def _mock_counts(mode, autocorr, cosmology, binfile, npibin, pimax_or_mu, RA1, DEC1, CZ1, weights1, RA2, DEC2, CZ2,
+                 weights2, is_comoving_dist, output_avg, isa, weight_type, nthreads):
+    if cosmology not in OMEGA_M:
+        raise RuntimeError("Cosmology=%d not implemented" % cosmology)
+    rupp = read_bins(binfile)
+    sets = [(RA1, DEC1, CZ1)] + ([] if autocorr else [(RA2, DEC2, CZ2)])
+    for ra, dec, cz in sets:
+        fix_ra_dec_cz(ra, dec, cz, is_comoving_dist)
+    czmax = 0.0
+    for _, _, cz in sets:
+        czmax = max(czmax, float(np.max(cz)))
+    zmax = czmax * (1.0 / SPEED_OF_LIGHT) + 0.01
+    pos1 = mock_xyz(RA1, DEC1, CZ1, is_comoving_dist, cosmology, zmax)
+    pos2 = pos1 if autocorr else mock_xyz(RA2, DEC2, CZ2, is_comoving_dist, cosmology, zmax)
+    need_w = weight_type is not None
+    w1 = _weights(weights1, len(RA1)) if need_w else None
+    w2 = (w1 if autocorr else _weights(weights2, len(RA2))) if need_w else None
+    if need_w and not autocorr:
+        w1 = np.ones(len(RA1)) if w1 is None else w1
+        w2 = np.ones(len(RA2)) if w2 is None else w2
+    fma, simd = _formula(isa)
+    lat = ([0.0] * 3, [0.0] * 3, [1, 1, 1], [0.0] * 3, [0, 0, 0])
+    c, a, w = _count(mode, autocorr, pos1, w1, pos2, w2, rupp * rupp, lat, fma, simd, npibin=npibin,
+                     pimax=pimax_or_mu, need_avg=output_avg, need_w=need_w, nthreads=nthreads)
+    c, a, w = _finalize(c, a, w, autocorr, False, npibin + 1, len(RA1), 0.0, output_avg, need_w)
+    return rupp, c, a, w
+
+
+def DDrppi_mocks(autocorr, cosmology, pimax, binfile, RA1, DEC1, CZ1, weights1=None, RA2=None, DEC2=None, CZ2=None,
+                 weights2=None, is_comoving_dist=False, output_rpavg=False, isa="fallback", weight_type=None,
+                 nthreads=0):
+    from corrfunc_gb300.mocks import DDRPPI_MOCKS_DTYPE
+    npibin = int(pimax)
+    rupp, c, a, w = _mock_counts(RPPI_MOCK, autocorr, cosmology, binfile, npibin, pimax, RA1, DEC1, CZ1, weights1,
+                                 RA2, DEC2, CZ2, weights2, is_comoving_dist, output_rpavg, isa, weight_type, nthreads)
+    dpi = pimax / npibin
+    rows = []
+    for i in range(1, len(rupp)):
+        for j in range(npibin):
+            k = i * (npibin + 1) + j
+            rows.append((rupp[i - 1], rupp[i], a[k], (j + 1) * dpi, c[k], w[k]))
+    return np.array(rows, dtype=DDRPPI_MOCKS_DTYPE)
+
+
+def DDsmu_mocks(autocorr, cosmology, mu_max, nmu_bins, binfile, RA1, DEC1, CZ1, weights1=None, RA2=None, DEC2=None,
+                CZ2=None, weights2=None, is_comoving_dist=False, output_savg=False, isa="fallback", weight_type=None,
+                nthreads=0):
+    from corrfunc_gb300.mocks import DDSMU_MOCKS_DTYPE
+    rupp, c, a, w = _mock_counts(SMU_MOCK, autocorr, cosmology, binfile, nmu_bins, mu_max, RA1, DEC1, CZ1, weights1,
+                                 RA2, DEC2, CZ2, weights2, is_comoving_dist, output_savg, isa, weight_type, nthreads)
+    dmu = mu_max / nmu_bins
+    rows = []
+    for i in range(1, len(rupp)):
+        for j in range(nmu_bins):
+            k = i * (nmu_bins + 1) + j
+            rows.append((rupp[i - 1], rupp[i], a[k], (j + 1) * dmu, c[k], w[k]))
+    return np.array(rows, dtype=DDSMU_MOCKS_DTYPE)

@@ -246,6 +246,41 @@ def test_smu_rejects_bad_mu(lib):
         assert rc == 1
 
 
+def _call_mocks(lib, smu=False, cosmology=1, dec_value=10.0, mu_max=1.0, nmu=5, bins=(0.5, 1.0, 2.0), pimax=10.0):
+    from corrfunc_gb300 import _capi as C
+    ra = np.array([150.0, 150.1, 150.2])
+    dec = np.array([10.0, 10.1, dec_value])
+    cz = np.array([8000.0, 8010.0, 8020.0])
+    o = C.get_config_options()
+    e = C.get_extra_options()
+    with C.BinFile(list(bins)) as bf:
+        if smu:
+            res = C.ResultsSMu()
+            return lib.countpairs_mocks_s_mu(3, C.ptr(ra), C.ptr(dec), C.ptr(cz), 3, C.ptr(ra), C.ptr(dec), C.ptr(cz), 1,
+                                             1, bf.encode(), mu_max, nmu, cosmology, ctypes.byref(res),
+                                             ctypes.byref(o), ctypes.byref(e))
+        res = C.ResultsRpPi()
+        return lib.countpairs_mocks(3, C.ptr(ra), C.ptr(dec), C.ptr(cz), 3, C.ptr(ra), C.ptr(dec), C.ptr(cz), 1, 1,
+                                    bf.encode(), pimax, cosmology, ctypes.byref(res), ctypes.byref(o),
+                                    ctypes.byref(e))
+
+
+@pytest.mark.parametrize("smu", [False, True])
+def test_mocks_reject_bad_inputs(lib, smu):
+    """Unknown cosmology, DEC above 180 and a zero lower separation edge fail as in
+    mocks/DDrppi_mocks/countpairs_rp_pi_mocks_impl.c.src:62-66,283-298 (and the DDsmu_mocks copies);
+    mu_max outside (0, 1] and nmu_bins < 1 fail for DDsmu_mocks."""
+    assert _call_mocks(lib, smu, cosmology=3) == 1
+    assert _call_mocks(lib, smu, dec_value=190.0) == 1
+    assert _call_mocks(lib, smu, bins=(0.0, 1.0, 2.0)) == 1
+    if smu:
+        assert _call_mocks(lib, True, mu_max=1.5) == 1
+        assert _call_mocks(lib, True, mu_max=0.0) == 1
+        assert _call_mocks(lib, True, nmu=0) == 1
+    else:
+        assert _call_mocks(lib, False, pimax=0.5) == 1
+
+
 def test_no_gpu_fails_loudly_not_silently(lib):
     """Without a usable GPU the library reports failure; it never falls back to the CPU."""
     import corrfunc_gb300

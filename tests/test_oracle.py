@@ -210,3 +210,44 @@ def test_oracle_reproduces_mr19_wtheta_golden(orc):
     assert list(res["npairs"]) == [int(v) for v in gold[:, 0]]
     np.testing.assert_allclose(res["thetaavg"], gold[:, 1], rtol=1e-6, atol=1e-9)
     np.testing.assert_allclose(res["weightavg"], gold[:, 4], rtol=1e-6, atol=1e-9)
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF_ROOT, "mocks", "tests")), reason="reference tree not present")
+def test_oracle_reproduces_mr19_rppi_mocks_golden(orc):
+    """mocks/tests/Mr19_mock.DD (Corrfunc/tests/test_mocks.py:14-34) on its own input: cz -> comoving
+    distance with cosmology 1, pimax 40, mocks/tests/bins, pair_product weights, rpavg."""
+    ra, dec, cz, w = _read_fastfood(os.path.join(REF_ROOT, "mocks", "tests", "data", "Mr19_mock_northonly.rdcz.ff"))
+    res = orc.DDrppi_mocks(1, 1, 40.0, os.path.join(REF_ROOT, "mocks", "tests", "bins"), ra.copy(), dec.copy(),
+                           cz.copy(), weights1=w, weight_type="pair_product", output_rpavg=True)
+    gold = np.loadtxt(os.path.join(REF_ROOT, "mocks", "tests", "Mr19_mock.DD"))
+    assert list(res["npairs"]) == [int(v) for v in gold[:, 0]]
+    np.testing.assert_allclose(res["rpavg"], gold[:, 1], rtol=1e-6, atol=1e-9)
+    np.testing.assert_allclose(res["weightavg"], gold[:, 4], rtol=1e-6, atol=1e-9)
+
+
+def test_oracle_mock_formula_families_agree_off_the_edges(orc):
+    """The three double-precision formula families (fallback, AVX/SSE, AVX512F) of DDrppi_mocks and
+    DDsmu_mocks differ only in rounding: on a small survey their counts agree except for pairs within
+    a few ulps of an edge, i.e. in practice everywhere, and the rp-pi counts sum to the pairs a
+    numpy restatement finds inside the (rp, pi) domain."""
+    from corrfunc_gb300 import catalogs as cat
+    ra, dec, cz = cat.survey(3000, 11)
+    bins = cat.log_bins(0.5, 15.0, 8)
+    outs = [orc.DDrppi_mocks(1, 1, 20.0, bins, ra.copy(), dec.copy(), cz.copy(), isa=isa)
+            for isa in ("fallback", "avx", "avx512f")]
+    for o in outs[1:]:
+        assert np.array_equal(o["npairs"], outs[0]["npairs"])
+    x, y, z = orc.mock_xyz(ra, dec, cz, False, 1, float(cz.max()) / orc.SPEED_OF_LIGHT + 0.01)
+    P = np.stack([x, y, z], 1)
+    s = P[None, :, :] - P[:, None, :]
+    l = P[None, :, :] + P[:, None, :]
+    pi2 = np.einsum("ijk,ijk->ij", s, l) ** 2 / np.einsum("ijk,ijk->ij", l, l)
+    rp2 = np.einsum("ijk,ijk->ij", s, s) - pi2
+    iu = np.triu_indices(len(x), 1)
+    inside = (rp2[iu] >= bins[0] ** 2) & (rp2[iu] < bins[-1] ** 2) & (pi2[iu] < 20.0 ** 2)
+    assert int(outs[0]["npairs"].sum()) == 2 * int(inside.sum())
+    smu = [orc.DDsmu_mocks(1, 2, 1.0, 5, bins, ra.copy(), dec.copy(), cz.copy(), isa=isa)
+           for isa in ("fallback", "avx", "avx512f")]
+    for o in smu[1:]:
+        assert np.array_equal(o["npairs"], smu[0]["npairs"])
+    assert smu[0]["npairs"].sum() > 0
