@@ -539,6 +539,133 @@ static PyObject *py_countpairs_theta_mocks(PyObject *self, PyObject *args, PyObj
     return with_time(list, &o);
 }
 
+/* Shared body of countpairs_rp_pi_mocks / countpairs_s_mu_mocks: kwlists and format strings of
+ * mocks/python_bindings/_countpairs_mocks.c:1124-1154 (rp_pi) and :1449-1479 (s_mu); rows
+ * (low, high, avg, (j + 1) * width, npairs, weightavg) as built at :1390-1404 and :1716-1730. */
+static PyObject *mocks_2d(PyObject *args, PyObject *kwargs, int smu)
+{
+    const char *fn = smu ? "countpairs_s_mu_mocks" : "countpairs_rp_pi_mocks";
+    static char *kw_rppi[] = {"autocorr", "cosmology", "nthreads", "pimax", "binfile", "RA1", "DEC1", "CZ1",
+                              "weights1", "RA2", "DEC2", "CZ2", "weights2", "is_comoving_dist", "verbose",
+                              "output_rpavg", "fast_divide_and_NR_steps", "xbin_refine_factor", "ybin_refine_factor",
+                              "zbin_refine_factor", "max_cells_per_dim", "copy_particles", "enable_min_sep_opt",
+                              "c_api_timer", "isa", "weight_type", NULL};
+    static char *kw_smu[] = {"autocorr", "cosmology", "nthreads", "mu_max", "nmu_bins", "binfile", "RA1", "DEC1",
+                             "CZ1", "weights1", "RA2", "DEC2", "CZ2", "weights2", "is_comoving_dist", "verbose",
+                             "output_savg", "fast_divide_and_NR_steps", "xbin_refine_factor", "ybin_refine_factor",
+                             "zbin_refine_factor", "max_cells_per_dim", "copy_particles", "enable_min_sep_opt",
+                             "c_api_timer", "isa", "weight_type", NULL};
+    int autocorr = 1, nthreads = 4, cosmology = 1, nmu_bins = 0;
+    double width_max = 0.0;  /* pimax or mu_max */
+    char *binfile = NULL, *wname = NULL;
+    cf_pyset s1 = {{0}}, s2 = {{0}};
+    struct config_options o = get_config_options();
+    o.is_comoving_dist = 0;
+    o.verbose = 0;
+    o.instruction_set = -1;
+    o.periodic = 0;
+    o.fast_divide_and_NR_steps = 0;
+    o.c_api_timer = 0;
+    o.enable_min_sep_opt = 1;
+    o.copy_particles = 1;
+    int8_t rx = o.bin_refine_factors[0], ry = o.bin_refine_factors[1], rz = o.bin_refine_factors[2];
+    int ok;
+    if (smu) {
+        ok = PyArg_ParseTupleAndKeywords(args, kwargs, "iiidisO!O!O!|O!O!O!O!O!bbbbbbbhbbbis", kw_smu, &autocorr,
+                                         &cosmology, &nthreads, &width_max, &nmu_bins, &binfile, &PyArray_Type,
+                                         &s1.in[0], &PyArray_Type, &s1.in[1], &PyArray_Type, &s1.in[2], &PyArray_Type,
+                                         &s1.in[3], &PyArray_Type, &s2.in[0], &PyArray_Type, &s2.in[1], &PyArray_Type,
+                                         &s2.in[2], &PyArray_Type, &s2.in[3], &o.is_comoving_dist, &o.verbose,
+                                         &o.need_avg_sep, &o.fast_divide_and_NR_steps, &rx, &ry, &rz,
+                                         &o.max_cells_per_dim, &o.copy_particles, &o.enable_min_sep_opt,
+                                         &o.c_api_timer, &o.instruction_set, &wname);
+    } else {
+        ok = PyArg_ParseTupleAndKeywords(args, kwargs, "iiidsO!O!O!|O!O!O!O!O!bbbbbbbhbbbis", kw_rppi, &autocorr,
+                                         &cosmology, &nthreads, &width_max, &binfile, &PyArray_Type, &s1.in[0],
+                                         &PyArray_Type, &s1.in[1], &PyArray_Type, &s1.in[2], &PyArray_Type, &s1.in[3],
+                                         &PyArray_Type, &s2.in[0], &PyArray_Type, &s2.in[1], &PyArray_Type, &s2.in[2],
+                                         &PyArray_Type, &s2.in[3], &o.is_comoving_dist, &o.verbose, &o.need_avg_sep,
+                                         &o.fast_divide_and_NR_steps, &rx, &ry, &rz, &o.max_cells_per_dim,
+                                         &o.copy_particles, &o.enable_min_sep_opt, &o.c_api_timer,
+                                         &o.instruction_set, &wname);
+    }
+    if (!ok) {
+        PyErr_Clear();
+        return fail(fn, "ArgumentError: could not parse the arguments");
+    }
+    refine_options(&o, rx, ry, rz);
+    struct extra_options extra;
+    int elem = 8;
+    if (prepare_sets(fn, autocorr, 3, &s1, &s2, wname, &extra, &elem) != 0) {
+        set_release(&s1);
+        set_release(&s2);
+        Py_RETURN_NONE;
+    }
+    o.float_type = (uint8_t)elem;
+    void *r2 = autocorr ? set_data(&s1, 0) : set_data(&s2, 0);
+    void *d2 = autocorr ? set_data(&s1, 1) : set_data(&s2, 1);
+    void *c2 = autocorr ? set_data(&s1, 2) : set_data(&s2, 2);
+    const int64_t n2 = autocorr ? s1.n : s2.n;
+    int rc;
+    PyObject *list = NULL;
+    if (smu) {
+        results_countpairs_mocks_s_mu r;
+        Py_BEGIN_ALLOW_THREADS
+        rc = countpairs_mocks_s_mu(s1.n, set_data(&s1, 0), set_data(&s1, 1), set_data(&s1, 2), n2, r2, d2, c2,
+                                   nthreads, autocorr, binfile, width_max, nmu_bins, cosmology, &r, &o, &extra);
+        Py_END_ALLOW_THREADS
+        set_release(&s1);
+        set_release(&s2);
+        if (rc != EXIT_SUCCESS) Py_RETURN_NONE;
+        list = PyList_New(0);
+        const double dmu = width_max / (double)r.nmu_bins;
+        for (int i = 1; list && r.npairs && i < r.nsbin; i++) {
+            for (int j = 0; j < r.nmu_bins; j++) {
+                const int b = i * (r.nmu_bins + 1) + j;
+                PyObject *it = Py_BuildValue("(ddddkd)", r.supp[i - 1], r.supp[i], r.savg[b], (j + 1) * dmu,
+                                             (unsigned long)r.npairs[b], r.weightavg[b]);
+                PyList_Append(list, it);
+                Py_XDECREF(it);
+            }
+        }
+        free_results_mocks_s_mu(&r);
+    } else {
+        results_countpairs_mocks r;
+        Py_BEGIN_ALLOW_THREADS
+        rc = countpairs_mocks(s1.n, set_data(&s1, 0), set_data(&s1, 1), set_data(&s1, 2), n2, r2, d2, c2, nthreads,
+                              autocorr, binfile, width_max, cosmology, &r, &o, &extra);
+        Py_END_ALLOW_THREADS
+        set_release(&s1);
+        set_release(&s2);
+        if (rc != EXIT_SUCCESS) Py_RETURN_NONE;
+        list = PyList_New(0);
+        const double dpi = width_max / (double)r.npibin;
+        for (int i = 1; list && r.npairs && i < r.nbin; i++) {
+            for (int j = 0; j < r.npibin; j++) {
+                const int b = i * (r.npibin + 1) + j;
+                PyObject *it = Py_BuildValue("(ddddkd)", r.rupp[i - 1], r.rupp[i], r.rpavg[b], (j + 1) * dpi,
+                                             (unsigned long)r.npairs[b], r.weightavg[b]);
+                PyList_Append(list, it);
+                Py_XDECREF(it);
+            }
+        }
+        free_results_mocks(&r);
+    }
+    return with_time(list, &o);
+}
+
+static PyObject *py_countpairs_rp_pi_mocks(PyObject *self, PyObject *args, PyObject *kwargs)
+{
+    (void)self;
+    return mocks_2d(args, kwargs, 0);
+}
+
+static PyObject *py_countpairs_s_mu_mocks(PyObject *self, PyObject *args, PyObject *kwargs)
+{
+    (void)self;
+    return mocks_2d(args, kwargs, 1);
+}
+
 /* ---------------- module tables ---------------- */
 
 static PyMethodDef theory_methods[] = {
@@ -557,6 +684,10 @@ static PyMethodDef theory_methods[] = {
 static PyMethodDef mocks_methods[] = {
     {"countpairs_theta_mocks", (PyCFunction)(void (*)(void))py_countpairs_theta_mocks, METH_VARARGS | METH_KEYWORDS,
      "Angular pair counts DD(theta) on the sky (countpairs_theta_mocks)."},
+    {"countpairs_rp_pi_mocks", (PyCFunction)(void (*)(void))py_countpairs_rp_pi_mocks, METH_VARARGS | METH_KEYWORDS,
+     "Pair counts in (rp, pi) of survey catalogues (countpairs_mocks)."},
+    {"countpairs_s_mu_mocks", (PyCFunction)(void (*)(void))py_countpairs_s_mu_mocks, METH_VARARGS | METH_KEYWORDS,
+     "Pair counts in (s, mu) of survey catalogues (countpairs_mocks_s_mu)."},
     {NULL, NULL, 0, NULL}};
 
 static struct PyModuleDef theory_module = {PyModuleDef_HEAD_INIT, "_countpairs",

@@ -16,7 +16,8 @@ def test_modules_export_the_reference_functions():
     cp, cpm = _modules()
     for name in ("countpairs", "countpairs_rp_pi", "countpairs_wp", "countpairs_xi", "countpairs_s_mu"):
         assert callable(getattr(cp, name))
-    assert callable(cpm.countpairs_theta_mocks)
+    for name in ("countpairs_theta_mocks", "countpairs_rp_pi_mocks", "countpairs_s_mu_mocks"):
+        assert callable(getattr(cpm, name))
 
 
 def test_argument_errors_return_none(capfd):
@@ -32,6 +33,8 @@ def test_argument_errors_return_none(capfd):
     # cross-correlation without the second set
     assert cp.countpairs(0, 1, bins, x, x, x) is None
     assert cpm.countpairs_theta_mocks(0, 1, bins, x, x) is None
+    assert cpm.countpairs_rp_pi_mocks(0, 1, 1, 10.0, bins, x, x, x) is None
+    assert cpm.countpairs_s_mu_mocks(1, 1, 1, 1.0, 5, bins, x, x, x.astype(np.float32)) is None
     assert "corrfunc_gb300" in capfd.readouterr().err
 
 
@@ -79,6 +82,17 @@ def test_modules_match_the_python_front_end():
     want = mocks.DDtheta_mocks(1, 2, tb, ra.copy(), dec.copy(), output_thetaavg=True)
     assert [r[3] for r in got] == list(want["npairs"])
     np.testing.assert_allclose([r[2] for r in got], want["thetaavg"], rtol=1e-12)
+
+    ra, dec, cz = cat.survey(4000, 6)
+    mb = cat.log_bins(0.5, 10.0, 6)
+    got, _ = cpm.countpairs_rp_pi_mocks(1, 1, 2, 12.0, _binfile(mb), ra.copy(), dec.copy(), cz.copy(),
+                                        output_rpavg=True)
+    want = mocks.DDrppi_mocks(1, 1, 2, 12.0, mb, ra.copy(), dec.copy(), cz.copy(), output_rpavg=True)
+    assert [r[4] for r in got] == list(want["npairs"])
+    assert [r[3] for r in got] == list(want["pimax"])
+    got, _ = cpm.countpairs_s_mu_mocks(1, 2, 2, 0.9, 6, _binfile(mb), ra.copy(), dec.copy(), cz.copy())
+    want = mocks.DDsmu_mocks(1, 2, 2, 0.9, 6, mb, ra.copy(), dec.copy(), cz.copy())
+    assert [r[4] for r in got] == list(want["npairs"])
 
 
 _FILES = []
