@@ -690,6 +690,7 @@ def other_counters(cf, cat, theory):
     }
     # survey catalogue of the reference's mocks tests' size and footprint (84,383 galaxies,
     # RA 110-266, DEC -4-70, cz 6,000-20,000 km/s), pimax 40 and 14 log rp bins 0.1-25
+    x4, y4, z4 = cat.clustered_box(1_000_000, 420.0, 3)
     sra, sdec, scz = cat.survey(84383, 5, ra=(110.0, 266.0), dec=(-4.0, 70.0), cz=(6000.0, 20000.0))
     sw = cat.weights(84383, 6)
     runs["mocks_DDrppi_mocks"] = lambda: mocks.DDrppi_mocks(1, 1, 1, 40.0, rp, sra.copy(), sdec.copy(), scz.copy(),
@@ -698,6 +699,9 @@ def other_counters(cf, cat, theory):
     runs["mocks_DDsmu_mocks"] = lambda: mocks.DDsmu_mocks(1, 1, 1, 1.0, 10, rp, sra.copy(), sdec.copy(), scz.copy(),
                                                           weights1=sw, weight_type="pair_product", output_savg=True,
                                                           isa="fallback")
+    # counts in spheres: 1M clustered points in L=420, spheres up to radius 10, 10 radii, p0..p5
+    runs["vpf_1M_nc1e4"] = lambda: theory.vpf(10.0, 10, 10000, 6, -1234, x4, y4, z4, periodic=True, boxsize=420.0)
+    runs["vpf_1M_nc1e6"] = lambda: theory.vpf(10.0, 10, 1000000, 6, -1234, x4, y4, z4, periodic=True, boxsize=420.0)
     for name, fn in runs.items():
         for prec in ("fp64", "fp32_refine"):
             cf.set_precision(prec)

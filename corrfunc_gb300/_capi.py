@@ -86,6 +86,12 @@ class ResultsXi(Structure):
                 ("ravg", POINTER(c_double)), ("weightavg", POINTER(c_double)), ("nbin", c_int)]
 
 
+class ResultsVpf(Structure):
+    """results_countspheres / results_countspheres_mocks (pN is an array of nbin rows)."""
+    _fields_ = [("pN", POINTER(POINTER(c_double))), ("rmax", c_double), ("nbin", c_int), ("nc", c_int),
+                ("num_pN", c_int)]
+
+
 class ResultsTheta(Structure):
     _fields_ = [("npairs", POINTER(c_uint64)), ("theta_upp", POINTER(c_double)),
                 ("theta_avg", POINTER(c_double)), ("weightavg", POINTER(c_double)), ("nbin", c_int)]
@@ -126,6 +132,13 @@ _PROTOS = {
                                c_int, ctypes.c_char_p, c_double, c_int, c_int, POINTER(ResultsSMu),
                                POINTER(ConfigOptions), POINTER(ExtraOptions)], c_int),
     "free_results_mocks_s_mu": ([POINTER(ResultsSMu)], None),
+    "countspheres": ([c_int64, c_void_p, c_void_p, c_void_p, c_double, c_int, c_int, c_int, ctypes.c_ulong,
+                      POINTER(ResultsVpf), POINTER(ConfigOptions), POINTER(ExtraOptions)], c_int),
+    "free_results_countspheres": ([POINTER(ResultsVpf)], None),
+    "countspheres_mocks": ([c_int64, c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_int,
+                            c_double, c_int, c_int, c_int, ctypes.c_char_p, c_int, POINTER(ResultsVpf),
+                            POINTER(ConfigOptions), POINTER(ExtraOptions)], c_int),
+    "free_results_countspheres_mocks": ([POINTER(ResultsVpf)], None),
 }
 
 _GPU_PROTOS = {
@@ -360,3 +373,15 @@ def carray(p, n, dtype):
     if n <= 0:
         return np.zeros(0, dtype=dtype)
     return np.ctypeslib.as_array(p, shape=(n,)).astype(dtype, copy=True)
+
+
+def vpf_rows(res, num_pN):
+    """(rmax_k, pN[k][0..num_pN-1]) rows as the reference's bindings build them
+    (theory/python_bindings/_countpairs.c:2674-2690): rmax_k = (k + 1) * rmax / nbin."""
+    dt = np.dtype([("rmax", np.float64), ("pN", (np.float64, num_pN))])
+    out = np.zeros(res.nbin, dtype=dt)
+    rstep = res.rmax / float(res.nbin) if res.nbin else 0.0
+    for k in range(res.nbin):
+        out["rmax"][k] = (k + 1) * rstep
+        out["pN"][k] = [res.pN[k][i] for i in range(num_pN)]
+    return out

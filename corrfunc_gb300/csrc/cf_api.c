@@ -1536,6 +1536,414 @@ void free_results_mocks_s_mu(results_countpairs_mocks_s_mu *results)
 }
 
 /* ========================= GB300 extensions ========================= */
+/* ========================= countspheres (vpf), countspheres_mocks (vpf_mocks) ========================= */
+
+static double **pn_matrix(int nbin, int num_pN)
+{
+    double **m = calloc((size_t)nbin, sizeof(double *));
+    if (m == NULL) return NULL;
+    for (int i = 0; i < nbin; i++) {
+        m[i] = calloc((size_t)num_pN, sizeof(double));
+        if (m[i] == NULL) {
+            for (int k = 0; k < i; k++) free(m[k]);
+            free(m);
+            return NULL;
+        }
+    }
+    return m;
+}
+
+static void pn_free(double **m, int nbin)
+{
+    if (m == NULL) return;
+    for (int i = 0; i < nbin; i++) free(m[i]);
+    free(m);
+}
+
+static void refine_check(struct config_options *options)
+{
+    if (options->max_cells_per_dim == 0) {
+        fprintf(stderr, "Warning: Max. cells per dimension is set to 0 - resetting to `NLATMAX' = %d\n", NLATMAX);
+        options->max_cells_per_dim = NLATMAX;
+    }
+    for (int i = 0; i < 3; i++) {
+        if (options->bin_refine_factors[i] < 1) {
+            fprintf(stderr, "Warning: bin refine factor along axis = %d *must* be >=1. Instead found bin refine factor =%d\n",
+                    i, options->bin_refine_factors[i]);
+            reset_bin_refine_factors(options);
+            break;
+        }
+    }
+}
+
+/* theory/vpf/countspheres.c:34-77 + theory/vpf/countspheres_impl.c.src:136-479 */
+int countspheres(const int64_t np, void *X, void *Y, void *Z, const double rmax, const int nbin, const int nc,
+                 const int num_pN, unsigned long seed, results_countspheres *results, struct config_options *options,
+                 struct extra_options *extra)
+{
+    (void)extra;
+    const double t0 = wall_now();
+    if (check_options(options, __func__) != EXIT_SUCCESS || results == NULL) return EXIT_FAILURE;
+    if (!(rmax > 0.0 && nbin > 0 && nc > 0 && num_pN > 0)) {
+        CF_ERR("Invalid input parameters. Expected rmax > 0, number of bins > 0, number of random spheres > 0, number of "
+               "pN's to calculate > 0.\nFound rmax = %lf, nbin = %d nspheres = %d num_pN = %d", rmax, nbin, nc, num_pN);
+        return EXIT_FAILURE;
+    }
+    if (np < 1) {
+        CF_ERR("vpf needs at least one particle");
+        return EXIT_FAILURE;
+    }
+    refine_check(options);
+    cf_mt19937 rng;
+    cf_mt_seed(&rng, seed);
+    const size_t es = options->float_type;
+    double *P = malloc(sizeof(double) * 3 * (size_t)np);
+    if (P == NULL) return EXIT_FAILURE;
+    double *px = P, *py = P + np, *pz = P + 2 * np;
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int64_t i = 0; i < np; i++) {
+        px[i] = wval(X, i, es);
+        py[i] = wval(Y, i, es);
+        pz[i] = wval(Z, i, es);
+        const double v[3] = {px[i], py[i], pz[i]};
+        for (int a = 0; a < 3; a++) {
+            if (v[a] < lo[a]) lo[a] = v[a];
+            if (v[a] > hi[a]) hi[a] = v[a];
+        }
+    }
+    if (options->periodic && options->boxsize == BOXSIZE_NOTGIVEN) {
+        fprintf(stderr, "boxsize = %g must be specified with periodic wrap. Please specify a non-zero boxsize, or zero to "
+                "detect the particle extent, or -1 to make a dimension non-periodic.\n", options->boxsize);
+        free(P);
+        return EXIT_FAILURE;
+    }
+    const double bsz[3] = {options->boxsize_x,
+                           options->boxsize_y == BOXSIZE_NOTGIVEN ? options->boxsize : options->boxsize_y,
+                           options->boxsize_z == BOXSIZE_NOTGIVEN ? options->boxsize : options->boxsize_z};
+    cf_vpf_job J;
+    memset(&J, 0, sizeof(J));
+    double wrap[3];
+    for (int a = 0; a < 3; a++) {
+        wrap[a] = (options->periodic && bsz[a] > 0) ? bsz[a] : (hi[a] - lo[a]);
+        double binsize;
+        if (cf_ref_binsize(hi[a] - lo[a], wrap[a], rmax, options->bin_refine_factors[a], options->max_cells_per_dim,
+                           &binsize, &J.nmesh[a]) != EXIT_SUCCESS) {
+            free(P);
+            return EXIT_FAILURE;
+        }
+        J.lat_min[a] = lo[a];
+        J.lat_inv[a] = binsize > 0 ? 1.0 / binsize : 0.0;
+        J.refine[a] = options->bin_refine_factors[a];
+        J.wrap[a] = wrap[a];
+    }
+    double *cen = malloc(sizeof(double) * 3 * (size_t)nc);
+    int *cell = malloc(sizeof(int) * 3 * (size_t)nc);
+    uint64_t *cnt = calloc((size_t)nbin * num_pN, sizeof(uint64_t));
+    int rc = (cen && cell && cnt) ? EXIT_SUCCESS : EXIT_FAILURE;
+    const double inv_wrap[3] = {1.0 / wrap[0], 1.0 / wrap[1], 1.0 / wrap[2]};
+    for (int ic = 0; rc == EXIT_SUCCESS && ic < nc;) {
+        double c[3];
+        for (int a = 0; a < 3; a++) c[a] = wrap[a] * cf_mt_uniform(&rng) + lo[a];
+        if (!options->periodic) {
+            int near = 0;
+            for (int a = 0; a < 3; a++) near |= (c[a] - lo[a]) < rmax || (hi[a] - c[a]) < rmax;
+            if (near) continue;
+        }
+        for (int a = 0; a < 3; a++) {
+            int k = (int)(J.nmesh[a] * (c[a] - lo[a]) * inv_wrap[a]);
+            if (k > J.nmesh[a] - 1) k--;
+            if (k < 0 || k >= J.nmesh[a]) {
+                CF_ERR("%c-position = %lf with index = %d should be in [0, %d)", 'x' + a, c[a], k, J.nmesh[a]);
+                rc = EXIT_FAILURE;
+            }
+            cen[3 * ic + a] = c[a];
+            cell[3 * ic + a] = k;
+        }
+        ic++;
+    }
+    if (rc == EXIT_SUCCESS) {
+        J.np = np;
+        J.x = px; J.y = py; J.z = pz;
+        J.periodic = options->periodic ? 1 : 0;
+        J.ncen = nc;
+        J.cen = cen;
+        J.cen_cell = cell;
+        J.rmax = rmax;
+        J.nbin = nbin;
+        J.num_pN = num_pN;
+        rc = cf_engine_vpf(&J, cnt);
+    }
+    if (rc == EXIT_SUCCESS) {
+        results->rmax = rmax;
+        results->nbin = nbin;
+        results->nc = nc;
+        results->num_pN = num_pN;
+        results->pN = pn_matrix(nbin, num_pN);
+        if (results->pN == NULL) rc = EXIT_FAILURE;
+        const double inv_nc = 1.0 / (double)nc;
+        for (int i = 0; rc == EXIT_SUCCESS && i < num_pN; i++)
+            for (int b = 0; b < nbin; b++) results->pN[b][i] = (double)cnt[(size_t)b * num_pN + i] * inv_nc;
+    }
+    free(P);
+    free(cen);
+    free(cell);
+    free(cnt);
+    if (rc != EXIT_SUCCESS) return EXIT_FAILURE;
+    reset_bin_refine_factors(options);
+    if (options->c_api_timer) options->c_api_time = wall_now() - t0;
+    return EXIT_SUCCESS;
+}
+
+void free_results_countspheres(results_countspheres *results)
+{
+    if (results == NULL) return;
+    pn_free(results->pN, results->nbin);
+    results->pN = NULL;
+    results->rmax = 0.0;
+    results->nbin = 0;
+    results->nc = 0;
+    results->num_pN = 0;
+}
+
+/* comoving XYZ of one catalogue shifted into the bounding cube; *dmax is raised to the largest
+ * distance (mocks/vpf_mocks/countspheres_mocks_impl.c.src:309-370) */
+static int vpf_mock_positions(int64_t n, const void *ra, const void *dec, const void *cz, size_t es, const double *zc,
+                              const double *dcs, int nz, double *X, double *Y, double *Z, double *dmax)
+{
+    const double inv_c = 1.0 / CF_SPEED_OF_LIGHT;
+    for (int64_t i = 0; i < n; i++) {
+        double D = wval(cz, i, es);
+        if (zc != NULL && interp_linear(zc, dcs, nz, D * inv_c, &D) != EXIT_SUCCESS) {
+            CF_ERR("cz[%lld] = %g is outside the comoving-distance table", (long long)i, wval(cz, i, es));
+            return EXIT_FAILURE;
+        }
+        if (D > *dmax) *dmax = D;
+        const double r = wval(ra, i, es), d = wval(dec, i, es);
+        X[i] = D * cos(d * CF_PI_OVER_180) * cos(r * CF_PI_OVER_180);
+        Y[i] = D * cos(d * CF_PI_OVER_180) * sin(r * CF_PI_OVER_180);
+        Z[i] = D * sin(d * CF_PI_OVER_180);
+    }
+    return EXIT_SUCCESS;
+}
+
+/* mocks/vpf_mocks/countspheres_mocks.c + countspheres_mocks_impl.c.src:208-638 */
+int countspheres_mocks(const int64_t Ngal, void *xgal, void *ygal, void *zgal, const int64_t Nran, void *xran,
+                       void *yran, void *zran, const int threshold_neighbors, const double rmax, const int nbin,
+                       const int nc, const int num_pN, const char *centers_file, const int cosmology,
+                       results_countspheres_mocks *results, struct config_options *options,
+                       struct extra_options *extra)
+{
+    (void)extra;
+    const double t0 = wall_now();
+    if (check_options(options, __func__) != EXIT_SUCCESS || results == NULL) return EXIT_FAILURE;
+    if (!(rmax > 0.0)) { CF_ERR("rmax=%lf has to be positive", rmax); return EXIT_FAILURE; }
+    if (nbin < 1) { CF_ERR("Number of bins=%d has to be at least 1", nbin); return EXIT_FAILURE; }
+    if (nc < 1) { CF_ERR("Number of spheres=%d has to be at least 1", nc); return EXIT_FAILURE; }
+    if (num_pN < 1) { CF_ERR("Number of pN's=%d requested must be at least 1", num_pN); return EXIT_FAILURE; }
+    double omega_m;
+    if (cosmology_omega_m(cosmology, &omega_m) != EXIT_SUCCESS) return EXIT_FAILURE;
+    options->periodic = 0;
+    const size_t es = options->float_type;
+    /* centres: the file when it holds at least nc centres for spheres of at least rmax, else
+     * randoms with more than threshold_neighbors randoms within rmax (then written to the file) */
+    int need_randoms = 0;
+    int64_t num_in_file = 0;
+    FILE *fpcen = centers_file ? fopen(centers_file, "r") : NULL;
+    if (fpcen != NULL) {
+        double rr = 0.0;
+        if (fscanf(fpcen, "%*f %*f %*f %lf", &rr) != 1) {
+            CF_ERR("Could not read max. sphere radius from the centers file");
+            fclose(fpcen);
+            return EXIT_FAILURE;
+        }
+        num_in_file = cf_getnumlines(centers_file, '#');
+        if (rr >= rmax && num_in_file >= nc) {
+            rewind(fpcen);
+        } else {
+            fclose(fpcen);
+            fpcen = NULL;
+            num_in_file = 0;
+            need_randoms = 1;
+        }
+    } else {
+        need_randoms = 1;
+    }
+    if (need_randoms) {
+        fpcen = centers_file ? fopen(centers_file, "w") : NULL;
+        if (fpcen == NULL) {
+            CF_ERR("could not open the centers file `%s' for writing", centers_file ? centers_file : "(null)");
+            return EXIT_FAILURE;
+        }
+    }
+    double *zc = NULL, *dcs = NULL;
+    int nz = 0, rc = EXIT_SUCCESS;
+    if (!options->is_comoving_dist) {
+        double czmax = 0.0;
+        for (int64_t i = 0; i < Ngal; i++) if (wval(zgal, i, es) > czmax) czmax = wval(zgal, i, es);
+        if (need_randoms)
+            for (int64_t i = 0; i < Nran; i++) if (wval(zran, i, es) > czmax) czmax = wval(zran, i, es);
+        const double zmax = czmax * (1.0 / CF_SPEED_OF_LIGHT) + 0.01;
+        zc = calloc(10000, sizeof(double));
+        dcs = calloc(10000, sizeof(double));
+        if (!zc || !dcs) rc = EXIT_FAILURE;
+        if (rc == EXIT_SUCCESS) nz = comoving_table(zmax, 10000, omega_m, zc, dcs);
+        if (rc == EXIT_SUCCESS && nz < 2) rc = EXIT_FAILURE;
+    }
+    const int64_t nr = need_randoms ? Nran : 0;
+    double *G = malloc(sizeof(double) * 3 * (size_t)(Ngal > 0 ? Ngal : 1));
+    double *R = malloc(sizeof(double) * 3 * (size_t)(nr > 0 ? nr : 1));
+    if (!G || !R) rc = EXIT_FAILURE;
+    double rcube = 0.0;
+    if (rc == EXIT_SUCCESS)
+        rc = vpf_mock_positions(Ngal, xgal, ygal, zgal, es, zc, dcs, nz, G, G + Ngal, G + 2 * Ngal, &rcube);
+    if (rc == EXIT_SUCCESS && nr > 0)
+        rc = vpf_mock_positions(nr, xran, yran, zran, es, zc, dcs, nz, R, R + nr, R + 2 * nr, &rcube);
+    free(zc);
+    free(dcs);
+    rcube = rcube + 1.;
+    for (int64_t i = 0; rc == EXIT_SUCCESS && i < 3 * Ngal; i++) G[i] += rcube;
+    for (int64_t i = 0; rc == EXIT_SUCCESS && i < 3 * nr; i++) R[i] += rcube;
+    rcube = 2.0 * rcube;
+    const double inv_rcube = 1.0 / rcube;
+    refine_check(options);
+    cf_vpf_job J;
+    memset(&J, 0, sizeof(J));
+    for (int a = 0; rc == EXIT_SUCCESS && a < 3; a++) {
+        double binsize;
+        rc = cf_ref_binsize(rcube, 0.0, rmax, options->bin_refine_factors[a], options->max_cells_per_dim, &binsize,
+                            &J.nmesh[a]);
+        J.lat_min[a] = 0.0;
+        J.lat_inv[a] = binsize > 0 ? 1.0 / binsize : 0.0;
+        J.refine[a] = options->bin_refine_factors[a];
+    }
+    J.periodic = 0;
+    J.rmax = rmax;
+    J.nbin = nbin;
+    J.num_pN = num_pN;
+    /* candidate centres and their cells */
+    const int64_t maxc = need_randoms ? nr : (Nran < nc ? Nran : nc);
+    double *cen = malloc(sizeof(double) * 3 * (size_t)(maxc > 0 ? maxc : 1));
+    int *cell = malloc(sizeof(int) * 3 * (size_t)(maxc > 0 ? maxc : 1));
+    uint32_t *ngb = need_randoms ? malloc(sizeof(uint32_t) * (size_t)(maxc > 0 ? maxc : 1)) : NULL;
+    if (!cen || !cell || (need_randoms && !ngb)) rc = EXIT_FAILURE;
+    int64_t ncand = 0;
+    for (int64_t t = 0; rc == EXIT_SUCCESS && t < maxc; t++) {
+        double c[3];
+        if (need_randoms) {
+            c[0] = R[t];
+            c[1] = R[nr + t];
+            c[2] = R[2 * nr + t];
+        } else {
+            char buf[10000];
+            double rr = 0.0;
+            if (fgets(buf, sizeof buf, fpcen) == NULL) {
+                CF_ERR("Could not read-in co-ordinates for the centers of the randoms spheres from file %s", centers_file);
+                rc = EXIT_FAILURE;
+                break;
+            }
+            if (sscanf(buf, "%lf %lf %lf %lf", &c[0], &c[1], &c[2], &rr) != 4) {
+                CF_ERR("Read the centers from the centers file (3 positions and 1 radius)");
+                rc = EXIT_FAILURE;
+                break;
+            }
+            if (!(rr >= rmax)) {
+                CF_ERR("Rmax from the center file is >= rmax");
+                rc = EXIT_FAILURE;
+                break;
+            }
+        }
+        for (int a = 0; a < 3; a++) {
+            int k = (int)(J.nmesh[a] * (c[a] - 0.0) * inv_rcube);
+            if (k > J.nmesh[a] - 1) k--;
+            if (k < 0 || k >= J.nmesh[a]) {
+                fprintf(stderr, "Error in countspheres_mocks> Positions are outside grid. (X,Y,Z) = (%lf,%lf,%lf) should have "
+                        "been within the range [0.0, %lf]\n", c[0], c[1], c[2], 1.0 / inv_rcube);
+                rc = EXIT_FAILURE;
+            }
+            cen[3 * t + a] = c[a];
+            cell[3 * t + a] = k;
+        }
+        ncand++;
+    }
+    /* neighbour counts of the random candidates, then the first nc with more than the threshold */
+    int64_t nacc = ncand;
+    if (rc == EXIT_SUCCESS && need_randoms) {
+        cf_vpf_job K = J;
+        K.np = nr;
+        K.x = R; K.y = R + nr; K.z = R + 2 * nr;
+        K.ncen = ncand;
+        K.cen = cen;
+        K.cen_cell = cell;
+        K.nbin = 1;
+        K.num_pN = 1;
+        K.counts_out = ngb;
+        uint64_t dummy = 0;
+        rc = cf_engine_vpf(&K, &dummy);
+        nacc = 0;
+        for (int64_t t = 0; rc == EXIT_SUCCESS && t < ncand && nacc < nc; t++) {
+            if ((int64_t)ngb[t] > threshold_neighbors) {
+                for (int a = 0; a < 3; a++) {
+                    cen[3 * nacc + a] = cen[3 * t + a];
+                    cell[3 * nacc + a] = cell[3 * t + a];
+                }
+                fprintf(fpcen, "%lf \t %lf \t %lf \t %lf\n", cen[3 * nacc], cen[3 * nacc + 1], cen[3 * nacc + 2], rmax);
+                nacc++;
+            }
+        }
+    }
+    if (fpcen) fclose(fpcen);
+    uint64_t *cnt = calloc((size_t)nbin * num_pN, sizeof(uint64_t));
+    if (rc == EXIT_SUCCESS && cnt == NULL) rc = EXIT_FAILURE;
+    if (rc == EXIT_SUCCESS && nacc <= 0) {
+        CF_ERR("Could not place even a single sphere within the volume. Please reduce the radius of the sphere "
+               "(currently set to %lf)", rmax);
+        rc = EXIT_FAILURE;
+    }
+    if (rc == EXIT_SUCCESS) {
+        if (nacc < nc)
+            fprintf(stderr, "WARNING: Could only place `%lld' out of requested `%d' spheres. Increase the random-sample "
+                    "size might improve the situation\n", (long long)nacc, nc);
+        J.np = Ngal;
+        J.x = G; J.y = G + Ngal; J.z = G + 2 * Ngal;
+        J.ncen = nacc;
+        J.cen = cen;
+        J.cen_cell = cell;
+        rc = cf_engine_vpf(&J, cnt);
+    }
+    if (rc == EXIT_SUCCESS) {
+        results->rmax = rmax;
+        results->nbin = nbin;
+        results->nc = nc;
+        results->num_pN = num_pN;
+        results->pN = pn_matrix(nbin, num_pN);
+        if (results->pN == NULL) rc = EXIT_FAILURE;
+        const double inv_nc = 1.0 / (double)nacc;
+        for (int i = 0; rc == EXIT_SUCCESS && i < num_pN; i++)
+            for (int b = 0; b < nbin; b++) results->pN[b][i] = (double)cnt[(size_t)b * num_pN + i] * inv_nc;
+    }
+    free(G);
+    free(R);
+    free(cen);
+    free(cell);
+    free(ngb);
+    free(cnt);
+    if (rc != EXIT_SUCCESS) return EXIT_FAILURE;
+    reset_bin_refine_factors(options);
+    if (options->c_api_timer) options->c_api_time = wall_now() - t0;
+    return EXIT_SUCCESS;
+}
+
+void free_results_countspheres_mocks(results_countspheres_mocks *results)
+{
+    if (results == NULL) return;
+    pn_free(results->pN, results->nbin);
+    results->pN = NULL;
+    results->rmax = 0.0;
+    results->nbin = 0;
+    results->nc = 0;
+    results->num_pN = 0;
+}
+
 int cf_gpu_set_precision(int mode) { return cf_engine_set_precision(mode); }
 
 int cf_gpu_get_precision(void) { return cf_engine_get_precision(); }

@@ -202,3 +202,40 @@ void cf_formula_for_isa(int isa, int *fma_formula, int *chord_formula)
     *fma_formula = eff == 9 ? 1 : 0;
     *chord_formula = (eff >= 6 && eff <= 9) ? 1 : 0;
 }
+
+int64_t cf_getnumlines(const char *fname, char comment) { return count_data_lines(fname, comment); }
+
+int cf_ref_binsize(double xdiff, double xwrap, double rmax, int refine, int max_cells, double *binsize, int *nmesh)
+{
+    return ref_binsize(xdiff, xwrap, rmax, refine, max_cells, binsize, nmesh);
+}
+
+/* MT19937: state recurrence with the twist constants 0x9908b0df, tempering shifts 11, 7 / 0x9d2c5680,
+ * 15 / 0xefc60000, 18, and the seeding x_i = 1812433253 (x_{i-1} ^ (x_{i-1} >> 30)) + i of the
+ * published 2002 reference implementation. */
+void cf_mt_seed(cf_mt19937 *g, unsigned long seed)
+{
+    if (seed == 0) seed = 4357;
+    g->mt[0] = (uint32_t)(seed & 0xffffffffUL);
+    for (int i = 1; i < 624; i++) g->mt[i] = 1812433253u * (g->mt[i - 1] ^ (g->mt[i - 1] >> 30)) + (uint32_t)i;
+    g->mti = 624;
+}
+
+uint32_t cf_mt_next(cf_mt19937 *g)
+{
+    if (g->mti >= 624) {
+        for (int k = 0; k < 624; k++) {
+            const uint32_t y = (g->mt[k] & 0x80000000u) | (g->mt[(k + 1) % 624] & 0x7fffffffu);
+            g->mt[k] = g->mt[(k + 397) % 624] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+        }
+        g->mti = 0;
+    }
+    uint32_t y = g->mt[g->mti++];
+    y ^= y >> 11;
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    y ^= y >> 18;
+    return y;
+}
+
+double cf_mt_uniform(cf_mt19937 *g) { return cf_mt_next(g) / 4294967296.0; }

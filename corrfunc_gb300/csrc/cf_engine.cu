@@ -2705,12 +2705,282 @@ static int batch_run_locked(BatchPlan *P, cf_hist *H)
     return EXIT_SUCCESS;
 }
 
+// ------------------------------------------------------------------------------------
+// counts in spheres (vpf): the points are sorted by their cell of the reference lattice; one
+// warp per sphere centre walks the same neighbour cells as the reference
+// (theory/vpf/countspheres_impl.c.src:332-415, mocks/vpf_mocks/countspheres_mocks_impl.c.src:
+// 520-548), with the same periodic shifts of the centre, and bins the FP64 distances into
+// shells exactly as the fallback kernels do (theory/vpf/vpf_kernels.c.src:281-302,
+// mocks/vpf_mocks/vpf_mocks_kernels.c.src:294-332).
+// ------------------------------------------------------------------------------------
+struct VpfLattice {
+    int n[3];
+    double lo[3], inv[3];
+};
+
+__global__ void k_vpf_cells(const double *x, const double *y, const double *z, int64_t np, VpfLattice L,
+                            uint32_t *cellid, uint32_t *count, unsigned long long *oob)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np; i += (int64_t)gridDim.x * blockDim.x) {
+        const double v[3] = {x[i], y[i], z[i]};
+        int c[3];
+        bool bad = false;
+        for (int a = 0; a < 3; a++) {
+            const double t = __dmul_rn(__dsub_rn(v[a], L.lo[a]), L.inv[a]);
+            int k = (t > -2.0e9 && t < 2.0e9) ? __double2int_rz(t) : -1;
+            if (k > L.n[a] - 1) k--;
+            if (k < 0 || k >= L.n[a]) {
+                bad = true;
+                k = 0;
+            }
+            c[a] = k;
+        }
+        if (bad) atomicAdd(oob, 1ull);
+        const uint32_t cell = ((uint32_t)c[0] * (uint32_t)L.n[1] + (uint32_t)c[1]) * (uint32_t)L.n[2] + (uint32_t)c[2];
+        cellid[i] = cell;
+        atomicAdd(&count[cell], 1u);
+    }
+}
+
+__global__ void k_vpf_scatter(const double *x, const double *y, const double *z, int64_t np, const uint32_t *cellid,
+                              const uint32_t *cell_start, uint32_t *fill, double4_32a *pts)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t c = cellid[i];
+        const uint32_t pos = cell_start[c] + atomicAdd(&fill[c], 1u);
+        pts[pos] = make_double4_32a(x[i], y[i], z[i], 0.0);
+    }
+}
+
+struct VpfArgs {
+    const double4_32a *pts;
+    const uint32_t *cell_start;
+    const double *cen;
+    const int *cen_cell;
+    int64_t ncen;
+    int n[3];
+    int refine[3];
+    int periodic;
+    double wrap[3];
+    double rmax_sqr, inv_rstep;
+    int nbin, num_pN;
+    unsigned long long *pN;
+    uint32_t *within;  // per-centre neighbour counts (r^2 < rmax^2) instead of pN, or null
+};
+
+// neighbour cell index and centre shift along one axis; false when a non-periodic lattice has no
+// such cell
+__device__ __forceinline__ bool vpf_axis(const VpfArgs &A, int a, int c, int d, int *cell, double *off)
+{
+    int k = c + d;
+    *off = 0.0;
+    if (A.periodic) {
+        if (k >= A.n[a]) *off = -A.wrap[a];
+        else if (k < 0) *off = A.wrap[a];
+        k %= A.n[a];
+        if (k < 0) k += A.n[a];
+    } else if (k < 0 || k >= A.n[a]) {
+        return false;
+    }
+    *cell = k;
+    return true;
+}
+
+__global__ void __launch_bounds__(256) k_vpf(VpfArgs A)
+{
+    extern __shared__ uint32_t s_shell[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t *cnt = s_shell + (size_t)warp * A.nbin;
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t c = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp; c < A.ncen; c += nw) {
+        for (int b = lane; b < A.nbin; b += 32) cnt[b] = 0;
+        __syncwarp();
+        const double xc = A.cen[3 * c], yc = A.cen[3 * c + 1], zc = A.cen[3 * c + 2];
+        const int ix = A.cen_cell[3 * c], iy = A.cen_cell[3 * c + 1], iz = A.cen_cell[3 * c + 2];
+        for (int dx = -A.refine[0]; dx <= A.refine[0]; dx++) {
+            int cx;
+            double ox;
+            if (!vpf_axis(A, 0, ix, dx, &cx, &ox)) continue;
+            const double px = __dadd_rn(xc, ox);
+            for (int dy = -A.refine[1]; dy <= A.refine[1]; dy++) {
+                int cy;
+                double oy;
+                if (!vpf_axis(A, 1, iy, dy, &cy, &oy)) continue;
+                const double py = __dadd_rn(yc, oy);
+                for (int dz = -A.refine[2]; dz <= A.refine[2]; dz++) {
+                    int cz;
+                    double oz;
+                    if (!vpf_axis(A, 2, iz, dz, &cz, &oz)) continue;
+                    const double pz = __dadd_rn(zc, oz);
+                    const uint32_t cell = ((uint32_t)cx * (uint32_t)A.n[1] + (uint32_t)cy) * (uint32_t)A.n[2] + (uint32_t)cz;
+                    const uint32_t j1 = A.cell_start[cell + 1];
+                    for (uint32_t j = A.cell_start[cell] + lane; j < j1; j += 32) {
+                        const double4_32a p = A.pts[j];
+                        const double ddx = __dsub_rn(p.x, px), ddy = __dsub_rn(p.y, py), ddz = __dsub_rn(p.z, pz);
+                        const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)), __dmul_rn(ddz, ddz));
+                        if (r2 >= A.rmax_sqr) continue;
+                        if (A.within) {
+                            atomicAdd(&cnt[0], 1u);
+                            continue;
+                        }
+                        const int ib = __double2int_rz(__dmul_rn(__dsqrt_rn(r2), A.inv_rstep));
+                        if (ib < A.nbin) atomicAdd(&cnt[ib], 1u);
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        if (A.within) {
+            if (lane == 0) A.within[c] = cnt[0];
+        } else if (lane == 0) {
+            uint32_t cum = 0;
+            for (int b = 0; b < A.nbin; b++) {
+                cum += cnt[b];
+                if (cum < (uint32_t)A.num_pN) atomicAdd(&A.pN[(size_t)b * A.num_pN + cum], 1ull);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+struct VpfBufs {
+    DevBuf xyz, cellid, count, fill, cell_start, pts, cen, cen_cell, pN, oob, within;
+    HostBuf h_out;
+};
+static VpfBufs g_vpf;
+
+static int vpf_locked(const cf_vpf_job *J, uint64_t *pN)
+{
+    if (engine_init() != EXIT_SUCCESS) return EXIT_FAILURE;
+    cudaStream_t st = g_eng.stream;
+    g_eng.launches = 0;
+    memset(&g_eng.last, 0, sizeof(g_eng.last));
+    const size_t npn = (size_t)J->nbin * J->num_pN;
+    memset(pN, 0, sizeof(uint64_t) * npn);
+    if (J->nbin < 1 || J->num_pN < 1 || J->nbin > 4096) CF_FAIL("vpf: 1 <= nbin <= 4096 and num_pN >= 1 are supported");
+    if (J->np < 0 || J->np >= (1ll << 31) || J->ncen < 0) CF_FAIL("vpf: unsupported sizes");
+    double ncells_d = 1.0;
+    for (int a = 0; a < 3; a++) {
+        if (J->nmesh[a] < 1) CF_FAIL("vpf: empty lattice");
+        ncells_d *= J->nmesh[a];
+    }
+    if (ncells_d > (double)(1u << 30)) CF_FAIL("vpf: lattice of %.0f cells is too large", ncells_d);
+    const uint32_t ncells = (uint32_t)ncells_d;
+    const int64_t np = J->np;
+    VpfBufs &B = g_vpf;
+    if (ensure(B.xyz, sizeof(double) * 3 * (size_t)(np > 0 ? np : 1)) || ensure(B.cellid, sizeof(uint32_t) * (size_t)(np > 0 ? np : 1)) ||
+        ensure(B.count, sizeof(uint32_t) * ncells) || ensure(B.fill, sizeof(uint32_t) * ncells) ||
+        ensure(B.cell_start, sizeof(uint32_t) * ((size_t)ncells + 1)) ||
+        ensure(B.pts, sizeof(double4_32a) * (size_t)(np > 0 ? np : 1)) ||
+        ensure(B.cen, sizeof(double) * 3 * (size_t)(J->ncen > 0 ? J->ncen : 1)) ||
+        ensure(B.cen_cell, sizeof(int) * 3 * (size_t)(J->ncen > 0 ? J->ncen : 1)) ||
+        ensure(B.pN, sizeof(unsigned long long) * npn) || ensure(B.oob, sizeof(unsigned long long)) ||
+        ensure(B.within, sizeof(uint32_t) * (size_t)(J->ncen > 0 ? J->ncen : 1)) ||
+        ensure_host(B.h_out, sizeof(unsigned long long) * (npn + 1)))
+        return EXIT_FAILURE;
+    CF_CUDA(cudaEventRecord(g_eng.ev[0], st));
+    double *dx = (double *)B.xyz.p, *dy = dx + np, *dz = dy + np;
+    if (np > 0) {
+        CF_CUDA(cudaMemcpyAsync(dx, J->x, sizeof(double) * np, cudaMemcpyHostToDevice, st));
+        CF_CUDA(cudaMemcpyAsync(dy, J->y, sizeof(double) * np, cudaMemcpyHostToDevice, st));
+        CF_CUDA(cudaMemcpyAsync(dz, J->z, sizeof(double) * np, cudaMemcpyHostToDevice, st));
+    }
+    if (J->ncen > 0) {
+        CF_CUDA(cudaMemcpyAsync(B.cen.p, J->cen, sizeof(double) * 3 * J->ncen, cudaMemcpyHostToDevice, st));
+        CF_CUDA(cudaMemcpyAsync(B.cen_cell.p, J->cen_cell, sizeof(int) * 3 * J->ncen, cudaMemcpyHostToDevice, st));
+    }
+    CF_CUDA(cudaMemsetAsync(B.count.p, 0, sizeof(uint32_t) * ncells, st));
+    CF_CUDA(cudaMemsetAsync(B.fill.p, 0, sizeof(uint32_t) * ncells, st));
+    CF_CUDA(cudaMemsetAsync(B.pN.p, 0, sizeof(unsigned long long) * npn, st));
+    CF_CUDA(cudaMemsetAsync(B.oob.p, 0, sizeof(unsigned long long), st));
+    VpfLattice L;
+    for (int a = 0; a < 3; a++) {
+        L.n[a] = J->nmesh[a];
+        L.lo[a] = J->lat_min[a];
+        L.inv[a] = J->lat_inv[a];
+    }
+    if (np > 0) {
+        const int grid = grid_for(np, 256);
+        k_vpf_cells<<<grid, 256, 0, st>>>(dx, dy, dz, np, L, (uint32_t *)B.cellid.p, (uint32_t *)B.count.p,
+                                          (unsigned long long *)B.oob.p);
+        CF_CUDA(cudaGetLastError());
+        g_eng.launches++;
+    }
+    if (scan_u32(g_eng.ws, (const uint32_t *)B.count.p, (uint32_t *)B.cell_start.p, ncells, 0) != EXIT_SUCCESS)
+        return EXIT_FAILURE;
+    if (np > 0) {
+        k_vpf_scatter<<<grid_for(np, 256), 256, 0, st>>>(dx, dy, dz, np, (const uint32_t *)B.cellid.p,
+                                                          (const uint32_t *)B.cell_start.p, (uint32_t *)B.fill.p,
+                                                          (double4_32a *)B.pts.p);
+        CF_CUDA(cudaGetLastError());
+        g_eng.launches++;
+    }
+    CF_CUDA(cudaEventRecord(g_eng.ev[1], st));
+    VpfArgs A;
+    A.pts = (const double4_32a *)B.pts.p;
+    A.cell_start = (const uint32_t *)B.cell_start.p;
+    A.cen = (const double *)B.cen.p;
+    A.cen_cell = (const int *)B.cen_cell.p;
+    A.ncen = J->ncen;
+    for (int a = 0; a < 3; a++) {
+        A.n[a] = J->nmesh[a];
+        A.refine[a] = J->refine[a];
+        A.wrap[a] = J->wrap[a];
+    }
+    A.periodic = J->periodic;
+    A.rmax_sqr = J->rmax * J->rmax;
+    A.inv_rstep = 1.0 / (J->rmax / (double)J->nbin);
+    A.nbin = J->nbin;
+    A.num_pN = J->num_pN;
+    A.pN = (unsigned long long *)B.pN.p;
+    A.within = J->counts_out ? (uint32_t *)B.within.p : nullptr;
+    CF_CUDA(cudaEventRecord(g_eng.ev[2], st));
+    if (J->ncen > 0) {
+        const size_t smem = sizeof(uint32_t) * 8 * (size_t)J->nbin;
+        CF_CUDA(cudaFuncSetAttribute(k_vpf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int64_t blocks = (J->ncen + 7) / 8;
+        const int64_t cap = (int64_t)g_eng.num_sms * 8;
+        if (blocks > cap) blocks = cap;
+        k_vpf<<<(int)blocks, 256, smem, st>>>(A);
+        CF_CUDA(cudaGetLastError());
+        g_eng.launches++;
+    }
+    CF_CUDA(cudaEventRecord(g_eng.ev[3], st));
+    unsigned long long *h = (unsigned long long *)B.h_out.p;
+    CF_CUDA(cudaMemcpyAsync(h, B.pN.p, sizeof(unsigned long long) * npn, cudaMemcpyDeviceToHost, st));
+    CF_CUDA(cudaMemcpyAsync(h + npn, B.oob.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    if (J->counts_out && J->ncen > 0)
+        CF_CUDA(cudaMemcpyAsync(J->counts_out, B.within.p, sizeof(uint32_t) * J->ncen, cudaMemcpyDeviceToHost, st));
+    CF_CUDA(cudaEventRecord(g_eng.ev[4], st));
+    CF_CUDA(cudaStreamSynchronize(st));
+    if (h[npn] > 0) CF_FAIL("%llu particles are out of bounds. Check periodic wrapping?", h[npn]);
+    for (size_t k = 0; k < npn; k++) pN[k] = h[k];
+    float ms_pairs = 0.f, ms_grid = 0.f, ms_total = 0.f;
+    CF_CUDA(cudaEventElapsedTime(&ms_pairs, g_eng.ev[2], g_eng.ev[3]));
+    CF_CUDA(cudaEventElapsedTime(&ms_grid, g_eng.ev[0], g_eng.ev[1]));
+    CF_CUDA(cudaEventElapsedTime(&ms_total, g_eng.ev[0], g_eng.ev[4]));
+    g_eng.last.pair_kernel_ms = ms_pairs;
+    g_eng.last.gridlink_ms = ms_grid;
+    g_eng.last.total_gpu_ms = ms_total;
+    g_eng.last.num_cells = (int)ncells;
+    g_eng.last.kernel_launches = g_eng.launches;
+    return EXIT_SUCCESS;
+}
+
 }  // namespace
 
 extern "C" int cf_engine_run(cf_job *job, cf_hist *out)
 {
     pthread_mutex_lock(&g_lock);
     const int rc = run_locked(job, out);
+    pthread_mutex_unlock(&g_lock);
+    return rc;
+}
+
+extern "C" int cf_engine_vpf(const cf_vpf_job *job, uint64_t *pN)
+{
+    pthread_mutex_lock(&g_lock);
+    const int rc = vpf_locked(job, pN);
     pthread_mutex_unlock(&g_lock);
     return rc;
 }

@@ -114,6 +114,33 @@ int cf_engine_batch_plan(const cf_job *tmpl, int nbatch, const int64_t *n1, cons
                          cf_batch **out);
 int cf_engine_batch_run(cf_batch *plan, cf_hist *out);
 void cf_engine_batch_free(cf_batch *plan);
+/* Counts in spheres (vpf).  Points (double, host) are binned into the reference lattice
+ * (cell = (int)((x - lat_min) * lat_inv), clamped down at the top, as gridlink assigns them);
+ * every centre walks the neighbour cells c + d, |d_a| <= refine[a], of its given cell: periodic
+ * lattices wrap the index and shift the centre by -/+ wrap, others skip cells outside.  Shell
+ * counts of (int)(sqrt(r^2) / rstep) for r^2 < rmax^2, cumulated over shells, fill
+ * pN[bin * num_pN + N] (counts of centres with exactly N points within (bin + 1) * rstep). */
+typedef struct {
+    int64_t np;
+    const double *x, *y, *z;
+    int nmesh[3];
+    double lat_min[3];
+    double lat_inv[3];
+    int refine[3];
+    int periodic;
+    double wrap[3];
+    int64_t ncen;
+    const double *cen;    /* 3 * ncen: x, y, z */
+    const int *cen_cell;  /* 3 * ncen: cell index per axis */
+    double rmax;
+    int nbin;
+    int num_pN;
+    /* when set: instead of pN, the number of points with r^2 < rmax^2 around every centre
+     * (the neighbour count of count_neighbors, mocks/vpf_mocks/countspheres_mocks_impl.c.src:140-206) */
+    uint32_t *counts_out;
+} cf_vpf_job;
+int cf_engine_vpf(const cf_vpf_job *J, uint64_t *pN);
+
 int cf_engine_set_precision(int mode);
 int cf_engine_get_precision(void);
 

@@ -666,6 +666,128 @@ static PyObject *py_countpairs_s_mu_mocks(PyObject *self, PyObject *args, PyObje
     return mocks_2d(args, kwargs, 1);
 }
 
+/* rows [rmax_k, pN[k][0], ..., pN[k][num_pN-1]] with rmax_k = (k + 1) * rmax / nbin
+ * (theory/python_bindings/_countpairs.c:2674-2690) */
+static PyObject *vpf_list(double **pN, double rmax, int nbin, int num_pN)
+{
+    PyObject *ret = PyList_New(0);
+    const double rstep = rmax / (double)nbin;
+    for (int b = 0; ret && b < nbin; b++) {
+        PyObject *item = PyList_New(0);
+        PyObject *v = Py_BuildValue("d", (b + 1) * rstep);
+        PyList_Append(item, v);
+        Py_XDECREF(v);
+        for (int i = 0; i < num_pN; i++) {
+            v = Py_BuildValue("d", pN[b][i]);
+            PyList_Append(item, v);
+            Py_XDECREF(v);
+        }
+        PyList_Append(ret, item);
+        Py_XDECREF(item);
+    }
+    return ret;
+}
+
+/* countspheres_vpf: kwlist and format of theory/python_bindings/_countpairs.c:2552-2586 */
+static PyObject *py_countspheres_vpf(PyObject *self, PyObject *args, PyObject *kwargs)
+{
+    (void)self;
+    static char *kw[] = {"rmax", "nbins", "nspheres", "num_pN", "seed", "X", "Y", "Z", "periodic", "verbose",
+                         "boxsize", "xbin_refine_factor", "ybin_refine_factor", "zbin_refine_factor",
+                         "max_cells_per_dim", "copy_particles", "c_api_timer", "isa", NULL};
+    double rmax;
+    int nbin, nc, num_pN;
+    unsigned long seed = (unsigned long)-1;
+    cf_pyset s1 = {{0}}, s2 = {{0}};
+    struct config_options o = get_config_options();
+    o.verbose = 0;
+    o.periodic = 1;
+    o.instruction_set = -1;
+    o.copy_particles = 1;
+    o.c_api_timer = 0;
+    for (int k = 0; k < 3; k++) o.bin_refine_factors[k] = 1;
+    int8_t rx = 1, ry = 1, rz = 1;
+    if (!PyArg_ParseTupleAndKeywords(args, kwargs, "diiikO!O!O!|bb(ddd)bbbhbbi", kw, &rmax, &nbin, &nc, &num_pN, &seed,
+                                     &PyArray_Type, &s1.in[0], &PyArray_Type, &s1.in[1], &PyArray_Type, &s1.in[2],
+                                     &o.periodic, &o.verbose, &o.boxsize_x, &o.boxsize_y, &o.boxsize_z, &rx, &ry, &rz,
+                                     &o.max_cells_per_dim, &o.copy_particles, &o.c_api_timer, &o.instruction_set)) {
+        PyErr_Clear();
+        return fail("countspheres_vpf", "ArgumentError: could not parse the arguments");
+    }
+    refine_options(&o, rx, ry, rz);
+    struct extra_options extra;
+    int elem = 8;
+    if (prepare_sets("countspheres_vpf", 1, 3, &s1, &s2, NULL, &extra, &elem) != 0) {
+        set_release(&s1);
+        Py_RETURN_NONE;
+    }
+    o.float_type = (uint8_t)elem;
+    results_countspheres r;
+    int rc;
+    Py_BEGIN_ALLOW_THREADS
+    rc = countspheres(s1.n, set_data(&s1, 0), set_data(&s1, 1), set_data(&s1, 2), rmax, nbin, nc, num_pN, seed, &r, &o,
+                      &extra);
+    Py_END_ALLOW_THREADS
+    set_release(&s1);
+    if (rc != EXIT_SUCCESS) Py_RETURN_NONE;
+    PyObject *list = vpf_list(r.pN, rmax, r.nbin, num_pN);
+    free_results_countspheres(&r);
+    return with_time(list, &o);
+}
+
+/* countspheres_vpf_mocks: kwlist and format of mocks/python_bindings/_countpairs_mocks.c:2067-2108 */
+static PyObject *py_countspheres_vpf_mocks(PyObject *self, PyObject *args, PyObject *kwargs)
+{
+    (void)self;
+    static char *kw[] = {"rmax", "nbins", "numSpheres", "numpN", "threshold", "centers_file", "cosmology", "X1", "Y1",
+                         "Z1", "X2", "Y2", "Z2", "is_comoving_dist", "verbose", "xbin_refine_factor",
+                         "ybin_refine_factor", "zbin_refine_factor", "max_cells_per_dim", "copy_particles",
+                         "c_api_timer", "isa", NULL};
+    double rmax;
+    int nbin, nc, num_pN, threshold, cosmology = 1;
+    char *centers_file = NULL;
+    cf_pyset s1 = {{0}}, s2 = {{0}};
+    struct config_options o = get_config_options();
+    o.is_comoving_dist = 0;
+    o.verbose = 0;
+    o.instruction_set = -1;
+    o.copy_particles = 1;
+    o.c_api_timer = 0;
+    for (int k = 0; k < 3; k++) o.bin_refine_factors[k] = 1;
+    int8_t rx = 1, ry = 1, rz = 1;
+    if (!PyArg_ParseTupleAndKeywords(args, kwargs, "diiiisiO!O!O!O!O!O!|bbbbbhbbi", kw, &rmax, &nbin, &nc, &num_pN,
+                                     &threshold, &centers_file, &cosmology, &PyArray_Type, &s1.in[0], &PyArray_Type,
+                                     &s1.in[1], &PyArray_Type, &s1.in[2], &PyArray_Type, &s2.in[0], &PyArray_Type,
+                                     &s2.in[1], &PyArray_Type, &s2.in[2], &o.is_comoving_dist, &o.verbose, &rx, &ry,
+                                     &rz, &o.max_cells_per_dim, &o.copy_particles, &o.c_api_timer,
+                                     &o.instruction_set)) {
+        PyErr_Clear();
+        return fail("countspheres_vpf_mocks", "ArgumentError: could not parse the arguments");
+    }
+    refine_options(&o, rx, ry, rz);
+    struct extra_options extra;
+    int elem = 8;
+    if (prepare_sets("countspheres_vpf_mocks", 0, 3, &s1, &s2, NULL, &extra, &elem) != 0) {
+        set_release(&s1);
+        set_release(&s2);
+        Py_RETURN_NONE;
+    }
+    o.float_type = (uint8_t)elem;
+    results_countspheres_mocks r;
+    int rc;
+    Py_BEGIN_ALLOW_THREADS
+    rc = countspheres_mocks(s1.n, set_data(&s1, 0), set_data(&s1, 1), set_data(&s1, 2), s2.n, set_data(&s2, 0),
+                            set_data(&s2, 1), set_data(&s2, 2), threshold, rmax, nbin, nc, num_pN, centers_file,
+                            cosmology, &r, &o, NULL);
+    Py_END_ALLOW_THREADS
+    set_release(&s1);
+    set_release(&s2);
+    if (rc != EXIT_SUCCESS) Py_RETURN_NONE;
+    PyObject *list = vpf_list(r.pN, rmax, r.nbin, num_pN);
+    free_results_countspheres_mocks(&r);
+    return with_time(list, &o);
+}
+
 /* ---------------- module tables ---------------- */
 
 static PyMethodDef theory_methods[] = {
@@ -679,6 +801,8 @@ static PyMethodDef theory_methods[] = {
      "Correlation function xi(r) in a periodic box (countpairs_xi)."},
     {"countpairs_s_mu", (PyCFunction)(void (*)(void))py_countpairs_s_mu, METH_VARARGS | METH_KEYWORDS,
      "Pair counts in (s, mu) (countpairs_s_mu)."},
+    {"countspheres_vpf", (PyCFunction)(void (*)(void))py_countspheres_vpf, METH_VARARGS | METH_KEYWORDS,
+     "Counts in spheres pN(r) (countspheres)."},
     {NULL, NULL, 0, NULL}};
 
 static PyMethodDef mocks_methods[] = {
@@ -688,6 +812,8 @@ static PyMethodDef mocks_methods[] = {
      "Pair counts in (rp, pi) of survey catalogues (countpairs_mocks)."},
     {"countpairs_s_mu_mocks", (PyCFunction)(void (*)(void))py_countpairs_s_mu_mocks, METH_VARARGS | METH_KEYWORDS,
      "Pair counts in (s, mu) of survey catalogues (countpairs_mocks_s_mu)."},
+    {"countspheres_vpf_mocks", (PyCFunction)(void (*)(void))py_countspheres_vpf_mocks, METH_VARARGS | METH_KEYWORDS,
+     "Counts in spheres of survey catalogues (countspheres_mocks)."},
     {NULL, NULL, 0, NULL}};
 
 static struct PyModuleDef theory_module = {PyModuleDef_HEAD_INIT, "_countpairs",

@@ -1,6 +1,7 @@
 """Python front ends for the survey-catalogue pair counters, mirroring Corrfunc.mocks:
 DDtheta_mocks (Corrfunc/mocks/DDtheta_mocks.py:19-357), DDrppi_mocks
-(Corrfunc/mocks/DDrppi_mocks.py:17-402) and DDsmu_mocks (Corrfunc/mocks/DDsmu_mocks.py:17-352)."""
+(Corrfunc/mocks/DDrppi_mocks.py:17-402), DDsmu_mocks (Corrfunc/mocks/DDsmu_mocks.py:17-352) and
+vpf_mocks (Corrfunc/mocks/vpf_mocks.py:17-285)."""
 import ctypes
 
 import numpy as np
@@ -225,3 +226,32 @@ def DDrppi_mocks(*args, **kwargs):
 def DDsmu_mocks(*args, **kwargs):
     """DD(s, mu) of survey catalogues; see Corrfunc.mocks.DDsmu_mocks."""
     return run_DDsmu_mocks(C.library(), *args, **kwargs)
+
+
+def run_vpf_mocks(lib, rmax, nbins, nspheres, numpN, threshold_ngb, centers_file, cosmology, RA, DEC, CZ, RAND_RA,
+                  RAND_DEC, RAND_CZ, verbose=False, is_comoving_dist=False, xbin_refine_factor=1, ybin_refine_factor=1,
+                  zbin_refine_factor=1, max_cells_per_dim=100, copy_particles=True, c_api_timer=False, isa="fastest"):
+    RA, DEC = _fix_ra_dec(RA, DEC)
+    RAND_RA, RAND_DEC = _fix_ra_dec(RAND_RA, RAND_DEC)
+    RA = C.as_positions(RA)
+    dt = RA.dtype
+    DEC, CZ, RAND_RA, RAND_DEC, RAND_CZ = (C.as_positions(a, dt) for a in (DEC, CZ, RAND_RA, RAND_DEC, RAND_CZ))
+    o = _mock_options(dt, 1, is_comoving_dist, verbose, False, 0,
+                      (xbin_refine_factor, ybin_refine_factor, zbin_refine_factor), max_cells_per_dim,
+                      copy_particles, True, c_api_timer, isa)
+    extra = C.get_extra_options()
+    res = C.ResultsVpf()
+    rc = lib.countspheres_mocks(len(RA), C.ptr(RA), C.ptr(DEC), C.ptr(CZ), len(RAND_RA), C.ptr(RAND_RA),
+                                C.ptr(RAND_DEC), C.ptr(RAND_CZ), int(threshold_ngb), float(rmax), int(nbins),
+                                int(nspheres), int(numpN), str(centers_file).encode(), int(cosmology),
+                                ctypes.byref(res), ctypes.byref(o), ctypes.byref(extra))
+    if rc != 0:
+        raise RuntimeError("RuntimeError occurred")
+    out = C.vpf_rows(res, int(numpN))
+    lib.free_results_countspheres_mocks(ctypes.byref(res))
+    return (out, o.c_api_time) if c_api_timer else out
+
+
+def vpf_mocks(*args, **kwargs):
+    """Counts in spheres of a survey catalogue; see Corrfunc.mocks.vpf_mocks."""
+    return run_vpf_mocks(C.library(), *args, **kwargs)

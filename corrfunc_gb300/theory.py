@@ -346,6 +346,33 @@ class DDCrossBatch:
             pass
 
 
+def run_vpf(lib, rmax, nbins, nspheres, numpN, seed, X, Y, Z, verbose=False, periodic=True, boxsize=None,
+            xbin_refine_factor=1, ybin_refine_factor=1, zbin_refine_factor=1, max_cells_per_dim=100,
+            copy_particles=True, c_api_timer=False, isa="fastest"):
+    """Counts in spheres: Corrfunc/theory/vpf.py:17-262 (countspheres)."""
+    X = C.as_positions(X)
+    dt = X.dtype
+    Y = C.as_positions(Y, dt)
+    Z = C.as_positions(Z, dt)
+    o = _common_options(1, periodic, boxsize, verbose, False, (xbin_refine_factor, ybin_refine_factor,
+                                                               zbin_refine_factor),
+                        max_cells_per_dim, copy_particles, True, c_api_timer, isa, dt)
+    extra = C.get_extra_options()
+    res = C.ResultsVpf()
+    rc = lib.countspheres(len(X), C.ptr(X), C.ptr(Y), C.ptr(Z), float(rmax), int(nbins), int(nspheres), int(numpN),
+                          int(seed) & 0xffffffffffffffff, ctypes.byref(res), ctypes.byref(o), ctypes.byref(extra))
+    if rc != 0:
+        raise RuntimeError("RuntimeError occurred")
+    out = C.vpf_rows(res, int(numpN))
+    lib.free_results_countspheres(ctypes.byref(res))
+    return (out, o.c_api_time) if c_api_timer else out
+
+
+def vpf(*args, **kwargs):
+    """Counts in spheres pN(r); see Corrfunc.theory.vpf."""
+    return run_vpf(C.library(), *args, **kwargs)
+
+
 def DD(*args, **kwargs):
     """3-D pair counts DD(r); see Corrfunc.theory.DD (Corrfunc/theory/DD.py:16)."""
     return run_DD(C.library(), *args, **kwargs)

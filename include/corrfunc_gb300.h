@@ -230,6 +230,24 @@ typedef struct {
     int nmu_bins;
 } results_countpairs_mocks_s_mu;
 
+/* theory/vpf/countspheres.h:20-26: pN[bin][N], bin = sphere radius (bin + 1) * rmax / nbin */
+typedef struct {
+    double **pN;
+    double rmax;
+    int nbin;
+    int nc;
+    int num_pN;
+} results_countspheres;
+
+/* mocks/vpf_mocks/countspheres_mocks.h:20-26 */
+typedef struct {
+    double **pN;
+    double rmax;
+    int nbin;
+    int nc;
+    int num_pN;
+} results_countspheres_mocks;
+
 /* ---------------- entry points ---------------- */
 
 /* Replaces countpairs(), theory/DD/countpairs.h:28-35 (3-D DD(r) counts). */
@@ -306,6 +324,27 @@ int countpairs_mocks_s_mu(const int64_t ND1, void *theta1, void *phi1, void *czD
                           struct config_options *options, struct extra_options *extra);
 /* Replaces free_results_mocks_s_mu(), mocks/DDsmu_mocks/countpairs_s_mu_mocks.h:42. */
 void free_results_mocks_s_mu(results_countpairs_mocks_s_mu *results);
+
+/* Replaces countspheres(), theory/vpf/countspheres.h:29-35: counts in spheres (void probability
+ * function and pN) of a 3-D point set; nc centres drawn from MT19937(seed) as the reference draws
+ * them from GSL's mt19937, counts on the GPU. */
+int countspheres(const int64_t np, void *X, void *Y, void *Z, const double rmax, const int nbin, const int nc,
+                 const int num_pN, unsigned long seed, results_countspheres *results,
+                 struct config_options *options, struct extra_options *extra);
+/* Replaces free_results_countspheres(), theory/vpf/countspheres.h:37. */
+void free_results_countspheres(results_countspheres *results);
+
+/* Replaces countspheres_mocks(), mocks/vpf_mocks/countspheres_mocks.h:28-36: counts in spheres of a
+ * survey catalogue, centres read from centers_file or drawn from the randoms (and then written to
+ * centers_file), as the reference does. */
+int countspheres_mocks(const int64_t Ngal, void *xgal, void *ygal, void *zgal,
+                       const int64_t Nran, void *xran, void *yran, void *zran,
+                       const int threshold_neighbors, const double rmax, const int nbin, const int nc,
+                       const int num_pN, const char *centers_file, const int cosmology,
+                       results_countspheres_mocks *results, struct config_options *options,
+                       struct extra_options *extra);
+/* Replaces free_results_countspheres_mocks(), mocks/vpf_mocks/countspheres_mocks.h:38. */
+void free_results_countspheres_mocks(results_countspheres_mocks *results);
 
 /* ---------------- GB300 extensions (no reference counterpart) ----------------
  * Counting precision of the GPU engine.  CF_PRECISION_FP32_REFINE (default) classifies

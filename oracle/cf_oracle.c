@@ -364,11 +364,11 @@ static int cfo_cosmo_table(double zmax, int max_size, double omega_m, double *zc
     return n;
 }
 
-/* Positions of one catalogue.  is_comoving: cz already holds the distance.  Otherwise the
+/* Positions of one catalogue (and, when dist is not NULL, the distances).  is_comoving: cz already holds the distance.  Otherwise the
  * table spans z up to zmax (max cz / c + 0.01 over the catalogues of the call).  Returns 0, or
  * -1 when a redshift falls outside the table. */
 int cfo_mock_xyz(int64_t n, const double *ra, const double *dec, const double *cz, int is_comoving, double omega_m,
-                 double zmax, double *x, double *y, double *z)
+                 double zmax, double *x, double *y, double *z, double *dist)
 {
     const double P = 0.017453292519943295769236907684886127134428718885417254560971;
     const int max_size = 10000;
@@ -393,6 +393,7 @@ int cfo_mock_xyz(int64_t n, const double *ra, const double *dec, const double *c
             }
             D = dc[lo] + (zz - zc[lo]) / (zc[lo + 1] - zc[lo]) * (dc[lo + 1] - dc[lo]);
         }
+        if (dist) dist[i] = D;
         x[i] = D * cos(dec[i] * P) * cos(ra[i] * P);
         y[i] = D * cos(dec[i] * P) * sin(ra[i] * P);
         z[i] = D * sin(dec[i] * P);
@@ -400,4 +401,123 @@ int cfo_mock_xyz(int64_t n, const double *ra, const double *dec, const double *c
     free(zc);
     free(dc);
     return rc;
+}
+
+/* ---- counts in spheres (vpf) ----
+ * MT19937 restated from its published description (Matsumoto & Nishimura 1998; 2002 seeding),
+ * seed 0 -> 4357 and uniform = output / 2^32 as GSL's mt19937 (theory/vpf/countspheres_impl.c.src:188-190,
+ * 281-283).  n uniforms into out. */
+void cfo_mt_uniforms(unsigned long seed, int64_t n, double *out)
+{
+    uint32_t mt[624];
+    if (seed == 0) seed = 4357;
+    mt[0] = (uint32_t)(seed & 0xffffffffUL);
+    for (int i = 1; i < 624; i++) mt[i] = 1812433253u * (mt[i - 1] ^ (mt[i - 1] >> 30)) + (uint32_t)i;
+    int idx = 624;
+    for (int64_t k = 0; k < n; k++) {
+        if (idx >= 624) {
+            for (int i = 0; i < 624; i++) {
+                const uint32_t y = (mt[i] & 0x80000000u) | (mt[(i + 1) % 624] & 0x7fffffffu);
+                mt[i] = mt[(i + 397) % 624] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+            }
+            idx = 0;
+        }
+        uint32_t y = mt[idx++];
+        y ^= y >> 11;
+        y ^= (y << 7) & 0x9d2c5680u;
+        y ^= (y << 15) & 0xefc60000u;
+        y ^= y >> 18;
+        out[k] = y / 4294967296.0;
+    }
+}
+
+/* Shell counts around every centre with the reference's cell walk
+ * (theory/vpf/countspheres_impl.c.src:332-415: cells c + d, |d| <= refine, wrapped with the
+ * centre shifted by -/+ wrap when periodic, skipped otherwise) and the fallback kernel's binning
+ * (theory/vpf/vpf_kernels.c.src:281-302): r2 = dx*dx + dy*dy + dz*dz, r2 < rmax^2,
+ * bin = (int)(sqrt(r2) * inv_rstep) < nbin.  Cumulative counts then fill pN[bin * num_pN + N].
+ * within != NULL: instead the number of points with r2 < rmax^2 per centre. */
+int cfo_vpf(int64_t np, const double *x, const double *y, const double *z, const int *nmesh, const double *lat_min,
+            const double *lat_inv, const int *refine, int periodic, const double *wrap, int64_t ncen,
+            const double *cen, const int *cen_cell, double rmax, int nbin, int num_pN, uint64_t *pN,
+            uint32_t *within)
+{
+    const int64_t ncells = (int64_t)nmesh[0] * nmesh[1] * nmesh[2];
+    int64_t *start = calloc((size_t)ncells + 1, sizeof(int64_t));
+    int64_t *cellof = malloc(sizeof(int64_t) * (size_t)(np > 0 ? np : 1));
+    int64_t *order = malloc(sizeof(int64_t) * (size_t)(np > 0 ? np : 1));
+    for (int64_t i = 0; i < np; i++) {
+        const double v[3] = {x[i], y[i], z[i]};
+        int c[3];
+        for (int a = 0; a < 3; a++) {
+            int k = (int)((v[a] - lat_min[a]) * lat_inv[a]);
+            if (k > nmesh[a] - 1) k--;
+            if (k < 0 || k >= nmesh[a]) { free(start); free(cellof); free(order); return -1; }
+            c[a] = k;
+        }
+        cellof[i] = ((int64_t)c[0] * nmesh[1] + c[1]) * nmesh[2] + c[2];
+        start[cellof[i] + 1]++;
+    }
+    for (int64_t c = 0; c < ncells; c++) start[c + 1] += start[c];
+    int64_t *fill = calloc((size_t)ncells, sizeof(int64_t));
+    for (int64_t i = 0; i < np; i++) order[start[cellof[i]] + fill[cellof[i]]++] = i;
+    free(fill);
+    const double rstep = rmax / (double)nbin, inv_rstep = 1.0 / rstep, rmax_sqr = rmax * rmax;
+    int *counts = malloc(sizeof(int) * (size_t)nbin);
+    if (pN) memset(pN, 0, sizeof(uint64_t) * (size_t)nbin * num_pN);
+    for (int64_t ic = 0; ic < ncen; ic++) {
+        memset(counts, 0, sizeof(int) * (size_t)nbin);
+        uint32_t nwithin = 0;
+        const int ix = cen_cell[3 * ic], iy = cen_cell[3 * ic + 1], iz = cen_cell[3 * ic + 2];
+        for (int dx = -refine[0]; dx <= refine[0]; dx++) {
+            int cx = ix + dx;
+            double ox = 0.0;
+            if (periodic) {
+                if (cx >= nmesh[0]) ox = -wrap[0]; else if (cx < 0) ox = wrap[0];
+                cx = ((cx % nmesh[0]) + nmesh[0]) % nmesh[0];
+            } else if (cx < 0 || cx >= nmesh[0]) continue;
+            const double px = cen[3 * ic] + ox;
+            for (int dy = -refine[1]; dy <= refine[1]; dy++) {
+                int cy = iy + dy;
+                double oy = 0.0;
+                if (periodic) {
+                    if (cy >= nmesh[1]) oy = -wrap[1]; else if (cy < 0) oy = wrap[1];
+                    cy = ((cy % nmesh[1]) + nmesh[1]) % nmesh[1];
+                } else if (cy < 0 || cy >= nmesh[1]) continue;
+                const double py = cen[3 * ic + 1] + oy;
+                for (int dz = -refine[2]; dz <= refine[2]; dz++) {
+                    int cz = iz + dz;
+                    double oz = 0.0;
+                    if (periodic) {
+                        if (cz >= nmesh[2]) oz = -wrap[2]; else if (cz < 0) oz = wrap[2];
+                        cz = ((cz % nmesh[2]) + nmesh[2]) % nmesh[2];
+                    } else if (cz < 0 || cz >= nmesh[2]) continue;
+                    const double pz = cen[3 * ic + 2] + oz;
+                    const int64_t cell = ((int64_t)cx * nmesh[1] + cy) * nmesh[2] + cz;
+                    for (int64_t k = start[cell]; k < start[cell + 1]; k++) {
+                        const int64_t j = order[k];
+                        const double ddx = x[j] - px, ddy = y[j] - py, ddz = z[j] - pz;
+                        volatile double t = ddx * ddx + ddy * ddy;
+                        const double r2 = t + ddz * ddz;
+                        if (r2 >= rmax_sqr) continue;
+                        nwithin++;
+                        const int ib = (int)(sqrt(r2) * inv_rstep);
+                        if (ib < nbin) counts[ib]++;
+                    }
+                }
+            }
+        }
+        if (within) {
+            within[ic] = nwithin;
+            continue;
+        }
+        for (int b = 1; b < nbin; b++) counts[b] += counts[b - 1];
+        for (int b = 0; b < nbin; b++)
+            if (counts[b] < num_pN) pN[(size_t)b * num_pN + counts[b]]++;
+    }
+    free(counts);
+    free(start);
+    free(cellof);
+    free(order);
+    return 0;
 }

@@ -452,7 +452,7 @@ def fix_ra_dec_cz(ra, dec, cz, is_comoving_dist):
         cz *= SPEED_OF_LIGHT
 
 
-def mock_xyz(ra, dec, cz, is_comoving_dist, cosmology, zmax):
+def mock_xyz(ra, dec, cz, is_comoving_dist, cosmology, zmax, with_dist=False):
     lib = _lib()
     ra, dec, cz = (np.ascontiguousarray(a, dtype=np.float64) for a in (ra, dec, cz))
     n = len(ra)
@@ -461,11 +461,15 @@ def mock_xyz(ra, dec, cz, is_comoving_dist, cosmology, zmax):
     def P(a):
         return a.ctypes.data_as(ctypes.c_void_p)
 
+    d = np.zeros(n)
     lib.cfo_mock_xyz.restype = ctypes.c_int
     rc = lib.cfo_mock_xyz(ctypes.c_int64(n), P(ra), P(dec), P(cz), ctypes.c_int(int(bool(is_comoving_dist))),
-                          ctypes.c_double(OMEGA_M.get(cosmology, 0.25)), ctypes.c_double(zmax), P(x), P(y), P(z))
+                          ctypes.c_double(OMEGA_M.get(cosmology, 0.25)), ctypes.c_double(zmax), P(x), P(y), P(z),
+                          P(d))
     if rc != 0:
         raise RuntimeError("redshift outside the comoving-distance table")
+    if with_dist:
+        return x, y, z, d
     return x, y, z
 
 
@@ -526,3 +530,168 @@ def DDsmu_mocks(autocorr, cosmology, mu_max, nmu_bins, binfile, RA1, DEC1, CZ1, 
             k = i * (nmu_bins + 1) + j
             rows.append((rupp[i - 1], rupp[i], a[k], (j + 1) * dmu, c[k], w[k]))
     return np.array(rows, dtype=DDSMU_MOCKS_DTYPE)
+
+
+# ---- counts in spheres ----
+
+VPF_DTYPE_CACHE = {}
+
+
+def vpf_dtype(num_pN):
+    return np.dtype([("rmax", np.float64), ("pN", (np.float64, num_pN))])
+
+
+def mt_uniforms(seed, n):
+    """n uniforms of MT19937 seeded as GSL's gsl_rng_mt19937 (cfo_mt_uniforms)."""
+    lib = _lib()
+    out = np.zeros(n)
+    lib.cfo_mt_uniforms(ctypes.c_ulong(seed & 0xffffffffffffffff), ctypes.c_int64(n),
+                        out.ctypes.data_as(ctypes.c_void_p))
+    return out
+
+
+def get_binsize(xdiff, xwrap, rmax, refine, max_cells):
+    """utils/gridlink_utils.c.src:31-49."""
+    n = int(refine * xdiff / rmax)
+    n = max(n, 1)
+    if xwrap > 0 and rmax >= xwrap / 2:
+        raise RuntimeError("rmax must be less than half of the periodic box")
+    n = min(n, max_cells)
+    n = max(n, 2)
+    return xdiff / n, n
+
+
+def _vpf_counts(pts, lat_min, lat_inv, nmesh, refine, periodic, wrap, cen, cell, rmax, nbin, num_pN, within=False):
+    lib = _lib()
+    x, y, z = (np.ascontiguousarray(a, dtype=np.float64) for a in pts)
+    cen = np.ascontiguousarray(cen, dtype=np.float64).reshape(-1)
+    cell = np.ascontiguousarray(cell, dtype=np.int32).reshape(-1)
+    ncen = len(cen) // 3
+
+    def P(a):
+        return a.ctypes.data_as(ctypes.c_void_p)
+
+    arr_i = lambda v: (ctypes.c_int * 3)(*[int(t) for t in v])  # noqa: E731
+    arr_d = lambda v: (ctypes.c_double * 3)(*[float(t) for t in v])  # noqa: E731
+    pN = np.zeros(nbin * num_pN, dtype=np.uint64)
+    ngb = np.zeros(max(ncen, 1), dtype=np.uint32)
+    lib.cfo_vpf.restype = ctypes.c_int
+    rc = lib.cfo_vpf(ctypes.c_int64(len(x)), P(x), P(y), P(z), arr_i(nmesh), arr_d(lat_min), arr_d(lat_inv),
+                     arr_i(refine), ctypes.c_int(int(periodic)), arr_d(wrap), ctypes.c_int64(ncen), P(cen), P(cell),
+                     ctypes.c_double(rmax), ctypes.c_int(nbin), ctypes.c_int(num_pN),
+                     None if within else P(pN), P(ngb) if within else None)
+    if rc != 0:
+        raise RuntimeError("points outside the lattice")
+    return ngb[:ncen] if within else pN.reshape(nbin, num_pN)
+
+
+def _vpf_rows(pn, rmax, nbin, num_pN, norm):
+    out = np.zeros(nbin, dtype=vpf_dtype(num_pN))
+    rstep = rmax / float(nbin)
+    for b in range(nbin):
+        out["rmax"][b] = (b + 1) * rstep
+        out["pN"][b] = [float(v) * (1.0 / float(norm)) for v in pn[b]]
+    return out
+
+
+def vpf(rmax, nbins, nspheres, numpN, seed, X, Y, Z, periodic=True, boxsize=None, refine=(1, 1, 1),
+        max_cells_per_dim=100):
+    """theory/vpf/countspheres_impl.c.src:136-479 restated; returns (results, counts)."""
+    pts = [np.ascontiguousarray(a, dtype=np.float64) for a in (X, Y, Z)]
+    lo = [float(np.min(a)) for a in pts]
+    hi = [float(np.max(a)) for a in pts]
+    b3 = _box3(boxsize)
+    wrap = [(b3[a] if (periodic and b3[a] > 0) else hi[a] - lo[a]) for a in range(3)]
+    nmesh, inv = [], []
+    for a in range(3):
+        bs, n = get_binsize(hi[a] - lo[a], wrap[a], rmax, refine[a], max_cells_per_dim)
+        nmesh.append(n)
+        inv.append(1.0 / bs if bs > 0 else 0.0)
+    inv_wrap = [1.0 / w for w in wrap]
+    need = 3 * nspheres * 4 + 64
+    while True:
+        u = mt_uniforms(seed, need)
+        cen, cell, k = [], [], 0
+        while len(cen) < nspheres and k + 3 <= need:
+            c = [wrap[a] * u[k + a] + lo[a] for a in range(3)]
+            k += 3
+            if not periodic and any((c[a] - lo[a]) < rmax or (hi[a] - c[a]) < rmax for a in range(3)):
+                continue
+            idx = []
+            for a in range(3):
+                t = int(nmesh[a] * (c[a] - lo[a]) * inv_wrap[a])
+                if t > nmesh[a] - 1:
+                    t -= 1
+                idx.append(t)
+            cen.append(c)
+            cell.append(idx)
+        if len(cen) == nspheres:
+            break
+        need *= 4
+    pn = _vpf_counts(pts, lo, inv, nmesh, refine, periodic, wrap, cen, cell, rmax, nbins, numpN)
+    return _vpf_rows(pn, rmax, nbins, numpN, nspheres), pn
+
+
+def vpf_mocks(rmax, nbins, nspheres, numpN, threshold_ngb, centers_file, cosmology, RA, DEC, CZ, RAND_RA, RAND_DEC,
+              RAND_CZ, is_comoving_dist=False, refine=(1, 1, 1), max_cells_per_dim=100):
+    """mocks/vpf_mocks/countspheres_mocks_impl.c.src:208-638 restated (the centres file is read,
+    never written); returns (results, counts, centres)."""
+    need_randoms = True
+    file_rows = None
+    if centers_file is not None and os.path.exists(centers_file):
+        rows = [ln for ln in open(centers_file).read().splitlines() if ln.strip() and not ln.strip().startswith("#")]
+        if rows and float(rows[0].split()[3]) >= rmax and len(rows) >= nspheres:
+            need_randoms = False
+            file_rows = rows
+    czs = [np.asarray(CZ, dtype=np.float64)] + ([np.asarray(RAND_CZ, dtype=np.float64)] if need_randoms else [])
+    zmax = max(0.0, max(float(np.max(c)) for c in czs)) * (1.0 / SPEED_OF_LIGHT) + 0.01
+    gx, gy, gz, gd = mock_xyz(RA, DEC, CZ, is_comoving_dist, cosmology, zmax, with_dist=True)
+    rcube = 0.0
+    for v in gd:
+        if v > rcube:
+            rcube = float(v)
+    if need_randoms:
+        rx, ry, rz, rd = mock_xyz(RAND_RA, RAND_DEC, RAND_CZ, is_comoving_dist, cosmology, zmax, with_dist=True)
+        for v in rd:
+            if v > rcube:
+                rcube = float(v)
+    rcube = rcube + 1.0
+    G = [gx + rcube, gy + rcube, gz + rcube]
+    rcube = 2.0 * rcube
+    inv_rcube = 1.0 / rcube
+    nmesh, inv = [], []
+    for a in range(3):
+        bs, n = get_binsize(rcube, 0.0, rmax, refine[a], max_cells_per_dim)
+        nmesh.append(n)
+        inv.append(1.0 / bs if bs > 0 else 0.0)
+
+    def cell_of(c):
+        idx = []
+        for a in range(3):
+            t = int(nmesh[a] * (c[a] - 0.0) * inv_rcube)
+            if t > nmesh[a] - 1:
+                t -= 1
+            idx.append(t)
+        return idx
+
+    nran = len(RAND_RA)
+    if need_randoms:
+        R = [rx + rcube / 2.0, ry + rcube / 2.0, rz + rcube / 2.0]
+        cand = [[R[0][t], R[1][t], R[2][t]] for t in range(nran)]
+        cells = [cell_of(c) for c in cand]
+        ngb = _vpf_counts(R, [0.0] * 3, inv, nmesh, refine, False, [0.0] * 3, cand, cells, rmax, 1, 1, within=True)
+        cen, cell = [], []
+        for t in range(nran):
+            if len(cen) >= nspheres:
+                break
+            if int(ngb[t]) > threshold_ngb:
+                cen.append(cand[t])
+                cell.append(cells[t])
+    else:
+        cen = []
+        for ln in file_rows[:min(nspheres, nran)]:
+            v = [float(t) for t in ln.split()[:4]]
+            cen.append(v[:3])
+        cell = [cell_of(c) for c in cen]
+    pn = _vpf_counts(G, [0.0] * 3, inv, nmesh, refine, False, [0.0] * 3, cen, cell, rmax, nbins, numpN)
+    return _vpf_rows(pn, rmax, nbins, numpN, len(cen)), pn, np.array(cen)

@@ -281,6 +281,25 @@ def test_mocks_reject_bad_inputs(lib, smu):
         assert _call_mocks(lib, False, pimax=0.5) == 1
 
 
+def test_vpf_rejects_bad_inputs(lib, tmp_path):
+    """countspheres / countspheres_mocks input checks (theory/vpf/countspheres_impl.c.src:162-167,
+    mocks/vpf_mocks/countspheres_mocks_impl.c.src:219-222, unknown cosmology)."""
+    from corrfunc_gb300 import _capi as C
+    x = np.linspace(1.0, 9.0, 30)
+    for rmax, nbin, nc, npn in [(0.0, 5, 10, 3), (1.0, 0, 10, 3), (1.0, 5, 0, 3), (1.0, 5, 10, 0)]:
+        o = C.get_config_options()
+        o.boxsize_x = o.boxsize_y = o.boxsize_z = 10.0
+        res = C.ResultsVpf()
+        assert lib.countspheres(len(x), C.ptr(x), C.ptr(x), C.ptr(x), rmax, nbin, nc, npn, 1, ctypes.byref(res),
+                                ctypes.byref(o), None) == 1
+    ra, dec, cz = np.full(5, 150.0), np.full(5, 10.0), np.full(5, 8000.0)
+    o = C.get_config_options()
+    res = C.ResultsVpf()
+    f = str(tmp_path / "centres.txt").encode()
+    assert lib.countspheres_mocks(5, C.ptr(ra), C.ptr(dec), C.ptr(cz), 5, C.ptr(ra), C.ptr(dec), C.ptr(cz), 1, 5.0, 5, 10,
+                                  3, f, 3, ctypes.byref(res), ctypes.byref(o), None) == 1
+
+
 def test_no_gpu_fails_loudly_not_silently(lib):
     """Without a usable GPU the library reports failure; it never falls back to the CPU."""
     import corrfunc_gb300

@@ -251,3 +251,25 @@ def test_oracle_mock_formula_families_agree_off_the_edges(orc):
     for o in smu[1:]:
         assert np.array_equal(o["npairs"], smu[0]["npairs"])
     assert smu[0]["npairs"].sum() > 0
+
+
+def test_oracle_mt19937_known_answers(orc):
+    """MT19937 with seed 5489: first output 3499211612 and 10,000th output 4123659995 (the published
+    known answers, the latter required of std::mt19937 by the C++ standard)."""
+    u = orc.mt_uniforms(5489, 10000) * 4294967296.0
+    assert int(u[0]) == 3499211612
+    assert int(u[-1]) == 4123659995
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF_ROOT, "mocks", "tests")), reason="reference tree not present")
+def test_oracle_reproduces_mr19_vpf_mocks_golden(orc):
+    """mocks/tests/Mr19_mock_vpf (Corrfunc/tests/test_mocks.py:83-113): 10,000 spheres of radius up to 10
+    from the reference's centres file, 10 radii, p0..p5, cosmology 1 -- every count exact."""
+    ra, dec, cz, _ = _read_fastfood(os.path.join(REF_ROOT, "mocks", "tests", "data", "Mr19_mock_northonly.rdcz.ff"))
+    centers = os.path.join(REF_ROOT, "mocks", "tests", "data", "Mr19_centers_xyz_forVPF_rmax_10Mpc.txt")
+    res, counts, cen = orc.vpf_mocks(10.0, 10, 10000, 6, 1, centers, 1, ra.copy(), dec.copy(), cz.copy(), ra.copy(),
+                                     dec.copy(), cz.copy())
+    gold = np.genfromtxt(os.path.join(REF_ROOT, "mocks", "tests", "Mr19_mock_vpf"))
+    assert len(cen) == 10000
+    assert np.array_equal(np.rint(gold[:, 1:] * 10000).astype(np.int64), counts.astype(np.int64))
+    np.testing.assert_allclose(res["pN"], gold[:, 1:], rtol=1e-6, atol=1e-9)
