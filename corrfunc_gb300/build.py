@@ -46,7 +46,7 @@ def build(verbose=False, extra_nvcc=()):
     cuda = _cuda_root(nvcc)
     inc = ["-I" + INCLUDE, "-I" + CSRC, "-I" + os.path.join(cuda, "include")]
     jobs = []
-    for c in ("cf_api.c", "cf_common.c"):
+    for c in ("cf_api.c", "cf_common.c", "cf_io.c"):
         obj = os.path.join(BUILD, c[:-2] + ".o")
         jobs.append(["gcc", "-std=gnu11", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
                     + inc + ["-c", os.path.join(CSRC, c), "-o", obj])
@@ -61,13 +61,34 @@ def build(verbose=False, extra_nvcc=()):
         for r in ex.map(_run, jobs):
             if verbose and (r.stdout or r.stderr):
                 print(r.stdout, r.stderr)
-    objs = [os.path.join(BUILD, "cf_api.o"), os.path.join(BUILD, "cf_common.o")] + cu_objs
+    objs = [os.path.join(BUILD, "cf_api.o"), os.path.join(BUILD, "cf_common.o"), os.path.join(BUILD, "cf_io.o")] + cu_objs
     tmp = LIB + ".tmp"
     _run([nvcc] + NVCC_ARCH + ["-shared", "-o", tmp] + objs
          + ["-L" + os.path.join(cuda, "lib64"), "-lcudart_static", "-lpthread", "-ldl", "-lrt", "-lm"])
     os.replace(tmp, LIB)
     build_python_modules(verbose)
+    build_cli()
     return LIB
+
+
+CLI_COMMANDS = ("DD", "DDrppi", "DDsmu", "wp", "xi", "vpf", "DDtheta_mocks", "DDrppi_mocks", "DDsmu_mocks", "vpf_mocks")
+
+
+def build_cli():
+    """The reference's command-line programs as one binary (csrc/cf_cli.c) in bin/, linked against
+    libcorrfunc_gb300.so, with one link per command name."""
+    bindir = os.path.join(HERE, "bin")
+    os.makedirs(bindir, exist_ok=True)
+    exe = os.path.join(bindir, "corrfunc_gb300_cli")
+    _run(["gcc", "-std=gnu11", "-O2", "-Wall", "-Wno-unused-function", "-I" + INCLUDE, os.path.join(CSRC, "cf_cli.c"),
+          "-o", exe + ".tmp", "-L" + HERE, "-lcorrfunc_gb300", "-lm", "-Wl,-rpath,$ORIGIN/.."])
+    os.replace(exe + ".tmp", exe)
+    for name in CLI_COMMANDS:
+        link = os.path.join(bindir, name)
+        if os.path.lexists(link):
+            os.remove(link)
+        os.symlink("corrfunc_gb300_cli", link)
+    return exe
 
 
 def python_module_paths():

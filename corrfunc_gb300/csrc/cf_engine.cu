@@ -2996,6 +2996,28 @@ extern "C" int cf_engine_set_precision(int mode)
 
 extern "C" int cf_engine_get_precision(void) { return g_eng.precision; }
 
+extern "C" int cf_engine_to_device(const void *src, size_t bytes, void **dev)
+{
+    pthread_mutex_lock(&g_lock);
+    int rc = engine_init();
+    void *p = nullptr;
+    if (rc == EXIT_SUCCESS && cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) rc = EXIT_FAILURE;
+    if (rc == EXIT_SUCCESS && bytes && cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice) != cudaSuccess) rc = EXIT_FAILURE;
+    pthread_mutex_unlock(&g_lock);
+    if (rc != EXIT_SUCCESS) {
+        if (p) cudaFree(p);
+        fprintf(stderr, "corrfunc_gb300: could not copy %zu bytes to the device\n", bytes);
+        return EXIT_FAILURE;
+    }
+    *dev = p;
+    return EXIT_SUCCESS;
+}
+
+extern "C" void cf_engine_free_device(void *dev)
+{
+    if (dev) cudaFree(dev);
+}
+
 extern "C" int cf_engine_copy_to_host(void *dst, const void *src, size_t bytes)
 {
     CF_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));

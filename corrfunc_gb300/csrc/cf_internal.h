@@ -162,6 +162,9 @@ typedef struct {
 int cf_engine_last_stats(cf_engine_stats *out);
 int cf_engine_fp32_peak(double *tflops);
 int cf_engine_copy_to_host(void *dst, const void *src, size_t bytes);
+/* new device buffer holding a copy of bytes of host memory; and its release */
+int cf_engine_to_device(const void *src, size_t bytes, void **dev);
+void cf_engine_free_device(void *dev);
 
 #ifdef __cplusplus
 }

@@ -346,6 +346,14 @@ int countspheres_mocks(const int64_t Ngal, void *xgal, void *ygal, void *zgal,
 /* Replaces free_results_countspheres_mocks(), mocks/vpf_mocks/countspheres_mocks.h:38. */
 void free_results_countspheres_mocks(results_countspheres_mocks *results);
 
+/* ---------------- particle-file readers (io/io.h:15-16) ----------------
+ * Replace read_positions() / read_columns_into_array(), io/io.c:29-284: fast-food ("f"),
+ * ASCII ("a") or CSV ("c") files; num_fields arrays of size 4 or 8 bytes per value, malloc'ed
+ * (the caller frees them); returns the number of particles or -1. */
+int64_t read_positions(const char *filename, const char *format, const size_t size, const int num_fields, ...);
+int64_t read_columns_into_array(const char *filename, const char *format, const size_t size, const int num_fields,
+                                void **data);
+
 /* ---------------- GB300 extensions (no reference counterpart) ----------------
  * Counting precision of the GPU engine.  CF_PRECISION_FP32_REFINE (default) classifies
  * every pair in FP32 and re-evaluates in FP64, with the reference's formula, the pairs
@@ -410,6 +418,13 @@ void cf_gpu_batch_free(cf_gpu_batch *plan);
 /* Measured FP32 fused-multiply-add throughput of the current device in TFLOP/s (a calibration
  * kernel; denominator of the pair kernels' FP32 roofline fraction).  No reference counterpart. */
 int cf_gpu_fp32_peak_tflops(double *tflops);
+
+/* Extension (no counterpart in the reference): read_columns_into_array() followed by a copy of
+ * every field into a new device buffer (device_fields[i], released with cf_gpu_free_device), for
+ * cf_gpu_countpairs_device.  Returns the number of particles or -1. */
+int64_t cf_gpu_read_positions_device(const char *filename, const char *format, const size_t size, const int num_fields,
+                                     void **device_fields);
+void cf_gpu_free_device(void *device_ptr);
 
 /* The algorithmic work unit of countpairs(): the number of candidate pairs the reference's own
  * lattice and cell-pair list (utils/gridlink_impl.c.src:65-625) would evaluate for these

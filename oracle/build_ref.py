@@ -1,8 +1,8 @@
 #!/usr/bin/env python3
 """Build recipe for the *reference* Corrfunc 2.5.3 pair counters (test infrastructure only).
 
-This compiles the reference's own C sources for the six pair-counting modules into
-per-module shared libraries under ``oracle/_ref/`` so that the tests and the CPU baseline
+This compiles the reference's own C sources for the six pair-counting modules (and its
+particle-file readers, ``io/io.c``) into per-module shared libraries under ``oracle/_ref/`` so that the tests and the CPU baseline
 leg of ``bench.py`` can call the reference through its public C API
 (``theory/DD/countpairs.h:28-35`` and siblings).  Nothing in the product links it.
 
@@ -37,6 +37,7 @@ REF_DIR = os.environ.get("CORRFUNC_REF_DIR", "/root/reference")
 VERSION = "2.5.3"
 
 UTILS_PLAIN = ["utils.c", "progressbar.c", "cpu_features.c"]
+IO_FILES = ["io.c", "io.h", "ftread.c", "ftread.h"]
 UTILS_HEADERS = ["defs.h", "macros.h", "utils.h", "progressbar.h", "cpu_features.h",
                  "function_precision.h", "sglib.h", "avx512_calls.h", "avx2_calls.h",
                  "avx_calls.h", "sse_calls.h", "fast_acos.h"]
@@ -103,6 +104,11 @@ def stage():
             _expand(os.path.join(msrc, impl + ".c.src"), os.path.join(mdst, "%s_%s.c" % (impl, prec)), prec)
             _expand(os.path.join(msrc, impl + ".h.src"), os.path.join(mdst, "%s_%s.h" % (impl, prec)), prec)
             _expand(os.path.join(msrc, kern + ".c.src"), os.path.join(mdst, "%s_%s.c" % (kern, prec)), prec)
+    # the particle-file readers (io/io.c, io/ftread.c), for the reader tests
+    idst = os.path.join(SRC_OUT, "io")
+    os.makedirs(idst)
+    for fn in IO_FILES:
+        shutil.copy(os.path.join(REF_DIR, "io", fn), idst)
     print("build_ref: staged reference sources into %s" % SRC_OUT)
     return True
 
@@ -139,12 +145,32 @@ def _compile_module(name):
     return so
 
 
+def _compile_io():
+    idst = os.path.join(SRC_OUT, "io")
+    udst = os.path.join(SRC_OUT, "utils")
+    if not os.path.isdir(idst):
+        return None
+    objdir = os.path.join(REF_OUT, "obj", "io")
+    os.makedirs(objdir, exist_ok=True)
+    objs = []
+    for s in [os.path.join(idst, "io.c"), os.path.join(idst, "ftread.c")] + [os.path.join(udst, fn) for fn in UTILS_PLAIN]:
+        o = os.path.join(objdir, os.path.basename(s)[:-2] + ".o")
+        subprocess.check_call(["gcc"] + _cflags() + ["-I" + idst, "-I" + udst, "-c", s, "-o", o])
+        objs.append(o)
+    so = os.path.join(REF_OUT, "libcf_ref_io.so")
+    subprocess.check_call(["gcc", "-shared", "-fopenmp", "-o", so] + objs + ["-lm"])
+    return so
+
+
 def compile_all():
     if not os.path.isdir(SRC_OUT):
         print("build_ref: no staged sources in %s; reference libraries not built" % SRC_OUT)
         return []
-    with ThreadPoolExecutor(max_workers=min(6, os.cpu_count() or 1)) as ex:
+    with ThreadPoolExecutor(max_workers=min(7, os.cpu_count() or 1)) as ex:
         sos = list(ex.map(_compile_module, MODULES))
+        io = ex.submit(_compile_io).result()
+    if io:
+        sos.append(io)
     print("build_ref: built %d reference libraries" % len(sos))
     return sos
 
