@@ -719,7 +719,8 @@ def other_counters(cf, cat, theory):
                                           "gpu_evaluated_pairs": best["pairs_evaluated"],
                                           "fp32_slow_path": best["pairs_slow"],
                                           "fp64_refined": best["pairs_refined"],
-                                          "npairs_sum": int(np.sum(r["npairs"]))}
+                                          "npairs_sum": int(np.sum(r["npairs"])) if "npairs" in r.dtype.names
+                                          else None}
     return out
 
 

@@ -106,6 +106,10 @@ struct PairArgs {
     float inv_dmu_f;
     float dz_err;                  // bound on |dz_f32 - dz_ref|
     float dxy_err;                 // bound on |(dx,dy)_f32 - (dx,dy)_ref|
+    // survey (mock) modes
+    float s2_cut_f;                // FP32 |s|^2 at or above this: certainly beyond the largest separation
+    float l2_min_f;                // FP32 |l|^2 below this (pairs near the observer): exact path
+    float mu_band_rel;             // part of the mu error bound independent of |s|
 
     // fixed-point scales for the per-warp accumulators
     const float *g_ascale;      // per separation bin: fixed-point scale of the separation sums

@@ -73,7 +73,7 @@ constexpr int kZFine = CF_Z_SLABS;  // z slabs per rmax_z
 constexpr int kScanTile = 4096;
 
 // modes with an FP32 classification kernel (the others always run the FP64 kernel)
-constexpr bool has_f32_path(int mode) { return !mode_is_mock(mode); }
+constexpr bool has_f32_path(int mode) { return mode >= 0 && mode < kNumModes; }
 template <int MODE>
 constexpr bool kHasF32 = has_f32_path(MODE);
 
@@ -82,6 +82,7 @@ constexpr bool kHasF32 = has_f32_path(MODE);
 // ------------------------------------------------------------------------------------
 struct Geom {
     double origin[3];
+    double hi_origin[3];  // origin of the hi / lo split (the lattice origin, or 0 for survey positions)
     double inv_s[3];
     double s[3];
     int n[3];  // n[0] x columns, n[1] y columns, n[2] z slabs
@@ -307,9 +308,9 @@ __global__ void k_scatter(const T *x, const T *y, const T *z, const T *w, int64_
         const double wv = w ? ld(w, i) : 1.0;
         if (g.extent_err && w && !(fabs(wv) <= g.chk_wmax)) atomicAdd(g.extent_err, 1ull);
         float hx, hy, hz, lx, ly, lz;
-        split_hi_lo(a - g.origin[0], g.q[0], g.inv_q[0], &hx, &lx);
-        split_hi_lo(b - g.origin[1], g.q[1], g.inv_q[1], &hy, &ly);
-        split_hi_lo(cz - g.origin[2], g.q[2], g.inv_q[2], &hz, &lz);
+        split_hi_lo(a - g.hi_origin[0], g.q[0], g.inv_q[0], &hx, &lx);
+        split_hi_lo(b - g.hi_origin[1], g.q[1], g.inv_q[1], &hy, &ly);
+        split_hi_lo(cz - g.hi_origin[2], g.q[2], g.inv_q[2], &hz, &lz);
         L.hi[pos] = make_float4(hx, hy, hz, (float)wv);
         L.lo[pos] = make_float4(lx, ly, lz, 0.f);
         L.dbl[pos] = make_double4_32a(a, b, cz, wv);
@@ -729,6 +730,29 @@ __device__ __forceinline__ int classify_q(const PairArgs &A, const float *glo, c
     return m;
 }
 
+// FP32 quantities of a survey pair.  Positions are split at the observer (x = hi + lo, hi on a
+// power-of-two grid): s = x_j - x_i is the exact hi difference plus the lo difference, the line of
+// sight l = x_i + x_j (per i point a = hi_i + lo_i), and
+//   s2 = |s|^2,  pi = |s.l| / |l|,  rp2 = |s x l|^2 / |l|^2
+// (the cross product keeps rp accurate to a few ulps of |s| where s^2 - pi^2 would cancel).
+template <int MODE>
+__device__ __forceinline__ void mock_terms(float4 pj, float4 pjl, float xi, float yi, float zi, float xil, float yil,
+                                           float zil, float ax, float ay, float az, float &s2, float &l2, float &pi,
+                                           float &rp2)
+{
+    const float sx = (pj.x - xi) + (pjl.x - xil), sy = (pj.y - yi) + (pjl.y - yil), sz = (pj.z - zi) + (pjl.z - zil);
+    const float lx = ax + (pj.x + pjl.x), ly = ay + (pj.y + pjl.y), lz = az + (pj.z + pjl.z);
+    s2 = fmaf(sz, sz, fmaf(sy, sy, sx * sx));
+    l2 = fmaf(lz, lz, fmaf(ly, ly, lx * lx));
+    const float rl = rsqrtf(l2);
+    pi = fabsf(fmaf(lz, sz, fmaf(ly, sy, lx * sx))) * rl;
+    rp2 = 0.f;
+    if (MODE == MODE_RPPI_MOCK) {
+        const float cx = fmaf(sy, lz, -(sz * ly)), cy = fmaf(sz, lx, -(sx * lz)), cz = fmaf(sx, ly, -(sy * lx));
+        rp2 = fmaf(cz, cz, fmaf(cy, cy, cx * cx)) * (rl * rl);
+    }
+}
+
 // Exact FP32 classification of one candidate whose LUT bucket is flagged: guard scan and the
 // 2-D bin checks.  Returns the flat bin (with its FP32 accumulator terms), -1 when the pair is
 // provably not counted, or -2 when it lies inside an error band and needs the reference's FP64
@@ -736,8 +760,43 @@ __device__ __forceinline__ int classify_q(const PairArgs &A, const float *glo, c
 template <int MODE, bool NEED_AVG, bool NEED_W>
 __device__ __noinline__ int slow_candidate(const PairArgs &A, const float *glo, const float *ghi, float4 pj, float4 pjl,
                                            float xi, float yi, float zi, float xil, float yil, float zil, float wi,
-                                           float *favg, float *fw)
+                                           float ax, float ay, float az, float *favg, float *fw)
 {
+    if (MODE == MODE_RPPI_MOCK || MODE == MODE_SMU_MOCK) {
+        float s2, l2, pi, rp2;
+        mock_terms<MODE>(pj, pjl, xi, yi, zi, xil, yil, zil, ax, ay, az, s2, l2, pi, rp2);
+        if (!(s2 < A.s2_cut_f)) return -1;
+        if (!(l2 >= A.l2_min_f)) return -2;  // near the observer: the bands do not hold
+        bool amb;
+        const int m = classify_q(A, glo, ghi, fmaxf(MODE == MODE_RPPI_MOCK ? rp2 : s2, A.q_floor), &amb);
+        if (m == 0) return -1;
+        int pb;
+        if (MODE == MODE_RPPI_MOCK) {
+            if (pi >= A.pimax_hi_f) return -1;
+            if (pi > A.pimax_lo_f) amb = true;
+            const float tpi = pi * A.inv_dpi_f;
+            pb = (int)tpi;
+            const float fr = tpi - (float)pb;
+            if ((pb >= 1 && fr < A.pibin_band) || (1.f - fr) < A.pibin_band) amb = true;
+            if (NEED_AVG) amb = true;  // rp averages need the FP64 rp of every counted pair
+        } else {
+            const float inv_s = rsqrtf(fmaxf(s2, 1e-30f));
+            const float mu = pi * inv_s;
+            const float emu = fmaf(A.mu_band_abs, inv_s, A.mu_band_rel);
+            if (mu >= A.mu_max_f + emu) return -1;
+            if (mu > A.mu_max_f - emu) amb = true;
+            const float tmu = mu * A.inv_dmu_f;
+            pb = (int)tmu;
+            const float bt = emu * A.inv_dmu_f + 4e-7f * tmu;
+            const float fr = tmu - (float)pb;
+            if ((pb >= 1 && fr < bt) || (1.f - fr) < bt) amb = true;
+        }
+        if (amb) return -2;
+        pb = pb > A.npibin ? A.npibin : pb;
+        if (NEED_AVG) *favg = sqrtf(s2);
+        if (NEED_W) *fw = wi * pj.w;
+        return m * (A.npibin + 1) + pb;
+    }
     const float dx = pj.x - xi, dy = pj.y - yi, dz = pj.z - zi;
     float q;  // the fast path's expression, so that the pair lands in the same flagged bucket
     if (MODE == MODE_RPPI || MODE == MODE_WP) q = fmaf(dy, dy, fmaf(dx, dx, A.q_floor));
@@ -814,9 +873,48 @@ template <int MODE, bool NEED_AVG, bool NEED_W, bool OWN>
 __device__ __forceinline__ uint32_t pair_offset(const PairArgs &A, const float4 *__restrict__ sjhi,
                                                 const float4 *__restrict__ sjlo, const uint32_t *__restrict__ lut,
                                                 const float *__restrict__ ascale, int k, uint32_t jb, uint32_t i, float xi, float yi, float zi,
-                                                float xil, float yil, float zil, float wis, uint32_t &slow,
-                                                int &vw, int &vavg)
+                                                float xil, float yil, float zil, float wis, float ax, float ay, float az,
+                                                uint32_t &slow, int &vw, int &vavg)
 {
+    if (MODE == MODE_RPPI_MOCK || MODE == MODE_SMU_MOCK) {
+        const float4 pj = sjhi[k], pjl = sjlo[k];
+        float s2, l2, pi, rp2;
+        mock_terms<MODE>(pj, pjl, xi, yi, zi, xil, yil, zil, ax, ay, az, s2, l2, pi, rp2);
+        const float q = fmaxf(MODE == MODE_RPPI_MOCK ? rp2 : s2, A.q_floor);
+        const uint32_t e = lut[lut_bucket(A, q)];
+        uint32_t off = e & 0x003fffffu, sl = e;
+        if (OWN) {
+            const bool keep = jb + (uint32_t)k > i;
+            off = keep ? off : A.trash_off;
+            sl = keep ? sl : 0u;
+        }
+        const bool real = off != A.trash_off;
+        const bool near = !(l2 >= A.l2_min_f);  // also NaN (padding far away)
+        bool rej, amb;
+        uint32_t add;
+        if (MODE == MODE_RPPI_MOCK) {
+            rej = !(pi < A.pimax_hi_f);
+            amb = pi > A.pimax_lo_f || NEED_AVG;
+            const int v = __float_as_int(fmaf(pi, A.inv_dpi256_f, 12582912.0f)) - 0x4B400000;
+            amb = amb || (((v + A.pi_band_q) & 255) < 2 * A.pi_band_q);
+            add = (uint32_t)min(v >> 8, A.npibin) * A.row_bytes;
+        } else {
+            const float inv_s = rsqrtf(q);
+            const float mu = pi * inv_s;
+            const float emu = fmaf(A.mu_band_abs, inv_s, A.mu_band_rel);
+            rej = !(mu < A.mu_max_f + emu);
+            const float tmu = mu * A.inv_dmu_f;
+            const float rt = rintf(tmu);
+            amb = (mu > A.mu_max_f - emu) || (fabsf(tmu - rt) < emu * A.inv_dmu_f + 4e-7f * tmu && rt >= 0.5f);
+            add = (uint32_t)min((int)tmu, A.npibin) * A.row_bytes;
+        }
+        rej = !(s2 < A.s2_cut_f) || (rej && !near);
+        slow = (!rej && ((sl >> 31) || near || (real && amb))) ? 0x80000000u : 0u;
+        off = (real && !rej && !amb && !near) ? off + add : A.trash_off;
+        if (NEED_W) vw = __float2int_rn(wis * pj.w);
+        if (NEED_AVG) vavg = MODE == MODE_SMU_MOCK ? __float2int_rn(sqrtf(s2) * ascale[(e >> 22) & 0x1ffu]) : 0;
+        return off;
+    }
     const float4 pj = sjhi[k];
     const float dx = pj.x - xi, dy = pj.y - yi, dz = pj.z - zi;
     // q_floor (1e-30 when rmin <= 0, else 0) keeps exact-zero separations inside the table
@@ -881,7 +979,8 @@ __device__ __forceinline__ void pairs_group(const PairArgs &A, const float4 *__r
                                             const float4 *__restrict__ sjlo, const uint32_t *__restrict__ lut,
                                             const float *__restrict__ ascale, int k0,
                                             uint32_t jb, uint32_t i, float xi, float yi, float zi, float xil, float yil,
-                                            float zil, float wis, uint32_t cnt_s, uint32_t &slowbits)
+                                            float zil, float wis, float ax, float ay, float az, uint32_t cnt_s,
+                                            uint32_t &slowbits)
 {
     uint32_t off[U];
     int vw[U], va[U];
@@ -891,7 +990,7 @@ __device__ __forceinline__ void pairs_group(const PairArgs &A, const float4 *__r
         vw[u] = 0;
         va[u] = 0;
         off[u] = pair_offset<MODE, NEED_AVG, NEED_W, OWN>(A, sjhi, sjlo, lut, ascale, k0 + u, jb, i, xi, yi, zi, xil, yil, zil,
-                                                          wis, sl, vw[u], va[u]);
+                                                          wis, ax, ay, az, sl, vw[u], va[u]);
         slowbits = __funnelshift_l(sl, slowbits, 1);  // pair k of n ends at bit n - 1 - k
     }
 #pragma unroll
@@ -914,18 +1013,20 @@ __device__ __forceinline__ uint32_t tile_fast(const PairArgs &A, const float4 *_
                                               const float4 *__restrict__ sjlo, const uint32_t *__restrict__ lut,
                                               const float *__restrict__ ascale, int nj,
                                               uint32_t jb, uint32_t i, float xi, float yi, float zi, float xil, float yil,
-                                              float zil, float wis, uint32_t cnt_s)
+                                              float zil, float wis, float ax, float ay, float az, uint32_t cnt_s)
 {
     uint32_t slowbits = 0;
     if (nj == 32) {
+        // the survey modes keep more values per pair in flight: smaller groups stay in registers
+        constexpr int kGroup = mode_is_mock(MODE) ? 2 : CF_PAIR_GROUP;
 #pragma unroll
-        for (int k0 = 0; k0 < 32; k0 += CF_PAIR_GROUP)
-            pairs_group<MODE, NEED_AVG, NEED_W, OWN, CF_PAIR_GROUP>(A, sjhi, sjlo, lut, ascale, k0, jb, i, xi, yi, zi, xil,
-                                                                    yil, zil, wis, cnt_s, slowbits);
+        for (int k0 = 0; k0 < 32; k0 += kGroup)
+            pairs_group<MODE, NEED_AVG, NEED_W, OWN, kGroup>(A, sjhi, sjlo, lut, ascale, k0, jb, i, xi, yi, zi, xil, yil,
+                                                             zil, wis, ax, ay, az, cnt_s, slowbits);
     } else {
         for (int k = 0; k < nj; k++)
             pairs_group<MODE, NEED_AVG, NEED_W, OWN, 1>(A, sjhi, sjlo, lut, ascale, k, jb, i, xi, yi, zi, xil, yil, zil, wis,
-                                                        cnt_s, slowbits);
+                                                        ax, ay, az, cnt_s, slowbits);
     }
     return slowbits;
 }
@@ -965,16 +1066,17 @@ __device__ __noinline__ void slow_batch(const PairArgs &A, const double *se, con
         const float xi = pi.x - A.ohi[0][mx + 1], yi = pi.y - A.ohi[1][my + 1], zi = pi.z - A.ohi[2][mz + 1];
         float xil = 0.f, yil = 0.f, zil = 0.f;
         float4 pjl = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (NEED_AVG) {
+        if (NEED_AVG || mode_is_mock(MODE)) {
             const float4 pl = A.lo1[e.i];
             xil = pl.x - A.olo[0][mx + 1];
             yil = pl.y - A.olo[1][my + 1];
             zil = pl.z - A.olo[2][mz + 1];
             pjl = A.lo2[e.j];
         }
+        const float ax = xi + xil, ay = yi + yil, az = zi + zil;
         float favg = 0.f, fw = 0.f;
         const int bin = slow_candidate<MODE, NEED_AVG, NEED_W>(A, glo, ghi, pj, pjl, xi, yi, zi, xil, yil, zil, pi.w,
-                                                               &favg, &fw);
+                                                               ax, ay, az, &favg, &fw);
         if (bin >= 0) {
             accumulate<NEED_AVG, NEED_W>(A, h, bin, bin * h.ls + hl, (double)favg, (double)fw);
         } else if (bin == -2) {
@@ -1065,31 +1167,33 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
         // j is shifted by the image offset o; equivalently shift i by -o (exact on the grid)
         const float xi = pi.x - A.ohi[0][mx + 1], yi = pi.y - A.ohi[1][my + 1], zi = pi.z - A.ohi[2][mz + 1];
         float xil = 0.f, yil = 0.f, zil = 0.f;
-        if (NEED_AVG) {
+        constexpr bool kLo = NEED_AVG || mode_is_mock(MODE);  // survey modes always use the lo parts
+        if (kLo) {
             const float4 pl = ivalid ? A.lo1[i] : make_float4(0.f, 0.f, 0.f, 0.f);
             xil = pl.x - A.olo[0][mx + 1];
             yil = pl.y - A.olo[1][my + 1];
             zil = pl.z - A.olo[2][mz + 1];
         }
+        const float ax = xi + xil, ay = yi + yil, az = zi + zil;  // survey modes: the i point from the observer
         for (uint32_t jb = T.j_begin; jb < T.j_end; jb += 32) {
             int nj = (int)min(32u, T.j_end - jb);
             if (lane < nj) {
                 sjhi[lane] = A.hi2[jb + lane];
-                if (NEED_AVG) sjlo[lane] = A.lo2[jb + lane];
+                if (kLo) sjlo[lane] = A.lo2[jb + lane];
             } else if (nj > kPadMin) {
                 // pad a partial tile with far-away points and run it fully unrolled: q overflows to
                 // +inf (the reject bucket, zero weight) against valid i points and against the
                 // +1e30 stand-in of lanes without an i point alike
                 sjhi[lane] = make_float4(-1e30f, -1e30f, -1e30f, 0.f);
-                if (NEED_AVG) sjlo[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (kLo) sjlo[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
             }
             if (nj > kPadMin) nj = 32;
             __syncwarp();
             const float wi_s = pi.w * A.w_scale_f;
             uint32_t slowbits = own ? tile_fast<MODE, NEED_AVG, NEED_W, true>(A, sjhi, sjlo, lut, h.ascale, nj, jb, i, xi, yi, zi,
-                                                                           xil, yil, zil, wi_s, cnt_s)
+                                                                           xil, yil, zil, wi_s, ax, ay, az, cnt_s)
                                     : tile_fast<MODE, NEED_AVG, NEED_W, false>(A, sjhi, sjlo, lut, h.ascale, nj, jb, i, xi, yi,
-                                                                            zi, xil, yil, zil, wi_s, cnt_s);
+                                                                            zi, xil, yil, zil, wi_s, ax, ay, az, cnt_s);
             // candidates in flagged buckets go to the warp's slow queue, one bit per lane per round
             // (a round appends at most 32 entries, so the queue never holds more than 63)
             while (true) {
@@ -1661,6 +1765,41 @@ static int launch_pairs(int mode, const PairArgs &A, bool f64, bool avg, bool w,
     CF_FAIL("unknown mode %d", mode);
 }
 
+// Survey modes: the FP32 classification holds for pairs with FP32 |s|^2 below s2_cut (larger
+// ones are certainly beyond the largest separation and rejected) and |l| of at least twice the
+// largest |s| (pairs nearer the observer go to the exact path).  S = sqrt(s2_cut) with margin.
+static double mock_s2_cut(const cf_job *J, int mode)
+{
+    const double e = J->edges[J->nedges - 1];
+    const double m2 = mode == MODE_RPPI_MOCK ? e + J->pimax * J->pimax : e;
+    return m2 * (1.0 + 1e-5);
+}
+
+static double mock_smax(const cf_job *J, int mode) { return sqrt(mock_s2_cut(J, mode) * (1.0 + 1e-6)); }
+
+// FP32 error bounds of the survey quantities (u = 2^-24, rsqrtf taken as 8 ulps, q the hi grid):
+//   |s_f - s| <= u|s| + 3.5uq,  |l_f - l| <= u(2|l| + 2|s|) + 2uq  ->  |l^_f - l^| <= 6u + 2uq/|l|
+//   |pi_f - pi| <= |s|(12.7u + 8u) + 3.5uq                      (mock_pi_err, with |s| <= S)
+//   rp via |s x l| / |l|:  |rp_f - rp| <= D = 6uS + 4.5uq + 3u rp, relative factor eta = 25u on rp^2
+//   s^2:  |s2_f - s^2| <= 5.2u s^2 + 7uq|s|
+static double mock_pi_err(double S, double q)
+{
+    const double u = 5.9604644775390625e-08;
+    return 24.0 * u * S + 4.0 * u * q + 1e-13 * S;
+}
+
+static double mock_edge_band(int mode, double e, double S, double q)
+{
+    const double u = 5.9604644775390625e-08;
+    const double re = sqrt(fabs(e));
+    if (mode == MODE_RPPI_MOCK) {
+        const double D = 6.0 * u * S + 4.5 * u * q + 3.0 * u * re;
+        const double eta = 25.0 * u;
+        return 2.0 * (2.0 * re * D + D * D + eta * (re + D) * (re + D) + 1e-14 * (S * S + 1.0));
+    }
+    return 2.0 * (6.0 * u * fabs(e) + 8.0 * u * q * re + 1e-14 * (fabs(e) + 1.0));
+}
+
 // error band for an edge value e given the per-axis coordinate error bound |delta|
 static double edge_band(double e, double delta)
 {
@@ -1715,6 +1854,8 @@ static int build_tables(Workspace &W, const cf_job *J, int mode, int nbins, bool
         if (mode == MODE_THETA) {
             e = 2.0 * (1.0 - J->edges[k]);
             band = edge_band(e, dlim) + 8e-15;
+        } else if (mode_is_mock(mode)) {
+            band = mock_edge_band(mode, e, mock_smax(J, mode), fmax(delta[0], fmax(delta[1], delta[2])));
         } else {
             band = edge_band(e, dlim);
         }
@@ -1844,10 +1985,17 @@ static int gpu_geometry(const cf_job *J, const cf_geometry &geo, const double lo
         }
         g.n[a] = n;
         g.origin[a] = lo[a];
+        g.hi_origin[a] = lo[a];
         g.s[a] = ext > 0.0 ? ext / n : 1.0;
         g.inv_s[a] = 1.0 / g.s[a];
         span[a] = fmax(ext, 1e-300) + (per ? 2.0 * geo.wrap[a] : 0.0);
         g.q[a] = pow2_ceil(span[a]) * ldexp(1.0, -23);
+        if (mode_is_mock(J->mode)) {
+            // survey positions keep their offset from the observer in the split (the line of sight
+            // x_i + x_j is then accurate to a few ulps of its own length): |hi| <= max |x| < 2^23 q
+            g.hi_origin[a] = 0.0;
+            g.q[a] = pow2_ceil(fmax(fmax(fabs(lo[a]), fabs(hi[a])), 1e-300)) * ldexp(1.0, -22);
+        }
         g.inv_q[a] = 1.0 / g.q[a];
         const double maxabs = fmax(fabs(lo[a]), fabs(hi[a])) + (per ? geo.wrap[a] : 0.0);
         delta[a] = 1.5 * g.q[a] + ldexp(1.0, -49) * (maxabs + span[a]);
@@ -1944,13 +2092,31 @@ static void pair_constants(PairArgs &A, const cf_job *J, int mode, int nbins, bo
     A.g_guard = (const float *)W.guards.p;
     A.dz_err = (float)(2.0 * delta[2]);
     A.dxy_err = (float)(2.0 * dxy);
-    if (mode == MODE_RPPI_MOCK) {
-        A.pimax = J->pimax;
-        A.inv_dpi = 1.0 / (J->pimax / J->npibin);
-    }
-    if (mode == MODE_SMU_MOCK) {
-        A.sqr_mu_max = J->mu_max * J->mu_max;
-        A.inv_dmu = 1.0 / (J->mu_max / J->npibin);
+    if (mode_is_mock(mode)) {
+        const double S = mock_smax(J, mode), qm = fmax(delta[0], fmax(delta[1], delta[2]));
+        const double u = 5.9604644775390625e-08;
+        A.s2_cut_f = f_up(mock_s2_cut(J, mode));
+        A.l2_min_f = f_up(4.0 * S * S * (1.0 + 1e-5));
+        const double epi = mock_pi_err(S, qm);
+        if (mode == MODE_RPPI_MOCK) {
+            A.pimax = J->pimax;
+            A.inv_dpi = 1.0 / (J->pimax / J->npibin);
+            A.pimax_lo_f = f_down(J->pimax - 2.0 * epi);
+            A.pimax_hi_f = f_up(J->pimax + 2.0 * epi);
+            A.inv_dpi_f = (float)A.inv_dpi;
+            A.pibin_band = (float)(2.0 * (epi * A.inv_dpi + 3.0 * 5.96e-8 * (double)J->npibin + 1e-12));
+            A.inv_dpi256_f = (float)(A.inv_dpi * 256.0);
+            A.pi_band_q = (int)ceil(A.pibin_band * 256.0) + 2;
+            if ((double)J->npibin * 256.0 > 4.0e6 || A.pi_band_q > 100) A.pi_band_q = 128;  // everything slow
+        } else {
+            A.sqr_mu_max = J->mu_max * J->mu_max;
+            A.inv_dmu = 1.0 / (J->mu_max / J->npibin);
+            A.mu_max_f = (float)J->mu_max;
+            A.inv_dmu_f = (float)A.inv_dmu;
+            // |mu_f - mu| <= |pi_f - pi| / |s| + mu (8u + 5u + u) + 3.5uq / |s|
+            A.mu_band_abs = (float)(2.0 * (4.0 * u * qm + 3.5 * u * qm));
+            A.mu_band_rel = (float)(2.0 * (24.0 * u + 14.0 * u) + 1e-12);
+        }
     }
     if (mode == MODE_RPPI || mode == MODE_WP) {
         A.pimax = J->pimax;
