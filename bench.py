@@ -49,6 +49,11 @@ WORKLOADS["cfg5"] = dict(workload="batched DD cross-correlations: 64 clustered c
                           nbatch=64, nmin=50_000, nmax=500_000, n2=5_000_000, boxsize=1000.0, nbins=20, rmin=0.1,
                           rmax=25.0, size_seed=100, seeds="0-63", random_seed=1000, weights="U[0.5,1.5]",
                           kind="batched", autocorr=0)
+WORKLOADS["survey"] = dict(workload="DDrppi_mocks auto-correlation of a synthetic redshift survey of 84,383 galaxies "
+                                    "(RA 110-266, DEC -4-70, cz 6,000-20,000 km/s, 60% in groups), cosmology 1, "
+                                    "pimax 40, 14 log rp bins 0.1-25, pair_product weights, float64",
+                           n1=84_383, n2=0, nbins=14, rmin=0.1, rmax=25.0, pimax=40.0, seeds=[5, 6],
+                           weights="U[0.5,1.5]", kind="survey", autocorr=1)
 WORKLOAD = dict(WORKLOADS["cfg2"])
 FLOP_PER_PAIR = 8  # 3 FADD + 1 FMUL + 2 FFMA per 3-D separation
 # dram__bytes_read.sum + dram__bytes_write.sum of one FP32 pair-kernel launch per workload, from
@@ -414,6 +419,11 @@ def run_reference_arm(args):
     rank, world, _ = _rank_env()
     if rank != 0:
         return
+    if WORKLOAD.get("kind") == "survey":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference's DDrppi_mocks sources include GSL "
+                          "headers and GSL is not installed, so it cannot be built here; the survey line reports the "
+                          "oracle port as its cpu_baseline"}))
+        return
     if WORKLOAD.get("kind") == "batched":
         cats, rand, bins = make_batch_workload()
         times, works = [], []
@@ -467,6 +477,108 @@ def run_reference_arm(args):
     print(json.dumps(line))
 
 
+SURVEY_METRIC = "catalogue pairs/sec (N(N-1)/2 per call), DDrppi_mocks auto-correlation"
+# FP32 operations of one survey pair in the classification (s, l, s.s, l.l, s.l, rsqrt, pi, s x l,
+# |s x l|^2 / |l|^2; an FMA counts two)
+SURVEY_FLOP_PER_PAIR = 48
+
+
+def run_survey_workload(args):
+    """DDrppi_mocks (countpairs_mocks) on the survey workload: device time of the count (upload,
+    lattice, work list, pair kernel; the RA/DEC/cz -> XYZ conversion is host work, as in the
+    reference) and the API call's wall time as e2e; DDsmu_mocks and vpf timed beside it."""
+    rank, world, local = _rank_env()
+    if rank != 0:
+        return
+    import torch
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    import corrfunc_gb300 as cf
+    from corrfunc_gb300 import catalogs as cat
+    from corrfunc_gb300 import mocks, theory
+    cf.set_precision(args.precision)
+    W = WORKLOAD
+    ra, dec, cz = cat.survey(W["n1"], W["seeds"][0], ra=(110.0, 266.0), dec=(-4.0, 70.0), cz=(6000.0, 20000.0))
+    w = cat.weights(W["n1"], W["seeds"][1])
+    bins = cat.log_bins(W["rmin"], W["rmax"], W["nbins"])
+
+    def call():
+        t0 = time.perf_counter()
+        r = mocks.DDrppi_mocks(1, 1, 1, W["pimax"], bins, ra.copy(), dec.copy(), cz.copy(), weights1=w,
+                               weight_type="pair_product", isa="fallback")
+        return r, time.perf_counter() - t0, cf.last_stats()
+
+    for _ in range(max(args.warmup, 3)):
+        ref, _, _ = call()
+        flush_l2(torch, dev)
+    npair = W["n1"] * (W["n1"] - 1) / 2.0
+    gpu_ms, pair_ms, walls, launches = [], [], [], 0
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            r, wall, st = call()
+            if not np.array_equal(r["npairs"], ref["npairs"]):
+                raise RuntimeError("non-deterministic pair counts between steps")
+            gpu_ms.append(st["total_gpu_ms"])
+            pair_ms.append(st["pair_kernel_ms"])
+            walls.append(wall)
+            launches += st["kernel_launches"]
+            flush_l2(torch, dev)
+    peak = ctypes.c_double()
+    lib = cf.library()
+    lib.cf_gpu_fp32_peak_tflops.argtypes = [ctypes.POINTER(ctypes.c_double)]
+    lib.cf_gpu_fp32_peak_tflops(ctypes.byref(peak))
+    pair_s = sum(pair_ms) / 1e3 / args.steps
+    achieved = st["pairs_evaluated"] * SURVEY_FLOP_PER_PAIR / pair_s / 1e12
+    line = {"metric": SURVEY_METRIC, "value": npair * args.steps / (sum(gpu_ms) / 1e3), "unit": "pairs/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": sum(gpu_ms) / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64-refine" if args.precision == "fp32_refine" else "f64",
+            "data": "synthetic (seeded survey catalogue, numpy PCG64)",
+            "config": dict(W, precision=args.precision, l2="flushed between steps (256 MB write)"),
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
+                         "frac": achieved / peak.value if peak.value else None, "traffic": None,
+                         "kernel": "k_pairs_f32<MODE_RPPI_MOCK,false,true>",
+                         "peak_source": "measured: FP32 FMA calibration kernel (cf_gpu_fp32_peak_tflops) in this run",
+                         "flop_per_pair": SURVEY_FLOP_PER_PAIR, "pairs_evaluated": st["pairs_evaluated"]},
+            "e2e": {"value": npair * args.steps / sum(walls), "unit": "pairs/s",
+                    "h2d_bytes_per_step": 4 * 8 * W["n1"], "d2h_bytes_per_step": 15 * 41 * 32,
+                    "ms_per_step": 1e3 * sum(walls) / args.steps},
+            "gpu_launches": launches,
+            "kernel_ms": {"pair_kernel": sum(pair_ms) / args.steps, "step_total": sum(gpu_ms) / args.steps},
+            "pairs": {"gpu_evaluated": st["pairs_evaluated"], "fp32_slow_path": st["pairs_slow"],
+                      "fp64_refined": st["pairs_refined"], "counted": int(np.sum(ref["npairs"]))},
+            "clocks": clocks.summary()}
+    beside = {}
+    for name, fn in [("DDsmu_mocks_ms", lambda: mocks.DDsmu_mocks(1, 1, 1, 1.0, 10, bins, ra.copy(), dec.copy(),
+                                                                  cz.copy(), isa="fallback")),
+                     ("DDrppi_mocks_rpavg_ms", lambda: mocks.DDrppi_mocks(1, 1, 1, W["pimax"], bins, ra.copy(),
+                                                                          dec.copy(), cz.copy(), output_rpavg=True,
+                                                                          isa="fallback"))]:
+        fn()
+        t = []
+        for _ in range(3):
+            fn()
+            t.append(cf.last_stats()["total_gpu_ms"])
+        beside[name] = min(t)
+    x4, y4, z4 = cat.clustered_box(1_000_000, 420.0, 3)
+    theory.vpf(10.0, 10, 100000, 6, -1234, x4, y4, z4, periodic=True, boxsize=420.0)
+    beside["vpf_1M_points_1e5_spheres_ms"] = cf.last_stats()["total_gpu_ms"]
+    line["beside"] = beside
+    if not args.no_cpu_baseline:
+        # the oracle's brute-force loop (the reference's mocks need GSL and do not build here) on
+        # all host threads, on the first 20,000 galaxies
+        sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "oracle"))
+        import oracle
+        n = 20000
+        t0 = time.perf_counter()
+        oracle.DDrppi_mocks(1, 1, W["pimax"], bins, ra[:n].copy(), dec[:n].copy(), cz[:n].copy(), weights1=w[:n],
+                            weight_type="pair_product")
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": n * (n - 1) / 2.0 / dt, "unit": "pairs/s", "cores": os.cpu_count(),
+                                "kind": "port", "sample": "first %d galaxies, one brute-force run" % n, "seconds": dt}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -484,6 +596,8 @@ def main():
         return run_reference_arm(args)
     if args.workload == "cfg5":
         return run_batch_workload(args)
+    if args.workload == "survey":
+        return run_survey_workload(args)
 
     rank, world, local = _rank_env()
     import torch
