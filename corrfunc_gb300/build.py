@@ -48,7 +48,7 @@ def build(verbose=False, extra_nvcc=()):
     jobs = []
     for c in ("cf_api.c", "cf_common.c", "cf_io.c"):
         obj = os.path.join(BUILD, c[:-2] + ".o")
-        jobs.append(["gcc", "-std=gnu11", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
+        jobs.append(["gcc", "-std=gnu11", "-O2", "-fPIC", "-ffp-contract=off", "-fopenmp", "-Wall", "-Wno-unused-function"]
                     + inc + ["-c", os.path.join(CSRC, c), "-o", obj])
     cu_objs = []
     for cu in ("cf_engine.cu", "cf_noalloc.cu"):
@@ -64,7 +64,7 @@ def build(verbose=False, extra_nvcc=()):
     objs = [os.path.join(BUILD, "cf_api.o"), os.path.join(BUILD, "cf_common.o"), os.path.join(BUILD, "cf_io.o")] + cu_objs
     tmp = LIB + ".tmp"
     _run([nvcc] + NVCC_ARCH + ["-shared", "-o", tmp] + objs
-         + ["-L" + os.path.join(cuda, "lib64"), "-lcudart_static", "-lpthread", "-ldl", "-lrt", "-lm"])
+         + ["-L" + os.path.join(cuda, "lib64"), "-lcudart_static", "-lpthread", "-ldl", "-lrt", "-lm", "-Xcompiler", "-fopenmp"])
     os.replace(tmp, LIB)
     build_python_modules(verbose)
     build_cli()

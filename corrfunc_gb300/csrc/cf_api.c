@@ -974,6 +974,7 @@ static int unit_vectors(int64_t n, const void *ra, const void *dec, const void *
     *Z = malloc(sizeof(double) * (n > 0 ? n : 1));
     *W = w ? malloc(sizeof(double) * (n > 0 ? n : 1)) : NULL;
     if (!*X || !*Y || !*Z || (w && !*W)) return EXIT_FAILURE;
+#pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; i++) {
         const double r = wval(ra, i, es), d = wval(dec, i, es);
         const double cd = cos(d * CF_PI_OVER_180);
@@ -1223,18 +1224,26 @@ static int mock_positions(int64_t n, const void *ra, const void *dec, const void
     *W = w ? malloc(sizeof(double) * m) : NULL;
     if (!*X || !*Y || !*Z || (w && !*W)) return EXIT_FAILURE;
     const double inv_c = 1.0 / CF_SPEED_OF_LIGHT;
+    int64_t bad = -1;
+#pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; i++) {
         double D = wval(cz, i, es);
         if (zc != NULL && interp_linear(zc, dcs, nz, D * inv_c, &D) != EXIT_SUCCESS) {
-            CF_ERR("cz[%lld] = %g is outside the comoving-distance table (z in [%g, %g])", (long long)i,
-                   wval(cz, i, es), zc[0], zc[nz - 1]);
-            return EXIT_FAILURE;
+#pragma omp critical
+            bad = (bad < 0 || i < bad) ? i : bad;
+            continue;
         }
         const double r = wval(ra, i, es), d = wval(dec, i, es);
-        (*X)[i] = D * cos(d * CF_PI_OVER_180) * cos(r * CF_PI_OVER_180);
-        (*Y)[i] = D * cos(d * CF_PI_OVER_180) * sin(r * CF_PI_OVER_180);
+        const double cd = cos(d * CF_PI_OVER_180);  /* the value the reference computes twice */
+        (*X)[i] = D * cd * cos(r * CF_PI_OVER_180);
+        (*Y)[i] = D * cd * sin(r * CF_PI_OVER_180);
         (*Z)[i] = D * sin(d * CF_PI_OVER_180);
         if (w) (*W)[i] = wval(w, i, es);
+    }
+    if (bad >= 0) {
+        CF_ERR("cz[%lld] = %g is outside the comoving-distance table (z in [%g, %g])", (long long)bad,
+               wval(cz, bad, es), zc[0], zc[nz - 1]);
+        return EXIT_FAILURE;
     }
     return EXIT_SUCCESS;
 }

@@ -69,6 +69,14 @@ constexpr int kZFine = CF_Z_SLABS;  // z slabs per rmax_z
 #ifndef CF_PAIR_GROUP
 #define CF_PAIR_GROUP 8
 #endif
+// survey modes: pairs per group and groups per unrolled loop body
+#ifndef CF_MOCK_GROUP
+#define CF_MOCK_GROUP 1
+#endif
+#ifndef CF_MOCK_UNROLL
+#define CF_MOCK_UNROLL 8
+#endif
+constexpr int kMockUnroll = CF_MOCK_UNROLL;
 
 constexpr int kScanTile = 4096;
 
@@ -1017,12 +1025,20 @@ __device__ __forceinline__ uint32_t tile_fast(const PairArgs &A, const float4 *_
 {
     uint32_t slowbits = 0;
     if (nj == 32) {
-        // the survey modes keep more values per pair in flight: smaller groups stay in registers
-        constexpr int kGroup = mode_is_mock(MODE) ? 2 : CF_PAIR_GROUP;
+        if (mode_is_mock(MODE)) {
+            // the survey modes keep more values per pair in flight and have longer bodies: small
+            // groups stay in registers and a partial unroll keeps the loop in the instruction cache
+            constexpr int kGroup = CF_MOCK_GROUP;
+#pragma unroll kMockUnroll
+            for (int k0 = 0; k0 < 32; k0 += kGroup)
+                pairs_group<MODE, NEED_AVG, NEED_W, OWN, kGroup>(A, sjhi, sjlo, lut, ascale, k0, jb, i, xi, yi, zi, xil,
+                                                                 yil, zil, wis, ax, ay, az, cnt_s, slowbits);
+            return slowbits;
+        }
 #pragma unroll
-        for (int k0 = 0; k0 < 32; k0 += kGroup)
-            pairs_group<MODE, NEED_AVG, NEED_W, OWN, kGroup>(A, sjhi, sjlo, lut, ascale, k0, jb, i, xi, yi, zi, xil, yil,
-                                                             zil, wis, ax, ay, az, cnt_s, slowbits);
+        for (int k0 = 0; k0 < 32; k0 += CF_PAIR_GROUP)
+            pairs_group<MODE, NEED_AVG, NEED_W, OWN, CF_PAIR_GROUP>(A, sjhi, sjlo, lut, ascale, k0, jb, i, xi, yi, zi, xil,
+                                                                    yil, zil, wis, ax, ay, az, cnt_s, slowbits);
     } else {
         for (int k = 0; k < nj; k++)
             pairs_group<MODE, NEED_AVG, NEED_W, OWN, 1>(A, sjhi, sjlo, lut, ascale, k, jb, i, xi, yi, zi, xil, yil, zil, wis,
