@@ -110,6 +110,7 @@ struct PairArgs {
     float s2_cut_f;                // FP32 |s|^2 at or above this: certainly beyond the largest separation
     float l2_min_f;                // FP32 |l|^2 below this (pairs near the observer): exact path
     float mu_band_rel;             // part of the mu error bound independent of |s|
+    int theta_series;              // angular averages: the arcsine series is exact for all counted chords
 
     // fixed-point scales for the per-warp accumulators
     const float *g_ascale;      // per separation bin: fixed-point scale of the separation sums

@@ -712,6 +712,22 @@ __device__ __noinline__ int refine_pair(const PairArgs &A, const double *se, uin
     return ref_eval<MODE>(A, se, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, -ox, -oy, -oz, avg_term);
 }
 
+// Angle in degrees subtended by a chord ch of the unit sphere, 2 asin(ch / 2).  For angular bins
+// up to 23 degrees (ch / 2 <= 0.2) the arcsine's Maclaurin series
+//   asin(x) = x (1 + x^2/6 + 3x^4/40 + 5x^6/112 + 35x^8/1152 + ...)
+// truncated after the x^9 term is within 3e-9 relative of it there, well inside FP32 rounding.
+template <bool SERIES>
+__device__ __forceinline__ float chord_degrees(float ch)
+{
+    const float x = 0.5f * ch;
+    if (SERIES) {
+        const float x2 = x * x;
+        const float p = fmaf(fmaf(fmaf(fmaf(35.f / 1152.f, x2, 5.f / 112.f), x2, 3.f / 40.f), x2, 1.f / 6.f), x2, 1.f);
+        return x * p * 114.59155902616465f;
+    }
+    return 2.f * asinf(x) * 57.29577951308232f;
+}
+
 // LUT bucket of the classified FP32 quantity q (r^2, rp^2, s^2 or chord^2): one mad.hi on the
 // float bits (bucket = (bits >> shift) - base), clamped to the reject entry lut_n.
 __device__ __forceinline__ uint32_t lut_bucket(const PairArgs &A, float q)
@@ -848,7 +864,7 @@ __device__ __noinline__ int slow_candidate(const PairArgs &A, const float *glo, 
             *favg = sqrtf(fmaf(dyp, dyp, dxp * dxp));
         } else if (MODE == MODE_THETA) {
             const float ch = sqrtf(fmaf(dzp, dzp, fmaf(dyp, dyp, dxp * dxp)));
-            *favg = 2.f * asinf(0.5f * ch) * 57.29577951308232f;
+            *favg = A.theta_series ? chord_degrees<true>(ch) : chord_degrees<false>(ch);
         } else {
             *favg = sqrtf(fmaf(dzp, dzp, fmaf(dyp, dyp, dxp * dxp)));
         }
@@ -877,7 +893,7 @@ __device__ __forceinline__ void red_shared_u32_at(uint32_t saddr, uint32_t v)
 // LUT entry is the byte offset of the histogram row the pair belongs to (a trash row when the
 // pair is rejected or deferred) with bit 31 set when the pair must go through the exact slow
 // path; the caller issues one unconditional conflict-free shared reduction per pair.
-template <int MODE, bool NEED_AVG, bool NEED_W, bool OWN>
+template <int MODE, bool NEED_AVG, bool NEED_W, bool OWN, bool SER>
 __device__ __forceinline__ uint32_t pair_offset(const PairArgs &A, const float4 *__restrict__ sjhi,
                                                 const float4 *__restrict__ sjlo, const uint32_t *__restrict__ lut,
                                                 const float *__restrict__ ascale, int k, uint32_t jb, uint32_t i, float xi, float yi, float zi,
@@ -973,7 +989,7 @@ __device__ __forceinline__ uint32_t pair_offset(const PairArgs &A, const float4 
             favg = sqrtf(fmaf(dyp, dyp, dxp * dxp));
         } else if (MODE == MODE_THETA) {
             const float ch = sqrtf(fmaf(dzp, dzp, fmaf(dyp, dyp, dxp * dxp)));
-            favg = 2.f * asinf(0.5f * ch) * 57.29577951308232f;
+            favg = chord_degrees<SER>(ch);
         } else {
             favg = sqrtf(fmaf(dzp, dzp, fmaf(dyp, dyp, dxp * dxp)));
         }
@@ -982,7 +998,7 @@ __device__ __forceinline__ uint32_t pair_offset(const PairArgs &A, const float4 
     return off;
 }
 
-template <int MODE, bool NEED_AVG, bool NEED_W, bool OWN, int U>
+template <int MODE, bool NEED_AVG, bool NEED_W, bool OWN, bool SER, int U>
 __device__ __forceinline__ void pairs_group(const PairArgs &A, const float4 *__restrict__ sjhi,
                                             const float4 *__restrict__ sjlo, const uint32_t *__restrict__ lut,
                                             const float *__restrict__ ascale, int k0,
@@ -997,7 +1013,7 @@ __device__ __forceinline__ void pairs_group(const PairArgs &A, const float4 *__r
         uint32_t sl;
         vw[u] = 0;
         va[u] = 0;
-        off[u] = pair_offset<MODE, NEED_AVG, NEED_W, OWN>(A, sjhi, sjlo, lut, ascale, k0 + u, jb, i, xi, yi, zi, xil, yil, zil,
+        off[u] = pair_offset<MODE, NEED_AVG, NEED_W, OWN, SER>(A, sjhi, sjlo, lut, ascale, k0 + u, jb, i, xi, yi, zi, xil, yil, zil,
                                                           wis, ax, ay, az, sl, vw[u], va[u]);
         slowbits = __funnelshift_l(sl, slowbits, 1);  // pair k of n ends at bit n - 1 - k
     }
@@ -1016,7 +1032,7 @@ __device__ __forceinline__ void pairs_group(const PairArgs &A, const float4 *__r
     }
 }
 
-template <int MODE, bool NEED_AVG, bool NEED_W, bool OWN>
+template <int MODE, bool NEED_AVG, bool NEED_W, bool OWN, bool SER>
 __device__ __forceinline__ uint32_t tile_fast(const PairArgs &A, const float4 *__restrict__ sjhi,
                                               const float4 *__restrict__ sjlo, const uint32_t *__restrict__ lut,
                                               const float *__restrict__ ascale, int nj,
@@ -1031,17 +1047,17 @@ __device__ __forceinline__ uint32_t tile_fast(const PairArgs &A, const float4 *_
             constexpr int kGroup = CF_MOCK_GROUP;
 #pragma unroll kMockUnroll
             for (int k0 = 0; k0 < 32; k0 += kGroup)
-                pairs_group<MODE, NEED_AVG, NEED_W, OWN, kGroup>(A, sjhi, sjlo, lut, ascale, k0, jb, i, xi, yi, zi, xil,
+                pairs_group<MODE, NEED_AVG, NEED_W, OWN, SER, kGroup>(A, sjhi, sjlo, lut, ascale, k0, jb, i, xi, yi, zi, xil,
                                                                  yil, zil, wis, ax, ay, az, cnt_s, slowbits);
             return slowbits;
         }
 #pragma unroll
         for (int k0 = 0; k0 < 32; k0 += CF_PAIR_GROUP)
-            pairs_group<MODE, NEED_AVG, NEED_W, OWN, CF_PAIR_GROUP>(A, sjhi, sjlo, lut, ascale, k0, jb, i, xi, yi, zi, xil,
+            pairs_group<MODE, NEED_AVG, NEED_W, OWN, SER, CF_PAIR_GROUP>(A, sjhi, sjlo, lut, ascale, k0, jb, i, xi, yi, zi, xil,
                                                                     yil, zil, wis, ax, ay, az, cnt_s, slowbits);
     } else {
         for (int k = 0; k < nj; k++)
-            pairs_group<MODE, NEED_AVG, NEED_W, OWN, 1>(A, sjhi, sjlo, lut, ascale, k, jb, i, xi, yi, zi, xil, yil, zil, wis,
+            pairs_group<MODE, NEED_AVG, NEED_W, OWN, SER, 1>(A, sjhi, sjlo, lut, ascale, k, jb, i, xi, yi, zi, xil, yil, zil, wis,
                                                         ax, ay, az, cnt_s, slowbits);
     }
     return slowbits;
@@ -1206,10 +1222,19 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
             if (nj > kPadMin) nj = 32;
             __syncwarp();
             const float wi_s = pi.w * A.w_scale_f;
-            uint32_t slowbits = own ? tile_fast<MODE, NEED_AVG, NEED_W, true>(A, sjhi, sjlo, lut, h.ascale, nj, jb, i, xi, yi, zi,
-                                                                           xil, yil, zil, wi_s, ax, ay, az, cnt_s)
-                                    : tile_fast<MODE, NEED_AVG, NEED_W, false>(A, sjhi, sjlo, lut, h.ascale, nj, jb, i, xi, yi,
-                                                                            zi, xil, yil, zil, wi_s, ax, ay, az, cnt_s);
+            uint32_t slowbits;
+            if (MODE == MODE_THETA && NEED_AVG && A.theta_series) {
+                // angular averages by the arcsine series: a separate copy of the unrolled tile loop
+                slowbits = own ? tile_fast<MODE, NEED_AVG, NEED_W, true, true>(A, sjhi, sjlo, lut, h.ascale, nj, jb, i, xi,
+                                                                             yi, zi, xil, yil, zil, wi_s, ax, ay, az, cnt_s)
+                               : tile_fast<MODE, NEED_AVG, NEED_W, false, true>(A, sjhi, sjlo, lut, h.ascale, nj, jb, i, xi,
+                                                                              yi, zi, xil, yil, zil, wi_s, ax, ay, az, cnt_s);
+            } else {
+                slowbits = own ? tile_fast<MODE, NEED_AVG, NEED_W, true, false>(A, sjhi, sjlo, lut, h.ascale, nj, jb, i, xi,
+                                                                              yi, zi, xil, yil, zil, wi_s, ax, ay, az, cnt_s)
+                               : tile_fast<MODE, NEED_AVG, NEED_W, false, false>(A, sjhi, sjlo, lut, h.ascale, nj, jb, i, xi,
+                                                                               yi, zi, xil, yil, zil, wi_s, ax, ay, az, cnt_s);
+            }
             // candidates in flagged buckets go to the warp's slow queue, one bit per lane per round
             // (a round appends at most 32 entries, so the queue never holds more than 63)
             while (true) {
@@ -2082,6 +2107,11 @@ static void pair_constants(PairArgs &A, const cf_job *J, int mode, int nbins, bo
     A.autocorr = autocorr;
     A.fma_formula = J->fma_formula;
     A.chord_formula = J->chord_formula;
+    A.theta_series = 0;
+    if (mode == MODE_THETA && J->nedges > 0) {
+        const double cmin = J->edges[J->nedges - 1];  // cos of the largest angle counted
+        A.theta_series = 0.5 * sqrt(fmax(0.0, 2.0 * (1.0 - cmin))) <= 0.2 ? 1 : 0;
+    }
     for (int a = 0; a < 3; a++) {
         for (int m = -1; m <= 1; m++) {
             const double o = (G.periodic[a]) ? m * geo.wrap[a] : 0.0;
