@@ -77,6 +77,20 @@ constexpr int kZFine = CF_Z_SLABS;  // z slabs per rmax_z
 #define CF_MOCK_UNROLL 8
 #endif
 constexpr int kMockUnroll = CF_MOCK_UNROLL;
+// Tile loops are unrolled only partly: the full 32-pair unroll overflows the instruction cache
+// once a pair's body grows (measured on this GPU: rp-pi, wp, s-mu and angular averages 1.4-2.2x,
+// weighted DD(r) 13 %, DD(r) with averages 1.8x faster than the full unroll).  Angular counts
+// without averages keep the full unroll.
+#ifndef CF_2D_GROUP
+#define CF_2D_GROUP 4
+#endif
+#ifndef CF_2D_UNROLL
+#define CF_2D_UNROLL 2
+#endif
+#ifndef CF_R3_UNROLL
+#define CF_R3_UNROLL 2
+#endif
+constexpr int kR3Unroll = CF_R3_UNROLL;
 
 constexpr int kScanTile = 4096;
 
@@ -1041,20 +1055,20 @@ __device__ __forceinline__ uint32_t tile_fast(const PairArgs &A, const float4 *_
 {
     uint32_t slowbits = 0;
     if (nj == 32) {
-        if (mode_is_mock(MODE)) {
-            // the survey modes keep more values per pair in flight and have longer bodies: small
-            // groups stay in registers and a partial unroll keeps the loop in the instruction cache
-            constexpr int kGroup = CF_MOCK_GROUP;
-#pragma unroll kMockUnroll
-            for (int k0 = 0; k0 < 32; k0 += kGroup)
-                pairs_group<MODE, NEED_AVG, NEED_W, OWN, SER, kGroup>(A, sjhi, sjlo, lut, ascale, k0, jb, i, xi, yi, zi, xil,
-                                                                 yil, zil, wis, ax, ay, az, cnt_s, slowbits);
-            return slowbits;
-        }
-#pragma unroll
-        for (int k0 = 0; k0 < 32; k0 += CF_PAIR_GROUP)
-            pairs_group<MODE, NEED_AVG, NEED_W, OWN, SER, CF_PAIR_GROUP>(A, sjhi, sjlo, lut, ascale, k0, jb, i, xi, yi, zi, xil,
-                                                                    yil, zil, wis, ax, ay, az, cnt_s, slowbits);
+        // group size (pairs whose table offsets are computed before their reductions) and
+        // groups per unrolled loop body, per mode
+        constexpr bool kMock = mode_is_mock(MODE);
+        constexpr bool kFull = MODE == MODE_THETA && !NEED_AVG;
+        constexpr int kGroup = kMock ? CF_MOCK_GROUP
+                               : kFull ? CF_PAIR_GROUP
+                               : MODE == MODE_R3 ? (NEED_AVG ? 4 : CF_PAIR_GROUP) : CF_2D_GROUP;
+        constexpr int kUnroll = kMock ? kMockUnroll
+                                : kFull ? 32 / CF_PAIR_GROUP
+                                : MODE == MODE_R3 ? (NEED_AVG ? 2 : kR3Unroll) : CF_2D_UNROLL;
+#pragma unroll kUnroll
+        for (int k0 = 0; k0 < 32; k0 += kGroup)
+            pairs_group<MODE, NEED_AVG, NEED_W, OWN, SER, kGroup>(A, sjhi, sjlo, lut, ascale, k0, jb, i, xi, yi, zi, xil,
+                                                                  yil, zil, wis, ax, ay, az, cnt_s, slowbits);
     } else {
         for (int k = 0; k < nj; k++)
             pairs_group<MODE, NEED_AVG, NEED_W, OWN, SER, 1>(A, sjhi, sjlo, lut, ascale, k, jb, i, xi, yi, zi, xil, yil, zil, wis,
