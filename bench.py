@@ -59,7 +59,7 @@ FLOP_PER_PAIR = 8  # 3 FADD + 1 FMUL + 2 FFMA per 3-D separation
 # dram__bytes_read.sum + dram__bytes_write.sum of one FP32 pair-kernel launch per workload, from
 # the ncu captures summarised in profiles/k_pairs_f32_cfg2_dram_traffic.md and
 # profiles/k_pairs_f32_northstar_full.md
-PAIR_KERNEL_TRAFFIC_BYTES = {"cfg2": 220_951_552 + 3_993_088, "northstar": 54_269_184 + 2_131_200}
+PAIR_KERNEL_TRAFFIC_BYTES = {"cfg2": 220_196_096 + 3_340_544, "northstar": 54_269_184 + 2_131_200}
 
 
 def _rank_env():

@@ -134,3 +134,42 @@ def test_mocks_errors_raise():
         mocks.DDsmu_mocks(1, 1, 1, 1.5, 5, bins, ra.copy(), dec.copy(), cz.copy())
     with pytest.raises(ValueError):
         mocks.DDrppi_mocks(0, 1, 1, 10.0, bins, ra.copy(), dec.copy(), cz.copy())
+
+
+def test_mocks_near_the_observer_and_fine_bins(orc):
+    """Galaxies from 1 to 40 Mpc/h: many pairs lie closer to the observer than twice the largest
+    separation, where the FP32 line-of-sight bound does not hold and the pair goes to FP64; fine rp
+    bins from 0.1 with weights and rpavg (every counted pair re-evaluated)."""
+    from corrfunc_gb300 import catalogs as cat
+    from corrfunc_gb300 import mocks
+    ra, dec, cz, w = _survey(9000, 61, cz=(100.0, 4000.0), ra=(0.0, 360.0), dec=(-60.0, 60.0))
+    bins = cat.log_bins(0.1, 15.0, 14)
+    kw = dict(weights1=w, weight_type="pair_product", output_rpavg=True)
+    got = mocks.DDrppi_mocks(1, 1, 1, 20.0, bins, ra.copy(), dec.copy(), cz.copy(), **kw)
+    want = orc.DDrppi_mocks(1, 1, 20.0, bins, ra.copy(), dec.copy(), cz.copy(), **kw)
+    assert got["npairs"].sum() > 0
+    _check(got, want, "rpavg")
+    got = mocks.DDsmu_mocks(1, 1, 1, 0.7, 14, bins, ra.copy(), dec.copy(), cz.copy(), output_savg=True)
+    want = orc.DDsmu_mocks(1, 1, 0.7, 14, bins, ra.copy(), dec.copy(), cz.copy(), output_savg=True)
+    _check(got, want, "savg")
+
+
+@pytest.mark.parametrize("precision", ["fp32_refine", "fp64"])
+def test_mocks_mr19_sized_survey(orc, precision):
+    """A survey of the reference test's size and footprint (40,000 galaxies of the 84,383, 14 rp bins
+    0.1-25, pimax 40): both precisions give the oracle's counts."""
+    import corrfunc_gb300 as cf
+    from corrfunc_gb300 import catalogs as cat
+    from corrfunc_gb300 import mocks
+    ra, dec, cz, w = _survey(40000, 71, ra=(110.0, 266.0), dec=(-4.0, 70.0), cz=(6000.0, 20000.0))
+    bins = cat.log_bins(0.1, 25.0, 14)
+    old = cf.get_precision()
+    cf.set_precision(precision)
+    try:
+        got = mocks.DDrppi_mocks(1, 1, 1, 40.0, bins, ra.copy(), dec.copy(), cz.copy(), weights1=w,
+                                 weight_type="pair_product")
+    finally:
+        cf.set_precision(old)
+    want = orc.DDrppi_mocks(1, 1, 40.0, bins, ra.copy(), dec.copy(), cz.copy(), weights1=w, weight_type="pair_product")
+    assert np.array_equal(got["npairs"], want["npairs"])
+    np.testing.assert_allclose(got["weightavg"], want["weightavg"], rtol=RTOL_AVG, atol=1e-9)
