@@ -921,13 +921,12 @@ __device__ __forceinline__ uint32_t pair_offset(const PairArgs &A, const float4 
         const float q = fmaxf(MODE == MODE_RPPI_MOCK ? rp2 : s2, A.q_floor);
         const uint32_t e = lut[lut_bucket(A, q)];
         uint32_t off = e & 0x003fffffu, sl = e;
-        if (OWN) {
-            const bool keep = jb + (uint32_t)k > i;
-            off = keep ? off : A.trash_off;
-            sl = keep ? sl : 0u;
-        }
+        // own column of an auto-correlation: only j > i (every outcome below is masked by keep)
+        const bool keep = !OWN || jb + (uint32_t)k > i;
+        off = keep ? off : A.trash_off;
+        sl = keep ? sl : 0u;
         const bool real = off != A.trash_off;
-        const bool near = !(l2 >= A.l2_min_f);  // also NaN (padding far away)
+        const bool near = keep && !(l2 >= A.l2_min_f);  // also NaN (padding far away)
         bool rej, amb;
         uint32_t add;
         if (MODE == MODE_RPPI_MOCK) {
