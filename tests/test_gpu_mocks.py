@@ -173,3 +173,22 @@ def test_mocks_mr19_sized_survey(orc, precision):
     want = orc.DDrppi_mocks(1, 1, 40.0, bins, ra.copy(), dec.copy(), cz.copy(), weights1=w, weight_type="pair_product")
     assert np.array_equal(got["npairs"], want["npairs"])
     np.testing.assert_allclose(got["weightavg"], want["weightavg"], rtol=RTOL_AVG, atol=1e-9)
+
+
+@pytest.mark.parametrize("avg", [False, True])
+def test_mocks_deep_survey(orc, avg):
+    """cz from 100,000 to 250,000 km/s (comoving distances near 1,000-2,000 Mpc/h): the hi grid is
+    coarse and |x| large; counts stay exact."""
+    from corrfunc_gb300 import catalogs as cat
+    from corrfunc_gb300 import mocks
+    ra, dec, cz, w = _survey(12000, 81, ra=(150.0, 160.0), dec=(0.0, 8.0), cz=(100000.0, 250000.0))
+    bins = cat.log_bins(0.5, 30.0, 10)
+    kw = dict(weights1=w, weight_type="pair_product", output_rpavg=avg)
+    got = mocks.DDrppi_mocks(1, 2, 1, 30.0, bins, ra.copy(), dec.copy(), cz.copy(), **kw)
+    want = orc.DDrppi_mocks(1, 2, 30.0, bins, ra.copy(), dec.copy(), cz.copy(), **kw)
+    assert got["npairs"].sum() > 0
+    _check(got, want, "rpavg")
+    kw = dict(output_savg=avg)
+    got = mocks.DDsmu_mocks(1, 2, 1, 1.0, 8, bins, ra.copy(), dec.copy(), cz.copy(), **kw)
+    want = orc.DDsmu_mocks(1, 2, 1.0, 8, bins, ra.copy(), dec.copy(), cz.copy(), **kw)
+    _check(got, want, "savg")
