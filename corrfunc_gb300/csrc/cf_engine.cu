@@ -1522,6 +1522,15 @@ static int engine_init(void)
     g_eng.smem_per_sm = prop.sharedMemPerMultiprocessor;
     CF_CUDA(cudaStreamCreateWithFlags(&g_eng.stream, cudaStreamNonBlocking));
     for (int k = 0; k < 6; k++) CF_CUDA(cudaEventCreate(&g_eng.ev[k]));
+    // CF_PAIR_LAYOUT="<lane stride>,<warps per block>" fixes the FP32 pair kernel's histogram
+    // layout instead of the scored choice (for layout measurements)
+    const char *lay = getenv("CF_PAIR_LAYOUT");
+    int ls = 0, wp = 0;
+    if (lay && sscanf(lay, "%d,%d", &ls, &wp) == 2 && (ls == 1 || ls == 4 || ls == 8 || ls == 16 || ls == 32) &&
+        (wp == 4 || wp == 8 || wp == 16)) {
+        g_eng.force_ls = ls;
+        g_eng.force_warps = wp;
+    }
     g_eng.init = true;
     return EXIT_SUCCESS;
 }
