@@ -782,6 +782,36 @@ def extras(lib, C, cf, torch, dev, args):
     return out
 
 
+def reference_cpu_beside(x, y, z, rp, sb, ra, dec, tb, L):
+    """The reference's own DDrppi / wp / DDsmu (oracle/_ref, all host threads, FALLBACK kernels on
+    aarch64) on the full configuration-3 workload, and its DDtheta on the first 200,000 points of the
+    configuration-4 cap (with the full-size estimate scaled by the number of point pairs)."""
+    from corrfunc_gb300 import _capi as C
+    from corrfunc_gb300 import mocks, theory
+    out = {}
+    nt = os.cpu_count() or 1
+    libs = {m: os.path.join(ROOT, "oracle", "_ref", "libcf_ref_%s.so" % m) for m in ("DDrppi", "wp", "DDsmu", "DDtheta")}
+    if not all(os.path.exists(v) for v in libs.values()):
+        return {"reference_cpu": "reference libraries not built in oracle/_ref"}
+    runs = {"cfg3_DDrppi": lambda lib: theory.run_DDrppi(lib, 1, nt, 40.0, rp, x, y, z, boxsize=L, isa="fastest"),
+            "cfg3_wp": lambda lib: theory.run_wp(lib, L, 40.0, nt, rp, x, y, z, isa="fastest"),
+            "cfg3_DDsmu": lambda lib: theory.run_DDsmu(lib, 1, nt, sb, 1.0, 10, x, y, z, boxsize=L, isa="fastest")}
+    mod = {"cfg3_DDrppi": "DDrppi", "cfg3_wp": "wp", "cfg3_DDsmu": "DDsmu"}
+    for name, fn in runs.items():
+        lib = C.bind(libs[mod[name]])
+        t0 = time.perf_counter()
+        fn(lib)
+        out["%s_reference_cpu_s" % name] = {"seconds": time.perf_counter() - t0, "cores": nt, "sample": "full workload"}
+    n = 200_000
+    lib = C.bind(libs["DDtheta"])
+    t0 = time.perf_counter()
+    mocks.run_DDtheta_mocks(lib, 1, nt, tb, ra[:n].copy(), dec[:n].copy(), output_thetaavg=True, isa="fastest")
+    dt = time.perf_counter() - t0
+    out["cfg4_DDtheta_reference_cpu_s"] = {"seconds": dt, "cores": nt, "sample": "first %d of %d points" % (n, len(ra)),
+                                           "full_size_estimate_s": dt * (len(ra) / n) ** 2}
+    return out
+
+
 def other_counters(cf, cat, theory):
     """The other pair counters on the survey's configurations 3 and 4 (timing only; units are the
     GPU's own evaluated pairs and the pairs counted, since the reference-lattice work unit is
@@ -816,6 +846,7 @@ def other_counters(cf, cat, theory):
     # counts in spheres: 1M clustered points in L=420, spheres up to radius 10, 10 radii, p0..p5
     runs["vpf_1M_nc1e4"] = lambda: theory.vpf(10.0, 10, 10000, 6, -1234, x4, y4, z4, periodic=True, boxsize=420.0)
     runs["vpf_1M_nc1e6"] = lambda: theory.vpf(10.0, 10, 1000000, 6, -1234, x4, y4, z4, periodic=True, boxsize=420.0)
+    out.update(reference_cpu_beside(x, y, z, rp, sb, ra, dec, tb, L))
     for name, fn in runs.items():
         for prec in ("fp64", "fp32_refine"):
             cf.set_precision(prec)
