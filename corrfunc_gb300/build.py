@@ -66,9 +66,25 @@ def build(verbose=False, extra_nvcc=()):
     _run([nvcc] + NVCC_ARCH + ["-shared", "-o", tmp] + objs
          + ["-L" + os.path.join(cuda, "lib64"), "-lcudart_static", "-lpthread", "-ldl", "-lrt", "-lm", "-Xcompiler", "-fopenmp"])
     os.replace(tmp, LIB)
+    link_module_names()
     build_python_modules(verbose)
     build_cli()
     return LIB
+
+
+# the reference's per-module library names (theory/*/Makefile, mocks/*/Makefile: LIBNAME)
+MODULE_LIBS = ("countpairs", "countpairs_rp_pi", "countpairs_s_mu", "countpairs_wp", "countpairs_xi", "countspheres",
+               "countpairs_theta_mocks", "countpairs_rp_pi_mocks", "countpairs_s_mu_mocks", "countspheres_mocks")
+
+
+def link_module_names():
+    """lib<module>.so links to libcorrfunc_gb300.so, so that -l<module> link lines of programs built
+    against the reference's per-module libraries resolve to this library."""
+    for name in MODULE_LIBS:
+        link = os.path.join(HERE, "lib%s.so" % name)
+        if os.path.lexists(link):
+            os.remove(link)
+        os.symlink(os.path.basename(LIB), link)
 
 
 CLI_COMMANDS = ("DD", "DDrppi", "DDsmu", "wp", "xi", "vpf", "DDtheta_mocks", "DDrppi_mocks", "DDsmu_mocks", "vpf_mocks")

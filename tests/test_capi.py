@@ -314,3 +314,70 @@ def test_no_gpu_fails_loudly_not_silently(lib):
     x = np.linspace(1.0, 9.0, 50)
     with pytest.raises(RuntimeError):
         theory.DD(1, 1, [0.5, 1.0, 2.0], x, x, x, boxsize=10.0)
+
+
+COMPAT_PROGRAM = r"""
+/* a program written against the reference's per-module headers and libraries */
+#include <stdio.h>
+#include <stdlib.h>
+#include "countpairs.h"
+#include "countpairs_rp_pi_mocks.h"
+#include "io.h"
+
+int main(int argc, char **argv)
+{
+    if (argc < 3) return 2;
+    double *x = NULL, *y = NULL, *z = NULL;
+    const int64_t n = read_positions(argv[1], "a", sizeof(double), 3, &x, &y, &z);
+    if (n <= 0) return 3;
+    struct config_options options = get_config_options();
+    options.boxsize = 100.0;
+    results_countpairs res;
+    if (countpairs(n, x, y, z, n, x, y, z, 4, 1, argv[2], &res, &options, NULL) != EXIT_SUCCESS) return 1;
+    for (int i = 1; i < res.nbin; i++) printf("%llu\n", (unsigned long long)res.npairs[i]);
+    free_results(&res);
+    free(x); free(y); free(z);
+    return 0;
+}
+"""
+
+
+def _build_compat(tmp_path):
+    import shutil
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "prog.c"
+    src.write_text(COMPAT_PROGRAM)
+    exe = tmp_path / "prog"
+    libdir = os.path.join(ROOT, "corrfunc_gb300")
+    r = subprocess.run(["gcc", "-std=c99", str(src), "-o", str(exe), "-I", os.path.join(ROOT, "include", "compat"),
+                        "-L" + libdir, "-lcountpairs", "-lcountpairs_rp_pi_mocks", "-Wl,-rpath," + libdir, "-lm"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return str(exe)
+
+
+def test_reference_header_and_library_names_build(tmp_path, lib):
+    """-I include/compat and -l<module> (the reference's per-module header and library names) build a
+    reference program unchanged; without a GPU it fails loudly with the library's message."""
+    exe = _build_compat(tmp_path)
+    pts = tmp_path / "pts.txt"
+    rng = np.random.default_rng(1)
+    np.savetxt(str(pts), rng.uniform(0, 100.0, (500, 3)))
+    bins = tmp_path / "bins"
+    bins.write_text("0.5 1.0\n1.0 5.0\n5.0 10.0\n")
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    r = subprocess.run([exe, str(pts), str(bins)], capture_output=True, text=True, timeout=300)
+    if has_gpu:
+        assert r.returncode == 0, r.stderr
+        from corrfunc_gb300 import theory
+        x, y, z = np.loadtxt(str(pts)).T
+        want = theory.DD(1, 4, [0.5, 1.0, 5.0, 10.0], x, y, z, periodic=True, boxsize=100.0)
+        assert [int(v) for v in r.stdout.split()] == list(want["npairs"])
+    else:
+        assert r.returncode == 1
+        assert "no CUDA device" in r.stderr or "corrfunc_gb300" in r.stderr
