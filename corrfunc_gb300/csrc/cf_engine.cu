@@ -120,7 +120,84 @@ struct Geom {
     unsigned long long *extent_err;
     double chk_lo[3], chk_hi[3];
     double chk_wmax;
+    // Integer view of the coordinates (the lattice kernels run no FP64 arithmetic: on this GPU
+    // the FP64 pipe issues at 1/64 of the FP32 rate).  A coordinate x becomes the fixed-point
+    // integer X = round(x / 2^e_fix) modulo 2^64 (e_fix = log2(q) - 31); the differences
+    // X - o_hi and X - o_cell are exact and give the hi / lo split and the cell index.
+    int e_fix[3];
+    unsigned long long o_hi[3], o_cell[3];  // X of hi_origin and of origin
+    float q_f[3], rho_f[3], inv_s_f[3];     // q, 2^e_fix, 1 / s
+    float eps_cell[3];                      // bound on the position error of the FP32 cell index
+    // order keys (okey0) of the extent checks, and of the range of coordinates that are inside
+    // the reference lattice whatever the rounding of its FP64 cell index (others take the exact test)
+    unsigned long long k_chk_lo[3], k_chk_hi[3], k_chk_wmax;
+    unsigned long long k_ref_lo[3], k_ref_hi[3];
+    // fixed-point X of ref_min (FP32 estimate of the reference cell index)
+    unsigned long long o_ref[3];
+    float ref_inv_f[3], ref_tol_f[3];  // 1 / reference cell, absolute error term of the estimate
+    // lo parts of the lattice records are written only for separation averages and survey modes
+    int write_lo;
 };
+
+// round(x / 2^e) modulo 2^64 of a finite double / float from its bits (ties away from zero)
+__host__ __device__ inline unsigned long long fix_round(unsigned long long m, int t, bool neg)
+{
+    unsigned long long v;
+    if (t >= 0) v = t >= 64 ? 0ull : m << t;
+    else v = -t >= 64 ? 0ull : ((m >> (-t - 1)) + 1ull) >> 1;
+    return neg ? 0ull - v : v;
+}
+__host__ __device__ inline unsigned long long fix_of(double x, int e)
+{
+    unsigned long long b;
+#ifdef __CUDA_ARCH__
+    b = (unsigned long long)__double_as_longlong(x);
+#else
+    memcpy(&b, &x, sizeof(b));
+#endif
+    int E = (int)((b >> 52) & 0x7ffu);
+    unsigned long long m = b & 0xfffffffffffffull;
+    if (E) m |= 1ull << 52;
+    else E = 1;
+    return fix_round(m, E - 1075 - e, (b >> 63) != 0);
+}
+__host__ __device__ inline unsigned long long fix_of(float x, int e)
+{
+    uint32_t b;
+#ifdef __CUDA_ARCH__
+    b = __float_as_uint(x);
+#else
+    memcpy(&b, &x, sizeof(b));
+#endif
+    int E = (int)((b >> 23) & 0xffu);
+    unsigned long long m = b & 0x7fffffu;
+    if (E) m |= 1ull << 23;
+    else E = 1;
+    return fix_round(m, E - 150 - e, (b >> 31) != 0);
+}
+
+// U = (x - origin) / 2^e_fix as N * 2^31 + L (N the nearest integer to U / 2^31, |L| <= 2^30):
+// hi = N q exactly (|N| < 2^24), lo = L 2^e_fix rounded once
+__device__ __forceinline__ void fix_split(unsigned long long U, float q, float rho, float *hi, float *lo)
+{
+    const long long N = ((long long)U + (1ll << 30)) >> 31;
+    const int L = (int)(long long)(U - ((unsigned long long)N << 31));
+    *hi = (float)(int)N * q;
+    *lo = (float)L * rho;
+}
+
+// order key of a double with -0 mapped to +0 (so that key order is the IEEE comparison order)
+__host__ __device__ inline unsigned long long okey0(double v)
+{
+    unsigned long long u;
+#ifdef __CUDA_ARCH__
+    u = (unsigned long long)__double_as_longlong(v);
+#else
+    memcpy(&u, &v, sizeof(u));
+#endif
+    if ((u << 1) == 0) u = 0;
+    return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
 
 __device__ __forceinline__ unsigned long long ord_enc(double v)
 {
@@ -140,9 +217,9 @@ template <typename T>
 __device__ __forceinline__ double ld(const T *p, int64_t i) { return (double)p[i]; }
 
 // Data extent.  Values are compared as order-preserving unsigned keys (integer min/max on the
-// ALU pipe; double min/max would run on the slow FP64 pipe): per block into partials[block][0..7]
-// (xmin, xmax, ymin, ymax, zmin, zmax keys, max |w| bits, non-finite flag), then one block folds
-// the partials into mm (slots as above, ord_enc of the double values) with a few atomics.
+// ALU pipe; double min/max would run on the slow FP64 pipe); every block folds its extremes
+// (xmin, xmax, ymin, ymax, zmin, zmax, max |w|, non-finite flag) into mm[0..7] (ord_enc of the
+// double values) with one atomic per slot.
 __device__ __forceinline__ uint32_t okey(float v)
 {
     const uint32_t u = __float_as_uint(v);
@@ -192,23 +269,29 @@ __device__ __forceinline__ unsigned long long warp_max(unsigned long long v)
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_minmax(const T *x, const T *y, const T *z, const T *w, int64_t n,
-                                                unsigned long long *partials)
+                                                unsigned long long *mm)
 {
     using K = decltype(okey(T(0)));
     K mn[3] = {(K)~(K)0, (K)~(K)0, (K)~(K)0}, mx[3] = {0, 0, 0}, wm = 0;
     uint32_t bad = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const T c[3] = {x[i], y[i], z[i]};
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    // two points per iteration: both sets of loads are issued before the compares
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += 2 * stride) {
+        const int64_t i2 = i + stride;
+        const bool two = i2 < n;
+        const T c[6] = {x[i], y[i], z[i], two ? x[i2] : x[i], two ? y[i2] : y[i], two ? z[i2] : z[i]};
 #pragma unroll
-        for (int a = 0; a < 3; a++) {
-            bad |= nonfinite(c[a]) ? 1u : 0u;
-            const K k = okey(c[a]);
-            mn[a] = k < mn[a] ? k : mn[a];
-            mx[a] = k > mx[a] ? k : mx[a];
+        for (int k = 0; k < 6; k++) {
+            const int a = k % 3;
+            bad |= nonfinite(c[k]) ? 1u : 0u;
+            const K key = okey(c[k]);
+            mn[a] = key < mn[a] ? key : mn[a];
+            mx[a] = key > mx[a] ? key : mx[a];
         }
         if (w) {
-            const K k = abskey(w[i]);
-            wm = k > wm ? k : wm;
+            const K k1 = abskey(w[i]), k2 = two ? abskey(w[i2]) : k1;
+            wm = k1 > wm ? k1 : wm;
+            wm = k2 > wm ? k2 : wm;
         }
     }
     __shared__ unsigned long long part[8][8];
@@ -225,43 +308,13 @@ __global__ void __launch_bounds__(256) k_minmax(const T *x, const T *y, const T 
         part[warp][7] = bad;
     }
     __syncthreads();
+    // the block's extremes go straight into mm (ord_enc of the double values; one atomic each)
     if (threadIdx.x < 8) {
         const int k = threadIdx.x;
-        unsigned long long v = part[0][k];
+        const bool is_min = k < 6 && (k & 1) == 0;
+        K v = (K)part[0][k];
         for (int q = 1; q < nwarps; q++) {
-            const unsigned long long o = part[q][k];
-            const bool is_min = k < 6 && (k & 1) == 0;
-            v = is_min ? (o < v ? o : v) : (o > v ? o : v);
-        }
-        partials[(size_t)blockIdx.x * 8 + k] = v;
-    }
-}
-
-// folds nblk partials (keys of type K) into mm; one block of 256 threads
-template <typename T>
-__global__ void __launch_bounds__(256) k_minmax_fold(const unsigned long long *partials, int nblk,
-                                                     unsigned long long *mm)
-{
-    using K = decltype(okey(T(0)));
-    __shared__ unsigned long long red[8][8];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int k = 0; k < 8; k++) {
-        const bool is_min = k < 6 && (k & 1) == 0;
-        K v = is_min ? (K)~(K)0 : (K)0;
-        for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
-            const K o = (K)partials[(size_t)b * 8 + k];
-            v = is_min ? (o < v ? o : v) : (o > v ? o : v);
-        }
-        v = is_min ? warp_min(v) : warp_max(v);
-        if (lane == 0) red[warp][k] = (unsigned long long)v;
-    }
-    __syncthreads();
-    if (threadIdx.x < 8) {
-        const int k = threadIdx.x;
-        const bool is_min = k < 6 && (k & 1) == 0;
-        K v = (K)red[0][k];
-        for (int q = 1; q < (int)(blockDim.x >> 5); q++) {
-            const K o = (K)red[q][k];
+            const K o = (K)part[q][k];
             v = is_min ? (o < v ? o : v) : (o > v ? o : v);
         }
         if (k == 7) {
@@ -271,17 +324,34 @@ __global__ void __launch_bounds__(256) k_minmax_fold(const unsigned long long *p
             atomicMax(&mm[6], ord_enc(wv));
         } else {
             const unsigned long long e = ord_enc(key_value(v));
-            if (is_min) atomicMin(&mm[k], e); else atomicMax(&mm[k], e);
+            if (is_min) atomicMin(&mm[k], e);
+            else atomicMax(&mm[k], e);
         }
     }
 }
 
-__device__ __forceinline__ int axis_cell(double c, const Geom &g, int a)
+// Cell index along axis a from the fixed-point coordinate X: (x - origin) / s in FP32, within
+// eps_cell (position units) of the exact value; the neighbour search margins cover it.
+__device__ __forceinline__ int axis_cell(unsigned long long X, const Geom &g, int a)
 {
-    int i = (int)floor((c - g.origin[a]) * g.inv_s[a]);
+    float h, l;
+    fix_split(X - g.o_cell[a], g.q_f[a], g.rho_f[a], &h, &l);
+    int i = (int)floorf((h + l) * g.inv_s_f[a]);
     i = i < 0 ? 0 : i;
     i = i >= g.n[a] ? g.n[a] - 1 : i;
     return i;
+}
+
+// cell index of a point in the reference lattice, in the reference's FP64 arithmetic
+// (utils/gridlink_impl.c.src:165-183)
+__device__ __forceinline__ void ref_axis_cells(const double *ref_min, const double *ref_inv, const int *ref_n, double a,
+                                               double b, double c, int *r)
+{
+    r[0] = (int)((a - ref_min[0]) * ref_inv[0]);
+    r[1] = (int)((b - ref_min[1]) * ref_inv[1]);
+    r[2] = (int)((c - ref_min[2]) * ref_inv[2]);
+    for (int k = 0; k < 3; k++)
+        if (r[k] > ref_n[k] - 1) r[k]--;
 }
 
 template <typename T>
@@ -289,35 +359,76 @@ __global__ void k_assign(const T *x, const T *y, const T *z, int64_t n, Geom g,
                          uint32_t *cellid, uint32_t *count, unsigned long long *oob)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double a = ld(x, i), b = ld(y, i), c = ld(z, i);
-        const int ix = axis_cell(a, g, 0), iy = axis_cell(b, g, 1), iz = axis_cell(c, g, 2);
-        const uint32_t cell = ((uint32_t)ix * g.n[1] + iy) * (uint32_t)g.n[2] + iz;
-        if (g.extent_err && !(a >= g.chk_lo[0] && a <= g.chk_hi[0] && b >= g.chk_lo[1] && b <= g.chk_hi[1] &&
-                              c >= g.chk_lo[2] && c <= g.chk_hi[2]))
-            atomicAdd(g.extent_err, 1ull);
+        const T c[3] = {x[i], y[i], z[i]};
+        int ic[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++) ic[a] = axis_cell(fix_of(c[a], g.e_fix[a]), g, a);
+        const uint32_t cell = ((uint32_t)ic[0] * g.n[1] + ic[1]) * (uint32_t)g.n[2] + ic[2];
+        if (g.extent_err) {
+            bool in = true;
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                const unsigned long long k = okey0((double)c[a]);
+                in = in && k >= g.k_chk_lo[a] && k <= g.k_chk_hi[a];
+            }
+            if (!in) atomicAdd(g.extent_err, 1ull);
+        }
         cellid[i] = cell;
         atomicAdd(&count[cell], 1u);
         if (g.check_ref_bounds) {
-            // out-of-bounds test of the reference lattice (utils/gridlink_impl.c.src:165-183)
-            int rx = (int)((a - g.ref_min[0]) * g.ref_inv[0]);
-            int ry = (int)((b - g.ref_min[1]) * g.ref_inv[1]);
-            int rz = (int)((c - g.ref_min[2]) * g.ref_inv[2]);
-            if (rx > g.ref_n[0] - 1) rx--;
-            if (ry > g.ref_n[1] - 1) ry--;
-            if (rz > g.ref_n[2] - 1) rz--;
-            if (rx < 0 || rx >= g.ref_n[0] || ry < 0 || ry >= g.ref_n[1] || rz < 0 || rz >= g.ref_n[2])
-                atomicAdd(oob, 1ull);
+            // out-of-bounds test of the reference lattice (utils/gridlink_impl.c.src:165-183):
+            // points well inside its range pass on their keys, the others take the FP64 test
+            bool safe = true;
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                const unsigned long long k = okey0((double)c[a]);
+                safe = safe && k >= g.k_ref_lo[a] && k <= g.k_ref_hi[a];
+            }
+            if (!safe) {
+                int r[3];
+                ref_axis_cells(g.ref_min, g.ref_inv, g.ref_n, (double)c[0], (double)c[1], (double)c[2], r);
+                if (r[0] < 0 || r[0] >= g.ref_n[0] || r[1] < 0 || r[1] >= g.ref_n[1] || r[2] < 0 || r[2] >= g.ref_n[2])
+                    atomicAdd(oob, 1ull);
+            }
         }
     }
 }
 
-__device__ __forceinline__ void split_hi_lo(double u, double q, double inv_q, float *hi, float *lo)
+// Reference-lattice cell index along axis a, equal to the reference's FP64
+// (int)((x - ref_min) * ref_inv) with its clamp of the top cell: an FP32 estimate t from the
+// fixed-point coordinate (|t - t_FP64| below 2^-22 |t| + 4 ref_inv 2^e_fix) decides when that
+// band is non-negative and holds no integer; otherwise the FP64 expression runs.
+template <typename T>
+__device__ __forceinline__ int ref_axis_cell(T x, unsigned long long X, const Geom &g, int a)
 {
-    const double h = rint(u * inv_q) * q;  // exact: q is a power of two
-    *hi = (float)h;                        // exact: |h| / q < 2^24
-    *lo = (float)(u - h);
+    const unsigned long long U = X - g.o_ref[a];
+    const long long N = ((long long)U + (1ll << 30)) >> 31;
+    int r = -1;
+    bool exact = true;
+    if (N > -(1ll << 23) && N < (1ll << 23)) {
+        const int L = (int)(long long)(U - ((unsigned long long)N << 31));
+        const float t = ((float)(int)N * g.q_f[a] + (float)L * g.rho_f[a]) * g.ref_inv_f[a];
+        const float e = fabsf(t) * 6e-7f + g.ref_tol_f[a];
+        const float lo = t - e, hi = t + e;
+        if (lo >= 0.f && hi < 1073741824.f && floorf(lo) == floorf(hi)) {
+            r = (int)lo;
+            exact = false;
+        }
+    }
+    if (exact) r = (int)(((double)x - g.ref_min[a]) * g.ref_inv[a]);
+    if (r > g.ref_n[a] - 1) r--;
+    return r;
 }
 
+// key order of |w| (the sign bit cleared; integer operations only)
+__device__ __forceinline__ unsigned long long abs_okey(double v)
+{
+    return ((unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull) | 0x8000000000000000ull;
+}
+__device__ __forceinline__ unsigned long long abs_okey(float v) { return abs_okey((double)v); }
+
+// Lattice records of every point at its slot of the counting sort.  L.lo (separation averages,
+// survey modes) and L.refcell (FP64 kernel) are written only when set.
 template <typename T>
 __global__ void k_scatter(const T *x, const T *y, const T *z, const T *w, int64_t n, Geom g,
                           const uint32_t *cellid, const uint32_t *cell_start, uint32_t *fill,
@@ -326,23 +437,23 @@ __global__ void k_scatter(const T *x, const T *y, const T *z, const T *w, int64_
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t c = cellid[i];
         const uint32_t pos = cell_start[c] + atomicAdd(&fill[c], 1u);
-        const double a = ld(x, i), b = ld(y, i), cz = ld(z, i);
-        const double wv = w ? ld(w, i) : 1.0;
-        if (g.extent_err && w && !(fabs(wv) <= g.chk_wmax)) atomicAdd(g.extent_err, 1ull);
-        float hx, hy, hz, lx, ly, lz;
-        split_hi_lo(a - g.hi_origin[0], g.q[0], g.inv_q[0], &hx, &lx);
-        split_hi_lo(b - g.hi_origin[1], g.q[1], g.inv_q[1], &hy, &ly);
-        split_hi_lo(cz - g.hi_origin[2], g.q[2], g.inv_q[2], &hz, &lz);
-        L.hi[pos] = make_float4(hx, hy, hz, (float)wv);
-        L.lo[pos] = make_float4(lx, ly, lz, 0.f);
-        L.dbl[pos] = make_double4_32a(a, b, cz, wv);
-        int rx = (int)((a - g.ref_min[0]) * g.ref_inv[0]);
-        int ry = (int)((b - g.ref_min[1]) * g.ref_inv[1]);
-        int rz = (int)((cz - g.ref_min[2]) * g.ref_inv[2]);
-        if (rx > g.ref_n[0] - 1) rx--;
-        if (ry > g.ref_n[1] - 1) ry--;
-        if (rz > g.ref_n[2] - 1) rz--;
-        L.refcell[pos] = (rx * g.ref_n[1] + ry) * g.ref_n[2] + rz;
+        const T p[3] = {x[i], y[i], z[i]};
+        const T wv = w ? w[i] : T(1);
+        if (g.extent_err && w && !(abs_okey(wv) <= g.k_chk_wmax)) atomicAdd(g.extent_err, 1ull);
+        float h[3], l[3];
+        unsigned long long X[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            X[a] = fix_of(p[a], g.e_fix[a]);
+            fix_split(X[a] - g.o_hi[a], g.q_f[a], g.rho_f[a], &h[a], &l[a]);
+        }
+        L.hi[pos] = make_float4(h[0], h[1], h[2], (float)wv);
+        if (L.lo) L.lo[pos] = make_float4(l[0], l[1], l[2], 0.f);
+        L.dbl[pos] = make_double4_32a((double)p[0], (double)p[1], (double)p[2], (double)wv);
+        int r[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++) r[a] = ref_axis_cell(p[a], X[a], g, a);
+        L.refcell[pos] = (r[0] * g.ref_n[1] + r[1]) * g.ref_n[2] + r[2];
         L.orig[pos] = (int)i;
         L.cellid[pos] = c;
     }
@@ -388,9 +499,11 @@ __global__ void k_scan_tile(const uint32_t *in, uint32_t *out, uint32_t n, uint3
     }
     if (t == 1023) {
         blocksums[blockIdx.x] = run;
+        if (gridDim.x == 1) out[n] = run;  // a single tile is the whole scan: write the total
     }
 }
 
+// adds the scanned tile sums (nblk + 1 entries, the last the total) and writes out[n] = total
 __global__ void k_scan_add(uint32_t *out, uint32_t n, const uint32_t *offs)
 {
     const uint32_t base = blockIdx.x * (uint32_t)kScanTile;
@@ -399,17 +512,7 @@ __global__ void k_scan_add(uint32_t *out, uint32_t n, const uint32_t *offs)
         const uint32_t idx = base + k;
         if (idx < n) out[idx] += add;
     }
-}
-
-__global__ void k_set_total(uint32_t *out, uint32_t n, const uint32_t *blocksum_scan, uint32_t nblk)
-{
-    // blocksum_scan holds the exclusive scan (nblk+1 entries, last = total)
-    out[n] = blocksum_scan[nblk];
-}
-
-__global__ void k_write_total_single(uint32_t *out, uint32_t n, const uint32_t *blocksums)
-{
-    out[n] = blocksums[0];
+    if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = offs[gridDim.x];
 }
 
 // ------------------------------------------------------------------------------------
@@ -440,6 +543,8 @@ __global__ void k_chunk_emit(const uint32_t *cell_start, int ncols, int nz, cons
     }
 }
 
+constexpr int kWzTab = 256;  // stencil columns whose z reach is tabulated in the task geometry
+
 struct TaskGeom {
     int nx, ny, nz;
     int periodic[3];
@@ -451,6 +556,11 @@ struct TaskGeom {
     double rmax_z;          // max |dz| (incl. margin)
     double rmax_3d;         // spherical limit (incl. margin), 0 = none
     uint32_t *error;        // set when a task would need an image beyond +-1
+    // z reach in slabs of every neighbour column offset c = (dx + reach_x) * (2 reach_y + 1) +
+    // dy + reach_y, -1 when the column is pruned; computed on the host (FP64) when the stencil
+    // has at most kWzTab columns (ntab > 0), else by each thread
+    int ntab;
+    int16_t wz_tab[kWzTab];
 };
 
 __device__ __forceinline__ int floordiv(int a, int b)
@@ -460,14 +570,30 @@ __device__ __forceinline__ int floordiv(int a, int b)
     return q;
 }
 
-// Tasks of one chunk against one neighbour column (dx, dy): one per periodic z image whose window
-// is not empty, split into ranges of at most kJMax points.  With EMIT == false only counted.
+// z reach (slabs) of neighbour column offset (dx, dy), -1 when the column is beyond reach
+__host__ __device__ inline int column_wz(const TaskGeom &G, int dx, int dy)
+{
+    const double rx = fmax(0.0, (double)(abs(dx) - 1)) * G.s[0];
+    const double ry = fmax(0.0, (double)(abs(dy) - 1)) * G.s[1];
+    const double rho2 = rx * rx + ry * ry;
+    if (rho2 >= G.rmax_xy * G.rmax_xy) return -1;
+    double W = G.rmax_z;
+    if (G.rmax_3d > 0.0) W = fmin(W, sqrt(fmax(0.0, G.rmax_3d * G.rmax_3d - rho2)));
+    const double wz = ceil(W / G.s[2]);
+    return wz > 1e9 ? 1000000000 : (int)wz;
+}
+
+// Tasks of one chunk against one neighbour column (dx, dy) (stencil index c): one per periodic z
+// image whose window is not empty, split into ranges of at most kJMax points.  With EMIT == false
+// only counted.
 template <bool EMIT>
 __device__ uint32_t chunk_col_tasks(const TaskGeom &G, uint32_t ib, uint32_t icount, const uint32_t *cellid1,
-                                    const uint32_t *cs2, Task *out, uint32_t cat, uint32_t room, int dx, int dy)
+                                    const uint32_t *cs2, Task *out, uint32_t cat, uint32_t room, int dx, int dy, int c)
 {
     if (icount == 0) return 0;  // unused chunk slot
     if (G.autocorr && (dx < 0 || (dx == 0 && dy < 0))) return 0;  // half stencil
+    const int wz = G.ntab ? (int)G.wz_tab[c] : column_wz(G, dx, dy);
+    if (wz < 0) return 0;
     const uint32_t c0 = cellid1[ib], c1 = cellid1[ib + icount - 1];
     const int nz = G.nz;
     const int col = (int)(c0 / nz);
@@ -483,13 +609,6 @@ __device__ uint32_t chunk_col_tasks(const TaskGeom &G, uint32_t ib, uint32_t ico
     int my = 0, cy = uy;
     if (G.periodic[1]) { my = floordiv(uy, G.ny); cy = uy - my * G.ny; }
     else if (uy < 0 || uy >= G.ny) return 0;
-    const double rx = fmax(0.0, (double)(abs(dx) - 1)) * G.s[0];
-    const double ry = fmax(0.0, (double)(abs(dy) - 1)) * G.s[1];
-    const double rho2 = rx * rx + ry * ry;
-    if (rho2 >= G.rmax_xy * G.rmax_xy) return 0;
-    double W = G.rmax_z;
-    if (G.rmax_3d > 0.0) W = fmin(W, sqrt(fmax(0.0, G.rmax_3d * G.rmax_3d - rho2)));
-    const int wz = (int)ceil(W / G.s[2]);
     const bool own = G.autocorr && dx == 0 && dy == 0;
     const int klo = own ? a : a - wz;
     const int khi = b + wz;
@@ -526,34 +645,36 @@ __device__ uint32_t chunk_col_tasks(const TaskGeom &G, uint32_t ib, uint32_t ico
     return ntask;
 }
 
-// One thread per (chunk slot, neighbour column): k = slot * ncoff + column offset index.
+// One thread per (chunk slot, neighbour column): slot = x index, stencil column c = blockIdx.y;
+// entry k = slot * ncoff + c.
 __global__ void k_task_count(TaskGeom G, uint32_t nslots, const uint32_t *chunk_begin, const uint32_t *chunk_count,
                              const uint32_t *cellid1, const uint32_t *cs2, uint32_t *ntasks)
 {
     const uint32_t ny = 2 * G.reach_y + 1, ncoff = (2 * G.reach_x + 1) * ny;
-    const uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (k >= (uint64_t)nslots * ncoff) return;
-    const uint32_t slot = (uint32_t)(k / ncoff), c = (uint32_t)(k % ncoff);
-    ntasks[k] = chunk_col_tasks<false>(G, chunk_begin[slot], chunk_count[slot], cellid1, cs2, nullptr, 0, 0,
-                                       (int)(c / ny) - G.reach_x, (int)(c % ny) - G.reach_y);
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+    if (slot >= nslots) return;
+    ntasks[(uint64_t)slot * ncoff + c] = chunk_col_tasks<false>(G, chunk_begin[slot], chunk_count[slot], cellid1, cs2,
+                                                                nullptr, 0, 0, (int)(c / ny) - G.reach_x,
+                                                                (int)(c % ny) - G.reach_y, (int)c);
 }
 
 // Writes the tasks of every (chunk, column) at its offset; with a capacity smaller than the total
-// the tail is dropped and *overflow set (the caller resizes and runs again).
+// the tail is dropped and *overflow set (the caller resizes and runs again).  flags[1] receives
+// the total (task_off[nslots * ncoff]), flags[3] the overflow.
 __global__ void k_task_emit(TaskGeom G, uint32_t nslots, const uint32_t *chunk_begin, const uint32_t *chunk_count,
                             const uint32_t *cellid1, const uint32_t *cs2, const uint32_t *task_off, Task *tasks,
-                            const uint16_t *chunk_cat, uint32_t capacity, uint32_t *overflow)
+                            const uint16_t *chunk_cat, uint32_t capacity, uint32_t *flags)
 {
     const uint32_t ny = 2 * G.reach_y + 1, ncoff = (2 * G.reach_x + 1) * ny;
-    const uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (k >= (uint64_t)nslots * ncoff) return;
-    const uint32_t slot = (uint32_t)(k / ncoff), c = (uint32_t)(k % ncoff);
-    const uint32_t off = task_off[k];
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+    if (slot == 0 && c == 0) flags[1] = task_off[(uint64_t)nslots * ncoff];
+    if (slot >= nslots) return;
+    const uint32_t off = task_off[(uint64_t)slot * ncoff + c];
     const uint32_t room = off < capacity ? capacity - off : 0u;
     const uint32_t n = chunk_col_tasks<true>(G, chunk_begin[slot], chunk_count[slot], cellid1, cs2, tasks + off,
                                              chunk_cat ? (uint32_t)chunk_cat[slot] : 0u, room,
-                                             (int)(c / ny) - G.reach_x, (int)(c % ny) - G.reach_y);
-    if (n > room && overflow) atomicOr(overflow, 1u);
+                                             (int)(c / ny) - G.reach_x, (int)(c % ny) - G.reach_y, (int)c);
+    if (n > room) atomicOr(&flags[3], 1u);
 }
 
 // ------------------------------------------------------------------------------------
@@ -1448,10 +1569,40 @@ struct SetBufs {
 // a batch plan owns one, so that its captured graph never sees a buffer move.
 struct Workspace {
     SetBufs set[2];
-    DevBuf mm, mm_part, oob, scan_tmp[4], chunk_cnt, chunk_off, chunk_begin, chunk_count, chunk_cat, ntask, task_off, tasks;
-    DevBuf hist_cnt, hist_avg, hist_w, stats, counter, edges, guards, lut, ascale;
+    DevBuf mm, scan_tmp[4], chunk_cnt, chunk_off, chunk_begin, chunk_count, chunk_cat, ntask, task_off, tasks;
+    DevBuf res, tab;  // result block (ResView), bin tables (edges, guards, averages scale, lookup table)
     HostBuf h_small, h_tab, h_hist;
 };
+
+// The result block of one run, one device allocation read back by one copy (the pinned host
+// copy has the same layout), nb = bins x catalogues:
+//   u64 cnt[nb] | f64 avg[nb] | f64 w[nb] | u64 stats[4] | u32 flags[4] | u64 oob | u64 extent
+// stats: pairs evaluated, refined, queued; flags: [0] task counter of the pair kernel, [1] tasks
+// emitted, [2] periodic image beyond +-1, [3] work-list overflow; oob: points outside the
+// reference lattice; extent: points / weights outside a batch plan's range.
+struct ResView {
+    unsigned long long *cnt;
+    double *avg, *w;
+    unsigned long long *stats;
+    uint32_t *flags;
+    unsigned long long *oob, *extent;
+};
+static inline size_t res_bytes(size_t nb) { return sizeof(unsigned long long) * (3 * nb + 8); }
+// bytes zeroed before each pair-kernel launch: the sums, the statistics and the task counter
+static inline size_t res_zero_bytes(size_t nb) { return sizeof(unsigned long long) * (3 * nb + 4) + sizeof(uint32_t); }
+static inline ResView res_view(void *base, size_t nb)
+{
+    ResView R;
+    unsigned long long *u = (unsigned long long *)base;
+    R.cnt = u;
+    R.avg = (double *)(u + nb);
+    R.w = (double *)(u + 2 * nb);
+    R.stats = u + 3 * nb;
+    R.flags = (uint32_t *)(u + 3 * nb + 4);
+    R.oob = u + 3 * nb + 6;
+    R.extent = u + 3 * nb + 7;
+    return R;
+}
 
 static void release(DevBuf &b)
 {
@@ -1469,9 +1620,8 @@ static void release_workspace(Workspace &W)
         for (DevBuf *d : v) release(*d);
     }
     for (int k = 0; k < 4; k++) release(W.scan_tmp[k]);
-    DevBuf *v[] = {&W.mm, &W.mm_part, &W.oob, &W.chunk_cnt, &W.chunk_off, &W.chunk_begin, &W.chunk_count, &W.chunk_cat, &W.ntask,
-                   &W.task_off, &W.tasks, &W.hist_cnt, &W.hist_avg, &W.hist_w, &W.stats, &W.counter, &W.edges,
-                   &W.guards, &W.lut, &W.ascale};
+    DevBuf *v[] = {&W.mm, &W.chunk_cnt, &W.chunk_off, &W.chunk_begin, &W.chunk_count, &W.chunk_cat, &W.ntask,
+                   &W.task_off, &W.tasks, &W.res, &W.tab};
     for (DevBuf *d : v) release(*d);
     HostBuf *h[] = {&W.h_small, &W.h_tab, &W.h_hist};
     for (HostBuf *b : h) {
@@ -1551,16 +1701,9 @@ static int scan_u32(Workspace &W, const uint32_t *in, uint32_t *out, uint32_t n,
     k_scan_tile<<<nblk, 1024, 0, st>>>(in, out, n, bs);
     g_eng.launches++;
     CF_CUDA(cudaGetLastError());
-    if (nblk == 1) {
-        k_write_total_single<<<1, 1, 0, st>>>(out, n, bs);
-        g_eng.launches++;
-        CF_CUDA(cudaGetLastError());
-        return EXIT_SUCCESS;
-    }
+    if (nblk == 1) return EXIT_SUCCESS;  // the tile wrote out[n]
     if (scan_u32(W, bs, bs_scan, nblk, level + 1) != EXIT_SUCCESS) return EXIT_FAILURE;
     k_scan_add<<<nblk, 1024, 0, st>>>(out, n, bs_scan);
-    g_eng.launches++;
-    k_set_total<<<1, 1, 0, st>>>(out, n, bs_scan, nblk);
     g_eng.launches++;
     CF_CUDA(cudaGetLastError());
     return EXIT_SUCCESS;
@@ -1595,19 +1738,17 @@ static float f_up(double v)
     return f;
 }
 
-// extent of one catalogue folded into mm[0..7] (two passes, partials in W.mm_part)
+// extent of one catalogue folded into mm[0..7] (one pass; each block folds its extremes atomically)
 template <typename T>
 static int minmax_into(Workspace &W, const T *x, const T *y, const T *z, const T *w, int64_t n, unsigned long long *mm)
 {
     if (n <= 0) return EXIT_SUCCESS;
-    int grid = grid_for(n, 256);
-    if (grid > 4 * g_eng.num_sms) grid = 4 * g_eng.num_sms;
-    if (ensure(W.mm_part, sizeof(unsigned long long) * 8 * (size_t)grid) != EXIT_SUCCESS) return EXIT_FAILURE;
-    k_minmax<T><<<grid, 256, 0, g_eng.stream>>>(x, y, z, w, n, (unsigned long long *)W.mm_part.p);
+    int grid = grid_for((n + 1) / 2, 256);
+    if (grid > 8 * g_eng.num_sms) grid = 8 * g_eng.num_sms;
+    (void)W;
+    k_minmax<T><<<grid, 256, 0, g_eng.stream>>>(x, y, z, w, n, mm);
     CF_CUDA(cudaGetLastError());
-    k_minmax_fold<T><<<1, 256, 0, g_eng.stream>>>((const unsigned long long *)W.mm_part.p, grid, mm);
-    CF_CUDA(cudaGetLastError());
-    g_eng.launches += 2;
+    g_eng.launches += 1;
     return EXIT_SUCCESS;
 }
 
@@ -1640,31 +1781,31 @@ static int build_lattice_at(Workspace &W, SetBufs &B, int64_t n, int64_t base, c
                             const T *w, const Geom &g, uint32_t ncells, unsigned long long *oob)
 {
     cudaStream_t st = g_eng.stream;
-    if (ensure(B.count, sizeof(uint32_t) * ncells) || ensure(B.fill, sizeof(uint32_t) * ncells) ||
+    // per-cell occupancy and fill counters side by side (one memset)
+    if (ensure(B.count, sizeof(uint32_t) * 2 * (size_t)ncells) ||
         ensure(B.cell_start, sizeof(uint32_t) * ((size_t)ncells + 1)))
         return EXIT_FAILURE;
-    CF_CUDA(cudaMemsetAsync(B.count.p, 0, sizeof(uint32_t) * ncells, st));
-    CF_CUDA(cudaMemsetAsync(B.fill.p, 0, sizeof(uint32_t) * ncells, st));
+    uint32_t *count = (uint32_t *)B.count.p, *fill = count + ncells;
+    CF_CUDA(cudaMemsetAsync(count, 0, sizeof(uint32_t) * 2 * (size_t)ncells, st));
     if (n <= 0) {
         CF_CUDA(cudaMemsetAsync(B.cell_start.p, 0, sizeof(uint32_t) * ((size_t)ncells + 1), st));
         return EXIT_SUCCESS;
     }
     uint32_t *cellid_u = (uint32_t *)B.cellid_u.p + base;
     const int grid = grid_for(n, 256);
-    k_assign<T><<<grid, 256, 0, st>>>(x, y, z, n, g, cellid_u, (uint32_t *)B.count.p, oob);
+    k_assign<T><<<grid, 256, 0, st>>>(x, y, z, n, g, cellid_u, count, oob);
     g_eng.launches++;
     CF_CUDA(cudaGetLastError());
-    if (scan_u32(W, (const uint32_t *)B.count.p, (uint32_t *)B.cell_start.p, ncells, 0) != EXIT_SUCCESS) return EXIT_FAILURE;
+    if (scan_u32(W, count, (uint32_t *)B.cell_start.p, ncells, 0) != EXIT_SUCCESS) return EXIT_FAILURE;
     Lattice L;
     L.hi = (float4 *)B.hi.p + base;
-    L.lo = (float4 *)B.lo.p + base;
+    L.lo = g.write_lo ? (float4 *)B.lo.p + base : nullptr;
     L.dbl = (double4_32a *)B.dbl.p + base;
     L.refcell = (int *)B.refcell.p + base;
     L.orig = (int *)B.orig.p + base;
     L.cellid = (uint32_t *)B.cellid.p + base;
     L.cell_start = (uint32_t *)B.cell_start.p;
-    k_scatter<T><<<grid, 256, 0, st>>>(x, y, z, w, n, g, cellid_u, (const uint32_t *)B.cell_start.p,
-                                       (uint32_t *)B.fill.p, L);
+    k_scatter<T><<<grid, 256, 0, st>>>(x, y, z, w, n, g, cellid_u, (const uint32_t *)B.cell_start.p, fill, L);
     g_eng.launches++;
     CF_CUDA(cudaGetLastError());
     return EXIT_SUCCESS;
@@ -1878,7 +2019,11 @@ struct Tables {
     uint32_t row_bytes, trash;
     float q_floor;
     double dxy, d3;
+    size_t guard_off, ascale_off, lut_off;  // byte offsets in W.tab (edges at 0)
 };
+
+// packed bin tables of one run: double edges[ne] | float guards[2 ne] | float ascale[ne] | u32 lut[]
+static inline size_t tab_align(size_t v) { return (v + 15) / 16 * 16; }
 
 static int build_tables(Workspace &W, const cf_job *J, int mode, int nbins, bool need_w, const double delta[3], Tables *T)
 {
@@ -1890,15 +2035,16 @@ static int build_tables(Workspace &W, const cf_job *J, int mode, int nbins, bool
     T->d3 = d3;
     const double dlim = (mode == MODE_RPPI || mode == MODE_WP) ? dxy : d3;
     // guards: for theta the classified quantity is the squared chord 2*(1 - cos)
-    if (ensure(W.edges, sizeof(double) * J->nedges) || ensure(W.guards, sizeof(float) * 2 * J->nedges) ||
-        ensure(W.ascale, sizeof(float) * J->nedges))
-        return EXIT_FAILURE;
-    const size_t tab_bytes = sizeof(double) * CF_MAX_EDGES + sizeof(float) * 3 * CF_MAX_EDGES + sizeof(uint32_t) * 4100;
-    if (ensure_host(W.h_tab, tab_bytes) != EXIT_SUCCESS) return EXIT_FAILURE;
+    const size_t ne = (size_t)J->nedges;
+    T->guard_off = tab_align(sizeof(double) * ne);
+    T->ascale_off = tab_align(T->guard_off + sizeof(float) * 2 * ne);
+    T->lut_off = tab_align(T->ascale_off + sizeof(float) * ne);
+    const size_t tab_max = T->lut_off + sizeof(uint32_t) * 4100;
+    if (ensure_host(W.h_tab, tab_max) != EXIT_SUCCESS || ensure(W.tab, tab_max) != EXIT_SUCCESS) return EXIT_FAILURE;
     double *edges_h = (double *)W.h_tab.p;
-    float *guards_h = (float *)(edges_h + CF_MAX_EDGES);
-    float *ascale_h = guards_h + 2 * CF_MAX_EDGES;
-    uint32_t *lut_h = (uint32_t *)(ascale_h + CF_MAX_EDGES);
+    float *guards_h = (float *)((char *)W.h_tab.p + T->guard_off);
+    float *ascale_h = (float *)((char *)W.h_tab.p + T->ascale_off);
+    uint32_t *lut_h = (uint32_t *)((char *)W.h_tab.p + T->lut_off);
     memcpy(edges_h, J->edges, sizeof(double) * J->nedges);
     // fixed-point scale of the separation sums per separation bin m (values in [edge m-1, edge m)):
     // one term stays below 2^30, i.e. a relative resolution of 2^-30 of the bin's upper edge
@@ -1941,7 +2087,6 @@ static int build_tables(Workspace &W, const cf_job *J, int mode, int nbins, bool
     while (((bhi >> shift) - (blo >> shift)) + 1 > 4096u) shift++;
     const int base = (int)(blo >> shift);
     const int n = (int)((bhi >> shift) - (blo >> shift)) + 1;
-    if (ensure(W.lut, sizeof(uint32_t) * (n + 1)) != EXIT_SUCCESS) return EXIT_FAILURE;
     // row byte offsets: the layout (private columns or shared row) is fixed before the launch
     const int ls = choose_layout(mode, false, J->need_avg != 0, need_w, J->nedges, nbins, n).lane_stride;
     const uint32_t ostride = mode_two_d(mode) ? (uint32_t)(J->npibin + 1) : 1u;
@@ -1964,10 +2109,7 @@ static int build_tables(Workspace &W, const cf_job *J, int mode, int nbins, bool
         lut_h[t] = definite ? ((uint32_t)mlo * ostride * row_bytes | ((uint32_t)mlo << 22)) : (trash | 0x80000000u);
     }
     lut_h[n] = trash;  // reject: below the first bucket (q < rmin^2) or above the last (q >= rmax^2)
-    CF_CUDA(cudaMemcpyAsync(W.lut.p, lut_h, sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice, st));
-    CF_CUDA(cudaMemcpyAsync(W.edges.p, edges_h, sizeof(double) * J->nedges, cudaMemcpyHostToDevice, st));
-    CF_CUDA(cudaMemcpyAsync(W.guards.p, guards_h, sizeof(float) * 2 * J->nedges, cudaMemcpyHostToDevice, st));
-    CF_CUDA(cudaMemcpyAsync(W.ascale.p, ascale_h, sizeof(float) * J->nedges, cudaMemcpyHostToDevice, st));
+    CF_CUDA(cudaMemcpyAsync(W.tab.p, W.h_tab.p, T->lut_off + sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice, st));
     T->lut_n = n;
     T->shift = shift;
     T->base = base;
@@ -2016,6 +2158,36 @@ static int choose_rxy(const cf_job *J, const double ext[3])
     return best;
 }
 
+// Integer forms of the lattice geometry for the lattice kernels: fixed-point origins, the
+// reference-lattice safe range and the extent-check keys.  Called after any change of origin,
+// s, n, the reference lattice or the checked extent.
+static void geom_keys(Geom &g)
+{
+    for (int a = 0; a < 3; a++) {
+        g.o_hi[a] = fix_of(g.hi_origin[a], g.e_fix[a]);
+        g.o_cell[a] = fix_of(g.origin[a], g.e_fix[a]);
+        g.inv_s_f[a] = (float)g.inv_s[a];
+        // coordinates in [ref_min - cell / 2, ref_min + (ref_n + 1/2) cells] get a reference cell in
+        // [0, ref_n] before the reference's clamp of the top cell, whatever the FP64 rounding
+        const double c = 1.0 / g.ref_inv[a];
+        const double rl = g.ref_min[a] - 0.5 * c, rh = g.ref_min[a] + (g.ref_n[a] + 0.5) * c;
+        if (g.ref_inv[a] > 0.0 && isfinite(c) && isfinite(rl) && isfinite(rh)) {
+            g.k_ref_lo[a] = okey0(rl);
+            g.k_ref_hi[a] = okey0(rh);
+        } else {
+            g.k_ref_lo[a] = ~0ull;  // empty: every point takes the FP64 test
+            g.k_ref_hi[a] = 0ull;
+        }
+        g.o_ref[a] = fix_of(g.ref_min[a], g.e_fix[a]);
+        const bool ref_ok = g.ref_inv[a] > 0.0 && isfinite(g.ref_inv[a]) && g.ref_inv[a] < 1e30;
+        g.ref_inv_f[a] = ref_ok ? (float)g.ref_inv[a] : NAN;
+        g.ref_tol_f[a] = ref_ok ? (float)(4.0 * ldexp(g.ref_inv[a], g.e_fix[a]) + 1e-30) : NAN;
+        g.k_chk_lo[a] = okey0(g.chk_lo[a]);
+        g.k_chk_hi[a] = okey0(g.chk_hi[a]);
+    }
+    g.k_chk_wmax = okey0(fabs(g.chk_wmax));
+}
+
 static int gpu_geometry(const cf_job *J, const cf_geometry &geo, const double lo[3], const double hi[3], Geom &g,
                         double delta[3])
 {
@@ -2029,6 +2201,12 @@ static int gpu_geometry(const cf_job *J, const cf_geometry &geo, const double lo
     }
     const int rxy = choose_rxy(J, ext0);
     const int refine[3] = {rxy, rxy, kZFine};
+    // position error of the FP32 cell index (a few ulps of x - origin, doubled), and the cell
+    // widening that keeps the neighbour reach at 'refine' cells with the search margins
+    // (2 eps_cell per axis, the plane taking the larger of x and y) added to the radii
+    double eps[3];
+    for (int a = 0; a < 3; a++) eps[a] = ldexp(1.0, -21) * fmax(ext0[a], 0.0);
+    const double eps_xy = fmax(eps[0], eps[1]);
     for (int a = 0; a < 3; a++) {
         const bool per = geo.periodic[a] && geo.wrap[a] > 0.0;
         double ext = hi[a] - lo[a];
@@ -2041,7 +2219,8 @@ static int gpu_geometry(const cf_job *J, const cf_geometry &geo, const double lo
         int n = 1;
         if (ext > 0.0 && rlim[a] > 0.0) {
             // cells slightly wider than rlim/refine so that the neighbour reach is exactly 'refine'
-            double nn = floor(ext / (rlim[a] / refine[a] * (1.0 + 1e-6)));
+            const double slack = 1e-6 + 4.0 * (a < 2 ? eps_xy : eps[2]) / rlim[a];
+            double nn = floor(ext / (rlim[a] / refine[a] * (1.0 + slack)));
             if (nn > 4096) nn = 4096;
             if (nn < 1) nn = 1;
             n = (int)nn;
@@ -2059,7 +2238,14 @@ static int gpu_geometry(const cf_job *J, const cf_geometry &geo, const double lo
             g.hi_origin[a] = 0.0;
             g.q[a] = pow2_ceil(fmax(fmax(fabs(lo[a]), fabs(hi[a])), 1e-300)) * ldexp(1.0, -22);
         }
+        // the fixed-point step 2^e_fix = q 2^-31 stays a normal float
+        if (g.q[a] < ldexp(1.0, -95)) g.q[a] = ldexp(1.0, -95);
+        if (g.q[a] > ldexp(1.0, 100)) CF_FAIL("coordinates of magnitude %g are out of range", fmax(fabs(lo[a]), fabs(hi[a])));
         g.inv_q[a] = 1.0 / g.q[a];
+        g.e_fix[a] = ilogb(g.q[a]) - 31;
+        g.q_f[a] = (float)g.q[a];
+        g.rho_f[a] = ldexpf(1.0f, g.e_fix[a]);
+        g.eps_cell[a] = (float)eps[a];
         const double maxabs = fmax(fabs(lo[a]), fabs(hi[a])) + (per ? geo.wrap[a] : 0.0);
         delta[a] = 1.5 * g.q[a] + ldexp(1.0, -49) * (maxabs + span[a]);
         g.ref_min[a] = geo.ref_min[a];
@@ -2082,20 +2268,22 @@ static int gpu_geometry(const cf_job *J, const cf_geometry &geo, const double lo
         }
     }
     g.check_ref_bounds = (J->rule.kind == CF_REF_BOX) ? 1 : 0;
+    geom_keys(g);
     return EXIT_SUCCESS;
 }
 
 // Neighbour-search parameters of the work list: reach in columns and the z / 3-D limits, with
-// margins that cover the FP64 rounding of the cell assignment.
+// margins that cover the rounding of the cell assignment.
 static int task_geometry(const cf_job *J, const cf_geometry &geo, const Geom &g, const double lo[3], const double hi[3],
                          bool autocorr, int mode, TaskGeom &G)
 {
-    // prune margins cover FP64 rounding of the cell assignment only (the FP32 error bounds
-    // matter for classification, not for which neighbours are visited)
+    // prune margins cover the rounding of the cell assignment only (the FP32 error bounds of the
+    // pair kernels matter for classification, not for which neighbours are visited)
     double maxabs_all = 0.0;
     for (int a = 0; a < 3; a++) maxabs_all = fmax(maxabs_all, fmax(fabs(lo[a]), fabs(hi[a])) + (geo.periodic[a] ? geo.wrap[a] : 0.0));
-    const double margin_xy = 1e-9 * fmax(g.s[0], g.s[1]) + 1e-13 * maxabs_all;
-    const double margin_z = 1e-9 * g.s[2] + 1e-13 * maxabs_all;
+    // ... plus twice the position error of the FP32 cell index of each point
+    const double margin_xy = 1e-9 * fmax(g.s[0], g.s[1]) + 1e-13 * maxabs_all + 2.0 * fmax(g.eps_cell[0], g.eps_cell[1]);
+    const double margin_z = 1e-9 * g.s[2] + 1e-13 * maxabs_all + 2.0 * (double)g.eps_cell[2];
     memset(&G, 0, sizeof(G));
     G.nx = g.n[0];
     G.ny = g.n[1];
@@ -2112,7 +2300,22 @@ static int task_geometry(const cf_job *J, const cf_geometry &geo, const Geom &g,
     G.reach_x = (int)ceil(G.rmax_xy / g.s[0]);
     G.reach_y = (int)ceil(G.rmax_xy / g.s[1]);
     if (G.reach_x > 64 || G.reach_y > 64) CF_FAIL("internal: neighbour reach too large");
+    const int ny = 2 * G.reach_y + 1, ncoff = (2 * G.reach_x + 1) * ny;
+    G.ntab = 0;
+    if (ncoff <= kWzTab) {
+        for (int c = 0; c < ncoff; c++) {
+            const int wz = column_wz(G, c / ny - G.reach_x, c % ny - G.reach_y);
+            G.wz_tab[c] = (int16_t)(wz > 32767 ? 32767 : wz);
+        }
+        G.ntab = ncoff;
+    }
     return EXIT_SUCCESS;
+}
+
+// launch grid of the task kernels: chunk slots along x, stencil columns along y
+static dim3 task_grid(const TaskGeom &G, uint32_t nslots)
+{
+    return dim3(nslots ? (nslots + 127) / 128 : 1u, (unsigned)((2 * G.reach_x + 1) * (2 * G.reach_y + 1)));
 }
 
 // Bin, band and accumulator constants of the pair kernels (everything but the buffers).
@@ -2144,8 +2347,8 @@ static void pair_constants(PairArgs &A, const cf_job *J, int mode, int nbins, bo
         }
     }
     const double dxy = T.dxy, d3 = T.d3;
-    A.g_lut = (const uint32_t *)W.lut.p;
-    A.g_ascale = (const float *)W.ascale.p;
+    A.g_lut = (const uint32_t *)((const char *)W.tab.p + T.lut_off);
+    A.g_ascale = (const float *)((const char *)W.tab.p + T.ascale_off);
     A.rbin_div = mode_two_d(mode) ? J->npibin + 1 : 1;
     A.trash_off = T.trash;
     A.row_bytes = T.row_bytes;
@@ -2156,8 +2359,8 @@ static void pair_constants(PairArgs &A, const cf_job *J, int mode, int nbins, bo
     A.lut_negbase = (uint32_t)(-T.base);
     A.lut_n = T.lut_n;
     A.q_floor = T.q_floor;
-    A.g_edges = (const double *)W.edges.p;
-    A.g_guard = (const float *)W.guards.p;
+    A.g_edges = (const double *)W.tab.p;
+    A.g_guard = (const float *)((const char *)W.tab.p + T.guard_off);
     A.dz_err = (float)(2.0 * delta[2]);
     A.dxy_err = (float)(2.0 * dxy);
     if (mode_is_mock(mode)) {
@@ -2291,9 +2494,12 @@ static int run_locked(cf_job *J, cf_hist *H)
     g_eng.last.num_cells = (int)ncells;
 
     // ---- lattices ----
-    if (ensure(W.oob, sizeof(unsigned long long)) != EXIT_SUCCESS) return EXIT_FAILURE;
-    unsigned long long *oob = (unsigned long long *)W.oob.p;
-    CF_CUDA(cudaMemsetAsync(oob, 0, sizeof(unsigned long long), st));
+    const bool f64 = g_eng.precision == CF_PRECISION_FP64 || !has_f32_path(mode);
+    g.write_lo = (J->need_avg != 0 || mode_is_mock(mode)) ? 1 : 0;
+    if (ensure(W.res, res_bytes(nbins)) != EXIT_SUCCESS) return EXIT_FAILURE;
+    const ResView R = res_view(W.res.p, nbins);
+    unsigned long long *oob = R.oob;
+    CF_CUDA(cudaMemsetAsync(R.flags, 0, sizeof(unsigned long long) * 4, st));  // flags, oob, extent
     for (int s = 0; s < nsets; s++) {
         const int64_t n = s ? n2 : n1;
         int rc = dev_float ? build_lattice<float>(W, s, n, need_w, g, ncells, oob)
@@ -2325,16 +2531,14 @@ static int run_locked(cf_job *J, cf_hist *H)
     CF_CUDA(cudaGetLastError());
 
     // ---- tasks: counted and emitted on the device into a buffer sized from earlier calls ----
-    if (ensure(W.counter, sizeof(uint32_t) * 4) != EXIT_SUCCESS) return EXIT_FAILURE;
-    CF_CUDA(cudaMemsetAsync(W.counter.p, 0, sizeof(uint32_t) * 4, st));
     TaskGeom G;
     if (task_geometry(J, geo, g, lo, hi, autocorr, mode, G) != EXIT_SUCCESS) return EXIT_FAILURE;
-    G.error = (uint32_t *)W.counter.p + 2;
+    G.error = R.flags + 2;
     const uint32_t nentries = max_chunks * (uint32_t)((2 * G.reach_x + 1) * (2 * G.reach_y + 1));
     if (ensure(W.ntask, sizeof(uint32_t) * ((size_t)nentries + 1)) ||
         ensure(W.task_off, sizeof(uint32_t) * ((size_t)nentries + 2)))
         return EXIT_FAILURE;
-    k_task_count<<<(nentries + 127) / 128, 128, 0, st>>>(G, max_chunks, (const uint32_t *)W.chunk_begin.p,
+    k_task_count<<<task_grid(G, max_chunks), 128, 0, st>>>(G, max_chunks, (const uint32_t *)W.chunk_begin.p,
                                                            (const uint32_t *)W.chunk_count.p,
                                                            (const uint32_t *)S1.cellid.p,
                                                            (const uint32_t *)S2.cell_start.p, (uint32_t *)W.ntask.p);
@@ -2365,68 +2569,49 @@ static int run_locked(cf_job *J, cf_hist *H)
     A.or2 = (const int *)S2.orig.p;
     A.ntask_dev = (const uint32_t *)W.task_off.p + nentries;
     pair_constants(A, J, mode, nbins, autocorr, G, geo, g, delta, T, wmax, W);
-    if (ensure(W.hist_cnt, sizeof(unsigned long long) * nbins) || ensure(W.hist_avg, sizeof(double) * nbins) ||
-        ensure(W.hist_w, sizeof(double) * nbins) || ensure(W.stats, sizeof(unsigned long long) * 4))
-        return EXIT_FAILURE;
-    A.g_cnt = (unsigned long long *)W.hist_cnt.p;
-    A.g_avg = (double *)W.hist_avg.p;
-    A.g_w = (double *)W.hist_w.p;
-    A.g_stats = (unsigned long long *)W.stats.p;
-    A.task_counter = (uint32_t *)W.counter.p;
-    if (ensure_host(W.h_hist, sizeof(uint64_t) * (3 * (size_t)nbins + 8)) != EXIT_SUCCESS) return EXIT_FAILURE;
-    uint64_t *cnt_h = (uint64_t *)W.h_hist.p;
-    double *avg_h = (double *)(cnt_h + nbins), *w_h = avg_h + nbins;
-    unsigned long long *stats_h = (unsigned long long *)(w_h + nbins);
-    const uint32_t *flags_h = (const uint32_t *)(stats_h + 4);  // counter[0..3]: task counter, -, image, overflow
-    const unsigned long long *oob_h = stats_h + 6;
-    const uint32_t *ntasks_h = (const uint32_t *)(stats_h + 7);
+    A.g_cnt = R.cnt;
+    A.g_avg = R.avg;
+    A.g_w = R.w;
+    A.g_stats = R.stats;
+    A.task_counter = R.flags;
+    if (ensure_host(W.h_hist, res_bytes(nbins)) != EXIT_SUCCESS) return EXIT_FAILURE;
+    const ResView Rh = res_view(W.h_hist.p, nbins);
 
     for (int attempt = 0; attempt < 2; attempt++) {
         A.tasks = (const Task *)W.tasks.p;
         A.ntasks = (uint32_t)cap;
-        k_task_emit<<<(nentries + 127) / 128, 128, 0, st>>>(G, max_chunks, (const uint32_t *)W.chunk_begin.p,
+        k_task_emit<<<task_grid(G, max_chunks), 128, 0, st>>>(G, max_chunks, (const uint32_t *)W.chunk_begin.p,
                                                               (const uint32_t *)W.chunk_count.p,
                                                               (const uint32_t *)S1.cellid.p,
                                                               (const uint32_t *)S2.cell_start.p,
                                                               (const uint32_t *)W.task_off.p, (Task *)W.tasks.p, nullptr,
-                                                              (uint32_t)cap, (uint32_t *)W.counter.p + 3);
+                                                              (uint32_t)cap, R.flags);
         g_eng.launches++;
         CF_CUDA(cudaGetLastError());
         CF_CUDA(cudaEventRecord(g_eng.ev[1], st));
-        CF_CUDA(cudaMemsetAsync(W.hist_cnt.p, 0, sizeof(unsigned long long) * nbins, st));
-        CF_CUDA(cudaMemsetAsync(W.hist_avg.p, 0, sizeof(double) * nbins, st));
-        CF_CUDA(cudaMemsetAsync(W.hist_w.p, 0, sizeof(double) * nbins, st));
-        CF_CUDA(cudaMemsetAsync(W.stats.p, 0, sizeof(unsigned long long) * 4, st));
-        CF_CUDA(cudaMemsetAsync(W.counter.p, 0, sizeof(uint32_t), st));  // task counter
+        CF_CUDA(cudaMemsetAsync(W.res.p, 0, res_zero_bytes(nbins), st));  // sums, statistics, task counter
         int launched = 0;
         CF_CUDA(cudaEventRecord(g_eng.ev[2], st));
-        const bool f64 = g_eng.precision == CF_PRECISION_FP64 || !has_f32_path(mode);
         if (launch_pairs(mode, A, f64, J->need_avg != 0, need_w, &launched) != EXIT_SUCCESS) return EXIT_FAILURE;
         CF_CUDA(cudaEventRecord(g_eng.ev[3], st));
-        CF_CUDA(cudaMemcpyAsync(cnt_h, W.hist_cnt.p, sizeof(uint64_t) * nbins, cudaMemcpyDeviceToHost, st));
-        CF_CUDA(cudaMemcpyAsync(avg_h, W.hist_avg.p, sizeof(double) * nbins, cudaMemcpyDeviceToHost, st));
-        CF_CUDA(cudaMemcpyAsync(w_h, W.hist_w.p, sizeof(double) * nbins, cudaMemcpyDeviceToHost, st));
-        CF_CUDA(cudaMemcpyAsync(stats_h, W.stats.p, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost, st));
-        CF_CUDA(cudaMemcpyAsync((void *)flags_h, W.counter.p, sizeof(uint32_t) * 4, cudaMemcpyDeviceToHost, st));
-        CF_CUDA(cudaMemcpyAsync((void *)oob_h, oob, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-        CF_CUDA(cudaMemcpyAsync((void *)ntasks_h, A.ntask_dev, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        CF_CUDA(cudaMemcpyAsync(W.h_hist.p, W.res.p, res_bytes(nbins), cudaMemcpyDeviceToHost, st));
         CF_CUDA(cudaEventRecord(g_eng.ev[4], st));
         CF_CUDA(cudaStreamSynchronize(st));
-        if (*oob_h > 0) CF_FAIL("%llu particles are out of bounds. Check periodic wrapping?", *oob_h);
-        if (flags_h[2]) CF_FAIL("internal: neighbour search needed a periodic image beyond +-1");
-        if (!flags_h[3]) break;
+        if (*Rh.oob > 0) CF_FAIL("%llu particles are out of bounds. Check periodic wrapping?", *Rh.oob);
+        if (Rh.flags[2]) CF_FAIL("internal: neighbour search needed a periodic image beyond +-1");
+        if (!Rh.flags[3]) break;
         // the work list outgrew the buffer: size it exactly and run the pair kernel again
         if (attempt == 1) CF_FAIL("internal: work list overflow after resizing");
-        cap = (size_t)*ntasks_h + 1024;
+        cap = (size_t)Rh.flags[1] + 1024;
         if (ensure(W.tasks, sizeof(Task) * cap) != EXIT_SUCCESS) return EXIT_FAILURE;
         cap = W.tasks.cap / sizeof(Task);
         if (cap > 0xffffffffu) cap = 0xffffffffu;
-        CF_CUDA(cudaMemsetAsync(W.counter.p, 0, sizeof(uint32_t) * 4, st));
+        CF_CUDA(cudaMemsetAsync(R.flags + 3, 0, sizeof(uint32_t), st));  // overflow flag
     }
-    g_eng.last.tasks = *ntasks_h;
-    memcpy(H->npairs, cnt_h, sizeof(uint64_t) * nbins);
-    memcpy(H->avg, avg_h, sizeof(double) * nbins);
-    memcpy(H->wsum, w_h, sizeof(double) * nbins);
+    g_eng.last.tasks = Rh.flags[1];
+    memcpy(H->npairs, Rh.cnt, sizeof(uint64_t) * nbins);
+    memcpy(H->avg, Rh.avg, sizeof(double) * nbins);
+    memcpy(H->wsum, Rh.w, sizeof(double) * nbins);
     float ms_pairs = 0.f, ms_grid = 0.f, ms_total = 0.f;
     CF_CUDA(cudaEventElapsedTime(&ms_pairs, g_eng.ev[2], g_eng.ev[3]));
     CF_CUDA(cudaEventElapsedTime(&ms_grid, g_eng.ev[0], g_eng.ev[1]));
@@ -2434,9 +2619,9 @@ static int run_locked(cf_job *J, cf_hist *H)
     g_eng.last.pair_kernel_ms = ms_pairs;
     g_eng.last.gridlink_ms = ms_grid;
     g_eng.last.total_gpu_ms = ms_total;
-    g_eng.last.pairs_evaluated = stats_h[0];
-    g_eng.last.pairs_refined = stats_h[1];
-    g_eng.last.pairs_slow = stats_h[2];
+    g_eng.last.pairs_evaluated = Rh.stats[0];
+    g_eng.last.pairs_refined = Rh.stats[1];
+    g_eng.last.pairs_slow = Rh.stats[2];
     g_eng.last.kernel_launches = g_eng.launches;
     return EXIT_SUCCESS;
 }
@@ -2480,11 +2665,15 @@ static int batch_lattices(BatchPlan &P)
 {
     Workspace &W = P.W;
     cudaStream_t st = g_eng.stream;
-    unsigned long long *oob = (unsigned long long *)W.oob.p;
+    const ResView R = res_view(W.res.p, (size_t)P.nbatch * P.nbins);
+    unsigned long long *oob = R.oob;
     Geom g1 = P.g, g2 = P.g;
-    g1.extent_err = g2.extent_err = oob + 1;
+    g1.extent_err = g2.extent_err = R.extent;
     g1.chk_wmax = P.wmax[0];
     g2.chk_wmax = P.wmax[1];
+    geom_keys(g1);
+    geom_keys(g2);
+    g1.write_lo = g2.write_lo = (P.J.need_avg != 0 || mode_is_mock(P.mode)) ? 1 : 0;
     const T *w2 = P.need_w ? (const T *)P.J.w2 : nullptr;
     if (build_lattice_at<T>(W, W.set[1], P.J.n2, 0, (const T *)P.J.x2, (const T *)P.J.y2, (const T *)P.J.z2, w2, g2,
                             P.ncells, oob) != EXIT_SUCCESS)
@@ -2530,30 +2719,26 @@ static int batch_enqueue(BatchPlan &P, int phase, bool timing)
     Workspace &W = P.W;
     cudaStream_t st = g_eng.stream;
     if (phase == 0) {
-        CF_CUDA(cudaMemsetAsync(W.counter.p, 0, sizeof(uint32_t) * 4, st));
-        CF_CUDA(cudaMemsetAsync(W.oob.p, 0, sizeof(unsigned long long) * 2, st));
+        CF_CUDA(cudaMemsetAsync(res_view(W.res.p, (size_t)P.nbatch * P.nbins).flags, 0, sizeof(unsigned long long) * 4,
+                                st));  // flags, oob, extent
         CF_CUDA(cudaMemsetAsync(W.chunk_count.p, 0, sizeof(uint32_t) * P.total_slots, st));
         const int rc = P.isf ? batch_lattices<float>(P) : batch_lattices<double>(P);
         if (rc != EXIT_SUCCESS) return EXIT_FAILURE;
-        k_task_count<<<(P.nentries + 127) / 128, 128, 0, st>>>(
+        k_task_count<<<task_grid(P.G, P.total_slots), 128, 0, st>>>(
             P.G, P.total_slots, (const uint32_t *)W.chunk_begin.p, (const uint32_t *)W.chunk_count.p,
             (const uint32_t *)W.set[0].cellid.p, (const uint32_t *)W.set[1].cell_start.p, (uint32_t *)W.ntask.p);
         g_eng.launches++;
         CF_CUDA(cudaGetLastError());
         return scan_u32(W, (const uint32_t *)W.ntask.p, (uint32_t *)W.task_off.p, P.nentries, 0);
     }
-    k_task_emit<<<(P.nentries + 127) / 128, 128, 0, st>>>(
+    k_task_emit<<<task_grid(P.G, P.total_slots), 128, 0, st>>>(
         P.G, P.total_slots, (const uint32_t *)W.chunk_begin.p, (const uint32_t *)W.chunk_count.p,
         (const uint32_t *)W.set[0].cellid.p, (const uint32_t *)W.set[1].cell_start.p, (const uint32_t *)W.task_off.p,
-        (Task *)W.tasks.p, (const uint16_t *)W.chunk_cat.p, P.task_cap, (uint32_t *)W.counter.p + 3);
+        (Task *)W.tasks.p, (const uint16_t *)W.chunk_cat.p, P.task_cap, res_view(W.res.p, (size_t)P.nbatch * P.nbins).flags);
     g_eng.launches++;
     CF_CUDA(cudaGetLastError());
-    const size_t hb = sizeof(uint64_t) * (size_t)P.nbatch * P.nbins;
-    CF_CUDA(cudaMemsetAsync(W.hist_cnt.p, 0, hb, st));
-    CF_CUDA(cudaMemsetAsync(W.hist_avg.p, 0, hb, st));
-    CF_CUDA(cudaMemsetAsync(W.hist_w.p, 0, hb, st));
-    CF_CUDA(cudaMemsetAsync(W.stats.p, 0, sizeof(unsigned long long) * 4, st));
-    CF_CUDA(cudaMemsetAsync(W.counter.p, 0, sizeof(uint32_t), st));  // task counter only
+    const size_t nb = (size_t)P.nbatch * P.nbins;
+    CF_CUDA(cudaMemsetAsync(W.res.p, 0, res_zero_bytes(nb), st));  // sums, statistics, task counter
     if (timing && record_event(P.ev[1]) != EXIT_SUCCESS) return EXIT_FAILURE;
     int launched = 0;
     const bool f64 = g_eng.precision == CF_PRECISION_FP64;
@@ -2565,15 +2750,7 @@ static int batch_enqueue(BatchPlan &P, int phase, bool timing)
     g_eng.force_warps = fw;
     if (rc != EXIT_SUCCESS) return EXIT_FAILURE;
     if (timing && record_event(P.ev[2]) != EXIT_SUCCESS) return EXIT_FAILURE;
-    uint64_t *cnt_h = (uint64_t *)W.h_hist.p;
-    double *avg_h = (double *)(cnt_h + (size_t)P.nbatch * P.nbins), *w_h = avg_h + (size_t)P.nbatch * P.nbins;
-    unsigned long long *stats_h = (unsigned long long *)(w_h + (size_t)P.nbatch * P.nbins);
-    CF_CUDA(cudaMemcpyAsync(cnt_h, W.hist_cnt.p, hb, cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaMemcpyAsync(avg_h, W.hist_avg.p, hb, cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaMemcpyAsync(w_h, W.hist_w.p, hb, cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaMemcpyAsync(stats_h, W.stats.p, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaMemcpyAsync(stats_h + 4, W.counter.p, sizeof(uint32_t) * 4, cudaMemcpyDeviceToHost, st));
-    CF_CUDA(cudaMemcpyAsync(stats_h + 6, W.oob.p, sizeof(unsigned long long) * 2, cudaMemcpyDeviceToHost, st));
+    CF_CUDA(cudaMemcpyAsync(W.h_hist.p, W.res.p, res_bytes(nb), cudaMemcpyDeviceToHost, st));
     return EXIT_SUCCESS;
 }
 
@@ -2582,24 +2759,21 @@ static int batch_collect(BatchPlan &P, cf_hist *H)
 {
     Workspace &W = P.W;
     const size_t nb = (size_t)P.nbatch * P.nbins;
-    const uint64_t *cnt_h = (const uint64_t *)W.h_hist.p;
-    const double *avg_h = (const double *)(cnt_h + nb), *w_h = avg_h + nb;
-    const unsigned long long *stats_h = (const unsigned long long *)(w_h + nb);
-    const uint32_t *flags = (const uint32_t *)(stats_h + 4);
-    if (stats_h[6] > 0) CF_FAIL("%llu particles are out of bounds. Check periodic wrapping?", stats_h[6]);
-    if (stats_h[7] > 0)
-        CF_FAIL("%llu points or weights left the box / weight range the batch was planned for; plan again", stats_h[7]);
-    if (flags[2]) CF_FAIL("internal: neighbour search needed a periodic image beyond +-1");
-    if (flags[3]) CF_FAIL("the batch work list outgrew its plan (catalogues changed since planning); plan again");
+    const ResView Rh = res_view(W.h_hist.p, nb);
+    if (*Rh.oob > 0) CF_FAIL("%llu particles are out of bounds. Check periodic wrapping?", *Rh.oob);
+    if (*Rh.extent > 0)
+        CF_FAIL("%llu points or weights left the box / weight range the batch was planned for; plan again", *Rh.extent);
+    if (Rh.flags[2]) CF_FAIL("internal: neighbour search needed a periodic image beyond +-1");
+    if (Rh.flags[3]) CF_FAIL("the batch work list outgrew its plan (catalogues changed since planning); plan again");
     for (int b = 0; b < P.nbatch; b++) {
         if (H[b].nbins != P.nbins) CF_FAIL("internal: histogram size mismatch");
-        memcpy(H[b].npairs, cnt_h + (size_t)b * P.nbins, sizeof(uint64_t) * P.nbins);
-        memcpy(H[b].avg, avg_h + (size_t)b * P.nbins, sizeof(double) * P.nbins);
-        memcpy(H[b].wsum, w_h + (size_t)b * P.nbins, sizeof(double) * P.nbins);
+        memcpy(H[b].npairs, Rh.cnt + (size_t)b * P.nbins, sizeof(uint64_t) * P.nbins);
+        memcpy(H[b].avg, Rh.avg + (size_t)b * P.nbins, sizeof(double) * P.nbins);
+        memcpy(H[b].wsum, Rh.w + (size_t)b * P.nbins, sizeof(double) * P.nbins);
     }
-    g_eng.last.pairs_evaluated = stats_h[0];
-    g_eng.last.pairs_refined = stats_h[1];
-    g_eng.last.pairs_slow = stats_h[2];
+    g_eng.last.pairs_evaluated = Rh.stats[0];
+    g_eng.last.pairs_refined = Rh.stats[1];
+    g_eng.last.pairs_slow = Rh.stats[2];
     return EXIT_SUCCESS;
 }
 
@@ -2736,6 +2910,7 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
             P->g.chk_lo[a] = glo[a];
             P->g.chk_hi[a] = per ? glo[a] + P->geo.wrap[a] : ghi[a];
         }
+        geom_keys(P->g);
         P->ncols = (uint32_t)P->g.n[0] * P->g.n[1];
         P->ncells = P->ncols * (uint32_t)P->g.n[2];
         g_eng.last.num_cells = (int)P->ncells;
@@ -2747,25 +2922,20 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
         const size_t nb = (size_t)nbatch * P->nbins;
         if ((rc = ensure_points(W.set[0], P->total1 > 0 ? P->total1 : 1)) != EXIT_SUCCESS ||
             (rc = ensure_points(W.set[1], P->J.n2)) != EXIT_SUCCESS ||
-            (rc = ensure(W.oob, sizeof(unsigned long long) * 2)) != EXIT_SUCCESS ||
-            (rc = ensure(W.counter, sizeof(uint32_t) * 4)) != EXIT_SUCCESS ||
+            (rc = ensure(W.res, res_bytes(nb))) != EXIT_SUCCESS ||
             (rc = ensure(W.chunk_cnt, sizeof(uint32_t) * P->ncols)) != EXIT_SUCCESS ||
             (rc = ensure(W.chunk_off, sizeof(uint32_t) * ((size_t)P->ncols + 1))) != EXIT_SUCCESS ||
             (rc = ensure(W.chunk_begin, sizeof(uint32_t) * ((size_t)P->total_slots + 1))) != EXIT_SUCCESS ||
             (rc = ensure(W.chunk_count, sizeof(uint32_t) * ((size_t)P->total_slots + 1))) != EXIT_SUCCESS ||
             (rc = ensure(W.chunk_cat, sizeof(uint16_t) * ((size_t)P->total_slots + 1))) != EXIT_SUCCESS ||
-            (rc = ensure(W.hist_cnt, sizeof(uint64_t) * nb)) != EXIT_SUCCESS ||
-            (rc = ensure(W.hist_avg, sizeof(double) * nb)) != EXIT_SUCCESS ||
-            (rc = ensure(W.hist_w, sizeof(double) * nb)) != EXIT_SUCCESS ||
-            (rc = ensure(W.stats, sizeof(unsigned long long) * 4)) != EXIT_SUCCESS ||
-            (rc = ensure_host(W.h_hist, sizeof(uint64_t) * (3 * nb + 10))) != EXIT_SUCCESS)
+            (rc = ensure_host(W.h_hist, res_bytes(nb))) != EXIT_SUCCESS)
             break;
         if ((rc = task_geometry(&P->J, P->geo, P->g, glo, ghi, false, MODE_R3, P->G)) != EXIT_SUCCESS) break;
         P->nentries = P->total_slots * (uint32_t)((2 * P->G.reach_x + 1) * (2 * P->G.reach_y + 1));
         if ((rc = ensure(W.ntask, sizeof(uint32_t) * ((size_t)P->nentries + 1))) != EXIT_SUCCESS ||
             (rc = ensure(W.task_off, sizeof(uint32_t) * ((size_t)P->nentries + 2))) != EXIT_SUCCESS)
             break;
-        P->G.error = (uint32_t *)W.counter.p + 2;
+        P->G.error = res_view(W.res.p, nb).flags + 2;
         if ((rc = build_tables(W, &P->J, MODE_R3, P->nbins, P->need_w, P->delta, &P->T)) != EXIT_SUCCESS) break;
 
         // ---- eager run: size the work list ----
@@ -2801,11 +2971,14 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
         A.ntasks = P->task_cap;
         A.ntask_dev = (const uint32_t *)W.task_off.p + P->nentries;
         pair_constants(A, &P->J, MODE_R3, P->nbins, false, P->G, P->geo, P->g, P->delta, P->T, P->wmax, W);
-        A.g_cnt = (unsigned long long *)W.hist_cnt.p;
-        A.g_avg = (double *)W.hist_avg.p;
-        A.g_w = (double *)W.hist_w.p;
-        A.g_stats = (unsigned long long *)W.stats.p;
-        A.task_counter = (uint32_t *)W.counter.p;
+        {
+            const ResView R = res_view(W.res.p, nb);
+            A.g_cnt = R.cnt;
+            A.g_avg = R.avg;
+            A.g_w = R.w;
+            A.g_stats = R.stats;
+            A.task_counter = R.flags;
+        }
         for (int k = 0; k < 4; k++)
             if (cudaEventCreate(&P->ev[k]) != cudaSuccess) rc = EXIT_FAILURE;
         if (rc != EXIT_SUCCESS) break;
@@ -2818,9 +2991,8 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
             break;
         }
         {
-            const unsigned long long *stats_h = (const unsigned long long *)((const uint64_t *)W.h_hist.p + 3 * nb);
-            const uint32_t *flags = (const uint32_t *)(stats_h + 4);
-            if (stats_h[6] > 0 || stats_h[7] > 0 || flags[2] || flags[3]) {
+            const ResView Rh = res_view(W.h_hist.p, nb);
+            if (*Rh.oob > 0 || *Rh.extent > 0 || Rh.flags[2] || Rh.flags[3]) {
                 fprintf(stderr, "corrfunc_gb300: batch planning failed (out-of-bounds points or work-list error)\n");
                 rc = EXIT_FAILURE;
                 break;
