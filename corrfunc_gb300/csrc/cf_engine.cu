@@ -527,16 +527,18 @@ __global__ void k_col_chunks(const uint32_t *cell_start, int ncols, int nz, uint
 }
 
 // chunk_begin holds absolute point indices (point_base + index within the catalogue's lattice);
-// chunk_cat, when given, receives the catalogue number of every chunk (batched counts)
+// chunk_cat, when given, receives the catalogue number of every chunk (batched counts).  One
+// warp per column, one chunk per lane.
 __global__ void k_chunk_emit(const uint32_t *cell_start, int ncols, int nz, const uint32_t *chunk_off,
                              uint32_t *chunk_begin, uint32_t *chunk_count, uint32_t point_base, uint16_t *chunk_cat,
                              uint16_t cat)
 {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
     if (c >= ncols) return;
     const uint32_t a = cell_start[(uint32_t)c * nz], b = cell_start[(uint32_t)(c + 1) * nz];
-    uint32_t o = chunk_off[c];
-    for (uint32_t p = a; p < b; p += kChunk, o++) {
+    const uint32_t o0 = chunk_off[c];
+    for (uint32_t k = lane; a + k * kChunk < b; k += 32) {
+        const uint32_t p = a + k * kChunk, o = o0 + k;
         chunk_begin[o] = point_base + p;
         chunk_count[o] = min((uint32_t)kChunk, b - p);
         if (chunk_cat) chunk_cat[o] = cat;
@@ -2523,7 +2525,7 @@ static int run_locked(cf_job *J, cf_hist *H)
     CF_CUDA(cudaGetLastError());
     if (scan_u32(W, (const uint32_t *)W.chunk_cnt.p, (uint32_t *)W.chunk_off.p, ncols, 0) != EXIT_SUCCESS)
         return EXIT_FAILURE;
-    k_chunk_emit<<<(ncols + 255) / 256, 256, 0, st>>>((const uint32_t *)S1.cell_start.p, (int)ncols, g.n[2],
+    k_chunk_emit<<<(ncols + 7) / 8, 256, 0, st>>>((const uint32_t *)S1.cell_start.p, (int)ncols, g.n[2],
                                                       (const uint32_t *)W.chunk_off.p,
                                                       (uint32_t *)W.chunk_begin.p, (uint32_t *)W.chunk_count.p,
                                                       0u, nullptr, 0);
@@ -2691,7 +2693,7 @@ static int batch_lattices(BatchPlan &P)
         CF_CUDA(cudaGetLastError());
         if (scan_u32(W, (const uint32_t *)W.chunk_cnt.p, (uint32_t *)W.chunk_off.p, P.ncols, 0) != EXIT_SUCCESS)
             return EXIT_FAILURE;
-        k_chunk_emit<<<(P.ncols + 255) / 256, 256, 0, st>>>(
+        k_chunk_emit<<<(P.ncols + 7) / 8, 256, 0, st>>>(
             (const uint32_t *)W.set[0].cell_start.p, (int)P.ncols, nz, (const uint32_t *)W.chunk_off.p,
             (uint32_t *)W.chunk_begin.p + P.cbase[b], (uint32_t *)W.chunk_count.p + P.cbase[b], (uint32_t)P.pbase[b],
             (uint16_t *)W.chunk_cat.p + P.cbase[b], (uint16_t)b);
