@@ -47,16 +47,20 @@ namespace {
 
 constexpr int kChunk = 32;          // points per i-chunk (one per lane)
 constexpr int kCatShift = 17;       // Task::meta bits 17-31: catalogue of a batched count
+// partial j tiles above this size run padded to 32 (fully unrolled); smaller ones pair by pair
+// (measured on this GPU: 16 is 2.7 % faster than 8 and 4.7 % faster than 4 on DD(r))
 #ifndef CF_PAD_MIN
-#define CF_PAD_MIN 8
+#define CF_PAD_MIN 16
 #endif
-constexpr int kPadMin = CF_PAD_MIN;  // partial j tiles above this size run padded to 32
+constexpr int kPadMin = CF_PAD_MIN;
 constexpr uint32_t kJMax = 2048;    // max j points per task
 constexpr int kRxy = 2;             // lattice columns per rmax_xy
+// z slabs per rmax_z: finer slabs trim the z windows of the work list (64 evaluates 0.9-1.2 %
+// fewer pairs than 32 on DD(r) at a few hundred kB of cell offsets)
 #ifndef CF_Z_SLABS
-#define CF_Z_SLABS 32
+#define CF_Z_SLABS 64
 #endif
-constexpr int kZFine = CF_Z_SLABS;  // z slabs per rmax_z
+constexpr int kZFine = CF_Z_SLABS;
 // the FP32 pair kernel's largest block and the resident blocks of that size per SM it is compiled
 // for: 2 x 512 threads caps it at 64 registers (32 resident warps per SM)
 #ifndef CF_PAIR_MAX_THREADS
@@ -2122,7 +2126,7 @@ static int build_tables(Workspace &W, const cf_job *J, int mode, int nbins, bool
 }
 
 // GPU lattice over the data extent [lo, hi] (or the periodic length): columns of about rlim/2 in
-// x and y, slabs of rlim_z/8 in z, a power-of-two FP32 grid q per axis and the coordinate error
+// x and y, slabs of rlim_z / kZFine in z, a power-of-two FP32 grid q per axis and the coordinate error
 // bound delta of the hi/lo split.
 // Columns per rmax in x and y.  A task pairs a chunk of 32 set-1 points of one column with the
 // z-window of each neighbour column; the candidates per chunk are the set-2 points in
