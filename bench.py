@@ -17,6 +17,7 @@ Prints one JSON line.  With --gpus N > 1 (launched by torchrun) every rank runs 
 replica of the workload on its own GPU ("replicas only": the path needs no collective).
 """
 import argparse
+import atexit
 import ctypes
 import json
 import os
@@ -137,45 +138,63 @@ def reference_work(lib, C, set1, set2, binfile, dtype):
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+    """nvidia-smi clocks / throttle reasons, sampled every 50 ms by one process that runs for the
+    whole benchmark.  A timed region is bracketed by `window()`; its summary takes the samples
+    from 0.3 s before to 0.3 s after the region (the warm-up and end-to-end loops around it keep
+    the GPU under load), since a region of a few milliseconds holds no sample of its own."""
 
     FIELDS = ["clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.hw_slowdown",
               "clocks_event_reasons.hw_thermal_slowdown", "clocks_event_reasons.sw_thermal_slowdown",
               "clocks_event_reasons.sw_power_cap"]
+    MARGIN_S = 0.3
+    _running = {}
 
     def __init__(self, device_index):
         self.dev = device_index
         self.proc = None
-        self.lines = []
+        self.lines = []  # (perf_counter time, csv line)
 
-    def __enter__(self):
+    @classmethod
+    def shared(cls, device_index):
+        if device_index not in cls._running:
+            smp = cls(device_index)
+            smp.start()
+            cls._running[device_index] = smp
+        return cls._running[device_index]
+
+    def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + ",".join(self.FIELDS),
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=subprocess.PIPE,
                                          stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            atexit.register(self.stop)
+            t_end = time.perf_counter() + 2.0  # wait for the first sample
+            while not self.lines and time.perf_counter() < t_end and self.proc.poll() is None:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
         return self
 
     def _read(self):
         for ln in self.proc.stdout:
-            self.lines.append(ln.strip())
+            self.lines.append((time.perf_counter(), ln.strip()))
 
-    def __exit__(self, *exc):
-        if self.proc is not None:
+    def stop(self):
+        if self.proc is not None and self.proc.poll() is None:
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
-        return False
 
-    def summary(self):
+    def summary(self, t0=None, t1=None):
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for t, ln in list(self.lines):
+            if t0 is not None and not (t0 - self.MARGIN_S <= t <= t1 + self.MARGIN_S):
+                continue
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 7:
                 continue
@@ -191,6 +210,32 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+class _ClockWindow:
+    """`with clock_window(dev) as clocks:` around a timed region; `clocks.summary()` afterwards
+    (called after the region and the loops that follow it, so that the trailing margin is in)."""
+
+    def __init__(self, device_index):
+        self.smp = ClockSampler.shared(device_index)
+
+    def __enter__(self):
+        self.t0 = time.perf_counter()
+        return self
+
+    def __exit__(self, *exc):
+        self.t1 = time.perf_counter()
+        return False
+
+    def summary(self):
+        wait = self.t1 + ClockSampler.MARGIN_S + 0.06 - time.perf_counter()
+        if wait > 0:
+            time.sleep(wait)
+        return self.smp.summary(self.t0, self.t1)
+
+
+def clock_window(device_index):
+    return _ClockWindow(device_index)
 
 
 def flush_l2(torch, dev):
@@ -301,6 +346,7 @@ def run_batch_workload(args):
         if not np.array_equal(first[k]["npairs"], npairs[1:]):
             raise RuntimeError("batched counts differ from countpairs() for catalogue %d" % k)
 
+    ClockSampler.shared(local)  # clock samples from the warm-up on
     for _ in range(max(args.warmup, 3)):
         batch.run()
         flush_l2(torch, dev)
@@ -308,7 +354,7 @@ def run_batch_workload(args):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize(dev)
-    with ClockSampler(local) as clocks:
+    with clock_window(local) as clocks:
         for _ in range(args.steps):
             out = batch.run()
             st = corrfunc_gb300.last_stats()
@@ -508,12 +554,13 @@ def run_survey_workload(args):
                                weight_type="pair_product", isa="fallback")
         return r, time.perf_counter() - t0, cf.last_stats()
 
+    ClockSampler.shared(local)  # clock samples from the warm-up on
     for _ in range(max(args.warmup, 3)):
         ref, _, _ = call()
         flush_l2(torch, dev)
     npair = W["n1"] * (W["n1"] - 1) / 2.0
     gpu_ms, pair_ms, walls, launches = [], [], [], 0
-    with ClockSampler(local) as clocks:
+    with clock_window(local) as clocks:
         for _ in range(args.steps):
             r, wall, st = call()
             if not np.array_equal(r["npairs"], ref["npairs"]):
@@ -657,6 +704,7 @@ def main():
         lib.free_results(ctypes.byref(res))
         return npairs, corrfunc_gb300.last_stats()
 
+    ClockSampler.shared(local)  # clock samples from the warm-up on
     for _ in range(max(args.warmup, 3)):
         ref_np, _ = step_device()
         flush_l2(torch, dev)
@@ -665,7 +713,7 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize(dev)
-    with ClockSampler(local) as clocks:
+    with clock_window(local) as clocks:
         for _ in range(args.steps):
             t0 = time.perf_counter()
             npairs, st = step_device()
