@@ -311,3 +311,45 @@ def test_gpu_many_bins_and_fine_2d_histograms(gpu, orc):
     got = theory.DDsmu(1, 1, rp, 1.0, 90, x, y, z, periodic=True, boxsize=L)
     want = orc.DDsmu(1, rp, 1.0, 90, x, y, z, periodic=True, boxsize=L)
     assert np.array_equal(got["npairs"], want["npairs"])
+
+
+COORD_RANGES = {
+    # non-periodic clouds whose coordinates exercise the integer (fixed-point) lattice build:
+    # far from the origin, negative, a tiny extent, one flat axis, values straddling +-0
+    "far_offset": dict(lo=(1.0e6, -2.5e5, 3.0e7), span=(40.0, 40.0, 40.0), bins=(0.3, 12.0)),
+    "negative": dict(lo=(-300.0, -280.0, -260.0), span=(30.0, 30.0, 30.0), bins=(0.2, 9.0)),
+    "tiny_extent": dict(lo=(5.0, 5.0, 5.0), span=(2e-4, 2e-4, 2e-4), bins=(2e-6, 1.5e-4)),
+    "flat_z": dict(lo=(0.0, 0.0, 7.25), span=(25.0, 25.0, 0.0), bins=(0.2, 8.0)),
+    "around_zero": dict(lo=(-1e-3, -1e-3, -1e-3), span=(2e-3, 2e-3, 2e-3), bins=(1e-6, 1.2e-3)),
+}
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32], ids=["f64", "f32"])
+@pytest.mark.parametrize("name", sorted(COORD_RANGES))
+def test_gpu_coordinate_ranges(gpu, orc, precision, name, dtype):
+    """Counts and averages follow the oracle for coordinate ranges that stress the fixed-point
+    hi / lo split, the FP32 cell index and its margins, in both precisions."""
+    from corrfunc_gb300 import theory
+    c = COORD_RANGES[name]
+    rng = np.random.default_rng(sum(ord(ch) for ch in name))
+    n = 1500
+    pos = [np.asarray(c["lo"][a] + rng.random(n) * c["span"][a], dtype=dtype) for a in range(3)]
+    if name == "around_zero":
+        pos[0][:20] = 0.0
+        pos[1][:10] = -0.0
+        pos[2][:5] = 0.0
+    bins = np.logspace(np.log10(c["bins"][0]), np.log10(c["bins"][1]), 11)
+    w = rng.uniform(0.5, 1.5, n).astype(dtype)
+    kw = dict(weights1=w, weight_type="pair_product", periodic=False, output_ravg=True)
+    got = theory.DD(1, 1, bins, *pos, **kw)
+    want = orc.DD(1, bins, *(p.astype(np.float64) for p in pos), weights1=w.astype(np.float64),
+                  weight_type="pair_product", periodic=False, output_ravg=True)
+    assert np.array_equal(got["npairs"], want["npairs"])
+    assert int(got["npairs"].sum()) > 0
+    rtol = RTOL_AVG if dtype == np.float64 else 1e-4
+    np.testing.assert_allclose(got["ravg"], want["ravg"], rtol=rtol, atol=1e-12)
+    np.testing.assert_allclose(got["weightavg"], want["weightavg"], rtol=rtol, atol=1e-12)
+    pimax = max(float(np.ceil(c["bins"][1])), 1.0)  # whole pi bins of 1
+    got = theory.DDrppi(1, 1, pimax, bins, *pos, periodic=False)
+    want = orc.DDrppi(1, pimax, bins, *(p.astype(np.float64) for p in pos), periodic=False)
+    assert np.array_equal(got["npairs"], want["npairs"])
