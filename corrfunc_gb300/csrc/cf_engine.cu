@@ -97,6 +97,7 @@ constexpr int kMockUnroll = CF_MOCK_UNROLL;
 constexpr int kR3Unroll = CF_R3_UNROLL;
 
 constexpr int kScanTile = 4096;
+constexpr uint32_t kLutMax = 8192;  // largest bucket table (32 KB of shared memory)
 
 // modes with an FP32 classification kernel (the others always run the FP64 kernel)
 constexpr bool has_f32_path(int mode) { return mode >= 0 && mode < kNumModes; }
@@ -714,7 +715,7 @@ struct RefineEntry {
 constexpr int kColumnTerms = 1 << 15;
 
 __host__ __device__ inline SmemLayout smem_layout(int nedges, int nbins, int warps, bool f64, int lut_n, int lane_stride,
-                                                  bool need_avg, bool need_w, bool store_dz)
+                                                  bool need_avg, bool need_w, bool store_dz, bool lo_stage)
 {
     SmemLayout L;
     L.need_avg = need_avg;
@@ -738,7 +739,10 @@ __host__ __device__ inline SmemLayout smem_layout(int nedges, int nbins, int war
     L.lut_off = o;
     o = align_up(o + sizeof(uint32_t) * (lut_n + 1), 16);
     L.stage_off = o;
-    // f32: float4 hi[32] + float4 lo[32] + refine queue; f64: double4_32a[32] + int rc[32] + int orig[32]
+    // f32: float4 hi[32] + float4 lo[32] + refine and slow queues (the lo half is laid out even
+    // where it stays unused: the histogram layouts were measured with it);
+    // f64: double4_32a[32] + int rc[32] + int orig[32]
+    (void)lo_stage;
     L.per_warp_stage = f64 ? (32 * sizeof(double4_32a) + 64 * sizeof(int))
                            : (64 * sizeof(float4) + (kRefineQueue + kSlowQueue) * sizeof(RefineEntry) + 16);
     o = align_up(o + L.per_warp_stage * warps, 16);
@@ -1879,25 +1883,58 @@ static int pair_kernel_regs(int mode, bool f64, bool avg, bool w)
 // Histogram layout and block size.  Lanes l and l + lane_stride share a column; the score is the
 // resident warps per SM (shared memory and registers) discounted by the expected contention of
 // shared columns (1 = private, 2 = 2-way, ... 32 = the whole warp on one row).
+// warps of the FP32 pair kernel resident per SM with layout c (shared memory, threads, registers)
+static int layout_resident(const SmemLayout &c, int mode, bool avg, bool w)
+{
+    if (c.total > 220 * 1024) return 0;
+    (void)mode;
+    const int regs = pair_kernel_regs(mode, false, avg, w);
+    const int warps_by_regs = 65536 / (32 * ((regs + 7) / 8 * 8));
+    int blocks = (int)(g_eng.smem_per_sm / (c.total + 1024));
+    const int max_blocks_threads = 2048 / (32 * c.warps);
+    if (blocks > max_blocks_threads) blocks = max_blocks_threads;
+    const int max_blocks_regs = warps_by_regs / c.warps;
+    if (blocks > max_blocks_regs) blocks = max_blocks_regs;
+    return blocks * c.warps;
+}
+
+// resident warps weighted by the measured cost of lanes sharing histogram columns
+static double lane_factor(int lane_stride)
+{
+    // measured: 2-way sharing costs a few per cent, 4-way about a third (64-bit weight sums)
+    switch (lane_stride) {
+    case 32: return 1.0;
+    case 16: return 0.92;
+    case 8: return 0.6;
+    case 4: return 0.45;
+    default: return 0.2;
+    }
+}
+static double layout_score(const SmemLayout &c, int mode, bool avg, bool w)
+{
+    int resident = layout_resident(c, mode, avg, w);
+    if (resident > 48) resident = 48;
+    return resident * lane_factor(c.lane_stride);
+}
+
 static SmemLayout choose_layout(int mode, bool f64, bool avg, bool w, int nedges, int nbins, int lut_n)
 {
     const bool dz = (mode == MODE_RPPI || mode == MODE_WP || mode == MODE_SMU || mode_is_mock(mode));
+    const bool los = avg || mode_is_mock(mode);
     if (!f64 && g_eng.force_ls > 0 && g_eng.force_warps > 0) {
-        const SmemLayout c = smem_layout(nedges, nbins, g_eng.force_warps, f64, lut_n, g_eng.force_ls, avg, w, dz);
+        const SmemLayout c = smem_layout(nedges, nbins, g_eng.force_warps, f64, lut_n, g_eng.force_ls, avg, w, dz, los);
         if (c.total <= 220 * 1024) return c;
     }
     const int regs = pair_kernel_regs(mode, f64, avg, w);
     const int warps_by_regs = 65536 / (32 * ((regs + 7) / 8 * 8));
-    SmemLayout SL = smem_layout(nedges, nbins, 8, f64, lut_n, 1, avg, w, dz);
+    SmemLayout SL = smem_layout(nedges, nbins, 8, f64, lut_n, 1, avg, w, dz, los);
     double best = -1.0;
     const int lstrides[5] = {32, 16, 8, 4, 1};
-    // measured: 2-way sharing costs a few per cent, 4-way about a third (64-bit weight sums)
-    const double lfactor[5] = {1.0, 0.92, 0.6, 0.45, 0.2};
     const int max_warps = f64 ? 8 : CF_PAIR_MAX_THREADS / 32;
     const int wopts[3] = {max_warps, max_warps / 2, max_warps / 4};
     for (int li = 0; li < 5; li++) {
         for (int wi = 0; wi < 3; wi++) {
-            const SmemLayout c = smem_layout(nedges, nbins, wopts[wi], f64, lut_n, lstrides[li], avg, w, dz);
+            const SmemLayout c = smem_layout(nedges, nbins, wopts[wi], f64, lut_n, lstrides[li], avg, w, dz, los);
             if (c.total > 220 * 1024) continue;
             int blocks = (int)(g_eng.smem_per_sm / (c.total + 1024));
             const int max_blocks_threads = 2048 / (32 * wopts[wi]);
@@ -1906,7 +1943,7 @@ static SmemLayout choose_layout(int mode, bool f64, bool avg, bool w, int nedges
             if (blocks > max_blocks_regs) blocks = max_blocks_regs;
             int resident = blocks * wopts[wi];
             if (resident > 48) resident = 48;
-            const double score = resident * lfactor[li] + 1e-3 * wopts[wi];
+            const double score = resident * lane_factor(lstrides[li]) + 1e-3 * wopts[wi];
             if (score > best) {
                 best = score;
                 SL = c;
@@ -2045,7 +2082,7 @@ static int build_tables(Workspace &W, const cf_job *J, int mode, int nbins, bool
     T->guard_off = tab_align(sizeof(double) * ne);
     T->ascale_off = tab_align(T->guard_off + sizeof(float) * 2 * ne);
     T->lut_off = tab_align(T->ascale_off + sizeof(float) * ne);
-    const size_t tab_max = T->lut_off + sizeof(uint32_t) * 4100;
+    const size_t tab_max = T->lut_off + sizeof(uint32_t) * (kLutMax + 4);
     if (ensure_host(W.h_tab, tab_max) != EXIT_SUCCESS || ensure(W.tab, tab_max) != EXIT_SUCCESS) return EXIT_FAILURE;
     double *edges_h = (double *)W.h_tab.p;
     float *guards_h = (float *)((char *)W.h_tab.p + T->guard_off);
@@ -2089,8 +2126,25 @@ static int build_tables(Workspace &W, const cf_job *J, int mode, int nbins, bool
     uint32_t blo, bhi;
     memcpy(&blo, &qlo, 4);
     memcpy(&bhi, &qhi, 4);
-    int shift = 1;
-    while (((bhi >> shift) - (blo >> shift)) + 1 > 4096u) shift++;
+    // Bucket width: the finest that gives at most kLutMax buckets while the histogram layout
+    // scores as well as with a table of kLutMax / 2 (same resident warps and column sharing; a
+    // bucket holding a guard sends its pairs to the exact path, so finer buckets send fewer).
+    auto lut_shift = [&](uint32_t limit) {
+        int sh = 1;
+        while (((bhi >> sh) - (blo >> sh)) + 1 > limit) sh++;
+        return sh;
+    };
+    int shift = lut_shift(kLutMax / 2);
+    {
+        const int sh2 = lut_shift(kLutMax);
+        const int n1 = (int)((bhi >> shift) - (blo >> shift)) + 1, n2 = (int)((bhi >> sh2) - (blo >> sh2)) + 1;
+        if (sh2 < shift &&
+            layout_score(choose_layout(mode, false, J->need_avg != 0, need_w, J->nedges, nbins, n2), mode, J->need_avg != 0,
+                         need_w) >=
+                layout_score(choose_layout(mode, false, J->need_avg != 0, need_w, J->nedges, nbins, n1), mode,
+                             J->need_avg != 0, need_w))
+            shift = sh2;
+    }
     const int base = (int)(blo >> shift);
     const int n = (int)((bhi >> shift) - (blo >> shift)) + 1;
     // row byte offsets: the layout (private columns or shared row) is fixed before the launch
@@ -3014,7 +3068,7 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
             for (int li = 0; li < 3 && rc == EXIT_SUCCESS; li++) {
                 for (int wi = 0; wi < 3 && rc == EXIT_SUCCESS; wi++) {
                     const SmemLayout c = smem_layout(P->J.nedges, P->nbins, cand_w[wi], false, P->T.lut_n, cand_ls[li],
-                                                     P->J.need_avg != 0, P->need_w, false);
+                                                     P->J.need_avg != 0, P->need_w, false, P->J.need_avg != 0);
                     if (c.total > 220 * 1024) continue;
                     g_eng.force_ls = cand_ls[li];
                     g_eng.force_warps = cand_w[wi];
