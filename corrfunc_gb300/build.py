@@ -73,8 +73,10 @@ def build(verbose=False, extra_nvcc=()):
 
 
 # the reference's per-module library names (theory/*/Makefile, mocks/*/Makefile: LIBNAME)
+# per-module library names of the reference's makefiles, and the generic GPU link name
 MODULE_LIBS = ("countpairs", "countpairs_rp_pi", "countpairs_s_mu", "countpairs_wp", "countpairs_xi", "countspheres",
-               "countpairs_theta_mocks", "countpairs_rp_pi_mocks", "countpairs_s_mu_mocks", "countspheres_mocks")
+               "countpairs_theta_mocks", "countpairs_rp_pi_mocks", "countpairs_s_mu_mocks", "countspheres_mocks",
+               "corrfunc_gpu")
 
 
 def link_module_names():

@@ -351,7 +351,7 @@ def _build_compat(tmp_path):
     exe = tmp_path / "prog"
     libdir = os.path.join(ROOT, "corrfunc_gb300")
     r = subprocess.run(["gcc", "-std=c99", str(src), "-o", str(exe), "-I", os.path.join(ROOT, "include", "compat"),
-                        "-L" + libdir, "-lcountpairs", "-lcountpairs_rp_pi_mocks", "-Wl,-rpath," + libdir, "-lm"],
+                        "-L" + libdir, "-lcountpairs", "-lcountpairs_rp_pi_mocks", "-lcorrfunc_gpu", "-Wl,-rpath," + libdir, "-lm"],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     return str(exe)
