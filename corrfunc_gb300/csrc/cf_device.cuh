@@ -28,9 +28,7 @@ struct Lattice {
     float4 *hi;       // x_hi, y_hi, z_hi on the per-axis grid q (exact differences), w as float
     float4 *lo;       // x - x_hi, y - y_hi, z - z_hi (float), unused
     double4_32a *dbl;     // original coordinates (x, y, z, w) in double
-    int *refcell;     // cell index of the point in the reference lattice (first-point rule)
-    int *orig;        // index of the point in the caller's arrays
-    uint32_t *cellid; // GPU lattice cell of each sorted point
+    int2 *ro;         // reference-lattice cell (first-point rule), index in the caller's arrays
     uint32_t *cell_start; // ncells + 1 offsets
 };
 
@@ -50,10 +48,10 @@ struct PairArgs {
     // lattices (set 1 = i points, set 2 = j points; identical for auto-correlations)
     const float4 *hi1, *lo1;
     const double4_32a *d1;
-    const int *rc1, *or1;
+    const int2 *ro1;  // per point: reference-lattice cell, index in the caller's arrays
     const float4 *hi2, *lo2;
     const double4_32a *d2;
-    const int *rc2, *or2;
+    const int2 *ro2;
 
     const Task *tasks;
     uint32_t ntasks;            // task count, or the work-list capacity when ntask_dev is set

@@ -433,7 +433,7 @@ __device__ __forceinline__ unsigned long long abs_okey(double v)
 __device__ __forceinline__ unsigned long long abs_okey(float v) { return abs_okey((double)v); }
 
 // Lattice records of every point at its slot of the counting sort.  L.lo (separation averages,
-// survey modes) and L.refcell (FP64 kernel) are written only when set.
+// survey modes) is written only when set.
 template <typename T>
 __global__ void k_scatter(const T *x, const T *y, const T *z, const T *w, int64_t n, Geom g,
                           const uint32_t *cellid, const uint32_t *cell_start, uint32_t *fill,
@@ -458,9 +458,7 @@ __global__ void k_scatter(const T *x, const T *y, const T *z, const T *w, int64_
         int r[3];
 #pragma unroll
         for (int a = 0; a < 3; a++) r[a] = ref_axis_cell(p[a], X[a], g, a);
-        L.refcell[pos] = (r[0] * g.ref_n[1] + r[1]) * g.ref_n[2] + r[2];
-        L.orig[pos] = (int)i;
-        L.cellid[pos] = c;
+        L.ro[pos] = make_int2((r[0] * g.ref_n[1] + r[1]) * g.ref_n[2] + r[2], (int)i);
     }
 }
 
@@ -531,21 +529,37 @@ __global__ void k_col_chunks(const uint32_t *cell_start, int ncols, int nz, uint
     chunks_per_col[c] = (b - a + kChunk - 1) / kChunk;
 }
 
+// z slab of sorted point p of a column whose slab offsets are cs[0..nz] (the last slab whose
+// offset is <= p; empty slabs before it share its offset)
+__device__ __forceinline__ uint32_t slab_of(const uint32_t *cs, int nz, uint32_t p)
+{
+    int lo = 0, hi = nz;  // cs[lo] <= p < cs[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (cs[mid] <= p) lo = mid;
+        else hi = mid;
+    }
+    return (uint32_t)lo;
+}
+
 // chunk_begin holds absolute point indices (point_base + index within the catalogue's lattice);
+// chunk_info the chunk's size (bits 0-5), first and last z slab (bits 6-17, 18-29) and column;
 // chunk_cat, when given, receives the catalogue number of every chunk (batched counts).  One
 // warp per column, one chunk per lane.
 __global__ void k_chunk_emit(const uint32_t *cell_start, int ncols, int nz, const uint32_t *chunk_off,
-                             uint32_t *chunk_begin, uint32_t *chunk_count, uint32_t point_base, uint16_t *chunk_cat,
+                             uint32_t *chunk_begin, uint2 *chunk_info, uint32_t point_base, uint16_t *chunk_cat,
                              uint16_t cat)
 {
     const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
     if (c >= ncols) return;
-    const uint32_t a = cell_start[(uint32_t)c * nz], b = cell_start[(uint32_t)(c + 1) * nz];
+    const uint32_t *cs = cell_start + (uint32_t)c * nz;
+    const uint32_t a = cs[0], b = cs[nz];
     const uint32_t o0 = chunk_off[c];
     for (uint32_t k = lane; a + k * kChunk < b; k += 32) {
         const uint32_t p = a + k * kChunk, o = o0 + k;
+        const uint32_t cnt = min((uint32_t)kChunk, b - p);
         chunk_begin[o] = point_base + p;
-        chunk_count[o] = min((uint32_t)kChunk, b - p);
+        chunk_info[o] = make_uint2(cnt | (slab_of(cs, nz, p) << 6) | (slab_of(cs, nz, p + cnt - 1) << 18), (uint32_t)c);
         if (chunk_cat) chunk_cat[o] = cat;
     }
 }
@@ -594,17 +608,17 @@ __host__ __device__ inline int column_wz(const TaskGeom &G, int dx, int dy)
 // image whose window is not empty, split into ranges of at most kJMax points.  With EMIT == false
 // only counted.
 template <bool EMIT>
-__device__ uint32_t chunk_col_tasks(const TaskGeom &G, uint32_t ib, uint32_t icount, const uint32_t *cellid1,
-                                    const uint32_t *cs2, Task *out, uint32_t cat, uint32_t room, int dx, int dy, int c)
+__device__ uint32_t chunk_col_tasks(const TaskGeom &G, uint32_t ib, uint2 info, const uint32_t *cs2, Task *out,
+                                    uint32_t cat, uint32_t room, int dx, int dy, int c)
 {
+    const uint32_t icount = info.x & 63u;
     if (icount == 0) return 0;  // unused chunk slot
     if (G.autocorr && (dx < 0 || (dx == 0 && dy < 0))) return 0;  // half stencil
     const int wz = G.ntab ? (int)G.wz_tab[c] : column_wz(G, dx, dy);
     if (wz < 0) return 0;
-    const uint32_t c0 = cellid1[ib], c1 = cellid1[ib + icount - 1];
     const int nz = G.nz;
-    const int col = (int)(c0 / nz);
-    const int a = (int)(c0 % nz), b = (int)(c1 % nz);
+    const int col = (int)info.y;
+    const int a = (int)((info.x >> 6) & 4095u), b = (int)((info.x >> 18) & 4095u);
     const int ix = col / G.ny, iy = col % G.ny;
     // periodic images are encoded in two bits; the lattice construction keeps |m| <= 1
     // (neighbour reach < half the period), anything else is reported and skipped.
@@ -654,23 +668,23 @@ __device__ uint32_t chunk_col_tasks(const TaskGeom &G, uint32_t ib, uint32_t ico
 
 // One thread per (chunk slot, neighbour column): slot = x index, stencil column c = blockIdx.y;
 // entry k = slot * ncoff + c.
-__global__ void k_task_count(TaskGeom G, uint32_t nslots, const uint32_t *chunk_begin, const uint32_t *chunk_count,
-                             const uint32_t *cellid1, const uint32_t *cs2, uint32_t *ntasks)
+__global__ void k_task_count(TaskGeom G, uint32_t nslots, const uint32_t *chunk_begin, const uint2 *chunk_info,
+                             const uint32_t *cs2, uint32_t *ntasks)
 {
     const uint32_t ny = 2 * G.reach_y + 1, ncoff = (2 * G.reach_x + 1) * ny;
     const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
     if (slot >= nslots) return;
-    ntasks[(uint64_t)slot * ncoff + c] = chunk_col_tasks<false>(G, chunk_begin[slot], chunk_count[slot], cellid1, cs2,
-                                                                nullptr, 0, 0, (int)(c / ny) - G.reach_x,
-                                                                (int)(c % ny) - G.reach_y, (int)c);
+    ntasks[(uint64_t)slot * ncoff + c] = chunk_col_tasks<false>(G, chunk_begin[slot], chunk_info[slot], cs2, nullptr, 0,
+                                                                0, (int)(c / ny) - G.reach_x, (int)(c % ny) - G.reach_y,
+                                                                (int)c);
 }
 
 // Writes the tasks of every (chunk, column) at its offset; with a capacity smaller than the total
 // the tail is dropped and *overflow set (the caller resizes and runs again).  flags[1] receives
 // the total (task_off[nslots * ncoff]), flags[3] the overflow.
-__global__ void k_task_emit(TaskGeom G, uint32_t nslots, const uint32_t *chunk_begin, const uint32_t *chunk_count,
-                            const uint32_t *cellid1, const uint32_t *cs2, const uint32_t *task_off, Task *tasks,
-                            const uint16_t *chunk_cat, uint32_t capacity, uint32_t *flags)
+__global__ void k_task_emit(TaskGeom G, uint32_t nslots, const uint32_t *chunk_begin, const uint2 *chunk_info,
+                            const uint32_t *cs2, const uint32_t *task_off, Task *tasks, const uint16_t *chunk_cat,
+                            uint32_t capacity, uint32_t *flags)
 {
     const uint32_t ny = 2 * G.reach_y + 1, ncoff = (2 * G.reach_x + 1) * ny;
     const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
@@ -678,7 +692,7 @@ __global__ void k_task_emit(TaskGeom G, uint32_t nslots, const uint32_t *chunk_b
     if (slot >= nslots) return;
     const uint32_t off = task_off[(uint64_t)slot * ncoff + c];
     const uint32_t room = off < capacity ? capacity - off : 0u;
-    const uint32_t n = chunk_col_tasks<true>(G, chunk_begin[slot], chunk_count[slot], cellid1, cs2, tasks + off,
+    const uint32_t n = chunk_col_tasks<true>(G, chunk_begin[slot], chunk_info[slot], cs2, tasks + off,
                                              chunk_cat ? (uint32_t)chunk_cat[slot] : 0u, room,
                                              (int)(c / ny) - G.reach_x, (int)(c % ny) - G.reach_y, (int)c);
     if (n > room) atomicOr(&flags[3], 1u);
@@ -834,10 +848,10 @@ __device__ __forceinline__ void flush_hist(const PairArgs &A, WarpHist h, int la
 // first-point rule of the reference for wrapped auto-correlation pairs
 __device__ __forceinline__ bool j_is_first(const PairArgs &A, uint32_t i, uint32_t j, double zi, double zj)
 {
-    const int ri = A.rc1[i], rj = A.rc2[j];
-    if (rj != ri) return rj > ri;
+    const int2 ri = A.ro1[i], rj = A.ro2[j];
+    if (rj.x != ri.x) return rj.x > ri.x;
     if (zj != zi) return zj < zi;
-    return A.or2[j] < A.or1[i];
+    return rj.y < ri.y;
 }
 
 template <int MODE>
@@ -1436,8 +1450,7 @@ __global__ void __launch_bounds__(256) k_pairs_f64(PairArgs A, SmemLayout SL)
         asc[k] = A.g_ascale[k];
     }
     double4_32a *sj = (double4_32a *)(smem + SL.stage_off + SL.per_warp_stage * warp);
-    int *srcell = (int *)(sj + 32);
-    int *sorig = srcell + 32;
+    int2 *sro = (int2 *)(sj + 32);  // reference cell, caller index
     WarpHist h = warp_hist(smem, SL, warp);
     zero_hist(h, SL, lane);
     const int hl = lane & (SL.lane_stride - 1);
@@ -1468,15 +1481,14 @@ __global__ void __launch_bounds__(256) k_pairs_f64(PairArgs A, SmemLayout SL)
         const uint32_t i = T.i_begin + lane;
         const bool ivalid = lane < icount;
         const double4_32a pi = ivalid ? A.d1[i] : make_double4_32a(0, 0, 0, 0);
-        const int rci = ivalid ? A.rc1[i] : 0;
-        const int ori = ivalid ? A.or1[i] : 0;
+        const int2 roi = ivalid ? A.ro1[i] : make_int2(0, 0);
+        const int rci = roi.x, ori = roi.y;
         const double ox = A.odbl[0][mx + 1], oy = A.odbl[1][my + 1], oz = A.odbl[2][mz + 1];
         for (uint32_t jb = T.j_begin; jb < T.j_end; jb += 32) {
             const uint32_t nj = min(32u, T.j_end - jb);
             if ((uint32_t)lane < nj) {
                 sj[lane] = A.d2[jb + lane];
-                srcell[lane] = A.rc2[jb + lane];
-                sorig[lane] = A.or2[jb + lane];
+                sro[lane] = A.ro2[jb + lane];
             }
             __syncwarp();
             if (ivalid) {
@@ -1487,7 +1499,7 @@ __global__ void __launch_bounds__(256) k_pairs_f64(PairArgs A, SmemLayout SL)
                     double avg_term = 0.0;
                     int bin;
                     if (MODE != MODE_THETA && A.autocorr && wrapped &&
-                        (srcell[k] > rci || (srcell[k] == rci && (pj.z < pi.z || (pj.z == pi.z && sorig[k] < ori))))) {
+                        (sro[k].x > rci || (sro[k].x == rci && (pj.z < pi.z || (pj.z == pi.z && sro[k].y < ori))))) {
                         bin = ref_eval<MODE>(A, se, pj.x, pj.y, pj.z, pi.x, pi.y, pi.z, ox, oy, oz, &avg_term);
                     } else {
                         bin = ref_eval<MODE>(A, se, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, -ox, -oy, -oz, &avg_term);
@@ -1572,14 +1584,14 @@ struct SetBufs {
     DevBuf raw[4];  // device copies of x, y, z, w as given (float or double)
     const void *in[4];  // arrays the lattice is built from: raw[] or caller-owned device arrays
     DevBuf cellid_u, count, fill, cell_start;
-    DevBuf hi, lo, dbl, refcell, orig, cellid;
+    DevBuf hi, lo, dbl, ro;
 };
 
 // Every device and pinned buffer one count uses.  Single calls share the engine's workspace;
 // a batch plan owns one, so that its captured graph never sees a buffer move.
 struct Workspace {
     SetBufs set[2];
-    DevBuf mm, scan_tmp[4], chunk_cnt, chunk_off, chunk_begin, chunk_count, chunk_cat, ntask, task_off, tasks;
+    DevBuf mm, scan_tmp[4], chunk_cnt, chunk_off, chunk_begin, chunk_info, chunk_cat, ntask, task_off, tasks;
     DevBuf res, tab;  // result block (ResView), bin tables (edges, guards, averages scale, lookup table)
     HostBuf h_small, h_tab, h_hist;
 };
@@ -1626,11 +1638,11 @@ static void release_workspace(Workspace &W)
     for (int s = 0; s < 2; s++) {
         SetBufs &B = W.set[s];
         for (int k = 0; k < 4; k++) release(B.raw[k]);
-        DevBuf *v[] = {&B.cellid_u, &B.count, &B.fill, &B.cell_start, &B.hi, &B.lo, &B.dbl, &B.refcell, &B.orig, &B.cellid};
+        DevBuf *v[] = {&B.cellid_u, &B.count, &B.fill, &B.cell_start, &B.hi, &B.lo, &B.dbl, &B.ro};
         for (DevBuf *d : v) release(*d);
     }
     for (int k = 0; k < 4; k++) release(W.scan_tmp[k]);
-    DevBuf *v[] = {&W.mm, &W.chunk_cnt, &W.chunk_off, &W.chunk_begin, &W.chunk_count, &W.chunk_cat, &W.ntask,
+    DevBuf *v[] = {&W.mm, &W.chunk_cnt, &W.chunk_off, &W.chunk_begin, &W.chunk_info, &W.chunk_cat, &W.ntask,
                    &W.task_off, &W.tasks, &W.res, &W.tab};
     for (DevBuf *d : v) release(*d);
     HostBuf *h[] = {&W.h_small, &W.h_tab, &W.h_hist};
@@ -1811,9 +1823,7 @@ static int build_lattice_at(Workspace &W, SetBufs &B, int64_t n, int64_t base, c
     L.hi = (float4 *)B.hi.p + base;
     L.lo = g.write_lo ? (float4 *)B.lo.p + base : nullptr;
     L.dbl = (double4_32a *)B.dbl.p + base;
-    L.refcell = (int *)B.refcell.p + base;
-    L.orig = (int *)B.orig.p + base;
-    L.cellid = (uint32_t *)B.cellid.p + base;
+    L.ro = (int2 *)B.ro.p + base;
     L.cell_start = (uint32_t *)B.cell_start.p;
     k_scatter<T><<<grid, 256, 0, st>>>(x, y, z, w, n, g, cellid_u, (const uint32_t *)B.cell_start.p, fill, L);
     g_eng.launches++;
@@ -1824,8 +1834,7 @@ static int build_lattice_at(Workspace &W, SetBufs &B, int64_t n, int64_t base, c
 static int ensure_points(SetBufs &B, int64_t n)
 {
     if (ensure(B.cellid_u, sizeof(uint32_t) * n) || ensure(B.hi, sizeof(float4) * n) || ensure(B.lo, sizeof(float4) * n) ||
-        ensure(B.dbl, sizeof(double4_32a) * n) || ensure(B.refcell, sizeof(int) * n) || ensure(B.orig, sizeof(int) * n) ||
-        ensure(B.cellid, sizeof(uint32_t) * n))
+        ensure(B.dbl, sizeof(double4_32a) * n) || ensure(B.ro, sizeof(int2) * n))
         return EXIT_FAILURE;
     return EXIT_SUCCESS;
 }
@@ -2574,9 +2583,9 @@ static int run_locked(cf_job *J, cf_hist *H)
     // ---- chunks: fixed slot range (empty slots hold 0 points), no host wait ----
     const uint32_t max_chunks = (uint32_t)((n1 + kChunk - 1) / kChunk + ncols);
     if (ensure(W.chunk_cnt, sizeof(uint32_t) * ncols) || ensure(W.chunk_off, sizeof(uint32_t) * ((size_t)ncols + 1)) ||
-        ensure(W.chunk_begin, sizeof(uint32_t) * max_chunks) || ensure(W.chunk_count, sizeof(uint32_t) * max_chunks))
+        ensure(W.chunk_begin, sizeof(uint32_t) * max_chunks) || ensure(W.chunk_info, sizeof(uint2) * max_chunks))
         return EXIT_FAILURE;
-    CF_CUDA(cudaMemsetAsync(W.chunk_count.p, 0, sizeof(uint32_t) * max_chunks, st));
+    CF_CUDA(cudaMemsetAsync(W.chunk_info.p, 0, sizeof(uint2) * max_chunks, st));
     k_col_chunks<<<(ncols + 255) / 256, 256, 0, st>>>((const uint32_t *)S1.cell_start.p, (int)ncols, g.n[2],
                                                       (uint32_t *)W.chunk_cnt.p);
     g_eng.launches++;
@@ -2585,7 +2594,7 @@ static int run_locked(cf_job *J, cf_hist *H)
         return EXIT_FAILURE;
     k_chunk_emit<<<(ncols + 7) / 8, 256, 0, st>>>((const uint32_t *)S1.cell_start.p, (int)ncols, g.n[2],
                                                       (const uint32_t *)W.chunk_off.p,
-                                                      (uint32_t *)W.chunk_begin.p, (uint32_t *)W.chunk_count.p,
+                                                      (uint32_t *)W.chunk_begin.p, (uint2 *)W.chunk_info.p,
                                                       0u, nullptr, 0);
     g_eng.launches++;
     CF_CUDA(cudaGetLastError());
@@ -2599,8 +2608,7 @@ static int run_locked(cf_job *J, cf_hist *H)
         ensure(W.task_off, sizeof(uint32_t) * ((size_t)nentries + 2)))
         return EXIT_FAILURE;
     k_task_count<<<task_grid(G, max_chunks), 128, 0, st>>>(G, max_chunks, (const uint32_t *)W.chunk_begin.p,
-                                                           (const uint32_t *)W.chunk_count.p,
-                                                           (const uint32_t *)S1.cellid.p,
+                                                           (const uint2 *)W.chunk_info.p,
                                                            (const uint32_t *)S2.cell_start.p, (uint32_t *)W.ntask.p);
     g_eng.launches++;
     CF_CUDA(cudaGetLastError());
@@ -2620,13 +2628,11 @@ static int run_locked(cf_job *J, cf_hist *H)
     A.hi1 = (const float4 *)S1.hi.p;
     A.lo1 = (const float4 *)S1.lo.p;
     A.d1 = (const double4_32a *)S1.dbl.p;
-    A.rc1 = (const int *)S1.refcell.p;
-    A.or1 = (const int *)S1.orig.p;
+    A.ro1 = (const int2 *)S1.ro.p;
     A.hi2 = (const float4 *)S2.hi.p;
     A.lo2 = (const float4 *)S2.lo.p;
     A.d2 = (const double4_32a *)S2.dbl.p;
-    A.rc2 = (const int *)S2.refcell.p;
-    A.or2 = (const int *)S2.orig.p;
+    A.ro2 = (const int2 *)S2.ro.p;
     A.ntask_dev = (const uint32_t *)W.task_off.p + nentries;
     pair_constants(A, J, mode, nbins, autocorr, G, geo, g, delta, T, wmax, W);
     A.g_cnt = R.cnt;
@@ -2641,8 +2647,7 @@ static int run_locked(cf_job *J, cf_hist *H)
         A.tasks = (const Task *)W.tasks.p;
         A.ntasks = (uint32_t)cap;
         k_task_emit<<<task_grid(G, max_chunks), 128, 0, st>>>(G, max_chunks, (const uint32_t *)W.chunk_begin.p,
-                                                              (const uint32_t *)W.chunk_count.p,
-                                                              (const uint32_t *)S1.cellid.p,
+                                                              (const uint2 *)W.chunk_info.p,
                                                               (const uint32_t *)S2.cell_start.p,
                                                               (const uint32_t *)W.task_off.p, (Task *)W.tasks.p, nullptr,
                                                               (uint32_t)cap, R.flags);
@@ -2753,7 +2758,7 @@ static int batch_lattices(BatchPlan &P)
             return EXIT_FAILURE;
         k_chunk_emit<<<(P.ncols + 7) / 8, 256, 0, st>>>(
             (const uint32_t *)W.set[0].cell_start.p, (int)P.ncols, nz, (const uint32_t *)W.chunk_off.p,
-            (uint32_t *)W.chunk_begin.p + P.cbase[b], (uint32_t *)W.chunk_count.p + P.cbase[b], (uint32_t)P.pbase[b],
+            (uint32_t *)W.chunk_begin.p + P.cbase[b], (uint2 *)W.chunk_info.p + P.cbase[b], (uint32_t)P.pbase[b],
             (uint16_t *)W.chunk_cat.p + P.cbase[b], (uint16_t)b);
         g_eng.launches++;
         CF_CUDA(cudaGetLastError());
@@ -2781,19 +2786,19 @@ static int batch_enqueue(BatchPlan &P, int phase, bool timing)
     if (phase == 0) {
         CF_CUDA(cudaMemsetAsync(res_view(W.res.p, (size_t)P.nbatch * P.nbins).flags, 0, sizeof(unsigned long long) * 4,
                                 st));  // flags, oob, extent
-        CF_CUDA(cudaMemsetAsync(W.chunk_count.p, 0, sizeof(uint32_t) * P.total_slots, st));
+        CF_CUDA(cudaMemsetAsync(W.chunk_info.p, 0, sizeof(uint2) * P.total_slots, st));
         const int rc = P.isf ? batch_lattices<float>(P) : batch_lattices<double>(P);
         if (rc != EXIT_SUCCESS) return EXIT_FAILURE;
         k_task_count<<<task_grid(P.G, P.total_slots), 128, 0, st>>>(
-            P.G, P.total_slots, (const uint32_t *)W.chunk_begin.p, (const uint32_t *)W.chunk_count.p,
-            (const uint32_t *)W.set[0].cellid.p, (const uint32_t *)W.set[1].cell_start.p, (uint32_t *)W.ntask.p);
+            P.G, P.total_slots, (const uint32_t *)W.chunk_begin.p, (const uint2 *)W.chunk_info.p,
+            (const uint32_t *)W.set[1].cell_start.p, (uint32_t *)W.ntask.p);
         g_eng.launches++;
         CF_CUDA(cudaGetLastError());
         return scan_u32(W, (const uint32_t *)W.ntask.p, (uint32_t *)W.task_off.p, P.nentries, 0);
     }
     k_task_emit<<<task_grid(P.G, P.total_slots), 128, 0, st>>>(
-        P.G, P.total_slots, (const uint32_t *)W.chunk_begin.p, (const uint32_t *)W.chunk_count.p,
-        (const uint32_t *)W.set[0].cellid.p, (const uint32_t *)W.set[1].cell_start.p, (const uint32_t *)W.task_off.p,
+        P.G, P.total_slots, (const uint32_t *)W.chunk_begin.p, (const uint2 *)W.chunk_info.p,
+        (const uint32_t *)W.set[1].cell_start.p, (const uint32_t *)W.task_off.p,
         (Task *)W.tasks.p, (const uint16_t *)W.chunk_cat.p, P.task_cap, res_view(W.res.p, (size_t)P.nbatch * P.nbins).flags);
     g_eng.launches++;
     CF_CUDA(cudaGetLastError());
@@ -2986,7 +2991,7 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
             (rc = ensure(W.chunk_cnt, sizeof(uint32_t) * P->ncols)) != EXIT_SUCCESS ||
             (rc = ensure(W.chunk_off, sizeof(uint32_t) * ((size_t)P->ncols + 1))) != EXIT_SUCCESS ||
             (rc = ensure(W.chunk_begin, sizeof(uint32_t) * ((size_t)P->total_slots + 1))) != EXIT_SUCCESS ||
-            (rc = ensure(W.chunk_count, sizeof(uint32_t) * ((size_t)P->total_slots + 1))) != EXIT_SUCCESS ||
+            (rc = ensure(W.chunk_info, sizeof(uint2) * ((size_t)P->total_slots + 1))) != EXIT_SUCCESS ||
             (rc = ensure(W.chunk_cat, sizeof(uint16_t) * ((size_t)P->total_slots + 1))) != EXIT_SUCCESS ||
             (rc = ensure_host(W.h_hist, res_bytes(nb))) != EXIT_SUCCESS)
             break;
@@ -3020,13 +3025,11 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
         A.hi1 = (const float4 *)W.set[0].hi.p;
         A.lo1 = (const float4 *)W.set[0].lo.p;
         A.d1 = (const double4_32a *)W.set[0].dbl.p;
-        A.rc1 = (const int *)W.set[0].refcell.p;
-        A.or1 = (const int *)W.set[0].orig.p;
+        A.ro1 = (const int2 *)W.set[0].ro.p;
         A.hi2 = (const float4 *)W.set[1].hi.p;
         A.lo2 = (const float4 *)W.set[1].lo.p;
         A.d2 = (const double4_32a *)W.set[1].dbl.p;
-        A.rc2 = (const int *)W.set[1].refcell.p;
-        A.or2 = (const int *)W.set[1].orig.p;
+        A.ro2 = (const int2 *)W.set[1].ro.p;
         A.tasks = (const Task *)W.tasks.p;
         A.ntasks = P->task_cap;
         A.ntask_dev = (const uint32_t *)W.task_off.p + P->nentries;
