@@ -698,6 +698,38 @@ __global__ void k_task_emit(TaskGeom G, uint32_t nslots, const uint32_t *chunk_b
     if (n > room) atomicOr(&flags[3], 1u);
 }
 
+// Counts and writes the tasks of every (chunk, column) in one pass: each warp reserves room for
+// its tasks with one atomic on flags[1] (the running total, also past the capacity) and every
+// lane writes its own at its offset; tasks beyond the capacity are dropped and flags[3] set (the
+// caller resizes to flags[1] and runs again).  The order of the work list is the order in which
+// warps reserve, which only changes which warp of the pair kernel takes which task.
+__global__ void k_task_list(TaskGeom G, uint32_t nslots, const uint32_t *chunk_begin, const uint2 *chunk_info,
+                            const uint32_t *cs2, Task *tasks, uint32_t capacity, uint32_t *flags)
+{
+    const uint32_t ny = 2 * G.reach_y + 1;
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+    const int lane = threadIdx.x & 31;
+    const int dx = (int)(c / ny) - G.reach_x, dy = (int)(c % ny) - G.reach_y;
+    const bool live = slot < nslots;
+    const uint32_t ib = live ? chunk_begin[slot] : 0u;
+    const uint2 info = live ? chunk_info[slot] : make_uint2(0u, 0u);
+    const uint32_t n = chunk_col_tasks<false>(G, ib, info, cs2, nullptr, 0, 0, dx, dy, (int)c);
+    uint32_t incl = n;  // inclusive warp scan of the task counts
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    uint32_t base = 0;
+    if (lane == 31 && total) base = atomicAdd(&flags[1], total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    if (n == 0) return;
+    const uint32_t off = base + incl - n;
+    const uint32_t room = off < capacity ? capacity - off : 0u;
+    chunk_col_tasks<true>(G, ib, info, cs2, tasks + off, 0u, room, dx, dy, (int)c);
+    if (n > room) atomicOr(&flags[3], 1u);
+}
+
 // ------------------------------------------------------------------------------------
 // pair kernels
 // ------------------------------------------------------------------------------------
@@ -2599,21 +2631,10 @@ static int run_locked(cf_job *J, cf_hist *H)
     g_eng.launches++;
     CF_CUDA(cudaGetLastError());
 
-    // ---- tasks: counted and emitted on the device into a buffer sized from earlier calls ----
+    // ---- tasks: listed on the device in one pass into a buffer sized from earlier calls ----
     TaskGeom G;
     if (task_geometry(J, geo, g, lo, hi, autocorr, mode, G) != EXIT_SUCCESS) return EXIT_FAILURE;
     G.error = R.flags + 2;
-    const uint32_t nentries = max_chunks * (uint32_t)((2 * G.reach_x + 1) * (2 * G.reach_y + 1));
-    if (ensure(W.ntask, sizeof(uint32_t) * ((size_t)nentries + 1)) ||
-        ensure(W.task_off, sizeof(uint32_t) * ((size_t)nentries + 2)))
-        return EXIT_FAILURE;
-    k_task_count<<<task_grid(G, max_chunks), 128, 0, st>>>(G, max_chunks, (const uint32_t *)W.chunk_begin.p,
-                                                           (const uint2 *)W.chunk_info.p,
-                                                           (const uint32_t *)S2.cell_start.p, (uint32_t *)W.ntask.p);
-    g_eng.launches++;
-    CF_CUDA(cudaGetLastError());
-    if (scan_u32(W, (const uint32_t *)W.ntask.p, (uint32_t *)W.task_off.p, nentries, 0) != EXIT_SUCCESS)
-        return EXIT_FAILURE;
     // capacity: what this lattice needed last time, else about one task per neighbour column
     const size_t guess = (size_t)max_chunks * (2 * G.reach_x + 1) * (2 * G.reach_y + 1) * 5 / 4 + 1024;
     size_t cap = W.tasks.cap / sizeof(Task);
@@ -2633,7 +2654,7 @@ static int run_locked(cf_job *J, cf_hist *H)
     A.lo2 = (const float4 *)S2.lo.p;
     A.d2 = (const double4_32a *)S2.dbl.p;
     A.ro2 = (const int2 *)S2.ro.p;
-    A.ntask_dev = (const uint32_t *)W.task_off.p + nentries;
+    A.ntask_dev = R.flags + 1;  // tasks listed (capped by the capacity in the kernel)
     pair_constants(A, J, mode, nbins, autocorr, G, geo, g, delta, T, wmax, W);
     A.g_cnt = R.cnt;
     A.g_avg = R.avg;
@@ -2646,10 +2667,9 @@ static int run_locked(cf_job *J, cf_hist *H)
     for (int attempt = 0; attempt < 2; attempt++) {
         A.tasks = (const Task *)W.tasks.p;
         A.ntasks = (uint32_t)cap;
-        k_task_emit<<<task_grid(G, max_chunks), 128, 0, st>>>(G, max_chunks, (const uint32_t *)W.chunk_begin.p,
+        k_task_list<<<task_grid(G, max_chunks), 128, 0, st>>>(G, max_chunks, (const uint32_t *)W.chunk_begin.p,
                                                               (const uint2 *)W.chunk_info.p,
-                                                              (const uint32_t *)S2.cell_start.p,
-                                                              (const uint32_t *)W.task_off.p, (Task *)W.tasks.p, nullptr,
+                                                              (const uint32_t *)S2.cell_start.p, (Task *)W.tasks.p,
                                                               (uint32_t)cap, R.flags);
         g_eng.launches++;
         CF_CUDA(cudaGetLastError());
@@ -2671,7 +2691,7 @@ static int run_locked(cf_job *J, cf_hist *H)
         if (ensure(W.tasks, sizeof(Task) * cap) != EXIT_SUCCESS) return EXIT_FAILURE;
         cap = W.tasks.cap / sizeof(Task);
         if (cap > 0xffffffffu) cap = 0xffffffffu;
-        CF_CUDA(cudaMemsetAsync(R.flags + 3, 0, sizeof(uint32_t), st));  // overflow flag
+        CF_CUDA(cudaMemsetAsync(R.flags + 1, 0, 3 * sizeof(uint32_t), st));  // task total, image error, overflow
     }
     g_eng.last.tasks = Rh.flags[1];
     memcpy(H->npairs, Rh.cnt, sizeof(uint64_t) * nbins);
