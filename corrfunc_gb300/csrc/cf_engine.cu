@@ -272,6 +272,8 @@ __device__ __forceinline__ unsigned long long warp_max(unsigned long long v)
     return v;
 }
 
+constexpr int kMinmaxUnroll = 4;
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_minmax(const T *x, const T *y, const T *z, const T *w, int64_t n,
                                                 unsigned long long *mm)
@@ -280,13 +282,18 @@ __global__ void __launch_bounds__(256) k_minmax(const T *x, const T *y, const T 
     K mn[3] = {(K)~(K)0, (K)~(K)0, (K)~(K)0}, mx[3] = {0, 0, 0}, wm = 0;
     uint32_t bad = 0;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    // two points per iteration: both sets of loads are issued before the compares
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += 2 * stride) {
-        const int64_t i2 = i + stride;
-        const bool two = i2 < n;
-        const T c[6] = {x[i], y[i], z[i], two ? x[i2] : x[i], two ? y[i2] : y[i], two ? z[i2] : z[i]};
+    // kMinmaxUnroll points per iteration: all their loads are issued before the compares
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += kMinmaxUnroll * stride) {
+        T c[3 * kMinmaxUnroll];
 #pragma unroll
-        for (int k = 0; k < 6; k++) {
+        for (int u = 0; u < kMinmaxUnroll; u++) {
+            const int64_t iu = i + u * stride < n ? i + u * stride : i;  // repeats of point i are harmless
+            c[3 * u] = x[iu];
+            c[3 * u + 1] = y[iu];
+            c[3 * u + 2] = z[iu];
+        }
+#pragma unroll
+        for (int k = 0; k < 3 * kMinmaxUnroll; k++) {
             const int a = k % 3;
             bad |= nonfinite(c[k]) ? 1u : 0u;
             const K key = okey(c[k]);
@@ -294,9 +301,12 @@ __global__ void __launch_bounds__(256) k_minmax(const T *x, const T *y, const T 
             mx[a] = key > mx[a] ? key : mx[a];
         }
         if (w) {
-            const K k1 = abskey(w[i]), k2 = two ? abskey(w[i2]) : k1;
-            wm = k1 > wm ? k1 : wm;
-            wm = k2 > wm ? k2 : wm;
+#pragma unroll
+            for (int u = 0; u < kMinmaxUnroll; u++) {
+                const int64_t iu = i + u * stride < n ? i + u * stride : i;
+                const K kw = abskey(w[iu]);
+                wm = kw > wm ? kw : wm;
+            }
         }
     }
     __shared__ unsigned long long part[8][8];
@@ -1797,8 +1807,8 @@ template <typename T>
 static int minmax_into(Workspace &W, const T *x, const T *y, const T *z, const T *w, int64_t n, unsigned long long *mm)
 {
     if (n <= 0) return EXIT_SUCCESS;
-    int grid = grid_for((n + 1) / 2, 256);
-    if (grid > 8 * g_eng.num_sms) grid = 8 * g_eng.num_sms;
+    int grid = grid_for((n + kMinmaxUnroll - 1) / kMinmaxUnroll, 256);
+    if (grid > 4 * g_eng.num_sms) grid = 4 * g_eng.num_sms;
     (void)W;
     k_minmax<T><<<grid, 256, 0, g_eng.stream>>>(x, y, z, w, n, mm);
     CF_CUDA(cudaGetLastError());
