@@ -131,8 +131,12 @@ struct Geom {
     // X - o_hi and X - o_cell are exact and give the hi / lo split and the cell index.
     int e_fix[3];
     unsigned long long o_hi[3], o_cell[3];  // X of hi_origin and of origin
-    float q_f[3], rho_f[3], inv_s_f[3];     // q, 2^e_fix, 1 / s
-    float eps_cell[3];                      // bound on the position error of the FP32 cell index
+    float q_f[3], rho_f[3];                 // q, 2^e_fix
+    // cell index = umulhi(X - o_cell, cell_mul) >> cell_shift: (x - origin) / s in 64-bit
+    // fixed point, within eps_cell (position units) of the exact value
+    unsigned long long cell_mul[3];
+    int cell_shift[3];
+    double eps_cell[3];
     // order keys (okey0) of the extent checks, and of the range of coordinates that are inside
     // the reference lattice whatever the rounding of its FP64 cell index (others take the exact test)
     unsigned long long k_chk_lo[3], k_chk_hi[3], k_chk_wmax;
@@ -345,16 +349,15 @@ __global__ void __launch_bounds__(256) k_minmax(const T *x, const T *y, const T 
     }
 }
 
-// Cell index along axis a from the fixed-point coordinate X: (x - origin) / s in FP32, within
-// eps_cell (position units) of the exact value; the neighbour search margins cover it.
+// Cell index along axis a from the fixed-point coordinate X: (x - origin) / s by a 64-bit
+// reciprocal multiply, within eps_cell (position units) of the exact value; the neighbour search
+// margins cover it.  Points below the origin (none in a valid call) go to cell 0.
 __device__ __forceinline__ int axis_cell(unsigned long long X, const Geom &g, int a)
 {
-    float h, l;
-    fix_split(X - g.o_cell[a], g.q_f[a], g.rho_f[a], &h, &l);
-    int i = (int)floorf((h + l) * g.inv_s_f[a]);
-    i = i < 0 ? 0 : i;
-    i = i >= g.n[a] ? g.n[a] - 1 : i;
-    return i;
+    const unsigned long long U = X - g.o_cell[a];
+    if ((long long)U < 0) return 0;
+    const unsigned long long t = __umul64hi(U, g.cell_mul[a]) >> g.cell_shift[a];
+    return t >= (unsigned long long)g.n[a] ? g.n[a] - 1 : (int)t;
 }
 
 // cell index of a point in the reference lattice, in the reference's FP64 arithmetic
@@ -2277,7 +2280,17 @@ static void geom_keys(Geom &g)
     for (int a = 0; a < 3; a++) {
         g.o_hi[a] = fix_of(g.hi_origin[a], g.e_fix[a]);
         g.o_cell[a] = fix_of(g.origin[a], g.e_fix[a]);
-        g.inv_s_f[a] = (float)g.inv_s[a];
+        // reciprocal of the cell size in fixed-point units S = s / 2^e_fix, with the largest
+        // shift k that keeps cell_mul = 2^(64+k) / S below 2^63
+        const double S = ldexp(g.s[a], -g.e_fix[a]);
+        int k = ilogb(S) - 1;
+        k = k < 0 ? 0 : (k > 63 ? 63 : k);
+        const double m = ldexp(1.0, 64 + k) / S;
+        g.cell_shift[a] = k;
+        g.cell_mul[a] = m >= 0x1p64 ? ~0ull : (unsigned long long)m;
+        // |cell - (x - origin)/s| <= t 2^-51 + 2^-k cells (rounding of the reciprocal, truncation)
+        // plus the fixed-point rounding of x and of the origin (2^e_fix each)
+        g.eps_cell[a] = ldexp(g.s[a] * (double)g.n[a], -50) + ldexp(g.s[a], 1 - k) + ldexp(4.0, g.e_fix[a]);
         // coordinates in [ref_min - cell / 2, ref_min + (ref_n + 1/2) cells] get a reference cell in
         // [0, ref_n] before the reference's clamp of the top cell, whatever the FP64 rounding
         const double c = 1.0 / g.ref_inv[a];
@@ -2312,11 +2325,11 @@ static int gpu_geometry(const cf_job *J, const cf_geometry &geo, const double lo
     }
     const int rxy = choose_rxy(J, ext0);
     const int refine[3] = {rxy, rxy, kZFine};
-    // position error of the FP32 cell index (a few ulps of x - origin, doubled), and the cell
+    // estimate of the position error of the cell index (set exactly in geom_keys), and the cell
     // widening that keeps the neighbour reach at 'refine' cells with the search margins
     // (2 eps_cell per axis, the plane taking the larger of x and y) added to the radii
     double eps[3];
-    for (int a = 0; a < 3; a++) eps[a] = ldexp(1.0, -21) * fmax(ext0[a], 0.0);
+    for (int a = 0; a < 3; a++) eps[a] = ldexp(1.0, -40) * fmax(ext0[a], 0.0);
     const double eps_xy = fmax(eps[0], eps[1]);
     for (int a = 0; a < 3; a++) {
         const bool per = geo.periodic[a] && geo.wrap[a] > 0.0;
@@ -2356,7 +2369,6 @@ static int gpu_geometry(const cf_job *J, const cf_geometry &geo, const double lo
         g.e_fix[a] = ilogb(g.q[a]) - 31;
         g.q_f[a] = (float)g.q[a];
         g.rho_f[a] = ldexpf(1.0f, g.e_fix[a]);
-        g.eps_cell[a] = (float)eps[a];
         const double maxabs = fmax(fabs(lo[a]), fabs(hi[a])) + (per ? geo.wrap[a] : 0.0);
         delta[a] = 1.5 * g.q[a] + ldexp(1.0, -49) * (maxabs + span[a]);
         g.ref_min[a] = geo.ref_min[a];
@@ -2394,7 +2406,7 @@ static int task_geometry(const cf_job *J, const cf_geometry &geo, const Geom &g,
     for (int a = 0; a < 3; a++) maxabs_all = fmax(maxabs_all, fmax(fabs(lo[a]), fabs(hi[a])) + (geo.periodic[a] ? geo.wrap[a] : 0.0));
     // ... plus twice the position error of the FP32 cell index of each point
     const double margin_xy = 1e-9 * fmax(g.s[0], g.s[1]) + 1e-13 * maxabs_all + 2.0 * fmax(g.eps_cell[0], g.eps_cell[1]);
-    const double margin_z = 1e-9 * g.s[2] + 1e-13 * maxabs_all + 2.0 * (double)g.eps_cell[2];
+    const double margin_z = 1e-9 * g.s[2] + 1e-13 * maxabs_all + 2.0 * g.eps_cell[2];
     memset(&G, 0, sizeof(G));
     G.nx = g.n[0];
     G.ny = g.n[1];
