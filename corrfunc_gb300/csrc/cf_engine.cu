@@ -2,8 +2,9 @@
 //
 // Replaces the reference's three hot stages:
 //   * gridlink (utils/gridlink_impl.c.src:65-436): a device counting sort of the points into
-//     a lattice of (x,y) columns x fine z slabs, written as SoA records (FP32 hi/lo grid
-//     coordinates, FP64 copies, reference-lattice cell ids);
+//     a lattice of (x,y) columns x fine z slabs, in integer and FP32 arithmetic on fixed-point
+//     coordinates, written as SoA records (FP32 hi/lo grid coordinates, FP64 copies,
+//     reference-lattice cell and caller index);
 //   * generate_cell_pairs (utils/gridlink_impl.c.src:439-625): a device-built worklist of
 //     (32-point column chunk, neighbouring column z-window) tasks with periodic images, the
 //     auto-correlation half stencil and a min-separation prune;
