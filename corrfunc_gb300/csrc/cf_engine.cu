@@ -1708,6 +1708,7 @@ struct Engine {
     Workspace ws;
     int regs_cache[kNumModes][4][2] = {};  // registers per thread of each pair kernel (0 = not queried)
     int force_ls = 0, force_warps = 0;  // FP32 pair-kernel layout chosen by the batch tuner (0 = scored)
+    uint32_t task_cap0 = 0;  // first work-list capacity of a call (0 = from the lattice; CF_TASK_CAPACITY)
     int precision = CF_PRECISION_FP32_REFINE;
     int launches = 0;  // kernels launched by the current call
     size_t smem_per_sm = 228 * 1024;
@@ -1749,6 +1750,10 @@ static int engine_init(void)
         g_eng.force_ls = ls;
         g_eng.force_warps = wp;
     }
+    // CF_TASK_CAPACITY=<n> starts every single call with a work-list buffer of n tasks (tests use
+    // a small n to exercise the resize-and-rerun path)
+    const char *tc = getenv("CF_TASK_CAPACITY");
+    if (tc && atoi(tc) > 0) g_eng.task_cap0 = (uint32_t)atoi(tc);
     g_eng.init = true;
     return EXIT_SUCCESS;
 }
@@ -2665,6 +2670,7 @@ static int run_locked(cf_job *J, cf_hist *H)
     if (ensure(W.tasks, sizeof(Task) * cap) != EXIT_SUCCESS) return EXIT_FAILURE;
     cap = W.tasks.cap / sizeof(Task);
     if (cap > 0xffffffffu) cap = 0xffffffffu;
+    if (g_eng.task_cap0 > 0 && g_eng.task_cap0 < cap) cap = g_eng.task_cap0;
 
     // ---- pair-kernel arguments ----
     PairArgs A;

@@ -353,3 +353,32 @@ def test_gpu_coordinate_ranges(gpu, orc, precision, name, dtype):
     got = theory.DDrppi(1, 1, pimax, bins, *pos, periodic=False)
     want = orc.DDrppi(1, pimax, bins, *(p.astype(np.float64) for p in pos), periodic=False)
     assert np.array_equal(got["npairs"], want["npairs"])
+
+
+def test_gpu_work_list_resize(gpu, tmp_path):
+    """A work list that outgrows its first buffer (forced by CF_TASK_CAPACITY=100 in a child
+    process) is resized and the count rerun: the same counts and averages as the default path."""
+    import subprocess
+    from corrfunc_gb300 import theory
+    rng = np.random.default_rng(91)
+    x, y, z = (rng.random(20000) * 100.0 for _ in range(3))
+    path = tmp_path / "pts.npy"
+    np.save(str(path), np.stack([x, y, z]))
+    bins = np.logspace(-1, np.log10(12.0), 10)
+    want = theory.DD(1, 1, bins, x, y, z, periodic=True, boxsize=100.0, output_ravg=True)
+    code = ("import sys, numpy as np; sys.path.insert(0, %r)\n"
+            "from corrfunc_gb300 import theory\n"
+            "import corrfunc_gb300\n"
+            "x, y, z = np.load(%r)\n"
+            "r = theory.DD(1, 1, np.logspace(-1, np.log10(12.0), 10), x, y, z, periodic=True, boxsize=100.0,"
+            " output_ravg=True)\n"
+            "print(' '.join(str(int(v)) for v in r['npairs']))\n"
+            "print(' '.join(repr(float(v)) for v in r['ravg']))\n"
+            "print(corrfunc_gb300.last_stats()['tasks'])\n") % (os.path.dirname(HERE), str(path))
+    env = dict(os.environ, CF_TASK_CAPACITY="100")
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=300)
+    assert out.returncode == 0, out.stderr
+    lines = out.stdout.split("\n")
+    assert [int(v) for v in lines[0].split()] == [int(v) for v in want["npairs"]]
+    np.testing.assert_allclose([float(v) for v in lines[1].split()], want["ravg"], rtol=1e-12, atol=1e-15)
+    assert int(lines[2]) > 100  # the list did outgrow the forced buffer
