@@ -21,10 +21,10 @@ def _fix_ra_dec(ra, dec):
     any DEC > 90 (the caller's arrays are modified, as with the reference)."""
     if not hasattr(ra, "dtype") or not hasattr(dec, "dtype"):
         raise TypeError("Input RA array must be a numpy array")
-    if min(ra) < 0.0:
+    if np.min(ra) < 0.0:  # numpy reductions: the builtins iterate element by element in Python
         print("Warning: found negative RA values, wrapping into [0.0, 360.0]  range")
         ra += 180.0
-    if max(dec) > 90.0:
+    if np.max(dec) > 90.0:
         print("Warning: found DEC values more than 90.0; wrapping into [-90.0, 90.0] range")
         dec -= 90.0
     return ra, dec
