@@ -10,6 +10,7 @@
 #define _GNU_SOURCE
 #include <math.h>
 #include <stdint.h>
+#include <pthread.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -1164,7 +1165,54 @@ static int cosmology_omega_m(int cosmology, double *omega_m)
  * step dz = 1e-2 / max_size on 1/E(z), one sample every 1/max_size in z up to zmax.  The
  * operation order is the reference's (this file is compiled without contractions).  Returns
  * the number of samples. */
+/* The table of the most recent call with the largest zmax so far, per (omega_m, max_size).  The
+ * Simpson loop below visits the same z values in the same order whatever zmax is, so the table for
+ * a smaller zmax is a prefix of a longer one (its entries recorded before the loop reached zmax):
+ * later calls copy that prefix instead of integrating again. */
+static pthread_mutex_t g_cosmo_lock = PTHREAD_MUTEX_INITIALIZER;
+static struct {
+    double omega_m, zmax;
+    int max_size, n;
+    double *z, *d;
+} g_cosmo = {0.0, 0.0, 0, 0, NULL, NULL};
+
+static int comoving_table_compute(double zmax, int max_size, double omega_m, double *zc, double *dc);
+
 static int comoving_table(double zmax, int max_size, double omega_m, double *zc, double *dc)
+{
+    int n = -1;
+    pthread_mutex_lock(&g_cosmo_lock);
+    if (g_cosmo.z && g_cosmo.omega_m == omega_m && g_cosmo.max_size == max_size && zmax <= g_cosmo.zmax) {
+        n = 0;
+        while (n < g_cosmo.n && g_cosmo.z[n] < zmax) n++;
+        memcpy(zc, g_cosmo.z, sizeof(double) * (size_t)n);
+        memcpy(dc, g_cosmo.d, sizeof(double) * (size_t)n);
+    }
+    pthread_mutex_unlock(&g_cosmo_lock);
+    if (n >= 0) return n;
+    n = comoving_table_compute(zmax, max_size, omega_m, zc, dc);
+    pthread_mutex_lock(&g_cosmo_lock);
+    double *z = malloc(sizeof(double) * (size_t)(n > 0 ? n : 1)), *d = malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+    if (z && d) {
+        memcpy(z, zc, sizeof(double) * (size_t)n);
+        memcpy(d, dc, sizeof(double) * (size_t)n);
+        free(g_cosmo.z);
+        free(g_cosmo.d);
+        g_cosmo.z = z;
+        g_cosmo.d = d;
+        g_cosmo.n = n;
+        g_cosmo.zmax = zmax;
+        g_cosmo.omega_m = omega_m;
+        g_cosmo.max_size = max_size;
+    } else {
+        free(z);
+        free(d);
+    }
+    pthread_mutex_unlock(&g_cosmo_lock);
+    return n;
+}
+
+static int comoving_table_compute(double zmax, int max_size, double omega_m, double *zc, double *dc)
 {
     const double omega_l = 1.0 - omega_m;
     const double omega_k = 1.0 - omega_m - omega_l;
