@@ -126,8 +126,9 @@ struct Geom {
     unsigned long long *extent_err;
     double chk_lo[3], chk_hi[3];
     double chk_wmax;
-    // Integer view of the coordinates (the lattice kernels run no FP64 arithmetic: on this GPU
-    // the FP64 pipe issues at 1/64 of the FP32 rate).  A coordinate x becomes the fixed-point
+    // Integer view of the coordinates (the lattice kernels keep FP64 arithmetic off their common
+    // path -- on this GPU the FP64 pipe issues at 1/64 of the FP32 rate -- and use it only for
+    // the rare points near a reference-cell boundary).  A coordinate x becomes the fixed-point
     // integer X = round(x / 2^e_fix) modulo 2^64 (e_fix = log2(q) - 31); the differences
     // X - o_hi and X - o_cell are exact and give the hi / lo split and the cell index.
     int e_fix[3];
