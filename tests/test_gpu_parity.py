@@ -382,3 +382,23 @@ def test_gpu_work_list_resize(gpu, tmp_path):
     assert [int(v) for v in lines[0].split()] == [int(v) for v in want["npairs"]]
     np.testing.assert_allclose([float(v) for v in lines[1].split()], want["ravg"], rtol=1e-12, atol=1e-15)
     assert int(lines[2]) > 100  # the list did outgrow the forced buffer
+
+
+@pytest.mark.parametrize("func", ["wp", "xi"])
+def test_gpu_points_outside_the_box_fail_loudly(gpu, capfd, func):
+    """wp / xi lattice the periodic box [0, L): a point well outside it makes the call fail with
+    a message (the reference's gridlink reports it out of bounds, utils/gridlink_impl.c.src:183;
+    here the data span beyond the periodic length is reported first) instead of counting it."""
+    from corrfunc_gb300 import theory
+    rng = np.random.default_rng(5)
+    L = 100.0
+    x, y, z = (rng.random(2000) * L for _ in range(3))
+    x[7] = 1.5 * L
+    bins = np.logspace(-1, 1, 8)
+    with pytest.raises(RuntimeError):
+        if func == "wp":
+            theory.wp(L, 10.0, 1, bins, x, y, z)
+        else:
+            theory.xi(L, 1, bins, x, y, z)
+    err = capfd.readouterr().err
+    assert "out of bounds" in err or "more than the periodic length" in err
