@@ -38,3 +38,22 @@ def test_record_arrays_and_errors():
         utils.convert_rp_pi_counts_to_wp(1, 1, 1, 1, [1] * 6, [1] * 6, [1] * 6, [1] * 6, 2, 3.0, dpi=0.0)
     with pytest.raises(ValueError):
         utils.convert_rp_pi_counts_to_wp(1, 1, 1, 1, [1] * 6, [1] * 6, [1] * 6, [1] * 6, 2, 4.0, dpi=1.0)
+
+
+def test_ra_dec_fixups_follow_the_reference(capsys):
+    """The survey front ends wrap RA by +180 when any RA < 0 and DEC by -90 when any DEC > 90,
+    in place on the caller's arrays (Corrfunc/utils.py:421-461); other arrays are untouched."""
+    from corrfunc_gb300 import mocks
+    ra = np.array([-10.0, 20.0, 30.0])
+    dec = np.array([10.0, 95.0, -5.0])
+    r, d = mocks._fix_ra_dec(ra, dec)
+    assert r is ra and d is dec
+    assert list(ra) == [170.0, 200.0, 210.0]
+    assert list(dec) == [-80.0, 5.0, -95.0]
+    out = capsys.readouterr().out
+    assert "negative RA" in out and "DEC values more than 90.0" in out
+    ra2, dec2 = np.array([0.0, 359.0]), np.array([-90.0, 90.0])
+    mocks._fix_ra_dec(ra2, dec2)
+    assert list(ra2) == [0.0, 359.0] and list(dec2) == [-90.0, 90.0]
+    with pytest.raises(TypeError):
+        mocks._fix_ra_dec([1.0], np.array([1.0]))
