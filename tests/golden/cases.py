@@ -8,9 +8,16 @@ import numpy as np
 from corrfunc_gb300 import catalogs as cat
 
 
+# shift of the "offset" kind: a uniform box far from the origin on every axis
+OFFSET = (1.0e5, -3.0e4, 2.0e6)
+
+
 def _box(kind, n, L, seed, dtype):
     if kind == "uniform":
         return cat.uniform_box(n, L, seed, dtype)
+    if kind == "offset":
+        x, y, z = cat.uniform_box(n, L, seed, np.float64)
+        return tuple(np.asarray(a + o, dtype=dtype) for a, o in zip((x, y, z), OFFSET))
     return cat.clustered_box(n, L, seed, dtype=dtype, sigma=L / 200.0, mean_occupancy=40.0)
 
 
@@ -39,11 +46,26 @@ CASES = [
          bins=("log", 0.01, 10.0, 10), weights=False, avg=True, dtype="f8"),
     dict(name="theta_cross_weighted", func="DDtheta", autocorr=0, kind="cap", n1=3000, n2=2500, seed=62,
          bins=("log", 0.05, 8.0, 8), weights=True, avg=True, dtype="f8"),
+    # coordinates far from the origin (non-periodic), bins from zero (self pairs), float32 runs
+    dict(name="dd_auto_far_offset", func="DD", autocorr=1, kind="offset", n1=4000, L=60.0, seed=15,
+         bins=("log", 0.2, 9.0, 10), periodic=False, weights=True, avg=True, dtype="f8"),
+    dict(name="dd_auto_rmin0", func="DD", autocorr=1, kind="clustered", n1=3000, L=50.0, seed=16,
+         bins=("lin", 0.0, 6.0, 12), periodic=True, weights=True, avg=True, dtype="f8"),
+    dict(name="rppi_cross_far_offset", func="DDrppi", autocorr=0, kind="offset", n1=2500, n2=3000, L=50.0,
+         seed=23, bins=("log", 0.3, 8.0, 7), pimax=7.0, periodic=False, weights=True, avg=True, dtype="f8"),
+    dict(name="smu_auto_float32", func="DDsmu", autocorr=1, kind="clustered", n1=4000, L=100.0, seed=33,
+         bins=("log", 0.4, 15.0, 7), mu_max=0.8, nmu=8, periodic=True, weights=True, avg=True, dtype="f4"),
+    dict(name="wp_float32_weighted", func="wp", autocorr=1, kind="clustered", n1=4000, L=100.0, seed=42,
+         bins=("log", 0.3, 12.0, 8), pimax=15.0, periodic=True, weights=True, avg=True, dtype="f4"),
+    dict(name="xi_uniform_rmin0", func="xi", autocorr=1, kind="uniform", n1=4000, L=80.0, seed=52,
+         bins=("lin", 0.0, 10.0, 10), periodic=True, weights=True, avg=True, dtype="f8"),
 ]
 
 
 def bin_edges(spec):
     kind, lo, hi, n = spec
+    if kind == "lin":
+        return [float(v) for v in np.linspace(lo, hi, n + 1)]
     return list(cat.log_bins(lo, hi, n))
 
 
