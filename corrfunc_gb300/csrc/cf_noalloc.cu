@@ -18,9 +18,10 @@
 //
 // Scratch: one file-scope device array (kScratchDoubles doubles, 4 KB) holding the squared bin
 // edges and the per-bin count / sum accumulators.  Its address is looked up once per device with
-// cudaGetSymbolAddress.  Each call copies the squared edges and zeros over the accumulators
-// itself before counting, so nothing has to be cleared beforehand; after the call the array
-// holds that call's raw sums.
+// cudaGetSymbolAddress and kept for the life of the process, so a cudaDeviceReset, or another
+// context made current on the same device, is not supported after the first call.  Each call
+// copies the squared edges and zeros over the accumulators itself before counting, so nothing
+// has to be cleared beforehand; after the call the array holds that call's raw sums.
 
 #include <cuda_runtime.h>
 #include <math.h>
@@ -194,10 +195,12 @@ extern "C" int cf_gpu_countpairs_cross_noalloc(const int64_t ND1, const double *
         if (k > 0 && !(edges[k] > edges[k - 1])) NA_FAIL("bin edges must increase (edge %d = %g)", k, edges[k]);
     }
     const double rmax = edges[nedges - 1];
-    const double box[3] = {boxsize_x, boxsize_y > 0.0 ? boxsize_y : boxsize_x, boxsize_z > 0.0 ? boxsize_z : boxsize_x};
+    const double box[3] = {boxsize_x, boxsize_y, boxsize_z};
     if (periodic) {
+        // every axis wraps: the reference's per-axis "no wrap" value (-1) is not supported here
         for (int a = 0; a < 3; a++) {
-            if (!(box[a] > 0.0) || !isfinite(box[a])) NA_FAIL("periodic wrapping needs a positive box size");
+            if (!(box[a] > 0.0) || !isfinite(box[a]))
+                NA_FAIL("periodic wrapping needs a positive, finite box size on every axis (axis %d: %g)", a, box[a]);
             if (!(rmax < 0.49 * box[a]))
                 NA_FAIL("rmax = %g must stay below 0.49 times the box size (%g) along every axis", rmax, box[a]);
         }

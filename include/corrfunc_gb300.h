@@ -443,8 +443,9 @@ int cf_reference_candidate_pairs(const int64_t ND1, void *X1, void *Y1, void *Z1
  *              (pair_product weights).
  *   edges      host array of the nedges bin edges as a bin file lists them (rmin, then each
  *              upper edge); 2 <= nedges <= 128, larger values are rejected with an error.
- *   periodic   minimum-image wrapping with the given box sizes (boxsize_y/_z <= 0 take
- *              boxsize_x); needs rmax < 0.49 * box size along every axis.
+ *   periodic   minimum-image wrapping on all three axes with the given box sizes, each of which
+ *              must be positive (the reference's per-axis -1, "no wrap on this axis", is rejected
+ *              with an error); needs rmax < 0.49 * box size along every axis.
  *   instruction_set  the reference isa whose double-precision formula the counts follow
  *              (AVX512F chains fused multiply-adds, the others do not; < 0 picks this host's).
  *   npairs, ravg, weightavg  caller-provided host arrays of nedges entries (ravg / weightavg
@@ -454,7 +455,9 @@ int cf_reference_candidate_pairs(const int64_t ND1, void *X1, void *Y1, void *Z1
  *              the stream has drained.
  *
  * Scratch is a fixed 4 KB device array inside the library.  The first call on each device looks
- * up its address (set-up); make that first call before any stream capture begins.  Each call
+ * up its address (set-up); make that first call before any stream capture begins.  The address is
+ * kept for the life of the process: after the first call, neither cudaDeviceReset nor another
+ * context made current on that device is supported.  Each call
  * writes the squared edges and zeros over the accumulators itself, so nothing has to be cleared
  * beforehand.  All calls on one device share that array: calls that overlap in time (two host
  * threads, or two streams) race and corrupt each other's counts, so serialise them.  Cost grows

@@ -29,7 +29,7 @@ def _noalloc(lib, torch, s1, s2, bins, periodic, boxsize, isa, weights, ravg=Tru
         len(s1[0]), p(dev[0]), p(dev[1]), p(dev[2]), p(w[0]),
         len(s2[0]), p(dev[3]), p(dev[4]), p(dev[5]), p(w[1]),
         n, edges.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), int(periodic),
-        float(boxsize), float(boxsize), float(boxsize), C.translate_isa(isa),
+        *(float(b) for b in np.broadcast_to(np.asarray(boxsize, dtype=float), (3,))), C.translate_isa(isa),
         npairs.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
         avg.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) if ravg else None,
         wavg.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), None)
@@ -105,6 +105,10 @@ def test_noalloc_rejects_too_many_edges_and_bad_arguments(env):
     # non-increasing edges
     rc, _, _, _ = _noalloc(lib, torch, s1, s2, np.array([0.0, 2.0, 2.0]), True, 50.0, "fallback", False)
     assert rc != 0
+    # periodic wrapping needs a positive box size on every axis (no per-axis "no wrap" value)
+    for box in ((50.0, -1.0, 50.0), (50.0, 50.0, 0.0)):
+        rc, _, _, _ = _noalloc(lib, torch, s1, s2, np.array([0.0, 1.0, 2.0]), True, box, "fallback", False)
+        assert rc != 0
 
 
 def test_noalloc_empty_sets(env):
