@@ -115,6 +115,9 @@ struct PairArgs {
     int rbin_div;               // flat bin / rbin_div = separation bin (npibin + 1 for 2-D histograms)
     float w_scale_f;
     double w_unscale;
+    // FP64 kernel only: weight sums accumulate in double precision (per-warp rows of doubles in
+    // shared memory) instead of fixed point, for weights spanning a wide range
+    int w_exact;
 };
 
 // ---------------------------------------------------------------------------------------

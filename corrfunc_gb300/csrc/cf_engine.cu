@@ -125,7 +125,7 @@ struct Geom {
     // counted in *extent_err (null: no check)
     unsigned long long *extent_err;
     double chk_lo[3], chk_hi[3];
-    double chk_wmax;
+    double chk_wmax, chk_wmin;  // planned largest |w| and smallest non-zero |w| (0: no lower check)
     // Integer view of the coordinates (the lattice kernels keep FP64 arithmetic off their common
     // path -- on this GPU the FP64 pipe issues at 1/64 of the FP32 rate -- and use it only for
     // the rare points near a reference-cell boundary).  A coordinate x becomes the fixed-point
@@ -141,7 +141,7 @@ struct Geom {
     double eps_cell[3];
     // order keys (okey0) of the extent checks, and of the range of coordinates that are inside
     // the reference lattice whatever the rounding of its FP64 cell index (others take the exact test)
-    unsigned long long k_chk_lo[3], k_chk_hi[3], k_chk_wmax;
+    unsigned long long k_chk_lo[3], k_chk_hi[3], k_chk_wmax, k_chk_wmin;
     unsigned long long k_ref_lo[3], k_ref_hi[3];
     // fixed-point X of ref_min (FP32 estimate of the reference cell index)
     unsigned long long o_ref[3];
@@ -279,13 +279,38 @@ __device__ __forceinline__ unsigned long long warp_max(unsigned long long v)
 }
 
 constexpr int kMinmaxUnroll = 4;
+// extent slots of one catalogue: xmin, xmax, ymin, ymax, zmin, zmax, max |w|, non-finite flag,
+// smallest non-zero |w|; catalogue s folds into mm[kMmSlots * s ...]
+constexpr int kMmUsed = 9;
+constexpr int kMmSlots = 16;
+// initial value of extent slot k (minima start at the largest key, maxima and flags at 0)
+__host__ inline unsigned long long mm_init_value(int k)
+{
+    k %= kMmSlots;
+    return (k == 0 || k == 2 || k == 4 || k == 8) ? ~0ull : 0ull;
+}
+// smallest non-zero |w| of a catalogue's extent slots (0 when it has no non-zero weight)
+__host__ inline double mm_wmin(const unsigned long long *mmh) { return mmh[8] == ~0ull ? 0.0 : ord_dec(mmh[8]); }
+
+// Weight sums are 32-bit fixed-point terms at one scale per call (the largest |w1 w2| maps to
+// just below 2^30), so a term's rounding error is at most 2^-30 of the largest product; terms
+// much smaller than it could all round the same way.  When the largest product exceeds the
+// smallest non-zero one by more than kWeightSpanFixed (then every term is still resolved to
+// 2^-30 * 512 < 5e-7 of itself), the count runs the FP64 pair kernel with the weight sums in
+// double precision instead.
+constexpr double kWeightSpanFixed = 512.0;
+__host__ inline bool weights_wide(const double wmax[2], const double wmin[2])
+{
+    if (!(wmin[0] > 0.0) || !(wmin[1] > 0.0)) return false;  // no non-zero products
+    return wmax[0] * wmax[1] > kWeightSpanFixed * (wmin[0] * wmin[1]);
+}
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_minmax(const T *x, const T *y, const T *z, const T *w, int64_t n,
                                                 unsigned long long *mm)
 {
     using K = decltype(okey(T(0)));
-    K mn[3] = {(K)~(K)0, (K)~(K)0, (K)~(K)0}, mx[3] = {0, 0, 0}, wm = 0;
+    K mn[3] = {(K)~(K)0, (K)~(K)0, (K)~(K)0}, mx[3] = {0, 0, 0}, wm = 0, wn = (K)~(K)0;
     uint32_t bad = 0;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     // kMinmaxUnroll points per iteration: all their loads are issued before the compares
@@ -312,10 +337,11 @@ __global__ void __launch_bounds__(256) k_minmax(const T *x, const T *y, const T 
                 const int64_t iu = i + u * stride < n ? i + u * stride : i;
                 const K kw = abskey(w[iu]);
                 wm = kw > wm ? kw : wm;
+                wn = (kw != 0 && kw < wn) ? kw : wn;  // smallest non-zero |w|
             }
         }
     }
-    __shared__ unsigned long long part[8][8];
+    __shared__ unsigned long long part[8][kMmUsed];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
     K r[7];
     for (int a = 0; a < 3; a++) {
@@ -323,16 +349,18 @@ __global__ void __launch_bounds__(256) k_minmax(const T *x, const T *y, const T 
         r[2 * a + 1] = warp_max(mx[a]);
     }
     r[6] = warp_max(wm);
+    wn = warp_min(wn);
     bad = __any_sync(0xffffffffu, bad != 0) ? 1u : 0u;
     if (lane == 0) {
         for (int k = 0; k < 7; k++) part[warp][k] = (unsigned long long)r[k];
         part[warp][7] = bad;
+        part[warp][8] = (unsigned long long)wn;
     }
     __syncthreads();
     // the block's extremes go straight into mm (ord_enc of the double values; one atomic each)
-    if (threadIdx.x < 8) {
+    if (threadIdx.x < kMmUsed) {
         const int k = threadIdx.x;
-        const bool is_min = k < 6 && (k & 1) == 0;
+        const bool is_min = (k < 6 && (k & 1) == 0) || k == 8;
         K v = (K)part[0][k];
         for (int q = 1; q < nwarps; q++) {
             const K o = (K)part[q][k];
@@ -340,9 +368,11 @@ __global__ void __launch_bounds__(256) k_minmax(const T *x, const T *y, const T 
         }
         if (k == 7) {
             if (v) atomicMax(&mm[7], 1ull);
-        } else if (k == 6) {
+        } else if (k == 6 || k == 8) {
+            if (k == 8 && v == (K)~(K)0) return;  // no non-zero weight in this block
             const double wv = key_value((K)(v | ((K)1 << (sizeof(K) * 8 - 1))));  // non-negative value
-            atomicMax(&mm[6], ord_enc(wv));
+            if (k == 6) atomicMax(&mm[6], ord_enc(wv));
+            else atomicMin(&mm[8], ord_enc(wv));
         } else {
             const unsigned long long e = ord_enc(key_value(v));
             if (is_min) atomicMin(&mm[k], e);
@@ -459,7 +489,12 @@ __global__ void k_scatter(const T *x, const T *y, const T *z, const T *w, int64_
         const uint32_t pos = cell_start[c] + atomicAdd(&fill[c], 1u);
         const T p[3] = {x[i], y[i], z[i]};
         const T wv = w ? w[i] : T(1);
-        if (g.extent_err && w && !(abs_okey(wv) <= g.k_chk_wmax)) atomicAdd(g.extent_err, 1ull);
+        if (g.extent_err && w) {
+            // a replayed batch keeps its weights inside the planned range (the scale of the weight
+            // sums was chosen for it); zero weights are always inside
+            const unsigned long long kw = abs_okey(wv);
+            if (!(kw <= g.k_chk_wmax) || (kw > 0x8000000000000000ull && kw < g.k_chk_wmin)) atomicAdd(g.extent_err, 1ull);
+        }
         float h[3], l[3];
         unsigned long long X[3];
 #pragma unroll
@@ -754,6 +789,7 @@ struct SmemLayout {
     bool need_avg, need_w;
     int entry_words;  // 32-bit words per histogram entry: count [, avg hi, avg lo] [, w hi, w lo]
     size_t edges_off, guard_off, ascale_off, lut_off, stage_off, hist_off, per_warp_hist, per_warp_stage, total;
+    size_t wd_off, per_warp_wd;  // FP64 kernel with weights: one double weight sum per row and warp
 };
 
 __host__ __device__ inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -782,7 +818,6 @@ __host__ __device__ inline SmemLayout smem_layout(int nedges, int nbins, int war
     L.need_avg = need_avg;
     L.need_w = need_w;
     L.entry_words = 1 + (need_avg ? 2 : 0) + (need_w ? 2 : 0);
-    (void)f64;
     L.nedges = nedges;
     L.nbins = nbins;
     L.warps = warps;
@@ -810,6 +845,9 @@ __host__ __device__ inline SmemLayout smem_layout(int nedges, int nbins, int war
     L.hist_off = o;
     L.per_warp_hist = align_up((size_t)L.nrows * lane_stride * 4 * L.entry_words + 32, 16);
     o += L.per_warp_hist * warps;
+    L.wd_off = o;
+    L.per_warp_wd = (f64 && need_w) ? align_up(sizeof(double) * (size_t)L.nrows, 16) : 0;
+    o += L.per_warp_wd * warps;
     L.total = o;
     return L;
 }
@@ -850,7 +888,7 @@ __device__ __forceinline__ void add_term(uint32_t *hi_lo, int v)
 }
 
 template <bool NEED_AVG, bool NEED_W>
-__device__ __forceinline__ void flush_hist(const PairArgs &A, WarpHist h, int lane, uint32_t cat = 0)
+__device__ __forceinline__ void flush_hist(const PairArgs &A, WarpHist h, int lane, uint32_t cat = 0, double *wd = nullptr)
 {
     __syncwarp();
     unsigned long long *g_cnt = A.g_cnt + (size_t)cat * A.nbins;
@@ -886,7 +924,12 @@ __device__ __forceinline__ void flush_hist(const PairArgs &A, WarpHist h, int la
         }
         if (NEED_W) {
             const long long vw = wh * 65536ll + (long long)wl;
-            if (vw) atomicAdd(&g_w[b], (double)vw * A.w_unscale);
+            double v = (double)vw * A.w_unscale;
+            if (wd) {
+                v += wd[b];
+                wd[b] = 0.0;
+            }
+            if (v != 0.0) atomicAdd(&g_w[b], v);
         }
     }
     __syncwarp();
@@ -1500,6 +1543,10 @@ __global__ void __launch_bounds__(256) k_pairs_f64(PairArgs A, SmemLayout SL)
     int2 *sro = (int2 *)(sj + 32);  // reference cell, caller index
     WarpHist h = warp_hist(smem, SL, warp);
     zero_hist(h, SL, lane);
+    // weights over a wide range: the warp's weight sums in double, one per histogram row
+    double *wd = (NEED_W && A.w_exact) ? (double *)(smem + SL.wd_off + SL.per_warp_wd * warp) : nullptr;
+    if (wd)
+        for (int b = lane; b < SL.nrows; b += 32) wd[b] = 0.0;
     const int hl = lane & (SL.lane_stride - 1);
     __syncthreads();
     uint64_t evaluated = 0;
@@ -1516,7 +1563,7 @@ __global__ void __launch_bounds__(256) k_pairs_f64(PairArgs A, SmemLayout SL)
         const Task T = A.tasks[t];
         const uint32_t cat = T.meta >> kCatShift;
         if (cat != cur_cat) {
-            flush_hist<NEED_AVG, NEED_W>(A, h, lane, cur_cat);
+            flush_hist<NEED_AVG, NEED_W>(A, h, lane, cur_cat, wd);
             cur_cat = cat;
             col_terms = 0;
         }
@@ -1552,19 +1599,24 @@ __global__ void __launch_bounds__(256) k_pairs_f64(PairArgs A, SmemLayout SL)
                         bin = ref_eval<MODE>(A, se, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, -ox, -oy, -oz, &avg_term);
                     }
                     if (bin < 0) continue;
-                    accumulate<NEED_AVG, NEED_W>(A, h, bin, bin * h.ls + hl, avg_term, pi.w * pj.w);
+                    if (wd) {
+                        accumulate<NEED_AVG, false>(A, h, bin, bin * h.ls + hl, avg_term, 0.0);
+                        atomicAdd(&wd[bin], pi.w * pj.w);
+                    } else {
+                        accumulate<NEED_AVG, NEED_W>(A, h, bin, bin * h.ls + hl, avg_term, pi.w * pj.w);
+                    }
                 }
             }
             __syncwarp();
             col_terms += tile_terms;
             if (col_terms + tile_terms > (uint32_t)kColumnTerms) {
-                flush_hist<NEED_AVG, NEED_W>(A, h, lane, cur_cat);
+                flush_hist<NEED_AVG, NEED_W>(A, h, lane, cur_cat, wd);
                 col_terms = 0;
             }
         }
         evaluated += (uint64_t)icount * (T.j_end - T.j_begin);
     }
-    flush_hist<NEED_AVG, NEED_W>(A, h, lane, cur_cat);
+    flush_hist<NEED_AVG, NEED_W>(A, h, lane, cur_cat, wd);
     if (lane == 0) atomicAdd(&A.g_stats[0], (unsigned long long)evaluated);
 }
 
@@ -2317,6 +2369,7 @@ static void geom_keys(Geom &g)
         g.k_chk_hi[a] = okey0(g.chk_hi[a]);
     }
     g.k_chk_wmax = okey0(fabs(g.chk_wmax));
+    g.k_chk_wmin = okey0(fabs(g.chk_wmin));
 }
 
 static int gpu_geometry(const cf_job *J, const cf_geometry &geo, const double lo[3], const double hi[3], Geom &g,
@@ -2576,38 +2629,40 @@ static int run_locked(cf_job *J, cf_hist *H)
     CF_CUDA(cudaStreamSynchronize(st));  // pinned staging is reused: nothing of a failed call may be pending
     CF_CUDA(cudaEventRecord(g_eng.ev[0], st));
     // ---- upload + extent ----
-    if (ensure(W.mm, sizeof(unsigned long long) * 16) != EXIT_SUCCESS) return EXIT_FAILURE;
+    if (ensure(W.mm, sizeof(unsigned long long) * 2 * kMmSlots) != EXIT_SUCCESS) return EXIT_FAILURE;
     unsigned long long *mm = (unsigned long long *)W.mm.p;
-    if (ensure_host(W.h_small, sizeof(unsigned long long) * 32) != EXIT_SUCCESS) return EXIT_FAILURE;
+    if (ensure_host(W.h_small, sizeof(unsigned long long) * 4 * kMmSlots) != EXIT_SUCCESS) return EXIT_FAILURE;
     unsigned long long *mm_init = (unsigned long long *)W.h_small.p;
-    unsigned long long *mmh = mm_init + 16;
-    for (int k = 0; k < 16; k++) mm_init[k] = (k % 8 == 6 || k % 8 == 7 || (k % 8) % 2 == 1) ? 0ull : ~0ull;
-    CF_CUDA(cudaMemcpyAsync(mm, mm_init, sizeof(unsigned long long) * 16, cudaMemcpyHostToDevice, st));
+    unsigned long long *mmh = mm_init + 2 * kMmSlots;
+    for (int k = 0; k < 2 * kMmSlots; k++) mm_init[k] = mm_init_value(k);
+    CF_CUDA(cudaMemcpyAsync(mm, mm_init, sizeof(unsigned long long) * 2 * kMmSlots, cudaMemcpyHostToDevice, st));
     const int nsets = autocorr ? 1 : 2;
     for (int s = 0; s < nsets; s++) {
         const int64_t n = s ? n2 : n1;
         const void *x = s ? J->x2 : J->x1, *y = s ? J->y2 : J->y1, *z = s ? J->z2 : J->z1;
         const void *w = need_w ? (s ? J->w2 : J->w1) : nullptr;
         if (!x || !y || !z || (need_w && !w)) CF_FAIL("NULL input array");
-        int rc = isf ? upload_and_minmax<float>(W, s, n, x, y, z, w, J->inputs_on_device != 0, mm + 8 * s)
-                     : upload_and_minmax<double>(W, s, n, x, y, z, w, J->inputs_on_device != 0, mm + 8 * s);
+        int rc = isf ? upload_and_minmax<float>(W, s, n, x, y, z, w, J->inputs_on_device != 0, mm + kMmSlots * s)
+                     : upload_and_minmax<double>(W, s, n, x, y, z, w, J->inputs_on_device != 0, mm + kMmSlots * s);
         if (rc != EXIT_SUCCESS) return EXIT_FAILURE;
     }
     const bool dev_float = isf;
-    CF_CUDA(cudaMemcpyAsync(mmh, mm, sizeof(unsigned long long) * 16, cudaMemcpyDeviceToHost, st));
+    CF_CUDA(cudaMemcpyAsync(mmh, mm, sizeof(unsigned long long) * 2 * kMmSlots, cudaMemcpyDeviceToHost, st));
     CF_CUDA(cudaStreamSynchronize(st));
-    double lo[3], hi[3], wmax[2] = {0, 0};
+    double lo[3], hi[3], wmax[2] = {0, 0}, wmin[2] = {0, 0};
     for (int a = 0; a < 3; a++) {
         lo[a] = ord_dec(mmh[2 * a]);
         hi[a] = ord_dec(mmh[2 * a + 1]);
         if (nsets == 2) {
-            lo[a] = fmin(lo[a], ord_dec(mmh[8 + 2 * a]));
-            hi[a] = fmax(hi[a], ord_dec(mmh[8 + 2 * a + 1]));
+            lo[a] = fmin(lo[a], ord_dec(mmh[kMmSlots + 2 * a]));
+            hi[a] = fmax(hi[a], ord_dec(mmh[kMmSlots + 2 * a + 1]));
         }
     }
     wmax[0] = ord_dec(mmh[6]);
-    wmax[1] = nsets == 2 ? ord_dec(mmh[14]) : wmax[0];
-    if (mmh[7] != 0 || (nsets == 2 && mmh[15] != 0)) CF_FAIL("non-finite input coordinates");
+    wmax[1] = nsets == 2 ? ord_dec(mmh[kMmSlots + 6]) : wmax[0];
+    wmin[0] = mm_wmin(mmh);
+    wmin[1] = nsets == 2 ? mm_wmin(mmh + kMmSlots) : wmin[0];
+    if (mmh[7] != 0 || (nsets == 2 && mmh[kMmSlots + 7] != 0)) CF_FAIL("non-finite input coordinates");
     for (int a = 0; a < 3; a++) {
         if (!isfinite(lo[a]) || !isfinite(hi[a])) CF_FAIL("non-finite input coordinates");
     }
@@ -2624,7 +2679,8 @@ static int run_locked(cf_job *J, cf_hist *H)
     g_eng.last.num_cells = (int)ncells;
 
     // ---- lattices ----
-    const bool f64 = g_eng.precision == CF_PRECISION_FP64 || !has_f32_path(mode);
+    const bool w_exact = need_w && weights_wide(wmax, wmin);
+    const bool f64 = g_eng.precision == CF_PRECISION_FP64 || !has_f32_path(mode) || w_exact;
     g.write_lo = (J->need_avg != 0 || mode_is_mock(mode)) ? 1 : 0;
     if (ensure(W.res, res_bytes(nbins)) != EXIT_SUCCESS) return EXIT_FAILURE;
     const ResView R = res_view(W.res.p, nbins);
@@ -2686,6 +2742,7 @@ static int run_locked(cf_job *J, cf_hist *H)
     A.ro2 = (const int2 *)S2.ro.p;
     A.ntask_dev = R.flags + 1;  // tasks listed (capped by the capacity in the kernel)
     pair_constants(A, J, mode, nbins, autocorr, G, geo, g, delta, T, wmax, W);
+    A.w_exact = w_exact ? 1 : 0;
     A.g_cnt = R.cnt;
     A.g_avg = R.avg;
     A.g_w = R.w;
@@ -2766,7 +2823,8 @@ struct BatchPlan {
     Tables T;
     PairArgs A;
     cf_geometry geo;
-    double delta[3], wmax[2];
+    double delta[3], wmax[2], wmin[2];
+    bool w_exact = false;   // weight products span too wide a range for the FP32 kernel's sums
     int ls = 0, warps = 0;  // chosen FP32 layout (0: scored)
     int kernels = 0;        // kernels in one run
     cudaGraph_t graph = nullptr;
@@ -2786,6 +2844,8 @@ static int batch_lattices(BatchPlan &P)
     g1.extent_err = g2.extent_err = R.extent;
     g1.chk_wmax = P.wmax[0];
     g2.chk_wmax = P.wmax[1];
+    g1.chk_wmin = P.w_exact ? 0.0 : P.wmin[0];
+    g2.chk_wmin = P.w_exact ? 0.0 : P.wmin[1];
     geom_keys(g1);
     geom_keys(g2);
     g1.write_lo = g2.write_lo = (P.J.need_avg != 0 || mode_is_mock(P.mode)) ? 1 : 0;
@@ -2856,7 +2916,7 @@ static int batch_enqueue(BatchPlan &P, int phase, bool timing)
     CF_CUDA(cudaMemsetAsync(W.res.p, 0, res_zero_bytes(nb), st));  // sums, statistics, task counter
     if (timing && record_event(P.ev[1]) != EXIT_SUCCESS) return EXIT_FAILURE;
     int launched = 0;
-    const bool f64 = g_eng.precision == CF_PRECISION_FP64;
+    const bool f64 = g_eng.precision == CF_PRECISION_FP64 || P.w_exact;
     const int fls = g_eng.force_ls, fw = g_eng.force_warps;
     g_eng.force_ls = P.ls;
     g_eng.force_warps = P.warps;
@@ -2958,12 +3018,13 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
     int rc = EXIT_SUCCESS;
     do {
         // ---- extent of everything (set 1 in slots 0-7, set 2 in 8-15) ----
-        if ((rc = ensure(W.mm, sizeof(unsigned long long) * 16)) != EXIT_SUCCESS) break;
-        if ((rc = ensure_host(W.h_small, sizeof(unsigned long long) * 32)) != EXIT_SUCCESS) break;
+        if ((rc = ensure(W.mm, sizeof(unsigned long long) * 2 * kMmSlots)) != EXIT_SUCCESS) break;
+        if ((rc = ensure_host(W.h_small, sizeof(unsigned long long) * 4 * kMmSlots)) != EXIT_SUCCESS) break;
         unsigned long long *mm = (unsigned long long *)W.mm.p;
-        unsigned long long *mm_init = (unsigned long long *)W.h_small.p, *mmh = mm_init + 16;
-        for (int k = 0; k < 16; k++) mm_init[k] = (k % 8 == 6 || k % 8 == 7 || (k % 8) % 2 == 1) ? 0ull : ~0ull;
-        if (cudaMemcpyAsync(mm, mm_init, sizeof(unsigned long long) * 16, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+        unsigned long long *mm_init = (unsigned long long *)W.h_small.p, *mmh = mm_init + 2 * kMmSlots;
+        for (int k = 0; k < 2 * kMmSlots; k++) mm_init[k] = mm_init_value(k);
+        if (cudaMemcpyAsync(mm, mm_init, sizeof(unsigned long long) * 2 * kMmSlots, cudaMemcpyHostToDevice, st) !=
+            cudaSuccess) {
             rc = EXIT_FAILURE;
             break;
         }
@@ -2973,7 +3034,7 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
             if (n == 0) continue;
             const void *x = r ? P->J.x2 : P->x1[s], *y = r ? P->J.y2 : P->y1[s], *z = r ? P->J.z2 : P->z1[s];
             const void *w = P->need_w ? (r ? P->J.w2 : P->w1[s]) : nullptr;
-            unsigned long long *slot = mm + (r ? 8 : 0);
+            unsigned long long *slot = mm + (r ? kMmSlots : 0);
             rc = P->isf ? minmax_into<float>(W, (const float *)x, (const float *)y, (const float *)z, (const float *)w,
                                              n, slot)
                         : minmax_into<double>(W, (const double *)x, (const double *)y, (const double *)z,
@@ -2981,7 +3042,8 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
             if (rc != EXIT_SUCCESS) break;
         }
         if (rc != EXIT_SUCCESS) break;
-        if (cudaMemcpyAsync(mmh, mm, sizeof(unsigned long long) * 16, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        if (cudaMemcpyAsync(mmh, mm, sizeof(unsigned long long) * 2 * kMmSlots, cudaMemcpyDeviceToHost, st) !=
+                cudaSuccess ||
             cudaStreamSynchronize(st) != cudaSuccess) {
             fprintf(stderr, "corrfunc_gb300: CUDA error '%s' while measuring the batch extent\n",
                     cudaGetErrorString(cudaGetLastError()));
@@ -2990,12 +3052,15 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
         }
         double lo[3], hi[3];
         for (int a = 0; a < 3; a++) {
-            lo[a] = fmin(ord_dec(mmh[2 * a]), ord_dec(mmh[8 + 2 * a]));
-            hi[a] = fmax(ord_dec(mmh[2 * a + 1]), ord_dec(mmh[8 + 2 * a + 1]));
+            lo[a] = fmin(ord_dec(mmh[2 * a]), ord_dec(mmh[kMmSlots + 2 * a]));
+            hi[a] = fmax(ord_dec(mmh[2 * a + 1]), ord_dec(mmh[kMmSlots + 2 * a + 1]));
         }
         P->wmax[0] = ord_dec(mmh[6]);
-        P->wmax[1] = ord_dec(mmh[14]);
-        if (mmh[7] != 0 || mmh[15] != 0) {
+        P->wmax[1] = ord_dec(mmh[kMmSlots + 6]);
+        P->wmin[0] = mm_wmin(mmh);
+        P->wmin[1] = mm_wmin(mmh + kMmSlots);
+        P->w_exact = P->need_w && weights_wide(P->wmax, P->wmin);
+        if (mmh[7] != 0 || mmh[kMmSlots + 7] != 0) {
             fprintf(stderr, "corrfunc_gb300: non-finite input coordinates\n");
             rc = EXIT_FAILURE;
             break;
@@ -3055,7 +3120,7 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
 
         // ---- eager run: size the work list ----
         if ((rc = batch_enqueue(*P, 0, false)) != EXIT_SUCCESS) break;
-        uint32_t *cnt_h = (uint32_t *)(mmh + 8);
+        uint32_t *cnt_h = (uint32_t *)(mmh + kMmSlots);
         if (cudaMemcpyAsync(cnt_h, (uint32_t *)W.task_off.p + P->nentries, sizeof(uint32_t), cudaMemcpyDeviceToHost,
                             st) != cudaSuccess ||
             cudaStreamSynchronize(st) != cudaSuccess) {
@@ -3084,6 +3149,7 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
         A.ntasks = P->task_cap;
         A.ntask_dev = (const uint32_t *)W.task_off.p + P->nentries;
         pair_constants(A, &P->J, MODE_R3, P->nbins, false, P->G, P->geo, P->g, P->delta, P->T, P->wmax, W);
+        A.w_exact = P->w_exact ? 1 : 0;
         {
             const ResView R = res_view(W.res.p, nb);
             A.g_cnt = R.cnt;
@@ -3113,7 +3179,7 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
         }
 
         // ---- tuner: time the FP32 layouts that fit, keep the fastest ----
-        if (tune && g_eng.precision == CF_PRECISION_FP32_REFINE) {
+        if (tune && g_eng.precision == CF_PRECISION_FP32_REFINE && !P->w_exact) {
             const int cand_ls[3] = {32, 16, 8};
             const int cand_w[3] = {16, 8, 4};
             float best = 1e30f;

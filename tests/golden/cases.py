@@ -59,7 +59,32 @@ CASES = [
          bins=("log", 0.3, 12.0, 8), pimax=15.0, periodic=True, weights=True, avg=True, dtype="f4"),
     dict(name="xi_uniform_rmin0", func="xi", autocorr=1, kind="uniform", n1=4000, L=80.0, seed=52,
          bins=("lin", 0.0, 10.0, 10), periodic=True, weights=True, avg=True, dtype="f8"),
+    # weights over a wide range (1 % of the points weigh 100, the rest 0.005-0.015: products span
+    # 1e8) and over a moderate one (0.06-1: products span about 300)
+    dict(name="dd_auto_wide_weights", func="DD", autocorr=1, kind="uniform", n1=4000, L=80.0, seed=17,
+         bins=("log", 0.3, 12.0, 10), periodic=True, weights=True, wkind="wide", avg=True, dtype="f8"),
+    dict(name="dd_cross_moderate_weights", func="DD", autocorr=0, kind="clustered", n1=3000, n2=3500, L=120.0,
+         seed=18, bins=("log", 0.2, 20.0, 12), periodic=True, weights=True, wkind="moderate", avg=True, dtype="f8"),
+    dict(name="rppi_auto_wide_weights", func="DDrppi", autocorr=1, kind="clustered", n1=3000, L=100.0, seed=24,
+         bins=("log", 0.2, 12.0, 8), pimax=10.0, periodic=True, weights=True, wkind="wide", avg=True, dtype="f8"),
+    dict(name="theta_auto_wide_weights", func="DDtheta", autocorr=1, kind="cap", n1=3000, seed=63,
+         bins=("log", 0.02, 8.0, 9), weights=True, wkind="wide", avg=True, dtype="f8"),
 ]
+
+
+def case_weights(case, n, seed, dtype):
+    """Per-point weights of a case: U[0.5, 1.5] by default; "wide": 1 % of the points weigh 100,
+    the others U[0.005, 0.015]; "moderate": U[0.06, 1]."""
+    kind = case.get("wkind", "default")
+    if kind == "default":
+        return cat.weights(n, seed, dtype=dtype)
+    rng = np.random.default_rng(seed)
+    if kind == "wide":
+        w = rng.uniform(0.005, 0.015, n)
+        w[rng.random(n) < 0.01] = 100.0
+    else:
+        w = rng.uniform(0.06, 1.0, n)
+    return np.ascontiguousarray(w, dtype=dtype)
 
 
 def bin_edges(spec):
@@ -69,8 +94,9 @@ def bin_edges(spec):
     return list(cat.log_bins(lo, hi, n))
 
 
-def make_inputs(case):
-    """Returns (args, kwargs) for corrfunc_gb300.theory/mocks functions (without the library)."""
+def make_inputs(case, isa="fallback"):
+    """Returns (args, kwargs) for corrfunc_gb300.theory/mocks functions (without the library);
+    `isa` selects the reference formula family ("fallback" or "avx512f")."""
     dt = np.float32 if case["dtype"] == "f4" else np.float64
     seed = case["seed"]
     func = case["func"]
@@ -78,14 +104,14 @@ def make_inputs(case):
     auto = case["autocorr"]
     if func == "DDtheta":
         ra1, dec1 = cat.sky_cap(case["n1"], seed, dtype=dt)
-        kw = dict(output_thetaavg=case["avg"], isa="fallback")
+        kw = dict(output_thetaavg=case["avg"], isa=isa)
         if case["weights"]:
-            kw.update(weights1=cat.weights(case["n1"], seed + 1000, dtype=dt), weight_type="pair_product")
+            kw.update(weights1=case_weights(case, case["n1"], seed + 1000, dt), weight_type="pair_product")
         if not auto:
             ra2, dec2 = cat.sky_cap(case["n2"], seed + 1, dtype=dt)
             kw.update(RA2=ra2, DEC2=dec2)
             if case["weights"]:
-                kw.update(weights2=cat.weights(case["n2"], seed + 1001, dtype=dt))
+                kw.update(weights2=case_weights(case, case["n2"], seed + 1001, dt))
         return [auto, 1, bins, ra1, dec1], kw
     L = case["L"]
     x1, y1, z1 = _box(case["kind"], case["n1"], L, seed, dt)
@@ -94,19 +120,19 @@ def make_inputs(case):
         kw.update(weight_type="pair_product")
     if func in ("wp", "xi"):
         if case["weights"]:
-            kw["weights"] = cat.weights(case["n1"], seed + 1000, dtype=dt)
+            kw["weights"] = case_weights(case, case["n1"], seed + 1000, dt)
         kw["output_rpavg" if func == "wp" else "output_ravg"] = case["avg"]
-        kw["isa"] = "fallback"
+        kw["isa"] = isa
         if func == "wp":
             return [L, case["pimax"], 1, bins, x1, y1, z1], kw
         return [L, 1, bins, x1, y1, z1], kw
     if case["weights"]:
-        kw["weights1"] = cat.weights(case["n1"], seed + 1000, dtype=dt)
+        kw["weights1"] = case_weights(case, case["n1"], seed + 1000, dt)
     if not auto:
         x2, y2, z2 = _box(case["kind"], case["n2"], L, seed + 1, dt)
         kw.update(X2=x2, Y2=y2, Z2=z2)
         if case["weights"]:
-            kw["weights2"] = cat.weights(case["n2"], seed + 1001, dtype=dt)
+            kw["weights2"] = case_weights(case, case["n2"], seed + 1001, dt)
     kw["periodic"] = case["periodic"]
     kw["boxsize"] = L if case["periodic"] else None
     kw["isa"] = "fallback"

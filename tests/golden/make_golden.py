@@ -10,6 +10,9 @@ It records
   * for every seeded case in cases.py, the reference library's output (isa FALLBACK); for
     float32 inputs the reference's double-precision run on the upcast values (its float run,
     which accumulates in float, is stored beside it for information);
+  * the same cases run with the reference's AVX512F kernels (fused multiply-add separations,
+    theory/DD/countpairs_kernels.c.src:188-190 and siblings), in "avx512f_cases"; this needs an
+    x86-64 host with AVX512F;
   * the DD(r) known answer of the reference's Python doctest (Corrfunc/theory/DD.py:166-202):
     its bin edges (theory/tests/bins) and the printed table, plus the reference library's
     full-precision output on the same seeded input.
@@ -70,26 +73,33 @@ def doctest_case(refroot):
             "reference": result_dict("DD", res)}
 
 
+def run_case(case, isa):
+    args, kw = cases.make_inputs(case, isa=isa)
+    run = cases.runner(case["func"])
+    lib = ref_lib(cases.REF_MODULE[case["func"]])
+    res_f = None
+    if case["dtype"] == "f4":
+        # float inputs are pinned to the reference's double-precision run on the same values
+        # upcast to double; the reference's own float run (float accumulators) is kept for
+        # information only
+        res_f = run(lib, *args, **kw)
+        up = lambda a: a.astype(np.float64) if isinstance(a, np.ndarray) and a.dtype == np.float32 else a
+        args = [up(a) for a in args]
+        kw = {k: up(v) for k, v in kw.items()}
+    out = result_dict(case["func"], run(lib, *args, **kw))
+    if res_f is not None:
+        out["reference_float_run_npairs"] = [int(v) for v in res_f["npairs"]]
+    return out
+
+
 def main():
     refroot = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    out = {"generator": "tests/golden/make_golden.py", "isa": "FALLBACK", "cases": {}}
+    out = {"generator": "tests/golden/make_golden.py", "isa": "FALLBACK", "cases": {}, "avx512f_cases": {}}
     for case in cases.CASES:
-        args, kw = cases.make_inputs(case)
-        run = cases.runner(case["func"])
-        lib = ref_lib(cases.REF_MODULE[case["func"]])
-        if case["dtype"] == "f4":
-            # float inputs are pinned to the reference's double-precision run on the same values
-            # upcast to double; the reference's own float run (float accumulators) is kept for
-            # information only
-            res_f = run(lib, *args, **kw)
-            up = lambda a: a.astype(np.float64) if isinstance(a, np.ndarray) and a.dtype == np.float32 else a
-            args = [up(a) for a in args]
-            kw = {k: up(v) for k, v in kw.items()}
-        res = run(lib, *args, **kw)
-        out["cases"][case["name"]] = result_dict(case["func"], res)
-        if case["dtype"] == "f4":
-            out["cases"][case["name"]]["reference_float_run_npairs"] = [int(v) for v in res_f["npairs"]]
-        print("%-34s %12d pairs" % (case["name"], int(np.sum(res["npairs"]))))
+        out["cases"][case["name"]] = run_case(case, "fallback")
+        out["avx512f_cases"][case["name"]] = run_case(case, "avx512f")
+        print("%-34s %12d pairs (fallback) %12d (avx512f)" % (case["name"], sum(out["cases"][case["name"]]["npairs"]),
+                                                             sum(out["avx512f_cases"][case["name"]]["npairs"])))
     out["dd_doctest"] = doctest_case(refroot)
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(out, f, indent=1)

@@ -33,9 +33,9 @@ def precision(request, gpu):
     gpu.set_precision("fp32_refine")
 
 
-def _gpu_call(case):
+def _gpu_call(case, isa="fallback"):
     from corrfunc_gb300 import _capi as C
-    args, kw = cases.make_inputs(case)
+    args, kw = cases.make_inputs(case, isa=isa)
     return cases.runner(case["func"])(C.library(), *args, **kw)
 
 
@@ -48,10 +48,14 @@ def _check(func, got, want, rtol):
                                atol=1e-12)
 
 
+@pytest.mark.parametrize("isa", ["fallback", "avx512f"])
 @pytest.mark.parametrize("case", cases.CASES, ids=[c["name"] for c in cases.CASES])
-def test_gpu_matches_golden(gpu, precision, case):
-    got = _gpu_call(case)
-    gold = GOLDEN["cases"][case["name"]]
+def test_gpu_matches_golden(gpu, precision, case, isa):
+    """Every golden case in both formula families of the reference: the FALLBACK kernels' unfused
+    sums and the AVX512F kernels' fused multiply-add chains (theory/DD/countpairs_kernels.c.src:
+    188-190, theory/DDsmu/countpairs_s_mu_kernels.c.src:213-214)."""
+    got = _gpu_call(case, isa)
+    gold = GOLDEN["cases" if isa == "fallback" else "avx512f_cases"][case["name"]]
     assert [int(v) for v in got["npairs"]] == gold["npairs"]
     rtol = 1e-4 if case["dtype"] == "f4" else RTOL_AVG
     f = cases.AVG_FIELD[case["func"]]

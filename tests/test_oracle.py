@@ -17,8 +17,8 @@ GOLDEN = json.load(open(os.path.join(HERE, "golden", "golden.json")))
 REF_ROOT = os.environ.get("CORRFUNC_REF_DIR", "/root/reference")
 
 
-def _oracle_call(orc, case):
-    args, kw = cases.make_inputs(case)
+def _oracle_call(orc, case, isa="fallback"):
+    args, kw = cases.make_inputs(case, isa=isa)
     f = case["func"]
     if f == "DD":
         auto, _nt, bins, x, y, z = args
@@ -57,6 +57,13 @@ def check_result(func, res, gold, rtol=1e-9):
 def test_oracle_matches_golden(orc, case):
     res = _oracle_call(orc, case)
     check_result(case["func"], res, GOLDEN["cases"][case["name"]])
+
+
+@pytest.mark.parametrize("case", cases.CASES, ids=[c["name"] for c in cases.CASES])
+def test_oracle_matches_golden_avx512f(orc, case):
+    """The oracle's fused multiply-add formulas against the reference's AVX512F kernels."""
+    res = _oracle_call(orc, case, isa="avx512f")
+    check_result(case["func"], res, GOLDEN["avx512f_cases"][case["name"]])
 
 
 def test_oracle_reproduces_dd_doctest(orc):
