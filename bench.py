@@ -57,10 +57,11 @@ WORKLOADS["survey"] = dict(workload="DDrppi_mocks auto-correlation of a syntheti
                            weights="U[0.5,1.5]", kind="survey", autocorr=1)
 WORKLOAD = dict(WORKLOADS["cfg2"])
 FLOP_PER_PAIR = 8  # 3 FADD + 1 FMUL + 2 FFMA per 3-D separation
-# dram__bytes_read.sum + dram__bytes_write.sum of one FP32 pair-kernel launch per workload, from
-# the ncu captures summarised in profiles/k_pairs_f32_cfg2_dram_traffic.md and
-# profiles/k_pairs_f32_northstar_full.md
+# dram__bytes_read.sum + dram__bytes_write.sum of one FP32 pair-kernel launch per workload, from an
+# ncu capture of this kernel on that workload (a recorded constant, not measured by this script)
 PAIR_KERNEL_TRAFFIC_BYTES = {"cfg2": 220_196_096 + 3_340_544, "northstar": 54_269_184 + 2_131_200}
+TRAFFIC_SOURCE = ("ncu capture of the pair kernel on this workload (dram__bytes_read.sum + dram__bytes_write.sum "
+                  "per launch): a recorded constant, not measured in this run")
 
 
 def _rank_env():
@@ -120,21 +121,12 @@ def extra_for(C, w1, w2):
     return e
 
 
-def reference_work(lib, C, set1, set2, binfile, dtype):
-    lib.cf_reference_candidate_pairs.argtypes = ([ctypes.c_int64] + [ctypes.c_void_p] * 3 + [ctypes.c_int64]
-                                                 + [ctypes.c_void_p] * 3
-                                                 + [ctypes.c_int, ctypes.c_char_p, ctypes.POINTER(C.ConfigOptions),
-                                                    ctypes.POINTER(ctypes.c_uint64)])
-    lib.cf_reference_candidate_pairs.restype = ctypes.c_int
-    o = options_for(C, WORKLOAD["boxsize"], dtype)
-    out = ctypes.c_uint64()
+def reference_work(C, set1, set2, binfile, dtype, boxsize=None):
+    """Candidate pairs of the reference's lattice for this count (host-only library: loads no GPU
+    code, so the CPU-only reference arm can use it too)."""
+    o = options_for(C, WORKLOAD["boxsize"] if boxsize is None else boxsize, dtype)
     auto = 1 if set2[0] is set1[0] else 0
-    rc = lib.cf_reference_candidate_pairs(len(set1[0]), *(C.ptr(a) for a in set1[:3]), len(set2[0]),
-                                          *(C.ptr(a) for a in set2[:3]), auto, binfile.encode(), ctypes.byref(o),
-                                          ctypes.byref(out))
-    if rc != 0:
-        raise RuntimeError("cf_reference_candidate_pairs failed")
-    return int(out.value)
+    return C.reference_candidate_pairs(set1, set2, binfile, o, auto)
 
 
 class ClockSampler:
@@ -271,9 +263,8 @@ def cpu_reference_run(set1, set2, bins, nthreads, dtype, frac=1.0):
         theory.run_DD(ref, 0, nthreads, bins, s1[0], s1[1], s1[2], X2=s2[0], Y2=s2[1], Z2=s2[2], periodic=True,
                       boxsize=WORKLOAD["boxsize"], isa="fastest", **wkw)
     dt = time.perf_counter() - t0
-    gpu_lib = C.bind(C.LIB_PATH, gpu=True)
     with C.BinFile(bins) as bf:
-        work = reference_work(gpu_lib, C, s1, s2, bf, dtype)
+        work = reference_work(C, s1, s2, bf, dtype)
     return dt, work, n1, n2
 
 
@@ -315,7 +306,7 @@ def run_batch_workload(args):
     L = WORKLOAD["boxsize"]
     binf = C.BinFile(bins)
     binfile = binf.__enter__()
-    work = sum(reference_work(lib, C, c, rand, binfile, np.float32) for c in cats)
+    work = sum(reference_work(C, c, rand, binfile, np.float32) for c in cats)
 
     dcats = [[torch.from_numpy(a).to(dev) for a in c] for c in cats]
     drand = [torch.from_numpy(a).to(dev) for a in rand]
@@ -448,7 +439,6 @@ def cpu_batch_reference(cats, rand, bins, nthreads, ncat=4):
     if not os.path.exists(so):
         return None
     ref = C.bind(so)
-    gpu_lib = C.bind(C.LIB_PATH, gpu=True)
     dt, work = 0.0, 0
     with C.BinFile(bins) as bf:
         for c in cats[:ncat]:
@@ -457,7 +447,7 @@ def cpu_batch_reference(cats, rand, bins, nthreads, ncat=4):
                           weights1=c[3], weights2=rand[3], weight_type="pair_product", periodic=True,
                           boxsize=WORKLOAD["boxsize"], isa="fastest")
             dt += time.perf_counter() - t0
-            work += reference_work(gpu_lib, C, c, rand, bf, np.float32)
+            work += reference_work(C, c, rand, bf, np.float32)
     return dt, work, ncat
 
 
@@ -634,7 +624,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp32_refine", choices=["fp32_refine", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--extras", action="store_true", help="also time the FP64 form and the north-star workload")
+    ap.add_argument("--extras", action="store_true", help="also time the other counters (DDrppi, wp, DDsmu, "
+                                                          "DDtheta, survey counters, vpf)")
     ap.add_argument("--workload", default="cfg2", choices=sorted(WORKLOADS))
     args = ap.parse_args()
     WORKLOAD.clear()
@@ -665,26 +656,17 @@ def main():
     set1, set2, bins = make_workload()
     binf = C.BinFile(bins)
     binfile = binf.__enter__()
-    work = reference_work(lib, C, set1, set2, binfile, np.float64)
+    work = reference_work(C, set1, set2, binfile, np.float64)
+    o = options_for(C, WORKLOAD["boxsize"], np.float64)
+    counter = DeviceCounter(lib, C, corrfunc_gb300, binfile, o, WORKLOAD["autocorr"])
 
     # inputs resident in HBM
     d1 = [torch.from_numpy(a).to(dev) for a in set1]
     d2 = [torch.from_numpy(a).to(dev) for a in set2]
     torch.cuda.synchronize(dev)
-    o = options_for(C, WORKLOAD["boxsize"], np.float64)
 
     def step_device():
-        e = extra_for(C, d1[3].data_ptr(), d2[3].data_ptr())
-        res = C.ResultsDD()
-        rc = lib.cf_gpu_countpairs_device(len(set1[0]), *(ctypes.c_void_p(t.data_ptr()) for t in d1[:3]),
-                                          len(set2[0]), *(ctypes.c_void_p(t.data_ptr()) for t in d2[:3]), 1,
-                                          WORKLOAD["autocorr"],
-                                          binfile.encode(), ctypes.byref(res), ctypes.byref(o), ctypes.byref(e))
-        if rc != 0:
-            raise RuntimeError("countpairs on device inputs failed")
-        npairs = np.ctypeslib.as_array(res.npairs, shape=(res.nbin,)).copy()
-        lib.free_results(ctypes.byref(res))
-        return npairs, corrfunc_gb300.last_stats()
+        return counter.device(d1, d2)
 
     # host arrays in pinned memory for the end-to-end leg
     h1 = [torch.from_numpy(a).pin_memory() for a in set1]
@@ -692,21 +674,9 @@ def main():
     hn1 = [t.numpy() for t in h1]
     hn2 = [t.numpy() for t in h2]
 
-    def step_host():
-        e = extra_for(C, hn1[3].ctypes.data, hn2[3].ctypes.data)
-        res = C.ResultsDD()
-        rc = lib.countpairs(len(hn1[0]), *(C.ptr(a) for a in hn1[:3]), len(hn2[0]), *(C.ptr(a) for a in hn2[:3]),
-                            1, WORKLOAD["autocorr"], binfile.encode(), ctypes.byref(res), ctypes.byref(o),
-                            ctypes.byref(e))
-        if rc != 0:
-            raise RuntimeError("countpairs failed")
-        npairs = np.ctypeslib.as_array(res.npairs, shape=(res.nbin,)).copy()
-        lib.free_results(ctypes.byref(res))
-        return npairs, corrfunc_gb300.last_stats()
-
     ClockSampler.shared(local)  # clock samples from the warm-up on
     for _ in range(max(args.warmup, 3)):
-        ref_np, _ = step_device()
+        ref_np, ref_wavg, _ = step_device()
         flush_l2(torch, dev)
 
     gpu_ms, pair_ms, grid_ms, launches, evaluated, refined, wall = [], [], [], 0, 0, 0, []
@@ -716,7 +686,7 @@ def main():
     with clock_window(local) as clocks:
         for _ in range(args.steps):
             t0 = time.perf_counter()
-            npairs, st = step_device()
+            npairs, _wavg, st = step_device()
             wall.append(time.perf_counter() - t0)
             if not np.array_equal(npairs, ref_np):
                 raise RuntimeError("non-deterministic pair counts between steps")
@@ -731,18 +701,10 @@ def main():
     total_s = max_over_ranks(sum(gpu_ms) / 1e3, world, dev)
     value = replica_throughput(work, args.steps, total_s, world)
 
-    # end-to-end through the public C API with host (pinned) buffers
-    for _ in range(2):
-        step_host()
-    e2e_t = []
-    for _ in range(args.steps):
-        flush_l2(torch, dev)
-        t0 = time.perf_counter()
-        npairs_h, _st = step_host()
-        e2e_t.append(time.perf_counter() - t0)
-        if not np.array_equal(npairs_h, ref_np):
-            raise RuntimeError("host-buffer path disagrees with the device-buffer path")
-    e2e_value = world * work * args.steps / sum(e2e_t)
+    # end to end through the public C API with host buffers: pinned (page-locked) and pageable
+    # (plain numpy arrays, as a Python caller passes them)
+    e2e_value, e2e_ms = end_to_end(counter, hn1, hn2, ref_np, work, world, args.steps, torch, dev)
+    e2e_pg_value, e2e_pg_ms = end_to_end(counter, list(set1), list(set2), ref_np, work, world, args.steps, torch, dev)
     nper = 4 if WORKLOAD["weights"] else 3
     h2d = sum(a.nbytes for a in hn1[:nper]) + (0 if WORKLOAD["autocorr"] else sum(a.nbytes for a in hn2[:nper]))
     d2h = (WORKLOAD["nbins"] + 1) * (8 + 8 + 8 + 8)
@@ -751,6 +713,7 @@ def main():
     lib.cf_gpu_fp32_peak_tflops(ctypes.byref(peak))
     pair_s = sum(pair_ms) / 1e3 / args.steps
     achieved = work * FLOP_PER_PAIR / pair_s / 1e12
+    achieved_eval = (evaluated / args.steps) * FLOP_PER_PAIR / pair_s / 1e12
     traffic = PAIR_KERNEL_TRAFFIC_BYTES.get(args.workload) if args.precision == "fp32_refine" else None
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -761,13 +724,19 @@ def main():
                            reference_lattice_candidates=work),
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                          "frac": achieved / peak.value if peak.value else None, "traffic": traffic,
+                         "traffic_source": TRAFFIC_SOURCE if traffic else None,
                          "kernel": "%s<MODE_R3,false,%s>" % ("k_pairs_f32" if args.precision == "fp32_refine"
                                                              else "k_pairs_f64",
                                                              "true" if WORKLOAD["weights"] else "false"),
                          "peak_source": "measured: FP32 FMA calibration kernel (cf_gpu_fp32_peak_tflops) in this run",
-                         "flop_per_pair": FLOP_PER_PAIR},
+                         "flop_per_pair": FLOP_PER_PAIR,
+                         "work_unit": "reference-lattice candidate pairs",
+                         "achieved_gpu_evaluated": achieved_eval,
+                         "frac_gpu_evaluated": achieved_eval / peak.value if peak.value else None},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "ms_per_step": 1e3 * sum(e2e_t) / args.steps},
+                    "ms_per_step": e2e_ms, "host_memory": "pinned"},
+            "e2e_pageable": {"value": e2e_pg_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                             "ms_per_step": e2e_pg_ms, "host_memory": "pageable (numpy arrays)"},
             "gpu_launches": launches,
             "launch": {"blocks_per_sm": st["blocks_per_sm"], "warps_per_block": st["warps_per_block"],
                        "lane_stride": st["lane_stride"]},
@@ -778,20 +747,41 @@ def main():
                       "counted": int(np.sum(ref_np))},
             "clocks": clocks.summary()}
 
+    if rank == 0:
+        # the same workload with the pair kernel that evaluates every pair in FP64
+        line["fp64_form"] = fp64_form(counter, corrfunc_gb300, lambda: step_device(), ref_np, args.precision,
+                                      sum(pair_ms) / args.steps, sum(gpu_ms) / args.steps, torch, dev)
+        # the same draw as float32 positions and weights
+        f1 = [a.astype(np.float32) for a in set1]
+        f2 = [a.astype(np.float32) for a in set2]
+        line["float32"] = float32_variant(counter, f1, f2, work, args, torch, dev, local)
+        # 1M-point periodic DD auto-correlation (20 log bins to 25, L = 420)
+        line["northstar"] = northstar_record(lib, C, corrfunc_gb300, args, torch, dev, local, peak.value)
+
     if args.extras and rank == 0:
-        line["extras"] = extras(lib, C, corrfunc_gb300, torch, dev, args)
+        line["extras"] = extras(corrfunc_gb300, args)
         corrfunc_gb300.set_precision(args.precision)
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        r = cpu_reference_run(set1, set2, bins, os.cpu_count() or 1, np.float64,
-                              frac=float(os.environ.get("CF_BENCH_CPU_FRAC", "0.25")))
+        # the reference's own countpairs() on the whole workload (all host threads): the CPU
+        # baseline and the parity check of this run's counts, float64 and float32 (the reference's
+        # double run on the float32 values upcast)
+        r = reference_full_run(set1, set2, bins)
         if r is None:
             line["cpu_baseline"] = None
+            line["parity"] = {"checked": False, "why": "reference pair counters not built in oracle/_ref"}
         else:
-            dt, cw, n1, n2 = r
-            line["cpu_baseline"] = {"value": cw / dt, "unit": UNIT, "cores": os.cpu_count(), "kind": "reference",
-                                    "sample": "first %d and %d points of the two catalogues, one run" % (n1, n2),
-                                    "seconds": dt}
+            dt, ref_np_cpu, ref_wavg_cpu = r
+            line["cpu_baseline"] = {"value": work / dt, "unit": UNIT, "cores": os.cpu_count(), "kind": "reference",
+                                    "sample": "the whole workload, one run", "seconds": dt}
+            line["parity"] = parity_record(ref_np, ref_wavg, ref_np_cpu, ref_wavg_cpu)
+            r32 = reference_full_run([a.astype(np.float64) for a in f1], [a.astype(np.float64) for a in f2], bins)
+            f32 = line["float32"]
+            line["float32"]["parity"] = parity_record(f32.pop("_npairs"), f32.pop("_weightavg"), r32[1], r32[2],
+                                                      rtol=1e-4)
+            line["float32"]["parity"]["against"] = "the reference's double-precision run on the float32 values upcast"
+    for k in ("_npairs", "_weightavg"):
+        line.get("float32", {}).pop(k, None)
     binf.__exit__(None, None, None)
     if rank == 0:
         print(json.dumps(line))
@@ -799,33 +789,213 @@ def main():
         torch.distributed.destroy_process_group()
 
 
-def extras(lib, C, cf, torch, dev, args):
-    """FP64 form on the same workload, and the 1M-point periodic DD auto-correlation target."""
-    out = {}
+class DeviceCounter:
+    """countpairs() (DD(r)) on device-resident arrays (cf_gpu_countpairs_device) or on host
+    arrays (the public countpairs(), host-to-device copies inside the call)."""
+
+    def __init__(self, lib, C, cf, binfile, options, autocorr):
+        self.lib, self.C, self.cf = lib, C, cf
+        self.binfile, self.o, self.autocorr = binfile, options, autocorr
+
+    def _extra(self, w1, w2):
+        C = self.C
+        if WORKLOAD["weights"] is None:
+            return C.get_extra_options()
+        e = C.get_extra_options(C.WEIGHT_PAIR_PRODUCT)
+        e.weights0.weights[0] = w1
+        e.weights1.weights[0] = w2
+        e.weights0.num_weights = e.weights1.num_weights = 1
+        return e
+
+    def _finish(self, rc, res, what):
+        if rc != 0:
+            raise RuntimeError("%s failed" % what)
+        npairs = np.ctypeslib.as_array(res.npairs, shape=(res.nbin,)).copy()
+        wavg = np.ctypeslib.as_array(res.weightavg, shape=(res.nbin,)).copy()
+        self.lib.free_results(ctypes.byref(res))
+        return npairs, wavg, self.cf.last_stats()
+
+    def device(self, d1, d2, options=None):
+        C = self.C
+        o = self.o if options is None else options
+        e = self._extra(d1[3].data_ptr() if len(d1) > 3 else None, d2[3].data_ptr() if len(d2) > 3 else None)
+        res = C.ResultsDD()
+        rc = self.lib.cf_gpu_countpairs_device(len(d1[0]), *(ctypes.c_void_p(t.data_ptr()) for t in d1[:3]),
+                                               len(d2[0]), *(ctypes.c_void_p(t.data_ptr()) for t in d2[:3]), 1,
+                                               self.autocorr, self.binfile.encode(), ctypes.byref(res),
+                                               ctypes.byref(o), ctypes.byref(e))
+        return self._finish(rc, res, "countpairs on device inputs")
+
+    def host(self, h1, h2, options=None):
+        C = self.C
+        o = self.o if options is None else options
+        e = self._extra(h1[3].ctypes.data if len(h1) > 3 else None, h2[3].ctypes.data if len(h2) > 3 else None)
+        res = C.ResultsDD()
+        rc = self.lib.countpairs(len(h1[0]), *(C.ptr(a) for a in h1[:3]), len(h2[0]), *(C.ptr(a) for a in h2[:3]),
+                                 1, self.autocorr, self.binfile.encode(), ctypes.byref(res), ctypes.byref(o),
+                                 ctypes.byref(e))
+        return self._finish(rc, res, "countpairs")
+
+
+def end_to_end(counter, h1, h2, ref_np, work, world, steps, torch, dev, options=None):
+    """Throughput of the public countpairs() on host arrays (uploads and read-back inside)."""
+    for _ in range(2):
+        counter.host(h1, h2, options)
+    ts = []
+    for _ in range(steps):
+        flush_l2(torch, dev)
+        t0 = time.perf_counter()
+        npairs_h, _w, _st = counter.host(h1, h2, options)
+        ts.append(time.perf_counter() - t0)
+        if not np.array_equal(npairs_h, ref_np):
+            raise RuntimeError("host-buffer path disagrees with the device-buffer path")
+    return world * work * steps / sum(ts), 1e3 * sum(ts) / steps
+
+
+def fp64_form(counter, cf, step, ref_np, precision, pair_ms_fp32, step_ms_fp32, torch, dev):
+    """The same count with the pair kernel that evaluates every pair with the reference's FP64
+    formula: timing and identical counts."""
+    cf.set_precision("fp64")
+    try:
+        step()
+        flush_l2(torch, dev)
+        pm, sm = [], []
+        for _ in range(2):
+            npairs, _w, st = step()
+            if not np.array_equal(npairs, ref_np):
+                raise RuntimeError("FP64 form counts differ from the FP32+refine form")
+            pm.append(st["pair_kernel_ms"])
+            sm.append(st["total_gpu_ms"])
+            flush_l2(torch, dev)
+    finally:
+        cf.set_precision(precision)
+    return {"kernel": "k_pairs_f64", "pair_kernel_ms": min(pm), "step_ms": min(sm), "npairs_equal": True,
+            "fp32_refine_pair_kernel_ms": pair_ms_fp32, "fp32_refine_step_ms": step_ms_fp32,
+            "speedup_pair_kernel": min(pm) / pair_ms_fp32, "speedup_step": min(sm) / step_ms_fp32}
+
+
+def float32_variant(counter, f1, f2, work, args, torch, dev, local):
+    """The workload as float32 positions and weights (device-resident), timed like the main line."""
+    from corrfunc_gb300 import _capi as C
+    o = options_for(C, WORKLOAD["boxsize"], np.float32)
+    d1 = [torch.from_numpy(a).to(dev) for a in f1]
+    d2 = [torch.from_numpy(a).to(dev) for a in f2]
+    torch.cuda.synchronize(dev)
+    for _ in range(max(args.warmup, 3)):
+        ref, wavg, _ = counter.device(d1, d2, o)
+        flush_l2(torch, dev)
+    gpu_ms, pair_ms = [], []
+    with clock_window(local) as clocks:
+        for _ in range(args.steps):
+            npairs, _w, st = counter.device(d1, d2, o)
+            if not np.array_equal(npairs, ref):
+                raise RuntimeError("non-deterministic float32 counts")
+            gpu_ms.append(st["total_gpu_ms"])
+            pair_ms.append(st["pair_kernel_ms"])
+            flush_l2(torch, dev)
+    return {"value": work * args.steps / (sum(gpu_ms) / 1e3), "unit": UNIT, "ms_per_step": sum(gpu_ms) / args.steps,
+            "pair_kernel_ms": sum(pair_ms) / args.steps, "h2d_bytes_per_step": 0, "counted": int(np.sum(ref)),
+            "clocks": clocks.summary(), "_npairs": ref, "_weightavg": wavg}
+
+
+def northstar_record(lib, C, cf, args, torch, dev, local, peak):
+    """1,000,000 uniform points, periodic L = 420, DD auto-correlation, 20 log bins 0.1-25:
+    device throughput, its FP32 roofline fraction, end to end, and the FP64 form."""
+    from corrfunc_gb300 import catalogs as cat
+    W = WORKLOADS["northstar"]
+    L = W["boxsize"]
+    x, y, z = cat.uniform_box(W["n1"], L, W["seeds"][0])
+    s = (x, y, z)
+    bins = cat.log_bins(W["rmin"], W["rmax"], W["nbins"])
+    saved = dict(WORKLOAD)
+    WORKLOAD.clear()
+    WORKLOAD.update(W)
+    try:
+        with C.BinFile(bins) as bf:
+            work = reference_work(C, s, s, bf, np.float64)
+            o = options_for(C, L, np.float64)
+            counter = DeviceCounter(lib, C, cf, bf, o, 1)
+            d = [torch.from_numpy(a).to(dev) for a in s]
+            torch.cuda.synchronize(dev)
+            for _ in range(max(args.warmup, 3)):
+                ref, _w, _ = counter.device(d, d)
+                flush_l2(torch, dev)
+            gpu_ms, pair_ms, evaluated = [], [], 0
+            with clock_window(local) as clocks:
+                for _ in range(args.steps):
+                    npairs, _w, st = counter.device(d, d)
+                    if not np.array_equal(npairs, ref):
+                        raise RuntimeError("non-deterministic north-star counts")
+                    gpu_ms.append(st["total_gpu_ms"])
+                    pair_ms.append(st["pair_kernel_ms"])
+                    evaluated += st["pairs_evaluated"]
+                    flush_l2(torch, dev)
+            pair_s = sum(pair_ms) / 1e3 / args.steps
+            ach = work * FLOP_PER_PAIR / pair_s / 1e12
+            ach_eval = evaluated / args.steps * FLOP_PER_PAIR / pair_s / 1e12
+            hs = [torch.from_numpy(a).pin_memory().numpy() for a in s]
+            e2e_v, e2e_ms = end_to_end(counter, hs, hs, ref, work, 1, args.steps, torch, dev)
+            f64 = fp64_form(counter, cf, lambda: counter.device(d, d), ref, args.precision,
+                            sum(pair_ms) / args.steps, sum(gpu_ms) / args.steps, torch, dev)
+    finally:
+        WORKLOAD.clear()
+        WORKLOAD.update(saved)
+    return {"workload": W["workload"], "value": work * args.steps / (sum(gpu_ms) / 1e3), "unit": UNIT,
+            "ms_per_step": sum(gpu_ms) / args.steps, "pair_kernel_ms": sum(pair_ms) / args.steps,
+            "roofline": {"bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+                         "frac": ach / peak if peak else None, "kernel": "k_pairs_f32<MODE_R3,false,false>",
+                         "traffic": PAIR_KERNEL_TRAFFIC_BYTES["northstar"], "traffic_source": TRAFFIC_SOURCE,
+                         "achieved_gpu_evaluated": ach_eval, "frac_gpu_evaluated": ach_eval / peak if peak else None,
+                         "target_frac": 0.40},
+            "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": 3 * 8 * W["n1"],
+                    "d2h_bytes_per_step": (W["nbins"] + 1) * 32, "ms_per_step": e2e_ms, "host_memory": "pinned"},
+            "fp64_form": f64,
+            "pairs": {"reference_lattice_candidates": work, "gpu_evaluated": evaluated // args.steps,
+                      "counted": int(np.sum(ref))},
+            "clocks": clocks.summary()}
+
+
+def reference_full_run(set1, set2, bins):
+    """The reference's countpairs() (oracle/_ref, FALLBACK kernels where only those exist, all
+    host threads) on the whole workload: (seconds, npairs, weightavg), or None if not built."""
+    from corrfunc_gb300 import _capi as C
+    from corrfunc_gb300 import theory
+    so = os.path.join(ROOT, "oracle", "_ref", "libcf_ref_DD.so")
+    if not os.path.exists(so):
+        return None
+    ref = C.bind(so)
+    wkw = dict(weights1=set1[3], weights2=set2[3], weight_type="pair_product") if WORKLOAD["weights"] else {}
+    t0 = time.perf_counter()
+    if WORKLOAD["autocorr"]:
+        wkw.pop("weights2", None)
+        r = theory.run_DD(ref, 1, os.cpu_count() or 1, bins, set1[0], set1[1], set1[2], periodic=True,
+                          boxsize=WORKLOAD["boxsize"], isa="fastest", **wkw)
+    else:
+        r = theory.run_DD(ref, 0, os.cpu_count() or 1, bins, set1[0], set1[1], set1[2], X2=set2[0], Y2=set2[1],
+                          Z2=set2[2], periodic=True, boxsize=WORKLOAD["boxsize"], isa="fastest", **wkw)
+    dt = time.perf_counter() - t0
+    return dt, np.asarray(r["npairs"], np.uint64), np.asarray(r["weightavg"], float)
+
+
+def parity_record(gpu_np, gpu_wavg, ref_np, ref_wavg, rtol=1e-6):
+    """npairs (the C arrays carry the unused bin 0 first) bit-exact, weightavg within rtol."""
+    g = np.asarray(gpu_np, np.uint64)[1:]
+    gw = np.asarray(gpu_wavg, float)[1:]
+    eq = bool(np.array_equal(g, np.asarray(ref_np, np.uint64)))
+    m = np.asarray(ref_np) > 0
+    rel = float(np.max(np.abs(gw[m] - ref_wavg[m]) / np.abs(ref_wavg[m]))) if m.any() else 0.0
+    if not eq or rel > rtol:
+        raise RuntimeError("the GPU counts differ from the reference's countpairs() on this workload "
+                           "(npairs equal: %s, max rel weightavg %.3g)" % (eq, rel))
+    return {"checked": True, "against": "the reference's countpairs() (oracle/_ref) on the same inputs",
+            "npairs_equal": eq, "max_rel_weightavg": rel, "rtol": rtol, "bins_compared": int(len(g))}
+
+
+def extras(cf, args):
+    """The other pair counters, timed on the survey's configurations 3 and 4."""
     from corrfunc_gb300 import catalogs as cat
     from corrfunc_gb300 import theory
-    set1, set2, bins = make_workload()
-    for prec in ("fp64", "fp32_refine"):
-        cf.set_precision(prec)
-        theory.DD(0, 1, bins, *set1[:3], weights1=set1[3], X2=set2[0], Y2=set2[1], Z2=set2[2], weights2=set2[3],
-                  weight_type="pair_product", boxsize=WORKLOAD["boxsize"], isa="fallback")
-        st = cf.last_stats()
-        out["cfg2_" + prec + "_pair_kernel_ms"] = st["pair_kernel_ms"]
-    for L in (420.0, 1000.0):
-        x, y, z = cat.uniform_box(1_000_000, L, 0)
-        b = cat.log_bins(0.1, 25.0, 20)
-        with C.BinFile(b) as bf:
-            work = reference_work(lib, C, (x, y, z), (x, y, z), bf, np.float64) if False else None
-        for prec in ("fp64", "fp32_refine"):
-            cf.set_precision(prec)
-            ms = []
-            for _ in range(3):
-                r = theory.DD(1, 1, b, x, y, z, boxsize=L, isa="fallback")
-                ms.append(cf.last_stats())
-            out["northstar_L%d_%s" % (int(L), prec)] = {"pair_kernel_ms": min(s["pair_kernel_ms"] for s in ms),
-                                                        "total_gpu_ms": min(s["total_gpu_ms"] for s in ms),
-                                                        "npairs_sum": int(np.sum(r["npairs"]))}
-    out.update(other_counters(cf, cat, theory))
+    out = other_counters(cf, cat, theory)
     cf.set_precision(args.precision)
     return out
 

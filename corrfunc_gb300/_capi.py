@@ -168,6 +168,10 @@ _GPU_PROTOS["cf_gpu_countpairs_cross_noalloc"] = (
 
 PACKAGE_DIR = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PACKAGE_DIR, "libcorrfunc_gb300.so")
+# the benchmark's work unit (cf_reference_candidate_pairs) without the CUDA engine
+WORKUNIT_LIB_PATH = os.path.join(PACKAGE_DIR, "libcf_workunit.so")
+_WORKUNIT_PROTO = ([c_int64, c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_int,
+                    ctypes.c_char_p, POINTER(ConfigOptions), POINTER(c_uint64)], c_int)
 
 
 def bind(path, gpu=False):
@@ -199,6 +203,33 @@ def library():
                               "corrfunc_gb300 has no CPU fallback")
         _LIB = bind(LIB_PATH, gpu=True)
     return _LIB
+
+
+_WORKUNIT = None
+
+
+def workunit_library():
+    """Host-only library exporting cf_reference_candidate_pairs (loads no GPU code)."""
+    global _WORKUNIT
+    if _WORKUNIT is None:
+        if not os.path.exists(WORKUNIT_LIB_PATH):
+            raise ImportError("libcf_workunit.so is not built (run `python -m corrfunc_gb300.build`)")
+        lib = ctypes.CDLL(WORKUNIT_LIB_PATH)
+        lib.cf_reference_candidate_pairs.argtypes, lib.cf_reference_candidate_pairs.restype = _WORKUNIT_PROTO
+        _WORKUNIT = lib
+    return _WORKUNIT
+
+
+def reference_candidate_pairs(set1, set2, binfile, options, autocorr):
+    """The reference lattice's candidate pairs of a countpairs() call (the benchmark work unit)."""
+    lib = workunit_library()
+    out = c_uint64()
+    rc = lib.cf_reference_candidate_pairs(len(set1[0]), *(ptr(a) for a in set1[:3]), len(set2[0]),
+                                          *(ptr(a) for a in set2[:3]), int(autocorr), binfile.encode(),
+                                          ctypes.byref(options), ctypes.byref(out))
+    if rc != 0:
+        raise RuntimeError("cf_reference_candidate_pairs failed")
+    return int(out.value)
 
 
 def get_config_options():

@@ -18,6 +18,8 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcorrfunc_gb300.so")
+WORKUNIT_LIB = os.path.join(HERE, "libcf_workunit.so")
+HOST_SOURCES = ("cf_api.c", "cf_common.c", "cf_io.c", "cf_workunit.c")
 
 NVCC_ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -46,7 +48,7 @@ def build(verbose=False, extra_nvcc=()):
     cuda = _cuda_root(nvcc)
     inc = ["-I" + INCLUDE, "-I" + CSRC, "-I" + os.path.join(cuda, "include")]
     jobs = []
-    for c in ("cf_api.c", "cf_common.c", "cf_io.c"):
+    for c in HOST_SOURCES:
         obj = os.path.join(BUILD, c[:-2] + ".o")
         jobs.append(["gcc", "-std=gnu11", "-O2", "-fPIC", "-ffp-contract=off", "-fopenmp", "-Wall", "-Wno-unused-function"]
                     + inc + ["-c", os.path.join(CSRC, c), "-o", obj])
@@ -61,11 +63,15 @@ def build(verbose=False, extra_nvcc=()):
         for r in ex.map(_run, jobs):
             if verbose and (r.stdout or r.stderr):
                 print(r.stdout, r.stderr)
-    objs = [os.path.join(BUILD, "cf_api.o"), os.path.join(BUILD, "cf_common.o"), os.path.join(BUILD, "cf_io.o")] + cu_objs
+    objs = [os.path.join(BUILD, c[:-2] + ".o") for c in HOST_SOURCES] + cu_objs
     tmp = LIB + ".tmp"
     _run([nvcc] + NVCC_ARCH + ["-shared", "-o", tmp] + objs
          + ["-L" + os.path.join(cuda, "lib64"), "-lcudart_static", "-lpthread", "-ldl", "-lrt", "-lm", "-Xcompiler", "-fopenmp"])
     os.replace(tmp, LIB)
+    # the work unit alone, without the CUDA engine (CPU-only measurements load this one)
+    tmp = WORKUNIT_LIB + ".tmp"
+    _run(["gcc", "-shared", "-o", tmp, os.path.join(BUILD, "cf_workunit.o"), os.path.join(BUILD, "cf_common.o"), "-lm"])
+    os.replace(tmp, WORKUNIT_LIB)
     link_module_names()
     build_python_modules(verbose)
     build_cli()

@@ -11,6 +11,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include "corrfunc_gb300.h"
 #include "cf_internal.h"
 #include "cf_host.h"
 
@@ -239,3 +240,25 @@ uint32_t cf_mt_next(cf_mt19937 *g)
 }
 
 double cf_mt_uniform(cf_mt19937 *g) { return cf_mt_next(g) / 4294967296.0; }
+
+/* reference lattice rule of a call whose lattice spans the data extent (gridlink on the points'
+ * bounding box, theory/DD/countpairs_impl.c.src:231-332) */
+void cf_fill_rule_extent(cf_refrule *R, const struct config_options *options, double sx, double sy, double sz,
+                         int dfl_kind, int boost_kind, int64_t np1)
+{
+    memset(R, 0, sizeof(*R));
+    R->kind = CF_REF_EXTENT;
+    R->periodic = options->periodic;
+    R->boxsize[0] = options->boxsize_x;
+    R->boxsize[1] = options->boxsize_y == BOXSIZE_NOTGIVEN ? options->boxsize_x : options->boxsize_y;
+    R->boxsize[2] = options->boxsize_z == BOXSIZE_NOTGIVEN ? options->boxsize_x : options->boxsize_z;
+    R->max_size[0] = sx;
+    R->max_size[1] = sy;
+    R->max_size[2] = sz;
+    for (int a = 0; a < 3; a++) R->refine[a] = options->bin_refine_factors[a];
+    R->custom_refine = (options->binning_flags & BINNING_REF_MASK) == BINNING_CUST;
+    R->max_cells = options->max_cells_per_dim;
+    R->dfl_kind = dfl_kind;
+    R->boost_kind = boost_kind;
+    R->np1 = np1;
+}

@@ -65,6 +65,12 @@ typedef struct {
  * reference would fail. */
 int cf_resolve_geometry(const cf_refrule *rule, const double lo[3], const double hi[3], cf_geometry *out);
 
+/* The rule of a call whose reference lattice spans the data extent (cf_common.c); options is a
+ * struct config_options (corrfunc_gb300.h). */
+struct config_options;
+void cf_fill_rule_extent(cf_refrule *R, const struct config_options *options, double sx, double sy, double sz,
+                         int dfl_kind, int boost_kind, int64_t np1);
+
 typedef struct {
     int mode;
     int autocorr;
