@@ -75,6 +75,17 @@ struct PairArgs {
     uint32_t lut_mul;           // 2^(32 - lut_shift): bucket = mad.hi(bits, lut_mul, -lut_base)
     float q_floor;              // added to q in the fast path so that q = 0 stays in the table
     uint32_t lut_negbase;
+    // Byte table (DD(r), xi and DDtheta with at most 127 bins): the classified quantity is
+    //   q' = min(r^2 + b, cap)
+    // (r^2 the squared chord for DDtheta) with b a power of two below the smallest positive edge
+    // and cap the start of the first bucket beyond the last guard, so that its float bits lie in
+    // [bits(b), bits(cap)] and index the table with no lower clamp.  Entry = 2 * row + flag
+    // (flag: the bucket holds a guard and its pairs take the exact path).
+    int lut8;
+    float q_bias, q_cap;        // b, cap
+    uint32_t lut8_base;         // bits(b) >> lut_shift (bucket 0)
+    uint32_t half_row;          // half the bytes of a histogram row (entry * half_row = row offset)
+    uint32_t trash_e;           // entry of a rejected pair (2 * trash row)
 
     int nedges;
     int guard_search_top;       // largest power of two <= nedges - 1 (0 when nedges < 2)

@@ -823,15 +823,16 @@ __host__ __device__ inline SmemLayout smem_layout(int nedges, int nbins, int war
     L.warps = warps;
     L.lut_n = lut_n;
     L.lane_stride = lane_stride;
-    // trash rows: one for 1-D modes, one row of 2-D cells (npibin + 1 = nbins / nedges) otherwise
-    L.nrows = nbins + (store_dz && nbins > nedges ? nbins / nedges : 1);
+    // trash rows: two for 1-D modes (a flagged byte-table entry points half a row past the first),
+    // one row of 2-D cells (npibin + 1 = nbins / nedges) otherwise
+    L.nrows = nbins + (store_dz && nbins > nedges ? nbins / nedges : 2);
     size_t o = 0;
     L.edges_off = o;
     o = align_up(o + sizeof(double) * nedges, 16);
     L.guard_off = o;
     o = align_up(o + sizeof(float) * 2 * nedges, 16);
     L.ascale_off = o;
-    o = align_up(o + sizeof(float) * nedges, 16);
+    o = align_up(o + sizeof(float) * (nedges + 2), 16);
     L.lut_off = o;
     o = align_up(o + sizeof(uint32_t) * (lut_n + 1), 16);
     L.stage_off = o;
@@ -986,6 +987,15 @@ __device__ __forceinline__ uint32_t lut_bucket(const PairArgs &A, float q)
     return min(r, (uint32_t)A.lut_n);
 }
 
+// The byte table's classified quantity q' = min(r^2 + b, cap): (dx^2 + b) + dy^2 + dz^2 with one
+// rounding per fused multiply-add, capped at the start of the first bucket wholly beyond the
+// last guard (all farther pairs share that one reject entry, so their table loads broadcast).
+// q' >= b always (b a power of two), so its bits index the table from bits(b) with no lower clamp.
+__device__ __forceinline__ float q8(const PairArgs &A, float dx, float dy, float dz)
+{
+    return fminf(fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, A.q_bias))), A.q_cap);
+}
+
 // Exact FP32 classification of q against the guard bands: the bin m (1..nedges-1) with
 // *amb = false when q is provably on one side of every edge, *amb = true when q lies inside an
 // edge's band, or 0 when q is provably outside [rmin, rmax).
@@ -1030,7 +1040,7 @@ __device__ __forceinline__ void mock_terms(float4 pj, float4 pjl, float xi, floa
 // 2-D bin checks.  Returns the flat bin (with its FP32 accumulator terms), -1 when the pair is
 // provably not counted, or -2 when it lies inside an error band and needs the reference's FP64
 // formula.
-template <int MODE, bool NEED_AVG, bool NEED_W>
+template <int MODE, bool NEED_AVG, bool NEED_W, bool LUT8>
 __device__ __noinline__ int slow_candidate(const PairArgs &A, const float *glo, const float *ghi, float4 pj, float4 pjl,
                                            float xi, float yi, float zi, float xil, float yil, float zil, float wi,
                                            float ax, float ay, float az, float *favg, float *fw)
@@ -1072,7 +1082,8 @@ __device__ __noinline__ int slow_candidate(const PairArgs &A, const float *glo, 
     }
     const float dx = pj.x - xi, dy = pj.y - yi, dz = pj.z - zi;
     float q;  // the fast path's expression, so that the pair lands in the same flagged bucket
-    if (MODE == MODE_RPPI || MODE == MODE_WP) q = fmaf(dy, dy, fmaf(dx, dx, A.q_floor));
+    if (LUT8) q = q8(A, dx, dy, dz);
+    else if (MODE == MODE_RPPI || MODE == MODE_WP) q = fmaf(dy, dy, fmaf(dx, dx, A.q_floor));
     else q = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, A.q_floor)));
     bool amb;
     const int m = classify_q(A, glo, ghi, q, &amb);
@@ -1280,6 +1291,80 @@ __device__ __forceinline__ void pairs_group(const PairArgs &A, const float4 *__r
     }
 }
 
+// Byte-table fast path of a group of U pairs (DD(r), xi, DDtheta): q' from the scaled staged
+// points, the entry from the table at byte address mad.hi(bits(q'), 2^(32 - shift), lut_add), the
+// flag bit funnelled into slowbits (pair k of n ends at bit 32 - n + k), and one shared reduction
+// per pair at entry * half_row + cnt_s (a flagged entry points half a row into the spare rows).
+template <int MODE, bool NEED_AVG, bool NEED_W, bool OWN, bool SER, int U>
+__device__ __forceinline__ void pairs_group8(const PairArgs &A, const float4 *__restrict__ sjhi,
+                                             const float4 *__restrict__ sjlo, uint32_t lut_add,
+                                             const float *__restrict__ ascale, int k0, uint32_t jb, uint32_t i, float xi,
+                                             float yi, float zi, float xil, float yil, float zil, float wis,
+                                             uint32_t cnt_s, uint32_t &slowbits)
+{
+    uint32_t addr[U];
+    int vw[U], va[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+        const int k = k0 + u;
+        const float4 pj = sjhi[k];
+        const float dx = pj.x - xi, dy = pj.y - yi, dz = pj.z - zi;
+        const float q = q8(A, dx, dy, dz);
+        uint32_t a, e;
+        asm("mad.hi.u32 %0, %1, %2, %3;" : "=r"(a) : "r"(__float_as_uint(q)), "r"(A.lut_mul), "r"(lut_add));
+        asm("ld.shared.u8 %0, [%1];" : "=r"(e) : "r"(a));
+        if (OWN) e = jb + (uint32_t)k > i ? e : A.trash_e;  // own column: only j > i
+        slowbits = __funnelshift_r(slowbits, e, 1);
+        addr[u] = e * A.half_row + cnt_s;
+        vw[u] = 0;
+        va[u] = 0;
+        if (NEED_W) vw[u] = __float2int_rn(wis * pj.w);
+        if (NEED_AVG) {
+            const float4 pjl = sjlo[k];
+            const float dxp = dx + (pjl.x - xil), dyp = dy + (pjl.y - yil), dzp = dz + (pjl.z - zil);
+            const float d = sqrtf(fmaf(dzp, dzp, fmaf(dyp, dyp, dxp * dxp)));
+            const float favg = MODE == MODE_THETA ? chord_degrees<SER>(d) : d;
+            va[u] = __float2int_rn(favg * ascale[e >> 1]);
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+        red_shared_u32_at<0>(addr[u], 1u);
+        if (NEED_AVG) {
+            red_shared_u32_at<4 * avg_word<NEED_AVG>()>(addr[u], (uint32_t)(va[u] >> 16));
+            red_shared_u32_at<4 * avg_word<NEED_AVG>() + 4>(addr[u], (uint32_t)va[u] & 0xffffu);
+        }
+        if (NEED_W) {
+            red_shared_u32_at<4 * w_word<NEED_AVG>()>(addr[u], (uint32_t)(vw[u] >> 16));
+            red_shared_u32_at<4 * w_word<NEED_AVG>() + 4>(addr[u], (uint32_t)vw[u] & 0xffffu);
+        }
+    }
+}
+
+template <int MODE, bool NEED_AVG, bool NEED_W, bool OWN, bool SER>
+__device__ __forceinline__ uint32_t tile_fast8(const PairArgs &A, const float4 *__restrict__ sjhi,
+                                               const float4 *__restrict__ sjlo, uint32_t lut_add,
+                                               const float *__restrict__ ascale, int nj, uint32_t jb, uint32_t i,
+                                               float xi, float yi, float zi, float xil, float yil, float zil, float wis,
+                                               uint32_t cnt_s)
+{
+    uint32_t slowbits = 0;
+    if (nj == 32) {
+        constexpr bool kFull = MODE == MODE_THETA && !NEED_AVG;
+        constexpr int kGroup = kFull ? CF_PAIR_GROUP : (NEED_AVG ? 4 : CF_PAIR_GROUP);
+        constexpr int kUnroll = kFull ? 32 / CF_PAIR_GROUP : (NEED_AVG ? 2 : kR3Unroll);
+#pragma unroll kUnroll
+        for (int k0 = 0; k0 < 32; k0 += kGroup)
+            pairs_group8<MODE, NEED_AVG, NEED_W, OWN, SER, kGroup>(A, sjhi, sjlo, lut_add, ascale, k0, jb, i, xi, yi, zi,
+                                                                   xil, yil, zil, wis, cnt_s, slowbits);
+    } else {
+        for (int k = 0; k < nj; k++)
+            pairs_group8<MODE, NEED_AVG, NEED_W, OWN, SER, 1>(A, sjhi, sjlo, lut_add, ascale, k, jb, i, xi, yi, zi, xil,
+                                                              yil, zil, wis, cnt_s, slowbits);
+    }
+    return slowbits;
+}
+
 template <int MODE, bool NEED_AVG, bool NEED_W, bool OWN, bool SER>
 __device__ __forceinline__ uint32_t tile_fast(const PairArgs &A, const float4 *__restrict__ sjhi,
                                               const float4 *__restrict__ sjlo, const uint32_t *__restrict__ lut,
@@ -1332,7 +1417,7 @@ __device__ __noinline__ void refine_batch(const PairArgs &A, const double *se, c
 // one pass per flagged pair of its busiest lane).  Both points are re-read from the lattice
 // arrays, which the warp touched a moment ago.  Pairs inside an error band move on to the FP64
 // queue.
-template <int MODE, bool NEED_AVG, bool NEED_W>
+template <int MODE, bool NEED_AVG, bool NEED_W, bool LUT8>
 __device__ __noinline__ void slow_batch(const PairArgs &A, const double *se, const float *glo, const float *ghi,
                                         const RefineEntry *sq, int count, RefineEntry *rq, int *rq_count, WarpHist h,
                                         int hl, int lane, unsigned long long *refined)
@@ -1355,8 +1440,8 @@ __device__ __noinline__ void slow_batch(const PairArgs &A, const double *se, con
         }
         const float ax = xi + xil, ay = yi + yil, az = zi + zil;
         float favg = 0.f, fw = 0.f;
-        const int bin = slow_candidate<MODE, NEED_AVG, NEED_W>(A, glo, ghi, pj, pjl, xi, yi, zi, xil, yil, zil, pi.w,
-                                                               ax, ay, az, &favg, &fw);
+        const int bin = slow_candidate<MODE, NEED_AVG, NEED_W, LUT8>(A, glo, ghi, pj, pjl, xi, yi, zi, xil, yil, zil,
+                                                                     pi.w, ax, ay, az, &favg, &fw);
         if (bin >= 0) {
             accumulate<NEED_AVG, NEED_W>(A, h, bin, bin * h.ls + hl, (double)favg, (double)fw);
         } else if (bin == -2) {
@@ -1374,7 +1459,7 @@ __device__ __noinline__ void slow_batch(const PairArgs &A, const double *se, con
     }
 }
 
-template <int MODE, bool NEED_AVG, bool NEED_W>
+template <int MODE, bool NEED_AVG, bool NEED_W, bool LUT8>
 __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pairs_f32(PairArgs A, SmemLayout SL)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -1390,7 +1475,12 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
         ghi[k] = A.g_guard[A.nedges + k];
         asc[k] = A.g_ascale[k];
     }
+    // the scale entries after the last edge serve the trash rows of the byte table (index
+    // nbins = nedges, and nedges + 1 for flagged entries of the last row)
+    if (threadIdx.x < 2) asc[A.nedges + threadIdx.x] = 0.f;
     for (int k = threadIdx.x; k <= SL.lut_n; k += blockDim.x) lut[k] = A.g_lut[k];
+    // byte table: entry address = mad.hi(bits(q'), 2^(32 - shift), lut_add)
+    const uint32_t lut_add = (uint32_t)__cvta_generic_to_shared(lut) - A.lut8_base;
     float4 *sjhi = (float4 *)(smem + SL.stage_off + SL.per_warp_stage * warp);
     float4 *sjlo = sjhi + 32;
     RefineEntry *rq = (RefineEntry *)(sjlo + 32);
@@ -1424,7 +1514,7 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
             // queued pairs belong to the previous catalogue: settle them, then hand over
             __syncwarp();
             if (sq_n > 0) {
-                slow_batch<MODE, NEED_AVG, NEED_W>(A, se, glo, ghi, sq, sq_n, rq, rq_count, h, hl, lane, &refined);
+                slow_batch<MODE, NEED_AVG, NEED_W, LUT8>(A, se, glo, ghi, sq, sq_n, rq, rq_count, h, hl, lane, &refined);
                 sq_n = 0;
             }
             const int rest = *rq_count;
@@ -1471,7 +1561,25 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
             __syncwarp();
             const float wi_s = pi.w * A.w_scale_f;
             uint32_t slowbits;
-            if (MODE == MODE_THETA && NEED_AVG && A.theta_series) {
+            if constexpr (LUT8) {
+                // byte table: pair k of nj ends at bit 32 - nj + k (shifted into bit 0 of k = 0 below)
+                if (MODE == MODE_THETA && NEED_AVG && A.theta_series) {
+                    slowbits = own ? tile_fast8<MODE, NEED_AVG, NEED_W, true, true>(A, sjhi, sjlo, lut_add, h.ascale, nj,
+                                                                                  jb, i, xi, yi, zi, xil, yil, zil, wi_s,
+                                                                                  cnt_s)
+                                   : tile_fast8<MODE, NEED_AVG, NEED_W, false, true>(A, sjhi, sjlo, lut_add, h.ascale,
+                                                                                   nj, jb, i, xi, yi, zi, xil, yil, zil,
+                                                                                   wi_s, cnt_s);
+                } else {
+                    slowbits = own ? tile_fast8<MODE, NEED_AVG, NEED_W, true, false>(A, sjhi, sjlo, lut_add, h.ascale,
+                                                                                   nj, jb, i, xi, yi, zi, xil, yil, zil,
+                                                                                   wi_s, cnt_s)
+                                   : tile_fast8<MODE, NEED_AVG, NEED_W, false, false>(A, sjhi, sjlo, lut_add, h.ascale,
+                                                                                    nj, jb, i, xi, yi, zi, xil, yil, zil,
+                                                                                    wi_s, cnt_s);
+                }
+                slowbits >>= 32 - nj;  // pair k at bit k
+            } else if (MODE == MODE_THETA && NEED_AVG && A.theta_series) {
                 // angular averages by the arcsine series: a separate copy of the unrolled tile loop
                 slowbits = own ? tile_fast<MODE, NEED_AVG, NEED_W, true, true>(A, sjhi, sjlo, lut, h.ascale, nj, jb, i, xi,
                                                                              yi, zi, xil, yil, zil, wi_s, ax, ay, az, cnt_s)
@@ -1493,7 +1601,7 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
                     slowbits ^= 1u << b;
                     RefineEntry r;
                     r.i = i;
-                    r.j = jb + (uint32_t)(nj - 1 - b);  // bit n - 1 - k holds pair k
+                    r.j = jb + (uint32_t)(LUT8 ? b : nj - 1 - b);  // bit k (byte table) or n - 1 - k holds pair k
                     r.meta = T.meta;
                     sq[sq_n + __popc(want & ((1u << lane) - 1u))] = r;
                 }
@@ -1501,7 +1609,7 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
                 queued += __popc(want);
                 __syncwarp();
                 if (sq_n >= 32) {
-                    slow_batch<MODE, NEED_AVG, NEED_W>(A, se, glo, ghi, sq + (sq_n - 32), 32, rq, rq_count, h, hl,
+                    slow_batch<MODE, NEED_AVG, NEED_W, LUT8>(A, se, glo, ghi, sq + (sq_n - 32), 32, rq, rq_count, h, hl,
                                                        lane, &refined);
                     sq_n -= 32;
                 }
@@ -1516,7 +1624,7 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
         evaluated += (uint64_t)icount * (T.j_end - T.j_begin);
     }
     __syncwarp();
-    if (sq_n > 0) slow_batch<MODE, NEED_AVG, NEED_W>(A, se, glo, ghi, sq, sq_n, rq, rq_count, h, hl, lane, &refined);
+    if (sq_n > 0) slow_batch<MODE, NEED_AVG, NEED_W, LUT8>(A, se, glo, ghi, sq, sq_n, rq, rq_count, h, hl, lane, &refined);
     const int rest = *rq_count;
     if (rest > 0) refine_batch<MODE, NEED_AVG, NEED_W>(A, se, rq, rest, h, hl, lane);
     flush_hist<NEED_AVG, NEED_W>(A, h, lane, cur_cat);
@@ -1763,6 +1871,7 @@ struct Engine {
     int force_ls = 0, force_warps = 0;  // FP32 pair-kernel layout chosen by the batch tuner (0 = scored)
     uint32_t task_cap0 = 0;  // first work-list capacity of a call (0 = from the lattice; CF_TASK_CAPACITY)
     int precision = CF_PRECISION_FP32_REFINE;
+    int byte_table = 1;  // byte bucket table for DD(r), xi and DDtheta (CF_BYTE_TABLE=0: 32-bit table)
     int launches = 0;  // kernels launched by the current call
     size_t smem_per_sm = 228 * 1024;
     int last_blocks_per_sm = 0, last_warps_per_block = 0, last_lane_stride = 0;
@@ -1807,6 +1916,10 @@ static int engine_init(void)
     // a small n to exercise the resize-and-rerun path)
     const char *tc = getenv("CF_TASK_CAPACITY");
     if (tc && atoi(tc) > 0) g_eng.task_cap0 = (uint32_t)atoi(tc);
+    // CF_BYTE_TABLE=0 classifies DD(r), xi and DDtheta pairs with the 32-bit bucket table of the
+    // other modes (for measurements; both give the same counts)
+    const char *bt = getenv("CF_BYTE_TABLE");
+    if (bt && atoi(bt) == 0) g_eng.byte_table = 0;
     g_eng.init = true;
     return EXIT_SUCCESS;
 }
@@ -1961,7 +2074,8 @@ static int pair_kernel_regs_t(bool f64)
     cudaFuncAttributes fa;
     cudaError_t rc;
     if constexpr (kHasF32<MODE>) {
-        rc = f64 ? cudaFuncGetAttributes(&fa, k_pairs_f64<MODE, AVG, W>) : cudaFuncGetAttributes(&fa, k_pairs_f32<MODE, AVG, W>);
+        rc = f64 ? cudaFuncGetAttributes(&fa, k_pairs_f64<MODE, AVG, W>)
+                 : cudaFuncGetAttributes(&fa, k_pairs_f32<MODE, AVG, W, false>);
     } else {
         rc = cudaFuncGetAttributes(&fa, k_pairs_f64<MODE, AVG, W>);
     }
@@ -2082,7 +2196,10 @@ static int launch_pairs_t(const PairArgs &A, bool f64, int *launched)
         if (per_sm < 1) per_sm = 1;
         kern<<<g_eng.num_sms * per_sm, threads, SL.total, g_eng.stream>>>(A, SL);
     } else if constexpr (kHasF32<MODE>) {
-        auto kern = k_pairs_f32<MODE, AVG, W>;
+        auto kern = k_pairs_f32<MODE, AVG, W, false>;
+        if constexpr (MODE == MODE_R3 || MODE == MODE_THETA) {
+            if (A.lut8) kern = k_pairs_f32<MODE, AVG, W, true>;
+        }
         CF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SL.total));
         CF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, SL.total));
         if (per_sm < 1) per_sm = 1;
@@ -2176,7 +2293,105 @@ struct Tables {
     float q_floor;
     double dxy, d3;
     size_t guard_off, ascale_off, lut_off;  // byte offsets in W.tab (edges at 0)
+    // byte table (lut_n then counts 32-bit words of it, less one)
+    int lut8;
+    float qbias, qcap;
+    uint32_t trash_e;
 };
+
+constexpr int kLut8Max = 16384;  // largest byte table (entries)
+
+// Byte table of DD(r), xi and DDtheta (at most 127 bins): entry = 2 * row + flag for the buckets
+// of q' = min(r^2 + b, cap) (r^2 the squared chord for DDtheta).  Guards are built for q': an edge
+// e maps to e' = e + b (exact in double), the FP32 evaluation of q' (three roundings, each within
+// u of a partial sum at most q') is within 3.1 u q' of the exact value for the hi coordinates, and
+// those differ from the reference's by the coordinate bound dlim, as for the 32-bit table.
+// Returns false (building nothing) when the layout chosen for it would put a flagged entry at a
+// misaligned address, or the edges do not suit it.
+static bool build_lut8(const cf_job *J, int mode, int nbins, bool need_w, double dlim, float *guards_h, uint8_t *lut_h,
+                       Tables *T)
+{
+    const int ne = J->nedges;
+    const double u = 5.9604644775390625e-08;
+    // edges in the classified domain (r^2, or the squared chord 2 (1 - cos) for DDtheta)
+    double ev[CF_MAX_EDGES];
+    double epos = 0.0;
+    for (int k = 0; k < ne; k++) {
+        ev[k] = mode == MODE_THETA ? 2.0 * (1.0 - J->edges[k]) : J->edges[k];
+        if (ev[k] > 0.0 && (epos == 0.0 || ev[k] < epos)) epos = ev[k];
+    }
+    if (!(epos > 0.0) || !isfinite(ev[ne - 1])) return false;
+    // b: a power of two at most 1/16 of the smallest positive edge (a normal float)
+    const int kb = (int)floor(log2(epos / 16.0));
+    if (kb < -120 || kb > 100) return false;
+    const double b = ldexp(1.0, kb);
+    for (int k = 0; k < ne; k++) {
+        const double e1 = ev[k] + b;
+        const double re = sqrt(fabs(ev[k]));
+        double band = 2.0 * (3.1 * u * e1 + 2.0 * re * dlim + dlim * dlim + 1e-14 * (e1 + 1e-30));
+        if (mode == MODE_THETA) band += 8e-15;
+        guards_h[k] = f_down(e1 - band);
+        guards_h[ne + k] = f_up(e1 + band);
+    }
+    for (int k = ne - 2; k >= 0; k--) guards_h[k] = fminf(guards_h[k], guards_h[k + 1]);
+    for (int k = 1; k < ne; k++) guards_h[ne + k] = fmaxf(guards_h[ne + k], guards_h[ne + k - 1]);
+    const float bf = (float)b, gtop = guards_h[2 * ne - 1];
+    if (!(gtop > bf) || !isfinite(gtop) || gtop > 1e36f) return false;
+    uint32_t bb, bt;
+    memcpy(&bb, &bf, 4);
+    memcpy(&bt, &gtop, 4);
+    // buckets per octave: the finest power of two (at most 2^12) that fits kLut8Max entries from
+    // bucket(b) to the cap bucket
+    int lg = 12;
+    while (lg > 4 && (int)((bt >> (23 - lg)) - (bb >> (23 - lg))) + 2 > kLut8Max) lg--;
+    const int shift = 23 - lg;
+    const int base = (int)(bb >> shift);
+    const int nb = (int)(bt >> shift) + 1 - base;  // cap bucket: the first wholly beyond the last guard
+    if (nb + 1 > kLut8Max) return false;
+    const uint32_t bcap = (uint32_t)(base + nb) << shift;
+    float cap;
+    memcpy(&cap, &bcap, 4);
+    const int words = (nb + 1 + 3) / 4;
+    // layout: a flagged entry lands half a row past the trash row, which must stay 4-byte aligned
+    const int ls = choose_layout(mode, false, J->need_avg != 0, need_w, ne, nbins, words - 1).lane_stride;
+    const int ew = 1 + (J->need_avg ? 2 : 0) + (need_w ? 2 : 0);
+    if ((ew * ls) % 2 != 0) return false;
+    const uint32_t row_bytes = (uint32_t)(4 * ew * ls);
+    const float *glo = guards_h, *ghi = guards_h + ne;
+    const uint32_t trash_e = (uint32_t)nbins << 1;
+    int mlo = 0, mhi = 0;
+    for (int t = 0; t <= nb; t++) {
+        const uint32_t ulo = (uint32_t)(base + t) << shift;
+        const uint32_t uhi = (((uint32_t)(base + t + 1)) << shift) - 1u;
+        float vlo, vhi;
+        memcpy(&vlo, &ulo, 4);
+        memcpy(&vhi, &uhi, 4);
+        while (mlo < ne && glo[mlo] <= vlo) mlo++;
+        while (mhi < ne && glo[mhi] <= vhi) mhi++;
+        uint32_t e;
+        if (vhi < glo[0] || vlo >= ghi[ne - 1]) {
+            e = trash_e;  // certainly below the first edge or at / beyond the last
+        } else if (mlo == mhi && mlo >= 1 && mlo < ne && vlo >= ghi[mlo - 1] && vhi < ghi[ne - 1]) {
+            e = (uint32_t)mlo << 1;  // certainly in bin mlo
+        } else {
+            e = trash_e | 1u;  // a guard band reaches into the bucket: exact path
+        }
+        lut_h[t] = (uint8_t)e;
+    }
+    for (int t = nb + 1; t < 4 * words; t++) lut_h[t] = (uint8_t)trash_e;
+    T->lut8 = 1;
+    T->qbias = bf;
+    T->qcap = cap;
+    T->shift = shift;
+    T->base = base;
+    T->lut_n = words - 1;
+    T->ls = ls;
+    T->row_bytes = row_bytes;
+    T->trash = (uint32_t)nbins * row_bytes;
+    T->trash_e = trash_e;
+    T->q_floor = 0.f;
+    return true;
+}
 
 // packed bin tables of one run: double edges[ne] | float guards[2 ne] | float ascale[ne] | u32 lut[]
 static inline size_t tab_align(size_t v) { return (v + 15) / 16 * 16; }
@@ -2212,6 +2427,16 @@ static int build_tables(Workspace &W, const cf_job *J, int mode, int nbins, bool
         int ex = 30 - (int)ceil(log2(top));
         ex = ex > 100 ? 100 : (ex < -100 ? -100 : ex);
         ascale_h[m] = (float)ldexp(1.0, ex);
+    }
+    T->lut8 = 0;
+    T->qbias = 0.f;
+    T->qcap = 0.f;
+    T->trash_e = 0;
+    if ((mode == MODE_R3 || mode == MODE_THETA) && nbins <= 127 && g_eng.byte_table &&
+        build_lut8(J, mode, nbins, need_w, dlim, guards_h, (uint8_t *)lut_h, T)) {
+        CF_CUDA(cudaMemcpyAsync(W.tab.p, W.h_tab.p, T->lut_off + sizeof(uint32_t) * (T->lut_n + 1),
+                                cudaMemcpyHostToDevice, st));
+        return EXIT_SUCCESS;
     }
     for (int k = 0; k < J->nedges; k++) {
         double e = J->edges[k];
@@ -2542,6 +2767,12 @@ static void pair_constants(PairArgs &A, const cf_job *J, int mode, int nbins, bo
     A.lut_negbase = (uint32_t)(-T.base);
     A.lut_n = T.lut_n;
     A.q_floor = T.q_floor;
+    A.lut8 = T.lut8;
+    A.q_bias = T.qbias;
+    A.q_cap = T.qcap;
+    A.lut8_base = (uint32_t)T.base;
+    A.half_row = T.row_bytes / 2;
+    A.trash_e = T.trash_e;
     A.g_edges = (const double *)W.tab.p;
     A.g_guard = (const float *)((const char *)W.tab.p + T.guard_off);
     A.dz_err = (float)(2.0 * delta[2]);
