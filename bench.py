@@ -456,10 +456,7 @@ def run_reference_arm(args):
     if rank != 0:
         return
     if WORKLOAD.get("kind") == "survey":
-        print(json.dumps({"impl": "reference", "unavailable": "the reference's DDrppi_mocks sources include GSL "
-                          "headers and GSL is not installed, so it cannot be built here; the survey line reports the "
-                          "oracle port as its cpu_baseline"}))
-        return
+        return run_survey_reference(args)
     if WORKLOAD.get("kind") == "batched":
         cats, rand, bins = make_batch_workload()
         times, works = [], []
@@ -602,18 +599,58 @@ def run_survey_workload(args):
     beside["vpf_1M_points_1e5_spheres_ms"] = cf.last_stats()["total_gpu_ms"]
     line["beside"] = beside
     if not args.no_cpu_baseline:
-        # the oracle's brute-force loop (the reference's mocks need GSL and do not build here) on
-        # all host threads, on the first 20,000 galaxies
-        sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "oracle"))
-        import oracle
-        n = 20000
-        t0 = time.perf_counter()
-        oracle.DDrppi_mocks(1, 1, W["pimax"], bins, ra[:n].copy(), dec[:n].copy(), cz[:n].copy(), weights1=w[:n],
-                            weight_type="pair_product")
-        dt = time.perf_counter() - t0
-        line["cpu_baseline"] = {"value": n * (n - 1) / 2.0 / dt, "unit": "pairs/s", "cores": os.cpu_count(),
-                                "kind": "port", "sample": "first %d galaxies, one brute-force run" % n, "seconds": dt}
+        r = survey_reference_run(ra, dec, cz, w, bins)
+        if r is not None:
+            dt, npairs_ref = r
+            if not np.array_equal(np.asarray(npairs_ref), np.asarray(ref["npairs"])):
+                raise RuntimeError("the GPU survey counts differ from the reference's countpairs_mocks()")
+            line["cpu_baseline"] = {"value": npair / dt, "unit": "pairs/s", "cores": os.cpu_count(), "kind": "reference",
+                                    "sample": "the whole survey, one run (reference built against the test-only GSL "
+                                              "stand-in)", "seconds": dt}
+            line["parity"] = {"checked": True, "npairs_equal": True,
+                              "against": "the reference's countpairs_mocks() (oracle/_ref) on the same survey"}
     print(json.dumps(line))
+
+
+def survey_reference_run(ra, dec, cz, w, bins):
+    """The reference's own DDrppi_mocks (oracle/_ref, compiled against the test-only GSL stand-in),
+    all host threads, whole survey: (seconds, npairs), or None if not built."""
+    from corrfunc_gb300 import _capi as C
+    from corrfunc_gb300 import mocks
+    so = os.path.join(ROOT, "oracle", "_ref", "libcf_ref_DDrppi_mocks.so")
+    if not os.path.exists(so):
+        return None
+    lib = C.bind(so)
+    t0 = time.perf_counter()
+    r = mocks.run_DDrppi_mocks(lib, 1, 1, os.cpu_count() or 1, WORKLOAD["pimax"], bins, ra.copy(), dec.copy(),
+                               cz.copy(), weights1=w, weight_type="pair_product", isa="fallback")
+    return time.perf_counter() - t0, r["npairs"]
+
+
+def run_survey_reference(args):
+    from corrfunc_gb300 import catalogs as cat
+    W = WORKLOAD
+    ra, dec, cz = cat.survey(W["n1"], W["seeds"][0], ra=(110.0, 266.0), dec=(-4.0, 70.0), cz=(6000.0, 20000.0))
+    w = cat.weights(W["n1"], W["seeds"][1])
+    bins = cat.log_bins(W["rmin"], W["rmax"], W["nbins"])
+    times = []
+    for _ in range(args.steps):
+        r = survey_reference_run(ra, dec, cz, w, bins)
+        if r is None:
+            print(json.dumps({"impl": "reference", "unavailable": "reference survey counter not built in oracle/_ref"}))
+            return
+        times.append(r[0])
+    npair = W["n1"] * (W["n1"] - 1) / 2.0
+    value = npair * len(times) / sum(times)
+    sample = "the whole survey (reference DDrppi_mocks built against the test-only GSL stand-in)"
+    print(json.dumps({"metric": SURVEY_METRIC, "value": value, "unit": "pairs/s", "n_gpus": args.gpus,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                      "data": "synthetic (seeded survey catalogue)", "config": dict(W, sample=sample),
+                      "impl": "reference",
+                      "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": os.cpu_count(), "kind": "reference",
+                                       "sample": sample},
+                      "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
 
 def main():

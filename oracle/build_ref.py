@@ -1,10 +1,14 @@
 #!/usr/bin/env python3
 """Build recipe for the *reference* Corrfunc 2.5.3 pair counters (test infrastructure only).
 
-This compiles the reference's own C sources for the six pair-counting modules (and its
-particle-file readers, ``io/io.c``) into per-module shared libraries under ``oracle/_ref/`` so that the tests and the CPU baseline
-leg of ``bench.py`` can call the reference through its public C API
-(``theory/DD/countpairs.h:28-35`` and siblings).  Nothing in the product links it.
+This compiles the reference's own C sources for the six pair-counting modules, the survey
+counters (DDrppi_mocks, DDsmu_mocks), the counts-in-spheres modules (vpf, vpf_mocks) and its
+particle-file readers (``io/io.c``) into per-module shared libraries under ``oracle/_ref/`` so
+that the tests and the CPU baseline leg of ``bench.py`` can call the reference through its public
+C API (``theory/DD/countpairs.h:28-35`` and siblings).  Nothing in the product links it.  The
+survey and vpf sources include GSL headers; GSL is not installed here, so they are compiled
+against the test-only stand-in in ``oracle/gsl_shim`` (linear interpolation and MT19937 restated
+from their published descriptions).
 
 The reference generates ``X_double.c`` / ``X_float.c`` from ``X.c.src`` by a sed
 substitution of the token ``DOUBLE`` (``rules.mk:26-52``).  This recipe performs the same
@@ -40,7 +44,12 @@ UTILS_PLAIN = ["utils.c", "progressbar.c", "cpu_features.c"]
 IO_FILES = ["io.c", "io.h", "ftread.c", "ftread.h"]
 UTILS_HEADERS = ["defs.h", "macros.h", "utils.h", "progressbar.h", "cpu_features.h",
                  "function_precision.h", "sglib.h", "avx512_calls.h", "avx2_calls.h",
-                 "avx_calls.h", "sse_calls.h", "fast_acos.h"]
+                 "avx_calls.h", "sse_calls.h", "fast_acos.h", "set_cosmo_dist.h", "cosmology_params.h"]
+# plain sources of the survey modules (cz -> comoving distance), compiled only into those
+UTILS_COSMO = ["set_cosmo_dist.c", "cosmology_params.c"]
+# test-only stand-in for the GSL headers the survey counters and theory vpf include (GSL is not
+# installed here): oracle/gsl_shim/gsl/*.h
+GSL_SHIM = os.path.join(HERE, "gsl_shim")
 UTILS_SRC_TEMPLATES = ["gridlink_impl", "gridlink_utils", "gridlink_mocks_impl"]
 UTILS_HDR_TEMPLATES = ["gridlink_impl", "gridlink_utils", "gridlink_mocks_impl", "cellarray",
                        "cellarray_mocks", "cell_pair", "weight_defs", "weight_functions"]
@@ -59,7 +68,17 @@ MODULES = {
            ["gridlink_impl", "gridlink_utils"]),
     "DDtheta": ("mocks/DDtheta_mocks", "countpairs_theta_mocks.c", "countpairs_theta_mocks_impl",
                 "countpairs_theta_mocks_kernels", ["gridlink_mocks_impl", "gridlink_utils"]),
+    # these include GSL headers: compiled against the test-only stand-in in oracle/gsl_shim
+    "DDrppi_mocks": ("mocks/DDrppi_mocks", "countpairs_rp_pi_mocks.c", "countpairs_rp_pi_mocks_impl",
+                     "countpairs_rp_pi_mocks_kernels", ["gridlink_mocks_impl", "gridlink_utils"]),
+    "DDsmu_mocks": ("mocks/DDsmu_mocks", "countpairs_s_mu_mocks.c", "countpairs_s_mu_mocks_impl",
+                    "countpairs_s_mu_mocks_kernels", ["gridlink_mocks_impl", "gridlink_utils"]),
+    "vpf": ("theory/vpf", "countspheres.c", "countspheres_impl", "vpf_kernels", ["gridlink_impl", "gridlink_utils"]),
+    "vpf_mocks": ("mocks/vpf_mocks", "countspheres_mocks.c", "countspheres_mocks_impl", "vpf_mocks_kernels",
+                  ["gridlink_impl", "gridlink_utils"]),
 }
+# modules whose sources need the GSL stand-in and, for the survey ones, the cosmology sources
+GSL_MODULES = {"DDrppi_mocks": True, "DDsmu_mocks": True, "vpf": False, "vpf_mocks": True}
 
 
 def _expand(src, dst, prec):
@@ -86,7 +105,7 @@ def stage():
     udst = os.path.join(SRC_OUT, "utils")
     os.makedirs(udst)
     usrc = os.path.join(REF_DIR, "utils")
-    for fn in UTILS_PLAIN + UTILS_HEADERS:
+    for fn in UTILS_PLAIN + UTILS_HEADERS + UTILS_COSMO:
         shutil.copy(os.path.join(usrc, fn), udst)
     for stem in UTILS_SRC_TEMPLATES:
         for prec in ("double", "float"):
@@ -134,10 +153,15 @@ def _compile_module(name):
     srcs += [os.path.join(mdst, "%s_%s.c" % (impl, p)) for p in ("double", "float")]
     srcs += [os.path.join(udst, "%s_%s.c" % (u, p)) for u in utems for p in ("double", "float")]
     srcs += [os.path.join(udst, fn) for fn in UTILS_PLAIN]
+    inc = ["-I" + mdst, "-I" + udst]
+    if name in GSL_MODULES:
+        inc.append("-I" + GSL_SHIM)
+        if GSL_MODULES[name]:
+            srcs += [os.path.join(udst, fn) for fn in UTILS_COSMO]
     objs = []
     for s in srcs:
         o = os.path.join(objdir, os.path.basename(s)[:-2] + ".o")
-        cmd = ["gcc"] + _cflags() + ["-I" + mdst, "-I" + udst, "-c", s, "-o", o]
+        cmd = ["gcc"] + _cflags() + inc + ["-c", s, "-o", o]
         subprocess.check_call(cmd)
         objs.append(o)
     so = os.path.join(REF_OUT, "libcf_ref_%s.so" % name)
@@ -162,13 +186,23 @@ def _compile_io():
     return so
 
 
+def _compile_shim_check():
+    """libcf_gslshim.so: the GSL stand-in's generator and interpolant, for their known-answer tests."""
+    so = os.path.join(REF_OUT, "libcf_gslshim.so")
+    subprocess.check_call(["gcc", "-std=c99", "-O2", "-fPIC", "-shared", "-I" + GSL_SHIM,
+                           os.path.join(GSL_SHIM, "shim_check.c"), "-o", so, "-lm"])
+    return so
+
+
 def compile_all():
     if not os.path.isdir(SRC_OUT):
         print("build_ref: no staged sources in %s; reference libraries not built" % SRC_OUT)
         return []
-    with ThreadPoolExecutor(max_workers=min(7, os.cpu_count() or 1)) as ex:
-        sos = list(ex.map(_compile_module, MODULES))
+    mods = [m for m in MODULES if os.path.isdir(os.path.join(SRC_OUT, m))]
+    with ThreadPoolExecutor(max_workers=min(11, os.cpu_count() or 1)) as ex:
+        sos = list(ex.map(_compile_module, mods))
         io = ex.submit(_compile_io).result()
+        sos.append(ex.submit(_compile_shim_check).result())
     if io:
         sos.append(io)
     print("build_ref: built %d reference libraries" % len(sos))

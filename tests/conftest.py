@@ -31,6 +31,20 @@ def reflibs():
     return {m: C.bind(ref_lib_path(m)) for m in REF_MODULES}
 
 
+# reference modules that include GSL headers, compiled against the test-only stand-in
+REF_GSL_MODULES = ["DDrppi_mocks", "DDsmu_mocks", "vpf", "vpf_mocks"]
+
+
+@pytest.fixture(scope="session")
+def reflibs_gsl():
+    """ctypes handles of the reference's survey counters and counts-in-spheres modules (oracle/_ref,
+    built against the GSL stand-in in oracle/gsl_shim)."""
+    if not all(os.path.exists(ref_lib_path(m)) for m in REF_GSL_MODULES):
+        pytest.skip("reference survey / vpf libraries not built in oracle/_ref")
+    from corrfunc_gb300 import _capi as C
+    return {m: C.bind(ref_lib_path(m)) for m in REF_GSL_MODULES}
+
+
 @pytest.fixture(scope="session")
 def orc():
     import oracle

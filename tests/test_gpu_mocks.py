@@ -192,3 +192,32 @@ def test_mocks_deep_survey(orc, avg):
     got = mocks.DDsmu_mocks(1, 2, 1, 1.0, 8, bins, ra.copy(), dec.copy(), cz.copy(), **kw)
     want = orc.DDsmu_mocks(1, 2, 1.0, 8, bins, ra.copy(), dec.copy(), cz.copy(), **kw)
     _check(got, want, "savg")
+
+
+@pytest.mark.parametrize("func", ["DDrppi_mocks", "DDsmu_mocks"])
+def test_mocks_match_reference_library(reflibs_gsl, func):
+    """The GPU survey counters against the reference's own DDrppi_mocks / DDsmu_mocks (compiled
+    against the test-only GSL stand-in) on a 20,000-galaxy survey, weighted, with averages."""
+    from corrfunc_gb300 import _capi as C
+    from corrfunc_gb300 import catalogs as cat
+    from corrfunc_gb300 import mocks
+    ra, dec, cz = cat.survey(20000, 41, ra=(110.0, 200.0), dec=(-4.0, 50.0), cz=(5000.0, 18000.0))
+    w = cat.weights(20000, 42)
+    bins = cat.log_bins(0.1, 25.0, 14)
+    kw = dict(weights1=w, weight_type="pair_product", isa="fallback")
+    if func == "DDrppi_mocks":
+        a = mocks.run_DDrppi_mocks(C.library(), 1, 1, 1, 40.0, bins, ra.copy(), dec.copy(), cz.copy(),
+                                   output_rpavg=True, **kw)
+        b = mocks.run_DDrppi_mocks(reflibs_gsl[func], 1, 1, 16, 40.0, bins, ra.copy(), dec.copy(), cz.copy(),
+                                   output_rpavg=True, **kw)
+        f = "rpavg"
+    else:
+        a = mocks.run_DDsmu_mocks(C.library(), 1, 2, 1, 1.0, 10, bins, ra.copy(), dec.copy(), cz.copy(),
+                                  output_savg=True, **kw)
+        b = mocks.run_DDsmu_mocks(reflibs_gsl[func], 1, 2, 16, 1.0, 10, bins, ra.copy(), dec.copy(), cz.copy(),
+                                  output_savg=True, **kw)
+        f = "savg"
+    assert np.array_equal(a["npairs"], b["npairs"])
+    assert int(np.sum(a["npairs"])) > 0
+    np.testing.assert_allclose(a[f], b[f], rtol=1e-6, atol=1e-12)
+    np.testing.assert_allclose(a["weightavg"], b["weightavg"], rtol=1e-6, atol=1e-12)

@@ -93,3 +93,19 @@ def test_vpf_pymodule_matches_front_end():
     assert [r[0] for r in rows] == list(want["rmax"])
     assert np.array_equal(np.array([r[1:] for r in rows]), want["pN"])
     assert t > 0.0
+
+
+@pytest.mark.parametrize("periodic", [True, False])
+def test_vpf_matches_reference_library(reflibs_gsl, periodic):
+    """countspheres on the GPU against the reference's own theory vpf (its MT19937 sphere centres
+    from the test-only GSL stand-in): 200,000 clustered points, 20,000 spheres, every pN count."""
+    from corrfunc_gb300 import _capi as C
+    from corrfunc_gb300 import catalogs as cat
+    from corrfunc_gb300 import theory
+    L = 300.0
+    x, y, z = cat.clustered_box(200000, L, 23)
+    got = theory.run_vpf(C.library(), 8.0, 8, 20000, 6, 77, x, y, z, periodic=periodic, boxsize=L)
+    want = theory.run_vpf(reflibs_gsl["vpf"], 8.0, 8, 20000, 6, 77, x, y, z, periodic=periodic, boxsize=L)
+    np.testing.assert_array_equal(got["rmax"], want["rmax"])
+    assert np.array_equal(_counts(got, 20000), _counts(want, 20000))
+    assert _counts(got, 20000)[:, 1:].sum() > 0

@@ -280,3 +280,98 @@ def test_oracle_reproduces_mr19_vpf_mocks_golden(orc):
     assert len(cen) == 10000
     assert np.array_equal(np.rint(gold[:, 1:] * 10000).astype(np.int64), counts.astype(np.int64))
     np.testing.assert_allclose(res["pN"], gold[:, 1:], rtol=1e-6, atol=1e-9)
+
+
+def _gslshim():
+    import ctypes
+    path = os.path.join(os.path.dirname(HERE), "oracle", "_ref", "libcf_gslshim.so")
+    if not os.path.exists(path):
+        pytest.skip("GSL stand-in check library not built")
+    lib = ctypes.CDLL(path)
+    lib.cf_shim_mt_nth.restype = ctypes.c_uint32
+    lib.cf_shim_mt_nth.argtypes = [ctypes.c_ulong, ctypes.c_int]
+    lib.cf_shim_interp.restype = ctypes.c_double
+    lib.cf_shim_interp.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.c_int,
+                                   ctypes.c_double]
+    return lib
+
+
+def test_gsl_stand_in_known_answers():
+    """The test-only GSL stand-in the reference's survey and vpf sources are compiled against:
+    MT19937's published known answers (seed 5489: first output 3499211612, 10,000th 4123659995),
+    agreement with the oracle's own restatement of the generator for other seeds (seed 0 standing
+    for GSL's default 4357), and the linear interpolant's formula."""
+    import ctypes
+    lib = _gslshim()
+    assert lib.cf_shim_mt_nth(5489, 1) == 3499211612
+    assert lib.cf_shim_mt_nth(5489, 10000) == 4123659995
+    import oracle
+    oracle.build()
+    for seed in (0, 4357, 1, 2**31 + 5):
+        u = oracle.mt_uniforms(seed, 700) * 4294967296.0
+        assert [int(lib.cf_shim_mt_nth(seed, k)) for k in (1, 2, 624, 625, 700)] == \
+            [int(u[k - 1]) for k in (1, 2, 624, 625, 700)]
+    xa = np.array([0.0, 0.5, 1.25, 2.0, 4.0])
+    ya = np.array([1.0, 3.0, 2.0, 7.5, -1.0])
+    P = ctypes.POINTER(ctypes.c_double)
+    for x in (0.0, 0.3, 0.5, 1.9999, 2.0, 3.3, 4.0):
+        k = min(int(np.searchsorted(xa, x, side="right")) - 1, len(xa) - 2)
+        want = ya[k] + (x - xa[k]) / (xa[k + 1] - xa[k]) * (ya[k + 1] - ya[k])
+        assert lib.cf_shim_interp(xa.ctypes.data_as(P), ya.ctypes.data_as(P), len(xa), x) == want
+    assert np.isnan(lib.cf_shim_interp(xa.ctypes.data_as(P), ya.ctypes.data_as(P), len(xa), 4.5))
+
+
+SURVEY_ISAS = ["fallback"] + (["avx", "avx512f"] if platform.machine() in ("x86_64", "AMD64") else [])
+
+
+@pytest.mark.parametrize("isa", SURVEY_ISAS)
+@pytest.mark.parametrize("func", ["DDrppi_mocks", "DDsmu_mocks"])
+def test_oracle_matches_reference_survey_counters(orc, reflibs_gsl, func, isa):
+    """The oracle's survey counters against the reference's own DDrppi_mocks / DDsmu_mocks (compiled
+    against the GSL stand-in): auto and cross, both cosmologies, weights, averages."""
+    from corrfunc_gb300 import catalogs as cat
+    from corrfunc_gb300 import mocks
+    ra, dec, cz = cat.survey(2500, 31, ra=(120.0, 170.0), dec=(0.0, 40.0), cz=(3000.0, 15000.0))
+    ra2, dec2, cz2 = cat.survey(2000, 32, ra=(120.0, 170.0), dec=(0.0, 40.0), cz=(3000.0, 15000.0))
+    w = cat.weights(2500, 33)
+    w2 = cat.weights(2000, 34)
+    bins = cat.log_bins(0.3, 18.0, 9)
+    lib = reflibs_gsl[func]
+    for auto, cosmo in ((1, 1), (0, 2)):
+        kw = dict(weights1=w, weight_type="pair_product", isa=isa)
+        okw = dict(weights1=w, weight_type="pair_product", isa=isa)
+        if not auto:
+            kw.update(RA2=ra2.copy(), DEC2=dec2.copy(), CZ2=cz2.copy(), weights2=w2)
+            okw.update(RA2=ra2.copy(), DEC2=dec2.copy(), CZ2=cz2.copy(), weights2=w2)
+        if func == "DDrppi_mocks":
+            r = mocks.run_DDrppi_mocks(lib, auto, cosmo, 2, 25.0, bins, ra.copy(), dec.copy(), cz.copy(),
+                                       output_rpavg=True, **kw)
+            o = orc.DDrppi_mocks(auto, cosmo, 25.0, bins, ra.copy(), dec.copy(), cz.copy(), output_rpavg=True, **okw)
+            f = "rpavg"
+        else:
+            r = mocks.run_DDsmu_mocks(lib, auto, cosmo, 2, 0.9, 6, bins, ra.copy(), dec.copy(), cz.copy(),
+                                      output_savg=True, **kw)
+            o = orc.DDsmu_mocks(auto, cosmo, 0.9, 6, bins, ra.copy(), dec.copy(), cz.copy(), output_savg=True, **okw)
+            f = "savg"
+        assert np.array_equal(r["npairs"], o["npairs"])
+        assert int(np.sum(r["npairs"])) > 0
+        np.testing.assert_allclose(o[f], r[f], rtol=1e-10, atol=1e-14)
+        np.testing.assert_allclose(o["weightavg"], r["weightavg"], rtol=1e-10, atol=1e-14)
+
+
+@pytest.mark.parametrize("periodic,refine,seed", [(True, (1, 1, 1), -1234), (True, (2, 2, 1), 7),
+                                                  (False, (1, 1, 1), 11), (False, (2, 1, 3), 0)])
+def test_oracle_matches_reference_vpf(orc, reflibs_gsl, periodic, refine, seed):
+    """The oracle's counts in spheres against the reference's own theory vpf (its MT19937 centres
+    from the GSL stand-in): every pN entry equal."""
+    from corrfunc_gb300 import catalogs as cat
+    from corrfunc_gb300 import theory
+    L = 120.0
+    x, y, z = cat.clustered_box(20000, L, 21)
+    kw = dict(periodic=periodic, boxsize=L)
+    r = theory.run_vpf(reflibs_gsl["vpf"], 7.0, 7, 2000, 6, seed, x, y, z, xbin_refine_factor=refine[0],
+                       ybin_refine_factor=refine[1], zbin_refine_factor=refine[2], **kw)
+    o, counts = orc.vpf(7.0, 7, 2000, 6, seed, x, y, z, refine=refine, **kw)
+    np.testing.assert_array_equal(r["rmax"], o["rmax"])
+    assert np.array_equal(np.rint(r["pN"] * 2000).astype(np.int64), counts.astype(np.int64))
+    assert counts[:, 1:].sum() > 0
