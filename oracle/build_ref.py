@@ -123,6 +123,15 @@ def stage():
             _expand(os.path.join(msrc, impl + ".c.src"), os.path.join(mdst, "%s_%s.c" % (impl, prec)), prec)
             _expand(os.path.join(msrc, impl + ".h.src"), os.path.join(mdst, "%s_%s.h" % (impl, prec)), prec)
             _expand(os.path.join(msrc, kern + ".c.src"), os.path.join(mdst, "%s_%s.c" % (kern, prec)), prec)
+    # the reference's Python wrappers (Corrfunc/*.py, theory/*.py, mocks/*.py), unchanged, so
+    # that tests can run them on this project's CPython extension modules
+    pdst = os.path.join(SRC_OUT, "py", "Corrfunc")
+    for sub in ("", "theory", "mocks"):
+        d = os.path.join(REF_DIR, "Corrfunc", sub)
+        os.makedirs(os.path.join(pdst, sub), exist_ok=True)
+        for fn in sorted(os.listdir(d)):
+            if fn.endswith(".py"):
+                shutil.copy(os.path.join(d, fn), os.path.join(pdst, sub, fn))
     # the particle-file readers (io/io.c, io/ftread.c), for the reader tests
     idst = os.path.join(SRC_OUT, "io")
     os.makedirs(idst)
