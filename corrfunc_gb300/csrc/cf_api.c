@@ -9,6 +9,7 @@
  */
 #define _GNU_SOURCE
 #include <math.h>
+#include <stddef.h>
 #include <stdint.h>
 #include <pthread.h>
 #include <stdio.h>
@@ -20,6 +21,10 @@
 #include "corrfunc_gb300.h"
 #include "cf_internal.h"
 #include "cf_host.h"
+
+/* per-task timings are handed over as the reference's per cell-pair records */
+_Static_assert(sizeof(cf_task_time) == sizeof(struct api_cell_timings), "task timing layout");
+_Static_assert(offsetof(cf_task_time, warp) == offsetof(struct api_cell_timings, tid), "task timing layout");
 
 static double wall_now(void)
 {
@@ -732,6 +737,7 @@ int countpairs_wp(const int64_t ND, void *X, void *Y, void *Z, const double boxs
     J.npibin = 1;
     J.nedges = nrpbins;
     for (int i = 0; i < nrpbins; i++) J.edges[i] = rupp[i] * rupp[i];
+    J.task_timer = options->c_cell_timer ? 1 : 0;
     cf_hist H;
     if (alloc_hist(&H, nrpbins) != EXIT_SUCCESS) {
         free(rupp);
@@ -740,8 +746,16 @@ int countpairs_wp(const int64_t ND, void *X, void *Y, void *Z, const double boxs
     if (cf_engine_run(&J, &H) != EXIT_SUCCESS) {
         free_hist(&H);
         free(rupp);
+        free(J.task_times);
         return EXIT_FAILURE;
     }
+    /* per cell-pair timings (theory/wp/countpairs_wp_impl.c.src:330-332, 433-463): on the GPU one
+     * record per work-list task (an i-chunk of a lattice column against one z-window of a
+     * neighbouring column), with the warp that ran it as the thread id */
+    if (options->c_cell_timer && J.ntask_times > 0)
+        assign_cell_timer((struct api_cell_timings *)J.task_times, J.ntask_times, options);
+    free(J.task_times);
+    J.task_times = NULL;
     const double self_w = (need_w && rupp[0] <= 0.0) ? self_weight_sum(J.w1, ND, options->float_type) : 0.0;
     finalize_hist(&H, 1, rupp[0] <= 0.0, 1, ND, self_w, options->need_avg_sep, need_w, 0);
     results->nbin = nrpbins;
@@ -783,7 +797,6 @@ int countpairs_wp(const int64_t ND, void *X, void *Y, void *Z, const double boxs
     free_hist(&H);
     free(rupp);
     reset_bin_refine_factors(options);
-    options->totncells_timings = 0; /* per cell-pair CPU timings do not exist on the GPU path */
     if (options->c_api_timer) options->c_api_time = (wall_now() - t0) * 1e9; /* nanoseconds, as the reference's wp */
     return EXIT_SUCCESS;
 }

@@ -129,6 +129,8 @@ struct PairArgs {
     // FP64 kernel only: weight sums accumulate in double precision (per-warp rows of doubles in
     // shared memory) instead of fixed point, for weights spanning a wide range
     int w_exact;
+    // per-task timer (null: off): [2 t] elapsed SM clock cycles of task t, [2 t + 1] global warp
+    unsigned long long *task_clock;
 };
 
 // ---------------------------------------------------------------------------------------

@@ -100,7 +100,21 @@ typedef struct {
 
     int need_avg;
     int need_weight;
+
+    /* per-task timings (the GPU's analogue of the reference's per cell-pair timer): when set,
+     * the engine returns a malloc'd array of ntask_times records in task_times (caller frees) */
+    int task_timer;
+    struct cf_task_time *task_times;
+    int64_t ntask_times;
 } cf_job;
+
+/* One work-list task's timing: the i-chunk size and the j-range length, the warp's elapsed time
+ * on it, the first sorted point of each, and the global warp that ran it (the layout of the
+ * reference's struct api_cell_timings). */
+typedef struct cf_task_time {
+    int64_t n1, n2, time_in_ns;
+    int i_first, j_first, warp;
+} cf_task_time;
 
 typedef struct {
     int nbins;           /* total flat bins: nedges, or nedges*(npibin+1) for 2-D modes */

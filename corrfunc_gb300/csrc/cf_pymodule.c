@@ -421,8 +421,19 @@ static PyObject *py_countpairs_wp(PyObject *self, PyObject *args, PyObject *kwar
         Py_XDECREF(it);
     }
     free_results_wp(&r);
-    /* per cell-pair timings are not recorded on the GPU: an empty list */
+    /* per cell-pair timings (theory/python_bindings/_countpairs.c:1972-1983): one tuple per GPU
+     * work-list task, (N1, N2, time_in_ns, first index, second index, warp) */
     PyObject *cells = PyList_New(0);
+    if (o.c_cell_timer && cells) {
+        const struct api_cell_timings *c = o.cell_timings;
+        for (int64_t k = 0; k < o.totncells_timings; k++, c++) {
+            PyObject *it = Py_BuildValue("(LLLiii)", (long long)c->N1, (long long)c->N2, (long long)c->time_in_ns,
+                                         c->first_cellindex, c->second_cellindex, c->tid);
+            PyList_Append(cells, it);
+            Py_XDECREF(it);
+        }
+        free_cell_timings(&o);
+    }
     PyObject *t = Py_BuildValue("(OdO)", list, o.c_api_timer ? o.c_api_time : 0.0, cells);
     Py_XDECREF(list);
     Py_XDECREF(cells);

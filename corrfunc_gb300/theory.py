@@ -219,10 +219,30 @@ def run_wp(lib, boxsize, pimax, nthreads, binfile, X, Y, Z, weights=None, weight
         if c_api_timer:
             ret.append(o.c_api_time)
         if c_cell_timer:
-            ret.append(np.zeros(0, dtype=[("N1", np.int64), ("N2", np.int64), ("time_in_ns", np.int64),
-                                          ("first_cellindex", np.int32), ("second_cellindex", np.int32),
-                                          ("tid", np.int32)]))
+            ret.append(_cell_timings(o))
         return tuple(ret)
+    return out
+
+
+# field names of Corrfunc/theory/wp.py:271-276; aligned as the C struct api_cell_timings (40 bytes)
+CELL_TIMER_DTYPE = np.dtype([("N1", np.int64), ("N2", np.int64), ("time_in_ns", np.int64), ("cellidx1", np.int32),
+                             ("cellidx2", np.int32), ("tid", np.int32)], align=True)
+
+
+def _cell_timings(o):
+    """options->cell_timings as the structured array of Corrfunc/theory/wp.py:243-280 (one record
+    per GPU work-list task: i-chunk size, j-range length, time, first indices, warp), then freed."""
+    n = int(o.totncells_timings)
+    if n <= 0 or not o.cell_timings:
+        return np.zeros(0, dtype=CELL_TIMER_DTYPE)
+    raw = np.ctypeslib.as_array(ctypes.cast(o.cell_timings, ctypes.POINTER(ctypes.c_uint8)),
+                                shape=(n * CELL_TIMER_DTYPE.itemsize,))
+    out = np.frombuffer(raw.tobytes(), dtype=CELL_TIMER_DTYPE).copy()
+    libc = ctypes.CDLL(None)
+    libc.free.argtypes = [ctypes.c_void_p]
+    libc.free(ctypes.cast(o.cell_timings, ctypes.c_void_p))
+    o.cell_timings = None
+    o.totncells_timings = 0
     return out
 
 

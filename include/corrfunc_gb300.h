@@ -557,6 +557,34 @@ static inline struct config_options get_config_options(void)
     return options;
 }
 
+/* per cell-pair timer storage (utils/defs.h:438-473): the library fills options->cell_timings
+ * (totncells_timings records) when options->c_cell_timer is set; the caller releases it */
+static inline void free_cell_timings(struct config_options *options)
+{
+    if (options->totncells_timings > 0 && options->cell_timings != NULL) free(options->cell_timings);
+    options->cell_timings = NULL;
+    options->totncells_timings = 0;
+}
+
+static inline void allocate_cell_timer(struct config_options *options, const int64_t num_cell_pairs)
+{
+    if (options->totncells_timings >= num_cell_pairs) return;
+    free_cell_timings(options);
+    options->cell_timings = (struct api_cell_timings *)calloc((size_t)num_cell_pairs, sizeof(*options->cell_timings));
+    if (options->cell_timings == NULL)
+        fprintf(stderr, "Warning: In %s> Could not allocate memory to store the API timings per cell.\n", __func__);
+    else
+        options->totncells_timings = num_cell_pairs;
+}
+
+static inline void assign_cell_timer(struct api_cell_timings *cell_timings, const int64_t num_cell_pairs,
+                                     struct config_options *options)
+{
+    allocate_cell_timer(options, num_cell_pairs);
+    if (options->totncells_timings >= num_cell_pairs)
+        memmove(options->cell_timings, cell_timings, sizeof(struct api_cell_timings) * (size_t)num_cell_pairs);
+}
+
 static inline int get_num_weights_by_method(const weight_method_t method)
 {
     return method == PAIR_PRODUCT ? 1 : 0;
