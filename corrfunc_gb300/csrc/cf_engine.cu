@@ -17,10 +17,12 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <pthread.h>
+#include <signal.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <unistd.h>
 
 #include "cf_device.cuh"
 #include "cf_internal.h"
@@ -1509,6 +1511,7 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
         t = __shfl_sync(0xffffffffu, t, 0);
         if (t >= ntasks) break;
         const Task T = A.tasks[t];
+        const long long t_start = A.task_clock ? clock64() : 0;
         const uint32_t cat = T.meta >> kCatShift;
         if (cat != cur_cat) {
             // queued pairs belong to the previous catalogue: settle them, then hand over
@@ -1622,6 +1625,10 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
             }
         }
         evaluated += (uint64_t)icount * (T.j_end - T.j_begin);
+        if (A.task_clock && lane == 0) {
+            A.task_clock[2 * (size_t)t] = (unsigned long long)(clock64() - t_start);
+            A.task_clock[2 * (size_t)t + 1] = (blockIdx.x * (blockDim.x >> 5)) + warp;
+        }
     }
     __syncwarp();
     if (sq_n > 0) slow_batch<MODE, NEED_AVG, NEED_W, LUT8>(A, se, glo, ghi, sq, sq_n, rq, rq_count, h, hl, lane, &refined);
@@ -1669,6 +1676,7 @@ __global__ void __launch_bounds__(256) k_pairs_f64(PairArgs A, SmemLayout SL)
         t = __shfl_sync(0xffffffffu, t, 0);
         if (t >= ntasks) break;
         const Task T = A.tasks[t];
+        const long long t_start = A.task_clock ? clock64() : 0;
         const uint32_t cat = T.meta >> kCatShift;
         if (cat != cur_cat) {
             flush_hist<NEED_AVG, NEED_W>(A, h, lane, cur_cat, wd);
@@ -1723,6 +1731,10 @@ __global__ void __launch_bounds__(256) k_pairs_f64(PairArgs A, SmemLayout SL)
             }
         }
         evaluated += (uint64_t)icount * (T.j_end - T.j_begin);
+        if (A.task_clock && lane == 0) {
+            A.task_clock[2 * (size_t)t] = (unsigned long long)(clock64() - t_start);
+            A.task_clock[2 * (size_t)t + 1] = (blockIdx.x * (blockDim.x >> 5)) + warp;
+        }
     }
     flush_hist<NEED_AVG, NEED_W>(A, h, lane, cur_cat, wd);
     if (lane == 0) atomicAdd(&A.g_stats[0], (unsigned long long)evaluated);
@@ -1754,6 +1766,8 @@ struct DevBuf {
     size_t cap = 0;
 };
 
+static bool injected_alloc_failure(size_t bytes);
+
 static int ensure(DevBuf &b, size_t bytes)
 {
     if (bytes == 0) bytes = 16;
@@ -1762,6 +1776,7 @@ static int ensure(DevBuf &b, size_t bytes)
     b.p = nullptr;
     b.cap = 0;
     size_t want = bytes + bytes / 4;
+    if (injected_alloc_failure(want)) return EXIT_FAILURE;
     CF_CUDA(cudaMalloc(&b.p, want));
     b.cap = want;
     return EXIT_SUCCESS;
@@ -1782,6 +1797,7 @@ static int ensure_host(HostBuf &b, size_t bytes)
     b.p = nullptr;
     b.cap = 0;
     size_t want = bytes + bytes / 4;
+    if (injected_alloc_failure(want)) return EXIT_FAILURE;
     CF_CUDA(cudaHostAlloc(&b.p, want, cudaHostAllocDefault));
     b.cap = want;
     return EXIT_SUCCESS;
@@ -1800,6 +1816,7 @@ struct Workspace {
     SetBufs set[2];
     DevBuf mm, scan_tmp[4], chunk_cnt, chunk_off, chunk_begin, chunk_info, chunk_cat, ntask, task_off, tasks;
     DevBuf res, tab;  // result block (ResView), bin tables (edges, guards, averages scale, lookup table)
+    DevBuf task_clock;  // per-task timer records (only when asked for)
     HostBuf h_small, h_tab, h_hist;
 };
 
@@ -1850,7 +1867,7 @@ static void release_workspace(Workspace &W)
     }
     for (int k = 0; k < 4; k++) release(W.scan_tmp[k]);
     DevBuf *v[] = {&W.mm, &W.chunk_cnt, &W.chunk_off, &W.chunk_begin, &W.chunk_info, &W.chunk_cat, &W.ntask,
-                   &W.task_off, &W.tasks, &W.res, &W.tab};
+                   &W.task_off, &W.tasks, &W.res, &W.tab, &W.task_clock};
     for (DevBuf *d : v) release(*d);
     HostBuf *h[] = {&W.h_small, &W.h_tab, &W.h_hist};
     for (HostBuf *b : h) {
@@ -1872,6 +1889,12 @@ struct Engine {
     uint32_t task_cap0 = 0;  // first work-list capacity of a call (0 = from the lattice; CF_TASK_CAPACITY)
     int precision = CF_PRECISION_FP32_REFINE;
     int byte_table = 1;  // byte bucket table for DD(r), xi and DDtheta (CF_BYTE_TABLE=0: 32-bit table)
+    int clock_khz = 0;   // SM clock rate (per-task timer: cycles to nanoseconds)
+    // test hooks (environment, read once): CF_TEST_FAIL_ALLOC=n makes the n-th device or pinned
+    // allocation of the process fail as an out-of-memory would; CF_TEST_SIGNAL=n raises SIGINT
+    // on the host just before the n-th pair-kernel launch of the process
+    long fail_alloc_at = 0, alloc_count = 0;
+    long test_signal = 0, pair_launches = 0;
     int launches = 0;  // kernels launched by the current call
     size_t smem_per_sm = 228 * 1024;
     int last_blocks_per_sm = 0, last_warps_per_block = 0, last_lane_stride = 0;
@@ -1880,6 +1903,55 @@ struct Engine {
 
 static Engine g_eng;
 static pthread_mutex_t g_lock = PTHREAD_MUTEX_INITIALIZER;
+
+static bool injected_alloc_failure(size_t bytes)
+{
+    if (g_eng.fail_alloc_at <= 0 || ++g_eng.alloc_count != g_eng.fail_alloc_at) return false;
+    fprintf(stderr, "corrfunc_gb300: allocation of %zu bytes failed (injected by CF_TEST_FAIL_ALLOC)\n", bytes);
+    return true;
+}
+
+// ------------------------------------------------------------------------------------
+// Interrupts (utils/macros.h:145-167, theory/DD/countpairs_impl.c.src:31-37): while a count runs,
+// SIGTERM, SIGINT and SIGHUP only set a flag (and say so on stderr); the host checks it between
+// launches and returns EXIT_FAILURE.  The kernels already in flight finish (milliseconds); the
+// previous handlers are restored when the call returns.
+// ------------------------------------------------------------------------------------
+static volatile sig_atomic_t g_signal = 0;
+
+static void on_interrupt(int signo)
+{
+    g_signal = signo;
+    static const char msg[] = "corrfunc_gb300: received an interrupt signal; aborting the count\n";
+    const ssize_t w = write(2, msg, sizeof(msg) - 1);
+    (void)w;
+}
+
+struct InterruptGuard {
+    static constexpr int kN = 3;
+    const int sigs[kN] = {SIGTERM, SIGINT, SIGHUP};
+    struct sigaction prev[kN];
+    bool saved[kN];
+    InterruptGuard()
+    {
+        g_signal = 0;
+        struct sigaction sa;
+        memset(&sa, 0, sizeof(sa));
+        sa.sa_handler = on_interrupt;
+        sigemptyset(&sa.sa_mask);
+        for (int k = 0; k < kN; k++) saved[k] = sigaction(sigs[k], &sa, &prev[k]) == 0;
+    }
+    ~InterruptGuard()
+    {
+        for (int k = 0; k < kN; k++)
+            if (saved[k]) sigaction(sigs[k], &prev[k], nullptr);
+    }
+};
+
+#define CF_CHECK_INTERRUPT()                                                                   \
+    do {                                                                                        \
+        if (g_signal) CF_FAIL("interrupted by signal %d; the count was abandoned", (int)g_signal); \
+    } while (0)
 
 static int engine_init(void)
 {
@@ -1901,6 +1973,7 @@ static int engine_init(void)
     g_eng.device = dev;
     g_eng.num_sms = prop.multiProcessorCount;
     g_eng.smem_per_sm = prop.sharedMemPerMultiprocessor;
+    if (cudaDeviceGetAttribute(&g_eng.clock_khz, cudaDevAttrClockRate, dev) != cudaSuccess) g_eng.clock_khz = 0;
     CF_CUDA(cudaStreamCreateWithFlags(&g_eng.stream, cudaStreamNonBlocking));
     for (int k = 0; k < 6; k++) CF_CUDA(cudaEventCreate(&g_eng.ev[k]));
     // CF_PAIR_LAYOUT="<lane stride>,<warps per block>" fixes the FP32 pair kernel's histogram
@@ -1920,6 +1993,10 @@ static int engine_init(void)
     // other modes (for measurements; both give the same counts)
     const char *bt = getenv("CF_BYTE_TABLE");
     if (bt && atoi(bt) == 0) g_eng.byte_table = 0;
+    const char *fa = getenv("CF_TEST_FAIL_ALLOC");
+    if (fa && atol(fa) > 0) g_eng.fail_alloc_at = atol(fa);
+    const char *ts = getenv("CF_TEST_SIGNAL");
+    if (ts && atol(ts) > 0) g_eng.test_signal = atol(ts);
     g_eng.init = true;
     return EXIT_SUCCESS;
 }
@@ -2880,6 +2957,7 @@ static int run_locked(cf_job *J, cf_hist *H)
     const bool dev_float = isf;
     CF_CUDA(cudaMemcpyAsync(mmh, mm, sizeof(unsigned long long) * 2 * kMmSlots, cudaMemcpyDeviceToHost, st));
     CF_CUDA(cudaStreamSynchronize(st));
+    CF_CHECK_INTERRUPT();
     double lo[3], hi[3], wmax[2] = {0, 0}, wmin[2] = {0, 0};
     for (int a = 0; a < 3; a++) {
         lo[a] = ord_dec(mmh[2 * a]);
@@ -2982,9 +3060,16 @@ static int run_locked(cf_job *J, cf_hist *H)
     if (ensure_host(W.h_hist, res_bytes(nbins)) != EXIT_SUCCESS) return EXIT_FAILURE;
     const ResView Rh = res_view(W.h_hist.p, nbins);
 
+    J->task_times = nullptr;
+    J->ntask_times = 0;
     for (int attempt = 0; attempt < 2; attempt++) {
         A.tasks = (const Task *)W.tasks.p;
         A.ntasks = (uint32_t)cap;
+        A.task_clock = nullptr;
+        if (J->task_timer) {
+            if (ensure(W.task_clock, 2 * sizeof(unsigned long long) * cap) != EXIT_SUCCESS) return EXIT_FAILURE;
+            A.task_clock = (unsigned long long *)W.task_clock.p;
+        }
         k_task_list<<<task_grid(G, max_chunks), 128, 0, st>>>(G, max_chunks, (const uint32_t *)W.chunk_begin.p,
                                                               (const uint2 *)W.chunk_info.p,
                                                               (const uint32_t *)S2.cell_start.p, (Task *)W.tasks.p,
@@ -2994,12 +3079,15 @@ static int run_locked(cf_job *J, cf_hist *H)
         CF_CUDA(cudaEventRecord(g_eng.ev[1], st));
         CF_CUDA(cudaMemsetAsync(W.res.p, 0, res_zero_bytes(nbins), st));  // sums, statistics, task counter
         int launched = 0;
+        if (g_eng.test_signal > 0 && ++g_eng.pair_launches == g_eng.test_signal) raise(SIGINT);
+        CF_CHECK_INTERRUPT();
         CF_CUDA(cudaEventRecord(g_eng.ev[2], st));
         if (launch_pairs(mode, A, f64, J->need_avg != 0, need_w, &launched) != EXIT_SUCCESS) return EXIT_FAILURE;
         CF_CUDA(cudaEventRecord(g_eng.ev[3], st));
         CF_CUDA(cudaMemcpyAsync(W.h_hist.p, W.res.p, res_bytes(nbins), cudaMemcpyDeviceToHost, st));
         CF_CUDA(cudaEventRecord(g_eng.ev[4], st));
         CF_CUDA(cudaStreamSynchronize(st));
+        CF_CHECK_INTERRUPT();
         if (*Rh.oob > 0) CF_FAIL("%llu particles are out of bounds. Check periodic wrapping?", *Rh.oob);
         if (Rh.flags[2]) CF_FAIL("internal: neighbour search needed a periodic image beyond +-1");
         if (!Rh.flags[3]) break;
@@ -3012,6 +3100,39 @@ static int run_locked(cf_job *J, cf_hist *H)
         CF_CUDA(cudaMemsetAsync(R.flags + 1, 0, 3 * sizeof(uint32_t), st));  // task total, image error, overflow
     }
     g_eng.last.tasks = Rh.flags[1];
+    if (J->task_timer && Rh.flags[1] > 0) {
+        // per-task timings: the task list and the timer records back to the host
+        const size_t nt = Rh.flags[1];
+        Task *th = (Task *)malloc(sizeof(Task) * nt);
+        unsigned long long *ch = (unsigned long long *)malloc(2 * sizeof(unsigned long long) * nt);
+        cf_task_time *out = (cf_task_time *)calloc(nt, sizeof(cf_task_time));
+        if (!th || !ch || !out) {
+            free(th);
+            free(ch);
+            free(out);
+            CF_FAIL("out of host memory for the per-task timings");
+        }
+        if (cudaMemcpy(th, W.tasks.p, sizeof(Task) * nt, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(ch, W.task_clock.p, 2 * sizeof(unsigned long long) * nt, cudaMemcpyDeviceToHost) != cudaSuccess) {
+            free(th);
+            free(ch);
+            free(out);
+            CF_FAIL("could not read the per-task timings back");
+        }
+        const double ns_per_cycle = g_eng.clock_khz > 0 ? 1e6 / g_eng.clock_khz : 1.0;
+        for (size_t t = 0; t < nt; t++) {
+            out[t].n1 = (int64_t)(th[t].meta & 63u) + 1;
+            out[t].n2 = (int64_t)th[t].j_end - (int64_t)th[t].j_begin;
+            out[t].time_in_ns = (int64_t)((double)ch[2 * t] * ns_per_cycle);
+            out[t].i_first = (int)th[t].i_begin;
+            out[t].j_first = (int)th[t].j_begin;
+            out[t].warp = (int)ch[2 * t + 1];
+        }
+        free(th);
+        free(ch);
+        J->task_times = out;
+        J->ntask_times = (int64_t)nt;
+    }
     memcpy(H->npairs, Rh.cnt, sizeof(uint64_t) * nbins);
     memcpy(H->avg, Rh.avg, sizeof(double) * nbins);
     memcpy(H->wsum, Rh.w, sizeof(double) * nbins);
@@ -3504,8 +3625,10 @@ static int batch_run_locked(BatchPlan *P, cf_hist *H)
     cudaStream_t st = g_eng.stream;
     CF_CUDA(cudaStreamSynchronize(st));
     memset(&g_eng.last, 0, sizeof(g_eng.last));
+    CF_CHECK_INTERRUPT();
     CF_CUDA(cudaGraphLaunch(P->exec, st));
     CF_CUDA(cudaStreamSynchronize(st));
+    CF_CHECK_INTERRUPT();
     if (batch_collect(*P, H) != EXIT_SUCCESS) return EXIT_FAILURE;
     float ms_total = 0.f, ms_pairs = 0.f;
     CF_CUDA(cudaEventElapsedTime(&ms_total, P->ev[0], P->ev[3]));
@@ -3769,6 +3892,7 @@ static int vpf_locked(const cf_vpf_job *J, uint64_t *pN)
         CF_CUDA(cudaMemcpyAsync(J->counts_out, B.within.p, sizeof(uint32_t) * J->ncen, cudaMemcpyDeviceToHost, st));
     CF_CUDA(cudaEventRecord(g_eng.ev[4], st));
     CF_CUDA(cudaStreamSynchronize(st));
+    CF_CHECK_INTERRUPT();
     if (h[npn] > 0) CF_FAIL("%llu particles are out of bounds. Check periodic wrapping?", h[npn]);
     for (size_t k = 0; k < npn; k++) pN[k] = h[k];
     float ms_pairs = 0.f, ms_grid = 0.f, ms_total = 0.f;
@@ -3788,6 +3912,7 @@ static int vpf_locked(const cf_vpf_job *J, uint64_t *pN)
 extern "C" int cf_engine_run(cf_job *job, cf_hist *out)
 {
     pthread_mutex_lock(&g_lock);
+    InterruptGuard guard;
     const int rc = run_locked(job, out);
     pthread_mutex_unlock(&g_lock);
     return rc;
@@ -3796,6 +3921,7 @@ extern "C" int cf_engine_run(cf_job *job, cf_hist *out)
 extern "C" int cf_engine_vpf(const cf_vpf_job *job, uint64_t *pN)
 {
     pthread_mutex_lock(&g_lock);
+    InterruptGuard guard;
     const int rc = vpf_locked(job, pN);
     pthread_mutex_unlock(&g_lock);
     return rc;
@@ -3891,6 +4017,7 @@ extern "C" int cf_engine_batch_run(cf_batch *plan, cf_hist *out)
 {
     if (!plan || !out) return EXIT_FAILURE;
     pthread_mutex_lock(&g_lock);
+    InterruptGuard guard;
     const int rc = batch_run_locked((BatchPlan *)plan, out);
     pthread_mutex_unlock(&g_lock);
     return rc;
