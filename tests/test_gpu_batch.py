@@ -127,3 +127,30 @@ def test_batch_replay_outside_planned_box_fails_loudly(torch):
             batch.run()
     finally:
         batch.close()
+
+
+def test_batch_matches_reference_library(torch, reflibs):
+    """A few catalogues of a batch against the reference's own countpairs() (oracle/_ref) on the
+    same float64 values: clustered catalogues against one uniform catalogue, pair_product weights,
+    ravg -- npairs bit-exact, averages within 1e-6."""
+    from corrfunc_gb300 import theory
+    L = 300.0
+    bins = np.logspace(np.log10(0.1), np.log10(25.0), 21)
+    cats, second = _catalogues(np.float64, [40000, 9000, 25000], 60000, L, 31)
+    dev = [_dev(torch, c) for c in cats]
+    dsec = _dev(torch, second)
+    torch.cuda.synchronize()
+    batch = theory.DDCrossBatch(bins, dev, dsec, periodic=True, boxsize=L, output_ravg=True,
+                                weight_type="pair_product", autotune=False)
+    try:
+        got = batch.run()
+    finally:
+        batch.close()
+    for c, g in zip(cats, got):
+        want = theory.run_DD(reflibs["DD"], 0, 8, bins, c[0], c[1], c[2], weights1=c[3], X2=second[0], Y2=second[1],
+                             Z2=second[2], weights2=second[3], weight_type="pair_product", periodic=True, boxsize=L,
+                             output_ravg=True, isa="fallback")
+        assert np.array_equal(g["npairs"], want["npairs"])
+        assert int(g["npairs"].sum()) > 0
+        np.testing.assert_allclose(g["ravg"], want["ravg"], rtol=1e-6, atol=1e-12)
+        np.testing.assert_allclose(g["weightavg"], want["weightavg"], rtol=1e-6, atol=1e-12)
