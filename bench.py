@@ -268,25 +268,41 @@ def cpu_reference_run(set1, set2, bins, nthreads, dtype, frac=1.0):
     return dt, work, n1, n2
 
 
+def _batch_catalogue(args):
+    """One clustered float32 catalogue of the batched workload (run in a worker process)."""
+    n, L, k = args
+    sys.path.insert(0, ROOT)
+    from corrfunc_gb300 import catalogs as cat
+    x, y, z = cat.clustered_box(int(n), L, k, dtype=np.float32)
+    return (x, y, z, cat.weights(int(n), 200 + k, dtype=np.float32))
+
+
 def make_batch_workload():
+    import multiprocessing as mp
     from corrfunc_gb300 import catalogs as cat
     W = WORKLOAD
     rng = np.random.default_rng(W["size_seed"])
     sizes = np.round(np.exp(rng.uniform(np.log(W["nmin"]), np.log(W["nmax"]), W["nbatch"]))).astype(np.int64)
     L = W["boxsize"]
-    cats = []
-    for k, n in enumerate(sizes):
-        x, y, z = cat.clustered_box(int(n), L, k, dtype=np.float32)
-        cats.append((x, y, z, cat.weights(int(n), 200 + k, dtype=np.float32)))
+    # worker processes started by spawn (this process may already hold a CUDA context)
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+        cats = pool.map(_batch_catalogue, [(int(n), L, k) for k, n in enumerate(sizes)])
     x, y, z = cat.uniform_box(W["n2"], L, W["random_seed"], dtype=np.float32)
     rand = (x, y, z, cat.weights(W["n2"], 2000, dtype=np.float32))
     bins = cat.log_bins(W["rmin"], W["rmax"], W["nbins"])
     return cats, rand, bins
 
 
+def batch_work(C, cats, rand, binfile):
+    """Reference-lattice candidates of every catalogue against the random catalogue (host counter,
+    one thread per catalogue: ctypes releases the interpreter lock during the call)."""
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+        return sum(ex.map(lambda c: reference_work(C, c, rand, binfile, np.float32), cats))
+
+
 def run_batch_workload(args):
-    """Configuration 5: all catalogues in one replayed CUDA graph (one pair-kernel launch) against
-    the same catalogues counted by 64 sequential countpairs() calls."""
+    """Configuration 5 as the headline line (``--workload cfg5``)."""
     rank, world, local = _rank_env()
     import torch
     dev = torch.device("cuda", local)
@@ -295,139 +311,165 @@ def run_batch_workload(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     import corrfunc_gb300
-    from corrfunc_gb300 import _capi as C
-    from corrfunc_gb300 import theory
-    lib = corrfunc_gb300.library()
-    lib.cf_gpu_countpairs_device.argtypes = lib.countpairs.argtypes
-    lib.cf_gpu_countpairs_device.restype = ctypes.c_int
-    lib.cf_gpu_fp32_peak_tflops.argtypes = [ctypes.POINTER(ctypes.c_double)]
     corrfunc_gb300.set_precision(args.precision)
-    cats, rand, bins = make_batch_workload()
-    L = WORKLOAD["boxsize"]
-    binf = C.BinFile(bins)
-    binfile = binf.__enter__()
-    work = sum(reference_work(C, c, rand, binfile, np.float32) for c in cats)
-
-    dcats = [[torch.from_numpy(a).to(dev) for a in c] for c in cats]
-    drand = [torch.from_numpy(a).to(dev) for a in rand]
-    torch.cuda.synchronize(dev)
-    t0 = time.perf_counter()
-    batch = theory.DDCrossBatch(bins, dcats, drand, periodic=True, boxsize=L, weight_type="pair_product",
-                                autotune=True)
-    plan_s = time.perf_counter() - t0
-    o = options_for(C, L, np.float32)
-
-    def one_plain(k):
-        c = dcats[k]
-        e = extra_for(C, c[3].data_ptr(), drand[3].data_ptr())
-        res = C.ResultsDD()
-        rc = lib.cf_gpu_countpairs_device(len(cats[k][0]), *(ctypes.c_void_p(t.data_ptr()) for t in c[:3]),
-                                          WORKLOAD["n2"], *(ctypes.c_void_p(t.data_ptr()) for t in drand[:3]), 1, 0,
-                                          binfile.encode(), ctypes.byref(res), ctypes.byref(o), ctypes.byref(e))
-        if rc != 0:
-            raise RuntimeError("countpairs on device inputs failed")
-        npairs = np.ctypeslib.as_array(res.npairs, shape=(res.nbin,)).copy()
-        lib.free_results(ctypes.byref(res))
-        return npairs, corrfunc_gb300.last_stats()
-
-    # parity of the batch against the plain path on every catalogue (outside the timed region)
-    first = batch.run()
-    for k in range(len(cats)):
-        npairs, _ = one_plain(k)
-        if not np.array_equal(first[k]["npairs"], npairs[1:]):
-            raise RuntimeError("batched counts differ from countpairs() for catalogue %d" % k)
-
-    ClockSampler.shared(local)  # clock samples from the warm-up on
-    for _ in range(max(args.warmup, 3)):
-        batch.run()
-        flush_l2(torch, dev)
-    gpu_ms, pair_ms, launches, evaluated, refined = [], [], 0, 0, 0
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize(dev)
-    with clock_window(local) as clocks:
-        for _ in range(args.steps):
-            out = batch.run()
-            st = corrfunc_gb300.last_stats()
-            if not all(np.array_equal(a["npairs"], b["npairs"]) for a, b in zip(out, first)):
-                raise RuntimeError("non-deterministic batched counts")
-            gpu_ms.append(st["total_gpu_ms"])
-            pair_ms.append(st["pair_kernel_ms"])
-            launches += st["kernel_launches"]
-            evaluated += st["pairs_evaluated"]
-            refined += st["pairs_refined"]
-            flush_l2(torch, dev)
-    torch.cuda.synchronize(dev)
-    total_s = max_over_ranks(sum(gpu_ms) / 1e3, world, dev)
-    value = replica_throughput(work, args.steps, total_s, world)
-
-    # the same 64 counts as 64 sequential plain calls (device inputs), GPU time per call summed
-    seq_ms = []
-    for _ in range(2):
-        tot = 0.0
-        for k in range(len(cats)):
-            _, st = one_plain(k)
-            tot += st["total_gpu_ms"]
-        seq_ms.append(tot)
-        flush_l2(torch, dev)
-
-    # end to end: copy every catalogue from pinned host memory, replay, read the histograms back
-    hcats = [[torch.from_numpy(a).pin_memory() for a in c] for c in cats]
-    hrand = [torch.from_numpy(a).pin_memory() for a in rand]
-    h2d = sum(t.numel() * t.element_size() for c in hcats for t in c) + sum(t.numel() * t.element_size()
-                                                                          for t in hrand)
-    d2h = len(cats) * (WORKLOAD["nbins"] + 1) * 3 * 8
-    e2e_t = []
-    for _ in range(args.steps):
-        flush_l2(torch, dev)
-        t0 = time.perf_counter()
-        for dc, hc in zip(dcats, hcats):
-            for d, h in zip(dc, hc):
-                d.copy_(h, non_blocking=True)
-        for d, h in zip(drand, hrand):
-            d.copy_(h, non_blocking=True)
-        torch.cuda.synchronize(dev)
-        out = batch.run()
-        e2e_t.append(time.perf_counter() - t0)
-    e2e_value = world * work * args.steps / sum(e2e_t)
-
-    peak = ctypes.c_double()
-    lib.cf_gpu_fp32_peak_tflops(ctypes.byref(peak))
-    pair_s = sum(pair_ms) / 1e3 / args.steps
-    achieved = work * FLOP_PER_PAIR / pair_s / 1e12
-    st = corrfunc_gb300.last_stats()
+    rec = batch_record(args, torch, dev, local, world, e2e=True)
     line = {"metric": "pair evaluations/sec (reference-lattice candidate pairs), batched DD cross-correlations",
-            "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
-            "ms_per_step": sum(gpu_ms) / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32+f64-refine" if args.precision == "fp32_refine" else "f64",
+            "value": rec["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
+            "ms_per_step": rec["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64-refine" if args.precision == "fp32_refine" else "f64",
             "data": "synthetic (seeded clustered and uniform catalogues, numpy PCG64)",
             "config": dict(WORKLOAD, precision=args.precision, l2="flushed between steps (256 MB write)",
-                           reference_lattice_candidates=work, catalogue_points=int(sum(len(c[0]) for c in cats))),
-            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
-                         "frac": achieved / peak.value if peak.value else None, "traffic": None,
-                         "kernel": "k_pairs_f32<MODE_R3,false,true> (one launch for all catalogues)",
-                         "peak_source": "measured: FP32 FMA calibration kernel (cf_gpu_fp32_peak_tflops) in this run",
-                         "flop_per_pair": FLOP_PER_PAIR},
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "ms_per_step": 1e3 * sum(e2e_t) / args.steps},
-            "gpu_launches": launches,
-            "batch": {"graph_ms": sum(gpu_ms) / args.steps, "pair_kernel_ms": sum(pair_ms) / args.steps,
-                      "sequential_64_calls_ms": min(seq_ms), "speedup_vs_sequential": min(seq_ms) / (sum(gpu_ms) / args.steps),
-                      "plan_s": plan_s, "kernels_per_graph": st["kernel_launches"],
-                      "tuned_layout": {"lane_stride": st["lane_stride"], "warps_per_block": st["warps_per_block"]}},
-            "pairs": {"reference_lattice_candidates": work, "gpu_evaluated": evaluated // args.steps,
-                      "fp64_refined": refined // args.steps,
-                      "counted": int(sum(int(a["npairs"].sum()) for a in first))},
-            "clocks": clocks.summary()}
+                           reference_lattice_candidates=rec["pairs"]["reference_lattice_candidates"],
+                           catalogue_points=rec["catalogue_points"])}
+    for k in ("roofline", "e2e", "gpu_launches", "batch", "pairs", "clocks"):
+        line[k] = rec[k]
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cats, rand, bins = rec.pop("_data")
         r = cpu_batch_reference(cats, rand, bins, os.cpu_count() or 1)
         line["cpu_baseline"] = None if r is None else {
             "value": r[1] / r[0], "unit": UNIT, "cores": os.cpu_count(), "kind": "reference",
             "sample": "the first %d catalogues against the full random catalogue, one run" % r[2], "seconds": r[0]}
-    batch.close()
-    binf.__exit__(None, None, None)
+    rec.pop("_data", None)
     if rank == 0:
         print(json.dumps(line))
+
+
+def batch_record(args, torch, dev, local, world=1, e2e=False):
+    """Configuration 5: 64 clustered catalogues (50k-500k points) against one 5M-point uniform
+    catalogue, all in one replayed CUDA graph (one pair-kernel launch), against the same catalogues
+    counted by 64 sequential countpairs() calls (which the batch must equal, catalogue by
+    catalogue).  Returns the measurement as a dict (with the data under "_data")."""
+    import corrfunc_gb300
+    from corrfunc_gb300 import _capi as C
+    from corrfunc_gb300 import theory
+    saved = dict(WORKLOAD)
+    WORKLOAD.clear()
+    WORKLOAD.update(WORKLOADS["cfg5"])
+    try:
+        lib = corrfunc_gb300.library()
+        lib.cf_gpu_countpairs_device.argtypes = lib.countpairs.argtypes
+        lib.cf_gpu_countpairs_device.restype = ctypes.c_int
+        lib.cf_gpu_fp32_peak_tflops.argtypes = [ctypes.POINTER(ctypes.c_double)]
+        cats, rand, bins = make_batch_workload()
+        L = WORKLOAD["boxsize"]
+        binf = C.BinFile(bins)
+        binfile = binf.__enter__()
+        work = batch_work(C, cats, rand, binfile)
+        dcats = [[torch.from_numpy(a).to(dev) for a in c] for c in cats]
+        drand = [torch.from_numpy(a).to(dev) for a in rand]
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        batch = theory.DDCrossBatch(bins, dcats, drand, periodic=True, boxsize=L, weight_type="pair_product",
+                                    autotune=True)
+        plan_s = time.perf_counter() - t0
+        o = options_for(C, L, np.float32)
+
+        def one_plain(k):
+            c = dcats[k]
+            e = extra_for(C, c[3].data_ptr(), drand[3].data_ptr())
+            res = C.ResultsDD()
+            rc = lib.cf_gpu_countpairs_device(len(cats[k][0]), *(ctypes.c_void_p(t.data_ptr()) for t in c[:3]),
+                                              WORKLOAD["n2"], *(ctypes.c_void_p(t.data_ptr()) for t in drand[:3]), 1,
+                                              0, binfile.encode(), ctypes.byref(res), ctypes.byref(o), ctypes.byref(e))
+            if rc != 0:
+                raise RuntimeError("countpairs on device inputs failed")
+            npairs = np.ctypeslib.as_array(res.npairs, shape=(res.nbin,)).copy()
+            lib.free_results(ctypes.byref(res))
+            return npairs, corrfunc_gb300.last_stats()
+
+        # parity of the batch against the plain path on every catalogue (outside the timed region)
+        first = batch.run()
+        for k in range(len(cats)):
+            npairs, _ = one_plain(k)
+            if not np.array_equal(first[k]["npairs"], npairs[1:]):
+                raise RuntimeError("batched counts differ from countpairs() for catalogue %d" % k)
+
+        ClockSampler.shared(local)
+        for _ in range(max(args.warmup, 3)):
+            batch.run()
+            flush_l2(torch, dev)
+        gpu_ms, pair_ms, launches, evaluated, refined = [], [], 0, 0, 0
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+        with clock_window(local) as clocks:
+            for _ in range(args.steps):
+                out = batch.run()
+                st = corrfunc_gb300.last_stats()
+                if not all(np.array_equal(a["npairs"], b["npairs"]) for a, b in zip(out, first)):
+                    raise RuntimeError("non-deterministic batched counts")
+                gpu_ms.append(st["total_gpu_ms"])
+                pair_ms.append(st["pair_kernel_ms"])
+                launches += st["kernel_launches"]
+                evaluated += st["pairs_evaluated"]
+                refined += st["pairs_refined"]
+                flush_l2(torch, dev)
+        torch.cuda.synchronize(dev)
+        total_s = max_over_ranks(sum(gpu_ms) / 1e3, world, dev)
+        value = replica_throughput(work, args.steps, total_s, world)
+
+        # the same 64 counts as 64 sequential plain calls (device inputs), GPU time per call summed
+        seq_ms = []
+        for _ in range(2):
+            tot = 0.0
+            for k in range(len(cats)):
+                _, st2 = one_plain(k)
+                tot += st2["total_gpu_ms"]
+            seq_ms.append(tot)
+            flush_l2(torch, dev)
+
+        rec_e2e = None
+        if e2e:
+            # end to end: copy every catalogue from pinned host memory, replay, read the histograms back
+            hcats = [[torch.from_numpy(a).pin_memory() for a in c] for c in cats]
+            hrand = [torch.from_numpy(a).pin_memory() for a in rand]
+            h2d = sum(t.numel() * t.element_size() for c in hcats for t in c) + sum(t.numel() * t.element_size()
+                                                                                  for t in hrand)
+            d2h = len(cats) * (WORKLOAD["nbins"] + 1) * 3 * 8
+            e2e_t = []
+            for _ in range(args.steps):
+                flush_l2(torch, dev)
+                t0 = time.perf_counter()
+                for dc, hc in zip(dcats, hcats):
+                    for d, h in zip(dc, hc):
+                        d.copy_(h, non_blocking=True)
+                for d, h in zip(drand, hrand):
+                    d.copy_(h, non_blocking=True)
+                torch.cuda.synchronize(dev)
+                batch.run()
+                e2e_t.append(time.perf_counter() - t0)
+            rec_e2e = {"value": world * work * args.steps / sum(e2e_t), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                       "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * sum(e2e_t) / args.steps}
+
+        peak = ctypes.c_double()
+        lib.cf_gpu_fp32_peak_tflops(ctypes.byref(peak))
+        pair_s = sum(pair_ms) / 1e3 / args.steps
+        achieved = work * FLOP_PER_PAIR / pair_s / 1e12
+        st = corrfunc_gb300.last_stats()
+        rec = {"workload": WORKLOAD["workload"], "value": value, "unit": UNIT, "ms_per_step": sum(gpu_ms) / args.steps,
+               "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
+                            "frac": achieved / peak.value if peak.value else None, "traffic": None,
+                            "kernel": "k_pairs_f32<MODE_R3,false,true> (one launch for all catalogues)",
+                            "peak_source": "measured: FP32 FMA calibration kernel (cf_gpu_fp32_peak_tflops) in this run",
+                            "flop_per_pair": FLOP_PER_PAIR},
+               "e2e": rec_e2e, "gpu_launches": launches,
+               "batch": {"graph_ms": sum(gpu_ms) / args.steps, "pair_kernel_ms": sum(pair_ms) / args.steps,
+                         "sequential_64_calls_ms": min(seq_ms),
+                         "speedup_vs_sequential": min(seq_ms) / (sum(gpu_ms) / args.steps),
+                         "plan_s": plan_s, "kernels_per_graph": st["kernel_launches"],
+                         "tuned_layout": {"lane_stride": st["lane_stride"], "warps_per_block": st["warps_per_block"]},
+                         "parity": "every catalogue equal to countpairs() on the same device arrays"},
+               "pairs": {"reference_lattice_candidates": work, "gpu_evaluated": evaluated // args.steps,
+                         "fp64_refined": refined // args.steps,
+                         "counted": int(sum(int(a["npairs"].sum()) for a in first))},
+               "catalogue_points": int(sum(len(c[0]) for c in cats)),
+               "clocks": clocks.summary(), "_data": (cats, rand, bins)}
+        batch.close()
+        binf.__exit__(None, None, None)
+        return rec
+    finally:
+        WORKLOAD.clear()
+        WORKLOAD.update(saved)
 
 
 def cpu_batch_reference(cats, rand, bins, nthreads, ncat=4):
@@ -664,6 +706,7 @@ def main():
     ap.add_argument("--extras", action="store_true", help="also time the other counters (DDrppi, wp, DDsmu, "
                                                           "DDtheta, survey counters, vpf)")
     ap.add_argument("--workload", default="cfg2", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-batch", action="store_true", help="leave the batched-workload record out of the line")
     args = ap.parse_args()
     WORKLOAD.clear()
     WORKLOAD.update(WORKLOADS[args.workload])
@@ -794,6 +837,11 @@ def main():
         line["float32"] = float32_variant(counter, f1, f2, work, args, torch, dev, local)
         # 1M-point periodic DD auto-correlation (20 log bins to 25, L = 420)
         line["northstar"] = northstar_record(lib, C, corrfunc_gb300, args, torch, dev, local, peak.value)
+        # 64 catalogues against one 5M-point catalogue in one replayed CUDA graph
+        if not args.no_batch:
+            rec = batch_record(args, torch, dev, local)
+            rec.pop("_data", None)
+            line["cfg5"] = rec
 
     if args.extras and rank == 0:
         line["extras"] = extras(corrfunc_gb300, args)

@@ -131,6 +131,11 @@ struct PairArgs {
     int w_exact;
     // per-task timer (null: off): [2 t] elapsed SM clock cycles of task t, [2 t + 1] global warp
     unsigned long long *task_clock;
+    // FP64 kernel only, for points outside the reference lattice (where the reference's cell-pair
+    // list can leave out pairs in range across the periodic boundary): a pair counts only where the
+    // reference lattice links the two cells (ref_n cells, ref_reach neighbours per axis)
+    int ref_links;
+    int ref_n[3], ref_reach[3];
 };
 
 // ---------------------------------------------------------------------------------------

@@ -72,6 +72,14 @@ constexpr int kZFine = CF_Z_SLABS;
 #ifndef CF_PAIR_MIN_BLOCKS
 #define CF_PAIR_MIN_BLOCKS 2
 #endif
+// DD(r) / xi with weights or separation averages (not both): 2 x 384 threads (up to 85
+// registers, 24 warps per SM) -- measured 4 % faster on the weighted 2M x 2M cross-correlation and
+// 8 % on the 300k auto-correlation with averages than 2 x 512, which spills at 64 registers; plain
+// counts (4 % faster) and counts with both sums (6 %) keep 2 x 512
+constexpr int pair_max_threads(int mode, bool avg, bool w)
+{
+    return (mode == MODE_R3 && avg != w && CF_PAIR_MAX_THREADS > 384) ? 384 : CF_PAIR_MAX_THREADS;
+}
 // pairs whose table offsets are computed before their shared reductions are issued
 #ifndef CF_PAIR_GROUP
 #define CF_PAIR_GROUP 8
@@ -408,7 +416,7 @@ __device__ __forceinline__ void ref_axis_cells(const double *ref_min, const doub
 
 template <typename T>
 __global__ void k_assign(const T *x, const T *y, const T *z, int64_t n, Geom g,
-                         uint32_t *cellid, uint32_t *count, unsigned long long *oob)
+                         uint32_t *cellid, uint32_t *rank, uint32_t *count, unsigned long long *oob)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const T c[3] = {x[i], y[i], z[i]};
@@ -426,7 +434,7 @@ __global__ void k_assign(const T *x, const T *y, const T *z, int64_t n, Geom g,
             if (!in) atomicAdd(g.extent_err, 1ull);
         }
         cellid[i] = cell;
-        atomicAdd(&count[cell], 1u);
+        rank[i] = atomicAdd(&count[cell], 1u);  // the point's slot within its cell
         if (g.check_ref_bounds) {
             // out-of-bounds test of the reference lattice (utils/gridlink_impl.c.src:165-183):
             // points well inside its range pass on their keys, the others take the FP64 test
@@ -483,12 +491,11 @@ __device__ __forceinline__ unsigned long long abs_okey(float v) { return abs_oke
 // survey modes) is written only when set.
 template <typename T>
 __global__ void k_scatter(const T *x, const T *y, const T *z, const T *w, int64_t n, Geom g,
-                          const uint32_t *cellid, const uint32_t *cell_start, uint32_t *fill,
-                          Lattice L)
+                          const uint32_t *cellid, const uint32_t *rank, const uint32_t *cell_start, Lattice L)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t c = cellid[i];
-        const uint32_t pos = cell_start[c] + atomicAdd(&fill[c], 1u);
+        const uint32_t pos = cell_start[c] + rank[i];
         const T p[3] = {x[i], y[i], z[i]};
         const T wv = w ? w[i] : T(1);
         if (g.extent_err && w) {
@@ -571,16 +578,8 @@ __global__ void k_scan_add(uint32_t *out, uint32_t n, const uint32_t *offs)
 }
 
 // ------------------------------------------------------------------------------------
-// chunks (32 consecutive points of one column) and tasks
+// chunks (up to 32 consecutive points of one column) and tasks
 // ------------------------------------------------------------------------------------
-__global__ void k_col_chunks(const uint32_t *cell_start, int ncols, int nz, uint32_t *chunks_per_col)
-{
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncols) return;
-    const uint32_t a = cell_start[(uint32_t)c * nz], b = cell_start[(uint32_t)(c + 1) * nz];
-    chunks_per_col[c] = (b - a + kChunk - 1) / kChunk;
-}
-
 // z slab of sorted point p of a column whose slab offsets are cs[0..nz] (the last slab whose
 // offset is <= p; empty slabs before it share its offset)
 __device__ __forceinline__ uint32_t slab_of(const uint32_t *cs, int nz, uint32_t p)
@@ -594,26 +593,102 @@ __device__ __forceinline__ uint32_t slab_of(const uint32_t *cs, int nz, uint32_t
     return (uint32_t)lo;
 }
 
-// chunk_begin holds absolute point indices (point_base + index within the catalogue's lattice);
-// chunk_info the chunk's size (bits 0-5), first and last z slab (bits 6-17, 18-29) and column;
-// chunk_cat, when given, receives the catalogue number of every chunk (batched counts).  One
-// warp per column, one chunk per lane.
-__global__ void k_chunk_emit(const uint32_t *cell_start, int ncols, int nz, const uint32_t *chunk_off,
-                             uint32_t *chunk_begin, uint2 *chunk_info, uint32_t point_base, uint16_t *chunk_cat,
-                             uint16_t cat)
+// The chunks of one column, walked by one warp: the column's points split into runs at every gap
+// of at least `gap` empty z slabs (a chunk spanning such a gap would pull in the j points of the
+// whole gap; split, its two parts' windows leave most of it out), and each run into chunks of 32
+// consecutive points.  Returns the column's chunk count; with EMIT the chunks are written from
+// slot o0 (slots at or beyond cap are not written and set bit 2 of *err): chunk_begin = absolute
+// first point (point_base + index), chunk_info = size (bits 0-5), first and last z slab (bits
+// 6-17, 18-29) and column, chunk_cat = catalogue (batched counts).  gap < 0: no splits.
+template <bool EMIT>
+__device__ uint32_t column_chunks(const uint32_t *cs, int nz, int gap, int col, int lane, uint32_t o0, uint32_t cap,
+                                  uint32_t *err, uint32_t *chunk_begin, uint2 *chunk_info, uint32_t point_base,
+                                  uint16_t *chunk_cat, uint16_t cat)
+{
+    uint32_t count = 0;
+    auto close_run = [&](uint32_t p0, uint32_t p1) {
+        const uint32_t n = (p1 - p0 + kChunk - 1) / kChunk;
+        if (EMIT) {
+            for (uint32_t k = lane; k < n; k += 32) {
+                const uint32_t p = p0 + k * kChunk, o = o0 + count + k;
+                if (o >= cap) {
+                    if (err) atomicOr(err, 2u);
+                    continue;
+                }
+                const uint32_t cnt = min((uint32_t)kChunk, p1 - p);
+                chunk_begin[o] = point_base + p;
+                chunk_info[o] =
+                    make_uint2(cnt | (slab_of(cs, nz, p) << 6) | (slab_of(cs, nz, p + cnt - 1) << 18), (uint32_t)col);
+                if (chunk_cat) chunk_cat[o] = cat;
+            }
+        }
+        count += n;
+    };
+    const uint32_t a = cs[0], b = cs[nz];
+    if (b == a) return 0;
+    if (gap < 0) {
+        close_run(a, b);
+        return count;
+    }
+    int prev = -1;        // last non-empty slab before the current batch of 32 slabs
+    uint32_t run_p0 = a;  // first point of the open run
+    bool open = false;
+    for (int z0 = 0; z0 < nz; z0 += 32) {
+        const int z = z0 + lane;
+        const bool ne = z < nz && cs[z + 1] > cs[z];
+        // last non-empty slab before z: exclusive max-scan over the batch, with the carry
+        int incl = ne ? z : -1;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl = max(incl, t);
+        }
+        int before = __shfl_up_sync(0xffffffffu, incl, 1);
+        if (lane == 0) before = -1;
+        before = max(before, prev);
+        uint32_t starts = __ballot_sync(0xffffffffu, ne && (before < 0 || z - before > gap));
+        while (starts) {
+            const int bl = __ffs(starts) - 1;
+            starts &= starts - 1;
+            const uint32_t ps = cs[z0 + bl];
+            if (open) close_run(run_p0, ps);
+            run_p0 = ps;
+            open = true;
+        }
+        prev = max(prev, __shfl_sync(0xffffffffu, incl, 31));
+    }
+    if (open) close_run(run_p0, b);
+    return count;
+}
+
+// chunk count of every column (one warp per column)
+__global__ void k_col_chunks(const uint32_t *cell_start, int ncols, int nz, int gap, uint32_t *chunks_per_col)
 {
     const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
-    if (c >= ncols) return;
-    const uint32_t *cs = cell_start + (uint32_t)c * nz;
-    const uint32_t a = cs[0], b = cs[nz];
-    const uint32_t o0 = chunk_off[c];
-    for (uint32_t k = lane; a + k * kChunk < b; k += 32) {
-        const uint32_t p = a + k * kChunk, o = o0 + k;
-        const uint32_t cnt = min((uint32_t)kChunk, b - p);
-        chunk_begin[o] = point_base + p;
-        chunk_info[o] = make_uint2(cnt | (slab_of(cs, nz, p) << 6) | (slab_of(cs, nz, p + cnt - 1) << 18), (uint32_t)c);
-        if (chunk_cat) chunk_cat[o] = cat;
-    }
+    if (c >= ncols) return;  // warp-uniform
+    const uint32_t n = column_chunks<false>(cell_start + (uint32_t)c * nz, nz, gap, c, lane, 0u, 0u, nullptr, nullptr,
+                                            nullptr, 0u, nullptr, 0);
+    if (lane == 0) chunks_per_col[c] = n;
+}
+
+// the chunks of every column at its offset chunk_off[c] (one warp per column; cap: chunk slots)
+__global__ void k_chunk_emit(const uint32_t *cell_start, int ncols, int nz, int gap, const uint32_t *chunk_off,
+                             uint32_t cap, uint32_t *err, uint32_t *chunk_begin, uint2 *chunk_info,
+                             uint32_t point_base, uint16_t *chunk_cat, uint16_t cat)
+{
+    const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (c >= ncols) return;  // warp-uniform
+    column_chunks<true>(cell_start + (uint32_t)c * nz, nz, gap, c, lane, chunk_off[c], cap, err, chunk_begin,
+                        chunk_info, point_base, chunk_cat, cat);
+}
+
+// Chunk slots reserved for n1 points in ncols columns of nz slabs: a run of n points makes at
+// most n/32 + 1 chunks, and a column holds at most nz / (gap + 1) + 1 runs (k runs separated by
+// at least gap empty slabs take k + (k - 1) gap slabs), and no more runs than points.
+static inline uint64_t chunk_slots(uint64_t n1, uint64_t ncols, int nz, int gap)
+{
+    const uint64_t per_col = ncols * ((uint64_t)nz / (uint64_t)(gap + 1) + 1);
+    const uint64_t runs = gap < 0 ? ncols : (per_col < n1 ? per_col : n1);
+    return (n1 + kChunk - 1) / kChunk + runs;
 }
 
 constexpr int kWzTab = 256;  // stencil columns whose z reach is tabulated in the task geometry
@@ -654,6 +729,20 @@ __host__ __device__ inline int column_wz(const TaskGeom &G, int dx, int dy)
     if (G.rmax_3d > 0.0) W = fmin(W, sqrt(fmax(0.0, G.rmax_3d * G.rmax_3d - rho2)));
     const double wz = ceil(W / G.s[2]);
     return wz > 1e9 ? 1000000000 : (int)wz;
+}
+
+// Empty z slabs at which a column's chunks are split: two and a half times the own column's z
+// reach (a split there takes at least half a reach of j slabs out of every neighbour column's
+// window, against one more task per column).  -1 (no splits) when the reach spans the column, or
+// when the set-1 points are so dense (n1 points in ncols columns) that a column would hold 16
+// points or more in such a gap on average.
+static int chunk_gap(const TaskGeom &G, int64_t n1, uint32_t ncols)
+{
+    const int wz = column_wz(G, 0, 0);
+    if (wz < 0 || wz >= G.nz) return -1;
+    const int gap = 2 * wz + wz / 2;
+    if ((double)n1 * gap >= 16.0 * (double)ncols * (double)G.nz) return -1;
+    return gap;
 }
 
 // Tasks of one chunk against one neighbour column (dx, dy) (stencil index c): one per periodic z
@@ -947,6 +1036,20 @@ __device__ __forceinline__ bool j_is_first(const PairArgs &A, uint32_t i, uint32
     return rj.y < ri.y;
 }
 
+// Whether the reference's cell-pair list holds reference cells ci, cj (linear indices) with the
+// periodic image M of the second point: per axis the second cell is the first one's neighbour at
+// an offset of at most the refine factor, wrapped across the lattice edge with the image of the
+// side it leaves (utils/gridlink_impl.c.src:494-521).
+__device__ __forceinline__ bool ref_linked(const PairArgs &A, int ci, int cj, int Mx, int My, int Mz)
+{
+    const int n1 = A.ref_n[1], n2 = A.ref_n[2];
+    const int ti = ci / n2, tj = cj / n2;
+    const int dz = cj - tj * n2 - (ci - ti * n2) + Mz * n2;
+    const int dy = tj % n1 - ti % n1 + My * n1;
+    const int dx = tj / n1 - ti / n1 + Mx * A.ref_n[0];
+    return abs(dx) <= A.ref_reach[0] && abs(dy) <= A.ref_reach[1] && abs(dz) <= A.ref_reach[2];
+}
+
 template <int MODE>
 __device__ __noinline__ int refine_pair(const PairArgs &A, const double *se, uint32_t i, uint32_t j,
                                         int mx, int my, int mz, double *avg_term, double *wprod)
@@ -993,6 +1096,31 @@ __device__ __forceinline__ uint32_t lut_bucket(const PairArgs &A, float q)
 // rounding per fused multiply-add, capped at the start of the first bucket wholly beyond the
 // last guard (all farther pairs share that one reject entry, so their table loads broadcast).
 // q' >= b always (b a power of two), so its bits index the table from bits(b) with no lower clamp.
+// Two FP32 lanes in one 64-bit register: the paired (f32x2) arithmetic evaluates two pairs per
+// instruction, each lane rounded exactly as its scalar counterpart.
+__device__ __forceinline__ unsigned long long f2_pack(float a, float b)
+{
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(unsigned long long v, float &a, float &b)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsigned long long b)
+{
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b, unsigned long long c)
+{
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
 __device__ __forceinline__ float q8(const PairArgs &A, float dx, float dy, float dz)
 {
     return fminf(fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, A.q_bias))), A.q_cap);
@@ -1293,10 +1421,12 @@ __device__ __forceinline__ void pairs_group(const PairArgs &A, const float4 *__r
     }
 }
 
-// Byte-table fast path of a group of U pairs (DD(r), xi, DDtheta): q' from the scaled staged
-// points, the entry from the table at byte address mad.hi(bits(q'), 2^(32 - shift), lut_add), the
-// flag bit funnelled into slowbits (pair k of n ends at bit 32 - n + k), and one shared reduction
-// per pair at entry * half_row + cnt_s (a flagged entry points half a row into the spare rows).
+// Byte-table fast path of a group of U pairs (DD(r), xi, DDtheta): the staged j coordinates are
+// read four points per 16-byte broadcast load (the stage is laid out coordinate by coordinate),
+// q' from the points, the entry from the table at byte address mad.hi(bits(q'), 2^(32 - shift),
+// lut_add), the flag bit funnelled into slowbits (pair k of n ends at bit 32 - n + k), and one
+// shared reduction per pair at entry * half_row + cnt_s (a flagged entry points half a row into
+// the spare rows).
 template <int MODE, bool NEED_AVG, bool NEED_W, bool OWN, bool SER, int U>
 __device__ __forceinline__ void pairs_group8(const PairArgs &A, const float4 *__restrict__ sjhi,
                                              const float4 *__restrict__ sjlo, uint32_t lut_add,
@@ -1304,29 +1434,64 @@ __device__ __forceinline__ void pairs_group8(const PairArgs &A, const float4 *__
                                              float yi, float zi, float xil, float yil, float zil, float wis,
                                              uint32_t cnt_s, uint32_t &slowbits)
 {
+    static_assert(U % 4 == 0, "the byte-table stage is read four j points at a time");
+    const float *S = (const float *)sjhi, *SL8 = (const float *)sjlo;
+    const unsigned long long xi2 = f2_pack(xi, xi), yi2 = f2_pack(yi, yi), zi2 = f2_pack(zi, zi),
+                             b2 = f2_pack(A.q_bias, A.q_bias);
     uint32_t addr[U];
     int vw[U], va[U];
 #pragma unroll
-    for (int u = 0; u < U; u++) {
-        const int k = k0 + u;
-        const float4 pj = sjhi[k];
-        const float dx = pj.x - xi, dy = pj.y - yi, dz = pj.z - zi;
-        const float q = q8(A, dx, dy, dz);
-        uint32_t a, e;
-        asm("mad.hi.u32 %0, %1, %2, %3;" : "=r"(a) : "r"(__float_as_uint(q)), "r"(A.lut_mul), "r"(lut_add));
-        asm("ld.shared.u8 %0, [%1];" : "=r"(e) : "r"(a));
-        if (OWN) e = jb + (uint32_t)k > i ? e : A.trash_e;  // own column: only j > i
-        slowbits = __funnelshift_r(slowbits, e, 1);
-        addr[u] = e * A.half_row + cnt_s;
-        vw[u] = 0;
-        va[u] = 0;
-        if (NEED_W) vw[u] = __float2int_rn(wis * pj.w);
+    for (int g = 0; g < U; g += 4) {
+        const int kq = k0 + g;
+        const float4 X = *(const float4 *)(S + kq), Y = *(const float4 *)(S + 32 + kq),
+                     Z = *(const float4 *)(S + 64 + kq);
+        float4 Wj = make_float4(0.f, 0.f, 0.f, 0.f), LX = Wj, LY = Wj, LZ = Wj;
+        if (NEED_W) Wj = *(const float4 *)(S + 96 + kq);
         if (NEED_AVG) {
-            const float4 pjl = sjlo[k];
-            const float dxp = dx + (pjl.x - xil), dyp = dy + (pjl.y - yil), dzp = dz + (pjl.z - zil);
-            const float d = sqrtf(fmaf(dzp, dzp, fmaf(dyp, dyp, dxp * dxp)));
-            const float favg = MODE == MODE_THETA ? chord_degrees<SER>(d) : d;
-            va[u] = __float2int_rn(favg * ascale[e >> 1]);
+            LX = *(const float4 *)(SL8 + kq);
+            LY = *(const float4 *)(SL8 + 32 + kq);
+            LZ = *(const float4 *)(SL8 + 64 + kq);
+        }
+        // separations and q' of the four pairs, two per paired instruction (the scalar q8 chain,
+        // lane by lane)
+        float dxv[4], dyv[4], dzv[4], qv[4];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const unsigned long long dx2 = f2_sub(h ? f2_pack(X.z, X.w) : f2_pack(X.x, X.y), xi2);
+            const unsigned long long dy2 = f2_sub(h ? f2_pack(Y.z, Y.w) : f2_pack(Y.x, Y.y), yi2);
+            const unsigned long long dz2 = f2_sub(h ? f2_pack(Z.z, Z.w) : f2_pack(Z.x, Z.y), zi2);
+            const unsigned long long q2 = f2_fma(dz2, dz2, f2_fma(dy2, dy2, f2_fma(dx2, dx2, b2)));
+            f2_unpack(dx2, dxv[2 * h], dxv[2 * h + 1]);
+            f2_unpack(dy2, dyv[2 * h], dyv[2 * h + 1]);
+            f2_unpack(dz2, dzv[2 * h], dzv[2 * h + 1]);
+            f2_unpack(q2, qv[2 * h], qv[2 * h + 1]);
+        }
+#pragma unroll
+        for (int v = 0; v < 4; v++) {
+            const int u = g + v, k = kq + v;
+            const float dx = dxv[v], dy = dyv[v], dz = dzv[v];
+            const float q = fminf(qv[v], A.q_cap);
+            uint32_t a, e;
+            asm("mad.hi.u32 %0, %1, %2, %3;" : "=r"(a) : "r"(__float_as_uint(q)), "r"(A.lut_mul), "r"(lut_add));
+            asm("ld.shared.u8 %0, [%1];" : "=r"(e) : "r"(a));
+            if (OWN) e = jb + (uint32_t)k > i ? e : A.trash_e;  // own column: only j > i
+            slowbits = __funnelshift_r(slowbits, e, 1);
+            addr[u] = e * A.half_row + cnt_s;
+            vw[u] = 0;
+            va[u] = 0;
+            if (NEED_W) {
+                const float jw = v == 0 ? Wj.x : v == 1 ? Wj.y : v == 2 ? Wj.z : Wj.w;
+                vw[u] = __float2int_rn(wis * jw);
+            }
+            if (NEED_AVG) {
+                const float lx = v == 0 ? LX.x : v == 1 ? LX.y : v == 2 ? LX.z : LX.w;
+                const float ly = v == 0 ? LY.x : v == 1 ? LY.y : v == 2 ? LY.z : LY.w;
+                const float lz = v == 0 ? LZ.x : v == 1 ? LZ.y : v == 2 ? LZ.z : LZ.w;
+                const float dxp = dx + (lx - xil), dyp = dy + (ly - yil), dzp = dz + (lz - zil);
+                const float d = sqrtf(fmaf(dzp, dzp, fmaf(dyp, dyp, dxp * dxp)));
+                const float favg = MODE == MODE_THETA ? chord_degrees<SER>(d) : d;
+                va[u] = __float2int_rn(favg * ascale[e >> 1]);
+            }
         }
     }
 #pragma unroll
@@ -1360,8 +1525,9 @@ __device__ __forceinline__ uint32_t tile_fast8(const PairArgs &A, const float4 *
             pairs_group8<MODE, NEED_AVG, NEED_W, OWN, SER, kGroup>(A, sjhi, sjlo, lut_add, ascale, k0, jb, i, xi, yi, zi,
                                                                    xil, yil, zil, wis, cnt_s, slowbits);
     } else {
-        for (int k = 0; k < nj; k++)
-            pairs_group8<MODE, NEED_AVG, NEED_W, OWN, SER, 1>(A, sjhi, sjlo, lut_add, ascale, k, jb, i, xi, yi, zi, xil,
+        // a partial tile, padded to a multiple of 4 points
+        for (int k = 0; k < nj; k += 4)
+            pairs_group8<MODE, NEED_AVG, NEED_W, OWN, SER, 4>(A, sjhi, sjlo, lut_add, ascale, k, jb, i, xi, yi, zi, xil,
                                                               yil, zil, wis, cnt_s, slowbits);
     }
     return slowbits;
@@ -1462,7 +1628,8 @@ __device__ __noinline__ void slow_batch(const PairArgs &A, const double *se, con
 }
 
 template <int MODE, bool NEED_AVG, bool NEED_W, bool LUT8>
-__global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pairs_f32(PairArgs A, SmemLayout SL)
+__global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_PAIR_MIN_BLOCKS)
+    k_pairs_f32(PairArgs A, SmemLayout SL)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1550,17 +1717,43 @@ __global__ void __launch_bounds__(CF_PAIR_MAX_THREADS, CF_PAIR_MIN_BLOCKS) k_pai
         const float ax = xi + xil, ay = yi + yil, az = zi + zil;  // survey modes: the i point from the observer
         for (uint32_t jb = T.j_begin; jb < T.j_end; jb += 32) {
             int nj = (int)min(32u, T.j_end - jb);
-            if (lane < nj) {
-                sjhi[lane] = A.hi2[jb + lane];
-                if (kLo) sjlo[lane] = A.lo2[jb + lane];
-            } else if (nj > kPadMin) {
-                // pad a partial tile with far-away points and run it fully unrolled: q overflows to
-                // +inf (the reject bucket, zero weight) against valid i points and against the
-                // +1e30 stand-in of lanes without an i point alike
-                sjhi[lane] = make_float4(-1e30f, -1e30f, -1e30f, 0.f);
-                if (kLo) sjlo[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if constexpr (LUT8) {
+                // byte table: the stage holds x[32] | y[32] | z[32] | w[32] (and the lo parts
+                // x[32] | y[32] | z[32]) so that one 16-byte shared load broadcasts a coordinate of
+                // four j points; a partial tile is padded to 32 points above kPadMin and to a
+                // multiple of 4 otherwise, with far-away points (q' = cap: the reject entry)
+                const int njp = nj > kPadMin ? 32 : ((nj + 3) & ~3);
+                float *S = (float *)sjhi, *SL8 = (float *)sjlo;
+                if (lane < njp) {
+                    float4 p = make_float4(-1e30f, -1e30f, -1e30f, 0.f), pl = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (lane < nj) {
+                        p = A.hi2[jb + lane];
+                        if (kLo) pl = A.lo2[jb + lane];
+                    }
+                    S[lane] = p.x;
+                    S[32 + lane] = p.y;
+                    S[64 + lane] = p.z;
+                    if (NEED_W) S[96 + lane] = p.w;
+                    if (kLo) {
+                        SL8[lane] = pl.x;
+                        SL8[32 + lane] = pl.y;
+                        SL8[64 + lane] = pl.z;
+                    }
+                }
+                nj = njp;
+            } else {
+                if (lane < nj) {
+                    sjhi[lane] = A.hi2[jb + lane];
+                    if (kLo) sjlo[lane] = A.lo2[jb + lane];
+                } else if (nj > kPadMin) {
+                    // pad a partial tile with far-away points and run it fully unrolled: q overflows
+                    // to +inf (the reject bucket, zero weight) against valid i points and against the
+                    // +1e30 stand-in of lanes without an i point alike
+                    sjhi[lane] = make_float4(-1e30f, -1e30f, -1e30f, 0.f);
+                    if (kLo) sjlo[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+                if (nj > kPadMin) nj = 32;
             }
-            if (nj > kPadMin) nj = 32;
             __syncwarp();
             const float wi_s = pi.w * A.w_scale_f;
             uint32_t slowbits;
@@ -1708,6 +1901,8 @@ __global__ void __launch_bounds__(256) k_pairs_f64(PairArgs A, SmemLayout SL)
                     const double4_32a pj = sj[k];
                     double avg_term = 0.0;
                     int bin;
+                    // points outside the reference lattice: only pairs of linked reference cells
+                    if (A.ref_links && !ref_linked(A, rci, sro[k].x, mx, my, mz)) continue;
                     if (MODE != MODE_THETA && A.autocorr && wrapped &&
                         (sro[k].x > rci || (sro[k].x == rci && (pj.z < pi.z || (pj.z == pi.z && sro[k].y < ori))))) {
                         bin = ref_eval<MODE>(A, se, pj.x, pj.y, pj.z, pi.x, pi.y, pi.z, ox, oy, oz, &avg_term);
@@ -1806,7 +2001,7 @@ static int ensure_host(HostBuf &b, size_t bytes)
 struct SetBufs {
     DevBuf raw[4];  // device copies of x, y, z, w as given (float or double)
     const void *in[4];  // arrays the lattice is built from: raw[] or caller-owned device arrays
-    DevBuf cellid_u, count, fill, cell_start;
+    DevBuf cellid_u, count, fill, cell_start;  // fill: slot of every point within its cell
     DevBuf hi, lo, dbl, ro;
 };
 
@@ -1981,7 +2176,7 @@ static int engine_init(void)
     const char *lay = getenv("CF_PAIR_LAYOUT");
     int ls = 0, wp = 0;
     if (lay && sscanf(lay, "%d,%d", &ls, &wp) == 2 && (ls == 1 || ls == 4 || ls == 8 || ls == 16 || ls == 32) &&
-        (wp == 4 || wp == 8 || wp == 16)) {
+        (wp == 3 || wp == 4 || wp == 6 || wp == 8 || wp == 12 || wp == 16)) {
         g_eng.force_ls = ls;
         g_eng.force_warps = wp;
     }
@@ -2097,19 +2292,20 @@ static int build_lattice_at(Workspace &W, SetBufs &B, int64_t n, int64_t base, c
                             const T *w, const Geom &g, uint32_t ncells, unsigned long long *oob)
 {
     cudaStream_t st = g_eng.stream;
-    // per-cell occupancy and fill counters side by side (one memset)
-    if (ensure(B.count, sizeof(uint32_t) * 2 * (size_t)ncells) ||
+    // per-cell occupancy; every point gets its slot within its cell from the counting atomic
+    if (ensure(B.count, sizeof(uint32_t) * (size_t)ncells) ||
         ensure(B.cell_start, sizeof(uint32_t) * ((size_t)ncells + 1)))
         return EXIT_FAILURE;
-    uint32_t *count = (uint32_t *)B.count.p, *fill = count + ncells;
-    CF_CUDA(cudaMemsetAsync(count, 0, sizeof(uint32_t) * 2 * (size_t)ncells, st));
+    uint32_t *count = (uint32_t *)B.count.p;
+    CF_CUDA(cudaMemsetAsync(count, 0, sizeof(uint32_t) * (size_t)ncells, st));
     if (n <= 0) {
         CF_CUDA(cudaMemsetAsync(B.cell_start.p, 0, sizeof(uint32_t) * ((size_t)ncells + 1), st));
         return EXIT_SUCCESS;
     }
     uint32_t *cellid_u = (uint32_t *)B.cellid_u.p + base;
+    uint32_t *rank = (uint32_t *)B.fill.p + base;
     const int grid = grid_for(n, 256);
-    k_assign<T><<<grid, 256, 0, st>>>(x, y, z, n, g, cellid_u, count, oob);
+    k_assign<T><<<grid, 256, 0, st>>>(x, y, z, n, g, cellid_u, rank, count, oob);
     g_eng.launches++;
     CF_CUDA(cudaGetLastError());
     if (scan_u32(W, count, (uint32_t *)B.cell_start.p, ncells, 0) != EXIT_SUCCESS) return EXIT_FAILURE;
@@ -2119,7 +2315,7 @@ static int build_lattice_at(Workspace &W, SetBufs &B, int64_t n, int64_t base, c
     L.dbl = (double4_32a *)B.dbl.p + base;
     L.ro = (int2 *)B.ro.p + base;
     L.cell_start = (uint32_t *)B.cell_start.p;
-    k_scatter<T><<<grid, 256, 0, st>>>(x, y, z, w, n, g, cellid_u, (const uint32_t *)B.cell_start.p, fill, L);
+    k_scatter<T><<<grid, 256, 0, st>>>(x, y, z, w, n, g, cellid_u, rank, (const uint32_t *)B.cell_start.p, L);
     g_eng.launches++;
     CF_CUDA(cudaGetLastError());
     return EXIT_SUCCESS;
@@ -2127,7 +2323,8 @@ static int build_lattice_at(Workspace &W, SetBufs &B, int64_t n, int64_t base, c
 
 static int ensure_points(SetBufs &B, int64_t n)
 {
-    if (ensure(B.cellid_u, sizeof(uint32_t) * n) || ensure(B.hi, sizeof(float4) * n) || ensure(B.lo, sizeof(float4) * n) ||
+    if (ensure(B.cellid_u, sizeof(uint32_t) * n) || ensure(B.fill, sizeof(uint32_t) * n) ||
+        ensure(B.hi, sizeof(float4) * n) || ensure(B.lo, sizeof(float4) * n) ||
         ensure(B.dbl, sizeof(double4_32a) * n) || ensure(B.ro, sizeof(int2) * n))
         return EXIT_FAILURE;
     return EXIT_SUCCESS;
@@ -2225,7 +2422,8 @@ static SmemLayout choose_layout(int mode, bool f64, bool avg, bool w, int nedges
 {
     const bool dz = (mode == MODE_RPPI || mode == MODE_WP || mode == MODE_SMU || mode_is_mock(mode));
     const bool los = avg || mode_is_mock(mode);
-    if (!f64 && g_eng.force_ls > 0 && g_eng.force_warps > 0) {
+    const bool forced = g_eng.force_ls > 0 && g_eng.force_warps > 0 && 32 * g_eng.force_warps <= pair_max_threads(mode, avg, w);
+    if (!f64 && forced) {
         const SmemLayout c = smem_layout(nedges, nbins, g_eng.force_warps, f64, lut_n, g_eng.force_ls, avg, w, dz, los);
         if (c.total <= 220 * 1024) return c;
     }
@@ -2234,7 +2432,7 @@ static SmemLayout choose_layout(int mode, bool f64, bool avg, bool w, int nedges
     SmemLayout SL = smem_layout(nedges, nbins, 8, f64, lut_n, 1, avg, w, dz, los);
     double best = -1.0;
     const int lstrides[5] = {32, 16, 8, 4, 1};
-    const int max_warps = f64 ? 8 : CF_PAIR_MAX_THREADS / 32;
+    const int max_warps = f64 ? 8 : pair_max_threads(mode, avg, w) / 32;
     const int wopts[3] = {max_warps, max_warps / 2, max_warps / 4};
     for (int li = 0; li < 5; li++) {
         for (int wi = 0; wi < 3; wi++) {
@@ -2697,7 +2895,12 @@ static int gpu_geometry(const cf_job *J, const cf_geometry &geo, const double lo
         const bool per = geo.periodic[a] && geo.wrap[a] > 0.0;
         double ext = hi[a] - lo[a];
         if (per) {
-            if (ext > geo.wrap[a] * (1.0 + 1e-12)) {
+            // Points spanning more than the period: the reference counts them, but its cells at the
+            // two ends of the axis then overlap across the periodic boundary, and its neighbour
+            // pruning by cell bounds (utils/gridlink_impl.c.src:522-560, the min_dx / max_dz
+            // tests of the pair kernels) drops some pairs in range there; that pruning is not
+            // reproduced, so the call fails.
+            if (ext > geo.wrap[a]) {
                 CF_FAIL("points span %g along axis %d, more than the periodic length %g", ext, a, geo.wrap[a]);
             }
             ext = geo.wrap[a];
@@ -2989,7 +3192,17 @@ static int run_locked(cf_job *J, cf_hist *H)
 
     // ---- lattices ----
     const bool w_exact = need_w && weights_wide(wmax, wmin);
-    const bool f64 = g_eng.precision == CF_PRECISION_FP64 || !has_f32_path(mode) || w_exact;
+    // points outside the reference lattice on a periodic axis (xi / wp lattice the box [0, L) and
+    // take points up to a cell past its edges into the edge cells): the reference's cell-pair list
+    // can leave out pairs in range across the periodic boundary, and every pair then takes the FP64
+    // kernel, which applies the reference's cell links
+    bool ref_links = false;
+    for (int a = 0; a < 3; a++) {
+        if (!(geo.periodic[a] && geo.wrap[a] > 0.0)) continue;
+        if (J->rule.kind == CF_REF_BOX && (lo[a] < geo.ref_min[a] || hi[a] > geo.ref_min[a] + geo.wrap[a]))
+            ref_links = true;
+    }
+    const bool f64 = g_eng.precision == CF_PRECISION_FP64 || !has_f32_path(mode) || w_exact || ref_links;
     g.write_lo = (J->need_avg != 0 || mode_is_mock(mode)) ? 1 : 0;
     if (ensure(W.res, res_bytes(nbins)) != EXIT_SUCCESS) return EXIT_FAILURE;
     const ResView R = res_view(W.res.p, nbins);
@@ -3006,29 +3219,34 @@ static int run_locked(cf_job *J, cf_hist *H)
     Tables T;
     if (build_tables(W, J, mode, nbins, need_w, delta, &T) != EXIT_SUCCESS) return EXIT_FAILURE;
 
+    // ---- neighbour-search geometry ----
+    TaskGeom G;
+    if (task_geometry(J, geo, g, lo, hi, autocorr, mode, G) != EXIT_SUCCESS) return EXIT_FAILURE;
+    G.error = R.flags + 2;
+    const int gap = chunk_gap(G, n1, ncols);
+
     // ---- chunks: fixed slot range (empty slots hold 0 points), no host wait ----
-    const uint32_t max_chunks = (uint32_t)((n1 + kChunk - 1) / kChunk + ncols);
+    const uint64_t slots = chunk_slots((uint64_t)n1, ncols, g.n[2], gap);
+    if (slots > 0xffffffffull) CF_FAIL("too many chunks (%llu)", (unsigned long long)slots);
+    const uint32_t max_chunks = (uint32_t)slots;
     if (ensure(W.chunk_cnt, sizeof(uint32_t) * ncols) || ensure(W.chunk_off, sizeof(uint32_t) * ((size_t)ncols + 1)) ||
         ensure(W.chunk_begin, sizeof(uint32_t) * max_chunks) || ensure(W.chunk_info, sizeof(uint2) * max_chunks))
         return EXIT_FAILURE;
     CF_CUDA(cudaMemsetAsync(W.chunk_info.p, 0, sizeof(uint2) * max_chunks, st));
-    k_col_chunks<<<(ncols + 255) / 256, 256, 0, st>>>((const uint32_t *)S1.cell_start.p, (int)ncols, g.n[2],
-                                                      (uint32_t *)W.chunk_cnt.p);
+    k_col_chunks<<<(ncols + 7) / 8, 256, 0, st>>>((const uint32_t *)S1.cell_start.p, (int)ncols, g.n[2], gap,
+                                                  (uint32_t *)W.chunk_cnt.p);
     g_eng.launches++;
     CF_CUDA(cudaGetLastError());
     if (scan_u32(W, (const uint32_t *)W.chunk_cnt.p, (uint32_t *)W.chunk_off.p, ncols, 0) != EXIT_SUCCESS)
         return EXIT_FAILURE;
-    k_chunk_emit<<<(ncols + 7) / 8, 256, 0, st>>>((const uint32_t *)S1.cell_start.p, (int)ncols, g.n[2],
-                                                      (const uint32_t *)W.chunk_off.p,
+    k_chunk_emit<<<(ncols + 7) / 8, 256, 0, st>>>((const uint32_t *)S1.cell_start.p, (int)ncols, g.n[2], gap,
+                                                      (const uint32_t *)W.chunk_off.p, max_chunks, G.error,
                                                       (uint32_t *)W.chunk_begin.p, (uint2 *)W.chunk_info.p,
                                                       0u, nullptr, 0);
     g_eng.launches++;
     CF_CUDA(cudaGetLastError());
 
     // ---- tasks: listed on the device in one pass into a buffer sized from earlier calls ----
-    TaskGeom G;
-    if (task_geometry(J, geo, g, lo, hi, autocorr, mode, G) != EXIT_SUCCESS) return EXIT_FAILURE;
-    G.error = R.flags + 2;
     // capacity: what this lattice needed last time, else about one task per neighbour column
     const size_t guess = (size_t)max_chunks * (2 * G.reach_x + 1) * (2 * G.reach_y + 1) * 5 / 4 + 1024;
     size_t cap = W.tasks.cap / sizeof(Task);
@@ -3052,6 +3270,11 @@ static int run_locked(cf_job *J, cf_hist *H)
     A.ntask_dev = R.flags + 1;  // tasks listed (capped by the capacity in the kernel)
     pair_constants(A, J, mode, nbins, autocorr, G, geo, g, delta, T, wmax, W);
     A.w_exact = w_exact ? 1 : 0;
+    A.ref_links = ref_links ? 1 : 0;
+    for (int a = 0; a < 3; a++) {
+        A.ref_n[a] = g.ref_n[a];
+        A.ref_reach[a] = geo.refine_used[a];
+    }
     A.g_cnt = R.cnt;
     A.g_avg = R.avg;
     A.g_w = R.w;
@@ -3089,6 +3312,7 @@ static int run_locked(cf_job *J, cf_hist *H)
         CF_CUDA(cudaStreamSynchronize(st));
         CF_CHECK_INTERRUPT();
         if (*Rh.oob > 0) CF_FAIL("%llu particles are out of bounds. Check periodic wrapping?", *Rh.oob);
+        if (Rh.flags[2] & 2u) CF_FAIL("internal: the chunks outgrew their slots");
         if (Rh.flags[2]) CF_FAIL("internal: neighbour search needed a periodic image beyond +-1");
         if (!Rh.flags[3]) break;
         // the work list outgrew the buffer: size it exactly and run the pair kernel again
@@ -3172,6 +3396,7 @@ struct BatchPlan {
     uint32_t task_cap = 0, ntasks = 0;
     Geom g;
     TaskGeom G;
+    int gap = -1;  // z-slab gap that splits the catalogues' chunks (chunk_gap)
     Tables T;
     PairArgs A;
     cf_geometry geo;
@@ -3212,14 +3437,15 @@ static int batch_lattices(BatchPlan &P)
                                 (const T *)P.z1[b], w, g1, P.ncells, oob) != EXIT_SUCCESS)
             return EXIT_FAILURE;
         if (P.n1[b] == 0) continue;
-        k_col_chunks<<<(P.ncols + 255) / 256, 256, 0, st>>>((const uint32_t *)W.set[0].cell_start.p, (int)P.ncols, nz,
-                                                            (uint32_t *)W.chunk_cnt.p);
+        k_col_chunks<<<(P.ncols + 7) / 8, 256, 0, st>>>((const uint32_t *)W.set[0].cell_start.p, (int)P.ncols, nz,
+                                                        P.gap, (uint32_t *)W.chunk_cnt.p);
         g_eng.launches++;
         CF_CUDA(cudaGetLastError());
         if (scan_u32(W, (const uint32_t *)W.chunk_cnt.p, (uint32_t *)W.chunk_off.p, P.ncols, 0) != EXIT_SUCCESS)
             return EXIT_FAILURE;
         k_chunk_emit<<<(P.ncols + 7) / 8, 256, 0, st>>>(
-            (const uint32_t *)W.set[0].cell_start.p, (int)P.ncols, nz, (const uint32_t *)W.chunk_off.p,
+            (const uint32_t *)W.set[0].cell_start.p, (int)P.ncols, nz, P.gap, (const uint32_t *)W.chunk_off.p,
+            P.cbase[b + 1] - P.cbase[b], P.G.error,
             (uint32_t *)W.chunk_begin.p + P.cbase[b], (uint2 *)W.chunk_info.p + P.cbase[b], (uint32_t)P.pbase[b],
             (uint16_t *)W.chunk_cat.p + P.cbase[b], (uint16_t)b);
         g_eng.launches++;
@@ -3290,6 +3516,7 @@ static int batch_collect(BatchPlan &P, cf_hist *H)
     if (*Rh.oob > 0) CF_FAIL("%llu particles are out of bounds. Check periodic wrapping?", *Rh.oob);
     if (*Rh.extent > 0)
         CF_FAIL("%llu points or weights left the box / weight range the batch was planned for; plan again", *Rh.extent);
+    if (Rh.flags[2] & 2u) CF_FAIL("internal: the chunks outgrew their slots");
     if (Rh.flags[2]) CF_FAIL("internal: neighbour search needed a periodic image beyond +-1");
     if (Rh.flags[3]) CF_FAIL("the batch work list outgrew its plan (catalogues changed since planning); plan again");
     for (int b = 0; b < P.nbatch; b++) {
@@ -3448,8 +3675,19 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
         g_eng.last.num_cells = (int)P->ncells;
 
         // ---- buffers ----
-        for (int b = 0; b < nbatch; b++)
-            P->cbase[b + 1] = P->cbase[b] + (uint32_t)((P->n1[b] + kChunk - 1) / kChunk + (P->n1[b] > 0 ? P->ncols : 0));
+        if ((rc = task_geometry(&P->J, P->geo, P->g, glo, ghi, false, MODE_R3, P->G)) != EXIT_SUCCESS) break;
+        P->gap = chunk_gap(P->G, P->J.n1, P->ncols);
+        uint64_t slots = 0;
+        for (int b = 0; b < nbatch; b++) {
+            slots += P->n1[b] > 0 ? chunk_slots((uint64_t)P->n1[b], P->ncols, P->g.n[2], P->gap) : 0;
+            if (slots > 0xfffffff0ull) break;
+            P->cbase[b + 1] = (uint32_t)slots;
+        }
+        if (slots > 0xfffffff0ull) {
+            fprintf(stderr, "corrfunc_gb300: too many chunks in the batch\n");
+            rc = EXIT_FAILURE;
+            break;
+        }
         P->total_slots = P->cbase[nbatch];
         const size_t nb = (size_t)nbatch * P->nbins;
         if ((rc = ensure_points(W.set[0], P->total1 > 0 ? P->total1 : 1)) != EXIT_SUCCESS ||
@@ -3462,7 +3700,6 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
             (rc = ensure(W.chunk_cat, sizeof(uint16_t) * ((size_t)P->total_slots + 1))) != EXIT_SUCCESS ||
             (rc = ensure_host(W.h_hist, res_bytes(nb))) != EXIT_SUCCESS)
             break;
-        if ((rc = task_geometry(&P->J, P->geo, P->g, glo, ghi, false, MODE_R3, P->G)) != EXIT_SUCCESS) break;
         P->nentries = P->total_slots * (uint32_t)((2 * P->G.reach_x + 1) * (2 * P->G.reach_y + 1));
         if ((rc = ensure(W.ntask, sizeof(uint32_t) * ((size_t)P->nentries + 1))) != EXIT_SUCCESS ||
             (rc = ensure(W.task_off, sizeof(uint32_t) * ((size_t)P->nentries + 2))) != EXIT_SUCCESS)
@@ -3533,7 +3770,8 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
         // ---- tuner: time the FP32 layouts that fit, keep the fastest ----
         if (tune && g_eng.precision == CF_PRECISION_FP32_REFINE && !P->w_exact) {
             const int cand_ls[3] = {32, 16, 8};
-            const int cand_w[3] = {16, 8, 4};
+            const int mw = pair_max_threads(MODE_R3, P->J.need_avg != 0, P->need_w) / 32;
+            const int cand_w[3] = {mw, mw / 2, mw / 4};
             float best = 1e30f;
             int best_ls = 0, best_w = 0;
             for (int li = 0; li < 3 && rc == EXIT_SUCCESS; li++) {
