@@ -83,6 +83,7 @@ struct PairArgs {
     // (flag: the bucket holds a guard and its pairs take the exact path).
     int lut8;
     float q_bias, q_cap;        // b, cap
+    float q_cap2;               // cap of lanes 16-31: the bucket after cap (entry: the second trash row)
     uint32_t lut8_base;         // bits(b) >> lut_shift (bucket 0)
     uint32_t half_row;          // half the bytes of a histogram row (entry * half_row = row offset)
     uint32_t trash_e;           // entry of a rejected pair (2 * trash row)

@@ -72,13 +72,19 @@ constexpr int kZFine = CF_Z_SLABS;
 #ifndef CF_PAIR_MIN_BLOCKS
 #define CF_PAIR_MIN_BLOCKS 2
 #endif
-// DD(r) / xi with weights or separation averages (not both): 2 x 384 threads (up to 85
-// registers, 24 warps per SM) -- measured 4 % faster on the weighted 2M x 2M cross-correlation and
-// 8 % on the 300k auto-correlation with averages than 2 x 512, which spills at 64 registers; plain
-// counts (4 % faster) and counts with both sums (6 %) keep 2 x 512
+// DD(r) / xi / DDtheta with weights or separation averages (not both): 2 x 384 threads (up to 85
+// registers, 24 warps per SM) -- measured 4 % faster on the weighted 2M x 2M cross-correlation, 8 %
+// on the 300k auto-correlation with averages and 5 % on the 1M-point DDtheta with thetaavg than
+// 2 x 512, which spills at 64 registers; plain counts (4 % faster) and counts with both sums (6 %)
+// keep 2 x 512
+#ifndef CF_PAIR_SPLIT_THETA
+#define CF_PAIR_SPLIT_THETA 1  // 0: DDtheta keeps 2 x 512 throughout
+#endif
 constexpr int pair_max_threads(int mode, bool avg, bool w)
 {
-    return (mode == MODE_R3 && avg != w && CF_PAIR_MAX_THREADS > 384) ? 384 : CF_PAIR_MAX_THREADS;
+    return ((mode == MODE_R3 || (CF_PAIR_SPLIT_THETA && mode == MODE_THETA)) && avg != w && CF_PAIR_MAX_THREADS > 384)
+               ? 384
+               : CF_PAIR_MAX_THREADS;
 }
 // pairs whose table offsets are computed before their shared reductions are issued
 #ifndef CF_PAIR_GROUP
@@ -1432,7 +1438,7 @@ __device__ __forceinline__ void pairs_group8(const PairArgs &A, const float4 *__
                                              const float4 *__restrict__ sjlo, uint32_t lut_add,
                                              const float *__restrict__ ascale, int k0, uint32_t jb, uint32_t i, float xi,
                                              float yi, float zi, float xil, float yil, float zil, float wis,
-                                             uint32_t cnt_s, uint32_t &slowbits)
+                                             float qcap, uint32_t cnt_s, uint32_t &slowbits)
 {
     static_assert(U % 4 == 0, "the byte-table stage is read four j points at a time");
     const float *S = (const float *)sjhi, *SL8 = (const float *)sjlo;
@@ -1470,7 +1476,7 @@ __device__ __forceinline__ void pairs_group8(const PairArgs &A, const float4 *__
         for (int v = 0; v < 4; v++) {
             const int u = g + v, k = kq + v;
             const float dx = dxv[v], dy = dyv[v], dz = dzv[v];
-            const float q = fminf(qv[v], A.q_cap);
+            const float q = fminf(qv[v], qcap);
             uint32_t a, e;
             asm("mad.hi.u32 %0, %1, %2, %3;" : "=r"(a) : "r"(__float_as_uint(q)), "r"(A.lut_mul), "r"(lut_add));
             asm("ld.shared.u8 %0, [%1];" : "=r"(e) : "r"(a));
@@ -1513,7 +1519,7 @@ __device__ __forceinline__ uint32_t tile_fast8(const PairArgs &A, const float4 *
                                                const float4 *__restrict__ sjlo, uint32_t lut_add,
                                                const float *__restrict__ ascale, int nj, uint32_t jb, uint32_t i,
                                                float xi, float yi, float zi, float xil, float yil, float zil, float wis,
-                                               uint32_t cnt_s)
+                                               float qcap, uint32_t cnt_s)
 {
     uint32_t slowbits = 0;
     if (nj == 32) {
@@ -1523,12 +1529,12 @@ __device__ __forceinline__ uint32_t tile_fast8(const PairArgs &A, const float4 *
 #pragma unroll kUnroll
         for (int k0 = 0; k0 < 32; k0 += kGroup)
             pairs_group8<MODE, NEED_AVG, NEED_W, OWN, SER, kGroup>(A, sjhi, sjlo, lut_add, ascale, k0, jb, i, xi, yi, zi,
-                                                                   xil, yil, zil, wis, cnt_s, slowbits);
+                                                                   xil, yil, zil, wis, qcap, cnt_s, slowbits);
     } else {
         // a partial tile, padded to a multiple of 4 points
         for (int k = 0; k < nj; k += 4)
             pairs_group8<MODE, NEED_AVG, NEED_W, OWN, SER, 4>(A, sjhi, sjlo, lut_add, ascale, k, jb, i, xi, yi, zi, xil,
-                                                              yil, zil, wis, cnt_s, slowbits);
+                                                              yil, zil, wis, qcap, cnt_s, slowbits);
     }
     return slowbits;
 }
@@ -1650,6 +1656,11 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
     for (int k = threadIdx.x; k <= SL.lut_n; k += blockDim.x) lut[k] = A.g_lut[k];
     // byte table: entry address = mad.hi(bits(q'), 2^(32 - shift), lut_add)
     const uint32_t lut_add = (uint32_t)__cvta_generic_to_shared(lut) - A.lut8_base;
+    // byte table: lanes 16-31 clamp to a cap bucket of their own whose entry is the second trash
+    // row, so that a rejected pair of lane l and one of lane l + 16 (which share a histogram
+    // column below lane stride 32) do not reduce into the same word
+    // (plain counts, which run with private columns, keep the one cap: a register less)
+    const float qcap_l = (NEED_AVG || NEED_W) && lane >= 16 ? A.q_cap2 : A.q_cap;
     float4 *sjhi = (float4 *)(smem + SL.stage_off + SL.per_warp_stage * warp);
     float4 *sjlo = sjhi + 32;
     RefineEntry *rq = (RefineEntry *)(sjlo + 32);
@@ -1761,18 +1772,18 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
                 // byte table: pair k of nj ends at bit 32 - nj + k (shifted into bit 0 of k = 0 below)
                 if (MODE == MODE_THETA && NEED_AVG && A.theta_series) {
                     slowbits = own ? tile_fast8<MODE, NEED_AVG, NEED_W, true, true>(A, sjhi, sjlo, lut_add, h.ascale, nj,
-                                                                                  jb, i, xi, yi, zi, xil, yil, zil, wi_s,
+                                                                                  jb, i, xi, yi, zi, xil, yil, zil, wi_s, qcap_l,
                                                                                   cnt_s)
                                    : tile_fast8<MODE, NEED_AVG, NEED_W, false, true>(A, sjhi, sjlo, lut_add, h.ascale,
                                                                                    nj, jb, i, xi, yi, zi, xil, yil, zil,
-                                                                                   wi_s, cnt_s);
+                                                                                   wi_s, qcap_l, cnt_s);
                 } else {
                     slowbits = own ? tile_fast8<MODE, NEED_AVG, NEED_W, true, false>(A, sjhi, sjlo, lut_add, h.ascale,
                                                                                    nj, jb, i, xi, yi, zi, xil, yil, zil,
-                                                                                   wi_s, cnt_s)
+                                                                                   wi_s, qcap_l, cnt_s)
                                    : tile_fast8<MODE, NEED_AVG, NEED_W, false, false>(A, sjhi, sjlo, lut_add, h.ascale,
                                                                                     nj, jb, i, xi, yi, zi, xil, yil, zil,
-                                                                                    wi_s, cnt_s);
+                                                                                    wi_s, qcap_l, cnt_s);
                 }
                 slowbits >>= 32 - nj;  // pair k at bit k
             } else if (MODE == MODE_THETA && NEED_AVG && A.theta_series) {
@@ -2570,7 +2581,7 @@ struct Tables {
     size_t guard_off, ascale_off, lut_off;  // byte offsets in W.tab (edges at 0)
     // byte table (lut_n then counts 32-bit words of it, less one)
     int lut8;
-    float qbias, qcap;
+    float qbias, qcap, qcap2;
     uint32_t trash_e;
 };
 
@@ -2622,11 +2633,12 @@ static bool build_lut8(const cf_job *J, int mode, int nbins, bool need_w, double
     const int shift = 23 - lg;
     const int base = (int)(bb >> shift);
     const int nb = (int)(bt >> shift) + 1 - base;  // cap bucket: the first wholly beyond the last guard
-    if (nb + 1 > kLut8Max) return false;
-    const uint32_t bcap = (uint32_t)(base + nb) << shift;
-    float cap;
+    if (nb + 2 > kLut8Max) return false;
+    const uint32_t bcap = (uint32_t)(base + nb) << shift, bcap2 = (uint32_t)(base + nb + 1) << shift;
+    float cap, cap2;
     memcpy(&cap, &bcap, 4);
-    const int words = (nb + 1 + 3) / 4;
+    memcpy(&cap2, &bcap2, 4);
+    const int words = (nb + 2 + 3) / 4;
     // layout: a flagged entry lands half a row past the trash row, which must stay 4-byte aligned
     const int ls = choose_layout(mode, false, J->need_avg != 0, need_w, ne, nbins, words - 1).lane_stride;
     const int ew = 1 + (J->need_avg ? 2 : 0) + (need_w ? 2 : 0);
@@ -2654,9 +2666,13 @@ static bool build_lut8(const cf_job *J, int mode, int nbins, bool need_w, double
         lut_h[t] = (uint8_t)e;
     }
     for (int t = nb + 1; t < 4 * words; t++) lut_h[t] = (uint8_t)trash_e;
+    // the second cap bucket (lanes 16-31 where two lanes share a column): the second trash row
+    const bool cap_pair = ls < 32 && 2 * (nbins + 1) <= 255;
+    if (cap_pair) lut_h[nb + 1] = (uint8_t)(2 * (nbins + 1));
     T->lut8 = 1;
     T->qbias = bf;
     T->qcap = cap;
+    T->qcap2 = cap_pair ? cap2 : cap;
     T->shift = shift;
     T->base = base;
     T->lut_n = words - 1;
@@ -2706,6 +2722,7 @@ static int build_tables(Workspace &W, const cf_job *J, int mode, int nbins, bool
     T->lut8 = 0;
     T->qbias = 0.f;
     T->qcap = 0.f;
+    T->qcap2 = 0.f;
     T->trash_e = 0;
     if ((mode == MODE_R3 || mode == MODE_THETA) && nbins <= 127 && g_eng.byte_table &&
         build_lut8(J, mode, nbins, need_w, dlim, guards_h, (uint8_t *)lut_h, T)) {
@@ -3053,6 +3070,7 @@ static void pair_constants(PairArgs &A, const cf_job *J, int mode, int nbins, bo
     A.lut8_base = (uint32_t)T.base;
     A.half_row = T.row_bytes / 2;
     A.trash_e = T.trash_e;
+    A.q_cap2 = T.qcap2;
     A.g_edges = (const double *)W.tab.p;
     A.g_guard = (const float *)((const char *)W.tab.p + T.guard_off);
     A.dz_err = (float)(2.0 * delta[2]);

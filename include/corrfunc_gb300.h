@@ -455,9 +455,10 @@ int cf_reference_candidate_pairs(const int64_t ND1, void *X1, void *Y1, void *Z1
  *              the stream has drained.
  *
  * Scratch is a fixed 4 KB device array inside the library.  The first call on each device looks
- * up its address (set-up); make that first call before any stream capture begins.  The address is
- * kept for the life of the process: after the first call, neither cudaDeviceReset nor another
- * context made current on that device is supported.  Each call
+ * up its address; the address is kept for the life of the process: after the first call, neither
+ * cudaDeviceReset nor another context made current on that device is supported.  No call may be
+ * made while its stream is being captured into a CUDA graph: every call copies its edges from a
+ * host buffer and synchronises the stream, which a capture does not allow.  Each call
  * writes the squared edges and zeros over the accumulators itself, so nothing has to be cleared
  * beforehand.  All calls on one device share that array: calls that overlap in time (two host
  * threads, or two streams) race and corrupt each other's counts, so serialise them.  Cost grows
