@@ -59,7 +59,7 @@ WORKLOAD = dict(WORKLOADS["cfg2"])
 FLOP_PER_PAIR = 8  # 3 FADD + 1 FMUL + 2 FFMA per 3-D separation
 # dram__bytes_read.sum + dram__bytes_write.sum of one FP32 pair-kernel launch per workload, from an
 # ncu capture of this kernel on that workload (a recorded constant, not measured by this script)
-PAIR_KERNEL_TRAFFIC_BYTES = {"cfg2": 220_196_096 + 3_340_544, "northstar": 54_269_184 + 2_131_200}
+PAIR_KERNEL_TRAFFIC_BYTES = {"cfg2": 823_469_824 + 20_716_800, "northstar": 55_299_584 + 2_311_424}
 TRAFFIC_SOURCE = ("ncu capture of the pair kernel on this workload (dram__bytes_read.sum + dram__bytes_write.sum "
                   "per launch): a recorded constant, not measured in this run")
 
