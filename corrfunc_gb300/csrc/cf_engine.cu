@@ -497,7 +497,8 @@ __device__ __forceinline__ unsigned long long abs_okey(float v) { return abs_oke
 // survey modes) is written only when set.
 template <typename T>
 __global__ void k_scatter(const T *x, const T *y, const T *z, const T *w, int64_t n, Geom g,
-                          const uint32_t *cellid, const uint32_t *rank, const uint32_t *cell_start, Lattice L)
+                          const uint32_t *cellid, const uint32_t *rank, const uint32_t *cell_start, Lattice L,
+                          int ro_cat)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t c = cellid[i];
@@ -520,10 +521,14 @@ __global__ void k_scatter(const T *x, const T *y, const T *z, const T *w, int64_
         L.hi[pos] = make_float4(h[0], h[1], h[2], (float)wv);
         if (L.lo) L.lo[pos] = make_float4(l[0], l[1], l[2], 0.f);
         L.dbl[pos] = make_double4_32a((double)p[0], (double)p[1], (double)p[2], (double)wv);
-        int r[3];
+        if (ro_cat >= 0) {
+            L.ro[pos] = make_int2(ro_cat, (int)i);  // merged batch lattice: the catalogue instead
+        } else {
+            int r[3];
 #pragma unroll
-        for (int a = 0; a < 3; a++) r[a] = ref_axis_cell(p[a], X[a], g, a);
-        L.ro[pos] = make_int2((r[0] * g.ref_n[1] + r[1]) * g.ref_n[2] + r[2], (int)i);
+            for (int a = 0; a < 3; a++) r[a] = ref_axis_cell(p[a], X[a], g, a);
+            L.ro[pos] = make_int2((r[0] * g.ref_n[1] + r[1]) * g.ref_n[2] + r[2], (int)i);
+        }
     }
 }
 
@@ -1571,12 +1576,15 @@ __device__ __forceinline__ uint32_t tile_fast(const PairArgs &A, const float4 *_
 }
 
 // Dense FP64 re-evaluation of up to 32 queued pairs (one per lane).
+// (col_base >= 0: every pair goes to the column of its own i point, r.i - col_base, instead of the
+// processing lane's column hl -- counts whose lanes belong to different catalogues)
 template <int MODE, bool NEED_AVG, bool NEED_W>
 __device__ __noinline__ void refine_batch(const PairArgs &A, const double *se, const RefineEntry *q, int count,
-                                          WarpHist h, int hl, int lane)
+                                          WarpHist h, int hl, int lane, int col_base = -1)
 {
     if (lane < count) {
         const RefineEntry r = q[lane];
+        if (col_base >= 0) hl = (int)(r.i - (uint32_t)col_base);
         const int mx = (int)((r.meta >> 8) & 3u) - 1, my = (int)((r.meta >> 10) & 3u) - 1,
                   mz = (int)((r.meta >> 12) & 3u) - 1;
         double davg = 0.0, dw = 0.0;
@@ -1594,10 +1602,12 @@ __device__ __noinline__ void refine_batch(const PairArgs &A, const double *se, c
 template <int MODE, bool NEED_AVG, bool NEED_W, bool LUT8>
 __device__ __noinline__ void slow_batch(const PairArgs &A, const double *se, const float *glo, const float *ghi,
                                         const RefineEntry *sq, int count, RefineEntry *rq, int *rq_count, WarpHist h,
-                                        int hl, int lane, unsigned long long *refined)
+                                        int hl, int lane, unsigned long long *refined, int col_base = -1)
 {
+    const int hl0 = hl;
     if (lane < count) {
         const RefineEntry e = sq[lane];
+        if (col_base >= 0) hl = (int)(e.i - (uint32_t)col_base);
         const int mx = (int)((e.meta >> 8) & 3u) - 1, my = (int)((e.meta >> 10) & 3u) - 1,
                   mz = (int)((e.meta >> 12) & 3u) - 1;
         const float4 pi = A.hi1[e.i];
@@ -1627,7 +1637,7 @@ __device__ __noinline__ void slow_batch(const PairArgs &A, const double *se, con
     __syncwarp();
     const int cnt = *rq_count;
     if (cnt >= 32) {
-        refine_batch<MODE, NEED_AVG, NEED_W>(A, se, rq + (cnt - 32), 32, h, hl, lane);
+        refine_batch<MODE, NEED_AVG, NEED_W>(A, se, rq + (cnt - 32), 32, h, hl0, lane, col_base);
         if (lane == 0) *rq_count = cnt - 32;
         __syncwarp();
     }
@@ -1839,6 +1849,226 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
     const int rest = *rq_count;
     if (rest > 0) refine_batch<MODE, NEED_AVG, NEED_W>(A, se, rq, rest, h, hl, lane);
     flush_hist<NEED_AVG, NEED_W>(A, h, lane, cur_cat);
+    for (int off = 16; off; off >>= 1) refined += __shfl_down_sync(0xffffffffu, refined, off);
+    if (lane == 0) {
+        atomicAdd(&A.g_stats[0], (unsigned long long)evaluated);
+        atomicAdd(&A.g_stats[1], refined);
+        atomicAdd(&A.g_stats[2], queued);
+    }
+}
+
+// Flush of a warp histogram whose lanes count for different catalogues (private columns, lane
+// stride 32): lane l moves its own column into catalogue cat's sums and zeroes it.
+template <bool NEED_AVG, bool NEED_W>
+__device__ __forceinline__ void flush_lanes(const PairArgs &A, WarpHist h, int lane, uint32_t cat)
+{
+    __syncwarp();
+    unsigned long long *g_cnt = A.g_cnt + (size_t)cat * A.nbins;
+    double *g_avg = A.g_avg + (size_t)cat * A.nbins;
+    double *g_w = A.g_w + (size_t)cat * A.nbins;
+    for (int b = 0; b < A.nbins; b++) {
+        uint32_t *e = h.e + (size_t)(b * 32 + lane) * h.ew;
+        const uint32_t c = e[0];
+        if (c == 0) continue;  // no pair, so no sums either
+        e[0] = 0;
+        atomicAdd(&g_cnt[b], (unsigned long long)c);
+        if (NEED_AVG) {
+            uint32_t *s = e + avg_word<NEED_AVG>();
+            const long long va = (long long)(int)s[0] * 65536ll + (long long)s[1];
+            s[0] = 0;
+            s[1] = 0;
+            if (va) atomicAdd(&g_avg[b], (double)va / (double)h.ascale[b / A.rbin_div]);
+        }
+        if (NEED_W) {
+            uint32_t *s = e + w_word<NEED_AVG>();
+            const long long vw = (long long)(int)s[0] * 65536ll + (long long)s[1];
+            s[0] = 0;
+            s[1] = 0;
+            const double v = (double)vw * A.w_unscale;
+            if (v != 0.0) atomicAdd(&g_w[b], v);
+        }
+    }
+    __syncwarp();
+}
+
+// Batched cross-correlations on one merged set-1 lattice (every catalogue's points sorted
+// together by cell; ro1[i].x holds the catalogue of point i): a warp takes one chunk -- 32
+// consecutive points of a column, from any catalogues -- and walks its neighbour columns itself
+// (the ranges chunk_col_tasks would list), so the chunk's lanes keep their points, and with them
+// their catalogues, until the chunk is done.  Every lane owns a histogram column (lane stride 32)
+// that it flushes into its catalogue's sums.  Byte-table DD(r) only.
+template <bool NEED_AVG, bool NEED_W>
+__global__ void __launch_bounds__(pair_max_threads(MODE_R3, NEED_AVG, NEED_W), CF_PAIR_MIN_BLOCKS)
+    k_pairs_chunks(PairArgs A, SmemLayout SL, TaskGeom G, const uint32_t *chunk_begin, const uint2 *chunk_info,
+                   const uint32_t *cs2, uint32_t nchunk)
+{
+    constexpr int MODE = MODE_R3;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double *se = (double *)(smem + SL.edges_off);
+    float *glo = (float *)(smem + SL.guard_off);
+    float *ghi = glo + A.nedges;
+    uint32_t *lut = (uint32_t *)(smem + SL.lut_off);
+    float *asc = (float *)(smem + SL.ascale_off);
+    for (int k = threadIdx.x; k < A.nedges; k += blockDim.x) {
+        se[k] = A.g_edges[k];
+        glo[k] = A.g_guard[k];
+        ghi[k] = A.g_guard[A.nedges + k];
+        asc[k] = A.g_ascale[k];
+    }
+    if (threadIdx.x < 2) asc[A.nedges + threadIdx.x] = 0.f;
+    for (int k = threadIdx.x; k <= SL.lut_n; k += blockDim.x) lut[k] = A.g_lut[k];
+    const uint32_t lut_add = (uint32_t)__cvta_generic_to_shared(lut) - A.lut8_base;
+    float4 *sjhi = (float4 *)(smem + SL.stage_off + SL.per_warp_stage * warp);
+    float4 *sjlo = sjhi + 32;
+    RefineEntry *rq = (RefineEntry *)(sjlo + 32);
+    RefineEntry *sq = rq + kRefineQueue;
+    int *rq_count = (int *)(sq + kSlowQueue);
+    int sq_n = 0;
+    WarpHist h = warp_hist(smem, SL, warp);
+    zero_hist(h, SL, lane);
+    if (lane == 0) *rq_count = 0;
+    const int hl = lane;  // lane stride 32: private columns
+    const uint32_t cnt_s = (uint32_t)__cvta_generic_to_shared(h.e) + 4u * h.ew * hl;
+    __syncthreads();
+    uint64_t evaluated = 0;
+    unsigned long long refined = 0, queued = 0;
+    uint32_t col_terms = 0;
+    const uint32_t tile_terms = 32u + 64u;
+    const int nyc = 2 * G.reach_y + 1, ncoff = (2 * G.reach_x + 1) * nyc;
+    const int nz = G.nz;
+
+    while (true) {
+        uint32_t t = 0;
+        if (lane == 0) t = atomicAdd(A.task_counter, 1u);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= nchunk) break;
+        const uint2 info = chunk_info[t];
+        const int icount = (int)(info.x & 63u);
+        if (icount == 0) continue;
+        const uint32_t ib = chunk_begin[t];
+        const uint32_t i = ib + lane;
+        const bool ivalid = lane < icount;
+        const float4 pi = ivalid ? A.hi1[i] : make_float4(1e30f, 1e30f, 1e30f, 0.f);
+        float4 pl = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (NEED_AVG && ivalid) pl = A.lo1[i];
+        const uint32_t cat = ivalid ? (uint32_t)A.ro1[i].x : 0u;
+        const float wi_s = pi.w * A.w_scale_f;
+        const int a = (int)((info.x >> 6) & 4095u), b = (int)((info.x >> 18) & 4095u);
+        const int col = (int)info.y, ix = col / G.ny, iy = col % G.ny;
+        for (int c = 0; c < ncoff; c++) {
+            const int dx = c / nyc - G.reach_x, dy = c % nyc - G.reach_y;
+            const int wz = G.ntab ? (int)G.wz_tab[c] : column_wz(G, dx, dy);
+            if (wz < 0) continue;
+            const int ux = ix + dx, uy = iy + dy;
+            int mx = 0, cx = ux, my = 0, cy = uy;
+            if (G.periodic[0]) {
+                mx = floordiv(ux, G.nx);
+                cx = ux - mx * G.nx;
+            } else if (ux < 0 || ux >= G.nx) {
+                continue;
+            }
+            if (G.periodic[1]) {
+                my = floordiv(uy, G.ny);
+                cy = uy - my * G.ny;
+            } else if (uy < 0 || uy >= G.ny) {
+                continue;
+            }
+            const int klo = a - wz, khi = b + wz;
+            const int mlo = G.periodic[2] ? floordiv(klo, nz) : 0, mhi = G.periodic[2] ? floordiv(khi, nz) : 0;
+            if (mx < -1 || mx > 1 || my < -1 || my > 1 || mlo < -1 || mhi > 1) {
+                if (G.error && lane == 0) atomicOr(G.error, 1u);
+                continue;
+            }
+            const uint32_t *cs = cs2 + (uint32_t)(cx * G.ny + cy) * nz;
+            for (int mz = mlo; mz <= mhi; mz++) {
+                int s0 = klo - mz * nz, s1 = khi - mz * nz;
+                s0 = s0 < 0 ? 0 : s0;
+                s1 = s1 > nz - 1 ? nz - 1 : s1;
+                if (s0 > s1) continue;
+                const uint32_t jbeg = cs[s0], jend = cs[s1 + 1];
+                if (jend <= jbeg) continue;
+                // j is shifted by the image offset o; equivalently shift i by -o (exact on the grid)
+                const float xi = pi.x - A.ohi[0][mx + 1], yi = pi.y - A.ohi[1][my + 1], zi = pi.z - A.ohi[2][mz + 1];
+                float xil = 0.f, yil = 0.f, zil = 0.f;
+                if (NEED_AVG) {
+                    xil = pl.x - A.olo[0][mx + 1];
+                    yil = pl.y - A.olo[1][my + 1];
+                    zil = pl.z - A.olo[2][mz + 1];
+                }
+                const uint32_t meta = task_meta(1, mx, my, mz, 0);
+                for (uint32_t jb = jbeg; jb < jend; jb += 32) {
+                    int nj = (int)min(32u, jend - jb);
+                    const int njp = nj > kPadMin ? 32 : ((nj + 3) & ~3);
+                    float *S = (float *)sjhi, *SL8 = (float *)sjlo;
+                    if (lane < njp) {
+                        float4 p = make_float4(-1e30f, -1e30f, -1e30f, 0.f), q = make_float4(0.f, 0.f, 0.f, 0.f);
+                        if (lane < nj) {
+                            p = A.hi2[jb + lane];
+                            if (NEED_AVG) q = A.lo2[jb + lane];
+                        }
+                        S[lane] = p.x;
+                        S[32 + lane] = p.y;
+                        S[64 + lane] = p.z;
+                        if (NEED_W) S[96 + lane] = p.w;
+                        if (NEED_AVG) {
+                            SL8[lane] = q.x;
+                            SL8[32 + lane] = q.y;
+                            SL8[64 + lane] = q.z;
+                        }
+                    }
+                    nj = njp;
+                    __syncwarp();
+                    uint32_t slowbits = tile_fast8<MODE, NEED_AVG, NEED_W, false, false>(
+                        A, sjhi, sjlo, lut_add, h.ascale, nj, jb, i, xi, yi, zi, xil, yil, zil, wi_s, A.q_cap, cnt_s);
+                    slowbits >>= 32 - nj;
+                    while (true) {
+                        const uint32_t want = __ballot_sync(0xffffffffu, slowbits != 0);
+                        if (!want) break;
+                        if (slowbits) {
+                            const int bb = (int)(__float_as_uint(__uint2float_rz(slowbits)) >> 23) - 127;
+                            slowbits ^= 1u << bb;
+                            RefineEntry r;
+                            r.i = i;
+                            r.j = jb + (uint32_t)bb;
+                            r.meta = meta;
+                            sq[sq_n + __popc(want & ((1u << lane) - 1u))] = r;
+                        }
+                        sq_n += __popc(want);
+                        queued += __popc(want);
+                        __syncwarp();
+                        if (sq_n >= 32) {
+                            slow_batch<MODE, NEED_AVG, NEED_W, true>(A, se, glo, ghi, sq + (sq_n - 32), 32, rq, rq_count,
+                                                                     h, hl, lane, &refined, (int)ib);
+                            sq_n -= 32;
+                        }
+                    }
+                    __syncwarp();
+                    col_terms += tile_terms;
+                    if (col_terms + tile_terms > (uint32_t)kColumnTerms) {
+                        flush_lanes<NEED_AVG, NEED_W>(A, h, lane, cat);
+                        col_terms = 0;
+                    }
+                }
+                evaluated += (uint64_t)icount * (jend - jbeg);
+            }
+        }
+        // the chunk's queued pairs, then every lane's column into its catalogue
+        __syncwarp();
+        if (sq_n > 0) {
+            slow_batch<MODE, NEED_AVG, NEED_W, true>(A, se, glo, ghi, sq, sq_n, rq, rq_count, h, hl, lane, &refined,
+                                                     (int)ib);
+            sq_n = 0;
+        }
+        const int rest = *rq_count;
+        if (rest > 0) {
+            refine_batch<MODE, NEED_AVG, NEED_W>(A, se, rq, rest, h, hl, lane, (int)ib);
+            if (lane == 0) *rq_count = 0;
+            __syncwarp();
+        }
+        flush_lanes<NEED_AVG, NEED_W>(A, h, lane, cat);
+        col_terms = 0;
+    }
     for (int off = 16; off; off >>= 1) refined += __shfl_down_sync(0xffffffffu, refined, off);
     if (lane == 0) {
         atomicAdd(&A.g_stats[0], (unsigned long long)evaluated);
@@ -2298,6 +2528,42 @@ static int upload_and_minmax(Workspace &W, int s, int64_t n, const void *x, cons
 
 // Counting sort of one catalogue into lattice records at point offset `base` of B (whose
 // per-point buffers already hold base + n points); B's per-cell arrays are reused.
+// The counting sort of one catalogue into a lattice, in two halves around the scan of the cell
+// occupancy: cell index and slot within the cell of every point (the occupancy counts must have
+// been zeroed; several catalogues may count into one lattice), then the records at their slots
+// (from record rec_base on; ro_cat >= 0: the catalogue number takes the place of the reference
+// cell).  base: the catalogue's first point in the per-point cell and slot arrays.
+template <typename T>
+static int lattice_assign_at(SetBufs &B, int64_t n, int64_t base, const T *x, const T *y, const T *z, const Geom &g,
+                             unsigned long long *oob)
+{
+    if (n <= 0) return EXIT_SUCCESS;
+    k_assign<T><<<grid_for(n, 256), 256, 0, g_eng.stream>>>(x, y, z, n, g, (uint32_t *)B.cellid_u.p + base,
+                                                           (uint32_t *)B.fill.p + base, (uint32_t *)B.count.p, oob);
+    g_eng.launches++;
+    CF_CUDA(cudaGetLastError());
+    return EXIT_SUCCESS;
+}
+
+template <typename T>
+static int lattice_scatter_at(SetBufs &B, int64_t n, int64_t base, int64_t rec_base, const T *x, const T *y,
+                              const T *z, const T *w, const Geom &g, int ro_cat)
+{
+    if (n <= 0) return EXIT_SUCCESS;
+    Lattice L;
+    L.hi = (float4 *)B.hi.p + rec_base;
+    L.lo = g.write_lo ? (float4 *)B.lo.p + rec_base : nullptr;
+    L.dbl = (double4_32a *)B.dbl.p + rec_base;
+    L.ro = (int2 *)B.ro.p + rec_base;
+    L.cell_start = (uint32_t *)B.cell_start.p;
+    k_scatter<T><<<grid_for(n, 256), 256, 0, g_eng.stream>>>(x, y, z, w, n, g, (const uint32_t *)B.cellid_u.p + base,
+                                                            (const uint32_t *)B.fill.p + base,
+                                                            (const uint32_t *)B.cell_start.p, L, ro_cat);
+    g_eng.launches++;
+    CF_CUDA(cudaGetLastError());
+    return EXIT_SUCCESS;
+}
+
 template <typename T>
 static int build_lattice_at(Workspace &W, SetBufs &B, int64_t n, int64_t base, const T *x, const T *y, const T *z,
                             const T *w, const Geom &g, uint32_t ncells, unsigned long long *oob)
@@ -2313,23 +2579,9 @@ static int build_lattice_at(Workspace &W, SetBufs &B, int64_t n, int64_t base, c
         CF_CUDA(cudaMemsetAsync(B.cell_start.p, 0, sizeof(uint32_t) * ((size_t)ncells + 1), st));
         return EXIT_SUCCESS;
     }
-    uint32_t *cellid_u = (uint32_t *)B.cellid_u.p + base;
-    uint32_t *rank = (uint32_t *)B.fill.p + base;
-    const int grid = grid_for(n, 256);
-    k_assign<T><<<grid, 256, 0, st>>>(x, y, z, n, g, cellid_u, rank, count, oob);
-    g_eng.launches++;
-    CF_CUDA(cudaGetLastError());
+    if (lattice_assign_at<T>(B, n, base, x, y, z, g, oob) != EXIT_SUCCESS) return EXIT_FAILURE;
     if (scan_u32(W, count, (uint32_t *)B.cell_start.p, ncells, 0) != EXIT_SUCCESS) return EXIT_FAILURE;
-    Lattice L;
-    L.hi = (float4 *)B.hi.p + base;
-    L.lo = g.write_lo ? (float4 *)B.lo.p + base : nullptr;
-    L.dbl = (double4_32a *)B.dbl.p + base;
-    L.ro = (int2 *)B.ro.p + base;
-    L.cell_start = (uint32_t *)B.cell_start.p;
-    k_scatter<T><<<grid, 256, 0, st>>>(x, y, z, w, n, g, cellid_u, rank, (const uint32_t *)B.cell_start.p, L);
-    g_eng.launches++;
-    CF_CUDA(cudaGetLastError());
-    return EXIT_SUCCESS;
+    return lattice_scatter_at<T>(B, n, base, base, x, y, z, w, g, -1);
 }
 
 static int ensure_points(SetBufs &B, int64_t n)
@@ -3415,6 +3667,9 @@ struct BatchPlan {
     Geom g;
     TaskGeom G;
     int gap = -1;  // z-slab gap that splits the catalogues' chunks (chunk_gap)
+    // one lattice for all set-1 catalogues, chunk tasks with per-lane catalogues (k_pairs_chunks);
+    // else one lattice and chunk range per catalogue and the per-column work list
+    bool merged = false;
     Tables T;
     PairArgs A;
     cf_geometry geo;
@@ -3449,6 +3704,40 @@ static int batch_lattices(BatchPlan &P)
                             P.ncells, oob) != EXIT_SUCCESS)
         return EXIT_FAILURE;
     const int nz = P.g.n[2];
+    if (P.merged) {
+        // every catalogue counted into one occupancy array, one scan, every catalogue scattered
+        // (points carry their catalogue), one set of chunks
+        SetBufs &B = W.set[0];
+        if (ensure(B.count, sizeof(uint32_t) * (size_t)P.ncells) ||
+            ensure(B.cell_start, sizeof(uint32_t) * ((size_t)P.ncells + 1)))
+            return EXIT_FAILURE;
+        CF_CUDA(cudaMemsetAsync(B.count.p, 0, sizeof(uint32_t) * (size_t)P.ncells, st));
+        for (int b = 0; b < P.nbatch; b++)
+            if (lattice_assign_at<T>(B, P.n1[b], P.pbase[b], (const T *)P.x1[b], (const T *)P.y1[b],
+                                     (const T *)P.z1[b], g1, oob) != EXIT_SUCCESS)
+                return EXIT_FAILURE;
+        if (scan_u32(W, (const uint32_t *)B.count.p, (uint32_t *)B.cell_start.p, P.ncells, 0) != EXIT_SUCCESS)
+            return EXIT_FAILURE;
+        for (int b = 0; b < P.nbatch; b++) {
+            const T *w = P.need_w ? (const T *)P.w1[b] : nullptr;
+            if (lattice_scatter_at<T>(B, P.n1[b], P.pbase[b], 0, (const T *)P.x1[b], (const T *)P.y1[b],
+                                      (const T *)P.z1[b], w, g1, b) != EXIT_SUCCESS)
+                return EXIT_FAILURE;
+        }
+        k_col_chunks<<<(P.ncols + 7) / 8, 256, 0, st>>>((const uint32_t *)B.cell_start.p, (int)P.ncols, nz, P.gap,
+                                                        (uint32_t *)W.chunk_cnt.p);
+        g_eng.launches++;
+        CF_CUDA(cudaGetLastError());
+        if (scan_u32(W, (const uint32_t *)W.chunk_cnt.p, (uint32_t *)W.chunk_off.p, P.ncols, 0) != EXIT_SUCCESS)
+            return EXIT_FAILURE;
+        k_chunk_emit<<<(P.ncols + 7) / 8, 256, 0, st>>>((const uint32_t *)B.cell_start.p, (int)P.ncols, nz, P.gap,
+                                                        (const uint32_t *)W.chunk_off.p, P.total_slots, P.G.error,
+                                                        (uint32_t *)W.chunk_begin.p, (uint2 *)W.chunk_info.p, 0u,
+                                                        nullptr, 0);
+        g_eng.launches++;
+        CF_CUDA(cudaGetLastError());
+        return EXIT_SUCCESS;
+    }
     for (int b = 0; b < P.nbatch; b++) {
         const T *w = P.need_w ? (const T *)P.w1[b] : nullptr;
         if (build_lattice_at<T>(W, W.set[0], P.n1[b], P.pbase[b], (const T *)P.x1[b], (const T *)P.y1[b],
@@ -3483,8 +3772,46 @@ static int record_event(cudaEvent_t ev)
     return EXIT_SUCCESS;
 }
 
+// The chunk-task pair kernel of a merged batch (layout: private columns, P.warps per block).
+template <bool AVG, bool W>
+static int launch_chunks_t(BatchPlan &P)
+{
+    const int fls = g_eng.force_ls, fw = g_eng.force_warps;
+    g_eng.force_ls = 32;
+    g_eng.force_warps = P.warps;
+    const SmemLayout SL = choose_layout(MODE_R3, false, AVG, W, P.A.nedges, P.nbins, P.A.lut_n);
+    g_eng.force_ls = fls;
+    g_eng.force_warps = fw;
+    if (SL.lane_stride != 32 || SL.lane_stride != P.A.lane_stride_hint)
+        CF_FAIL("internal: the merged batch needs private histogram columns");
+    auto kern = k_pairs_chunks<AVG, W>;
+    int per_sm = 1;
+    CF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SL.total));
+    CF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, SL.warps * 32, SL.total));
+    if (per_sm < 1) per_sm = 1;
+    kern<<<g_eng.num_sms * per_sm, SL.warps * 32, SL.total, g_eng.stream>>>(
+        P.A, SL, P.G, (const uint32_t *)P.W.chunk_begin.p, (const uint2 *)P.W.chunk_info.p,
+        (const uint32_t *)P.W.set[1].cell_start.p, P.total_slots);
+    CF_CUDA(cudaGetLastError());
+    g_eng.launches++;
+    g_eng.last.blocks_per_sm = per_sm;
+    g_eng.last.warps_per_block = SL.warps;
+    g_eng.last.lane_stride = 32;
+    return EXIT_SUCCESS;
+}
+
+static int launch_chunks(BatchPlan &P)
+{
+    const bool avg = P.J.need_avg != 0, w = P.need_w;
+    if (avg && w) return launch_chunks_t<true, true>(P);
+    if (avg) return launch_chunks_t<true, false>(P);
+    if (w) return launch_chunks_t<false, true>(P);
+    return launch_chunks_t<false, false>(P);
+}
+
 // Enqueues lattices and task counts (phase 0), or task emission, pair kernel and read-back
-// (phase 1), on the engine stream.  No host waits inside either phase.
+// (phase 1), on the engine stream.  No host waits inside either phase.  A merged batch has no
+// work list: phase 0 builds the lattices and chunks, phase 1 runs the chunk-task kernel.
 static int batch_enqueue(BatchPlan &P, int phase, bool timing)
 {
     Workspace &W = P.W;
@@ -3495,12 +3822,22 @@ static int batch_enqueue(BatchPlan &P, int phase, bool timing)
         CF_CUDA(cudaMemsetAsync(W.chunk_info.p, 0, sizeof(uint2) * P.total_slots, st));
         const int rc = P.isf ? batch_lattices<float>(P) : batch_lattices<double>(P);
         if (rc != EXIT_SUCCESS) return EXIT_FAILURE;
+        if (P.merged) return EXIT_SUCCESS;
         k_task_count<<<task_grid(P.G, P.total_slots), 128, 0, st>>>(
             P.G, P.total_slots, (const uint32_t *)W.chunk_begin.p, (const uint2 *)W.chunk_info.p,
             (const uint32_t *)W.set[1].cell_start.p, (uint32_t *)W.ntask.p);
         g_eng.launches++;
         CF_CUDA(cudaGetLastError());
         return scan_u32(W, (const uint32_t *)W.ntask.p, (uint32_t *)W.task_off.p, P.nentries, 0);
+    }
+    if (P.merged) {
+        const size_t nbm = (size_t)P.nbatch * P.nbins;
+        CF_CUDA(cudaMemsetAsync(W.res.p, 0, res_zero_bytes(nbm), st));  // sums, statistics, chunk counter
+        if (timing && record_event(P.ev[1]) != EXIT_SUCCESS) return EXIT_FAILURE;
+        if (launch_chunks(P) != EXIT_SUCCESS) return EXIT_FAILURE;
+        if (timing && record_event(P.ev[2]) != EXIT_SUCCESS) return EXIT_FAILURE;
+        CF_CUDA(cudaMemcpyAsync(W.h_hist.p, W.res.p, res_bytes(nbm), cudaMemcpyDeviceToHost, st));
+        return EXIT_SUCCESS;
     }
     k_task_emit<<<task_grid(P.G, P.total_slots), 128, 0, st>>>(
         P.G, P.total_slots, (const uint32_t *)W.chunk_begin.p, (const uint2 *)W.chunk_info.p,
@@ -3695,11 +4032,41 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
         // ---- buffers ----
         if ((rc = task_geometry(&P->J, P->geo, P->g, glo, ghi, false, MODE_R3, P->G)) != EXIT_SUCCESS) break;
         P->gap = chunk_gap(P->G, P->J.n1, P->ncols);
+        // the merged form wherever the byte table and private histogram columns fit (FP32
+        // classification; CF_BATCH_MERGED=0 keeps one lattice per catalogue, for measurements)
+        P->merged = false;
+        const int mw = pair_max_threads(MODE_R3, P->J.need_avg != 0, P->need_w) / 32;
+        const char *bm = getenv("CF_BATCH_MERGED");
+        if (g_eng.precision == CF_PRECISION_FP32_REFINE && !P->w_exact && g_eng.byte_table && P->nbins <= 126 &&
+            !(bm && atoi(bm) == 0)) {
+            for (int wv = mw; wv >= 1 && !P->merged && rc == EXIT_SUCCESS; wv /= 2) {
+                g_eng.force_ls = 32;
+                g_eng.force_warps = wv;
+                Tables Tm;
+                rc = build_tables(W, &P->J, MODE_R3, P->nbins, P->need_w, P->delta, &Tm);
+                g_eng.force_ls = 0;
+                g_eng.force_warps = 0;
+                if (rc == EXIT_SUCCESS && Tm.lut8 && Tm.ls == 32) {
+                    P->merged = true;
+                    P->T = Tm;
+                    P->ls = 32;
+                    P->warps = wv;
+                }
+            }
+            if (rc != EXIT_SUCCESS) break;
+        }
         uint64_t slots = 0;
-        for (int b = 0; b < nbatch; b++) {
-            slots += P->n1[b] > 0 ? chunk_slots((uint64_t)P->n1[b], P->ncols, P->g.n[2], P->gap) : 0;
-            if (slots > 0xfffffff0ull) break;
-            P->cbase[b + 1] = (uint32_t)slots;
+        if (P->merged) {
+            P->gap = chunk_gap(P->G, P->total1, P->ncols);
+            slots = chunk_slots((uint64_t)P->total1, P->ncols, P->g.n[2], P->gap);
+            for (int b = 0; b <= nbatch; b++) P->cbase[b] = 0;
+            if (slots <= 0xfffffff0ull) P->cbase[nbatch] = (uint32_t)slots;
+        } else {
+            for (int b = 0; b < nbatch; b++) {
+                slots += P->n1[b] > 0 ? chunk_slots((uint64_t)P->n1[b], P->ncols, P->g.n[2], P->gap) : 0;
+                if (slots > 0xfffffff0ull) break;
+                P->cbase[b + 1] = (uint32_t)slots;
+            }
         }
         if (slots > 0xfffffff0ull) {
             fprintf(stderr, "corrfunc_gb300: too many chunks in the batch\n");
@@ -3718,29 +4085,35 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
             (rc = ensure(W.chunk_cat, sizeof(uint16_t) * ((size_t)P->total_slots + 1))) != EXIT_SUCCESS ||
             (rc = ensure_host(W.h_hist, res_bytes(nb))) != EXIT_SUCCESS)
             break;
-        P->nentries = P->total_slots * (uint32_t)((2 * P->G.reach_x + 1) * (2 * P->G.reach_y + 1));
+        P->nentries = P->merged ? 0u : P->total_slots * (uint32_t)((2 * P->G.reach_x + 1) * (2 * P->G.reach_y + 1));
         if ((rc = ensure(W.ntask, sizeof(uint32_t) * ((size_t)P->nentries + 1))) != EXIT_SUCCESS ||
             (rc = ensure(W.task_off, sizeof(uint32_t) * ((size_t)P->nentries + 2))) != EXIT_SUCCESS)
             break;
         P->G.error = res_view(W.res.p, nb).flags + 2;
-        if ((rc = build_tables(W, &P->J, MODE_R3, P->nbins, P->need_w, P->delta, &P->T)) != EXIT_SUCCESS) break;
+        if (!P->merged && (rc = build_tables(W, &P->J, MODE_R3, P->nbins, P->need_w, P->delta, &P->T)) != EXIT_SUCCESS)
+            break;
 
         // ---- eager run: size the work list ----
         if ((rc = batch_enqueue(*P, 0, false)) != EXIT_SUCCESS) break;
-        uint32_t *cnt_h = (uint32_t *)(mmh + kMmSlots);
-        if (cudaMemcpyAsync(cnt_h, (uint32_t *)W.task_off.p + P->nentries, sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                            st) != cudaSuccess ||
-            cudaStreamSynchronize(st) != cudaSuccess) {
-            fprintf(stderr, "corrfunc_gb300: CUDA error '%s' while building the batch work list\n",
-                    cudaGetErrorString(cudaGetLastError()));
-            rc = EXIT_FAILURE;
-            break;
+        if (P->merged) {
+            P->ntasks = 0;
+            P->task_cap = 0;
+        } else {
+            uint32_t *cnt_h = (uint32_t *)(mmh + kMmSlots);
+            if (cudaMemcpyAsync(cnt_h, (uint32_t *)W.task_off.p + P->nentries, sizeof(uint32_t),
+                                cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                cudaStreamSynchronize(st) != cudaSuccess) {
+                fprintf(stderr, "corrfunc_gb300: CUDA error '%s' while building the batch work list\n",
+                        cudaGetErrorString(cudaGetLastError()));
+                rc = EXIT_FAILURE;
+                break;
+            }
+            P->ntasks = *cnt_h;
+            // room for replays on catalogues of the same sizes whose points moved: twice the planned
+            // work list plus eight tasks per chunk of set 1 (a replay that still outgrows it fails)
+            P->task_cap = 2 * P->ntasks + 8 * (uint32_t)((P->total1 + kChunk - 1) / kChunk) + 1024;
+            if ((rc = ensure(W.tasks, sizeof(Task) * (size_t)P->task_cap)) != EXIT_SUCCESS) break;
         }
-        P->ntasks = *cnt_h;
-        // room for replays on catalogues of the same sizes whose points moved: twice the planned
-        // work list plus eight tasks per chunk of set 1 (a replay that still outgrows it fails)
-        P->task_cap = 2 * P->ntasks + 8 * (uint32_t)((P->total1 + kChunk - 1) / kChunk) + 1024;
-        if ((rc = ensure(W.tasks, sizeof(Task) * (size_t)P->task_cap)) != EXIT_SUCCESS) break;
 
         PairArgs &A = P->A;
         memset(&A, 0, sizeof(A));
@@ -3752,9 +4125,9 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
         A.lo2 = (const float4 *)W.set[1].lo.p;
         A.d2 = (const double4_32a *)W.set[1].dbl.p;
         A.ro2 = (const int2 *)W.set[1].ro.p;
-        A.tasks = (const Task *)W.tasks.p;
+        A.tasks = P->merged ? nullptr : (const Task *)W.tasks.p;
         A.ntasks = P->task_cap;
-        A.ntask_dev = (const uint32_t *)W.task_off.p + P->nentries;
+        A.ntask_dev = P->merged ? nullptr : (const uint32_t *)W.task_off.p + P->nentries;
         pair_constants(A, &P->J, MODE_R3, P->nbins, false, P->G, P->geo, P->g, P->delta, P->T, P->wmax, W);
         A.w_exact = P->w_exact ? 1 : 0;
         {
@@ -3788,11 +4161,11 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
         // ---- tuner: time the FP32 layouts that fit, keep the fastest ----
         if (tune && g_eng.precision == CF_PRECISION_FP32_REFINE && !P->w_exact) {
             const int cand_ls[3] = {32, 16, 8};
-            const int mw = pair_max_threads(MODE_R3, P->J.need_avg != 0, P->need_w) / 32;
             const int cand_w[3] = {mw, mw / 2, mw / 4};
             float best = 1e30f;
             int best_ls = 0, best_w = 0;
-            for (int li = 0; li < 3 && rc == EXIT_SUCCESS; li++) {
+            // (a merged batch keeps private columns: lane stride 32 only)
+            for (int li = 0; li < (P->merged ? 1 : 3) && rc == EXIT_SUCCESS; li++) {
                 for (int wi = 0; wi < 3 && rc == EXIT_SUCCESS; wi++) {
                     const SmemLayout c = smem_layout(P->J.nedges, P->nbins, cand_w[wi], false, P->T.lut_n, cand_ls[li],
                                                      P->J.need_avg != 0, P->need_w, false, P->J.need_avg != 0);
