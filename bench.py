@@ -64,6 +64,30 @@ TRAFFIC_SOURCE = ("ncu capture of the pair kernel on this workload (dram__bytes_
                   "per launch): a recorded constant, not measured in this run")
 
 
+def gridlink_roofline(ms, ncells):
+    """The lattice build against the HBM copy rate, by the byte count of the path's survey: per
+    lattice N (3 + nw) x (input element) read, N (3 + nw) x (4 + 8) written (FP32 cell-local and FP64
+    copies), N x 4 x 2 (cell ids written and read) and ncells x 8 x 2 (counts and offsets)."""
+    ew = 8 if WORKLOAD.get("dtype", "float64") == "float64" else 4
+    nw = 1 if WORKLOAD["weights"] else 0
+    sets = [WORKLOAD["n1"]] + ([] if WORKLOAD["autocorr"] else [WORKLOAD["n2"]])
+    nbytes = sum(n * (3 + nw) * ew + n * (3 + nw) * 12 + n * 8 + ncells * 16 for n in sets)
+    peak = measured_hbm_gbs()
+    gbs = nbytes / (ms / 1e3) / 1e9 if ms > 0 else None
+    return {"bound": "hbm", "bytes": nbytes, "ms": ms, "achieved": gbs, "peak": peak, "unit": "GB/s",
+            "frac": gbs / peak if (gbs and peak) else None,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peak else None,
+            "kernels": "k_assign, k_scan_tile / k_scan_add, k_scatter (CUDA events around the lattice build)"}
+
+
+def measured_hbm_gbs():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except Exception:
+        return None
+
+
 def _rank_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
@@ -820,8 +844,12 @@ def main():
             "gpu_launches": launches,
             "launch": {"blocks_per_sm": st["blocks_per_sm"], "warps_per_block": st["warps_per_block"],
                        "lane_stride": st["lane_stride"]},
-            "kernel_ms": {"pair_kernel": sum(pair_ms) / args.steps, "gridlink_and_worklist": sum(grid_ms) / args.steps,
+            "kernel_ms": {"pair_kernel": sum(pair_ms) / args.steps, "gridlink": sum(grid_ms) / args.steps,
+                          "extent_worklist_and_gaps": (sum(gpu_ms) - sum(pair_ms) - sum(grid_ms)) / args.steps,
                           "step_total": sum(gpu_ms) / args.steps, "host_wall": 1e3 * sum(wall) / args.steps},
+            "gridlink_roofline": gridlink_roofline(sum(grid_ms) / args.steps, st["num_cells"]),
+            "in_range_pairs_per_s": (int(np.sum(ref_np)) // (2 if WORKLOAD["autocorr"] else 1))
+                                    / (sum(gpu_ms) / 1e3 / args.steps),
             "pairs": {"reference_lattice_candidates": work, "gpu_evaluated": evaluated // args.steps,
                       "fp32_slow_path": st["pairs_slow"], "fp64_refined": refined // args.steps,
                       "counted": int(np.sum(ref_np))},

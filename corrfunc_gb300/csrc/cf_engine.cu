@@ -2318,7 +2318,7 @@ struct Engine {
     int device = -1;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev[6];
+    cudaEvent_t ev[8];
     Workspace ws;
     int regs_cache[kNumModes][4][2] = {};  // registers per thread of each pair kernel (0 = not queried)
     int force_ls = 0, force_warps = 0;  // FP32 pair-kernel layout chosen by the batch tuner (0 = scored)
@@ -2411,7 +2411,7 @@ static int engine_init(void)
     g_eng.smem_per_sm = prop.sharedMemPerMultiprocessor;
     if (cudaDeviceGetAttribute(&g_eng.clock_khz, cudaDevAttrClockRate, dev) != cudaSuccess) g_eng.clock_khz = 0;
     CF_CUDA(cudaStreamCreateWithFlags(&g_eng.stream, cudaStreamNonBlocking));
-    for (int k = 0; k < 6; k++) CF_CUDA(cudaEventCreate(&g_eng.ev[k]));
+    for (int k = 0; k < 8; k++) CF_CUDA(cudaEventCreate(&g_eng.ev[k]));
     // CF_PAIR_LAYOUT="<lane stride>,<warps per block>" fixes the FP32 pair kernel's histogram
     // layout instead of the scored choice (for layout measurements)
     const char *lay = getenv("CF_PAIR_LAYOUT");
@@ -3478,12 +3478,14 @@ static int run_locked(cf_job *J, cf_hist *H)
     const ResView R = res_view(W.res.p, nbins);
     unsigned long long *oob = R.oob;
     CF_CUDA(cudaMemsetAsync(R.flags, 0, sizeof(unsigned long long) * 4, st));  // flags, oob, extent
+    CF_CUDA(cudaEventRecord(g_eng.ev[6], st));  // the lattice build (gridlink) proper
     for (int s = 0; s < nsets; s++) {
         const int64_t n = s ? n2 : n1;
         int rc = dev_float ? build_lattice<float>(W, s, n, need_w, g, ncells, oob)
                            : build_lattice<double>(W, s, n, need_w, g, ncells, oob);
         if (rc != EXIT_SUCCESS) return EXIT_FAILURE;
     }
+    CF_CUDA(cudaEventRecord(g_eng.ev[7], st));
     SetBufs &S1 = W.set[0];
     SetBufs &S2 = W.set[nsets - 1];
     Tables T;
@@ -3632,7 +3634,7 @@ static int run_locked(cf_job *J, cf_hist *H)
     memcpy(H->wsum, Rh.w, sizeof(double) * nbins);
     float ms_pairs = 0.f, ms_grid = 0.f, ms_total = 0.f;
     CF_CUDA(cudaEventElapsedTime(&ms_pairs, g_eng.ev[2], g_eng.ev[3]));
-    CF_CUDA(cudaEventElapsedTime(&ms_grid, g_eng.ev[0], g_eng.ev[1]));
+    CF_CUDA(cudaEventElapsedTime(&ms_grid, g_eng.ev[6], g_eng.ev[7]));  // cell index, offsets, scatter
     CF_CUDA(cudaEventElapsedTime(&ms_total, g_eng.ev[0], g_eng.ev[4]));
     g_eng.last.pair_kernel_ms = ms_pairs;
     g_eng.last.gridlink_ms = ms_grid;

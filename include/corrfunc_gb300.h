@@ -368,8 +368,8 @@ int cf_gpu_get_precision(void);
  * measured with CUDA events, lattice-build time, and the number of evaluated / refined pairs. */
 typedef struct {
     double pair_kernel_ms;
-    double gridlink_ms;
-    double total_gpu_ms;
+    double gridlink_ms;  /* single counts: the lattice build proper (cell index, offsets, scatter) */
+    double total_gpu_ms; /* the whole count on the device, extent read-back and work list included */
     uint64_t pairs_evaluated;
     uint64_t pairs_refined;
     uint64_t tasks;
