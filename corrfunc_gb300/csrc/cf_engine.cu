@@ -1125,6 +1125,18 @@ __device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsig
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
     return r;
 }
+__device__ __forceinline__ unsigned long long f2_add(unsigned long long a, unsigned long long b)
+{
+    unsigned long long r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ unsigned long long f2_mul(unsigned long long a, unsigned long long b)
+{
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
 __device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b, unsigned long long c)
 {
     unsigned long long r;
@@ -1449,6 +1461,7 @@ __device__ __forceinline__ void pairs_group8(const PairArgs &A, const float4 *__
     const float *S = (const float *)sjhi, *SL8 = (const float *)sjlo;
     const unsigned long long xi2 = f2_pack(xi, xi), yi2 = f2_pack(yi, yi), zi2 = f2_pack(zi, zi),
                              b2 = f2_pack(A.q_bias, A.q_bias);
+    const unsigned long long xil2 = f2_pack(xil, xil), yil2 = f2_pack(yil, yil), zil2 = f2_pack(zil, zil);
     uint32_t addr[U];
     int vw[U], va[U];
 #pragma unroll
@@ -1465,22 +1478,26 @@ __device__ __forceinline__ void pairs_group8(const PairArgs &A, const float4 *__
         }
         // separations and q' of the four pairs, two per paired instruction (the scalar q8 chain,
         // lane by lane)
-        float dxv[4], dyv[4], dzv[4], qv[4];
+        float qv[4], sv[4];  // q' and, with averages, the squared separation from the lo-corrected points
 #pragma unroll
         for (int h = 0; h < 2; h++) {
             const unsigned long long dx2 = f2_sub(h ? f2_pack(X.z, X.w) : f2_pack(X.x, X.y), xi2);
             const unsigned long long dy2 = f2_sub(h ? f2_pack(Y.z, Y.w) : f2_pack(Y.x, Y.y), yi2);
             const unsigned long long dz2 = f2_sub(h ? f2_pack(Z.z, Z.w) : f2_pack(Z.x, Z.y), zi2);
             const unsigned long long q2 = f2_fma(dz2, dz2, f2_fma(dy2, dy2, f2_fma(dx2, dx2, b2)));
-            f2_unpack(dx2, dxv[2 * h], dxv[2 * h + 1]);
-            f2_unpack(dy2, dyv[2 * h], dyv[2 * h + 1]);
-            f2_unpack(dz2, dzv[2 * h], dzv[2 * h + 1]);
             f2_unpack(q2, qv[2 * h], qv[2 * h + 1]);
+            if (NEED_AVG) {
+                // dx + (lx - xil) and the sum of squares, as the scalar form rounds them
+                const unsigned long long dxp = f2_add(dx2, f2_sub(h ? f2_pack(LX.z, LX.w) : f2_pack(LX.x, LX.y), xil2));
+                const unsigned long long dyp = f2_add(dy2, f2_sub(h ? f2_pack(LY.z, LY.w) : f2_pack(LY.x, LY.y), yil2));
+                const unsigned long long dzp = f2_add(dz2, f2_sub(h ? f2_pack(LZ.z, LZ.w) : f2_pack(LZ.x, LZ.y), zil2));
+                const unsigned long long s2 = f2_fma(dzp, dzp, f2_fma(dyp, dyp, f2_mul(dxp, dxp)));
+                f2_unpack(s2, sv[2 * h], sv[2 * h + 1]);
+            }
         }
 #pragma unroll
         for (int v = 0; v < 4; v++) {
             const int u = g + v, k = kq + v;
-            const float dx = dxv[v], dy = dyv[v], dz = dzv[v];
             const float q = fminf(qv[v], qcap);
             uint32_t a, e;
             asm("mad.hi.u32 %0, %1, %2, %3;" : "=r"(a) : "r"(__float_as_uint(q)), "r"(A.lut_mul), "r"(lut_add));
@@ -1495,11 +1512,7 @@ __device__ __forceinline__ void pairs_group8(const PairArgs &A, const float4 *__
                 vw[u] = __float2int_rn(wis * jw);
             }
             if (NEED_AVG) {
-                const float lx = v == 0 ? LX.x : v == 1 ? LX.y : v == 2 ? LX.z : LX.w;
-                const float ly = v == 0 ? LY.x : v == 1 ? LY.y : v == 2 ? LY.z : LY.w;
-                const float lz = v == 0 ? LZ.x : v == 1 ? LZ.y : v == 2 ? LZ.z : LZ.w;
-                const float dxp = dx + (lx - xil), dyp = dy + (ly - yil), dzp = dz + (lz - zil);
-                const float d = sqrtf(fmaf(dzp, dzp, fmaf(dyp, dyp, dxp * dxp)));
+                const float d = sqrtf(sv[v]);
                 const float favg = MODE == MODE_THETA ? chord_degrees<SER>(d) : d;
                 va[u] = __float2int_rn(favg * ascale[e >> 1]);
             }

@@ -1,6 +1,7 @@
 """Batched DD(r) cross-correlations (cf_gpu_batch_plan / cf_gpu_batch_run): every catalogue's
 result equals countpairs() on the same arrays, across replays of the captured graph, with and
-without the layout tuner, for float64 and float32 positions, weighted and not."""
+without the layout tuner, for float64 and float32 positions, weighted and not, in the merged form
+(one lattice for all catalogues, chunk tasks) and the per-catalogue form."""
 import numpy as np
 import pytest
 
@@ -72,6 +73,33 @@ def test_batch_matches_countpairs(torch, dtype, weights, autotune):
         assert sum(int(g["npairs"].sum()) for g in got) > 0
     finally:
         batch.close()
+
+
+@pytest.mark.parametrize("form", ["per_catalogue", "many_bins"])
+def test_batch_other_forms_match_countpairs(torch, monkeypatch, form):
+    """The per-catalogue form of a batch (one lattice and chunk range per catalogue on one work
+    list): chosen with CF_BATCH_MERGED=0, and by itself for more bins than the byte table holds."""
+    from corrfunc_gb300 import theory
+    L = 200.0
+    if form == "per_catalogue":
+        monkeypatch.setenv("CF_BATCH_MERGED", "0")
+        bins = np.logspace(np.log10(0.3), np.log10(15.0), 13)
+    else:
+        bins = np.logspace(np.log10(0.3), np.log10(15.0), 141)
+    cats, second = _catalogues(np.float64, [3000, 9000, 700], 20000, L, 17)
+    dev = [_dev(torch, c) for c in cats]
+    dsec = _dev(torch, second)
+    torch.cuda.synchronize()
+    batch = theory.DDCrossBatch(bins, dev, dsec, periodic=True, boxsize=L, output_ravg=True,
+                                weight_type="pair_product", autotune=False)
+    try:
+        got = batch.run()
+    finally:
+        batch.close()
+    for c, g in zip(cats, got):
+        want = theory.DD(0, 1, bins, c[0], c[1], c[2], weights1=c[3], X2=second[0], Y2=second[1], Z2=second[2],
+                         weights2=second[3], weight_type="pair_product", periodic=True, boxsize=L, output_ravg=True)
+        _check(g, want, np.float64)
 
 
 def test_batch_replays_new_contents(torch):
