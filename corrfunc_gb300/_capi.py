@@ -151,7 +151,7 @@ class GpuStats(Structure):
     _fields_ = [("pair_kernel_ms", c_double), ("gridlink_ms", c_double), ("total_gpu_ms", c_double),
                 ("pairs_evaluated", c_uint64), ("pairs_refined", c_uint64), ("tasks", c_uint64),
                 ("kernel_launches", c_int), ("num_cells", c_int), ("blocks_per_sm", c_int),
-                ("warps_per_block", c_int), ("lane_stride", c_int), ("reserved", c_int), ("pairs_slow", c_uint64)]
+                ("warps_per_block", c_int), ("lane_stride", c_int), ("column_split", c_int), ("pairs_slow", c_uint64)]
 
 
 _GPU_PROTOS["cf_gpu_last_stats"] = ([POINTER(GpuStats)], c_int)

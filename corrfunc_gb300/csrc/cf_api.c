@@ -2014,7 +2014,7 @@ int cf_gpu_last_stats(cf_gpu_stats *out)
     out->blocks_per_sm = s.blocks_per_sm;
     out->warps_per_block = s.warps_per_block;
     out->lane_stride = s.lane_stride;
-    out->reserved = 0;
+    out->column_split = s.column_split;
     out->pairs_slow = s.pairs_slow;
     return EXIT_SUCCESS;
 }

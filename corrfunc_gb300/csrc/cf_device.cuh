@@ -9,13 +9,26 @@ namespace cf {
 // One unit of pair work: up to 32 consecutive points of one lattice column ("i-chunk")
 // against one contiguous range of points of a neighbouring column ("j-range") with a fixed
 // periodic image.  meta packs: bits 0-5 i_count-1, bits 8/10/12 (2 bits each) image+1 per
-// axis, bit 16 'own' (auto-correlation, same column, same image: count only j > i).
+// axis, bit 14 'images' (packed: some range has a periodic image), bit 15 'packed', bit 16 'own'
+// (auto-correlation, same column, same image: count only j > i).
+//
+// A packed task ("item") takes its j points from a list of ranges (JRange records, one per
+// split j column and periodic image) that the chunk's whole neighbourhood concatenates:
+// j_begin = first record, j_end bits 0-10 = points - 1, bits 11-31 = item number m; the item
+// covers list positions [m kJMax, m kJMax + points).
 struct Task {
     uint32_t i_begin;
     uint32_t j_begin;
     uint32_t j_end;
     uint32_t meta;
 };
+constexpr uint32_t kTaskImages = 1u << 14;
+constexpr uint32_t kTaskPacked = 1u << 15;
+
+// One range of a chunk's concatenated j list: x = first j point (lattice index), y = its list
+// position, z = image code (bits 0-5, as Task::meta bits 8-13) | bit 31 on the chunk's last
+// record, w = list position after the range.
+typedef uint4 JRange;
 
 __host__ __device__ inline uint32_t task_meta(int icount, int mx, int my, int mz, int own)
 {
@@ -54,6 +67,7 @@ struct PairArgs {
     const int2 *ro2;
 
     const Task *tasks;
+    const JRange *jrec;         // range records of packed tasks
     uint32_t ntasks;            // task count, or the work-list capacity when ntask_dev is set
     const uint32_t *ntask_dev;  // device-resident task count (batched work lists), or null
     uint32_t *task_counter;

@@ -150,11 +150,16 @@ struct Geom {
     int e_fix[3];
     unsigned long long o_hi[3], o_cell[3];  // X of hi_origin and of origin
     float q_f[3], rho_f[3];                 // q, 2^e_fix
-    // cell index = umulhi(X - o_cell, cell_mul) >> cell_shift: (x - origin) / s in 64-bit
-    // fixed point, within eps_cell (position units) of the exact value
+    // fixed-point index t = umulhi(X - o_cell, cell_mul) >> cell_shift: (x - origin) / (s / cdiv)
+    // in 64-bit fixed point, within eps_cell (position units) of the exact value, clamped below
+    // tmax; the cell index is t / cdiv.  With two lattices of split columns in one call (the j
+    // lattice's columns split every i-lattice column cdiv x cdiv, its z slabs merge cdiv i-lattice
+    // slabs) both take t from the same product, so that a j-lattice cell lies inside exactly
+    // one i-lattice column and slab range.  cdiv = 1, tmax = n otherwise.
     unsigned long long cell_mul[3];
     int cell_shift[3];
     double eps_cell[3];
+    int cdiv[3], tmax[3];
     // order keys (okey0) of the extent checks, and of the range of coordinates that are inside
     // the reference lattice whatever the rounding of its FP64 cell index (others take the exact test)
     unsigned long long k_chk_lo[3], k_chk_hi[3], k_chk_wmax, k_chk_wmin;
@@ -405,7 +410,10 @@ __device__ __forceinline__ int axis_cell(unsigned long long X, const Geom &g, in
     const unsigned long long U = X - g.o_cell[a];
     if ((long long)U < 0) return 0;
     const unsigned long long t = __umul64hi(U, g.cell_mul[a]) >> g.cell_shift[a];
-    return t >= (unsigned long long)g.n[a] ? g.n[a] - 1 : (int)t;
+    const int div = g.cdiv[a] > 1 ? g.cdiv[a] : 1;
+    const unsigned long long nt = g.tmax[a] > 0 ? (unsigned long long)g.tmax[a] : (unsigned long long)g.n[a];
+    const int tf = t >= nt ? (int)nt - 1 : (int)t;
+    return div > 1 ? tf / div : tf;
 }
 
 // cell index of a point in the reference lattice, in the reference's FP64 arithmetic
@@ -702,7 +710,7 @@ static inline uint64_t chunk_slots(uint64_t n1, uint64_t ncols, int nz, int gap)
     return (n1 + kChunk - 1) / kChunk + runs;
 }
 
-constexpr int kWzTab = 256;  // stencil columns whose z reach is tabulated in the task geometry
+constexpr int kWzTab = 512;  // stencil columns whose z reach is tabulated in the task geometry
 
 struct TaskGeom {
     int nx, ny, nz;
@@ -715,11 +723,16 @@ struct TaskGeom {
     double rmax_z;          // max |dz| (incl. margin)
     double rmax_3d;         // spherical limit (incl. margin), 0 = none
     uint32_t *error;        // set when a task would need an image beyond +-1
-    // z reach in slabs of every neighbour column offset c = (dx + reach_x) * (2 reach_y + 1) +
+    // z reach in slabs of every neighbour column offset c = (dx + reach_x) * (2 reach_y + sub) +
     // dy + reach_y, -1 when the column is pruned; computed on the host (FP64) when the stencil
     // has at most kWzTab columns (ntab > 0), else by each thread
     int ntab;
     int16_t wz_tab[kWzTab];
+    // columns of this lattice per chunk column and axis (a j lattice of split columns: offsets
+    // dx, dy are counted from the first split column of the chunk's column, which spans 0 .. sub - 1)
+    int sub;
+    uint32_t j_off;  // packed tasks: lattice index of the split lattice's first point in the j arrays
+    int zshift, nzj;  // packed tasks: j-lattice slab = slab >> zshift, of nzj per column
 };
 
 __device__ __forceinline__ int floordiv(int a, int b)
@@ -729,11 +742,15 @@ __device__ __forceinline__ int floordiv(int a, int b)
     return q;
 }
 
-// z reach (slabs) of neighbour column offset (dx, dy), -1 when the column is beyond reach
+// z reach (slabs) of neighbour column offset (dx, dy), -1 when the column is beyond reach: the
+// radii against the gap between the chunk's column (offsets 0 .. sub - 1) and that column
 __host__ __device__ inline int column_wz(const TaskGeom &G, int dx, int dy)
 {
-    const double rx = fmax(0.0, (double)(abs(dx) - 1)) * G.s[0];
-    const double ry = fmax(0.0, (double)(abs(dy) - 1)) * G.s[1];
+    const int sub = G.sub > 1 ? G.sub : 1;
+    const int gx = dx < 0 ? -dx - 1 : (dx >= sub ? dx - sub : 0);
+    const int gy = dy < 0 ? -dy - 1 : (dy >= sub ? dy - sub : 0);
+    const double rx = (double)gx * G.s[0];
+    const double ry = (double)gy * G.s[1];
     const double rho2 = rx * rx + ry * ry;
     if (rho2 >= G.rmax_xy * G.rmax_xy) return -1;
     double W = G.rmax_z;
@@ -882,6 +899,235 @@ __global__ void k_task_list(TaskGeom G, uint32_t nslots, const uint32_t *chunk_b
     if (n > room) atomicOr(&flags[3], 1u);
 }
 
+// The neighbourhood of one chunk in a j lattice of split columns as packed tasks (one warp per
+// chunk slot).  Every split column within reach and every periodic z image of it whose window
+// holds points gives one range; the chunk's ranges are concatenated into one list (records
+// contiguous in recs, list positions from 0) and cut into items of kJMax positions.  An
+// auto-correlation takes only the split columns of forward neighbour columns (its own column's
+// pairs are listed from the i lattice).  Pass 0 counts, pass 1 writes: records and items are
+// reserved with one atomic each per chunk (rec_count, flags[1]); past either capacity nothing
+// is written, flags[3] is set and the counters still grow to the totals (the caller resizes
+// and runs again).
+static_assert(kJMax <= 2048, "an item's point count is stored in 11 bits");
+constexpr int kItemWarps = 8;          // warps per block of k_item_list: one reservation per block
+constexpr int kItemLanes = 4;          // lanes per chunk (they share its stencil list)
+constexpr int kItemUnroll = 4;         // stencil entries per lane and step (their loads issued together)
+constexpr int kItemStenShared = 4096;  // longest stencil list staged in shared memory (32 KB)
+
+// One z image of one stencil entry (0: none): the range of the j lattice's slabs that hold
+// window slabs [lo, hi] of periodic image mz, clamped to the lattice
+__device__ __forceinline__ void item_window(const TaskGeom &G, int lo, int hi, int mz, int &s0, int &s1)
+{
+    s0 = lo - mz * G.nz;
+    s1 = hi - mz * G.nz;
+    s0 = s0 < 0 ? 0 : s0;
+    s1 = s1 > G.nz - 1 ? G.nz - 1 : s1;
+}
+
+// The neighbourhood of every chunk in a j lattice of split columns as packed tasks: every
+// stencil entry (split column within reach) and periodic z image whose window holds points is
+// one range; a chunk's ranges are concatenated into one list (records contiguous, list
+// positions from 0) and cut into items of kJMax positions.  kItemLanes lanes per chunk (a warp
+// holds 32 / kItemLanes consecutive chunk slots, mostly of one lattice column, so that their
+// cell-offset loads for one entry fall close together) share the stencil list sten[0 .. nsten):
+// split-column offset (du, dv) = (low, high int16 of .x) and z reach .y, only the entries within
+// reach (and, for an auto-correlation, of forward neighbour columns).  Pass 0 counts, pass 1
+// writes: records and items are reserved with one atomic each per block (rec_count, flags[1]);
+// past either capacity nothing is written, flags[3] is set and the counters still grow to the
+// totals (the caller resizes and runs again).
+__global__ void __launch_bounds__(32 * kItemWarps) k_item_list(TaskGeom G, uint32_t nslots, const uint32_t *chunk_begin,
+                                                              const uint2 *chunk_info, const uint32_t *cs2,
+                                                              const int2 *sten, int nsten, Task *tasks,
+                                                              uint32_t task_cap, JRange *recs, uint32_t rec_cap,
+                                                              uint32_t *flags, uint32_t *rec_count)
+{
+    __shared__ uint32_t s_rec[kItemWarps], s_item[kItemWarps], s_base[2];
+    extern __shared__ int2 s_sten[];
+    const int lane = threadIdx.x & 31, g = lane % kItemLanes;
+    const uint32_t slot = (blockIdx.x * blockDim.x + threadIdx.x) / kItemLanes;
+    const uint2 info = slot < nslots ? chunk_info[slot] : make_uint2(0u, 0u);
+    const uint32_t icount = info.x & 63u;  // 0: unused chunk slot (or past the last)
+    const uint32_t ib = slot < nslots ? chunk_begin[slot] : 0u;
+    const int sub = G.sub, nz = G.nz;
+    const int nyc = G.ny / sub;
+    const int col = (int)info.y, ix = col / nyc, iy = col % nyc;
+    const int a = (int)((info.x >> 6) & 4095u), b = (int)((info.x >> 18) & 4095u);
+    const uint32_t meta = task_meta(icount ? (int)icount : 1, 0, 0, 0, 0) | kTaskPacked;
+    // the stencil list in shared memory
+    const bool sten_sh = nsten <= kItemStenShared;
+    if (sten_sh)
+        for (int e = threadIdx.x; e < nsten; e += blockDim.x) s_sten[e] = sten[e];
+    __syncthreads();
+    const int2 *stl = sten_sh ? (const int2 *)s_sten : sten;
+    uint32_t nrec = 0, npts = 0;  // pass 0: this lane's ranges and points
+    bool imgs = false;            // a range of the chunk has a periodic image
+    uint32_t ctot = 0;            // the chunk's points (all its lanes)
+    uint32_t r = 0, p = 0, rlast = 0, tb = 0;  // pass 1: next record, list position; the chunk's last record, first task
+    for (int pass = 0; pass < 2; pass++) {
+        auto emit = [&](uint32_t jb, uint32_t je, uint32_t img) {
+            if (je <= jb) return;
+            const uint32_t len = je - jb;
+            if (pass == 0) {
+                nrec++;
+                npts += len;
+                imgs = imgs || img != 0x15u;  // 0x15: no image on any axis
+                return;
+            }
+            recs[r] = make_uint4(jb + G.j_off, p, img | (r == rlast ? 0x80000000u : 0u), p + len);
+            // items whose first position falls in this range
+            for (uint32_t m = (p + kJMax - 1) / kJMax; m * kJMax < p + len; m++) {
+                const uint32_t cnt = min(kJMax, ctot - m * kJMax);
+                Task t;
+                t.i_begin = ib;
+                t.j_begin = r;
+                t.j_end = (cnt - 1) | (m << 11);
+                t.meta = meta | (imgs ? kTaskImages : 0u);
+                tasks[tb + m] = t;
+            }
+            r++;
+            p += len;
+        };
+        const int nl = icount ? nsten : 0;
+        for (int e0 = g; e0 < nl; e0 += kItemLanes * kItemUnroll) {
+            uint32_t jbv[kItemUnroll], jev[kItemUnroll], imgv[kItemUnroll];
+            int lov[kItemUnroll], hiv[kItemUnroll], cbv[kItemUnroll];
+#pragma unroll
+            for (int q = 0; q < kItemUnroll; q++) {
+                jbv[q] = jev[q] = imgv[q] = 0;
+                lov[q] = 0;
+                hiv[q] = -1;
+                cbv[q] = -1;
+                const int e = e0 + q * kItemLanes;
+                if (e >= nl) continue;
+                const int2 se = stl[e];
+                const int du = (int)(int16_t)(se.x & 0xffff), dv = se.x >> 16, wz = se.y;
+                const int ux = ix * sub + du, uy = iy * sub + dv;
+                int mx = 0, cx = ux, my = 0, cy = uy;
+                if (G.periodic[0]) {
+                    mx = ux < 0 ? -1 : (ux >= G.nx ? 1 : 0);
+                    cx = ux - mx * G.nx;
+                } else if (ux < 0 || ux >= G.nx) {
+                    continue;
+                }
+                if (G.periodic[1]) {
+                    my = uy < 0 ? -1 : (uy >= G.ny ? 1 : 0);
+                    cy = uy - my * G.ny;
+                } else if (uy < 0 || uy >= G.ny) {
+                    continue;
+                }
+                const int lo = a - wz, hi = b + wz;
+                if (cx < 0 || cx >= G.nx || cy < 0 || cy >= G.ny ||
+                    (G.periodic[2] && (lo < -nz || hi >= 2 * nz))) {  // an image beyond +-1
+                    if (pass == 0 && G.error) atomicOr(G.error, 1u);
+                    continue;
+                }
+                cbv[q] = (cx * G.ny + cy) * G.nzj;
+                lov[q] = lo;
+                hiv[q] = hi;
+                imgv[q] = (uint32_t)(mx + 1) | ((uint32_t)(my + 1) << 2);
+                // the window's own image (mz = 0), loaded with the others of this step
+                int s0, s1;
+                item_window(G, lo, hi, 0, s0, s1);
+                if (s0 <= s1) {
+                    jbv[q] = cs2[(size_t)cbv[q] + (s0 >> G.zshift)];
+                    jev[q] = cs2[(size_t)cbv[q] + (s1 >> G.zshift) + 1];
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < kItemUnroll; q++) {
+                if (cbv[q] < 0) continue;
+                // periodic z images -1 and +1 (windows across the lattice's z ends: rare)
+                if (G.periodic[2] && lov[q] < 0) {
+                    int s0, s1;
+                    item_window(G, lov[q], hiv[q], -1, s0, s1);
+                    if (s0 <= s1)
+                        emit(cs2[(size_t)cbv[q] + (s0 >> G.zshift)], cs2[(size_t)cbv[q] + (s1 >> G.zshift) + 1],
+                             imgv[q]);
+                }
+                emit(jbv[q], jev[q], imgv[q] | (1u << 4));
+                if (G.periodic[2] && hiv[q] >= nz) {
+                    int s0, s1;
+                    item_window(G, lov[q], hiv[q], 1, s0, s1);
+                    if (s0 <= s1)
+                        emit(cs2[(size_t)cbv[q] + (s0 >> G.zshift)], cs2[(size_t)cbv[q] + (s1 >> G.zshift) + 1],
+                             imgv[q] | (2u << 4));
+                }
+            }
+        }
+        if (pass == 1) break;
+        // the chunk's totals over its lanes, then block-wide offsets and one reservation
+        uint32_t cp = npts, crec = nrec;  // inclusive scans within the chunk's lanes
+        for (int o = 1; o < kItemLanes; o <<= 1) {
+            const uint32_t tp = __shfl_up_sync(0xffffffffu, cp, o, kItemLanes);
+            const uint32_t tr = __shfl_up_sync(0xffffffffu, crec, o, kItemLanes);
+            if (g >= o) {
+                cp += tp;
+                crec += tr;
+            }
+        }
+        ctot = __shfl_sync(0xffffffffu, cp, kItemLanes - 1, kItemLanes);
+        const uint32_t crtot = __shfl_sync(0xffffffffu, crec, kItemLanes - 1, kItemLanes);
+        imgs = ((__ballot_sync(0xffffffffu, imgs) >> (lane - g)) & ((1u << kItemLanes) - 1u)) != 0u;
+        const bool big = ctot >= 0x80000000u;  // list positions must stay below 2^31
+        const uint32_t myrec = big ? 0u : nrec;
+        const uint32_t nitems = (g == 0 && !big) ? (ctot + kJMax - 1) / kJMax : 0u;
+        uint32_t ir = myrec, it = nitems;  // inclusive scans over the warp
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t tr = __shfl_up_sync(0xffffffffu, ir, o), ti = __shfl_up_sync(0xffffffffu, it, o);
+            if (lane >= o) {
+                ir += tr;
+                it += ti;
+            }
+        }
+        const int warp = threadIdx.x >> 5;
+        if (lane == 31) {
+            s_rec[warp] = ir;
+            s_item[warp] = it;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t sr = 0, si = 0;
+            for (int w = 0; w < kItemWarps; w++) {
+                const uint32_t cr = s_rec[w], ci = s_item[w];
+                s_rec[w] = sr;
+                s_item[w] = si;
+                sr += cr;
+                si += ci;
+            }
+            s_base[0] = sr ? atomicAdd(rec_count, sr) : 0u;
+            s_base[1] = si ? atomicAdd(&flags[1], si) : 0u;
+        }
+        __syncthreads();
+        if (big && g == 0) atomicOr(&flags[3], 1u);
+        const uint32_t rb = s_base[0] + s_rec[warp] + ir - myrec;  // this lane's first record
+        const uint32_t tfirst = s_base[1] + s_item[warp] + it - nitems;
+        tb = __shfl_sync(0xffffffffu, tfirst, lane - g);                      // the chunk's first task
+        const uint32_t crb = __shfl_sync(0xffffffffu, rb, lane - g);          // and first record
+        const uint32_t nit = __shfl_sync(0xffffffffu, nitems, lane - g);
+        const bool over = (uint64_t)crb + (big ? 0u : crtot) > rec_cap || (uint64_t)tb + nit > task_cap;
+        if (big || crtot == 0) return;  // no barrier below
+        if (over) {
+            // reserved task slots below the capacity become empty tasks (the pair kernel runs
+            // before the host sees the overflow and reads every slot below the capacity)
+            if (g == 0) {
+                for (uint32_t m = 0; m < nit && (uint64_t)tb + m < task_cap; m++) {
+                    Task t;
+                    t.i_begin = ib;
+                    t.j_begin = 0;
+                    t.j_end = 0;
+                    t.meta = task_meta((int)icount, 0, 0, 0, 0);
+                    tasks[tb + m] = t;
+                }
+                atomicOr(&flags[3], 1u);
+            }
+            return;
+        }
+        r = rb;
+        p = cp - npts;  // this lane's first list position within the chunk
+        rlast = crb + crtot - 1;
+    }
+}
+
 // ------------------------------------------------------------------------------------
 // pair kernels
 // ------------------------------------------------------------------------------------
@@ -891,6 +1137,7 @@ struct SmemLayout {
     bool need_avg, need_w;
     int entry_words;  // 32-bit words per histogram entry: count [, avg hi, avg lo] [, w hi, w lo]
     size_t edges_off, guard_off, ascale_off, lut_off, stage_off, hist_off, per_warp_hist, per_warp_stage, total;
+    size_t shift_off;  // FP32 kernels: periodic shifts of j points by image code (hi then lo, 64 float4 each)
     size_t wd_off, per_warp_wd;  // FP64 kernel with weights: one double weight sum per row and warp
 };
 
@@ -914,7 +1161,8 @@ struct RefineEntry {
 constexpr int kColumnTerms = 1 << 15;
 
 __host__ __device__ inline SmemLayout smem_layout(int nedges, int nbins, int warps, bool f64, int lut_n, int lane_stride,
-                                                  bool need_avg, bool need_w, bool store_dz, bool lo_stage)
+                                                  bool need_avg, bool need_w, bool store_dz, bool lo_stage,
+                                                  bool packed = false)
 {
     SmemLayout L;
     L.need_avg = need_avg;
@@ -937,13 +1185,17 @@ __host__ __device__ inline SmemLayout smem_layout(int nedges, int nbins, int war
     o = align_up(o + sizeof(float) * (nedges + 2), 16);
     L.lut_off = o;
     o = align_up(o + sizeof(uint32_t) * (lut_n + 1), 16);
+    L.shift_off = o;
+    o = align_up(o + (f64 || !packed ? 0 : 2 * 64 * sizeof(float4)), 16);
     L.stage_off = o;
-    // f32: float4 hi[32] + float4 lo[32] + refine and slow queues (the lo half is laid out even
-    // where it stays unused: the histogram layouts were measured with it);
+    // f32: float4 hi[32] + float4 lo[32] + refine and slow queues + queue fill and counters (16
+    // bytes) + (packed tasks) the lattice index and image code of every staged j point (the lo
+    // half is laid out even where it stays unused: the histogram layouts were measured with it);
     // f64: double4_32a[32] + int rc[32] + int orig[32]
     (void)lo_stage;
     L.per_warp_stage = f64 ? (32 * sizeof(double4_32a) + 64 * sizeof(int))
-                           : (64 * sizeof(float4) + (kRefineQueue + kSlowQueue) * sizeof(RefineEntry) + 16);
+                           : (64 * sizeof(float4) + (kRefineQueue + kSlowQueue) * sizeof(RefineEntry) + 16 +
+                              (packed ? 32 * sizeof(uint32_t) + 32 : 0));
     o = align_up(o + L.per_warp_stage * warps, 16);
     L.hist_off = o;
     L.per_warp_hist = align_up((size_t)L.nrows * lane_stride * 4 * L.entry_words + 32, 16);
@@ -1656,7 +1908,7 @@ __device__ __noinline__ void slow_batch(const PairArgs &A, const double *se, con
     }
 }
 
-template <int MODE, bool NEED_AVG, bool NEED_W, bool LUT8>
+template <int MODE, bool NEED_AVG, bool NEED_W, bool LUT8, bool PACKED>
 __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_PAIR_MIN_BLOCKS)
     k_pairs_f32(PairArgs A, SmemLayout SL)
 {
@@ -1689,16 +1941,36 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
     RefineEntry *rq = (RefineEntry *)(sjlo + 32);
     RefineEntry *sq = rq + kRefineQueue;
     int *rq_count = (int *)(sq + kSlowQueue);
+    // pairs queued for the slow path and pairs evaluated by the warp (bytes 4-7 and 8-15 of the 16
+    // after the queue fill: kept off registers)
+    uint32_t *qd_s = (uint32_t *)((unsigned char *)rq_count + 4);
+    unsigned long long *ev_s = (unsigned long long *)((unsigned char *)rq_count + 8);
+    uint32_t *sidx = (uint32_t *)((unsigned char *)rq_count + 16);  // packed tasks: staged j points'
+    uint8_t *simg = (uint8_t *)(sidx + 32);                          // lattice indices and image codes
+    // periodic shift of a j point by image code (bits 0-5 as Task::meta bits 8-13)
+    float4 *shift_hi = (float4 *)(smem + SL.shift_off), *shift_lo = shift_hi + 64;
+    if constexpr (PACKED) {
+        for (int k = threadIdx.x; k < 64; k += blockDim.x) {
+            const int c0 = k & 3, c1 = (k >> 2) & 3, c2 = (k >> 4) & 3;
+            shift_hi[k] = make_float4(c0 < 3 ? A.ohi[0][c0] : 0.f, c1 < 3 ? A.ohi[1][c1] : 0.f,
+                                      c2 < 3 ? A.ohi[2][c2] : 0.f, 0.f);
+            shift_lo[k] = make_float4(c0 < 3 ? A.olo[0][c0] : 0.f, c1 < 3 ? A.olo[1][c1] : 0.f,
+                                      c2 < 3 ? A.olo[2][c2] : 0.f, 0.f);
+        }
+    }
     int sq_n = 0;  // warp-uniform fill of the slow queue (always < 32 between tiles)
     WarpHist h = warp_hist(smem, SL, warp);
     zero_hist(h, SL, lane);
-    if (lane == 0) *rq_count = 0;
+    if (lane == 0) {
+        *rq_count = 0;
+        *qd_s = 0u;
+        *ev_s = 0ull;
+    }
     const int hl = lane & (SL.lane_stride - 1);
     // shared-window address of this lane's entry in row 0; a pair's table entry is its row offset
     const uint32_t cnt_s = (uint32_t)__cvta_generic_to_shared(h.e) + 4u * h.ew * hl;
     __syncthreads();
-    uint64_t evaluated = 0;
-    unsigned long long refined = 0, queued = 0;
+    unsigned long long refined = 0;
     const uint32_t ntasks = A.ntask_dev ? min(*A.ntask_dev, A.ntasks) : A.ntasks;
     uint32_t cur_cat = 0;  // catalogue whose counts the warp's histogram holds (batched counts)
     // terms a column may have taken since the last flush: per tile 32 fast-path pairs per lane
@@ -1749,44 +2021,126 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
             zil = pl.z - A.olo[2][mz + 1];
         }
         const float ax = xi + xil, ay = yi + yil, az = zi + zil;  // survey modes: the i point from the observer
-        for (uint32_t jb = T.j_begin; jb < T.j_end; jb += 32) {
-            int nj = (int)min(32u, T.j_end - jb);
-            if constexpr (LUT8) {
-                // byte table: the stage holds x[32] | y[32] | z[32] | w[32] (and the lo parts
-                // x[32] | y[32] | z[32]) so that one 16-byte shared load broadcasts a coordinate of
-                // four j points; a partial tile is padded to 32 points above kPadMin and to a
-                // multiple of 4 otherwise, with far-away points (q' = cap: the reject entry)
-                const int njp = nj > kPadMin ? 32 : ((nj + 3) & ~3);
-                float *S = (float *)sjhi, *SL8 = (float *)sjlo;
-                if (lane < njp) {
-                    float4 p = make_float4(-1e30f, -1e30f, -1e30f, 0.f), pl = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (lane < nj) {
-                        p = A.hi2[jb + lane];
-                        if (kLo) pl = A.lo2[jb + lane];
-                    }
-                    S[lane] = p.x;
-                    S[32 + lane] = p.y;
-                    S[64 + lane] = p.z;
-                    if (NEED_W) S[96 + lane] = p.w;
-                    if (kLo) {
-                        SL8[lane] = pl.x;
-                        SL8[32 + lane] = pl.y;
-                        SL8[64 + lane] = pl.z;
-                    }
-                }
-                nj = njp;
-            } else {
+        // j points: a contiguous lattice range, or (packed task) list positions of the chunk's
+        // concatenated ranges, each range with its own periodic image applied to its j points
+        const bool packed = PACKED && (T.meta & kTaskPacked) != 0;
+        const uint32_t jbeg = packed ? (T.j_end >> 11) * kJMax : T.j_begin;
+        const uint32_t jend = packed ? jbeg + (T.j_end & 2047u) + 1u : T.j_end;
+        if (lane == 0) *ev_s += (unsigned long long)icount * (jend - jbeg);
+        const bool shifted = packed && (T.meta & kTaskImages) != 0;
+        uint32_t jrc = T.j_begin;  // packed: the record holding list position jb
+        for (uint32_t jb = jbeg; jb < jend; jb += 32) {
+            int nj = (int)min(32u, jend - jb);
+            uint32_t jx = jb + (uint32_t)lane, jimg = 0;  // this lane's j point (unpacked)
+            if (packed) {
+                // records jrc .. jrc + 31 (one per lane, cut after the chunk's last record): the
+                // ranges that start inside the tile set their bit, and a lane's record is the
+                // number of those starting at or before its position
+                const JRange rec = A.jrec[jrc + lane];
+                const uint32_t lastm = __ballot_sync(0xffffffffu, (rec.z >> 31) != 0u);
+                const int nval = lastm ? __ffs(lastm) : 32;
+                const uint32_t rel = rec.y - jb;
+                const uint32_t bit = (lane > 0 && lane < nval && rel - 1u < 31u) ? (1u << rel) : 0u;
+                const uint32_t starts = __reduce_or_sync(0xffffffffu, bit);
+                const int rl = __popc(starts & (0xffffffffu >> (31 - lane)));
+                const uint32_t j0 = __shfl_sync(0xffffffffu, rec.x, rl), p0 = __shfl_sync(0xffffffffu, rec.y, rl);
+                jimg = __shfl_sync(0xffffffffu, rec.z, rl) & 63u;
+                jx = j0 + (jb + (uint32_t)lane - p0);
+                // the next tile starts in the record holding position jb + 31, or in the one after
+                const int r31 = __shfl_sync(0xffffffffu, rl, 31);
+                const uint32_t e31 = __shfl_sync(0xffffffffu, rec.w, r31);
+                jrc += (uint32_t)r31 + (e31 == jb + 32u ? 1u : 0u);
+            }
+            if constexpr (PACKED) {
+                // far-away padding: q overflows to +inf (the reject bucket, zero weight) against valid i
+                // points and against the +1e30 stand-in of lanes without an i point alike
+                float4 p = make_float4(-1e30f, -1e30f, -1e30f, 0.f), pl = make_float4(0.f, 0.f, 0.f, 0.f);
                 if (lane < nj) {
-                    sjhi[lane] = A.hi2[jb + lane];
-                    if (kLo) sjlo[lane] = A.lo2[jb + lane];
-                } else if (nj > kPadMin) {
-                    // pad a partial tile with far-away points and run it fully unrolled: q overflows
-                    // to +inf (the reject bucket, zero weight) against valid i points and against the
-                    // +1e30 stand-in of lanes without an i point alike
-                    sjhi[lane] = make_float4(-1e30f, -1e30f, -1e30f, 0.f);
-                    if (kLo) sjlo[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    p = A.hi2[jx];
+                    if (kLo) pl = A.lo2[jx];
+                    if (shifted) {
+                        // j + o for image o (exact on the grid, as i - o is)
+                        const float4 sh = shift_hi[jimg];
+                        p.x += sh.x;
+                        p.y += sh.y;
+                        p.z += sh.z;
+                        if (kLo) {
+                            const float4 sl = shift_lo[jimg];
+                            pl.x += sl.x;
+                            pl.y += sl.y;
+                            pl.z += sl.z;
+                        }
+                    }
                 }
-                if (nj > kPadMin) nj = 32;
+                if (packed) {
+                    sidx[lane] = jx;
+                    simg[lane] = (uint8_t)jimg;
+                }
+                if constexpr (LUT8) {
+                    // byte table: the stage holds x[32] | y[32] | z[32] | w[32] (and the lo parts
+                    // x[32] | y[32] | z[32]) so that one 16-byte shared load broadcasts a coordinate of
+                    // four j points; a partial tile is padded to 32 points above kPadMin and to a
+                    // multiple of 4 otherwise, with far-away points (q' = cap: the reject entry)
+                    const int njp = nj > kPadMin ? 32 : ((nj + 3) & ~3);
+                    float *S = (float *)sjhi, *SL8 = (float *)sjlo;
+                    if (lane < njp) {
+                        S[lane] = p.x;
+                        S[32 + lane] = p.y;
+                        S[64 + lane] = p.z;
+                        if (NEED_W) S[96 + lane] = p.w;
+                        if (kLo) {
+                            SL8[lane] = pl.x;
+                            SL8[32 + lane] = pl.y;
+                            SL8[64 + lane] = pl.z;
+                        }
+                    }
+                    nj = njp;
+                } else {
+                    // a partial tile above kPadMin runs fully unrolled on its padding
+                    if (lane < nj || nj > kPadMin) {
+                        sjhi[lane] = p;
+                        if (kLo) sjlo[lane] = pl;
+                    }
+                    if (nj > kPadMin) nj = 32;
+                }
+            } else {
+                if constexpr (LUT8) {
+                    // byte table: the stage holds x[32] | y[32] | z[32] | w[32] (and the lo parts
+                    // x[32] | y[32] | z[32]) so that one 16-byte shared load broadcasts a coordinate of
+                    // four j points; a partial tile is padded to 32 points above kPadMin and to a
+                    // multiple of 4 otherwise, with far-away points (q' = cap: the reject entry)
+                    const int njp = nj > kPadMin ? 32 : ((nj + 3) & ~3);
+                    float *S = (float *)sjhi, *SL8 = (float *)sjlo;
+                    if (lane < njp) {
+                        float4 p = make_float4(-1e30f, -1e30f, -1e30f, 0.f), pl = make_float4(0.f, 0.f, 0.f, 0.f);
+                        if (lane < nj) {
+                            p = A.hi2[jb + lane];
+                            if (kLo) pl = A.lo2[jb + lane];
+                        }
+                        S[lane] = p.x;
+                        S[32 + lane] = p.y;
+                        S[64 + lane] = p.z;
+                        if (NEED_W) S[96 + lane] = p.w;
+                        if (kLo) {
+                            SL8[lane] = pl.x;
+                            SL8[32 + lane] = pl.y;
+                            SL8[64 + lane] = pl.z;
+                        }
+                    }
+                    nj = njp;
+                } else {
+                    if (lane < nj) {
+                        sjhi[lane] = A.hi2[jb + lane];
+                        if (kLo) sjlo[lane] = A.lo2[jb + lane];
+                    } else if (nj > kPadMin) {
+                        // pad a partial tile with far-away points and run it fully unrolled: q overflows
+                        // to +inf (the reject bucket, zero weight) against valid i points and against the
+                        // +1e30 stand-in of lanes without an i point alike
+                        sjhi[lane] = make_float4(-1e30f, -1e30f, -1e30f, 0.f);
+                        if (kLo) sjlo[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    }
+                    if (nj > kPadMin) nj = 32;
+                }
             }
             __syncwarp();
             const float wi_s = pi.w * A.w_scale_f;
@@ -1829,14 +2183,19 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
                 if (slowbits) {
                     const int b = (int)(__float_as_uint(__uint2float_rz(slowbits)) >> 23) - 127;
                     slowbits ^= 1u << b;
+                    const int k = LUT8 ? b : nj - 1 - b;  // bit k (byte table) or n - 1 - k holds pair k
                     RefineEntry r;
                     r.i = i;
-                    r.j = jb + (uint32_t)(LUT8 ? b : nj - 1 - b);  // bit k (byte table) or n - 1 - k holds pair k
-                    r.meta = T.meta;
+                    r.j = packed ? sidx[k] : jb + (uint32_t)k;
+                    r.meta = packed ? (T.meta & ~0x3f00u) | ((uint32_t)simg[k] << 8) : T.meta;
                     sq[sq_n + __popc(want & ((1u << lane) - 1u))] = r;
                 }
                 sq_n += __popc(want);
-                queued += __popc(want);
+                if (lane == 0) {
+                    const uint32_t qd = *qd_s + (uint32_t)__popc(want);
+                    if (qd >= 0x80000000u) atomicAdd(&A.g_stats[2], (unsigned long long)qd);
+                    *qd_s = qd >= 0x80000000u ? 0u : qd;
+                }
                 __syncwarp();
                 if (sq_n >= 32) {
                     slow_batch<MODE, NEED_AVG, NEED_W, LUT8>(A, se, glo, ghi, sq + (sq_n - 32), 32, rq, rq_count, h, hl,
@@ -1851,7 +2210,6 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
                 col_terms = 0;
             }
         }
-        evaluated += (uint64_t)icount * (T.j_end - T.j_begin);
         if (A.task_clock && lane == 0) {
             A.task_clock[2 * (size_t)t] = (unsigned long long)(clock64() - t_start);
             A.task_clock[2 * (size_t)t + 1] = (blockIdx.x * (blockDim.x >> 5)) + warp;
@@ -1864,9 +2222,9 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
     flush_hist<NEED_AVG, NEED_W>(A, h, lane, cur_cat);
     for (int off = 16; off; off >>= 1) refined += __shfl_down_sync(0xffffffffu, refined, off);
     if (lane == 0) {
-        atomicAdd(&A.g_stats[0], (unsigned long long)evaluated);
+        atomicAdd(&A.g_stats[0], *ev_s);
         atomicAdd(&A.g_stats[1], refined);
-        atomicAdd(&A.g_stats[2], queued);
+        atomicAdd(&A.g_stats[2], (unsigned long long)*qd_s);
     }
 }
 
@@ -2264,25 +2622,30 @@ struct SetBufs {
 struct Workspace {
     SetBufs set[2];
     DevBuf mm, scan_tmp[4], chunk_cnt, chunk_off, chunk_begin, chunk_info, chunk_cat, ntask, task_off, tasks;
+    DevBuf recs;  // range records of packed tasks (JRange)
+    DevBuf sten;  // stencil list of the split j lattice (k_item_list)
     DevBuf res, tab;  // result block (ResView), bin tables (edges, guards, averages scale, lookup table)
     DevBuf task_clock;  // per-task timer records (only when asked for)
-    HostBuf h_small, h_tab, h_hist;
+    HostBuf h_small, h_tab, h_hist, h_sten;
 };
 
 // The result block of one run, one device allocation read back by one copy (the pinned host
 // copy has the same layout), nb = bins x catalogues:
 //   u64 cnt[nb] | f64 avg[nb] | f64 w[nb] | u64 stats[4] | u32 flags[4] | u64 oob | u64 extent
+//   | u32 recs[2]
 // stats: pairs evaluated, refined, queued; flags: [0] task counter of the pair kernel, [1] tasks
 // emitted, [2] periodic image beyond +-1, [3] work-list overflow; oob: points outside the
-// reference lattice; extent: points / weights outside a batch plan's range.
+// reference lattice; extent: points / weights outside a batch plan's range; recs[0]: range
+// records of packed tasks emitted.
 struct ResView {
     unsigned long long *cnt;
     double *avg, *w;
     unsigned long long *stats;
     uint32_t *flags;
     unsigned long long *oob, *extent;
+    uint32_t *recs;
 };
-static inline size_t res_bytes(size_t nb) { return sizeof(unsigned long long) * (3 * nb + 8); }
+static inline size_t res_bytes(size_t nb) { return sizeof(unsigned long long) * (3 * nb + 9); }
 // bytes zeroed before each pair-kernel launch: the sums, the statistics and the task counter
 static inline size_t res_zero_bytes(size_t nb) { return sizeof(unsigned long long) * (3 * nb + 4) + sizeof(uint32_t); }
 static inline ResView res_view(void *base, size_t nb)
@@ -2296,6 +2659,7 @@ static inline ResView res_view(void *base, size_t nb)
     R.flags = (uint32_t *)(u + 3 * nb + 4);
     R.oob = u + 3 * nb + 6;
     R.extent = u + 3 * nb + 7;
+    R.recs = (uint32_t *)(u + 3 * nb + 8);
     return R;
 }
 
@@ -2316,9 +2680,9 @@ static void release_workspace(Workspace &W)
     }
     for (int k = 0; k < 4; k++) release(W.scan_tmp[k]);
     DevBuf *v[] = {&W.mm, &W.chunk_cnt, &W.chunk_off, &W.chunk_begin, &W.chunk_info, &W.chunk_cat, &W.ntask,
-                   &W.task_off, &W.tasks, &W.res, &W.tab, &W.task_clock};
+                   &W.task_off, &W.tasks, &W.recs, &W.sten, &W.res, &W.tab, &W.task_clock};
     for (DevBuf *d : v) release(*d);
-    HostBuf *h[] = {&W.h_small, &W.h_tab, &W.h_hist};
+    HostBuf *h[] = {&W.h_small, &W.h_tab, &W.h_hist, &W.h_sten};
     for (HostBuf *b : h) {
         if (b->p) cudaFreeHost(b->p);
         b->p = nullptr;
@@ -2338,6 +2702,8 @@ struct Engine {
     uint32_t task_cap0 = 0;  // first work-list capacity of a call (0 = from the lattice; CF_TASK_CAPACITY)
     int precision = CF_PRECISION_FP32_REFINE;
     int byte_table = 1;  // byte bucket table for DD(r), xi and DDtheta (CF_BYTE_TABLE=0: 32-bit table)
+    int lut8_lg = 12;    // finest byte-table resolution, log2 buckets per octave (CF_BYTE_TABLE_LG)
+    bool layout_packed = false;  // the current count's FP32 pair kernel takes packed tasks
     int clock_khz = 0;   // SM clock rate (per-task timer: cycles to nanoseconds)
     // test hooks (environment, read once): CF_TEST_FAIL_ALLOC=n makes the n-th device or pinned
     // allocation of the process fail as an out-of-memory would; CF_TEST_SIGNAL=n raises SIGINT
@@ -2442,6 +2808,10 @@ static int engine_init(void)
     // other modes (for measurements; both give the same counts)
     const char *bt = getenv("CF_BYTE_TABLE");
     if (bt && atoi(bt) == 0) g_eng.byte_table = 0;
+    // CF_BYTE_TABLE_LG=<4..12> caps the byte table at 2^n buckets per octave (for measurements;
+    // every resolution gives the same counts)
+    const char *bl = getenv("CF_BYTE_TABLE_LG");
+    if (bl && atoi(bl) >= 4 && atoi(bl) <= 12) g_eng.lut8_lg = atoi(bl);
     const char *fa = getenv("CF_TEST_FAIL_ALLOC");
     if (fa && atol(fa) > 0) g_eng.fail_alloc_at = atol(fa);
     const char *ts = getenv("CF_TEST_SIGNAL");
@@ -2560,14 +2930,15 @@ static int lattice_assign_at(SetBufs &B, int64_t n, int64_t base, const T *x, co
 
 template <typename T>
 static int lattice_scatter_at(SetBufs &B, int64_t n, int64_t base, int64_t rec_base, const T *x, const T *y,
-                              const T *z, const T *w, const Geom &g, int ro_cat)
+                              const T *z, const T *w, const Geom &g, int ro_cat, SetBufs *RB = nullptr)
 {
     if (n <= 0) return EXIT_SUCCESS;
+    SetBufs &D = RB ? *RB : B;  // the record buffers (B's own unless given)
     Lattice L;
-    L.hi = (float4 *)B.hi.p + rec_base;
-    L.lo = g.write_lo ? (float4 *)B.lo.p + rec_base : nullptr;
-    L.dbl = (double4_32a *)B.dbl.p + rec_base;
-    L.ro = (int2 *)B.ro.p + rec_base;
+    L.hi = (float4 *)D.hi.p + rec_base;
+    L.lo = g.write_lo ? (float4 *)D.lo.p + rec_base : nullptr;
+    L.dbl = (double4_32a *)D.dbl.p + rec_base;
+    L.ro = (int2 *)D.ro.p + rec_base;
     L.cell_start = (uint32_t *)B.cell_start.p;
     k_scatter<T><<<grid_for(n, 256), 256, 0, g_eng.stream>>>(x, y, z, w, n, g, (const uint32_t *)B.cellid_u.p + base,
                                                             (const uint32_t *)B.fill.p + base,
@@ -2577,9 +2948,11 @@ static int lattice_scatter_at(SetBufs &B, int64_t n, int64_t base, int64_t rec_b
     return EXIT_SUCCESS;
 }
 
+// (RB: the records go to RB's buffers from record rec_base on instead of B's from base)
 template <typename T>
 static int build_lattice_at(Workspace &W, SetBufs &B, int64_t n, int64_t base, const T *x, const T *y, const T *z,
-                            const T *w, const Geom &g, uint32_t ncells, unsigned long long *oob)
+                            const T *w, const Geom &g, uint32_t ncells, unsigned long long *oob,
+                            SetBufs *RB = nullptr, int64_t rec_base = -1)
 {
     cudaStream_t st = g_eng.stream;
     // per-cell occupancy; every point gets its slot within its cell from the counting atomic
@@ -2594,7 +2967,7 @@ static int build_lattice_at(Workspace &W, SetBufs &B, int64_t n, int64_t base, c
     }
     if (lattice_assign_at<T>(B, n, base, x, y, z, g, oob) != EXIT_SUCCESS) return EXIT_FAILURE;
     if (scan_u32(W, count, (uint32_t *)B.cell_start.p, ncells, 0) != EXIT_SUCCESS) return EXIT_FAILURE;
-    return lattice_scatter_at<T>(B, n, base, base, x, y, z, w, g, -1);
+    return lattice_scatter_at<T>(B, n, base, RB ? rec_base : base, x, y, z, w, g, -1, RB);
 }
 
 static int ensure_points(SetBufs &B, int64_t n)
@@ -2625,7 +2998,7 @@ static int pair_kernel_regs_t(bool f64)
     cudaError_t rc;
     if constexpr (kHasF32<MODE>) {
         rc = f64 ? cudaFuncGetAttributes(&fa, k_pairs_f64<MODE, AVG, W>)
-                 : cudaFuncGetAttributes(&fa, k_pairs_f32<MODE, AVG, W, false>);
+                 : cudaFuncGetAttributes(&fa, k_pairs_f32<MODE, AVG, W, false, false>);
     } else {
         rc = cudaFuncGetAttributes(&fa, k_pairs_f64<MODE, AVG, W>);
     }
@@ -2696,23 +3069,24 @@ static double layout_score(const SmemLayout &c, int mode, bool avg, bool w)
 
 static SmemLayout choose_layout(int mode, bool f64, bool avg, bool w, int nedges, int nbins, int lut_n)
 {
+    const bool pk = g_eng.layout_packed && !f64;  // a count with packed tasks
     const bool dz = (mode == MODE_RPPI || mode == MODE_WP || mode == MODE_SMU || mode_is_mock(mode));
     const bool los = avg || mode_is_mock(mode);
     const bool forced = g_eng.force_ls > 0 && g_eng.force_warps > 0 && 32 * g_eng.force_warps <= pair_max_threads(mode, avg, w);
     if (!f64 && forced) {
-        const SmemLayout c = smem_layout(nedges, nbins, g_eng.force_warps, f64, lut_n, g_eng.force_ls, avg, w, dz, los);
+        const SmemLayout c = smem_layout(nedges, nbins, g_eng.force_warps, f64, lut_n, g_eng.force_ls, avg, w, dz, los, pk);
         if (c.total <= 220 * 1024) return c;
     }
     const int regs = pair_kernel_regs(mode, f64, avg, w);
     const int warps_by_regs = 65536 / (32 * ((regs + 7) / 8 * 8));
-    SmemLayout SL = smem_layout(nedges, nbins, 8, f64, lut_n, 1, avg, w, dz, los);
+    SmemLayout SL = smem_layout(nedges, nbins, 8, f64, lut_n, 1, avg, w, dz, los, pk);
     double best = -1.0;
     const int lstrides[5] = {32, 16, 8, 4, 1};
     const int max_warps = f64 ? 8 : pair_max_threads(mode, avg, w) / 32;
     const int wopts[3] = {max_warps, max_warps / 2, max_warps / 4};
     for (int li = 0; li < 5; li++) {
         for (int wi = 0; wi < 3; wi++) {
-            const SmemLayout c = smem_layout(nedges, nbins, wopts[wi], f64, lut_n, lstrides[li], avg, w, dz, los);
+            const SmemLayout c = smem_layout(nedges, nbins, wopts[wi], f64, lut_n, lstrides[li], avg, w, dz, los, pk);
             if (c.total > 220 * 1024) continue;
             int blocks = (int)(g_eng.smem_per_sm / (c.total + 1024));
             const int max_blocks_threads = 2048 / (32 * wopts[wi]);
@@ -2747,9 +3121,15 @@ static int launch_pairs_t(const PairArgs &A, bool f64, int *launched)
         if (per_sm < 1) per_sm = 1;
         kern<<<g_eng.num_sms * per_sm, threads, SL.total, g_eng.stream>>>(A, SL);
     } else if constexpr (kHasF32<MODE>) {
-        auto kern = k_pairs_f32<MODE, AVG, W, false>;
+        auto kern = k_pairs_f32<MODE, AVG, W, false, false>;
         if constexpr (MODE == MODE_R3 || MODE == MODE_THETA) {
-            if (A.lut8) kern = k_pairs_f32<MODE, AVG, W, true>;
+            if (A.lut8) kern = k_pairs_f32<MODE, AVG, W, true, false>;
+        }
+        // work lists with packed tasks (split j columns, DD(r) and xi only)
+        if constexpr (MODE == MODE_R3) {
+            if (A.jrec) kern = A.lut8 ? k_pairs_f32<MODE, AVG, W, true, true> : k_pairs_f32<MODE, AVG, W, false, true>;
+        } else {
+            if (A.jrec) CF_FAIL("internal: packed tasks for mode %d", MODE);
         }
         CF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SL.total));
         CF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, SL.total));
@@ -2893,7 +3273,7 @@ static bool build_lut8(const cf_job *J, int mode, int nbins, bool need_w, double
     memcpy(&bt, &gtop, 4);
     // buckets per octave: the finest power of two (at most 2^12) that fits kLut8Max entries from
     // bucket(b) to the cap bucket
-    int lg = 12;
+    int lg = g_eng.lut8_lg;
     while (lg > 4 && (int)((bt >> (23 - lg)) - (bb >> (23 - lg))) + 2 > kLut8Max) lg--;
     const int shift = 23 - lg;
     const int base = (int)(bb >> shift);
@@ -3121,9 +3501,12 @@ static void geom_keys(Geom &g)
     for (int a = 0; a < 3; a++) {
         g.o_hi[a] = fix_of(g.hi_origin[a], g.e_fix[a]);
         g.o_cell[a] = fix_of(g.origin[a], g.e_fix[a]);
-        // reciprocal of the cell size in fixed-point units S = s / 2^e_fix, with the largest
-        // shift k that keeps cell_mul = 2^(64+k) / S below 2^63
-        const double S = ldexp(g.s[a], -g.e_fix[a]);
+        // reciprocal of the index step in fixed-point units S = (s / cdiv) / 2^e_fix, with the
+        // largest shift k that keeps cell_mul = 2^(64+k) / S below 2^63
+        if (g.cdiv[a] < 1) g.cdiv[a] = 1;
+        if (g.tmax[a] < 1) g.tmax[a] = g.n[a] * g.cdiv[a];
+        const double sw = g.s[a] / g.cdiv[a];
+        const double S = ldexp(sw, -g.e_fix[a]);
         int k = ilogb(S) - 1;
         k = k < 0 ? 0 : (k > 63 ? 63 : k);
         const double m = ldexp(1.0, 64 + k) / S;
@@ -3131,7 +3514,7 @@ static void geom_keys(Geom &g)
         g.cell_mul[a] = m >= 0x1p64 ? ~0ull : (unsigned long long)m;
         // |cell - (x - origin)/s| <= t 2^-51 + 2^-k cells (rounding of the reciprocal, truncation)
         // plus the fixed-point rounding of x and of the origin (2^e_fix each)
-        g.eps_cell[a] = ldexp(g.s[a] * (double)g.n[a], -50) + ldexp(g.s[a], 1 - k) + ldexp(4.0, g.e_fix[a]);
+        g.eps_cell[a] = ldexp(g.s[a] * (double)g.n[a], -50) + ldexp(sw, 1 - k) + ldexp(4.0, g.e_fix[a]);
         // coordinates in [ref_min - cell / 2, ref_min + (ref_n + 1/2) cells] get a reference cell in
         // [0, ref_n] before the reference's clamp of the top cell, whatever the FP64 rounding
         const double c = 1.0 / g.ref_inv[a];
@@ -3243,9 +3626,11 @@ static int gpu_geometry(const cf_job *J, const cf_geometry &geo, const double lo
 }
 
 // Neighbour-search parameters of the work list: reach in columns and the z / 3-D limits, with
-// margins that cover the rounding of the cell assignment.
+// margins that cover the rounding of the cell assignment.  sub > 1: the geometry of the j lattice
+// whose columns split every lattice column sub x sub (offsets counted from the chunk column's
+// first split column).
 static int task_geometry(const cf_job *J, const cf_geometry &geo, const Geom &g, const double lo[3], const double hi[3],
-                         bool autocorr, int mode, TaskGeom &G)
+                         bool autocorr, int mode, TaskGeom &G, int sub = 1)
 {
     // prune margins cover the rounding of the cell assignment only (the FP32 error bounds of the
     // pair kernels matter for classification, not for which neighbours are visited)
@@ -3255,22 +3640,23 @@ static int task_geometry(const cf_job *J, const cf_geometry &geo, const Geom &g,
     const double margin_xy = 1e-9 * fmax(g.s[0], g.s[1]) + 1e-13 * maxabs_all + 2.0 * fmax(g.eps_cell[0], g.eps_cell[1]);
     const double margin_z = 1e-9 * g.s[2] + 1e-13 * maxabs_all + 2.0 * g.eps_cell[2];
     memset(&G, 0, sizeof(G));
-    G.nx = g.n[0];
-    G.ny = g.n[1];
+    G.sub = sub;
+    G.nx = g.n[0] * sub;
+    G.ny = g.n[1] * sub;
     G.nz = g.n[2];
     for (int a = 0; a < 3; a++) G.periodic[a] = geo.periodic[a] && geo.wrap[a] > 0.0;
     G.autocorr = autocorr;
     G.mode = mode;
-    G.s[0] = g.s[0];
-    G.s[1] = g.s[1];
+    G.s[0] = g.s[0] / sub;
+    G.s[1] = g.s[1] / sub;
     G.s[2] = g.s[2];
     G.rmax_xy = J->rmax_xy + margin_xy;
     G.rmax_z = J->rmax_z + margin_z;
     G.rmax_3d = J->rmax_3d > 0.0 ? J->rmax_3d + fmax(margin_xy, margin_z) : 0.0;
-    G.reach_x = (int)ceil(G.rmax_xy / g.s[0]);
-    G.reach_y = (int)ceil(G.rmax_xy / g.s[1]);
-    if (G.reach_x > 64 || G.reach_y > 64) CF_FAIL("internal: neighbour reach too large");
-    const int ny = 2 * G.reach_y + 1, ncoff = (2 * G.reach_x + 1) * ny;
+    G.reach_x = (int)ceil(G.rmax_xy / G.s[0]);
+    G.reach_y = (int)ceil(G.rmax_xy / G.s[1]);
+    if (G.reach_x > 64 * sub || G.reach_y > 64 * sub) CF_FAIL("internal: neighbour reach too large");
+    const int ny = 2 * G.reach_y + sub, ncoff = (2 * G.reach_x + sub) * ny;
     G.ntab = 0;
     if (ncoff <= kWzTab) {
         for (int c = 0; c < ncoff; c++) {
@@ -3399,6 +3785,89 @@ static void pair_constants(PairArgs &A, const cf_job *J, int mode, int nbins, bo
 
 }
 
+// Split of the j lattice's columns (1: none) and its slab merge (*zdiv), DD(r) and xi only.
+// CF_COLUMN_SPLIT=<split>[,<slab merge>] fixes them (read on every call).  Otherwise a cost model
+// in pair evaluations per i point: the j points of every window (split columns against the
+// chunk column's reach, z windows widened to whole merged slabs), padding per range, the
+// packed path's per-pair overhead, and the split lattice's extra build (cells, and for an
+// auto-correlation a second lattice of the same points).  The j lattice keeps within 2^26 cells.
+static int choose_split(const cf_job *J, const Geom &g, int64_t n1, int64_t n2, bool autocorr, int mode, int *zdiv)
+{
+    *zdiv = 1;
+    if (mode != MODE_R3) return 1;
+    const double cells_c = (double)g.n[0] * g.n[1] * g.n[2];
+    auto fits = [&](int sub, int zd) { return cells_c * sub * sub / zd <= (double)(1u << 26); };
+    const char *e = getenv("CF_COLUMN_SPLIT");
+    if (e) {
+        int sub = 1, zd = 1;
+        const int k = sscanf(e, "%d,%d", &sub, &zd);
+        if (k >= 1 && sub >= 1 && sub <= 4) {
+            if (k < 2 || !(zd == 1 || zd == 2 || zd == 4 || zd == 8)) zd = 1;
+            while (sub > 1 && !fits(sub, zd)) sub--;
+            *zdiv = sub > 1 ? zd : 1;
+            return sub;
+        }
+    }
+    const double vol = g.s[0] * g.n[0] * g.s[1] * g.n[1] * g.s[2] * g.n[2];
+    const double rho1 = (double)n1 / vol, rho2 = (double)(autocorr ? n1 : n2) / vol;
+    const double r = J->rmax_xy, rz = J->rmax_z, r3 = J->rmax_3d;
+    if (!(vol > 0.0) || !(rho1 > 0.0) || !(r > 0.0)) return 1;
+    const double Ac = g.s[0] * g.s[1];
+    const double ez = fmin(kChunk / (rho1 * Ac), g.s[2] * g.n[2]);  // a chunk's z span
+    auto reach_w = [&](double d2) {                                     // z reach at plane distance^2
+        double W = rz;
+        if (r3 > 0.0) W = fmin(W, sqrt(fmax(0.0, r3 * r3 - d2)));
+        return W;
+    };
+    const double kPad = 8.0, kItemPad = 16.0, kPackedCost = 1.12, kBuildPerPoint = 100.0, kPerCell = 7.0;
+    auto windows = [&](int sub, int zd) {  // j points per i point, padding included
+        const double sf0 = g.s[0] / sub, sf1 = g.s[1] / sub, Af = sf0 * sf1;
+        const int rx = (int)ceil(r / sf0), ry = (int)ceil(r / sf1);
+        double pts = 0.0, ranges = 0.0;
+        for (int du = -rx; du <= sub - 1 + rx; du++) {
+            for (int dv = -ry; dv <= sub - 1 + ry; dv++) {
+                const int pdx = (int)floor((double)du / sub), pdy = (int)floor((double)dv / sub);
+                const bool own = pdx == 0 && pdy == 0;
+                if (autocorr && (pdx < 0 || (pdx == 0 && pdy < 0))) continue;
+                const int gx = du < 0 ? -du - 1 : (du >= sub ? du - sub : 0);
+                const int gy = dv < 0 ? -dv - 1 : (dv >= sub ? dv - sub : 0);
+                const double d2 = (gx * sf0) * (gx * sf0) + (gy * sf1) * (gy * sf1);
+                if (d2 >= r * r) continue;
+                const double W = reach_w(d2);
+                if (autocorr && own) {
+                    // own column: forward half, from the i lattice (unsplit, unmerged slabs)
+                    pts += Af * rho2 * (ez + W);
+                    if (du == 0 && dv == 0) ranges += 1.0;
+                    continue;
+                }
+                pts += Af * rho2 * (ez + 2.0 * W + (zd - 1) * g.s[2]);
+                ranges += 1.0;
+            }
+        }
+        return sub == 1 ? pts + kPad * ranges : pts + kItemPad + (autocorr ? kPad : 0.0);
+    };
+    double best = windows(1, 1);
+    const double base = best;
+    int bsub = 1, bzd = 1;
+    for (int sub = 2; sub <= 4; sub++) {
+        for (int zd = 1; zd <= 8; zd *= 2) {
+            if (!fits(sub, zd)) continue;
+            const double cells_j = ceil((double)g.n[2] / zd) * g.n[0] * g.n[1] * sub * sub;
+            const double extra = (autocorr ? kBuildPerPoint : 0.0) +
+                                 kPerCell * (cells_j - (autocorr ? 0.0 : cells_c)) / (double)n1;
+            const double c = windows(sub, zd) * kPackedCost + extra;
+            if (c < best) {
+                best = c;
+                bsub = sub;
+                bzd = zd;
+            }
+        }
+    }
+    if (bsub > 1 && best > 0.95 * base) return 1;  // not clearly cheaper
+    *zdiv = bzd;
+    return bsub;
+}
+
 static int run_locked(cf_job *J, cf_hist *H)
 {
     Workspace &W = g_eng.ws;
@@ -3406,6 +3875,7 @@ static int run_locked(cf_job *J, cf_hist *H)
     cudaStream_t st = g_eng.stream;
     memset(&g_eng.last, 0, sizeof(g_eng.last));
     g_eng.launches = 0;
+    g_eng.layout_packed = false;
     const int mode = J->mode;
     const int nbins = mode_two_d(mode) ? J->nedges * (J->npibin + 1) : J->nedges;
     if (H->nbins != nbins) CF_FAIL("internal: histogram size mismatch (%d vs %d)", H->nbins, nbins);
@@ -3487,20 +3957,72 @@ static int run_locked(cf_job *J, cf_hist *H)
     }
     const bool f64 = g_eng.precision == CF_PRECISION_FP64 || !has_f32_path(mode) || w_exact || ref_links;
     g.write_lo = (J->need_avg != 0 || mode_is_mock(mode)) ? 1 : 0;
+    // j points from a lattice whose columns split every lattice column jsub x jsub (FP32 path):
+    // the neighbour windows then follow each chunk's sphere of reach more closely.  Both lattices
+    // take their column from the same fixed-point index (the i lattice's is that index / jsub), so
+    // a split column lies inside exactly one lattice column.
+    int zdiv = 1;
+    const int jsub = f64 ? 1 : choose_split(J, g, n1, n2, autocorr, mode, &zdiv);
+    g_eng.layout_packed = jsub > 1;  // the histogram layouts of this count (tables and launch)
+    Geom gj = g;
+    uint32_t ncells_j = ncells;
+    if (jsub > 1) {
+        // the i lattice: columns of jsub x jsub index steps; the j lattice: one column per step,
+        // slabs of zdiv i-lattice slabs (the last one possibly shorter)
+        g.cdiv[0] = g.cdiv[1] = jsub;
+        g.cdiv[2] = 1;
+        for (int a = 0; a < 3; a++) g.tmax[a] = g.n[a] * g.cdiv[a];
+        geom_keys(g);
+        gj = g;
+        for (int a = 0; a < 2; a++) {
+            gj.n[a] = g.n[a] * jsub;
+            gj.s[a] = g.s[a] / jsub;
+            gj.inv_s[a] = 1.0 / gj.s[a];
+            gj.cdiv[a] = 1;
+        }
+        gj.n[2] = (g.n[2] + zdiv - 1) / zdiv;
+        gj.s[2] = g.s[2] * zdiv;
+        gj.inv_s[2] = 1.0 / gj.s[2];
+        gj.cdiv[2] = zdiv;
+        geom_keys(gj);
+        if (autocorr) gj.check_ref_bounds = 0;  // the i lattice already checks these points
+        ncells_j = (uint32_t)gj.n[0] * (uint32_t)gj.n[1] * (uint32_t)gj.n[2];
+    }
+    const bool split_auto = autocorr && jsub > 1;  // a second lattice of the same points
     if (ensure(W.res, res_bytes(nbins)) != EXIT_SUCCESS) return EXIT_FAILURE;
     const ResView R = res_view(W.res.p, nbins);
     unsigned long long *oob = R.oob;
-    CF_CUDA(cudaMemsetAsync(R.flags, 0, sizeof(unsigned long long) * 4, st));  // flags, oob, extent
+    CF_CUDA(cudaMemsetAsync(R.flags, 0, sizeof(unsigned long long) * 5, st));  // flags, oob, extent, records
     CF_CUDA(cudaEventRecord(g_eng.ev[6], st));  // the lattice build (gridlink) proper
-    for (int s = 0; s < nsets; s++) {
-        const int64_t n = s ? n2 : n1;
-        int rc = dev_float ? build_lattice<float>(W, s, n, need_w, g, ncells, oob)
-                           : build_lattice<double>(W, s, n, need_w, g, ncells, oob);
+    // an auto-correlation's split lattice: its cells in set 2's buffers, its records after the n1
+    // records of the i lattice (set 1's buffers hold both), so that the j points of the own
+    // column and of the split columns index one array
+    if (split_auto && ensure_points(W.set[0], 2 * n1) != EXIT_SUCCESS) return EXIT_FAILURE;
+    for (int s = 0; s < nsets + (split_auto ? 1 : 0); s++) {
+        const int64_t n = (s && !autocorr) ? n2 : n1;
+        const Geom &gs = s == 1 ? gj : g;
+        const uint32_t nc = s == 1 ? ncells_j : ncells;
+        int rc;
+        if (s == 1 && autocorr) {
+            SetBufs &B1 = W.set[1];
+            if (ensure(B1.cellid_u, sizeof(uint32_t) * n1) || ensure(B1.fill, sizeof(uint32_t) * n1)) return EXIT_FAILURE;
+            const SetBufs &B0 = W.set[0];
+            rc = dev_float ? build_lattice_at<float>(W, B1, n1, 0, (const float *)B0.in[0], (const float *)B0.in[1],
+                                                     (const float *)B0.in[2], need_w ? (const float *)B0.in[3] : nullptr,
+                                                     gs, nc, oob, &W.set[0], n1)
+                           : build_lattice_at<double>(W, B1, n1, 0, (const double *)B0.in[0], (const double *)B0.in[1],
+                                                      (const double *)B0.in[2], need_w ? (const double *)B0.in[3] : nullptr,
+                                                      gs, nc, oob, &W.set[0], n1);
+        } else {
+            rc = dev_float ? build_lattice<float>(W, s, n, need_w, gs, nc, oob)
+                           : build_lattice<double>(W, s, n, need_w, gs, nc, oob);
+        }
         if (rc != EXIT_SUCCESS) return EXIT_FAILURE;
     }
     CF_CUDA(cudaEventRecord(g_eng.ev[7], st));
     SetBufs &S1 = W.set[0];
-    SetBufs &S2 = W.set[nsets - 1];
+    SetBufs &S2 = W.set[nsets - 1];                          // j records
+    SetBufs &SC = W.set[(nsets == 2 || split_auto) ? 1 : 0];  // cells of the j lattice
     Tables T;
     if (build_tables(W, J, mode, nbins, need_w, delta, &T) != EXIT_SUCCESS) return EXIT_FAILURE;
 
@@ -3509,6 +4031,43 @@ static int run_locked(cf_job *J, cf_hist *H)
     if (task_geometry(J, geo, g, lo, hi, autocorr, mode, G) != EXIT_SUCCESS) return EXIT_FAILURE;
     G.error = R.flags + 2;
     const int gap = chunk_gap(G, n1, ncols);
+    // split j columns: packed tasks over the split columns (Gj), and an auto-correlation's own
+    // column from the i lattice (Gown: the own column alone)
+    TaskGeom Gj, Gown;
+    size_t rcap = 0;
+    int nsten = 0;
+    if (jsub > 1) {
+        if (task_geometry(J, geo, g, lo, hi, autocorr, mode, Gj, jsub) != EXIT_SUCCESS) return EXIT_FAILURE;
+        Gj.error = G.error;
+        Gj.zshift = zdiv == 8 ? 3 : zdiv == 4 ? 2 : zdiv == 2 ? 1 : 0;
+        Gj.nzj = gj.n[2];
+        // the stencil list: split-column offsets within reach (an auto-correlation's forward
+        // neighbour columns only; its own column is listed from the i lattice)
+        const int wxs = 2 * Gj.reach_x + jsub, wys = 2 * Gj.reach_y + jsub;
+        if (ensure_host(W.h_sten, sizeof(int2) * (size_t)wxs * wys) != EXIT_SUCCESS ||
+            ensure(W.sten, sizeof(int2) * (size_t)wxs * wys) != EXIT_SUCCESS)
+            return EXIT_FAILURE;
+        int2 *hs = (int2 *)W.h_sten.p;
+        for (int u = 0; u < wxs; u++) {
+            for (int v = 0; v < wys; v++) {
+                const int du = u - Gj.reach_x, dv = v - Gj.reach_y;
+                if (autocorr) {
+                    const int pdx = (int)floor((double)du / jsub), pdy = (int)floor((double)dv / jsub);
+                    if (pdx < 0 || (pdx == 0 && pdy <= 0)) continue;
+                }
+                const int wz = column_wz(Gj, du, dv);
+                if (wz < 0) continue;
+                hs[nsten++] = make_int2((int)(((uint32_t)du & 0xffffu) | ((uint32_t)dv << 16)), wz);
+            }
+        }
+        if (nsten > 0) CF_CUDA(cudaMemcpyAsync(W.sten.p, hs, sizeof(int2) * nsten, cudaMemcpyHostToDevice, st));
+        Gown = G;
+        Gown.reach_x = Gown.reach_y = 0;
+        const int wz0 = column_wz(G, 0, 0);
+        Gown.wz_tab[0] = (int16_t)(wz0 > 32767 ? 32767 : wz0);
+        Gown.ntab = 1;
+        Gj.j_off = split_auto ? (uint32_t)n1 : 0u;
+    }
 
     // ---- chunks: fixed slot range (empty slots hold 0 points), no host wait ----
     const uint64_t slots = chunk_slots((uint64_t)n1, ncols, g.n[2], gap);
@@ -3540,6 +4099,19 @@ static int run_locked(cf_job *J, cf_hist *H)
     cap = W.tasks.cap / sizeof(Task);
     if (cap > 0xffffffffu) cap = 0xffffffffu;
     if (g_eng.task_cap0 > 0 && g_eng.task_cap0 < cap) cap = g_eng.task_cap0;
+    if (jsub > 1) {
+        // range records: what this lattice needed last time, else about one per split column
+        // within reach (the forward half for an auto-correlation); 32 spare records stay
+        // readable past the last (the pair kernel reads records 32 at a time)
+        const size_t ncj = (size_t)(2 * Gj.reach_x + jsub) * (2 * Gj.reach_y + jsub);
+        const size_t rguess = (size_t)max_chunks * ncj / (autocorr ? 2 : 1) + 1024;
+        rcap = W.recs.cap / sizeof(JRange);
+        rcap = rcap > 32 ? rcap - 32 : 0;
+        if (rcap < rguess) rcap = rguess;
+        if (rcap > 0xffffffffu - 32) rcap = 0xffffffffu - 32;
+        if (ensure(W.recs, sizeof(JRange) * (rcap + 32)) != EXIT_SUCCESS) return EXIT_FAILURE;
+        if (g_eng.task_cap0 > 0 && g_eng.task_cap0 < rcap) rcap = g_eng.task_cap0;
+    }
 
     // ---- pair-kernel arguments ----
     PairArgs A;
@@ -3572,16 +4144,32 @@ static int run_locked(cf_job *J, cf_hist *H)
     J->ntask_times = 0;
     for (int attempt = 0; attempt < 2; attempt++) {
         A.tasks = (const Task *)W.tasks.p;
+        A.jrec = jsub > 1 ? (const JRange *)W.recs.p : nullptr;
         A.ntasks = (uint32_t)cap;
         A.task_clock = nullptr;
         if (J->task_timer) {
             if (ensure(W.task_clock, 2 * sizeof(unsigned long long) * cap) != EXIT_SUCCESS) return EXIT_FAILURE;
             A.task_clock = (unsigned long long *)W.task_clock.p;
         }
-        k_task_list<<<task_grid(G, max_chunks), 128, 0, st>>>(G, max_chunks, (const uint32_t *)W.chunk_begin.p,
-                                                              (const uint2 *)W.chunk_info.p,
-                                                              (const uint32_t *)S2.cell_start.p, (Task *)W.tasks.p,
-                                                              (uint32_t)cap, R.flags);
+        if (jsub > 1) {
+            if (autocorr) {
+                k_task_list<<<task_grid(Gown, max_chunks), 128, 0, st>>>(
+                    Gown, max_chunks, (const uint32_t *)W.chunk_begin.p, (const uint2 *)W.chunk_info.p,
+                    (const uint32_t *)S1.cell_start.p, (Task *)W.tasks.p, (uint32_t)cap, R.flags);
+                g_eng.launches++;
+                CF_CUDA(cudaGetLastError());
+            }
+            k_item_list<<<((size_t)max_chunks * kItemLanes + 32 * kItemWarps - 1) / (32 * kItemWarps), 32 * kItemWarps,
+                          nsten <= kItemStenShared ? sizeof(int2) * nsten : 0, st>>>(
+                Gj, max_chunks, (const uint32_t *)W.chunk_begin.p, (const uint2 *)W.chunk_info.p,
+                (const uint32_t *)SC.cell_start.p, (const int2 *)W.sten.p, nsten, (Task *)W.tasks.p, (uint32_t)cap,
+                (JRange *)W.recs.p, (uint32_t)rcap, R.flags, R.recs);
+        } else {
+            k_task_list<<<task_grid(G, max_chunks), 128, 0, st>>>(G, max_chunks, (const uint32_t *)W.chunk_begin.p,
+                                                                  (const uint2 *)W.chunk_info.p,
+                                                                  (const uint32_t *)S2.cell_start.p, (Task *)W.tasks.p,
+                                                                  (uint32_t)cap, R.flags);
+        }
         g_eng.launches++;
         CF_CUDA(cudaGetLastError());
         CF_CUDA(cudaEventRecord(g_eng.ev[1], st));
@@ -3606,7 +4194,13 @@ static int run_locked(cf_job *J, cf_hist *H)
         if (ensure(W.tasks, sizeof(Task) * cap) != EXIT_SUCCESS) return EXIT_FAILURE;
         cap = W.tasks.cap / sizeof(Task);
         if (cap > 0xffffffffu) cap = 0xffffffffu;
+        if (jsub > 1) {
+            rcap = (size_t)Rh.recs[0] + 1024;
+            if (rcap > 0xffffffffu - 32) rcap = 0xffffffffu - 32;
+            if (ensure(W.recs, sizeof(JRange) * (rcap + 32)) != EXIT_SUCCESS) return EXIT_FAILURE;
+        }
         CF_CUDA(cudaMemsetAsync(R.flags + 1, 0, 3 * sizeof(uint32_t), st));  // task total, image error, overflow
+        CF_CUDA(cudaMemsetAsync(R.recs, 0, sizeof(uint32_t), st));           // records
     }
     g_eng.last.tasks = Rh.flags[1];
     if (J->task_timer && Rh.flags[1] > 0) {
@@ -3630,11 +4224,12 @@ static int run_locked(cf_job *J, cf_hist *H)
         }
         const double ns_per_cycle = g_eng.clock_khz > 0 ? 1e6 / g_eng.clock_khz : 1.0;
         for (size_t t = 0; t < nt; t++) {
+            const bool packed = (th[t].meta & kTaskPacked) != 0;
             out[t].n1 = (int64_t)(th[t].meta & 63u) + 1;
-            out[t].n2 = (int64_t)th[t].j_end - (int64_t)th[t].j_begin;
+            out[t].n2 = packed ? (int64_t)(th[t].j_end & 2047u) + 1 : (int64_t)th[t].j_end - (int64_t)th[t].j_begin;
             out[t].time_in_ns = (int64_t)((double)ch[2 * t] * ns_per_cycle);
             out[t].i_first = (int)th[t].i_begin;
-            out[t].j_first = (int)th[t].j_begin;
+            out[t].j_first = packed ? -1 : (int)th[t].j_begin;
             out[t].warp = (int)ch[2 * t + 1];
         }
         free(th);
@@ -3656,6 +4251,7 @@ static int run_locked(cf_job *J, cf_hist *H)
     g_eng.last.pairs_refined = Rh.stats[1];
     g_eng.last.pairs_slow = Rh.stats[2];
     g_eng.last.kernel_launches = g_eng.launches;
+    g_eng.last.column_split = jsub;
     return EXIT_SUCCESS;
 }
 
@@ -3923,6 +4519,7 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
 {
     *out = nullptr;
     if (engine_init() != EXIT_SUCCESS) return EXIT_FAILURE;
+    g_eng.layout_packed = false;  // batched counts take no packed tasks
     if (nbatch < 1 || nbatch > (1 << 15) - 1) CF_FAIL("batch size %d outside [1, 32767]", nbatch);
     if (tmpl->mode != MODE_R3 || tmpl->autocorr) CF_FAIL("internal: batched counts are DD cross-correlations");
     if (tmpl->elem_size != 4 && tmpl->elem_size != 8) CF_FAIL("element size must be 4 or 8");
@@ -4265,6 +4862,7 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
 
 static int batch_run_locked(BatchPlan *P, cf_hist *H)
 {
+    g_eng.layout_packed = false;  // batched counts take no packed tasks
     if (engine_init() != EXIT_SUCCESS) return EXIT_FAILURE;
     cudaStream_t st = g_eng.stream;
     CF_CUDA(cudaStreamSynchronize(st));

@@ -176,7 +176,7 @@ typedef struct {
     int blocks_per_sm;
     int warps_per_block;
     int lane_stride;
-    int reserved;
+    int column_split;
     uint64_t pairs_slow;
 } cf_engine_stats;
 int cf_engine_last_stats(cf_engine_stats *out);

@@ -378,7 +378,7 @@ typedef struct {
     int blocks_per_sm;   /* launch shape of the last pair kernel */
     int warps_per_block;
     int lane_stride;     /* lanes l and l + lane_stride share one histogram column (32 = private) */
-    int reserved;
+    int column_split;    /* j-lattice columns per lattice column and axis (1: unsplit) */
     uint64_t pairs_slow; /* pairs in flagged table buckets (exact FP32 classification) */
 } cf_gpu_stats;
 int cf_gpu_last_stats(cf_gpu_stats *out);
