@@ -57,9 +57,11 @@ WORKLOADS["survey"] = dict(workload="DDrppi_mocks auto-correlation of a syntheti
                            weights="U[0.5,1.5]", kind="survey", autocorr=1)
 WORKLOAD = dict(WORKLOADS["cfg2"])
 FLOP_PER_PAIR = 8  # 3 FADD + 1 FMUL + 2 FFMA per 3-D separation
-# dram__bytes_read.sum + dram__bytes_write.sum of one FP32 pair-kernel launch per workload, from an
-# ncu capture of this kernel on that workload (a recorded constant, not measured by this script)
-PAIR_KERNEL_TRAFFIC_BYTES = {"cfg2": 823_469_824 + 20_716_800, "northstar": 55_299_584 + 2_311_424}
+# dram__bytes_read.sum + dram__bytes_write.sum of one FP32 pair-kernel launch per workload and split
+# of the j lattice's columns (1: unsplit), from an ncu capture of this kernel on that workload (a
+# recorded constant, not measured by this script)
+PAIR_KERNEL_TRAFFIC_BYTES = {("cfg2", 4): 548_401_664 + 9_282_560, ("cfg2", 1): 823_469_824 + 20_716_800,
+                             ("northstar", 1): 55_299_584 + 2_311_424}
 TRAFFIC_SOURCE = ("ncu capture of the pair kernel on this workload (dram__bytes_read.sum + dram__bytes_write.sum "
                   "per launch): a recorded constant, not measured in this run")
 
@@ -818,7 +820,8 @@ def main():
     pair_s = sum(pair_ms) / 1e3 / args.steps
     achieved = work * FLOP_PER_PAIR / pair_s / 1e12
     achieved_eval = (evaluated / args.steps) * FLOP_PER_PAIR / pair_s / 1e12
-    traffic = PAIR_KERNEL_TRAFFIC_BYTES.get(args.workload) if args.precision == "fp32_refine" else None
+    traffic = (PAIR_KERNEL_TRAFFIC_BYTES.get((args.workload, st["column_split"]))
+               if args.precision == "fp32_refine" else None)
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": sum(gpu_ms) / args.steps, "higher_is_better": True,
@@ -843,7 +846,7 @@ def main():
                              "ms_per_step": e2e_pg_ms, "host_memory": "pageable (numpy arrays)"},
             "gpu_launches": launches,
             "launch": {"blocks_per_sm": st["blocks_per_sm"], "warps_per_block": st["warps_per_block"],
-                       "lane_stride": st["lane_stride"]},
+                       "lane_stride": st["lane_stride"], "column_split": st["column_split"]},
             "kernel_ms": {"pair_kernel": sum(pair_ms) / args.steps, "gridlink": sum(grid_ms) / args.steps,
                           "extent_worklist_and_gaps": (sum(gpu_ms) - sum(pair_ms) - sum(grid_ms)) / args.steps,
                           "step_total": sum(gpu_ms) / args.steps, "host_wall": 1e3 * sum(wall) / args.steps},
@@ -1055,9 +1058,11 @@ def northstar_record(lib, C, cf, args, torch, dev, local, peak):
         WORKLOAD.update(saved)
     return {"workload": W["workload"], "value": work * args.steps / (sum(gpu_ms) / 1e3), "unit": UNIT,
             "ms_per_step": sum(gpu_ms) / args.steps, "pair_kernel_ms": sum(pair_ms) / args.steps,
+            "column_split": st["column_split"],
             "roofline": {"bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
                          "frac": ach / peak if peak else None, "kernel": "k_pairs_f32<MODE_R3,false,false>",
-                         "traffic": PAIR_KERNEL_TRAFFIC_BYTES["northstar"], "traffic_source": TRAFFIC_SOURCE,
+                         "traffic": PAIR_KERNEL_TRAFFIC_BYTES.get(("northstar", st["column_split"])),
+                         "traffic_source": TRAFFIC_SOURCE,
                          "achieved_gpu_evaluated": ach_eval, "frac_gpu_evaluated": ach_eval / peak if peak else None,
                          "target_frac": 0.40},
             "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": 3 * 8 * W["n1"],

@@ -1971,6 +1971,8 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
     const uint32_t cnt_s = (uint32_t)__cvta_generic_to_shared(h.e) + 4u * h.ew * hl;
     __syncthreads();
     unsigned long long refined = 0;
+    // unpacked kernels count in registers; packed ones (tighter on registers) in shared memory
+    unsigned long long evaluated = 0, queued = 0;
     const uint32_t ntasks = A.ntask_dev ? min(*A.ntask_dev, A.ntasks) : A.ntasks;
     uint32_t cur_cat = 0;  // catalogue whose counts the warp's histogram holds (batched counts)
     // terms a column may have taken since the last flush: per tile 32 fast-path pairs per lane
@@ -2026,7 +2028,11 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
         const bool packed = PACKED && (T.meta & kTaskPacked) != 0;
         const uint32_t jbeg = packed ? (T.j_end >> 11) * kJMax : T.j_begin;
         const uint32_t jend = packed ? jbeg + (T.j_end & 2047u) + 1u : T.j_end;
-        if (lane == 0) *ev_s += (unsigned long long)icount * (jend - jbeg);
+        if constexpr (PACKED) {
+            if (lane == 0) *ev_s += (unsigned long long)icount * (jend - jbeg);
+        } else {
+            evaluated += (unsigned long long)icount * (jend - jbeg);
+        }
         const bool shifted = packed && (T.meta & kTaskImages) != 0;
         uint32_t jrc = T.j_begin;  // packed: the record holding list position jb
         for (uint32_t jb = jbeg; jb < jend; jb += 32) {
@@ -2191,10 +2197,14 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
                     sq[sq_n + __popc(want & ((1u << lane) - 1u))] = r;
                 }
                 sq_n += __popc(want);
-                if (lane == 0) {
-                    const uint32_t qd = *qd_s + (uint32_t)__popc(want);
-                    if (qd >= 0x80000000u) atomicAdd(&A.g_stats[2], (unsigned long long)qd);
-                    *qd_s = qd >= 0x80000000u ? 0u : qd;
+                if constexpr (PACKED) {
+                    if (lane == 0) {
+                        const uint32_t qd = *qd_s + (uint32_t)__popc(want);
+                        if (qd >= 0x80000000u) atomicAdd(&A.g_stats[2], (unsigned long long)qd);
+                        *qd_s = qd >= 0x80000000u ? 0u : qd;
+                    }
+                } else {
+                    queued += __popc(want);
                 }
                 __syncwarp();
                 if (sq_n >= 32) {
@@ -2222,9 +2232,9 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
     flush_hist<NEED_AVG, NEED_W>(A, h, lane, cur_cat);
     for (int off = 16; off; off >>= 1) refined += __shfl_down_sync(0xffffffffu, refined, off);
     if (lane == 0) {
-        atomicAdd(&A.g_stats[0], *ev_s);
+        atomicAdd(&A.g_stats[0], evaluated + *ev_s);
         atomicAdd(&A.g_stats[1], refined);
-        atomicAdd(&A.g_stats[2], (unsigned long long)*qd_s);
+        atomicAdd(&A.g_stats[2], queued + (unsigned long long)*qd_s);
     }
 }
 
@@ -3796,7 +3806,14 @@ static int choose_split(const cf_job *J, const Geom &g, int64_t n1, int64_t n2, 
     *zdiv = 1;
     if (mode != MODE_R3) return 1;
     const double cells_c = (double)g.n[0] * g.n[1] * g.n[2];
-    auto fits = [&](int sub, int zd) { return cells_c * sub * sub / zd <= (double)(1u << 26); };
+    // the j lattice within 2^26 cells, and its range records (at most one per chunk and split
+    // column within reach, 16 bytes each) within 2 GB
+    const double chunks = (double)n1 / kChunk + (double)g.n[0] * g.n[1];
+    auto fits = [&](int sub, int zd) {
+        const double rx = ceil(J->rmax_xy * sub / g.s[0]), ry = ceil(J->rmax_xy * sub / g.s[1]);
+        const double recs = chunks * (2.0 * rx + sub) * (2.0 * ry + sub) * (autocorr ? 0.5 : 1.0) * 16.0;
+        return cells_c * sub * sub / zd <= (double)(1u << 26) && recs <= 2.0 * (1u << 30);
+    };
     const char *e = getenv("CF_COLUMN_SPLIT");
     if (e) {
         int sub = 1, zd = 1;
