@@ -1014,6 +1014,35 @@ def float32_variant(counter, f1, f2, work, args, torch, dev, local):
             "clocks": clocks.summary(), "_npairs": ref, "_weightavg": wavg}
 
 
+def split_form(counter, step, ref, work, peak, steps, torch, dev, split="4,2"):
+    """The same count with the j lattice's columns split (CF_COLUMN_SPLIT, read on every call):
+    its pair kernel and device step beside the unsplit form the cost model chose."""
+    old = os.environ.get("CF_COLUMN_SPLIT")
+    os.environ["CF_COLUMN_SPLIT"] = split
+    try:
+        for _ in range(3):
+            npairs, _w, st = step()
+            flush_l2(torch, dev)
+        pm, sm = [], []
+        for _ in range(steps):
+            npairs, _w, st = step()
+            if not np.array_equal(npairs, ref):
+                raise RuntimeError("split columns changed the counts")
+            pm.append(st["pair_kernel_ms"])
+            sm.append(st["total_gpu_ms"])
+            flush_l2(torch, dev)
+    finally:
+        if old is None:
+            os.environ.pop("CF_COLUMN_SPLIT", None)
+        else:
+            os.environ["CF_COLUMN_SPLIT"] = old
+    pair_s = sum(pm) / 1e3 / steps
+    ach = work * FLOP_PER_PAIR / pair_s / 1e12
+    return {"column_split": st["column_split"], "slab_merge": int(split.split(",")[1]),
+            "pair_kernel_ms": sum(pm) / steps, "step_ms": sum(sm) / steps, "npairs_equal": True,
+            "gpu_evaluated": st["pairs_evaluated"], "roofline_frac": ach / peak if peak else None}
+
+
 def northstar_record(lib, C, cf, args, torch, dev, local, peak):
     """1,000,000 uniform points, periodic L = 420, DD auto-correlation, 20 log bins 0.1-25:
     device throughput, its FP32 roofline fraction, end to end, and the FP64 form."""
@@ -1049,6 +1078,7 @@ def northstar_record(lib, C, cf, args, torch, dev, local, peak):
             pair_s = sum(pair_ms) / 1e3 / args.steps
             ach = work * FLOP_PER_PAIR / pair_s / 1e12
             ach_eval = evaluated / args.steps * FLOP_PER_PAIR / pair_s / 1e12
+            split = split_form(counter, lambda: counter.device(d, d), ref, work, peak, args.steps, torch, dev)
             hs = [torch.from_numpy(a).pin_memory().numpy() for a in s]
             e2e_v, e2e_ms = end_to_end(counter, hs, hs, ref, work, 1, args.steps, torch, dev)
             f64 = fp64_form(counter, cf, lambda: counter.device(d, d), ref, args.precision,
@@ -1068,6 +1098,7 @@ def northstar_record(lib, C, cf, args, torch, dev, local, peak):
             "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": 3 * 8 * W["n1"],
                     "d2h_bytes_per_step": (W["nbins"] + 1) * 32, "ms_per_step": e2e_ms, "host_memory": "pinned"},
             "fp64_form": f64,
+            "split_form": split,
             "pairs": {"reference_lattice_candidates": work, "gpu_evaluated": evaluated // args.steps,
                       "counted": int(np.sum(ref))},
             "clocks": clocks.summary()}

@@ -26,6 +26,17 @@ def get_precision():
     return {0: "fp32_refine", 1: "fp64"}[library().cf_gpu_get_precision()]
 
 
+def set_autotune(on):
+    """Single-count autotuner for DD(r) and xi: the first count of each shape times the splits of
+    the j lattice's columns and later counts of that shape use the fastest (counts are identical
+    for every split).  Off by default; turning it off forgets the shapes."""
+    library().cf_gpu_set_autotune(1 if on else 0)
+
+
+def get_autotune():
+    return bool(library().cf_gpu_get_autotune())
+
+
 def last_stats():
     """Kernel statistics of the most recent call (CUDA-event times, pairs evaluated/refined)."""
     import ctypes

@@ -144,6 +144,8 @@ _PROTOS = {
 _GPU_PROTOS = {
     "cf_gpu_set_precision": ([c_int], c_int),
     "cf_gpu_get_precision": ([], c_int),
+    "cf_gpu_set_autotune": ([c_int], c_int),
+    "cf_gpu_get_autotune": ([], c_int),
 }
 
 

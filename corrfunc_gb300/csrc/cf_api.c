@@ -1998,6 +1998,10 @@ int cf_gpu_set_precision(int mode) { return cf_engine_set_precision(mode); }
 
 int cf_gpu_get_precision(void) { return cf_engine_get_precision(); }
 
+int cf_gpu_set_autotune(int on) { return cf_engine_set_autotune(on); }
+
+int cf_gpu_get_autotune(void) { return cf_engine_get_autotune(); }
+
 int cf_gpu_last_stats(cf_gpu_stats *out)
 {
     if (out == NULL) return EXIT_FAILURE;

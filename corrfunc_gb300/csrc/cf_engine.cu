@@ -2714,6 +2714,15 @@ struct Engine {
     int byte_table = 1;  // byte bucket table for DD(r), xi and DDtheta (CF_BYTE_TABLE=0: 32-bit table)
     int lut8_lg = 12;    // finest byte-table resolution, log2 buckets per octave (CF_BYTE_TABLE_LG)
     bool layout_packed = false;  // the current count's FP32 pair kernel takes packed tasks
+    // single-count autotuner (cf_engine_set_autotune): per count shape, the fastest j-lattice
+    // column split found by timing the candidates on the first count of that shape
+    int autotune = 0;
+    int tune_force = 0, tune_zdiv = 1;  // split forced for the count being run (0: none)
+    struct TuneEntry {
+        unsigned long long key;
+        int split, zdiv;
+    } tune[32];
+    int ntune = 0, tune_next = 0;
     int clock_khz = 0;   // SM clock rate (per-task timer: cycles to nanoseconds)
     // test hooks (environment, read once): CF_TEST_FAIL_ALLOC=n makes the n-th device or pinned
     // allocation of the process fail as an out-of-memory would; CF_TEST_SIGNAL=n raises SIGINT
@@ -3814,6 +3823,13 @@ static int choose_split(const cf_job *J, const Geom &g, int64_t n1, int64_t n2, 
         const double recs = chunks * (2.0 * rx + sub) * (2.0 * ry + sub) * (autocorr ? 0.5 : 1.0) * 16.0;
         return cells_c * sub * sub / zd <= (double)(1u << 26) && recs <= 2.0 * (1u << 30);
     };
+    if (g_eng.tune_force > 0) {  // the autotuner's candidate or its choice
+        int sub = g_eng.tune_force;
+        const int zd = g_eng.tune_zdiv;
+        while (sub > 1 && !fits(sub, zd)) sub--;
+        *zdiv = sub > 1 ? zd : 1;
+        return sub;
+    }
     const char *e = getenv("CF_COLUMN_SPLIT");
     if (e) {
         int sub = 1, zd = 1;
@@ -5168,14 +5184,99 @@ static int vpf_locked(const cf_vpf_job *J, uint64_t *pN)
 
 }  // namespace
 
+// Shape of a count for the autotuner: everything but the coordinate values (sizes, mode,
+// options, the reference-lattice rule, radii and bin edges), FNV-1a over their bytes.
+static unsigned long long tune_key(const cf_job *J)
+{
+    unsigned long long h = 1469598103934665603ull;
+    auto mix = [&](const void *p, size_t n) {
+        const unsigned char *c = (const unsigned char *)p;
+        for (size_t k = 0; k < n; k++) h = (h ^ c[k]) * 1099511628211ull;
+    };
+    const int ints[7] = {J->mode, J->autocorr, J->elem_size, J->need_avg, J->need_weight, J->nedges, J->npibin};
+    mix(ints, sizeof(ints));
+    mix(&J->n1, sizeof(J->n1));
+    mix(&J->n2, sizeof(J->n2));
+    mix(&J->rule.kind, sizeof(J->rule.kind));
+    mix(&J->rule.periodic, sizeof(J->rule.periodic));
+    mix(J->rule.boxsize, sizeof(J->rule.boxsize));
+    mix(J->rule.refine, sizeof(J->rule.refine));
+    const double radii[3] = {J->rmax_xy, J->rmax_z, J->rmax_3d};
+    mix(radii, sizeof(radii));
+    mix(J->edges, sizeof(double) * (size_t)(J->nedges > 0 ? J->nedges : 0));
+    return h;
+}
+
+// A count under the autotuner: the first count of a shape runs with each j-lattice column split
+// (1, 2, 3, 4; slabs merged in pairs when split) twice, keeps the split whose second device time
+// is the shortest for later counts of that shape, and returns the results of a run with it.
+static int run_tuned(cf_job *J, cf_hist *H)
+{
+    const unsigned long long key = tune_key(J);
+    int split = 0, zdiv = 1;
+    for (int k = 0; k < g_eng.ntune; k++) {
+        if (g_eng.tune[k].key == key) {
+            split = g_eng.tune[k].split;
+            zdiv = g_eng.tune[k].zdiv;
+        }
+    }
+    int rc = EXIT_SUCCESS;
+    if (split == 0) {
+        const int cand[4][2] = {{1, 1}, {2, 2}, {3, 2}, {4, 2}};
+        double best = INFINITY;
+        int last = 0;
+        for (int c = 0; c < 4 && rc == EXIT_SUCCESS; c++) {
+            g_eng.tune_force = cand[c][0];
+            g_eng.tune_zdiv = cand[c][1];
+            for (int rep = 0; rep < 2 && rc == EXIT_SUCCESS; rep++) rc = run_locked(J, H);
+            if (rc != EXIT_SUCCESS || g_eng.last.column_split != cand[c][0]) continue;  // not allowed here
+            last = cand[c][0];
+            if (g_eng.last.total_gpu_ms < best) {
+                best = g_eng.last.total_gpu_ms;
+                split = cand[c][0];
+                zdiv = cand[c][1];
+            }
+        }
+        g_eng.tune_force = 0;
+        if (rc != EXIT_SUCCESS) return rc;
+        if (split == 0) split = 1;
+        auto &E = g_eng.tune[g_eng.tune_next];
+        E.key = key;
+        E.split = split;
+        E.zdiv = zdiv;
+        g_eng.tune_next = (g_eng.tune_next + 1) % 32;
+        if (g_eng.ntune < 32) g_eng.ntune++;
+        if (last == split) return EXIT_SUCCESS;  // H holds the chosen form's results
+    }
+    g_eng.tune_force = split;
+    g_eng.tune_zdiv = zdiv;
+    rc = run_locked(J, H);
+    g_eng.tune_force = 0;
+    return rc;
+}
+
 extern "C" int cf_engine_run(cf_job *job, cf_hist *out)
 {
     pthread_mutex_lock(&g_lock);
     InterruptGuard guard;
-    const int rc = run_locked(job, out);
+    // the autotuner covers the FP32 path of DD(r) and xi (the counts with split j columns)
+    const bool tuned = g_eng.autotune && job->mode == MODE_R3 && g_eng.precision == CF_PRECISION_FP32_REFINE &&
+                       !job->task_timer;
+    const int rc = tuned ? run_tuned(job, out) : run_locked(job, out);
     pthread_mutex_unlock(&g_lock);
     return rc;
 }
+
+extern "C" int cf_engine_set_autotune(int on)
+{
+    pthread_mutex_lock(&g_lock);
+    g_eng.autotune = on ? 1 : 0;
+    if (!on) g_eng.ntune = g_eng.tune_next = 0;  // forget the shapes
+    pthread_mutex_unlock(&g_lock);
+    return EXIT_SUCCESS;
+}
+
+extern "C" int cf_engine_get_autotune(void) { return g_eng.autotune; }
 
 extern "C" int cf_engine_vpf(const cf_vpf_job *job, uint64_t *pN)
 {

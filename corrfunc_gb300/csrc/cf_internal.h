@@ -162,6 +162,8 @@ typedef struct {
 int cf_engine_vpf(const cf_vpf_job *J, uint64_t *pN);
 
 int cf_engine_set_precision(int mode);
+int cf_engine_set_autotune(int on);
+int cf_engine_get_autotune(void);
 int cf_engine_get_precision(void);
 
 typedef struct {

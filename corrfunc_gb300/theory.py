@@ -413,6 +413,44 @@ def wp(*args, **kwargs):
     return run_wp(C.library(), *args, **kwargs)
 
 
+def find_fastest_wp_bin_refs(boxsize, pimax, nthreads, binfile, X, Y, Z, verbose=False, output_rpavg=False,
+                             max_cells_per_dim=100, isa="fastest", maxbinref=3, nrepeats=3, return_runtimes=False):
+    """The combination of bin refine factors (1 .. maxbinref per axis) with the shortest mean wp
+    runtime over nrepeats calls, as Corrfunc/theory/wp.py:17-216 finds it: returns (nx, ny, nz),
+    and with return_runtimes also the structured array of every combination's nx, ny, nz,
+    avg_time and sigma_time (seconds of the call).  Here the refine factors only define the
+    reference lattice whose cell pairs the counts follow, not the GPU's own lattice, so the
+    runtimes come out close to one another; ``corrfunc_gb300.set_autotune`` tunes the GPU's
+    lattice instead (DD and xi)."""
+    import itertools
+    import time
+    refs = range(1, int(maxbinref) + 1)
+    dtype = np.dtype([("nx", np.int64), ("ny", np.int64), ("nz", np.int64), ("avg_time", np.float64),
+                      ("sigma_time", np.float64)])
+    runtimes = np.zeros(int(maxbinref) ** 3, dtype=dtype)
+    runtimes["avg_time"] = runtimes["sigma_time"] = np.inf
+    for k, (nx, ny, nz) in enumerate(itertools.product(refs, refs, refs)):
+        total = total_sq = 0.0
+        for _ in range(int(nrepeats)):
+            t0 = time.time()
+            wp(boxsize, pimax, nthreads, binfile, X, Y, Z, verbose=verbose, output_rpavg=output_rpavg,
+               xbin_refine_factor=nx, ybin_refine_factor=ny, zbin_refine_factor=nz,
+               max_cells_per_dim=max_cells_per_dim, isa=isa)
+            dt = time.time() - t0
+            total += dt
+            total_sq += dt * dt
+        avg = total / nrepeats
+        sigma = np.sqrt(max(total_sq / nrepeats - avg * avg, 0.0))
+        runtimes[k] = (nx, ny, nz, avg, sigma)
+        if verbose:
+            print("nx = {0} ny = {1} nz = {2} avg time = {3:0.3g} sec".format(nx, ny, nz, avg))
+    best = runtimes[np.argmin(runtimes["avg_time"])]
+    best = (int(best["nx"]), int(best["ny"]), int(best["nz"]))
+    if return_runtimes:
+        return best, runtimes
+    return best
+
+
 def xi(*args, **kwargs):
     """3-D correlation function xi(r) in a periodic box; see Corrfunc.theory.xi."""
     return run_xi(C.library(), *args, **kwargs)

@@ -364,6 +364,15 @@ int64_t read_columns_into_array(const char *filename, const char *format, const 
 int cf_gpu_set_precision(int mode);
 int cf_gpu_get_precision(void);
 
+/* Single-count autotuner (off by default; the GPU's counterpart of the reference's
+ * find_fastest_wp_bin_refs, Corrfunc/theory/wp.py:17): with it on, the first DD(r) / xi count of
+ * each shape (sizes, mode, options, box, radii, bin edges) in this process runs with each split of
+ * the j lattice's columns (1-4) twice and keeps the split with the shortest device time for the
+ * later counts of that shape (up to 32 shapes); counts are identical for every split.  Turning it
+ * off forgets the shapes.  No reference counterpart in the C API. */
+int cf_gpu_set_autotune(int on);
+int cf_gpu_get_autotune(void);
+
 /* Kernel statistics of the last call on this thread (for benchmarking): pair-kernel time
  * measured with CUDA events, lattice-build time, and the number of evaluated / refined pairs. */
 typedef struct {

@@ -381,3 +381,14 @@ def test_reference_header_and_library_names_build(tmp_path, lib):
     else:
         assert r.returncode == 1
         assert "no CUDA device" in r.stderr or "corrfunc_gb300" in r.stderr
+
+
+def test_autotune_switch_needs_no_gpu():
+    """The single-count autotuner's switch is host state: set, read back and cleared without a
+    GPU."""
+    import corrfunc_gb300
+    lib = corrfunc_gb300.library()
+    assert lib.cf_gpu_get_autotune() == 0
+    assert lib.cf_gpu_set_autotune(1) == 0 and lib.cf_gpu_get_autotune() == 1
+    assert lib.cf_gpu_set_autotune(0) == 0 and lib.cf_gpu_get_autotune() == 0
+

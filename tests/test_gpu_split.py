@@ -149,3 +149,36 @@ def test_split_work_list_resize(gpu, monkeypatch, tmp_path):
     np.testing.assert_allclose([float(v) for v in lines[1].split()], want["ravg"], rtol=1e-12, atol=1e-15)
     tasks, split = (int(v) for v in lines[2].split())
     assert tasks > 100 and split == 3
+
+
+def test_autotune_keeps_counts_and_reuses_its_choice(gpu):
+    """The single-count autotuner: the first count of a shape times the splits and returns the
+    same counts as an untuned count; the second count of that shape runs with the kept split."""
+    from corrfunc_gb300 import theory
+    x, y, z = _uniform(30000, 100.0, 21)
+    bins = np.logspace(-1, np.log10(12.0), 12)
+    gpu.set_autotune(False)
+    want = theory.DD(1, 1, bins, x, y, z, periodic=True, boxsize=100.0, output_ravg=True)
+    gpu.set_autotune(True)
+    try:
+        assert gpu.get_autotune()
+        got1 = theory.DD(1, 1, bins, x, y, z, periodic=True, boxsize=100.0, output_ravg=True)
+        s1 = gpu.last_stats()["column_split"]
+        got2 = theory.DD(1, 1, bins, x, y, z, periodic=True, boxsize=100.0, output_ravg=True)
+        s2 = gpu.last_stats()["column_split"]
+    finally:
+        gpu.set_autotune(False)
+    assert 1 <= s1 <= 4 and s2 == s1
+    _compare(got1, want, 1e-6)
+    _compare(got2, got1, 0.0)
+
+
+def test_find_fastest_wp_bin_refs(gpu):
+    from corrfunc_gb300 import theory
+    x, y, z = _uniform(5000, 100.0, 23)
+    best, runtimes = theory.find_fastest_wp_bin_refs(100.0, 20.0, 1, np.logspace(-1, 1, 8), x, y, z, maxbinref=2,
+                                                     nrepeats=1, return_runtimes=True)
+    assert len(runtimes) == 8 and np.all(np.isfinite(runtimes["avg_time"]))
+    assert all(1 <= v <= 2 for v in best)
+    k = np.argmin(runtimes["avg_time"])
+    assert best == (runtimes["nx"][k], runtimes["ny"][k], runtimes["nz"][k])
