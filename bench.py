@@ -60,8 +60,8 @@ FLOP_PER_PAIR = 8  # 3 FADD + 1 FMUL + 2 FFMA per 3-D separation
 # dram__bytes_read.sum + dram__bytes_write.sum of one FP32 pair-kernel launch per workload and split
 # of the j lattice's columns (1: unsplit), from an ncu capture of this kernel on that workload (a
 # recorded constant, not measured by this script)
-PAIR_KERNEL_TRAFFIC_BYTES = {("cfg2", 4): 548_401_664 + 9_282_560, ("cfg2", 1): 823_469_824 + 20_716_800,
-                             ("northstar", 1): 55_299_584 + 2_311_424}
+PAIR_KERNEL_TRAFFIC_BYTES = {("cfg2", 1): 828_822_272 + 20_995_072, ("cfg2", 4): 548_401_664 + 9_282_560,
+                             ("northstar", 1): 55_237_120 + 1_390_848}
 TRAFFIC_SOURCE = ("ncu capture of the pair kernel on this workload (dram__bytes_read.sum + dram__bytes_write.sum "
                   "per launch): a recorded constant, not measured in this run")
 

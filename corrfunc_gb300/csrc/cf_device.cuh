@@ -98,6 +98,10 @@ struct PairArgs {
     int lut8;
     float q_bias, q_cap;        // b, cap
     float q_cap2;               // cap of lanes 16-31: the bucket after cap (entry: the second trash row)
+    // box pruning of the byte-table kernels (0: off): a j point whose FP32 squared distance to the
+    // bounding box of a chunk's points exceeds this pairs with none of them in range (the top
+    // edge's separation plus four coordinate error bounds, and 1e-5 relative, squared, rounded up)
+    float prune_r2;
     uint32_t lut8_base;         // bits(b) >> lut_shift (bucket 0)
     uint32_t half_row;          // half the bytes of a histogram row (entry * half_row = row offset)
     uint32_t trash_e;           // entry of a rejected pair (2 * trash row)

@@ -1138,6 +1138,7 @@ struct SmemLayout {
     int entry_words;  // 32-bit words per histogram entry: count [, avg hi, avg lo] [, w hi, w lo]
     size_t edges_off, guard_off, ascale_off, lut_off, stage_off, hist_off, per_warp_hist, per_warp_stage, total;
     size_t shift_off;  // FP32 kernels: periodic shifts of j points by image code (hi then lo, 64 float4 each)
+    bool extras;       // the per-warp stage holds staged j indices, image codes and a box (packed or pruned tiles)
     size_t wd_off, per_warp_wd;  // FP64 kernel with weights: one double weight sum per row and warp
 };
 
@@ -1162,7 +1163,7 @@ constexpr int kColumnTerms = 1 << 15;
 
 __host__ __device__ inline SmemLayout smem_layout(int nedges, int nbins, int warps, bool f64, int lut_n, int lane_stride,
                                                   bool need_avg, bool need_w, bool store_dz, bool lo_stage,
-                                                  bool packed = false)
+                                                  bool packed = false, bool prune = false)
 {
     SmemLayout L;
     L.need_avg = need_avg;
@@ -1189,13 +1190,15 @@ __host__ __device__ inline SmemLayout smem_layout(int nedges, int nbins, int war
     o = align_up(o + (f64 || !packed ? 0 : 2 * 64 * sizeof(float4)), 16);
     L.stage_off = o;
     // f32: float4 hi[32] + float4 lo[32] + refine and slow queues + queue fill and counters (16
-    // bytes) + (packed tasks) the lattice index and image code of every staged j point (the lo
-    // half is laid out even where it stays unused: the histogram layouts were measured with it);
+    // bytes) + the lattice index and image code of every staged j point (packed or pruned tiles)
+    // + the chunk's bounding box (pruned tiles) (the lo half is laid out even where it stays
+    // unused: the histogram layouts were measured with it);
     // f64: double4_32a[32] + int rc[32] + int orig[32]
     (void)lo_stage;
+    L.extras = !f64 && (packed || prune);
     L.per_warp_stage = f64 ? (32 * sizeof(double4_32a) + 64 * sizeof(int))
                            : (64 * sizeof(float4) + (kRefineQueue + kSlowQueue) * sizeof(RefineEntry) + 16 +
-                              (packed ? 32 * sizeof(uint32_t) + 32 : 0));
+                              (packed || prune ? 32 * sizeof(uint32_t) + 32 + 2 * sizeof(float4) : 0));
     o = align_up(o + L.per_warp_stage * warps, 16);
     L.hist_off = o;
     L.per_warp_hist = align_up((size_t)L.nrows * lane_stride * 4 * L.entry_words + 32, 16);
@@ -1947,6 +1950,9 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
     unsigned long long *ev_s = (unsigned long long *)((unsigned char *)rq_count + 8);
     uint32_t *sidx = (uint32_t *)((unsigned char *)rq_count + 16);  // packed tasks: staged j points'
     uint8_t *simg = (uint8_t *)(sidx + 32);                          // lattice indices and image codes
+    float4 *sbox = (float4 *)(simg + 32);  // pruned tiles: the chunk's box (lo, prune radius^2), (hi, -)
+    // box pruning: unpacked byte-table kernels (DD(r), xi, DDtheta)
+    constexpr bool kPrune = LUT8 && !PACKED;
     // periodic shift of a j point by image code (bits 0-5 as Task::meta bits 8-13)
     float4 *shift_hi = (float4 *)(smem + SL.shift_off), *shift_lo = shift_hi + 64;
     if constexpr (PACKED) {
@@ -2030,13 +2036,91 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
         const uint32_t jend = packed ? jbeg + (T.j_end & 2047u) + 1u : T.j_end;
         if constexpr (PACKED) {
             if (lane == 0) *ev_s += (unsigned long long)icount * (jend - jbeg);
-        } else {
-            evaluated += (unsigned long long)icount * (jend - jbeg);
+        } else if (!(kPrune && !own && A.prune_r2 > 0.f && SL.extras)) {
+            evaluated += (unsigned long long)icount * (jend - jbeg);  // pruned tasks count per tile
         }
         const bool shifted = packed && (T.meta & kTaskImages) != 0;
         uint32_t jrc = T.j_begin;  // packed: the record holding list position jb
-        for (uint32_t jb = jbeg; jb < jend; jb += 32) {
+        // Box pruning (unpacked byte-table tasks but the own column's): a j point farther than the
+        // prune radius (the top edge's separation plus the coordinate error bounds) from the
+        // chunk's bounding box pairs with none of its points in range, so it is never staged;
+        // the points kept fill whole tiles across the task's candidates.
+        const bool prune = kPrune && !own && A.prune_r2 > 0.f && SL.extras;
+        if (prune) {
+            // the box of the valid lanes' (image-shifted) points, by order-preserving integer keys
+            auto key = [](float v) { const int b = __float_as_int(v); return b ^ ((b >> 31) & 0x7fffffff); };
+            auto val = [](int k) { return __int_as_float(k ^ ((k >> 31) & 0x7fffffff)); };
+            const int big = 0x7f800000, small = (int)0x80800000;  // keys of +inf, -inf
+            const float bxl = val(__reduce_min_sync(0xffffffffu, ivalid ? key(xi) : big));
+            const float byl = val(__reduce_min_sync(0xffffffffu, ivalid ? key(yi) : big));
+            const float bzl = val(__reduce_min_sync(0xffffffffu, ivalid ? key(zi) : big));
+            const float bxh = val(__reduce_max_sync(0xffffffffu, ivalid ? key(xi) : small));
+            const float byh = val(__reduce_max_sync(0xffffffffu, ivalid ? key(yi) : small));
+            const float bzh = val(__reduce_max_sync(0xffffffffu, ivalid ? key(zi) : small));
+            if (lane == 0) {
+                sbox[0] = make_float4(bxl, byl, bzl, A.prune_r2);
+                sbox[1] = make_float4(bxh, byh, bzh, 0.f);
+            }
+            __syncwarp();
+        }
+        for (uint32_t jb = jbeg; jb < jend;) {
+            const uint32_t tile_j0 = jb;  // unpruned: the tile's first j point
             int nj = (int)min(32u, jend - jb);
+            if (prune) {
+                // rounds of 32 candidates until 32 points are staged or the range ends; a round
+                // that overfills the stage takes its first kept points and the next round starts
+                // after the last one taken
+                const float4 b0 = sbox[0], b1 = sbox[1];
+                float *S = (float *)sjhi, *SL8 = (float *)sjlo;
+                int f = 0;
+                while (f < 32 && jb < jend) {
+                    const uint32_t nc = min(32u, jend - jb);
+                    float4 p = make_float4(0.f, 0.f, 0.f, 0.f), pl = p;
+                    bool keep = false;
+                    if ((uint32_t)lane < nc) {
+                        p = A.hi2[jb + lane];
+                        const float dx = fmaxf(0.f, fmaxf(b0.x - p.x, p.x - b1.x));
+                        const float dy = fmaxf(0.f, fmaxf(b0.y - p.y, p.y - b1.y));
+                        const float dz = fmaxf(0.f, fmaxf(b0.z - p.z, p.z - b1.z));
+                        keep = fmaf(dz, dz, fmaf(dy, dy, dx * dx)) <= b0.w;
+                        if (kLo && keep) pl = A.lo2[jb + lane];
+                    }
+                    const uint32_t m = __ballot_sync(0xffffffffu, keep);
+                    const int room = 32 - f;
+                    const int rank = __popc(m & ((1u << lane) - 1u));
+                    const uint32_t taken = __ballot_sync(0xffffffffu, keep && rank < room);
+                    if (keep && rank < room) {
+                        const int pos = f + rank;
+                        S[pos] = p.x;
+                        S[32 + pos] = p.y;
+                        S[64 + pos] = p.z;
+                        if (NEED_W) S[96 + pos] = p.w;
+                        if (kLo) {
+                            SL8[pos] = pl.x;
+                            SL8[32 + pos] = pl.y;
+                            SL8[64 + pos] = pl.z;
+                        }
+                        sidx[pos] = jb + (uint32_t)lane;
+                    }
+                    const int nt = __popc(taken);
+                    jb += (uint32_t)__popc(m) <= (uint32_t)room ? nc : (uint32_t)(32 - __clz(taken));
+                    f += nt;
+                }
+                nj = f;
+                if (nj == 0) break;  // no candidate left in reach
+                evaluated += (unsigned long long)icount * (uint32_t)nj;
+                // a partial tile is padded (far-away points: the reject entry) to 32 above kPadMin
+                // and to a multiple of 4 otherwise
+                const int njp = nj > kPadMin ? 32 : ((nj + 3) & ~3);
+                if (lane >= nj && lane < njp) {
+                    S[lane] = -1e30f;
+                    S[32 + lane] = -1e30f;
+                    S[64 + lane] = -1e30f;
+                    if (NEED_W) S[96 + lane] = 0.f;
+                    if (kLo) SL8[lane] = SL8[32 + lane] = SL8[64 + lane] = 0.f;
+                }
+                nj = njp;
+            } else {
             uint32_t jx = jb + (uint32_t)lane, jimg = 0;  // this lane's j point (unpacked)
             if (packed) {
                 // records jrc .. jrc + 31 (one per lane, cut after the chunk's last record): the
@@ -2148,6 +2232,8 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
                     if (nj > kPadMin) nj = 32;
                 }
             }
+            jb += 32;
+            }
             __syncwarp();
             const float wi_s = pi.w * A.w_scale_f;
             uint32_t slowbits;
@@ -2155,30 +2241,30 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
                 // byte table: pair k of nj ends at bit 32 - nj + k (shifted into bit 0 of k = 0 below)
                 if (MODE == MODE_THETA && NEED_AVG && A.theta_series) {
                     slowbits = own ? tile_fast8<MODE, NEED_AVG, NEED_W, true, true>(A, sjhi, sjlo, lut_add, h.ascale, nj,
-                                                                                  jb, i, xi, yi, zi, xil, yil, zil, wi_s, qcap_l,
+                                                                                  tile_j0, i, xi, yi, zi, xil, yil, zil, wi_s, qcap_l,
                                                                                   cnt_s)
                                    : tile_fast8<MODE, NEED_AVG, NEED_W, false, true>(A, sjhi, sjlo, lut_add, h.ascale,
-                                                                                   nj, jb, i, xi, yi, zi, xil, yil, zil,
+                                                                                   nj, tile_j0, i, xi, yi, zi, xil, yil, zil,
                                                                                    wi_s, qcap_l, cnt_s);
                 } else {
                     slowbits = own ? tile_fast8<MODE, NEED_AVG, NEED_W, true, false>(A, sjhi, sjlo, lut_add, h.ascale,
-                                                                                   nj, jb, i, xi, yi, zi, xil, yil, zil,
+                                                                                   nj, tile_j0, i, xi, yi, zi, xil, yil, zil,
                                                                                    wi_s, qcap_l, cnt_s)
                                    : tile_fast8<MODE, NEED_AVG, NEED_W, false, false>(A, sjhi, sjlo, lut_add, h.ascale,
-                                                                                    nj, jb, i, xi, yi, zi, xil, yil, zil,
+                                                                                    nj, tile_j0, i, xi, yi, zi, xil, yil, zil,
                                                                                     wi_s, qcap_l, cnt_s);
                 }
                 slowbits >>= 32 - nj;  // pair k at bit k
             } else if (MODE == MODE_THETA && NEED_AVG && A.theta_series) {
                 // angular averages by the arcsine series: a separate copy of the unrolled tile loop
-                slowbits = own ? tile_fast<MODE, NEED_AVG, NEED_W, true, true>(A, sjhi, sjlo, lut, h.ascale, nj, jb, i, xi,
+                slowbits = own ? tile_fast<MODE, NEED_AVG, NEED_W, true, true>(A, sjhi, sjlo, lut, h.ascale, nj, tile_j0, i, xi,
                                                                              yi, zi, xil, yil, zil, wi_s, ax, ay, az, cnt_s)
-                               : tile_fast<MODE, NEED_AVG, NEED_W, false, true>(A, sjhi, sjlo, lut, h.ascale, nj, jb, i, xi,
+                               : tile_fast<MODE, NEED_AVG, NEED_W, false, true>(A, sjhi, sjlo, lut, h.ascale, nj, tile_j0, i, xi,
                                                                               yi, zi, xil, yil, zil, wi_s, ax, ay, az, cnt_s);
             } else {
-                slowbits = own ? tile_fast<MODE, NEED_AVG, NEED_W, true, false>(A, sjhi, sjlo, lut, h.ascale, nj, jb, i, xi,
+                slowbits = own ? tile_fast<MODE, NEED_AVG, NEED_W, true, false>(A, sjhi, sjlo, lut, h.ascale, nj, tile_j0, i, xi,
                                                                               yi, zi, xil, yil, zil, wi_s, ax, ay, az, cnt_s)
-                               : tile_fast<MODE, NEED_AVG, NEED_W, false, false>(A, sjhi, sjlo, lut, h.ascale, nj, jb, i, xi,
+                               : tile_fast<MODE, NEED_AVG, NEED_W, false, false>(A, sjhi, sjlo, lut, h.ascale, nj, tile_j0, i, xi,
                                                                                yi, zi, xil, yil, zil, wi_s, ax, ay, az, cnt_s);
             }
             // candidates in flagged buckets go to the warp's slow queue, one bit per lane per round
@@ -2192,7 +2278,7 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
                     const int k = LUT8 ? b : nj - 1 - b;  // bit k (byte table) or n - 1 - k holds pair k
                     RefineEntry r;
                     r.i = i;
-                    r.j = packed ? sidx[k] : jb + (uint32_t)k;
+                    r.j = (packed || prune) ? sidx[k] : tile_j0 + (uint32_t)k;
                     r.meta = packed ? (T.meta & ~0x3f00u) | ((uint32_t)simg[k] << 8) : T.meta;
                     sq[sq_n + __popc(want & ((1u << lane) - 1u))] = r;
                 }
@@ -2714,6 +2800,7 @@ struct Engine {
     int byte_table = 1;  // byte bucket table for DD(r), xi and DDtheta (CF_BYTE_TABLE=0: 32-bit table)
     int lut8_lg = 12;    // finest byte-table resolution, log2 buckets per octave (CF_BYTE_TABLE_LG)
     bool layout_packed = false;  // the current count's FP32 pair kernel takes packed tasks
+    bool layout_prune = false;   // ... or may prune j points by box (byte-table modes of single counts)
     // single-count autotuner (cf_engine_set_autotune): per count shape, the fastest j-lattice
     // column split found by timing the candidates on the first count of that shape
     int autotune = 0;
@@ -3089,23 +3176,24 @@ static double layout_score(const SmemLayout &c, int mode, bool avg, bool w)
 static SmemLayout choose_layout(int mode, bool f64, bool avg, bool w, int nedges, int nbins, int lut_n)
 {
     const bool pk = g_eng.layout_packed && !f64;  // a count with packed tasks
+    const bool pr = g_eng.layout_prune && !f64;   // a count whose kernel may prune
     const bool dz = (mode == MODE_RPPI || mode == MODE_WP || mode == MODE_SMU || mode_is_mock(mode));
     const bool los = avg || mode_is_mock(mode);
     const bool forced = g_eng.force_ls > 0 && g_eng.force_warps > 0 && 32 * g_eng.force_warps <= pair_max_threads(mode, avg, w);
     if (!f64 && forced) {
-        const SmemLayout c = smem_layout(nedges, nbins, g_eng.force_warps, f64, lut_n, g_eng.force_ls, avg, w, dz, los, pk);
+        const SmemLayout c = smem_layout(nedges, nbins, g_eng.force_warps, f64, lut_n, g_eng.force_ls, avg, w, dz, los, pk, pr);
         if (c.total <= 220 * 1024) return c;
     }
     const int regs = pair_kernel_regs(mode, f64, avg, w);
     const int warps_by_regs = 65536 / (32 * ((regs + 7) / 8 * 8));
-    SmemLayout SL = smem_layout(nedges, nbins, 8, f64, lut_n, 1, avg, w, dz, los, pk);
+    SmemLayout SL = smem_layout(nedges, nbins, 8, f64, lut_n, 1, avg, w, dz, los, pk, pr);
     double best = -1.0;
     const int lstrides[5] = {32, 16, 8, 4, 1};
     const int max_warps = f64 ? 8 : pair_max_threads(mode, avg, w) / 32;
     const int wopts[3] = {max_warps, max_warps / 2, max_warps / 4};
     for (int li = 0; li < 5; li++) {
         for (int wi = 0; wi < 3; wi++) {
-            const SmemLayout c = smem_layout(nedges, nbins, wopts[wi], f64, lut_n, lstrides[li], avg, w, dz, los, pk);
+            const SmemLayout c = smem_layout(nedges, nbins, wopts[wi], f64, lut_n, lstrides[li], avg, w, dz, los, pk, pr);
             if (c.total > 220 * 1024) continue;
             int blocks = (int)(g_eng.smem_per_sm / (c.total + 1024));
             const int max_blocks_threads = 2048 / (32 * wopts[wi]);
@@ -3130,6 +3218,7 @@ static int launch_pairs_t(const PairArgs &A, bool f64, int *launched)
     const int nedges = A.nedges;
     SmemLayout SL = choose_layout(MODE, f64, AVG, W, nedges, A.nbins, A.lut_n);
     if (!f64 && SL.lane_stride != A.lane_stride_hint) CF_FAIL("internal: histogram layout changed after the table was built");
+    if (!f64 && A.jrec && !SL.extras) CF_FAIL("internal: packed tasks without their stage space");
     if (SL.total > 220 * 1024) CF_FAIL("histogram too large for on-chip accumulation (%d bins)", A.nbins);
     const int threads = SL.warps * 32;
     int per_sm = 1;
@@ -3741,6 +3830,14 @@ static void pair_constants(PairArgs &A, const cf_job *J, int mode, int nbins, bo
     A.half_row = T.row_bytes / 2;
     A.trash_e = T.trash_e;
     A.q_cap2 = T.qcap2;
+    A.prune_r2 = 0.f;
+    if (T.lut8 && (mode == MODE_R3 || mode == MODE_THETA) && J->nedges > 0) {
+        double top = 0.0;  // the largest classified value in range: r^2, or the squared chord
+        for (int k = 0; k < J->nedges; k++)
+            top = fmax(top, mode == MODE_THETA ? 2.0 * (1.0 - J->edges[k]) : J->edges[k]);
+        const double rp = (sqrt(top) + 4.0 * d3) * (1.0 + 1e-5);
+        if (isfinite(rp) && rp * rp < 1e30) A.prune_r2 = f_up(rp * rp);
+    }
     A.g_edges = (const double *)W.tab.p;
     A.g_guard = (const float *)((const char *)W.tab.p + T.guard_off);
     A.dz_err = (float)(2.0 * delta[2]);
@@ -3808,8 +3905,9 @@ static void pair_constants(PairArgs &A, const cf_job *J, int mode, int nbins, bo
 // CF_COLUMN_SPLIT=<split>[,<slab merge>] fixes them (read on every call).  Otherwise a cost model
 // in pair evaluations per i point: the j points of every window (split columns against the
 // chunk column's reach, z windows widened to whole merged slabs), padding per range, the
-// packed path's per-pair overhead, and the split lattice's extra build (cells, and for an
-// auto-correlation a second lattice of the same points).  The j lattice keeps within 2^26 cells.
+// packed path's per-pair overhead, the split lattice's extra build (cells, and for an
+// auto-correlation a second lattice of the same points), and the box pruning of the unsplit
+// byte-table kernel.  The j lattice keeps within 2^26 cells.
 static int choose_split(const cf_job *J, const Geom &g, int64_t n1, int64_t n2, bool autocorr, int mode, int *zdiv)
 {
     *zdiv = 1;
@@ -3852,7 +3950,8 @@ static int choose_split(const cf_job *J, const Geom &g, int64_t n1, int64_t n2, 
         if (r3 > 0.0) W = fmin(W, sqrt(fmax(0.0, r3 * r3 - d2)));
         return W;
     };
-    const double kPad = 8.0, kItemPad = 16.0, kPackedCost = 1.12, kBuildPerPoint = 100.0, kPerCell = 7.0;
+    const double kPad = 8.0, kItemPad = 16.0, kPackedCost = 1.12, kBuildPerPoint = 100.0, kPerCell = 7.0,
+                 kPruneKeep = 0.7;
     auto windows = [&](int sub, int zd) {  // j points per i point, padding included
         const double sf0 = g.s[0] / sub, sf1 = g.s[1] / sub, Af = sf0 * sf1;
         const int rx = (int)ceil(r / sf0), ry = (int)ceil(r / sf1);
@@ -3879,7 +3978,10 @@ static int choose_split(const cf_job *J, const Geom &g, int64_t n1, int64_t n2, 
         }
         return sub == 1 ? pts + kPad * ranges : pts + kItemPad + (autocorr ? kPad : 0.0);
     };
-    double best = windows(1, 1);
+    // the unsplit byte-table kernel prunes j points by the chunk's bounding box (about 60-70 % of
+    // its window points stay); the packed kernel of split columns does not
+    const bool prunes = g_eng.byte_table && J->nedges >= 2 && J->nedges - 1 <= 127;
+    double best = windows(1, 1) * (prunes ? kPruneKeep : 1.0);
     const double base = best;
     int bsub = 1, bzd = 1;
     for (int sub = 2; sub <= 4; sub++) {
@@ -3908,7 +4010,7 @@ static int run_locked(cf_job *J, cf_hist *H)
     cudaStream_t st = g_eng.stream;
     memset(&g_eng.last, 0, sizeof(g_eng.last));
     g_eng.launches = 0;
-    g_eng.layout_packed = false;
+    g_eng.layout_packed = g_eng.layout_prune = false;
     const int mode = J->mode;
     const int nbins = mode_two_d(mode) ? J->nedges * (J->npibin + 1) : J->nedges;
     if (H->nbins != nbins) CF_FAIL("internal: histogram size mismatch (%d vs %d)", H->nbins, nbins);
@@ -3997,6 +4099,7 @@ static int run_locked(cf_job *J, cf_hist *H)
     int zdiv = 1;
     const int jsub = f64 ? 1 : choose_split(J, g, n1, n2, autocorr, mode, &zdiv);
     g_eng.layout_packed = jsub > 1;  // the histogram layouts of this count (tables and launch)
+    g_eng.layout_prune = mode == MODE_R3 || mode == MODE_THETA;
     Geom gj = g;
     uint32_t ncells_j = ncells;
     if (jsub > 1) {
@@ -4552,7 +4655,7 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
 {
     *out = nullptr;
     if (engine_init() != EXIT_SUCCESS) return EXIT_FAILURE;
-    g_eng.layout_packed = false;  // batched counts take no packed tasks
+    g_eng.layout_packed = g_eng.layout_prune = false;  // batched counts neither pack nor prune
     if (nbatch < 1 || nbatch > (1 << 15) - 1) CF_FAIL("batch size %d outside [1, 32767]", nbatch);
     if (tmpl->mode != MODE_R3 || tmpl->autocorr) CF_FAIL("internal: batched counts are DD cross-correlations");
     if (tmpl->elem_size != 4 && tmpl->elem_size != 8) CF_FAIL("element size must be 4 or 8");
@@ -4774,6 +4877,7 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
         A.ntasks = P->task_cap;
         A.ntask_dev = P->merged ? nullptr : (const uint32_t *)W.task_off.p + P->nentries;
         pair_constants(A, &P->J, MODE_R3, P->nbins, false, P->G, P->geo, P->g, P->delta, P->T, P->wmax, W);
+        A.prune_r2 = 0.f;  // batched counts do not prune (their layouts hold no box)
         A.w_exact = P->w_exact ? 1 : 0;
         {
             const ResView R = res_view(W.res.p, nb);
@@ -4821,6 +4925,7 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
                     if ((rc = build_tables(W, &P->J, MODE_R3, P->nbins, P->need_w, P->delta, &T2)) != EXIT_SUCCESS) break;
                     P->T = T2;
                     pair_constants(A, &P->J, MODE_R3, P->nbins, false, P->G, P->geo, P->g, P->delta, P->T, P->wmax, W);
+                    A.prune_r2 = 0.f;  // batched counts do not prune (their layouts hold no box)
                     P->ls = cand_ls[li];
                     P->warps = cand_w[wi];
                     float ms = 0.f;
@@ -4853,6 +4958,7 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
             if (rc != EXIT_SUCCESS) break;
             P->T = T2;
             pair_constants(A, &P->J, MODE_R3, P->nbins, false, P->G, P->geo, P->g, P->delta, P->T, P->wmax, W);
+            A.prune_r2 = 0.f;  // batched counts do not prune (their layouts hold no box)
             if (cudaStreamSynchronize(st) != cudaSuccess) {
                 rc = EXIT_FAILURE;
                 break;
@@ -4895,7 +5001,7 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
 
 static int batch_run_locked(BatchPlan *P, cf_hist *H)
 {
-    g_eng.layout_packed = false;  // batched counts take no packed tasks
+    g_eng.layout_packed = g_eng.layout_prune = false;  // batched counts neither pack nor prune
     if (engine_init() != EXIT_SUCCESS) return EXIT_FAILURE;
     cudaStream_t st = g_eng.stream;
     CF_CUDA(cudaStreamSynchronize(st));
