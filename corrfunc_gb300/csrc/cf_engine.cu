@@ -15,6 +15,7 @@
 //
 // Entry point: cf_engine_run() (C ABI, called by the C host layer).
 #include <cuda_runtime.h>
+#include <float.h>
 #include <math.h>
 #include <pthread.h>
 #include <signal.h>
@@ -1710,7 +1711,8 @@ __device__ __forceinline__ void pairs_group8(const PairArgs &A, const float4 *__
                                              const float4 *__restrict__ sjlo, uint32_t lut_add,
                                              const float *__restrict__ ascale, int k0, uint32_t jb, uint32_t i, float xi,
                                              float yi, float zi, float xil, float yil, float zil, float wis,
-                                             float qcap, uint32_t cnt_s, uint32_t &slowbits)
+                                             float qcap, uint32_t cnt_s, uint32_t &slowbits,
+                                             const uint32_t *__restrict__ jidx = nullptr)
 {
     static_assert(U % 4 == 0, "the byte-table stage is read four j points at a time");
     const float *S = (const float *)sjhi, *SL8 = (const float *)sjlo;
@@ -1757,7 +1759,10 @@ __device__ __forceinline__ void pairs_group8(const PairArgs &A, const float4 *__
             uint32_t a, e;
             asm("mad.hi.u32 %0, %1, %2, %3;" : "=r"(a) : "r"(__float_as_uint(q)), "r"(A.lut_mul), "r"(lut_add));
             asm("ld.shared.u8 %0, [%1];" : "=r"(e) : "r"(a));
-            if (OWN) e = jb + (uint32_t)k > i ? e : A.trash_e;  // own column: only j > i
+            if (OWN) {  // own column: only j > i (pruned tiles: the staged point's own index)
+                const uint32_t jj = jidx ? jidx[k] : jb + (uint32_t)k;
+                e = jj > i ? e : A.trash_e;
+            }
             slowbits = __funnelshift_r(slowbits, e, 1);
             addr[u] = e * A.half_row + cnt_s;
             vw[u] = 0;
@@ -1792,7 +1797,7 @@ __device__ __forceinline__ uint32_t tile_fast8(const PairArgs &A, const float4 *
                                                const float4 *__restrict__ sjlo, uint32_t lut_add,
                                                const float *__restrict__ ascale, int nj, uint32_t jb, uint32_t i,
                                                float xi, float yi, float zi, float xil, float yil, float zil, float wis,
-                                               float qcap, uint32_t cnt_s)
+                                               float qcap, uint32_t cnt_s, const uint32_t *__restrict__ jidx = nullptr)
 {
     uint32_t slowbits = 0;
     if (nj == 32) {
@@ -1802,12 +1807,12 @@ __device__ __forceinline__ uint32_t tile_fast8(const PairArgs &A, const float4 *
 #pragma unroll kUnroll
         for (int k0 = 0; k0 < 32; k0 += kGroup)
             pairs_group8<MODE, NEED_AVG, NEED_W, OWN, SER, kGroup>(A, sjhi, sjlo, lut_add, ascale, k0, jb, i, xi, yi, zi,
-                                                                   xil, yil, zil, wis, qcap, cnt_s, slowbits);
+                                                                   xil, yil, zil, wis, qcap, cnt_s, slowbits, jidx);
     } else {
         // a partial tile, padded to a multiple of 4 points
         for (int k = 0; k < nj; k += 4)
             pairs_group8<MODE, NEED_AVG, NEED_W, OWN, SER, 4>(A, sjhi, sjlo, lut_add, ascale, k, jb, i, xi, yi, zi, xil,
-                                                              yil, zil, wis, qcap, cnt_s, slowbits);
+                                                              yil, zil, wis, qcap, cnt_s, slowbits, jidx);
     }
     return slowbits;
 }
@@ -2036,17 +2041,17 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
         const uint32_t jend = packed ? jbeg + (T.j_end & 2047u) + 1u : T.j_end;
         if constexpr (PACKED) {
             if (lane == 0) *ev_s += (unsigned long long)icount * (jend - jbeg);
-        } else if (!(kPrune && !own && A.prune_r2 > 0.f && SL.extras)) {
+        } else if constexpr (!kPrune) {
             evaluated += (unsigned long long)icount * (jend - jbeg);  // pruned tasks count per tile
         }
         const bool shifted = packed && (T.meta & kTaskImages) != 0;
         uint32_t jrc = T.j_begin;  // packed: the record holding list position jb
-        // Box pruning (unpacked byte-table tasks but the own column's): a j point farther than the
-        // prune radius (the top edge's separation plus the coordinate error bounds) from the
-        // chunk's bounding box pairs with none of its points in range, so it is never staged;
-        // the points kept fill whole tiles across the task's candidates.
-        const bool prune = kPrune && !own && A.prune_r2 > 0.f && SL.extras;
-        if (prune) {
+        // Box pruning (the unpacked byte-table kernels): a j point farther than the prune radius
+        // (the top edge's separation plus the coordinate error bounds) from the chunk's bounding
+        // box pairs with none of its points in range, so it is never staged; the points kept
+        // fill whole tiles across the task's candidates.
+        constexpr bool prune = kPrune;
+        if constexpr (prune) {
             // the box of the valid lanes' (image-shifted) points, by order-preserving integer keys
             auto key = [](float v) { const int b = __float_as_int(v); return b ^ ((b >> 31) & 0x7fffffff); };
             auto val = [](int k) { return __int_as_float(k ^ ((k >> 31) & 0x7fffffff)); };
@@ -2066,7 +2071,7 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
         for (uint32_t jb = jbeg; jb < jend;) {
             const uint32_t tile_j0 = jb;  // unpruned: the tile's first j point
             int nj = (int)min(32u, jend - jb);
-            if (prune) {
+            if constexpr (prune) {
                 // rounds of 32 candidates until 32 points are staged or the range ends; a round
                 // that overfills the stage takes its first kept points and the next round starts
                 // after the last one taken
@@ -2242,14 +2247,14 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
                 if (MODE == MODE_THETA && NEED_AVG && A.theta_series) {
                     slowbits = own ? tile_fast8<MODE, NEED_AVG, NEED_W, true, true>(A, sjhi, sjlo, lut_add, h.ascale, nj,
                                                                                   tile_j0, i, xi, yi, zi, xil, yil, zil, wi_s, qcap_l,
-                                                                                  cnt_s)
+                                                                                  cnt_s, prune ? sidx : nullptr)
                                    : tile_fast8<MODE, NEED_AVG, NEED_W, false, true>(A, sjhi, sjlo, lut_add, h.ascale,
                                                                                    nj, tile_j0, i, xi, yi, zi, xil, yil, zil,
                                                                                    wi_s, qcap_l, cnt_s);
                 } else {
                     slowbits = own ? tile_fast8<MODE, NEED_AVG, NEED_W, true, false>(A, sjhi, sjlo, lut_add, h.ascale,
                                                                                    nj, tile_j0, i, xi, yi, zi, xil, yil, zil,
-                                                                                   wi_s, qcap_l, cnt_s)
+                                                                                   wi_s, qcap_l, cnt_s, prune ? sidx : nullptr)
                                    : tile_fast8<MODE, NEED_AVG, NEED_W, false, false>(A, sjhi, sjlo, lut_add, h.ascale,
                                                                                     nj, tile_j0, i, xi, yi, zi, xil, yil, zil,
                                                                                     wi_s, qcap_l, cnt_s);
@@ -3218,7 +3223,7 @@ static int launch_pairs_t(const PairArgs &A, bool f64, int *launched)
     const int nedges = A.nedges;
     SmemLayout SL = choose_layout(MODE, f64, AVG, W, nedges, A.nbins, A.lut_n);
     if (!f64 && SL.lane_stride != A.lane_stride_hint) CF_FAIL("internal: histogram layout changed after the table was built");
-    if (!f64 && A.jrec && !SL.extras) CF_FAIL("internal: packed tasks without their stage space");
+    if (!f64 && (A.jrec || A.lut8) && !SL.extras) CF_FAIL("internal: packed or pruned tiles without their stage space");
     if (SL.total > 220 * 1024) CF_FAIL("histogram too large for on-chip accumulation (%d bins)", A.nbins);
     const int threads = SL.warps * 32;
     int per_sm = 1;
@@ -3830,7 +3835,7 @@ static void pair_constants(PairArgs &A, const cf_job *J, int mode, int nbins, bo
     A.half_row = T.row_bytes / 2;
     A.trash_e = T.trash_e;
     A.q_cap2 = T.qcap2;
-    A.prune_r2 = 0.f;
+    A.prune_r2 = FLT_MAX;  // the byte-table kernels always test the box: no radius keeps every point
     if (T.lut8 && (mode == MODE_R3 || mode == MODE_THETA) && J->nedges > 0) {
         double top = 0.0;  // the largest classified value in range: r^2, or the squared chord
         for (int k = 0; k < J->nedges; k++)
@@ -4803,6 +4808,8 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
             }
             if (rc != EXIT_SUCCESS) break;
         }
+        // the per-catalogue form runs the single counts' kernel, which prunes by box
+        g_eng.layout_prune = !P->merged;
         uint64_t slots = 0;
         if (P->merged) {
             P->gap = chunk_gap(P->G, P->total1, P->ncols);
@@ -4877,7 +4884,6 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
         A.ntasks = P->task_cap;
         A.ntask_dev = P->merged ? nullptr : (const uint32_t *)W.task_off.p + P->nentries;
         pair_constants(A, &P->J, MODE_R3, P->nbins, false, P->G, P->geo, P->g, P->delta, P->T, P->wmax, W);
-        A.prune_r2 = 0.f;  // batched counts do not prune (their layouts hold no box)
         A.w_exact = P->w_exact ? 1 : 0;
         {
             const ResView R = res_view(W.res.p, nb);
@@ -4925,7 +4931,6 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
                     if ((rc = build_tables(W, &P->J, MODE_R3, P->nbins, P->need_w, P->delta, &T2)) != EXIT_SUCCESS) break;
                     P->T = T2;
                     pair_constants(A, &P->J, MODE_R3, P->nbins, false, P->G, P->geo, P->g, P->delta, P->T, P->wmax, W);
-                    A.prune_r2 = 0.f;  // batched counts do not prune (their layouts hold no box)
                     P->ls = cand_ls[li];
                     P->warps = cand_w[wi];
                     float ms = 0.f;
@@ -4958,7 +4963,6 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
             if (rc != EXIT_SUCCESS) break;
             P->T = T2;
             pair_constants(A, &P->J, MODE_R3, P->nbins, false, P->G, P->geo, P->g, P->delta, P->T, P->wmax, W);
-            A.prune_r2 = 0.f;  // batched counts do not prune (their layouts hold no box)
             if (cudaStreamSynchronize(st) != cudaSuccess) {
                 rc = EXIT_FAILURE;
                 break;
@@ -5001,7 +5005,8 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
 
 static int batch_run_locked(BatchPlan *P, cf_hist *H)
 {
-    g_eng.layout_packed = g_eng.layout_prune = false;  // batched counts neither pack nor prune
+    g_eng.layout_packed = false;  // batched counts take no packed tasks; the per-catalogue form prunes
+    g_eng.layout_prune = !P->merged;
     if (engine_init() != EXIT_SUCCESS) return EXIT_FAILURE;
     cudaStream_t st = g_eng.stream;
     CF_CUDA(cudaStreamSynchronize(st));
