@@ -2396,6 +2396,9 @@ __global__ void __launch_bounds__(pair_max_threads(MODE_R3, NEED_AVG, NEED_W), C
     RefineEntry *rq = (RefineEntry *)(sjlo + 32);
     RefineEntry *sq = rq + kRefineQueue;
     int *rq_count = (int *)(sq + kSlowQueue);
+    uint32_t *sidx = (uint32_t *)((unsigned char *)rq_count + 16);  // staged j points' lattice indices,
+    uint8_t *simg = (uint8_t *)(sidx + 32);                          // image codes
+    float4 *sbox = (float4 *)(simg + 32);                            // and the chunk's box
     int sq_n = 0;
     WarpHist h = warp_hist(smem, SL, warp);
     zero_hist(h, SL, lane);
@@ -2428,6 +2431,64 @@ __global__ void __launch_bounds__(pair_max_threads(MODE_R3, NEED_AVG, NEED_W), C
         const float wi_s = pi.w * A.w_scale_f;
         const int a = (int)((info.x >> 6) & 4095u), b = (int)((info.x >> 18) & 4095u);
         const int col = (int)info.y, ix = col / G.ny, iy = col % G.ny;
+        // Box pruning: a j point farther than the prune radius from the chunk's bounding box pairs
+        // with none of its points in range and is never staged.  Staged points carry their
+        // range's periodic image (j + o, exact on the grid as i - o is), so the points kept from
+        // every neighbour column and image fill whole tiles against the unshifted i points.
+        {
+            auto key = [](float v) { const int bk = __float_as_int(v); return bk ^ ((bk >> 31) & 0x7fffffff); };
+            auto val = [](int k) { return __int_as_float(k ^ ((k >> 31) & 0x7fffffff)); };
+            const int big = 0x7f800000, small = (int)0x80800000;  // keys of +inf, -inf
+            const float bxl = val(__reduce_min_sync(0xffffffffu, ivalid ? key(pi.x) : big));
+            const float byl = val(__reduce_min_sync(0xffffffffu, ivalid ? key(pi.y) : big));
+            const float bzl = val(__reduce_min_sync(0xffffffffu, ivalid ? key(pi.z) : big));
+            const float bxh = val(__reduce_max_sync(0xffffffffu, ivalid ? key(pi.x) : small));
+            const float byh = val(__reduce_max_sync(0xffffffffu, ivalid ? key(pi.y) : small));
+            const float bzh = val(__reduce_max_sync(0xffffffffu, ivalid ? key(pi.z) : small));
+            if (lane == 0) {
+                sbox[0] = make_float4(bxl, byl, bzl, A.prune_r2);
+                sbox[1] = make_float4(bxh, byh, bzh, 0.f);
+            }
+            __syncwarp();
+        }
+        const float xi = pi.x, yi = pi.y, zi = pi.z;
+        const float xil = pl.x, yil = pl.y, zil = pl.z;
+        float *S = (float *)sjhi, *SL8 = (float *)sjlo;
+        int f = 0;  // points staged
+        // one tile of the staged points (njp: 32, or a partial tile's padded size)
+        auto run_tile = [&](int njp) {
+            __syncwarp();
+            uint32_t slowbits = tile_fast8<MODE, NEED_AVG, NEED_W, false, false>(
+                A, sjhi, sjlo, lut_add, h.ascale, njp, 0u, i, xi, yi, zi, xil, yil, zil, wi_s, A.q_cap, cnt_s);
+            slowbits >>= 32 - njp;
+            while (true) {
+                const uint32_t want = __ballot_sync(0xffffffffu, slowbits != 0);
+                if (!want) break;
+                if (slowbits) {
+                    const int bb = (int)(__float_as_uint(__uint2float_rz(slowbits)) >> 23) - 127;
+                    slowbits ^= 1u << bb;
+                    RefineEntry r;
+                    r.i = i;
+                    r.j = sidx[bb];
+                    r.meta = (uint32_t)simg[bb] << 8;  // one i point per lane, the staged point's image
+                    sq[sq_n + __popc(want & ((1u << lane) - 1u))] = r;
+                }
+                sq_n += __popc(want);
+                queued += __popc(want);
+                __syncwarp();
+                if (sq_n >= 32) {
+                    slow_batch<MODE, NEED_AVG, NEED_W, true>(A, se, glo, ghi, sq + (sq_n - 32), 32, rq, rq_count, h,
+                                                             hl, lane, &refined, (int)ib);
+                    sq_n -= 32;
+                }
+            }
+            __syncwarp();
+            col_terms += tile_terms;
+            if (col_terms + tile_terms > (uint32_t)kColumnTerms) {
+                flush_lanes<NEED_AVG, NEED_W>(A, h, lane, cat);
+                col_terms = 0;
+            }
+        };
         for (int c = 0; c < ncoff; c++) {
             const int dx = c / nyc - G.reach_x, dy = c % nyc - G.reach_y;
             const int wz = G.ntab ? (int)G.wz_tab[c] : column_wz(G, dx, dy);
@@ -2460,70 +2521,74 @@ __global__ void __launch_bounds__(pair_max_threads(MODE_R3, NEED_AVG, NEED_W), C
                 if (s0 > s1) continue;
                 const uint32_t jbeg = cs[s0], jend = cs[s1 + 1];
                 if (jend <= jbeg) continue;
-                // j is shifted by the image offset o; equivalently shift i by -o (exact on the grid)
-                const float xi = pi.x - A.ohi[0][mx + 1], yi = pi.y - A.ohi[1][my + 1], zi = pi.z - A.ohi[2][mz + 1];
-                float xil = 0.f, yil = 0.f, zil = 0.f;
-                if (NEED_AVG) {
-                    xil = pl.x - A.olo[0][mx + 1];
-                    yil = pl.y - A.olo[1][my + 1];
-                    zil = pl.z - A.olo[2][mz + 1];
-                }
-                const uint32_t meta = task_meta(1, mx, my, mz, 0);
-                for (uint32_t jb = jbeg; jb < jend; jb += 32) {
-                    int nj = (int)min(32u, jend - jb);
-                    const int njp = nj > kPadMin ? 32 : ((nj + 3) & ~3);
-                    float *S = (float *)sjhi, *SL8 = (float *)sjlo;
-                    if (lane < njp) {
-                        float4 p = make_float4(-1e30f, -1e30f, -1e30f, 0.f), q = make_float4(0.f, 0.f, 0.f, 0.f);
-                        if (lane < nj) {
-                            p = A.hi2[jb + lane];
-                            if (NEED_AVG) q = A.lo2[jb + lane];
+                // this range's periodic image, applied to its j points
+                const float ox = A.ohi[0][mx + 1], oy = A.ohi[1][my + 1], oz = A.ohi[2][mz + 1];
+                const float olx = A.olo[0][mx + 1], oly = A.olo[1][my + 1], olz = A.olo[2][mz + 1];
+                const uint32_t img = (uint32_t)(mx + 1) | ((uint32_t)(my + 1) << 2) | ((uint32_t)(mz + 1) << 4);
+                for (uint32_t jb = jbeg; jb < jend;) {
+                    // a round of 32 candidates: the kept ones go to the stage (a round that
+                    // overfills it takes its first kept points; the next starts after the last)
+                    const float4 b0 = sbox[0], b1 = sbox[1];
+                    const uint32_t nc = min(32u, jend - jb);
+                    float4 p = make_float4(0.f, 0.f, 0.f, 0.f), q = p;
+                    bool keep = false;
+                    if ((uint32_t)lane < nc) {
+                        p = A.hi2[jb + lane];
+                        p.x += ox;
+                        p.y += oy;
+                        p.z += oz;
+                        const float dx = fmaxf(0.f, fmaxf(b0.x - p.x, p.x - b1.x));
+                        const float dy = fmaxf(0.f, fmaxf(b0.y - p.y, p.y - b1.y));
+                        const float dz = fmaxf(0.f, fmaxf(b0.z - p.z, p.z - b1.z));
+                        keep = fmaf(dz, dz, fmaf(dy, dy, dx * dx)) <= b0.w;
+                        if (NEED_AVG && keep) {
+                            q = A.lo2[jb + lane];
+                            q.x += olx;
+                            q.y += oly;
+                            q.z += olz;
                         }
-                        S[lane] = p.x;
-                        S[32 + lane] = p.y;
-                        S[64 + lane] = p.z;
-                        if (NEED_W) S[96 + lane] = p.w;
+                    }
+                    const uint32_t m = __ballot_sync(0xffffffffu, keep);
+                    const int room = 32 - f;
+                    const int rank = __popc(m & ((1u << lane) - 1u));
+                    const uint32_t taken = __ballot_sync(0xffffffffu, keep && rank < room);
+                    if (keep && rank < room) {
+                        const int pos = f + rank;
+                        S[pos] = p.x;
+                        S[32 + pos] = p.y;
+                        S[64 + pos] = p.z;
+                        if (NEED_W) S[96 + pos] = p.w;
                         if (NEED_AVG) {
-                            SL8[lane] = q.x;
-                            SL8[32 + lane] = q.y;
-                            SL8[64 + lane] = q.z;
+                            SL8[pos] = q.x;
+                            SL8[32 + pos] = q.y;
+                            SL8[64 + pos] = q.z;
                         }
+                        sidx[pos] = jb + (uint32_t)lane;
+                        simg[pos] = (uint8_t)img;
                     }
-                    nj = njp;
-                    __syncwarp();
-                    uint32_t slowbits = tile_fast8<MODE, NEED_AVG, NEED_W, false, false>(
-                        A, sjhi, sjlo, lut_add, h.ascale, nj, jb, i, xi, yi, zi, xil, yil, zil, wi_s, A.q_cap, cnt_s);
-                    slowbits >>= 32 - nj;
-                    while (true) {
-                        const uint32_t want = __ballot_sync(0xffffffffu, slowbits != 0);
-                        if (!want) break;
-                        if (slowbits) {
-                            const int bb = (int)(__float_as_uint(__uint2float_rz(slowbits)) >> 23) - 127;
-                            slowbits ^= 1u << bb;
-                            RefineEntry r;
-                            r.i = i;
-                            r.j = jb + (uint32_t)bb;
-                            r.meta = meta;
-                            sq[sq_n + __popc(want & ((1u << lane) - 1u))] = r;
-                        }
-                        sq_n += __popc(want);
-                        queued += __popc(want);
-                        __syncwarp();
-                        if (sq_n >= 32) {
-                            slow_batch<MODE, NEED_AVG, NEED_W, true>(A, se, glo, ghi, sq + (sq_n - 32), 32, rq, rq_count,
-                                                                     h, hl, lane, &refined, (int)ib);
-                            sq_n -= 32;
-                        }
-                    }
-                    __syncwarp();
-                    col_terms += tile_terms;
-                    if (col_terms + tile_terms > (uint32_t)kColumnTerms) {
-                        flush_lanes<NEED_AVG, NEED_W>(A, h, lane, cat);
-                        col_terms = 0;
+                    const int nt = __popc(taken);
+                    jb += (uint32_t)__popc(m) <= (uint32_t)room ? nc : (uint32_t)(32 - __clz(taken));
+                    f += nt;
+                    evaluated += (uint64_t)icount * (uint32_t)nt;
+                    if (f == 32) {
+                        run_tile(32);
+                        f = 0;
                     }
                 }
-                evaluated += (uint64_t)icount * (jend - jbeg);
             }
+        }
+        if (f > 0) {
+            // the last, partial tile: padded with far-away points (the reject entry) to 32 above
+            // kPadMin and to a multiple of 4 otherwise
+            const int njp = f > kPadMin ? 32 : ((f + 3) & ~3);
+            if (lane >= f && lane < njp) {
+                S[lane] = -1e30f;
+                S[32 + lane] = -1e30f;
+                S[64 + lane] = -1e30f;
+                if (NEED_W) S[96 + lane] = 0.f;
+                if (NEED_AVG) SL8[lane] = SL8[32 + lane] = SL8[64 + lane] = 0.f;
+            }
+            run_tile(njp);
         }
         // the chunk's queued pairs, then every lane's column into its catalogue
         __syncwarp();
@@ -4660,7 +4725,8 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
 {
     *out = nullptr;
     if (engine_init() != EXIT_SUCCESS) return EXIT_FAILURE;
-    g_eng.layout_packed = g_eng.layout_prune = false;  // batched counts neither pack nor prune
+    g_eng.layout_packed = false;  // batched counts take no packed tasks; both forms prune
+    g_eng.layout_prune = true;
     if (nbatch < 1 || nbatch > (1 << 15) - 1) CF_FAIL("batch size %d outside [1, 32767]", nbatch);
     if (tmpl->mode != MODE_R3 || tmpl->autocorr) CF_FAIL("internal: batched counts are DD cross-correlations");
     if (tmpl->elem_size != 4 && tmpl->elem_size != 8) CF_FAIL("element size must be 4 or 8");
@@ -4808,8 +4874,6 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
             }
             if (rc != EXIT_SUCCESS) break;
         }
-        // the per-catalogue form runs the single counts' kernel, which prunes by box
-        g_eng.layout_prune = !P->merged;
         uint64_t slots = 0;
         if (P->merged) {
             P->gap = chunk_gap(P->G, P->total1, P->ncols);
@@ -5005,8 +5069,8 @@ static int batch_plan_locked(const cf_job *tmpl, int nbatch, const int64_t *n1, 
 
 static int batch_run_locked(BatchPlan *P, cf_hist *H)
 {
-    g_eng.layout_packed = false;  // batched counts take no packed tasks; the per-catalogue form prunes
-    g_eng.layout_prune = !P->merged;
+    g_eng.layout_packed = false;  // batched counts take no packed tasks; both forms prune
+    g_eng.layout_prune = true;
     if (engine_init() != EXIT_SUCCESS) return EXIT_FAILURE;
     cudaStream_t st = g_eng.stream;
     CF_CUDA(cudaStreamSynchronize(st));
