@@ -2369,7 +2369,7 @@ __device__ __forceinline__ void flush_lanes(const PairArgs &A, WarpHist h, int l
 // (the ranges chunk_col_tasks would list), so the chunk's lanes keep their points, and with them
 // their catalogues, until the chunk is done.  Every lane owns a histogram column (lane stride 32)
 // that it flushes into its catalogue's sums.  Byte-table DD(r) only.
-template <bool NEED_AVG, bool NEED_W>
+template <bool NEED_AVG, bool NEED_W, bool SINGLE>
 __global__ void __launch_bounds__(pair_max_threads(MODE_R3, NEED_AVG, NEED_W), CF_PAIR_MIN_BLOCKS)
     k_pairs_chunks(PairArgs A, SmemLayout SL, TaskGeom G, const uint32_t *chunk_begin, const uint2 *chunk_info,
                    const uint32_t *cs2, uint32_t nchunk)
@@ -2403,7 +2403,8 @@ __global__ void __launch_bounds__(pair_max_threads(MODE_R3, NEED_AVG, NEED_W), C
     WarpHist h = warp_hist(smem, SL, warp);
     zero_hist(h, SL, lane);
     if (lane == 0) *rq_count = 0;
-    const int hl = lane;  // lane stride 32: private columns
+    // batches: lane stride 32 (private columns of the lanes' catalogues); one count: any stride
+    const int hl = SINGLE ? lane & (SL.lane_stride - 1) : lane;
     const uint32_t cnt_s = (uint32_t)__cvta_generic_to_shared(h.e) + 4u * h.ew * hl;
     __syncthreads();
     uint64_t evaluated = 0;
@@ -2427,7 +2428,7 @@ __global__ void __launch_bounds__(pair_max_threads(MODE_R3, NEED_AVG, NEED_W), C
         const float4 pi = ivalid ? A.hi1[i] : make_float4(1e30f, 1e30f, 1e30f, 0.f);
         float4 pl = make_float4(0.f, 0.f, 0.f, 0.f);
         if (NEED_AVG && ivalid) pl = A.lo1[i];
-        const uint32_t cat = ivalid ? (uint32_t)A.ro1[i].x : 0u;
+        const uint32_t cat = (!SINGLE && ivalid) ? (uint32_t)A.ro1[i].x : 0u;
         const float wi_s = pi.w * A.w_scale_f;
         const int a = (int)((info.x >> 6) & 4095u), b = (int)((info.x >> 18) & 4095u);
         const int col = (int)info.y, ix = col / G.ny, iy = col % G.ny;
@@ -2455,11 +2456,16 @@ __global__ void __launch_bounds__(pair_max_threads(MODE_R3, NEED_AVG, NEED_W), C
         const float xil = pl.x, yil = pl.y, zil = pl.z;
         float *S = (float *)sjhi, *SL8 = (float *)sjlo;
         int f = 0;  // points staged
-        // one tile of the staged points (njp: 32, or a partial tile's padded size)
-        auto run_tile = [&](int njp) {
+        const float qcap_l = (NEED_AVG || NEED_W) && SINGLE && SL.lane_stride < 32 && lane >= 16 ? A.q_cap2 : A.q_cap;
+        // one tile of the staged points (njp: 32, or a partial tile's padded size); own: the own
+        // column of an auto-correlation, which counts only j > i (by the staged point's index)
+        auto run_tile = [&](int njp, bool own) {
             __syncwarp();
-            uint32_t slowbits = tile_fast8<MODE, NEED_AVG, NEED_W, false, false>(
-                A, sjhi, sjlo, lut_add, h.ascale, njp, 0u, i, xi, yi, zi, xil, yil, zil, wi_s, A.q_cap, cnt_s);
+            uint32_t slowbits =
+                own ? tile_fast8<MODE, NEED_AVG, NEED_W, true, false>(A, sjhi, sjlo, lut_add, h.ascale, njp, 0u, i, xi,
+                                                                    yi, zi, xil, yil, zil, wi_s, qcap_l, cnt_s, sidx)
+                    : tile_fast8<MODE, NEED_AVG, NEED_W, false, false>(A, sjhi, sjlo, lut_add, h.ascale, njp, 0u, i,
+                                                                     xi, yi, zi, xil, yil, zil, wi_s, qcap_l, cnt_s);
             slowbits >>= 32 - njp;
             while (true) {
                 const uint32_t want = __ballot_sync(0xffffffffu, slowbits != 0);
@@ -2478,19 +2484,38 @@ __global__ void __launch_bounds__(pair_max_threads(MODE_R3, NEED_AVG, NEED_W), C
                 __syncwarp();
                 if (sq_n >= 32) {
                     slow_batch<MODE, NEED_AVG, NEED_W, true>(A, se, glo, ghi, sq + (sq_n - 32), 32, rq, rq_count, h,
-                                                             hl, lane, &refined, (int)ib);
+                                                             hl, lane, &refined, SINGLE ? -1 : (int)ib);
                     sq_n -= 32;
                 }
             }
             __syncwarp();
             col_terms += tile_terms;
             if (col_terms + tile_terms > (uint32_t)kColumnTerms) {
-                flush_lanes<NEED_AVG, NEED_W>(A, h, lane, cat);
+                if constexpr (SINGLE) flush_hist<NEED_AVG, NEED_W>(A, h, lane, 0u);
+                else flush_lanes<NEED_AVG, NEED_W>(A, h, lane, cat);
                 col_terms = 0;
             }
         };
+        // the staged points as a partial tile (padded with far-away points, the reject entry, to
+        // 32 above kPadMin and to a multiple of 4 otherwise)
+        auto run_partial = [&](bool own) {
+            const int njp = f > kPadMin ? 32 : ((f + 3) & ~3);
+            if (lane >= f && lane < njp) {
+                S[lane] = -1e30f;
+                S[32 + lane] = -1e30f;
+                S[64 + lane] = -1e30f;
+                if (NEED_W) S[96 + lane] = 0.f;
+                if (NEED_AVG) SL8[lane] = SL8[32 + lane] = SL8[64 + lane] = 0.f;
+                sidx[lane] = 0u;
+            }
+            run_tile(njp, own);
+            f = 0;
+        };
+        const bool autocorr = SINGLE && A.autocorr;
         for (int c = 0; c < ncoff; c++) {
             const int dx = c / nyc - G.reach_x, dy = c % nyc - G.reach_y;
+            if (autocorr && (dx < 0 || (dx == 0 && dy < 0))) continue;  // half stencil
+            const bool own = autocorr && dx == 0 && dy == 0;           // forward half of the own column
             const int wz = G.ntab ? (int)G.wz_tab[c] : column_wz(G, dx, dy);
             if (wz < 0) continue;
             const int ux = ix + dx, uy = iy + dy;
@@ -2507,7 +2532,7 @@ __global__ void __launch_bounds__(pair_max_threads(MODE_R3, NEED_AVG, NEED_W), C
             } else if (uy < 0 || uy >= G.ny) {
                 continue;
             }
-            const int klo = a - wz, khi = b + wz;
+            const int klo = own ? a : a - wz, khi = b + wz;
             const int mlo = G.periodic[2] ? floordiv(klo, nz) : 0, mhi = G.periodic[2] ? floordiv(khi, nz) : 0;
             if (mx < -1 || mx > 1 || my < -1 || my > 1 || mlo < -1 || mhi > 1) {
                 if (G.error && lane == 0) atomicOr(G.error, 1u);
@@ -2519,8 +2544,11 @@ __global__ void __launch_bounds__(pair_max_threads(MODE_R3, NEED_AVG, NEED_W), C
                 s0 = s0 < 0 ? 0 : s0;
                 s1 = s1 > nz - 1 ? nz - 1 : s1;
                 if (s0 > s1) continue;
-                const uint32_t jbeg = cs[s0], jend = cs[s1 + 1];
+                // the own column's own image starts at the chunk's first point, in tiles of its own
+                const bool ownr = own && mz == 0;
+                const uint32_t jbeg = ownr ? ib : cs[s0], jend = cs[s1 + 1];
                 if (jend <= jbeg) continue;
+                if (ownr && f > 0) run_partial(false);
                 // this range's periodic image, applied to its j points
                 const float ox = A.ohi[0][mx + 1], oy = A.ohi[1][my + 1], oz = A.ohi[2][mz + 1];
                 const float olx = A.olo[0][mx + 1], oly = A.olo[1][my + 1], olz = A.olo[2][mz + 1];
@@ -2571,25 +2599,15 @@ __global__ void __launch_bounds__(pair_max_threads(MODE_R3, NEED_AVG, NEED_W), C
                     f += nt;
                     evaluated += (uint64_t)icount * (uint32_t)nt;
                     if (f == 32) {
-                        run_tile(32);
+                        run_tile(32, ownr);
                         f = 0;
                     }
                 }
+                if (ownr && f > 0) run_partial(true);
             }
         }
-        if (f > 0) {
-            // the last, partial tile: padded with far-away points (the reject entry) to 32 above
-            // kPadMin and to a multiple of 4 otherwise
-            const int njp = f > kPadMin ? 32 : ((f + 3) & ~3);
-            if (lane >= f && lane < njp) {
-                S[lane] = -1e30f;
-                S[32 + lane] = -1e30f;
-                S[64 + lane] = -1e30f;
-                if (NEED_W) S[96 + lane] = 0.f;
-                if (NEED_AVG) SL8[lane] = SL8[32 + lane] = SL8[64 + lane] = 0.f;
-            }
-            run_tile(njp);
-        }
+        if (f > 0) run_partial(false);
+        if constexpr (SINGLE) continue;  // one catalogue: queues and columns carry over
         // the chunk's queued pairs, then every lane's column into its catalogue
         __syncwarp();
         if (sq_n > 0) {
@@ -2605,6 +2623,13 @@ __global__ void __launch_bounds__(pair_max_threads(MODE_R3, NEED_AVG, NEED_W), C
         }
         flush_lanes<NEED_AVG, NEED_W>(A, h, lane, cat);
         col_terms = 0;
+    }
+    if constexpr (SINGLE) {
+        __syncwarp();
+        if (sq_n > 0) slow_batch<MODE, NEED_AVG, NEED_W, true>(A, se, glo, ghi, sq, sq_n, rq, rq_count, h, hl, lane, &refined);
+        const int rest = *rq_count;
+        if (rest > 0) refine_batch<MODE, NEED_AVG, NEED_W>(A, se, rq, rest, h, hl, lane);
+        flush_hist<NEED_AVG, NEED_W>(A, h, lane, 0u);
     }
     for (int off = 16; off; off >>= 1) refined += __shfl_down_sync(0xffffffffu, refined, off);
     if (lane == 0) {
@@ -3335,6 +3360,41 @@ static int launch_pairs_m(const PairArgs &A, bool f64, bool avg, bool w, int *la
     if (avg) return launch_pairs_t<MODE, true, false>(A, f64, launched);
     if (w) return launch_pairs_t<MODE, false, true>(A, f64, launched);
     return launch_pairs_t<MODE, false, false>(A, f64, launched);
+}
+
+// A single DD(r) / xi count whose warps each walk a whole chunk's neighbourhood (k_pairs_chunks
+// with one catalogue): no work list, and the j points kept by the box fill whole tiles across
+// the chunk's neighbour columns.
+template <bool AVG, bool W>
+static int launch_walk_t(const PairArgs &A, const TaskGeom &G, const uint32_t *chunk_begin, const uint2 *chunk_info,
+                         const uint32_t *cs2, uint32_t nchunk, int *launched)
+{
+    const SmemLayout SL = choose_layout(MODE_R3, false, AVG, W, A.nedges, A.nbins, A.lut_n);
+    if (SL.lane_stride != A.lane_stride_hint) CF_FAIL("internal: histogram layout changed after the table was built");
+    if (!SL.extras) CF_FAIL("internal: pruned tiles without their stage space");
+    auto kern = k_pairs_chunks<AVG, W, true>;
+    int per_sm = 1;
+    CF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SL.total));
+    CF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, SL.warps * 32, SL.total));
+    if (per_sm < 1) per_sm = 1;
+    kern<<<g_eng.num_sms * per_sm, SL.warps * 32, SL.total, g_eng.stream>>>(A, SL, G, chunk_begin, chunk_info, cs2,
+                                                                            nchunk);
+    CF_CUDA(cudaGetLastError());
+    g_eng.launches++;
+    (*launched)++;
+    g_eng.last.blocks_per_sm = per_sm;
+    g_eng.last.warps_per_block = SL.warps;
+    g_eng.last.lane_stride = SL.lane_stride;
+    return EXIT_SUCCESS;
+}
+
+static int launch_walk(const PairArgs &A, bool avg, bool w, const TaskGeom &G, const uint32_t *chunk_begin,
+                       const uint2 *chunk_info, const uint32_t *cs2, uint32_t nchunk, int *launched)
+{
+    if (avg && w) return launch_walk_t<true, true>(A, G, chunk_begin, chunk_info, cs2, nchunk, launched);
+    if (avg) return launch_walk_t<true, false>(A, G, chunk_begin, chunk_info, cs2, nchunk, launched);
+    if (w) return launch_walk_t<false, true>(A, G, chunk_begin, chunk_info, cs2, nchunk, launched);
+    return launch_walk_t<false, false>(A, G, chunk_begin, chunk_info, cs2, nchunk, launched);
 }
 
 static int launch_pairs(int mode, const PairArgs &A, bool f64, bool avg, bool w, int *launched)
@@ -4231,6 +4291,13 @@ static int run_locked(cf_job *J, cf_hist *H)
     SetBufs &SC = W.set[(nsets == 2 || split_auto) ? 1 : 0];  // cells of the j lattice
     Tables T;
     if (build_tables(W, J, mode, nbins, need_w, delta, &T) != EXIT_SUCCESS) return EXIT_FAILURE;
+    // CF_CHUNK_WALK=1 (FP32 DD(r) / xi with the byte table and unsplit columns): the pair kernel
+    // walks every chunk's neighbourhood itself instead of taking a work list.  Off by default: its
+    // in-kernel cell-offset lookups cost more than the list saves (north star 1.016 ms against
+    // 0.862; the weighted 2M x 2M workload 5.19 against 5.24).
+    const char *cwalk = getenv("CF_CHUNK_WALK");
+    const bool walk = !f64 && mode == MODE_R3 && T.lut8 && jsub == 1 && !J->task_timer && g_eng.task_cap0 == 0 &&
+                      cwalk && atoi(cwalk) == 1;
 
     // ---- neighbour-search geometry ----
     TaskGeom G;
@@ -4357,7 +4424,9 @@ static int run_locked(cf_job *J, cf_hist *H)
             if (ensure(W.task_clock, 2 * sizeof(unsigned long long) * cap) != EXIT_SUCCESS) return EXIT_FAILURE;
             A.task_clock = (unsigned long long *)W.task_clock.p;
         }
-        if (jsub > 1) {
+        if (walk) {
+            // no work list
+        } else if (jsub > 1) {
             if (autocorr) {
                 k_task_list<<<task_grid(Gown, max_chunks), 128, 0, st>>>(
                     Gown, max_chunks, (const uint32_t *)W.chunk_begin.p, (const uint2 *)W.chunk_info.p,
@@ -4376,15 +4445,20 @@ static int run_locked(cf_job *J, cf_hist *H)
                                                                   (const uint32_t *)S2.cell_start.p, (Task *)W.tasks.p,
                                                                   (uint32_t)cap, R.flags);
         }
-        g_eng.launches++;
-        CF_CUDA(cudaGetLastError());
+        if (!walk) {
+            g_eng.launches++;
+            CF_CUDA(cudaGetLastError());
+        }
         CF_CUDA(cudaEventRecord(g_eng.ev[1], st));
         CF_CUDA(cudaMemsetAsync(W.res.p, 0, res_zero_bytes(nbins), st));  // sums, statistics, task counter
         int launched = 0;
         if (g_eng.test_signal > 0 && ++g_eng.pair_launches == g_eng.test_signal) raise(SIGINT);
         CF_CHECK_INTERRUPT();
         CF_CUDA(cudaEventRecord(g_eng.ev[2], st));
-        if (launch_pairs(mode, A, f64, J->need_avg != 0, need_w, &launched) != EXIT_SUCCESS) return EXIT_FAILURE;
+        if (walk ? launch_walk(A, J->need_avg != 0, need_w, G, (const uint32_t *)W.chunk_begin.p,
+                               (const uint2 *)W.chunk_info.p, (const uint32_t *)S2.cell_start.p, max_chunks, &launched)
+                 : launch_pairs(mode, A, f64, J->need_avg != 0, need_w, &launched))
+            return EXIT_FAILURE;
         CF_CUDA(cudaEventRecord(g_eng.ev[3], st));
         CF_CUDA(cudaMemcpyAsync(W.h_hist.p, W.res.p, res_bytes(nbins), cudaMemcpyDeviceToHost, st));
         CF_CUDA(cudaEventRecord(g_eng.ev[4], st));
@@ -4601,7 +4675,7 @@ static int launch_chunks_t(BatchPlan &P)
     g_eng.force_warps = fw;
     if (SL.lane_stride != 32 || SL.lane_stride != P.A.lane_stride_hint)
         CF_FAIL("internal: the merged batch needs private histogram columns");
-    auto kern = k_pairs_chunks<AVG, W>;
+    auto kern = k_pairs_chunks<AVG, W, false>;
     int per_sm = 1;
     CF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SL.total));
     CF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, SL.warps * 32, SL.total));

@@ -182,3 +182,20 @@ def test_find_fastest_wp_bin_refs(gpu):
     assert all(1 <= v <= 2 for v in best)
     k = np.argmin(runtimes["avg_time"])
     assert best == (runtimes["nx"][k], runtimes["ny"][k], runtimes["nz"][k])
+
+
+@pytest.mark.parametrize("name", ["auto_periodic", "auto_open_f32", "cross_weighted", "auto_dense"])
+def test_chunk_walk_matches_work_list(gpu, monkeypatch, name):
+    """CF_CHUNK_WALK=1: the pair kernel walks each chunk's neighbour columns itself (the own column's
+    forward half first, in tiles that count only j > i) instead of taking a work list; the same
+    counts and averages."""
+    c = CASES[name]
+    fn = _run_case(name, c)
+    want = fn()
+    monkeypatch.setenv("CF_CHUNK_WALK", "1")
+    got = fn()
+    stats = gpu.last_stats()
+    monkeypatch.delenv("CF_CHUNK_WALK")
+    assert stats["tasks"] == 0  # no work list
+    rtol = 1e-4 if c.get("dtype") == np.float32 else 1e-6
+    _compare(got, want, rtol)
