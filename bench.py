@@ -60,8 +60,8 @@ FLOP_PER_PAIR = 8  # 3 FADD + 1 FMUL + 2 FFMA per 3-D separation
 # dram__bytes_read.sum + dram__bytes_write.sum of one FP32 pair-kernel launch per workload and split
 # of the j lattice's columns (1: unsplit), from an ncu capture of this kernel on that workload (a
 # recorded constant, not measured by this script)
-PAIR_KERNEL_TRAFFIC_BYTES = {("cfg2", 1): 828_822_272 + 20_995_072, ("cfg2", 4): 548_401_664 + 9_282_560,
-                             ("northstar", 1): 55_237_120 + 1_390_848}
+PAIR_KERNEL_TRAFFIC_BYTES = {("cfg2", 1): 823_918_592 + 21_178_368, ("cfg2", 4): 548_401_664 + 9_282_560,
+                             ("northstar", 1): 55_332_864 + 2_163_456}
 TRAFFIC_SOURCE = ("ncu capture of the pair kernel on this workload (dram__bytes_read.sum + dram__bytes_write.sum "
                   "per launch): a recorded constant, not measured in this run")
 
@@ -431,6 +431,7 @@ def batch_record(args, torch, dev, local, world=1, e2e=False):
                 refined += st["pairs_refined"]
                 flush_l2(torch, dev)
         torch.cuda.synchronize(dev)
+        batch_st = st  # the replayed plan's statistics (the calls below overwrite them)
         total_s = max_over_ranks(sum(gpu_ms) / 1e3, world, dev)
         value = replica_throughput(work, args.steps, total_s, world)
 
@@ -471,11 +472,11 @@ def batch_record(args, torch, dev, local, world=1, e2e=False):
         lib.cf_gpu_fp32_peak_tflops(ctypes.byref(peak))
         pair_s = sum(pair_ms) / 1e3 / args.steps
         achieved = work * FLOP_PER_PAIR / pair_s / 1e12
-        st = corrfunc_gb300.last_stats()
+        st = batch_st
         rec = {"workload": WORKLOAD["workload"], "value": value, "unit": UNIT, "ms_per_step": sum(gpu_ms) / args.steps,
                "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                             "frac": achieved / peak.value if peak.value else None, "traffic": None,
-                            "kernel": "k_pairs_f32<MODE_R3,false,true> (one launch for all catalogues)",
+                            "kernel": "k_pairs_chunks<weights> (merged form; one launch for all catalogues)",
                             "peak_source": "measured: FP32 FMA calibration kernel (cf_gpu_fp32_peak_tflops) in this run",
                             "flop_per_pair": FLOP_PER_PAIR},
                "e2e": rec_e2e, "gpu_launches": launches,
