@@ -102,6 +102,9 @@ struct PairArgs {
     // bounding box of a chunk's points exceeds this pairs with none of them in range (the top
     // edge's separation plus four coordinate error bounds, and 1e-5 relative, squared, rounded up)
     float prune_r2;
+    // DDrppi / wp: a j point whose z distance to the box is at least this (the FP32 pi rejection
+    // bound) pairs with none of the chunk's points within pimax
+    float prune_z;
     uint32_t lut8_base;         // bits(b) >> lut_shift (bucket 0)
     uint32_t half_row;          // half the bytes of a histogram row (entry * half_row = row offset)
     uint32_t trash_e;           // entry of a rejected pair (2 * trash row)

@@ -1567,7 +1567,7 @@ __device__ __forceinline__ uint32_t pair_offset(const PairArgs &A, const float4 
                                                 const float4 *__restrict__ sjlo, const uint32_t *__restrict__ lut,
                                                 const float *__restrict__ ascale, int k, uint32_t jb, uint32_t i, float xi, float yi, float zi,
                                                 float xil, float yil, float zil, float wis, float ax, float ay, float az,
-                                                uint32_t &slow, int &vw, int &vavg)
+                                                uint32_t &slow, int &vw, int &vavg, const uint32_t *__restrict__ jidx)
 {
     if (MODE == MODE_RPPI_MOCK || MODE == MODE_SMU_MOCK) {
         const float4 pj = sjhi[k], pjl = sjlo[k];
@@ -1616,8 +1616,8 @@ __device__ __forceinline__ uint32_t pair_offset(const PairArgs &A, const float4 
     const uint32_t e = lut[lut_bucket(A, q)];
     uint32_t off = e & 0x003fffffu;  // bits 0-21: row byte offset, 22-30: separation bin, 31: flagged
     slow = e;
-    if (OWN) {
-        const bool keep = jb + (uint32_t)k > i;
+    if (OWN) {  // own column: only j > i (pruned tiles: the staged point's own index)
+        const bool keep = (jidx ? jidx[k] : jb + (uint32_t)k) > i;
         off = keep ? off : A.trash_off;
         slow = keep ? slow : 0u;
     }
@@ -1672,7 +1672,7 @@ __device__ __forceinline__ void pairs_group(const PairArgs &A, const float4 *__r
                                             const float *__restrict__ ascale, int k0,
                                             uint32_t jb, uint32_t i, float xi, float yi, float zi, float xil, float yil,
                                             float zil, float wis, float ax, float ay, float az, uint32_t cnt_s,
-                                            uint32_t &slowbits)
+                                            uint32_t &slowbits, const uint32_t *__restrict__ jidx)
 {
     uint32_t off[U];
     int vw[U], va[U];
@@ -1682,7 +1682,7 @@ __device__ __forceinline__ void pairs_group(const PairArgs &A, const float4 *__r
         vw[u] = 0;
         va[u] = 0;
         off[u] = pair_offset<MODE, NEED_AVG, NEED_W, OWN, SER>(A, sjhi, sjlo, lut, ascale, k0 + u, jb, i, xi, yi, zi, xil, yil, zil,
-                                                          wis, ax, ay, az, sl, vw[u], va[u]);
+                                                          wis, ax, ay, az, sl, vw[u], va[u], jidx);
         slowbits = __funnelshift_l(sl, slowbits, 1);  // pair k of n ends at bit n - 1 - k
     }
 #pragma unroll
@@ -1822,7 +1822,8 @@ __device__ __forceinline__ uint32_t tile_fast(const PairArgs &A, const float4 *_
                                               const float4 *__restrict__ sjlo, const uint32_t *__restrict__ lut,
                                               const float *__restrict__ ascale, int nj,
                                               uint32_t jb, uint32_t i, float xi, float yi, float zi, float xil, float yil,
-                                              float zil, float wis, float ax, float ay, float az, uint32_t cnt_s)
+                                              float zil, float wis, float ax, float ay, float az, uint32_t cnt_s,
+                                              const uint32_t *__restrict__ jidx = nullptr)
 {
     uint32_t slowbits = 0;
     if (nj == 32) {
@@ -1839,11 +1840,11 @@ __device__ __forceinline__ uint32_t tile_fast(const PairArgs &A, const float4 *_
 #pragma unroll kUnroll
         for (int k0 = 0; k0 < 32; k0 += kGroup)
             pairs_group<MODE, NEED_AVG, NEED_W, OWN, SER, kGroup>(A, sjhi, sjlo, lut, ascale, k0, jb, i, xi, yi, zi, xil,
-                                                                  yil, zil, wis, ax, ay, az, cnt_s, slowbits);
+                                                                  yil, zil, wis, ax, ay, az, cnt_s, slowbits, jidx);
     } else {
         for (int k = 0; k < nj; k++)
             pairs_group<MODE, NEED_AVG, NEED_W, OWN, SER, 1>(A, sjhi, sjlo, lut, ascale, k, jb, i, xi, yi, zi, xil, yil, zil, wis,
-                                                        ax, ay, az, cnt_s, slowbits);
+                                                        ax, ay, az, cnt_s, slowbits, jidx);
     }
     return slowbits;
 }
@@ -1957,7 +1958,8 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
     uint8_t *simg = (uint8_t *)(sidx + 32);                          // lattice indices and image codes
     float4 *sbox = (float4 *)(simg + 32);  // pruned tiles: the chunk's box (lo, prune radius^2), (hi, -)
     // box pruning: unpacked byte-table kernels (DD(r), xi, DDtheta)
-    constexpr bool kPrune = LUT8 && !PACKED;
+    // box pruning: the unpacked byte-table kernels (DD(r), xi, DDtheta) and DDrppi / wp / DDsmu
+    constexpr bool kPrune = !PACKED && (LUT8 || MODE == MODE_RPPI || MODE == MODE_WP || MODE == MODE_SMU);
     // periodic shift of a j point by image code (bits 0-5 as Task::meta bits 8-13)
     float4 *shift_hi = (float4 *)(smem + SL.shift_off), *shift_lo = shift_hi + 64;
     if constexpr (PACKED) {
@@ -2064,7 +2066,7 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
             const float bzh = val(__reduce_max_sync(0xffffffffu, ivalid ? key(zi) : small));
             if (lane == 0) {
                 sbox[0] = make_float4(bxl, byl, bzl, A.prune_r2);
-                sbox[1] = make_float4(bxh, byh, bzh, 0.f);
+                sbox[1] = make_float4(bxh, byh, bzh, A.prune_z);
             }
             __syncwarp();
         }
@@ -2087,7 +2089,10 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
                         const float dx = fmaxf(0.f, fmaxf(b0.x - p.x, p.x - b1.x));
                         const float dy = fmaxf(0.f, fmaxf(b0.y - p.y, p.y - b1.y));
                         const float dz = fmaxf(0.f, fmaxf(b0.z - p.z, p.z - b1.z));
-                        keep = fmaf(dz, dz, fmaf(dy, dy, dx * dx)) <= b0.w;
+                        // DDrppi / wp: rp from the box's xy rectangle and |dz| against the pi bound
+                        keep = (MODE == MODE_RPPI || MODE == MODE_WP)
+                                   ? fmaf(dy, dy, dx * dx) <= b0.w && dz < b1.w
+                                   : fmaf(dz, dz, fmaf(dy, dy, dx * dx)) <= b0.w;
                         if (kLo && keep) pl = A.lo2[jb + lane];
                     }
                     const uint32_t m = __ballot_sync(0xffffffffu, keep);
@@ -2096,14 +2101,19 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
                     const uint32_t taken = __ballot_sync(0xffffffffu, keep && rank < room);
                     if (keep && rank < room) {
                         const int pos = f + rank;
-                        S[pos] = p.x;
-                        S[32 + pos] = p.y;
-                        S[64 + pos] = p.z;
-                        if (NEED_W) S[96 + pos] = p.w;
-                        if (kLo) {
-                            SL8[pos] = pl.x;
-                            SL8[32 + pos] = pl.y;
-                            SL8[64 + pos] = pl.z;
+                        if constexpr (LUT8) {
+                            S[pos] = p.x;
+                            S[32 + pos] = p.y;
+                            S[64 + pos] = p.z;
+                            if (NEED_W) S[96 + pos] = p.w;
+                            if (kLo) {
+                                SL8[pos] = pl.x;
+                                SL8[32 + pos] = pl.y;
+                                SL8[64 + pos] = pl.z;
+                            }
+                        } else {
+                            sjhi[pos] = p;
+                            if (kLo) sjlo[pos] = pl;
                         }
                         sidx[pos] = jb + (uint32_t)lane;
                     }
@@ -2115,14 +2125,20 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
                 if (nj == 0) break;  // no candidate left in reach
                 evaluated += (unsigned long long)icount * (uint32_t)nj;
                 // a partial tile is padded (far-away points: the reject entry) to 32 above kPadMin
-                // and to a multiple of 4 otherwise
-                const int njp = nj > kPadMin ? 32 : ((nj + 3) & ~3);
+                // and (byte table) to a multiple of 4 otherwise; the other tables pair a tile of
+                // kPadMin points or fewer point by point
+                const int njp = nj > kPadMin ? 32 : LUT8 ? ((nj + 3) & ~3) : nj;
                 if (lane >= nj && lane < njp) {
-                    S[lane] = -1e30f;
-                    S[32 + lane] = -1e30f;
-                    S[64 + lane] = -1e30f;
-                    if (NEED_W) S[96 + lane] = 0.f;
-                    if (kLo) SL8[lane] = SL8[32 + lane] = SL8[64 + lane] = 0.f;
+                    if constexpr (LUT8) {
+                        S[lane] = -1e30f;
+                        S[32 + lane] = -1e30f;
+                        S[64 + lane] = -1e30f;
+                        if (NEED_W) S[96 + lane] = 0.f;
+                        if (kLo) SL8[lane] = SL8[32 + lane] = SL8[64 + lane] = 0.f;
+                    } else {
+                        sjhi[lane] = make_float4(-1e30f, -1e30f, -1e30f, 0.f);
+                        if (kLo) sjlo[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    }
                 }
                 nj = njp;
             } else {
@@ -2263,12 +2279,14 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
             } else if (MODE == MODE_THETA && NEED_AVG && A.theta_series) {
                 // angular averages by the arcsine series: a separate copy of the unrolled tile loop
                 slowbits = own ? tile_fast<MODE, NEED_AVG, NEED_W, true, true>(A, sjhi, sjlo, lut, h.ascale, nj, tile_j0, i, xi,
-                                                                             yi, zi, xil, yil, zil, wi_s, ax, ay, az, cnt_s)
+                                                                             yi, zi, xil, yil, zil, wi_s, ax, ay, az, cnt_s,
+                                                                             prune ? sidx : nullptr)
                                : tile_fast<MODE, NEED_AVG, NEED_W, false, true>(A, sjhi, sjlo, lut, h.ascale, nj, tile_j0, i, xi,
                                                                               yi, zi, xil, yil, zil, wi_s, ax, ay, az, cnt_s);
             } else {
                 slowbits = own ? tile_fast<MODE, NEED_AVG, NEED_W, true, false>(A, sjhi, sjlo, lut, h.ascale, nj, tile_j0, i, xi,
-                                                                              yi, zi, xil, yil, zil, wi_s, ax, ay, az, cnt_s)
+                                                                              yi, zi, xil, yil, zil, wi_s, ax, ay, az, cnt_s,
+                                                                              prune ? sidx : nullptr)
                                : tile_fast<MODE, NEED_AVG, NEED_W, false, false>(A, sjhi, sjlo, lut, h.ascale, nj, tile_j0, i, xi,
                                                                                yi, zi, xil, yil, zil, wi_s, ax, ay, az, cnt_s);
             }
@@ -3313,7 +3331,8 @@ static int launch_pairs_t(const PairArgs &A, bool f64, int *launched)
     const int nedges = A.nedges;
     SmemLayout SL = choose_layout(MODE, f64, AVG, W, nedges, A.nbins, A.lut_n);
     if (!f64 && SL.lane_stride != A.lane_stride_hint) CF_FAIL("internal: histogram layout changed after the table was built");
-    if (!f64 && (A.jrec || A.lut8) && !SL.extras) CF_FAIL("internal: packed or pruned tiles without their stage space");
+    const bool prunes = A.lut8 || MODE == MODE_RPPI || MODE == MODE_WP || MODE == MODE_SMU;  // the kernel's kPrune
+    if (!f64 && (A.jrec || prunes) && !SL.extras) CF_FAIL("internal: packed or pruned tiles without their stage space");
     if (SL.total > 220 * 1024) CF_FAIL("histogram too large for on-chip accumulation (%d bins)", A.nbins);
     const int threads = SL.warps * 32;
     int per_sm = 1;
@@ -3960,8 +3979,11 @@ static void pair_constants(PairArgs &A, const cf_job *J, int mode, int nbins, bo
     A.half_row = T.row_bytes / 2;
     A.trash_e = T.trash_e;
     A.q_cap2 = T.qcap2;
-    A.prune_r2 = FLT_MAX;  // the byte-table kernels always test the box: no radius keeps every point
-    if (T.lut8 && (mode == MODE_R3 || mode == MODE_THETA) && J->nedges > 0) {
+    A.prune_r2 = FLT_MAX;  // the pruning kernels always test the box: no radius keeps every point
+    A.prune_z = FLT_MAX;
+    const bool prunes = (T.lut8 && (mode == MODE_R3 || mode == MODE_THETA)) || mode == MODE_RPPI || mode == MODE_WP ||
+                        mode == MODE_SMU;
+    if (prunes && J->nedges > 0) {
         double top = 0.0;  // the largest classified value in range: r^2, or the squared chord
         for (int k = 0; k < J->nedges; k++)
             top = fmax(top, mode == MODE_THETA ? 2.0 * (1.0 - J->edges[k]) : J->edges[k]);
@@ -4013,6 +4035,7 @@ static void pair_constants(PairArgs &A, const cf_job *J, int mode, int nbins, bo
         A.inv_dpi256_f = (float)(A.inv_dpi * 256.0);
         A.pi_band_q = (int)ceil(A.pibin_band * 256.0) + 2;
         if ((double)J->npibin * 256.0 > 4.0e6 || A.pi_band_q > 100) A.pi_band_q = 128;  // everything slow
+        A.prune_z = A.pimax_hi_f;  // |dz| at or above it: rejected by the FP32 test itself
     }
     if (mode == MODE_SMU) {
         A.sqr_mu_max = J->mu_max * J->mu_max;
@@ -4229,7 +4252,7 @@ static int run_locked(cf_job *J, cf_hist *H)
     int zdiv = 1;
     const int jsub = f64 ? 1 : choose_split(J, g, n1, n2, autocorr, mode, &zdiv);
     g_eng.layout_packed = jsub > 1;  // the histogram layouts of this count (tables and launch)
-    g_eng.layout_prune = mode == MODE_R3 || mode == MODE_THETA;
+    g_eng.layout_prune = mode == MODE_R3 || mode == MODE_THETA || mode == MODE_RPPI || mode == MODE_WP || mode == MODE_SMU;
     Geom gj = g;
     uint32_t ncells_j = ncells;
     if (jsub > 1) {

@@ -410,7 +410,8 @@ def test_gpu_points_outside_the_box_fail_loudly(gpu, capfd, func):
 
 def test_gpu_wp_cell_timer(gpu):
     """wp with c_cell_timer (theory/wp/countpairs_wp_impl.c.src:330-332, 433-463): one record per
-    GPU work-list task; their pair counts add up to the pairs evaluated, the counts are unchanged."""
+    GPU work-list task; their pair counts (each task's window) bound the pairs evaluated (box
+    pruning skips the j points out of the chunk's reach), the counts are unchanged."""
     from corrfunc_gb300 import catalogs as cat
     from corrfunc_gb300 import theory
     x, y, z = cat.clustered_box(30000, 150.0, 12)
@@ -419,5 +420,6 @@ def test_gpu_wp_cell_timer(gpu):
     res, api_time, cells = theory.wp(150.0, 15.0, 1, bins, x, y, z, c_api_timer=True, c_cell_timer=True)
     assert np.array_equal(res["npairs"], plain["npairs"])
     assert api_time > 0 and len(cells) == gpu.last_stats()["tasks"]
-    assert int(np.sum(cells["N1"] * cells["N2"])) == gpu.last_stats()["pairs_evaluated"]
+    window = int(np.sum(cells["N1"] * cells["N2"]))
+    assert 0 < gpu.last_stats()["pairs_evaluated"] <= window
     assert (cells["time_in_ns"] > 0).all() and (cells["N1"] >= 1).all() and (cells["N1"] <= 32).all()

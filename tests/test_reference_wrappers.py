@@ -92,6 +92,8 @@ def test_reference_wp_wrapper_returns_cell_timings():
     assert len(cells) > 0
     assert set(cells.dtype.names) == {"N1", "N2", "time_in_ns", "cellidx1", "cellidx2", "tid"}
     assert (cells["N1"] > 0).all() and (cells["N2"] > 0).all() and (cells["time_in_ns"] >= 0).all()
-    # the per-task pair counts add up to the pairs the GPU evaluated
+    # the per-task pair counts (each task's window) bound the pairs the GPU evaluated (box pruning
+    # skips the j points out of a chunk's reach)
     import corrfunc_gb300
-    assert int(np.sum(cells["N1"].astype(np.int64) * cells["N2"])) == corrfunc_gb300.last_stats()["pairs_evaluated"]
+    window = int(np.sum(cells["N1"].astype(np.int64) * cells["N2"]))
+    assert 0 < corrfunc_gb300.last_stats()["pairs_evaluated"] <= window
