@@ -178,6 +178,45 @@ def test_gpu_pairs_on_bin_edges(gpu, orc, precision):
     assert s["pairs_refined"] > 0 or precision == "fp64"
 
 
+@pytest.mark.parametrize("periodic", [False, True])
+@pytest.mark.parametrize("func", ["DDrppi", "wp", "DDsmu"])
+def test_gpu_2d_pairs_at_the_pruning_bounds(gpu, orc, func, periodic):
+    """Pairs at |dz| = pimax, at rp (or s) equal to the top edge, and one ulp either side, in
+    groups far apart and amid uniform points: the box pruning of the 2-D kernels (rp from the
+    chunk box's xy rectangle, |dz| from its z range, s from the box) keeps every pair the oracle
+    counts."""
+    from corrfunc_gb300 import theory
+    L, pimax = 100.0, 6.0
+    edges = np.array([0.5, 1.0, 2.0, 4.0])
+    top = edges[-1]
+    xs, ys, zs = [], [], []
+    k = 0
+    for dxy in (np.nextafter(top, 0), top, np.nextafter(top, 100), 1.5):
+        for dz in (np.nextafter(pimax, 0), pimax, np.nextafter(pimax, 100), 0.25):
+            x0, y0 = 5.0 + 9.0 * (k % 10), 5.0 + 9.0 * (k // 10)
+            xs += [x0, x0 + dxy]
+            ys += [y0, y0]
+            zs += [20.0, 20.0 + dz]
+            k += 1
+    rng = np.random.default_rng(31)
+    xs += list(rng.random(3000) * L)
+    ys += list(rng.random(3000) * L)
+    zs += list(rng.random(3000) * L)
+    x, y, z = (np.array(a) for a in (xs, ys, zs))
+    if func == "DDrppi":
+        got = theory.DDrppi(1, 1, pimax, edges, x, y, z, periodic=periodic, boxsize=L)
+        want = orc.DDrppi(1, pimax, edges, x, y, z, periodic=periodic, boxsize=L)
+    elif func == "wp":
+        if not periodic:
+            pytest.skip("wp is periodic only")
+        got = theory.wp(L, pimax, 1, edges, x, y, z)
+        want = orc.wp(L, pimax, edges, x, y, z)
+    else:
+        got = theory.DDsmu(1, 1, edges, 1.0, 5, x, y, z, periodic=periodic, boxsize=L)
+        want = orc.DDsmu(1, edges, 1.0, 5, x, y, z, periodic=periodic, boxsize=L)
+    assert np.array_equal(np.asarray(got["npairs"], np.uint64), np.asarray(want["npairs"], np.uint64))
+
+
 @pytest.mark.parametrize("func", ["DD", "DDrppi", "DDsmu", "DDtheta"])
 def test_gpu_fp32_refine_equals_fp64(gpu, func):
     """The FP32+FP64-refinement form and the plain FP64 form give identical counts."""
