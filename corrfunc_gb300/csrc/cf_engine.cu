@@ -1576,8 +1576,9 @@ __device__ __forceinline__ uint32_t pair_offset(const PairArgs &A, const float4 
         const float q = fmaxf(MODE == MODE_RPPI_MOCK ? rp2 : s2, A.q_floor);
         const uint32_t e = lut[lut_bucket(A, q)];
         uint32_t off = e & 0x003fffffu, sl = e;
-        // own column of an auto-correlation: only j > i (every outcome below is masked by keep)
-        const bool keep = !OWN || jb + (uint32_t)k > i;
+        // own column of an auto-correlation: only j > i (every outcome below is masked by keep;
+        // pruned tiles: the staged point's own index)
+        const bool keep = !OWN || (jidx ? jidx[k] : jb + (uint32_t)k) > i;
         off = keep ? off : A.trash_off;
         sl = keep ? sl : 0u;
         const bool real = off != A.trash_off;
@@ -1958,8 +1959,10 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
     uint8_t *simg = (uint8_t *)(sidx + 32);                          // lattice indices and image codes
     float4 *sbox = (float4 *)(simg + 32);  // pruned tiles: the chunk's box (lo, prune radius^2), (hi, -)
     // box pruning: unpacked byte-table kernels (DD(r), xi, DDtheta)
-    // box pruning: the unpacked byte-table kernels (DD(r), xi, DDtheta) and DDrppi / wp / DDsmu
-    constexpr bool kPrune = !PACKED && (LUT8 || MODE == MODE_RPPI || MODE == MODE_WP || MODE == MODE_SMU);
+    // box pruning: the unpacked byte-table kernels (DD(r), xi, DDtheta), DDrppi / wp / DDsmu and
+    // the survey modes
+    constexpr bool kPrune = !PACKED && (LUT8 || MODE == MODE_RPPI || MODE == MODE_WP || MODE == MODE_SMU ||
+                                        mode_is_mock(MODE));
     // periodic shift of a j point by image code (bits 0-5 as Task::meta bits 8-13)
     float4 *shift_hi = (float4 *)(smem + SL.shift_off), *shift_lo = shift_hi + 64;
     if constexpr (PACKED) {
@@ -3331,7 +3334,8 @@ static int launch_pairs_t(const PairArgs &A, bool f64, int *launched)
     const int nedges = A.nedges;
     SmemLayout SL = choose_layout(MODE, f64, AVG, W, nedges, A.nbins, A.lut_n);
     if (!f64 && SL.lane_stride != A.lane_stride_hint) CF_FAIL("internal: histogram layout changed after the table was built");
-    const bool prunes = A.lut8 || MODE == MODE_RPPI || MODE == MODE_WP || MODE == MODE_SMU;  // the kernel's kPrune
+    // the kernel's kPrune
+    const bool prunes = A.lut8 || MODE == MODE_RPPI || MODE == MODE_WP || MODE == MODE_SMU || mode_is_mock(MODE);
     if (!f64 && (A.jrec || prunes) && !SL.extras) CF_FAIL("internal: packed or pruned tiles without their stage space");
     if (SL.total > 220 * 1024) CF_FAIL("histogram too large for on-chip accumulation (%d bins)", A.nbins);
     const int threads = SL.warps * 32;
@@ -3982,11 +3986,14 @@ static void pair_constants(PairArgs &A, const cf_job *J, int mode, int nbins, bo
     A.prune_r2 = FLT_MAX;  // the pruning kernels always test the box: no radius keeps every point
     A.prune_z = FLT_MAX;
     const bool prunes = (T.lut8 && (mode == MODE_R3 || mode == MODE_THETA)) || mode == MODE_RPPI || mode == MODE_WP ||
-                        mode == MODE_SMU;
+                        mode == MODE_SMU || mode_is_mock(mode);
     if (prunes && J->nedges > 0) {
-        double top = 0.0;  // the largest classified value in range: r^2, or the squared chord
+        // the largest classified value in range: r^2 (rp^2, s^2), the squared chord, or (survey
+        // modes) the squared separation cut beyond which every pair is rejected
+        double top = 0.0;
         for (int k = 0; k < J->nedges; k++)
             top = fmax(top, mode == MODE_THETA ? 2.0 * (1.0 - J->edges[k]) : J->edges[k]);
+        if (mode_is_mock(mode)) top = mock_s2_cut(J, mode);
         const double rp = (sqrt(top) + 4.0 * d3) * (1.0 + 1e-5);
         if (isfinite(rp) && rp * rp < 1e30) A.prune_r2 = f_up(rp * rp);
     }
@@ -4252,7 +4259,8 @@ static int run_locked(cf_job *J, cf_hist *H)
     int zdiv = 1;
     const int jsub = f64 ? 1 : choose_split(J, g, n1, n2, autocorr, mode, &zdiv);
     g_eng.layout_packed = jsub > 1;  // the histogram layouts of this count (tables and launch)
-    g_eng.layout_prune = mode == MODE_R3 || mode == MODE_THETA || mode == MODE_RPPI || mode == MODE_WP || mode == MODE_SMU;
+    g_eng.layout_prune = mode == MODE_R3 || mode == MODE_THETA || mode == MODE_RPPI || mode == MODE_WP || mode == MODE_SMU ||
+                         mode_is_mock(mode);
     Geom gj = g;
     uint32_t ncells_j = ncells;
     if (jsub > 1) {
