@@ -52,9 +52,10 @@ namespace {
 constexpr int kChunk = 32;          // points per i-chunk (one per lane)
 constexpr int kCatShift = 17;       // Task::meta bits 17-31: catalogue of a batched count
 // partial j tiles above this size run padded to 32 (fully unrolled); smaller ones pair by pair
-// (measured on this GPU: 16 is 2.7 % faster than 8 and 4.7 % faster than 4 on DD(r))
+// (measured on this GPU with box pruning: 24 is 1.2 % faster than 16 and 4 % faster than 8 on
+// DD(r), 1-3 % faster than 16 on the 2-D counters; 20 and 28 within 0.3 % of 24)
 #ifndef CF_PAD_MIN
-#define CF_PAD_MIN 16
+#define CF_PAD_MIN 24
 #endif
 constexpr int kPadMin = CF_PAD_MIN;
 constexpr uint32_t kJMax = 2048;    // max j points per task
