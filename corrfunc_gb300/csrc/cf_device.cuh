@@ -98,9 +98,10 @@ struct PairArgs {
     int lut8;
     float q_bias, q_cap;        // b, cap
     float q_cap2;               // cap of lanes 16-31: the bucket after cap (entry: the second trash row)
-    // box pruning of the byte-table kernels (0: off): a j point whose FP32 squared distance to the
-    // bounding box of a chunk's points exceeds this pairs with none of them in range (the top
-    // edge's separation plus four coordinate error bounds, and 1e-5 relative, squared, rounded up)
+    // box pruning (FLT_MAX: every point kept): a j point whose FP32 squared distance (DDrppi / wp:
+    // in the xy plane) to the bounding box of a chunk's points exceeds this pairs with none of
+    // them in range (the top edge's separation, or the survey modes' separation cut, plus four
+    // coordinate error bounds, and 1e-5 relative, squared, rounded up)
     float prune_r2;
     // DDrppi / wp: a j point whose z distance to the box is at least this (the FP32 pi rejection
     // bound) pairs with none of the chunk's points within pimax

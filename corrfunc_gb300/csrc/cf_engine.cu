@@ -1959,7 +1959,6 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
     uint32_t *sidx = (uint32_t *)((unsigned char *)rq_count + 16);  // packed tasks: staged j points'
     uint8_t *simg = (uint8_t *)(sidx + 32);                          // lattice indices and image codes
     float4 *sbox = (float4 *)(simg + 32);  // pruned tiles: the chunk's box (lo, prune radius^2), (hi, -)
-    // box pruning: unpacked byte-table kernels (DD(r), xi, DDtheta)
     // box pruning: the unpacked byte-table kernels (DD(r), xi, DDtheta), DDrppi / wp / DDsmu and
     // the survey modes
     constexpr bool kPrune = !PACKED && (LUT8 || MODE == MODE_RPPI || MODE == MODE_WP || MODE == MODE_SMU ||
@@ -2052,10 +2051,12 @@ __global__ void __launch_bounds__(pair_max_threads(MODE, NEED_AVG, NEED_W), CF_P
         }
         const bool shifted = packed && (T.meta & kTaskImages) != 0;
         uint32_t jrc = T.j_begin;  // packed: the record holding list position jb
-        // Box pruning (the unpacked byte-table kernels): a j point farther than the prune radius
-        // (the top edge's separation plus the coordinate error bounds) from the chunk's bounding
-        // box pairs with none of its points in range, so it is never staged; the points kept
-        // fill whole tiles across the task's candidates.
+        // Box pruning (unpacked kernels of every mode but vpf): a j point farther than the prune
+        // radius (the top edge's separation, or the survey modes' separation cut, plus the
+        // coordinate error bounds) from the chunk's bounding box pairs with none of its points in
+        // range, so it is never staged (DDrppi / wp also drop a j point whose z distance to the
+        // box reaches the pi rejection bound); the points kept fill whole tiles across the
+        // task's candidates.
         constexpr bool prune = kPrune;
         if constexpr (prune) {
             // the box of the valid lanes' (image-shifted) points, by order-preserving integer keys
