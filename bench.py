@@ -60,8 +60,8 @@ FLOP_PER_PAIR = 8  # 3 FADD + 1 FMUL + 2 FFMA per 3-D separation
 # dram__bytes_read.sum + dram__bytes_write.sum of one FP32 pair-kernel launch per workload and split
 # of the j lattice's columns (1: unsplit), from an ncu capture of this kernel on that workload (a
 # recorded constant, not measured by this script)
-PAIR_KERNEL_TRAFFIC_BYTES = {("cfg2", 1): 823_918_592 + 21_178_368, ("cfg2", 4): 548_401_664 + 9_282_560,
-                             ("northstar", 1): 55_332_864 + 2_163_456}
+PAIR_KERNEL_TRAFFIC_BYTES = {("cfg2", 1): 829_490_944 + 21_026_816, ("cfg2", 4): 548_401_664 + 9_282_560,
+                             ("northstar", 1): 55_271_424 + 2_289_920}
 TRAFFIC_SOURCE = ("ncu capture of the pair kernel on this workload (dram__bytes_read.sum + dram__bytes_write.sum "
                   "per launch): a recorded constant, not measured in this run")
 
